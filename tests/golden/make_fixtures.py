@@ -1,0 +1,264 @@
+"""Generate the golden fixtures under tests/golden/ from the reference Quanty binary.
+
+Test infrastructure only; run in a container that has the reference sources:
+
+    oracle/build_ref.sh                 # builds oracle/_ref/Quanty from the reference
+    python tests/golden/make_fixtures.py
+
+Each generator in tests/golden/gen/*.lua runs under the reference binary with one OpenMP
+thread and a pinned srand() seed; it writes operators and wavefunctions with Quanty's own
+``io.put`` and numbers with full precision.  Two generators wrap code taken at run time
+from the reference's own test scripts (the impurity-chain model and its golden tridiagonal
+tables from TestScripts/CreateSpectra.Quanty, the f-shell atom and its Mathematica
+eigenvalues from TestScripts/Eigensystem.Quanty), so those known answers are checked
+against the reference here and kept as fixtures.  The JSON files written here are what the
+tests read; nothing at test time touches the reference or its binary.
+"""
+import json
+import os
+import re
+import shutil
+import subprocess
+import sys
+import tempfile
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+from quanty_gb300.quanty_text import parse_operator, parse_wavefunction  # noqa: E402
+
+REF = os.environ.get("QUANTY_REFERENCE", "/root/reference")
+QUANTY = os.path.join(ROOT, "oracle", "_ref", "Quanty")
+
+
+def run(script_text, name):
+    work = tempfile.mkdtemp(prefix="qfx_")
+    shutil.copy(os.path.join(HERE, "gen", "common.lua"), work)
+    with open(os.path.join(work, name), "w") as f:
+        f.write(script_text)
+    os.makedirs(os.path.join(work, "dump"))
+    env = dict(os.environ, OMP_NUM_THREADS="1")
+    p = subprocess.run([QUANTY, name], cwd=work, env=env, capture_output=True, text=True, timeout=1800)
+    if p.returncode != 0 or "Error" in p.stdout:
+        sys.stderr.write(p.stdout[-3000:] + p.stderr[-3000:])
+        raise RuntimeError("generator %s failed" % name)
+    return work
+
+
+def fname(var):
+    """io.put file name of a Lua global: upper-case letters are written as ^ + lower case."""
+    return re.sub(r"[A-Z]", lambda m: "^" + m.group(0).lower(), var) + ".Quanty"
+
+
+def op(work, var):
+    o = parse_operator(open(os.path.join(work, "dump", fname(var))).read())
+    return {"nf": o["nf"], "terms": [[list(t[0]), t[1], t[2]] for t in o["terms"]]}
+
+
+def wf(work, var):
+    return parse_wavefunction(open(os.path.join(work, "dump", fname(var))).read())
+
+
+def reals(work, f):
+    return [float(x) for x in open(os.path.join(work, "dump", f)).read().split()]
+
+
+def complexes(work, f):
+    v = [float(x) for x in open(os.path.join(work, "dump", f)).read().split()]
+    return [[v[2 * i], v[2 * i + 1]] for i in range(len(v) // 2)]
+
+
+def tri(work, f):
+    v = open(os.path.join(work, "dump", f)).read().split()
+    na, nb = int(v[0]), int(v[1])
+    x = [float(t) for t in v[2:]]
+    return {"a": x[:na], "b": x[na:na + nb]}
+
+
+def spectra(work, f):
+    """Parse a Spectra.Print file: header lines then 'E Re0 Im0 Re1 Im1 ...' rows."""
+    lines = open(os.path.join(work, "dump", f)).read().splitlines()
+    n = int(lines[0].split(":")[1])
+    hdr = {}
+    for ln in lines[1:4]:
+        k = ln.split()[0]
+        hdr[k] = [float(t) for t in ln.split()[1:]]
+    rows = []
+    for ln in lines:
+        t = ln.split()
+        if not t:
+            continue
+        try:
+            rows.append([float(x) for x in t])
+        except ValueError:
+            continue
+    rows = [r for r in rows if len(r) == 1 + 2 * n]
+    return {
+        "nspec": n,
+        "emin": hdr["Emin______Emax"][0], "emax": hdr["Emin______Emax"][1],
+        "de": hdr["dE________Gamma"][0], "gamma": hdr["dE________Gamma"][1],
+        "energy": [r[0] for r in rows],
+        "re": [[r[1 + 2 * s] for r in rows] for s in range(n)],
+        "im": [[r[2 + 2 * s] for r in rows] for s in range(n)],
+    }
+
+
+def save(name, obj):
+    path = os.path.join(HERE, name)
+    with open(path, "w") as f:
+        json.dump(obj, f, separators=(",", ":"))
+    print("wrote %s (%d bytes)" % (path, os.path.getsize(path)))
+
+
+def gen_hpsi():
+    src = open(os.path.join(HERE, "gen", "hpsi_cases.lua")).read()
+    work = run(src, "hpsi_cases.lua")
+    names = sorted({f.split("_")[0] for f in os.listdir(os.path.join(work, "dump"))})
+    cases = []
+    for n in names:
+        lohi = reals(work, n + "_restriction.txt")
+        nf = wf(work, n + "_psi")["nf"]
+        mask = "".join("1" if i < nf // 2 else "0" for i in range(nf))
+        cases.append({
+            "name": n, "H": op(work, n + "_H"), "psi": wf(work, n + "_psi"),
+            "Hpsi": wf(work, n + "_Hpsi"), "Hpsir": wf(work, n + "_Hpsir"),
+            "restrictions": [[mask, int(lohi[0]), int(lohi[1])]],
+        })
+    save("hpsi_cases.json", {"source": "tests/golden/gen/hpsi_cases.lua", "cases": cases})
+
+
+def gen_c0():
+    work = run(open(os.path.join(HERE, "gen", "c0_xas.lua")).read(), "c0_xas.lua")
+    out = {"source": "tests/golden/gen/c0_xas.lua"}
+    for n in ["H", "HX", "Tx", "Ty", "Tz", "Tyd"]:
+        out[n] = op(work, n)
+    out["psi"] = [wf(work, "psi%d" % i) for i in (1, 2, 3)]
+    out["energies_dense"] = reals(work, "energies_dense.txt")
+    out["energies_krylov"] = reals(work, "energies_krylov.txt")
+    out["restrictions"] = [["1111110000000000", 6, 6], ["0000001111111111", 8, 8]]
+    out["spectra_opts"] = {"Emin": -10, "Emax": 20, "NE": 1024, "Gamma": 0.5}
+    for eps in ("0", "default"):
+        out["spec_eps" + eps] = spectra(work, "spec_eps%s.dat" % eps)
+        out["tri_eps" + eps] = [tri(work, "tri_eps%s_%d.txt" % (eps, i)) for i in range(1, 10)]
+    out["spec_dense"] = spectra(work, "spec_dense.dat")
+    out["rixs_opts"] = {"Emin1": -5, "Emax1": 15, "NE1": 4, "Gamma1": 0.8, "Emin2": -2, "Emax2": 8,
+                        "NE2": 256, "Gamma2": 0.3, "Epsilon": 0}
+    out["rixs"] = spectra(work, "rixs.dat")
+    save("c0_xas.json", out)
+
+
+def gen_c1():
+    work = run(open(os.path.join(HERE, "gen", "c1_lf.lua")).read(), "c1_lf.lua")
+    out = {"source": "tests/golden/gen/c1_lf.lua"}
+    for n in ["H", "HX", "Tx", "Ty", "Tz"]:
+        out[n] = op(work, n)
+    out["psi"] = [wf(work, "psi%d" % i) for i in (1, 2, 3)]
+    out["energies_krylov"] = reals(work, "energies_krylov.txt")
+    out["energies_dense"] = reals(work, "energies_dense.txt")
+    out["restrictions"] = [["11111100000000000000000000", 6, 6], ["00000011111111111111111111", 18, 18]]
+    out["spectra_opts"] = {"Emin": -10, "Emax": 20, "NE": 2048, "Gamma": 0.5, "NTri": 200, "Epsilon": 0}
+    out["spec_eps0"] = spectra(work, "spec_eps0.dat")
+    out["tri_eps0"] = [tri(work, "tri_eps0_%d.txt" % i) for i in range(1, 10)]
+    save("c1_lf.json", out)
+
+
+CHAIN_DRIVER = r"""
+dofile("common.lua")
+%s
+combos = {}
+for ih, Hname in ipairs({"H0", "H1", "H2"}) do
+  for _, Tn in ipairs({"Dn", "Up"}) do
+    for ip = 1, 2 do
+      combos[#combos + 1] = {Hname, "T" .. Tn, "psi" .. ip, "G" .. (ih - 1) .. Tn .. ip}
+    end
+  end
+end
+for _, n in ipairs({"H0", "H1", "H2", "TDn", "TUp", "psi1", "psi2"}) do io.put("dump", n) end
+dump_reals("dump/omega.txt", omegaList)
+for k, c in ipairs(combos) do
+  local gold = _G[c[4]]
+  local vals = {}
+  for i, w in ipairs(omegaList) do vals[i] = gold(w, 0.1) end
+  dump_complex("dump/gold_" .. k .. ".txt", vals)
+  dump_tri("dump/goldtri_" .. k .. ".txt", gold)
+  local spec, G = CreateSpectra(_G[c[1]], _G[c[2]], _G[c[3]], {{"DenseBorder", 1}, {"Tensor", false}})
+  G = G[1]
+  local got = {}
+  for i, w in ipairs(omegaList) do got[i] = G(w, 0.1) end
+  dump_complex("dump/ref_" .. k .. ".txt", got)
+  dump_tri("dump/reftri_" .. k .. ".txt", G)
+  local f = io.open("dump/combo_" .. k .. ".txt", "w"); f:write(table.concat(c, " ")); f:close()
+end
+print("chain done")
+"""
+
+
+def gen_chain():
+    lines = open(os.path.join(REF, "TestScripts", "CreateSpectra.Quanty")).read().splitlines()
+    s = next(i for i, l in enumerate(lines) if l.startswith("-- Define some model Hamiltonian"))
+    e = next(i for i, l in enumerate(lines) if l.startswith("threshold"))
+    model = "\n".join(lines[s:e + 1])
+    work = run(CHAIN_DRIVER % model, "chain.lua")
+    out = {"source": "TestScripts/CreateSpectra.Quanty:%d-%d (model, golden tables, omega list, threshold)" % (s + 1, e + 1),
+           "gamma": 0.1, "threshold": 1e-12, "omega": reals(work, "omega.txt")}
+    for n in ["H0", "H1", "H2", "TDn", "TUp"]:
+        out[n] = op(work, n)
+    out["psi1"] = wf(work, "psi1")
+    out["psi2"] = wf(work, "psi2")
+    combos = []
+    k = 1
+    while os.path.exists(os.path.join(work, "dump", "combo_%d.txt" % k)):
+        c = open(os.path.join(work, "dump", "combo_%d.txt" % k)).read().split()
+        combos.append({"H": c[0], "T": c[1], "psi": c[2], "golden": c[3],
+                       "golden_G": complexes(work, "gold_%d.txt" % k),
+                       "golden_tri": tri(work, "goldtri_%d.txt" % k),
+                       "ref_G": complexes(work, "ref_%d.txt" % k),
+                       "ref_tri": tri(work, "reftri_%d.txt" % k)})
+        k += 1
+    out["combos"] = combos
+    save("chain_spectra.json", out)
+
+
+FSHELL_DRIVER = r"""
+dofile("common.lua")
+%s
+io.put("dump", "Hamiltonian1")
+dump_reals("dump/expected.txt", expectedEn)
+f10 = Eigensystem(Hamiltonian1, StartRestrictions, 10)
+E = {}
+for i = 1, 10 do E[i] = Complex.Re(f10[i] * Hamiltonian1 * f10[i]) end
+dump_reals("dump/energies_default.txt", E)
+f10t = Eigensystem(Hamiltonian1, StartRestrictions, 10, {{"Zero", 1e-14}, {"Epsilon", 0}})
+E = {}
+for i = 1, 10 do E[i] = Complex.Re(f10t[i] * Hamiltonian1 * f10t[i]) end
+dump_reals("dump/energies_tight.txt", E)
+print("fshell done")
+"""
+
+
+def gen_fshell():
+    lines = open(os.path.join(REF, "TestScripts", "Eigensystem.Quanty")).read().splitlines()
+    a = next(i for i, l in enumerate(lines) if l.startswith("::atom::"))
+    keep = []
+    for i in range(a, len(lines)):
+        l = lines[i]
+        if re.match(r"^(Basis_dn|Basis_up|Hamiltonian1|StartRestrictions|expectedEn)\s*=", l):
+            keep.append((i + 1, l))
+        if l.startswith("expectedEn"):
+            break
+    model = "\n".join(l for _, l in keep)
+    work = run(FSHELL_DRIVER % model, "fshell.lua")
+    out = {"source": "TestScripts/Eigensystem.Quanty:" + ",".join(str(i) for i, _ in keep),
+           "H": op(work, "Hamiltonian1"), "restrictions": [["11111111111111", 6, 6]],
+           "expected_mathematica": reals(work, "expected.txt"),
+           "energies_default": reals(work, "energies_default.txt"),
+           "energies_tight": reals(work, "energies_tight.txt")}
+    save("fshell_eigen.json", out)
+
+
+if __name__ == "__main__":
+    if not os.path.exists(QUANTY):
+        sys.exit("build the reference first: oracle/build_ref.sh")
+    which = sys.argv[1:] or ["hpsi", "c0", "c1", "chain", "fshell"]
+    for w in which:
+        globals()["gen_" + w]()
