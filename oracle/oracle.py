@@ -1,0 +1,254 @@
+"""CPU oracle for the H*psi / Lanczos / continued-fraction path -- TEST INFRASTRUCTURE ONLY.
+
+This module is the checker: tests/ compare the CUDA library against it, and bench.py's
+CPU-baseline leg times it.  It loads ``oracle/_build/libqoracle.so`` (built by
+``oracle/Makefile`` from ``qoracle.c``, a plain-C restatement of the reference) and adds small
+numpy drivers.  The product under ``quanty_gb300/`` never imports it.
+
+Determinants are handled in the reference's byte layout (``Core/OperatorWaveFunction.cpp:7-43``):
+``nword = ceil(nf/8)`` bytes, orbital ``i`` in byte ``i>>3`` under mask ``128>>(i&7)``.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libqoracle.so")
+CREATION = 0x8000
+
+_lib = None
+
+
+def build():
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = C.CDLL(LIB_PATH)
+        P, I64, D, I = C.c_void_p, C.c_int64, C.c_double, C.c_int
+        L.qo_wf_from.restype = P
+        L.qo_wf_from.argtypes = [I, I64, P, P, P]
+        L.qo_wf_free.argtypes = [P]
+        L.qo_wf_size.restype = I64
+        L.qo_wf_size.argtypes = [P]
+        L.qo_wf_get.argtypes = [P, P, P, P]
+        L.qo_operator_psi.restype = P
+        L.qo_operator_psi.argtypes = [I, P, P, P, P, P, P, I, P, P, P]
+        L.qo_apply_conserve.argtypes = [I, P, P, P, P, P, P, I64, I64, P]
+        L.qo_count_nnz.restype = I64
+        L.qo_count_nnz.argtypes = [I, P, P, P, P, I64, I64]
+        L.qo_lanczos_tridiag.argtypes = [I, P, P, P, P, P, P, I, D, D, I, P, P, P, P, P]
+        L.qo_cf_spectrum.argtypes = [I, P, P, D, D, D, I, D, P, P]
+        L.qo_ladder.restype = I
+        L.qo_ladder.argtypes = [P, P, I]
+        L.qo_num_threads.restype = I
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+# ----------------------------------------------------------------------------- data helpers
+
+def nword(nf):
+    return (nf + 7) // 8
+
+
+def dets_to_bytes(dets, nf):
+    """'0101...' strings (orbital 0 first) -> uint8 array (n, nword), MSB-first bytes."""
+    nw = nword(nf)
+    out = np.zeros((len(dets), nw), dtype=np.uint8)
+    for r, s in enumerate(dets):
+        for i, ch in enumerate(s[:nf]):
+            if ch == "1":
+                out[r, i >> 3] |= 128 >> (i & 7)
+    return out
+
+
+def bytes_to_dets(b, nf):
+    out = []
+    for row in b:
+        out.append("".join("1" if row[i >> 3] & (128 >> (i & 7)) else "0" for i in range(nf)))
+    return out
+
+
+class Op:
+    """Flat term table: ladder strings concatenated, o[0] acting first, bit 15 = creation."""
+
+    def __init__(self, fixture_op):
+        self.nf = fixture_op["nf"]
+        terms = fixture_op["terms"]
+        self.len = np.array([len(t[0]) for t in terms], dtype=np.int32)
+        self.off = np.zeros(len(terms), dtype=np.int64)
+        if len(terms):
+            self.off[1:] = np.cumsum(self.len)[:-1]
+        flat = [o for t in terms for o in t[0]]
+        self.ops = np.array(flat if flat else [0], dtype=np.uint16)
+        self.vre = np.array([t[1] for t in terms], dtype=np.float64)
+        self.vim = np.array([t[2] for t in terms], dtype=np.float64)
+        self.nterms = len(terms)
+
+    def args(self):
+        return [self.nterms, _p(self.len), _p(self.off), _p(self.ops), _p(self.vre), _p(self.vim)]
+
+
+class Restr:
+    def __init__(self, nf, restrictions):
+        self.n = len(restrictions or [])
+        nw = nword(nf)
+        self.masks = np.zeros((max(self.n, 1), nw), dtype=np.uint8)
+        self.mn = np.zeros(max(self.n, 1), dtype=np.int32)
+        self.mx = np.zeros(max(self.n, 1), dtype=np.int32)
+        for r, (mask, lo, hi) in enumerate(restrictions or []):
+            self.masks[r] = dets_to_bytes([mask.replace(" ", "")], nf)[0]
+            self.mn[r] = lo
+            self.mx[r] = hi
+
+    def args(self):
+        return [self.n, _p(self.masks), _p(self.mn), _p(self.mx)]
+
+
+class WF:
+    """Wavefunction in the oracle's own representation (insertion-ordered determinants)."""
+
+    def __init__(self, nf, det_bytes, values):
+        self.nf = nf
+        self.det = np.ascontiguousarray(det_bytes, dtype=np.uint8).reshape(-1, nword(nf))
+        self.val = np.ascontiguousarray(values, dtype=np.complex128).reshape(-1)
+
+    @classmethod
+    def from_fixture(cls, f):
+        return cls(f["nf"], dets_to_bytes(f["dets"], f["nf"]), np.array(f["re"]) + 1j * np.array(f["im"]))
+
+    def handle(self):
+        re = np.ascontiguousarray(self.val.real)
+        im = np.ascontiguousarray(self.val.imag)
+        return lib().qo_wf_from(self.nf, len(self.val), _p(self.det), _p(re), _p(im))
+
+    @classmethod
+    def from_handle(cls, nf, h):
+        L = lib()
+        n = L.qo_wf_size(h)
+        det = np.zeros((n, nword(nf)), dtype=np.uint8)
+        re = np.zeros(n)
+        im = np.zeros(n)
+        if n:
+            L.qo_wf_get(h, _p(det), _p(re), _p(im))
+        L.qo_wf_free(h)
+        return cls(nf, det, re + 1j * im)
+
+    def as_dict(self):
+        return {bytes(r): v for r, v in zip(self.det, self.val)}
+
+
+# ----------------------------------------------------------------------------- algorithms
+
+def operator_psi(op, psi, restrictions=None):
+    """Growing-basis H*psi (reference OperatorPsi / OperatorPsiRestricted)."""
+    r = Restr(psi.nf, restrictions)
+    h = psi.handle()
+    out = lib().qo_operator_psi(*op.args(), h, *r.args())
+    lib().qo_wf_free(h)
+    return WF.from_handle(psi.nf, out)
+
+
+def apply_conserve(op, psi, row0=0, row1=None):
+    """Fixed-basis H*psi, push form (reference OperatorPsiConserveBasisPreAllocated)."""
+    row1 = len(psi.val) if row1 is None else row1
+    h = psi.handle()
+    y = np.zeros(2 * len(psi.val))
+    lib().qo_apply_conserve(*op.args(), h, row0, row1, _p(y))
+    lib().qo_wf_free(h)
+    return y[0::2] + 1j * y[1::2]
+
+
+def count_nnz(op, psi, row0=0, row1=None):
+    row1 = len(psi.val) if row1 is None else row1
+    h = psi.handle()
+    n = lib().qo_count_nnz(op.nterms, _p(op.len), _p(op.off), _p(op.ops), h, row0, row1)
+    lib().qo_wf_free(h)
+    return n
+
+
+def lanczos_tridiag(op, psi, ntri, eps, gamma, restrictions=None):
+    """Reference LanczosTriDiagonalize on a growing basis; returns a (ntri+1), b (ntri)."""
+    r = Restr(psi.nf, restrictions)
+    a = np.zeros(ntri + 1)
+    b = np.zeros(ntri)
+    h = psi.handle()
+    lib().qo_lanczos_tridiag(*op.args(), h, ntri, eps, gamma, *r.args(), _p(a), _p(b))
+    lib().qo_wf_free(h)
+    return a, b
+
+
+def cf_spectrum(a, b, e0, emin, de, ne, gamma):
+    """Continued fraction on NE+1 points (reference TriDiagonalMatrixToSpectrum)."""
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    gre = np.zeros(ne + 1)
+    gim = np.zeros(ne + 1)
+    lib().qo_cf_spectrum(len(b), _p(a), _p(b), e0, emin, de, ne, gamma, _p(gre), _p(gim))
+    return gre + 1j * gim
+
+
+def closure(op, seed, restrictions=None, max_rounds=10000):
+    """All determinants reachable from the seed determinants under repeated H (within the
+    restrictions); the seed comes first, then targets in discovery order."""
+    basis = WF(seed.nf, seed.det, np.ones(len(seed.val)))
+    known = {bytes(r) for r in basis.det}
+    frontier = basis
+    rounds = 0
+    while len(frontier.val) and rounds < max_rounds:
+        nxt = operator_psi(op, WF(seed.nf, frontier.det, np.ones(len(frontier.val))), restrictions)
+        new = [i for i, r in enumerate(nxt.det) if bytes(r) not in known]
+        for i in new:
+            known.add(bytes(nxt.det[i]))
+        frontier = WF(seed.nf, nxt.det[new], np.ones(len(new)))
+        basis = WF(seed.nf, np.concatenate([basis.det, frontier.det]), np.ones(len(basis.val) + len(new)))
+        rounds += 1
+    return basis
+
+
+def enumerate_restricted(nf, restrictions, nel=None):
+    """Every determinant on nf orbitals that satisfies the occupation windows (the complete
+    basis the reference builds for small systems, ExtendBasisCompletenessSmallSystems,
+    Core/BlockLanczos.cpp:102).  Brute force over 2^nf; meant for nf <= 26."""
+    masks = [int(m.replace(" ", "")[::-1], 2) for m, _, _ in restrictions]
+    rows = []
+    for x in range(1 << nf):
+        if nel is not None and bin(x).count("1") != nel:
+            continue
+        if all(lo <= bin(x & m).count("1") <= hi for m, (_, lo, hi) in zip(masks, restrictions)):
+            rows.append(x)
+    dets = ["".join("1" if (x >> i) & 1 else "0" for i in range(nf)) for x in rows]
+    return WF(nf, dets_to_bytes(dets, nf), np.ones(len(dets)))
+
+
+def dense_matrix(op, basis):
+    """<i|H|j> on a basis (columns from the fixed-basis apply on unit vectors)."""
+    n = len(basis.val)
+    M = np.zeros((n, n), dtype=np.complex128)
+    for j in range(n):
+        e = np.zeros(n, dtype=np.complex128)
+        e[j] = 1.0
+        M[:, j] = apply_conserve(op, WF(basis.nf, basis.det, e))
+    return M
+
+
+def exact_eigensystem(op, basis, k):
+    """Lowest k eigenpairs of H on a closed basis, by dense diagonalisation."""
+    M = dense_matrix(op, basis)
+    w, v = np.linalg.eigh(0.5 * (M + M.conj().T))
+    return w[:k], v[:, :k]
+
+
+def num_threads():
+    return lib().qo_num_threads()

@@ -1,0 +1,434 @@
+/*
+ * qoracle.c -- CPU oracle for the H*psi / Lanczos / continued-fraction path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is a plain-C restatement of the reference algorithm, used
+ * by tests/ as the checker and by bench.py as the timed CPU baseline.  The product (the
+ * CUDA library under quanty_gb300/csrc) never links, loads or calls it.
+ *
+ * Parity is pinned by tests/test_oracle_golden.py against fixtures the reference binary
+ * produced (the JSON files under tests/golden) and against the known answers of the reference's own tests
+ * (TestScripts/CreateSpectra.Quanty golden tridiagonal tables, TestScripts/Eigensystem.Quanty
+ * Mathematica eigenvalues).
+ *
+ * Layout follows the reference: a determinant is NWord = ceil(NF/8) bytes, orbital i in byte
+ * i>>3 under mask 128>>(i&7) (Core/OperatorWaveFunction.cpp:7-43,
+ * Core/WaveFunctionArithmetic.cpp:130).  A ladder code has bit 15 set for a creation
+ * operator (CrAnMask, Core/StructDef.cpp:46); code[0] acts first
+ * (Core/OperatorWaveFunction.cpp:98-113).  Bosons are not supported (NewWavefunction rejects
+ * them, LuaInterface/ssp.cpp:951-954).
+ */
+#include <float.h>
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define QO_CR 0x8000u
+#define QO_IDX 0x7FFFu
+
+/* ------------------------------------------------------------------ ladder operators */
+
+/* Parity of the occupied orbitals with index < i after the bit of orbital i has been
+ * toggled, as Core/OperatorWaveFunction.cpp:30-43 computes it (bits of byte k above the
+ * MSB-first position m, xor-folded with all lower bytes). */
+static int qo_parity_below(const uint8_t *det, unsigned i)
+{
+  unsigned k = i >> 3, m = i & 7, j;
+  unsigned acc = (unsigned)(det[k] >> (8 - m)) & 0xFFu;
+  if (m == 0) acc = 0;
+  for (j = 0; j < k; j++) acc ^= det[j];
+  acc ^= acc >> 4;
+  acc ^= acc >> 2;
+  acc ^= acc >> 1;
+  return acc & 1;
+}
+
+/* Apply one ladder string to det in place; return the sign (-1, 0, +1).
+ * Restates OperatorCr / OperatorAn / OperatorLader (Core/OperatorWaveFunction.cpp:7-115). */
+int qo_ladder(uint8_t *det, const uint16_t *o, int len)
+{
+  int phase = 1, t;
+  for (t = 0; t < len; t++) {
+    unsigned idx = o[t] & QO_IDX;
+    unsigned k = idx >> 3;
+    uint8_t bit = (uint8_t)(128u >> (idx & 7));
+    if (o[t] & QO_CR) {
+      if (det[k] & bit) return 0;
+      det[k] |= bit;
+    } else {
+      if (!(det[k] & bit)) return 0;
+      det[k] &= (uint8_t)~bit;
+    }
+    if (qo_parity_below(det, idx)) phase = -phase;
+  }
+  return phase;
+}
+
+/* Occupation-window filter; restates QDetNotRestricted (Core/OperatorWaveFunction.cpp:2260). */
+int qo_restricted_ok(const uint8_t *det, int nword, int nres, const uint8_t *masks,
+                     const int *mn, const int *mx)
+{
+  int r, j;
+  for (r = 0; r < nres; r++) {
+    int s = 0;
+    for (j = 0; j < nword; j++) s += __builtin_popcount((unsigned)(masks[r * nword + j] & det[j]));
+    if (s > mx[r] || s < mn[r]) return 0;
+  }
+  return 1;
+}
+
+/* ------------------------------------------------------------------ operator */
+
+typedef struct {
+  int nterms;
+  const int *len;       /* nterms */
+  const int64_t *off;   /* nterms, offset into ops */
+  const uint16_t *ops;
+  const double *vre, *vim;
+} qo_op;
+
+/* ------------------------------------------------------------------ wavefunction */
+
+/* A wavefunction: determinants in insertion order plus an open-addressing index.  The
+ * reference keeps a chained hash (Core/Hash.cpp:163 + KeyList/Next); the lookup structure
+ * is internal and does not change any result, the insertion order is kept as the
+ * reference's (append at N+1, Core/ComplexWaveFunctionArithmetic.cpp:64-190). */
+typedef struct {
+  int nf, nword;
+  int64_t n, cap;
+  uint8_t *det;
+  double *re, *im;
+  int64_t *slot; /* index+1, 0 = empty */
+  int64_t hcap;  /* power of two */
+} qo_wf;
+
+static uint64_t qo_hash_bytes(const uint8_t *d, int nword)
+{
+  uint64_t h = 1469598103934665603ull;
+  int i;
+  for (i = 0; i < nword; i++) { h ^= d[i]; h *= 1099511628211ull; }
+  h ^= h >> 29; h *= 0xbf58476d1ce4e5b9ull; h ^= h >> 32;
+  return h;
+}
+
+qo_wf *qo_wf_new(int nf, int64_t cap)
+{
+  qo_wf *w = (qo_wf *)calloc(1, sizeof(qo_wf));
+  w->nf = nf;
+  w->nword = (nf + 7) / 8;
+  if (cap < 16) cap = 16;
+  w->cap = cap;
+  w->det = (uint8_t *)malloc((size_t)cap * w->nword);
+  w->re = (double *)malloc(sizeof(double) * cap);
+  w->im = (double *)malloc(sizeof(double) * cap);
+  w->hcap = 64;
+  while (w->hcap < 2 * cap) w->hcap <<= 1;
+  w->slot = (int64_t *)calloc((size_t)w->hcap, sizeof(int64_t));
+  return w;
+}
+
+void qo_wf_free(qo_wf *w)
+{
+  if (!w) return;
+  free(w->det); free(w->re); free(w->im); free(w->slot); free(w);
+}
+
+static void qo_rehash(qo_wf *w, int64_t hcap)
+{
+  int64_t i;
+  free(w->slot);
+  w->hcap = hcap;
+  w->slot = (int64_t *)calloc((size_t)hcap, sizeof(int64_t));
+  for (i = 0; i < w->n; i++) {
+    uint64_t h = qo_hash_bytes(w->det + i * w->nword, w->nword) & (uint64_t)(hcap - 1);
+    while (w->slot[h]) h = (h + 1) & (uint64_t)(hcap - 1);
+    w->slot[h] = i + 1;
+  }
+}
+
+int64_t qo_wf_find(const qo_wf *w, const uint8_t *d)
+{
+  uint64_t h = qo_hash_bytes(d, w->nword) & (uint64_t)(w->hcap - 1);
+  while (w->slot[h]) {
+    int64_t i = w->slot[h] - 1;
+    if (memcmp(w->det + i * w->nword, d, (size_t)w->nword) == 0) return i;
+    h = (h + 1) & (uint64_t)(w->hcap - 1);
+  }
+  return -1;
+}
+
+/* psi += a |d>, appending d if absent (ComplexWaveFunctionAddElement,
+ * Core/ComplexWaveFunctionArithmetic.cpp:64). */
+void qo_wf_add(qo_wf *w, const uint8_t *d, double are, double aim)
+{
+  int64_t i = qo_wf_find(w, d);
+  uint64_t h;
+  if (i >= 0) { w->re[i] += are; w->im[i] += aim; return; }
+  if (w->n == w->cap) {
+    w->cap *= 2;
+    w->det = (uint8_t *)realloc(w->det, (size_t)w->cap * w->nword);
+    w->re = (double *)realloc(w->re, sizeof(double) * w->cap);
+    w->im = (double *)realloc(w->im, sizeof(double) * w->cap);
+  }
+  if (2 * (w->n + 1) > w->hcap) qo_rehash(w, w->hcap * 2);
+  memcpy(w->det + w->n * w->nword, d, (size_t)w->nword);
+  w->re[w->n] = are;
+  w->im[w->n] = aim;
+  h = qo_hash_bytes(d, w->nword) & (uint64_t)(w->hcap - 1);
+  while (w->slot[h]) h = (h + 1) & (uint64_t)(w->hcap - 1);
+  w->slot[h] = w->n + 1;
+  w->n++;
+}
+
+qo_wf *qo_wf_from(int nf, int64_t n, const uint8_t *det, const double *re, const double *im)
+{
+  qo_wf *w = qo_wf_new(nf, n);
+  int64_t i;
+  for (i = 0; i < n; i++) qo_wf_add(w, det + i * w->nword, re[i], im[i]);
+  return w;
+}
+
+int64_t qo_wf_size(const qo_wf *w) { return w->n; }
+void qo_wf_get(const qo_wf *w, uint8_t *det, double *re, double *im)
+{
+  memcpy(det, w->det, (size_t)w->n * w->nword);
+  memcpy(re, w->re, sizeof(double) * w->n);
+  memcpy(im, w->im, sizeof(double) * w->n);
+}
+
+static qo_wf *qo_wf_copy(const qo_wf *a)
+{
+  qo_wf *w = qo_wf_new(a->nf, a->n);
+  memcpy(w->det, a->det, (size_t)a->n * a->nword);
+  memcpy(w->re, a->re, sizeof(double) * a->n);
+  memcpy(w->im, a->im, sizeof(double) * a->n);
+  w->n = a->n;
+  qo_rehash(w, w->hcap);
+  return w;
+}
+
+/* ------------------------------------------------------------------ H*psi */
+
+/* Growing-basis H*psi: every (determinant, term) pair with a non-zero sign adds
+ * phase*V*psi_i to the target, appending new targets in visiting order (OperatorPsiCC and
+ * OperatorPsiRestrictedCC, Core/OperatorWaveFunction.cpp:1750-1823, :2288-2361).  With
+ * nres > 0 targets failing the occupation windows are dropped. */
+qo_wf *qo_operator_psi(int nterms, const int *len, const int64_t *off, const uint16_t *ops,
+                       const double *vre, const double *vim, const qo_wf *psi, int nres,
+                       const uint8_t *masks, const int *mn, const int *mx)
+{
+  qo_wf *out = qo_wf_new(psi->nf, psi->n * 4 + 16);
+  uint8_t tmp[64];
+  int64_t i;
+  int t;
+  for (i = 0; i < psi->n; i++) {
+    const uint8_t *src = psi->det + i * psi->nword;
+    double xr = psi->re[i], xi = psi->im[i];
+    for (t = 0; t < nterms; t++) {
+      int ph;
+      memcpy(tmp, src, (size_t)psi->nword);
+      ph = qo_ladder(tmp, ops + off[t], len[t]);
+      if (!ph) continue;
+      if (nres && !qo_restricted_ok(tmp, psi->nword, nres, masks, mn, mx)) continue;
+      qo_wf_add(out, tmp, ph * (vre[t] * xr - vim[t] * xi), ph * (vre[t] * xi + vim[t] * xr));
+    }
+  }
+  return out;
+}
+
+/* Fixed-basis H*psi, push form: y on the basis of x, contributions to determinants outside
+ * the basis dropped, contributions with |a|^2 < 100*DBL_MIN dropped
+ * (OperatorPsiConserveBasisPreAllocatedCC, Core/OperatorWaveFunction.cpp:784-838, and
+ * ComplexWaveFunctionAddElementConserveBasis, Core/ComplexWaveFunctionArithmetic.cpp:355-398).
+ * OpenMP over source determinants with atomic adds, as the reference.
+ * Sources are rows [row0, row1) of x; y (length x->n, interleaved re/im) is overwritten
+ * with zeros first. */
+void qo_apply_conserve(int nterms, const int *len, const int64_t *off, const uint16_t *ops,
+                       const double *vre, const double *vim, const qo_wf *x, int64_t row0,
+                       int64_t row1, double *y)
+{
+  int64_t i;
+  for (i = 0; i < 2 * x->n; i++) y[i] = 0.0;
+#pragma omp parallel for schedule(dynamic, 64)
+  for (i = row0; i < row1; i++) {
+    uint8_t tmp[64];
+    const uint8_t *src = x->det + i * x->nword;
+    double xr = x->re[i], xi = x->im[i];
+    int t;
+    for (t = 0; t < nterms; t++) {
+      int ph;
+      int64_t j;
+      double ar, ai;
+      memcpy(tmp, src, (size_t)x->nword);
+      ph = qo_ladder(tmp, ops + off[t], len[t]);
+      if (!ph) continue;
+      ar = ph * (vre[t] * xr - vim[t] * xi);
+      ai = ph * (vre[t] * xi + vim[t] * xr);
+      if (ar * ar + ai * ai < 100 * DBL_MIN) continue;
+      j = qo_wf_find(x, tmp);
+      if (j < 0) continue;
+#pragma omp atomic
+      y[2 * j] += ar;
+#pragma omp atomic
+      y[2 * j + 1] += ai;
+    }
+  }
+}
+
+/* Count the (determinant, term) pairs with a non-zero sign whose target lies in the basis,
+ * for rows [row0,row1). */
+int64_t qo_count_nnz(int nterms, const int *len, const int64_t *off, const uint16_t *ops,
+                     const qo_wf *x, int64_t row0, int64_t row1)
+{
+  int64_t i, nnz = 0;
+#pragma omp parallel for reduction(+ : nnz) schedule(dynamic, 64)
+  for (i = row0; i < row1; i++) {
+    uint8_t tmp[64];
+    int t;
+    for (t = 0; t < nterms; t++) {
+      memcpy(tmp, x->det + i * x->nword, (size_t)x->nword);
+      if (!qo_ladder(tmp, ops + off[t], len[t])) continue;
+      if (qo_wf_find(x, tmp) >= 0) nnz++;
+    }
+  }
+  return nnz;
+}
+
+/* ------------------------------------------------------------------ vector algebra */
+
+double qo_norm(const qo_wf *a)
+{ /* ComplexWaveFunctionCalculateNorm, Core/ComplexWaveFunctionArithmetic.cpp:870 */
+  double s = 0;
+  int64_t i;
+  for (i = 0; i < a->n; i++) s += a->re[i] * a->re[i] + a->im[i] * a->im[i];
+  return sqrt(s);
+}
+
+void qo_scale(qo_wf *a, double f)
+{ /* ComplexWaveFunctionMultiply by a real factor */
+  int64_t i;
+  for (i = 0; i < a->n; i++) { a->re[i] *= f; a->im[i] *= f; }
+}
+
+/* <a|b>, conjugating a (ComplexWaveFunctionDotProduct, Core/ComplexWaveFunctionArithmetic.cpp:991) */
+void qo_dot(const qo_wf *a, const qo_wf *b, double *dre, double *dim)
+{
+  double sr = 0, si = 0;
+  int64_t i;
+  for (i = 0; i < a->n; i++) {
+    int64_t j = qo_wf_find(b, a->det + i * a->nword);
+    if (j < 0) continue;
+    sr += a->re[i] * b->re[j] + a->im[i] * b->im[j];
+    si += a->re[i] * b->im[j] - a->im[i] * b->re[j];
+  }
+  *dre = sr;
+  *dim = si;
+}
+
+/* a += f*b on the union basis (ComplexWaveFunctionAddMultipliedUnionBasis, :601) */
+void qo_axpy_union(qo_wf *a, const qo_wf *b, double fre, double fim)
+{
+  int64_t i;
+  for (i = 0; i < b->n; i++)
+    qo_wf_add(a, b->det + i * b->nword, fre * b->re[i] - fim * b->im[i], fre * b->im[i] + fim * b->re[i]);
+}
+
+/* drop |a_i|^2 <= eps^2, keeping order (ComplexWaveFunctionTruncateBasis, :1073-1113) */
+void qo_truncate(qo_wf *a, double eps)
+{
+  double e2 = eps * eps;
+  int64_t i, k = 0;
+  for (i = 0; i < a->n; i++) {
+    if (a->re[i] * a->re[i] + a->im[i] * a->im[i] > e2) {
+      if (k != i) {
+        memcpy(a->det + k * a->nword, a->det + i * a->nword, (size_t)a->nword);
+        a->re[k] = a->re[i];
+        a->im[k] = a->im[i];
+      }
+      k++;
+    }
+  }
+  a->n = k;
+  qo_rehash(a, a->hcap);
+}
+
+/* ------------------------------------------------------------------ Lanczos */
+
+/* Three-term Lanczos tridiagonalisation on a growing basis with the reference's truncation
+ * schedule (LanczosTriDiagonalizeCC, Core/Lanczos.cpp:2169-2263):
+ *   a[0] = 0, b[0] = |psi|, v0 = psi/b0 truncated at eps;
+ *   v1 = H v0, a[1] = <v0|H|v0>;
+ *   for i = 1..ntri-1: v_i -= a_i v_{i-1}; b_i = |v_i|; v_i /= b_i; truncate at eps/err;
+ *                      err *= b_i^2/(b_i^2 + 4 gamma^2); w = H v_i; a_{i+1} = <v_i|w>;
+ *                      w -= b_i v_{i-1}.
+ * a has ntri+1 entries, b has ntri.  Restrictions (nres > 0) filter every H*v. */
+void qo_lanczos_tridiag(int nterms, const int *len, const int64_t *off, const uint16_t *ops,
+                        const double *vre, const double *vim, const qo_wf *psi, int ntri,
+                        double eps, double gamma, int nres, const uint8_t *masks, const int *mn,
+                        const int *mx, double *a, double *b)
+{
+  qo_wf *v[3];
+  double err = 1.0, junk;
+  int i;
+  v[0] = qo_wf_copy(psi);
+  v[1] = v[2] = NULL;
+  a[0] = 0;
+  b[0] = qo_norm(v[0]);
+  qo_scale(v[0], 1.0 / b[0]);
+  qo_truncate(v[0], eps);
+  v[1] = qo_operator_psi(nterms, len, off, ops, vre, vim, v[0], nres, masks, mn, mx);
+  qo_dot(v[1], v[0], &a[1], &junk);
+  for (i = 1; i < ntri; i++) {
+    int vip = (i + 1) % 3, vi = i % 3, vim_ = (i - 1) % 3;
+    qo_axpy_union(v[vi], v[vim_], -a[i], 0.0);
+    b[i] = qo_norm(v[vi]);
+    qo_scale(v[vi], 1.0 / b[i]);
+    qo_truncate(v[vi], eps / err);
+    err *= b[i] * b[i] / (b[i] * b[i] + 4 * gamma * gamma);
+    qo_wf_free(v[vip]);
+    v[vip] = qo_operator_psi(nterms, len, off, ops, vre, vim, v[vi], nres, masks, mn, mx);
+    qo_dot(v[vip], v[vi], &a[i + 1], &junk);
+    qo_axpy_union(v[vip], v[vim_], -b[i], 0.0);
+  }
+  qo_wf_free(v[0]);
+  qo_wf_free(v[1]);
+  qo_wf_free(v[2]);
+}
+
+/* ------------------------------------------------------------------ continued fraction */
+
+/* G(w_k) for w_k = emin + k*de + e0, k = 0..ne, with Gamma/2 imaginary shift:
+ * G = a0 + b0^2 / (w - a1 + i g/2 - b1^2 / (w - a2 + i g/2 - ...)), evaluated from the
+ * bottom as TriDiagonalMatrixToSpectrum does (Core/Spectral.cpp:1433-1473).  a has n+1
+ * entries, b has n. */
+void qo_cf_spectrum(int n, const double *a, const double *b, double e0, double emin, double de,
+                    int ne, double gamma, double *gre, double *gim)
+{
+  int k, j;
+  for (k = 0; k <= ne; k++) {
+    double w = (double)k * de + emin + e0;
+    double den = (gamma * 0.5) * (gamma * 0.5) + (w - a[n]) * (w - a[n]);
+    double vr = (w - a[n]) / den, vi = (-gamma * 0.5) / den;
+    for (j = (n > 1 ? n : 1) - 1; j >= 1; j--) {
+      double b2 = b[j] * b[j];
+      double zr = w - a[j] - vr * b2, zi = gamma * 0.5 - vi * b2;
+      den = zi * zi + zr * zr;
+      vr = zr / den;
+      vi = (vi * b2 - gamma * 0.5) / den;
+    }
+    gre[k] = a[0] + vr * b[0] * b[0];
+    gim[k] = vi * b[0] * b[0];
+  }
+}
+
+int qo_num_threads(void)
+{
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}

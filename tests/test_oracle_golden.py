@@ -1,0 +1,165 @@
+"""Pin the CPU oracle (oracle/qoracle.c) against the reference.
+
+The fixtures come from the reference Quanty binary (tests/golden/make_fixtures.py) and from
+the known answers in the reference's own tests: the golden tridiagonal tables of
+TestScripts/CreateSpectra.Quanty (checked at 1e-12 there) and the Mathematica eigenvalues of
+TestScripts/Eigensystem.Quanty.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from conftest import golden
+
+EPS_DEFAULT = math.sqrt(np.finfo(float).eps) / 100   # Core/StructDef.cpp:306
+
+
+def rel_err(a, b):
+    a = np.asarray(a)
+    b = np.asarray(b)
+    return np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300)
+
+
+@pytest.mark.parametrize("case", [c["name"] for c in golden("hpsi_cases.json")["cases"]])
+def test_operator_psi_matches_reference_order_and_values(oracle_mod, case):
+    O = oracle_mod
+    c = next(c for c in golden("hpsi_cases.json")["cases"] if c["name"] == case)
+    H = O.Op(c["H"])
+    psi = O.WF.from_fixture(c["psi"])
+    out = O.operator_psi(H, psi)
+    ref = O.WF.from_fixture(c["Hpsi"])
+    # single-threaded reference: the basis order is the (determinant, term) visiting order
+    assert np.array_equal(out.det, ref.det)
+    assert rel_err(out.val, ref.val) < 1e-12
+    outr = O.operator_psi(H, psi, c["restrictions"])
+    refr = O.WF.from_fixture(c["Hpsir"])
+    assert np.array_equal(outr.det, refr.det)
+    assert rel_err(outr.val, refr.val) < 1e-12
+
+
+@pytest.mark.parametrize("case", [c["name"] for c in golden("hpsi_cases.json")["cases"]])
+def test_conserve_basis_is_projection_of_growing(oracle_mod, case):
+    O = oracle_mod
+    c = next(c for c in golden("hpsi_cases.json")["cases"] if c["name"] == case)
+    H = O.Op(c["H"])
+    psi = O.WF.from_fixture(c["psi"])
+    y = O.apply_conserve(H, psi)
+    ref = O.WF.from_fixture(c["Hpsi"]).as_dict()
+    want = np.array([ref.get(bytes(r), 0.0) for r in psi.det])
+    assert rel_err(y, want) < 1e-12
+
+
+def test_ladder_sign_examples(oracle_mod):
+    O = oracle_mod
+    # c^dag_1 c^dag_0 c_1 c_0 on |1100> gives -|1100> (orbital 0 first, MSB-first bytes)
+    d = O.dets_to_bytes(["1100"], 4)[0].copy()
+    ops = np.array([0, 1, 0 | O.CREATION, 1 | O.CREATION], dtype=np.uint16)
+    assert O.lib().qo_ladder(O._p(d), O._p(ops), 4) == -1
+    assert O.bytes_to_dets([d], 4) == ["1100"]
+    # c^dag_9 c_2 on 10 orbitals: crosses bytes; sign = (-1)^(#occupied between)
+    d = O.dets_to_bytes(["1110000010"], 10)[0].copy()
+    ops = np.array([2, 9 | O.CREATION], dtype=np.uint16)
+    s = O.lib().qo_ladder(O._p(d), O._p(ops), 2)
+    assert O.bytes_to_dets([d], 10) == ["1100000011"]
+    # c_2: two occupied below (0,1) -> +; c^dag_9: occupied below 9 are 0,1,8 -> -
+    assert s == -1
+
+
+def test_chain_golden_tables(oracle_mod):
+    """TestScripts/CreateSpectra.Quanty: Lanczos on the impurity + 5-site chain reproduces the
+    golden response functions at the test's omega list to the test's 1e-12."""
+    O = oracle_mod
+    g = golden("chain_spectra.json")
+    for c in g["combos"]:
+        H = O.Op(g[c["H"]])
+        T = O.Op(g[c["T"]])
+        psi = O.WF.from_fixture(g[c["psi"]])
+        Tpsi = O.operator_psi(T, psi)
+        a, b = O.lanczos_tridiag(H, Tpsi, 200, EPS_DEFAULT, EPS_DEFAULT)
+        # CreateSpectra returns the table shifted by -<psi|H|psi> (ShiftTriDiagonalMatrix)
+        E0 = _expectation(O, H, psi)
+        ref = c["ref_tri"]
+        k = 12
+        assert np.allclose(a[1:k] - E0, ref["a"][1:k], atol=1e-10)
+        assert np.allclose(b[:k], ref["b"][:k], atol=1e-10)
+        gamma = g["gamma"]
+        shifted = a - np.r_[0, np.full(len(a) - 1, E0)]
+        got = [O.cf_spectrum(shifted, b, 0.0, w, 0.0, 0, gamma)[0] for w in g["omega"]]
+        gold = [complex(*z) for z in c["golden_G"]]
+        assert max(abs(x - y) for x, y in zip(got, gold)) < g["threshold"]
+
+
+def _expectation(O, H, psi):
+    """<psi|H|psi> with the reference's growing-basis H*psi and hashed dot."""
+    Hpsi = O.operator_psi(H, psi).as_dict()
+    return float(np.real(sum(np.conj(v) * Hpsi.get(bytes(r), 0.0) for r, v in zip(psi.det, psi.val))))
+
+
+def test_fshell_eigenvalues_match_mathematica(oracle_mod):
+    """TestScripts/Eigensystem.Quanty f-shell atom: exact diagonalisation on the closed basis
+    reproduces the Mathematica eigenvalues."""
+    O = oracle_mod
+    g = golden("fshell_eigen.json")
+    H = O.Op(g["H"])
+    basis = O.enumerate_restricted(14, g["restrictions"])
+    assert len(basis.val) == math.comb(14, 6)
+    w, _ = O.exact_eigensystem(H, basis, 10)
+    assert np.max(np.abs(w - np.array(g["expected_mathematica"]))) < 1e-10
+    assert np.max(np.abs(w - np.array(g["energies_tight"]))) < 1e-10
+
+
+@pytest.mark.parametrize("fx", ["c0_xas.json", "c1_lf.json"])
+def test_xas_spectra_match_reference(oracle_mod, fx):
+    O = oracle_mod
+    g = golden(fx)
+    HX = O.Op(g["HX"])
+    opts = g["spectra_opts"]
+    ntri = opts.get("NTri", 200)
+    emin, emax, ne, gamma = opts["Emin"], opts["Emax"], opts["NE"], opts["Gamma"]
+    de = (emax - emin) / ne
+    spec = g["spec_eps0"]
+    k = 0
+    for T in ("Tx", "Ty", "Tz"):
+        Top = O.Op(g[T])
+        for p in g["psi"]:
+            psi = O.WF.from_fixture(p)
+            E0 = _expectation(O, HX, psi)
+            Tpsi = O.operator_psi(Top, psi)
+            a, b = O.lanczos_tridiag(HX, Tpsi, ntri, 0.0, max(gamma, 0.0))
+            G = O.cf_spectrum(a, b, E0, emin, de, ne, gamma)
+            ref = np.array(spec["re"][k]) + 1j * np.array(spec["im"][k])
+            assert rel_err(G, ref) < 1e-8, (T, k, rel_err(G, ref))
+            ta = g["tri_eps0"][k]
+            assert abs(b[0] - ta["b"][0]) < 1e-12
+            assert abs(a[1] - E0 - ta["a"][1]) < 1e-10
+            k += 1
+
+
+def test_ground_energies_match_reference(oracle_mod):
+    O = oracle_mod
+    for fx in ("c0_xas.json", "c1_lf.json"):
+        g = golden(fx)
+        H = O.Op(g["H"])
+        basis = _sector(O, g)
+        w, _ = O.exact_eigensystem(H, basis, 3)
+        assert np.max(np.abs(w - np.array(g["energies_krylov"]))) < 1e-10, (fx, w, g["energies_krylov"])
+
+
+def _sector(O, g):
+    """All determinants of the restricted sector, built from combinations (2^26 is too many
+    to scan in Python)."""
+    import itertools
+    nf = g["H"]["nf"]
+    groups = []
+    for mask, lo, hi in g["restrictions"]:
+        assert lo == hi
+        groups.append(([i for i, ch in enumerate(mask) if ch == "1"], lo))
+    dets = []
+    for combo in itertools.product(*[itertools.combinations(idx, n) for idx, n in groups]):
+        s = ["0"] * nf
+        for part in combo:
+            for i in part:
+                s[i] = "1"
+        dets.append("".join(s))
+    return O.WF(nf, O.dets_to_bytes(dets, nf), np.ones(len(dets)))
