@@ -1,0 +1,310 @@
+"""Benchmark: fixed-basis H*psi on the large discretised-bath Anderson impurity.
+
+Workload (the largest single-GPU configuration of the reference's benchmark set): 86
+spin-orbitals (2p + 3d + 7 bath shells of 10), 47,481,880 determinants in 128-bit words,
+complex FP64 amplitudes; see quanty_gb300/workloads.py.  One step = one H*psi over the whole
+basis (OperatorPsiConserveBasisPreAllocated semantics).  Metric: determinant x term
+applications per second (N_det * N_terms / t), the work unit the reference's loop evaluates.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the reference algorithm on the host cores: the C restatement of the
+reference's push-form H*psi under OpenMP with all host threads, on a bounded sample of source
+rows of the same basis each step (the reference itself cannot be built on the GPU host: its
+sources are not there).  With N > 1 every rank runs an independent replica (the path does not
+shard); rank 0 prints the line.
+"""
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--shells", type=int, default=7)
+    p.add_argument("--cpu-seconds", type=float, default=15.0)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """DRAM bytes per launch of the H*psi kernel from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "hpsi_anderson86.md")
+    if not os.path.exists(p):
+        return None
+    m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", open(p).read())
+    return float(m.group(1)) if m else None
+
+
+def build_workload(api, shells):
+    from quanty_gb300 import workloads
+    H, R, seed, info = workloads.anderson_impurity(nshell=shells)
+    eng = api.engine()
+    basis = api.closure(H, api.dets_to_bytes([seed], H.nf), H.nf, R, -1, eng)
+    return H, R, basis, info
+
+
+def cpu_baseline(api, H, basis, seconds, threads=None):
+    """The reference's push-form H*psi (oracle restatement, OpenMP, all host threads) on the
+    first S source rows of the full basis, S sized for about `seconds` of work."""
+    from oracle import oracle as O
+    O.build()
+    dets = basis.dets_bytes()
+    n = len(dets)
+    rng = np.random.default_rng(0)
+    x = rng.normal(size=n) + 1j * rng.normal(size=n)
+    op = O.Op({"nf": H.nf, "terms": [[list(t[0]), t[1].real, t[1].imag] for t in H.terms]})
+    wf = O.WF(H.nf, dets, x)
+    h = wf.handle()
+    L = O.lib()
+    y = np.zeros(2 * n)
+    S = 2000
+    t0 = time.perf_counter()
+    L.qo_apply_conserve(*op.args(), h, 0, S, O._p(y))
+    dt = time.perf_counter() - t0
+    S2 = int(min(n, max(S, S * seconds / max(dt, 1e-6))))
+    t0 = time.perf_counter()
+    L.qo_apply_conserve(*op.args(), h, 0, S2, O._p(y))
+    dt = time.perf_counter() - t0
+    L.qo_wf_free(h)
+    nterms = op.nterms
+    return {"value": S2 * nterms / dt / 1e9, "unit": "Gdet·terms/s", "cores": O.num_threads(), "kind": "port",
+            "sample": "first %d of %d source determinants, full basis as lookup target, %d terms, %.1f s" %
+                      (S2, n, nterms, dt)}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    from oracle import oracle as O
+    O.build()
+    from quanty_gb300 import workloads
+    # the basis comes from the same closure rules, enumerated on the host without a GPU
+    H, R, seed, info = workloads.anderson_impurity(nshell=args.shells)
+    dets = workloads.anderson_sector_bytes(info, H.nf)
+    n = len(dets)
+    rng = np.random.default_rng(0)
+    x = rng.normal(size=n) + 1j * rng.normal(size=n)
+    op = O.Op({"nf": H.nf, "terms": [[list(t[0]), t[1].real, t[1].imag] for t in H.terms]})
+    wf = O.WF(H.nf, dets, x)
+    h = wf.handle()
+    L = O.lib()
+    y = np.zeros(2 * n)
+    S = 1000
+    t0 = time.perf_counter()
+    L.qo_apply_conserve(*op.args(), h, 0, S, O._p(y))
+    dt = time.perf_counter() - t0
+    per_step = max(10.0, 60.0 / max(args.steps + args.warmup, 1))
+    S2 = int(min(n, max(S, S * per_step / max(dt, 1e-6))))
+    for _ in range(args.warmup):
+        L.qo_apply_conserve(*op.args(), h, 0, min(S2, 1000), O._p(y))
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        L.qo_apply_conserve(*op.args(), h, 0, S2, O._p(y))
+        times.append(time.perf_counter() - t0)
+    L.qo_wf_free(h)
+    t = sum(times) / len(times)
+    val = S2 * op.nterms / t / 1e9
+    line = {"impl": "reference", "metric": "H·ψ det·terms/s", "value": val, "unit": "Gdet·terms/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
+            "data": "synthetic", "config": {"workload": "anderson_impurity_86so_hpsi", "n_det": n,
+                                           "n_terms": op.nterms},
+            "cpu_baseline": {"value": val, "unit": "Gdet·terms/s", "cores": O.num_threads(), "kind": "port",
+                             "sample": "first %d source determinants per step" % S2},
+            "e2e": {"value": val, "unit": "Gdet·terms/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    import torch
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    from quanty_gb300 import build
+    build.build()
+    from quanty_gb300 import api
+    api._engine = api.Engine(local)
+    eng = api.engine()
+    t_setup = time.perf_counter()
+    H, R, basis, info = build_workload(api, args.shells)
+    n = basis.n
+    t_setup = time.perf_counter() - t_setup
+    nterms = H.info()["nterms"]
+    nnz = api.count_nnz(H, basis)
+    # CPU baseline in a background thread (ctypes releases the GIL) while the GPU is timed
+    cpu = {}
+    cpu_thread = None
+    if rank == 0 and not args.no_cpu_baseline:
+        def go():
+            try:
+                cpu.update(cpu_baseline(api, H, basis, args.cpu_seconds))
+            except Exception as e:  # reported, never fatal to the GPU number
+                cpu.update({"value": None, "error": str(e)})
+        cpu_thread = threading.Thread(target=go, daemon=True)
+    rng = np.random.default_rng(1)
+    x = torch.from_numpy(rng.normal(size=(n, 1)) + 1j * rng.normal(size=(n, 1))).cuda()
+    y = eng.empty(n)
+    stream = torch.cuda.current_stream()
+
+    def step():
+        eng.check(eng.L.qg_apply(eng.ctx, H.handle(), basis.h, basis.h, api._ptr(x), api._ptr(y), 1))
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+    if cpu_thread is not None:
+        cpu_thread.start()
+    clocks = Clocks(local)
+    clocks.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    l0 = eng.launches()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        step()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    launches = eng.launches() - l0
+    # e2e: the host-buffer entry point, pinned host memory, copies inside the timed region
+    xh = torch.empty((n, 1), dtype=torch.complex128).pin_memory()
+    xh.copy_(x.cpu())
+    yh = torch.empty((n, 1), dtype=torch.complex128).pin_memory()
+    for _ in range(2):
+        eng.check(eng.L.qg_apply_host(eng.ctx, H.handle(), basis.h, basis.h, api._ptr(xh), api._ptr(yh), 1))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        eng.check(eng.L.qg_apply_host(eng.ctx, H.handle(), basis.h, basis.h, api._ptr(xh), api._ptr(yh), 1))
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    clk = clocks.stop()
+    t_ms = torch.tensor([ms, e2e_s * 1e3], device="cuda")
+    if dist:
+        dist.all_reduce(t_ms, op=dist.ReduceOp.MAX)
+    ms, e2e_ms = float(t_ms[0]), float(t_ms[1])
+    if cpu_thread is not None:
+        cpu_thread.join()
+    if rank != 0:
+        return 0
+    units = n * nterms * world
+    value = units / (ms * 1e-3) / 1e9
+    e2e_val = units / (e2e_ms * 1e-3) / 1e9
+    W = 16
+    term_bytes = nterms * (3 * W + 16) + 400 * (W + 16)
+    alg_bytes = n * (W + 16 + 16) + nnz * 16 + term_bytes
+    peak, peak_kind = measured_peak()
+    achieved = alg_bytes / (ms * 1e-3) / 1e9
+    line = {
+        "metric": "H·ψ det·terms/s", "value": value, "unit": "Gdet·terms/s", "n_gpus": world, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "c128", "data": "synthetic",
+        "config": {"workload": "anderson_impurity_86so_hpsi", "n_det": n, "n_terms": nterms, "nnz": nnz,
+                   "det_words_bits": 128, "l2": "inputs larger than L2 (x, y %d MB each)" % (n * 16 // 2**20),
+                   "setup_s": round(t_setup, 2), "parallelism": "replicas" if world > 1 else "single"},
+        "e2e": {"value": e2e_val, "unit": "Gdet·terms/s", "h2d_bytes_per_step": n * 16, "d2h_bytes_per_step": n * 16,
+                "ms_per_step": e2e_ms},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": profiled_traffic(), "peak_source": peak_kind,
+                     "algorithmic_bytes_per_launch": alg_bytes},
+        "cpu_baseline": cpu or None,
+        "clocks": clk,
+        "gpu_launches": launches,
+    }
+    print(json.dumps(line))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,199 @@
+/*
+ * qgpu.h -- C ABI of the GB300 (sm_103a) engine for second-quantized operators acting on
+ * Slater-determinant wavefunctions, and the Lanczos / block-Lanczos / continued-fraction
+ * iterations built on it.
+ *
+ * Every entry point is plain C: pointers, sizes and handles; no C++ or torch types.  Each
+ * returns a qg_status (0 = ok), the reference's convention of a uint32_t status where 1 means
+ * "out of memory" (Core/Lanczos.cpp:2196-2206 retries on it).  Pointers named *_dev are
+ * device pointers (cudaMalloc or any allocator); *_host are host pointers.  All work is
+ * issued on the context's CUDA stream; functions that return host data synchronise it.
+ *
+ * Layout at the boundary is the reference's:
+ *   - a determinant is NWord = ceil(nf/8) bytes, orbital i in byte i>>3 under mask
+ *     128>>(i&7) (Core/OperatorWaveFunction.cpp:7-43, Core/WaveFunctionArithmetic.cpp:130);
+ *   - an operator term is a ladder string o[0..len-1], o[0] acting first, bit 15 set for a
+ *     creation operator (CrAnMask, Core/StructDef.cpp:46; Core/OperatorWaveFunction.cpp:98);
+ *   - amplitudes are complex FP64, interleaved (re, im) -- the reference's ValueRe/ValueIm
+ *     pair (Core/StructDef.cpp:188-206) without the 2^14 blocking and without the unused
+ *     element 0 (Core/StructDef.cpp:33-42, :184-187).
+ * A multi-vector block stores vector k of determinant r at [r * nvec + k].
+ */
+#ifndef QGPU_H
+#define QGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  QG_OK = 0,
+  QG_ERR_OOM = 1,        /* allocation failed (reference: return 1 -> truncate and retry) */
+  QG_ERR_TABLE_FULL = 2, /* a device hash table ran out of room; the caller may retry */
+  QG_ERR_TIMEOUT = 3,    /* a bounded device wait or probe gave up */
+  QG_ERR_ARG = 4,        /* bad argument (unsupported size, null pointer, mismatch) */
+  QG_ERR_CUDA = 5,       /* CUDA runtime error; qg_last_error() has the text */
+  QG_ERR_NOT_HERMITIAN = 6
+} qg_status;
+
+typedef struct qg_context_s *qg_context;
+typedef struct qg_operator_s *qg_operator;
+typedef struct qg_basis_s *qg_basis;
+
+/* Occupation windows on orbital subsets (DeterminantRestrictionType,
+ * Core/StructDef.cpp:211-221): for each r < n the number of occupied orbitals under
+ * masks[r*nword .. r*nword+nword-1] must lie in [min[r], max[r]]
+ * (QDetNotRestricted, Core/OperatorWaveFunction.cpp:2260). */
+typedef struct {
+  int32_t n;
+  const uint8_t *masks; /* n * nword bytes, reference byte layout */
+  const int32_t *min;
+  const int32_t *max;
+} qg_restrictions;
+
+/* ------------------------------------------------------------------ context */
+
+/* One context per host thread (the reference is called from the single Lua thread). */
+qg_status qg_init(int device, qg_context *ctx);
+qg_status qg_finalize(qg_context ctx);
+/* stream: a cudaStream_t cast to void*; NULL selects the context's own stream. */
+qg_status qg_set_stream(qg_context ctx, void *stream);
+void *qg_get_stream(qg_context ctx);
+const char *qg_last_error(qg_context ctx);
+/* Number of kernels this library launched on the context since qg_init (for accounting). */
+int64_t qg_launch_count(qg_context ctx);
+qg_status qg_synchronize(qg_context ctx);
+
+/* ------------------------------------------------------------------ operators */
+
+/* Upload an operator: nterms ladder strings (lengths term_len[], codes concatenated in ops[])
+ * with complex values.  Replaces the OperatorType the reference's dispatchers receive
+ * (Core/StructDef.cpp:223-249) as built by NewOperator (LuaInterface/ssp.cpp:572).  Terms
+ * that annihilate twice or create twice on the same orbital are dropped (they vanish on
+ * every determinant).  nf <= 127. */
+qg_status qg_operator_create(qg_context ctx, int32_t nf, int32_t nterms, const int32_t *term_len,
+                             const uint16_t *ops, const double *v_re, const double *v_im,
+                             qg_operator *op);
+qg_status qg_operator_destroy(qg_operator op);
+/* Counts after upload: kept terms, distinct annihilation groups, and whether the term list is
+ * closed under Hermitian conjugation with conjugated values (QOperatorHermitian,
+ * Core/OperatorArithmetic.cpp:6517; 1 = Hermitian within 1e-12 relative). */
+qg_status qg_operator_info(qg_operator op, int32_t *nterms, int32_t *ngroups, int32_t *hermitian);
+
+/* ------------------------------------------------------------------ bases */
+
+/* Build a basis from n determinants (reference byte layout, n * ceil(nf/8) bytes, host
+ * memory).  Duplicates are merged.  The basis is kept sorted on the device (its own order);
+ * perm_host (optional, n entries) receives for each input determinant its index in the
+ * basis.  This is the determinant + hash part of WaveFunctionType
+ * (Core/StructDef.cpp:188-206, Core/Hash.cpp:163). */
+qg_status qg_basis_create(qg_context ctx, int32_t nf, int64_t n, const uint8_t *dets_host,
+                          qg_basis *basis, int64_t *perm_host);
+qg_status qg_basis_destroy(qg_basis basis);
+int64_t qg_basis_size(qg_basis basis);
+/* Copy the basis determinants out in reference byte layout (host, size * nword bytes). */
+qg_status qg_basis_get_dets(qg_basis basis, uint8_t *dets_host);
+/* Index of each of n determinants in the basis (-1 if absent); host in, host out. */
+qg_status qg_basis_find(qg_basis basis, int64_t n, const uint8_t *dets_host, int64_t *index_host);
+
+/* Targets of op on the determinants of basis_in: every determinant reached with a non-zero
+ * sign by some term (and passing the restrictions, if any).  This is the basis OperatorPsi
+ * builds (Core/OperatorWaveFunction.cpp:1750-1823; :2288-2361 with restrictions;
+ * dispatchers :5573, :5598); the amplitudes follow from qg_apply(op, out, basis_in, ...).
+ * Device open-addressing hash with atomicCAS insert. */
+qg_status qg_operator_psi_basis(qg_context ctx, qg_operator op, qg_basis basis_in,
+                                const qg_restrictions *res, qg_basis *basis_out);
+
+/* Closure of a seed basis under repeated application of op (breadth first, device hash),
+ * within the restrictions: the basis the reference's growing Lanczos / BlockGroundState
+ * loops reach (Core/Lanczos.cpp:2169-2263 grows one H*psi per step;
+ * Core/BlockLanczos.cpp:5843-5884 grows until converged).  max_rounds < 0 means until
+ * closed; rounds_done receives the number of expansion rounds made. */
+qg_status qg_basis_closure(qg_context ctx, qg_operator op, qg_basis seed, const qg_restrictions *res,
+                           int32_t max_rounds, qg_basis *closed, int32_t *rounds_done);
+
+/* Union of two bases on the same orbitals (ComplexWaveFunctionAddMultipliedUnionBasis's
+ * basis, Core/ComplexWaveFunctionArithmetic.cpp:601). */
+qg_status qg_basis_union(qg_context ctx, qg_basis a, qg_basis b, qg_basis *out);
+
+/* Re-index amplitudes between bases: y[rows of dst] = x[rows of src] for determinants present
+ * in both, zero elsewhere (nvec vectors, device pointers). */
+qg_status qg_basis_map(qg_context ctx, qg_basis src, const double *x_dev, qg_basis dst, double *y_dev,
+                       int32_t nvec);
+
+/* ------------------------------------------------------------------ H * psi */
+
+/* y = op x with x on basis_src and y on basis_dst (nvec vectors each), pull form: every row
+ * of y gathers its sources through the adjoint ladder strings, so no float atomics are
+ * used.  With basis_dst == basis_src this is OperatorPsiConserveBasisPreAllocated
+ * (Core/OperatorWaveFunction.cpp:784-1127, dispatcher :5541): contributions whose source
+ * lies outside the basis are absent.  With basis_dst = qg_operator_psi_basis(op, basis_src)
+ * it gives the amplitudes of OperatorPsi (:1750, dispatcher :5598).  The multi-vector form is
+ * BlockOperatorPsi (Core/BlockWaveFunctionArithmetic.cpp:1575). */
+qg_status qg_apply(qg_context ctx, qg_operator op, qg_basis basis_dst, qg_basis basis_src,
+                   const double *x_dev, double *y_dev, int32_t nvec);
+
+/* qg_apply with host buffers: copies x_host to the device, applies, copies y back (the
+ * reference's calling convention, where psi and Opsi live in host memory).  Device staging
+ * buffers are kept in the context between calls; pinned host buffers give full copy speed. */
+qg_status qg_apply_host(qg_context ctx, qg_operator op, qg_basis basis_dst, qg_basis basis_src,
+                        const double *x_host, double *y_host, int32_t nvec);
+
+/* Number of non-zero (row, term) connections of qg_apply(op, b, b) (sources inside b). */
+qg_status qg_count_nnz(qg_context ctx, qg_operator op, qg_basis basis, int64_t *nnz);
+
+/* <psi|op|psi> for nvec vectors on one basis, complex result per vector (host out)
+ * (PsiOperatorPsi / PsiHermitianOperatorPsi, Core/OperatorWaveFunction.cpp:5680, :5710). */
+qg_status qg_expectation(qg_context ctx, qg_operator op, qg_basis basis, const double *x_dev,
+                         int32_t nvec, double *val_host);
+
+/* ------------------------------------------------------------------ vector algebra */
+
+/* <x_k|y_k> per vector (conjugating x; ComplexWaveFunctionDotProductSameBasis,
+ * Core/ComplexWaveFunctionArithmetic.cpp:961), host out, 2*nvec doubles. */
+qg_status qg_dot(qg_context ctx, int64_t n, int32_t nvec, const double *x_dev, const double *y_dev,
+                 double *dot_host);
+/* ||x_k|| per vector (ComplexWaveFunctionCalculateNorm, :870), host out. */
+qg_status qg_norm(qg_context ctx, int64_t n, int32_t nvec, const double *x_dev, double *norm_host);
+/* y_k += alpha_k x_k (alpha complex per vector, host; ...AddComplexMultipliedSameBasis :541). */
+qg_status qg_axpy(qg_context ctx, int64_t n, int32_t nvec, const double *alpha_host, const double *x_dev,
+                  double *y_dev);
+
+/* ------------------------------------------------------------------ Krylov drivers */
+
+/* Three-term Lanczos tridiagonalisation of op from nvec starting vectors at once (all on
+ * one basis), NTri steps, the reference's truncation schedule (drop |v|<=eps/err with
+ * err *= b^2/(b^2+4 gamma^2)) applied as zeroing on the fixed basis; no reorthogonalisation
+ * (LanczosTriDiagonalize{RC,CC,MC,RR} and the Restricted variants, Core/Lanczos.cpp:1905-2830,
+ * dispatchers :5228, :5274).  v0_dev is not modified.  a_host receives nvec*(ntri+1)
+ * entries (vector k at [k*(ntri+1)], a[0] = 0), b_host nvec*ntri (b[0] = |v0_k|).
+ * krylov_dev (optional, ntri * n * nvec complex) receives the normalised Krylov vectors
+ * (LanczosTriDiagonalizeKrylov, :5405). */
+qg_status qg_lanczos_tridiag(qg_context ctx, qg_operator op, qg_basis basis, const double *v0_dev,
+                             int32_t nvec, int32_t ntri, double eps, double gamma, double *a_host,
+                             double *b_host, double *krylov_dev);
+
+/* Continued fraction G_s(w_k) = a0 + b0^2/(w - a1 + i g/2 - b1^2/(...)) for nspec spectra
+ * and w_k = emin + k*de + e0[s], k = 0..ne, in one kernel (TriDiagonalMatrixToSpectrum,
+ * Core/Spectral.cpp:1433).  Spectrum s uses a[s*(ntri+1) ..], b[s*ntri ..]; host in; g_host
+ * receives nspec*(ne+1) complex values (interleaved). */
+qg_status qg_cf_spectra(qg_context ctx, int32_t nspec, int32_t ntri, const double *a_host,
+                        const double *b_host, const double *e0_host, double emin, double de,
+                        int32_t ne, double gamma, double *g_host);
+
+/* Lowest nvec eigenpairs of a Hermitian op on a fixed basis by restarted block (band)
+ * Lanczos with full reorthogonalisation (BlockLanczosGroundStateConserveBasis,
+ * Core/BlockLanczos.cpp:5707, its Krylov solver :5350).  x_dev holds nvec start vectors
+ * on input (n * nvec) and the eigenvectors on output; energies_host nvec doubles.
+ * tol is the reference's "Zero" (variance convergence), max_krylov its NKrylovMax. */
+qg_status qg_block_groundstate(qg_context ctx, qg_operator op, qg_basis basis, int32_t nvec,
+                               double *x_dev, double *energies_host, double tol, int32_t max_krylov,
+                               int32_t max_restarts, int32_t *iterations);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* QGPU_H */

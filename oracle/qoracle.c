@@ -432,3 +432,78 @@ int qo_num_threads(void)
   return 1;
 #endif
 }
+
+/* ------------------------------------------------------------------ enumeration */
+
+/* All determinants on nf orbitals with exactly nel electrons that satisfy the occupation
+ * windows (nres masks in the reference byte layout), in lexicographic order of the
+ * determinant string (orbital 0 first, '1' before '0' reversed: ascending binary).  Depth-first
+ * over orbitals with pruning on every window.  Returns a malloc'd n*nword byte array. */
+typedef struct {
+  int nf, nword, nres, nel;
+  const uint8_t *masks;
+  const int *mn, *mx;
+  int *cnt;      /* electrons so far per window */
+  int *left;     /* [orbital][window]: mask orbitals at index >= orbital */
+  uint8_t *cur;
+  uint8_t *out;
+  int64_t n, cap;
+} qo_enum_state;
+
+static int qo_in(const uint8_t *m, int i) { return (m[i >> 3] & (128 >> (i & 7))) != 0; }
+
+static void qo_enum_rec(qo_enum_state *s, int i, int ne)
+{
+  int r, ok;
+  if (ne > s->nel || ne + (s->nf - i) < s->nel) return;
+  for (r = 0; r < s->nres; r++) {
+    if (s->cnt[r] > s->mx[r]) return;
+    if (s->cnt[r] + s->left[i * s->nres + r] < s->mn[r]) return;
+  }
+  if (i == s->nf) {
+    if (s->n == s->cap) {
+      s->cap = s->cap ? 2 * s->cap : 1024;
+      s->out = (uint8_t *)realloc(s->out, (size_t)s->cap * s->nword);
+    }
+    memcpy(s->out + s->n * s->nword, s->cur, (size_t)s->nword);
+    s->n++;
+    return;
+  }
+  /* orbital i empty first, then occupied: ascending order of the reversed-bit key */
+  qo_enum_rec(s, i + 1, ne);
+  ok = 1;
+  for (r = 0; r < s->nres; r++)
+    if (qo_in(s->masks + r * s->nword, i)) s->cnt[r]++;
+  s->cur[i >> 3] |= (uint8_t)(128 >> (i & 7));
+  if (ok) qo_enum_rec(s, i + 1, ne + 1);
+  s->cur[i >> 3] &= (uint8_t)~(128 >> (i & 7));
+  for (r = 0; r < s->nres; r++)
+    if (qo_in(s->masks + r * s->nword, i)) s->cnt[r]--;
+}
+
+uint8_t *qo_enumerate(int nf, int nel, int nres, const uint8_t *masks, const int *mn, const int *mx, int64_t *n_out)
+{
+  qo_enum_state s;
+  int i, r;
+  memset(&s, 0, sizeof(s));
+  s.nf = nf;
+  s.nword = (nf + 7) / 8;
+  s.nres = nres;
+  s.nel = nel;
+  s.masks = masks;
+  s.mn = mn;
+  s.mx = mx;
+  s.cnt = (int *)calloc((size_t)(nres > 0 ? nres : 1), sizeof(int));
+  s.left = (int *)calloc((size_t)(nf + 1) * (nres > 0 ? nres : 1), sizeof(int));
+  s.cur = (uint8_t *)calloc((size_t)s.nword, 1);
+  for (i = nf - 1; i >= 0; i--)
+    for (r = 0; r < nres; r++) s.left[i * nres + r] = s.left[(i + 1) * nres + r] + qo_in(masks + r * s.nword, i);
+  qo_enum_rec(&s, 0, 0);
+  free(s.cnt);
+  free(s.left);
+  free(s.cur);
+  *n_out = s.n;
+  return s.out;
+}
+
+void qo_free(void *p) { free(p); }

@@ -1,0 +1,544 @@
+"""Host-side mirror of the reference's operator / wavefunction interface for the H*psi path.
+
+The names follow the reference's Lua and C entry points so code written against them reads the
+same: ``NewOperator``, ``NewWavefunction``, ``OperatorPsi`` (``H*psi``,
+``Core/OperatorWaveFunction.cpp:5598``), ``OperatorPsiConserveBasis`` (:5507/:5541),
+``PsiOperatorPsi`` (:5680), ``LanczosTriDiagonalize`` (``Core/Lanczos.cpp:5274``),
+``TriDiagonalMatrixToSpectrum`` (``Core/Spectral.cpp:1433``), ``CreateSpectra``
+(``LuaInterface/ssp.cpp:1906``) and ``Eigensystem`` (``LuaInterface/ssp.cpp:4039``).  Options
+take the reference's names and defaults (``InitConvergenceSettings``,
+``Core/StructDef.cpp:291-320``).  Every numerical step runs in libqgpu.so on the GPU; this module
+only converts layouts, owns handles and sequences calls.
+"""
+import ctypes as C
+import math
+
+import numpy as np
+
+from . import qgpu
+
+CREATION = 0x8000
+DBL_EPSILON = np.finfo(float).eps
+DEFAULTS = {
+    "DenseBorder": 1513, "NKrylovStart": 100, "NKrylovMax": 500, "NKrylovStep": 10, "NTri": 200,
+    "NTri1": 100, "NTri2": 100, "Zero": 100 * math.sqrt(DBL_EPSILON), "Epsilon": math.sqrt(DBL_EPSILON) / 100,
+    "Emin": None, "Emax": None, "NE": 1000, "Gamma": 0.0, "NBitsKey": 16,
+}
+
+_engine = None
+
+
+def _torch():
+    import torch
+    if not torch.cuda.is_available():
+        raise RuntimeError("quanty_gb300 needs a CUDA GPU; there is no CPU path")
+    return torch
+
+
+class Engine:
+    """One qg_context on one device, running on torch's current CUDA stream."""
+
+    def __init__(self, device=0):
+        torch = _torch()
+        self.torch = torch
+        self.L = qgpu.load()
+        self.device = device
+        torch.cuda.set_device(device)
+        h = C.c_void_p()
+        self.check(self.L.qg_init(device, C.byref(h)), ctx=None)
+        self.ctx = h
+        stream = torch.cuda.current_stream(device).cuda_stream
+        self.check(self.L.qg_set_stream(self.ctx, C.c_void_p(stream)))
+
+    def check(self, st, ctx="self"):
+        if st != 0:
+            msg = ""
+            if ctx == "self" and getattr(self, "ctx", None):
+                msg = self.L.qg_last_error(self.ctx).decode(errors="replace")
+            raise qgpu.QGError(st, msg)
+
+    def launches(self):
+        return int(self.L.qg_launch_count(self.ctx))
+
+    def empty(self, n, nvec=1):
+        return self.torch.zeros((max(n, 1), nvec), dtype=self.torch.complex128, device="cuda:%d" % self.device)
+
+    def close(self):
+        if getattr(self, "ctx", None):
+            self.L.qg_finalize(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def engine():
+    global _engine
+    if _engine is None:
+        _engine = Engine(0)
+    return _engine
+
+
+def _ptr(a):
+    return C.c_void_p(a.ctypes.data) if isinstance(a, np.ndarray) else C.c_void_p(a.data_ptr())
+
+
+def nword(nf):
+    return (nf + 7) // 8
+
+
+# ----------------------------------------------------------------------------- determinants
+
+def dets_to_bytes(dets, nf):
+    """'0110...' strings (orbital 0 first) -> uint8 (n, ceil(nf/8)), reference byte layout."""
+    nw = nword(nf)
+    n = len(dets)
+    bits = np.zeros((n, nw * 8), dtype=np.uint8)
+    if n:
+        arr = np.frombuffer("".join(d.replace(" ", "")[:nf].ljust(nf, "0") for d in dets).encode(), dtype=np.uint8)
+        bits[:, :nf] = (arr.reshape(n, nf) == ord("1"))
+    return np.packbits(bits, axis=1, bitorder="big")
+
+
+def bytes_to_dets(b, nf):
+    bits = np.unpackbits(np.asarray(b, dtype=np.uint8), axis=1, bitorder="big")[:, :nf]
+    return ["".join("1" if x else "0" for x in row) for row in bits]
+
+
+# ----------------------------------------------------------------------------- operators
+
+class Operator:
+    """A second-quantized operator: sum of ladder strings with complex values.
+
+    ``terms``: iterable of ``(ops, value)`` where ``ops`` is a sequence of ladder codes with
+    ``ops[0]`` acting first and bit 15 set for a creation operator (the reference's
+    OperatorFixedLengthType strings, ``Core/StructDef.cpp:223``)."""
+
+    def __init__(self, nf, terms, name="Operator"):
+        self.nf = int(nf)
+        self.name = name
+        self.terms = [(tuple(int(o) for o in ops), complex(v)) for ops, v in terms]
+        self._handles = {}
+
+    @classmethod
+    def from_fixture(cls, d):
+        return cls(d["nf"], [(t[0], complex(t[1], t[2])) for t in d["terms"]])
+
+    def handle(self, eng=None):
+        eng = eng or engine()
+        key = id(eng)
+        if key not in self._handles:
+            n = len(self.terms)
+            lens = np.array([len(t[0]) for t in self.terms], dtype=np.int32)
+            flat = np.array([o for t in self.terms for o in t[0]] or [0], dtype=np.uint16)
+            vre = np.array([t[1].real for t in self.terms] or [0.0])
+            vim = np.array([t[1].imag for t in self.terms] or [0.0])
+            h = C.c_void_p()
+            eng.check(eng.L.qg_operator_create(eng.ctx, self.nf, n, _ptr(lens), _ptr(flat), _ptr(vre), _ptr(vim),
+                                               C.byref(h)))
+            self._handles[key] = (eng, h, (lens, flat, vre, vim))
+        return self._handles[key][1]
+
+    def info(self, eng=None):
+        eng = eng or engine()
+        a, b, c = C.c_int32(), C.c_int32(), C.c_int32()
+        eng.check(eng.L.qg_operator_info(self.handle(eng), C.byref(a), C.byref(b), C.byref(c)))
+        return {"nterms": a.value, "ngroups": b.value, "hermitian": bool(c.value)}
+
+    def __add__(self, other):
+        return Operator(self.nf, self.terms + other.terms)
+
+    def __mul__(self, other):
+        if isinstance(other, Wavefunction):
+            return OperatorPsi(self, other)
+        return Operator(self.nf, [(o, v * other) for o, v in self.terms])
+
+    __rmul__ = __mul__
+
+    def __del__(self):
+        for eng, h, _ in self._handles.values():
+            try:
+                if eng.ctx:
+                    eng.L.qg_operator_destroy(h)
+            except Exception:
+                pass
+
+
+def NewOperator(nf, nb, terms):
+    """Lua-style constructor: each term is ``[i1, i2, ..., value]`` with a non-negative index
+    for a creation and a negative index (or -0.0) for an annihilation operator, leftmost factor
+    first as in ``NewOperator(NF, 0, {{0, -0, 1, -1, U}})``."""
+    if nb:
+        raise ValueError("bosons are not supported")
+    out = []
+    for t in terms:
+        *idx, v = t
+        ops = []
+        for i in idx:
+            neg = (i < 0) or (isinstance(i, float) and math.copysign(1.0, i) < 0)
+            ops.append(int(abs(i)) if neg else (int(i) | CREATION))
+        ops.reverse()  # the rightmost factor acts first
+        out.append((ops, v))
+    return Operator(nf, out)
+
+
+# ----------------------------------------------------------------------------- wavefunctions
+
+class Wavefunction:
+    """Determinants (reference byte layout) with complex FP64 amplitudes."""
+
+    def __init__(self, nf, det_bytes, values):
+        self.nf = int(nf)
+        self.det = np.ascontiguousarray(det_bytes, dtype=np.uint8).reshape(-1, nword(nf))
+        self.val = np.ascontiguousarray(values, dtype=np.complex128).reshape(-1)
+        assert len(self.det) == len(self.val)
+
+    @classmethod
+    def from_fixture(cls, d):
+        return cls(d["nf"], dets_to_bytes(d["dets"], d["nf"]), np.array(d["re"]) + 1j * np.array(d["im"]))
+
+    @property
+    def N(self):
+        return len(self.val)
+
+    def dets(self):
+        return bytes_to_dets(self.det, self.nf)
+
+    def as_dict(self):
+        return {bytes(r): v for r, v in zip(self.det, self.val)}
+
+    def norm(self):
+        return float(np.linalg.norm(self.val))
+
+
+def NewWavefunction(nf, nb, entries):
+    if nb:
+        raise ValueError("bosons are not supported")
+    dets = [e[0] for e in entries]
+    vals = [complex(e[1]) for e in entries]
+    return Wavefunction(nf, dets_to_bytes(dets, nf), vals)
+
+
+class Basis:
+    """A device basis (sorted determinants + lookup hash)."""
+
+    def __init__(self, eng, handle, nf):
+        self.eng, self.h, self.nf = eng, handle, nf
+
+    @classmethod
+    def from_bytes(cls, nf, det_bytes, eng=None):
+        eng = eng or engine()
+        det_bytes = np.ascontiguousarray(det_bytes, dtype=np.uint8)
+        n = len(det_bytes)
+        perm = np.zeros(max(n, 1), dtype=np.int64)
+        h = C.c_void_p()
+        eng.check(eng.L.qg_basis_create(eng.ctx, nf, n, _ptr(det_bytes), C.byref(h), _ptr(perm)))
+        b = cls(eng, h, nf)
+        return b, perm[:n]
+
+    @property
+    def n(self):
+        return int(self.eng.L.qg_basis_size(self.h))
+
+    def dets_bytes(self):
+        out = np.zeros((max(self.n, 1), nword(self.nf)), dtype=np.uint8)
+        self.eng.check(self.eng.L.qg_basis_get_dets(self.h, _ptr(out)))
+        return out[:self.n]
+
+    def find(self, det_bytes):
+        det_bytes = np.ascontiguousarray(det_bytes, dtype=np.uint8)
+        out = np.zeros(max(len(det_bytes), 1), dtype=np.int64)
+        self.eng.check(self.eng.L.qg_basis_find(self.h, len(det_bytes), _ptr(det_bytes), _ptr(out)))
+        return out[:len(det_bytes)]
+
+    def __del__(self):
+        try:
+            if self.eng.ctx and self.h:
+                self.eng.L.qg_basis_destroy(self.h)
+        except Exception:
+            pass
+
+
+class _Res:
+    """qg_restrictions built from [(mask string, min, max), ...]."""
+
+    def __init__(self, nf, restrictions):
+        self.r = qgpu.Restrictions()
+        rs = list(restrictions or [])
+        self.masks = dets_to_bytes([m for m, _, _ in rs], nf) if rs else np.zeros((1, nword(nf)), np.uint8)
+        self.mn = np.array([lo for _, lo, _ in rs] or [0], dtype=np.int32)
+        self.mx = np.array([hi for _, _, hi in rs] or [0], dtype=np.int32)
+        self.r.n = len(rs)
+        self.r.masks = self.masks.ctypes.data
+        self.r.min = self.mn.ctypes.data
+        self.r.max = self.mx.ctypes.data
+
+    def ptr(self):
+        return C.byref(self.r) if self.r.n else None
+
+
+def parse_restrictions(R):
+    """Accept the Lua form {NF, NB, {"mask", min, max}, ...} or a list of (mask, min, max)."""
+    if R is None:
+        return None
+    R = list(R)
+    if R and isinstance(R[0], (int, np.integer)):
+        R = R[2:]
+    return [(str(m).replace(" ", ""), int(lo), int(hi)) for m, lo, hi in R]
+
+
+def _upload(eng, basis, perm, values, nvec=1):
+    """Host amplitudes in input order -> device block in basis order (n x nvec)."""
+    torch = eng.torch
+    n = basis.n
+    v = np.zeros((max(n, 1), nvec), dtype=np.complex128)
+    vals = np.asarray(values).reshape(len(perm), nvec)
+    np.add.at(v, perm, vals)
+    return torch.from_numpy(v).to("cuda:%d" % eng.device)
+
+
+# ----------------------------------------------------------------------------- H * psi
+
+def OperatorPsiBasis(O, basis, restrictions=None, eng=None):
+    eng = eng or engine()
+    res = _Res(O.nf, parse_restrictions(restrictions))
+    h = C.c_void_p()
+    eng.check(eng.L.qg_operator_psi_basis(eng.ctx, O.handle(eng), basis.h, res.ptr(), C.byref(h)))
+    return Basis(eng, h, O.nf)
+
+
+def OperatorPsi(O, psi, restrictions=None, eng=None):
+    """O|psi> with basis growth (reference OperatorPsi / OperatorPsiRestricted).  The output
+    determinants are the targets of all non-zero (determinant, term) pairs, in sorted order."""
+    eng = eng or engine()
+    if O.nf != psi.nf:
+        raise ValueError("operator and wavefunction have different numbers of fermions")
+    src, perm = Basis.from_bytes(psi.nf, psi.det, eng)
+    x = _upload(eng, src, perm, psi.val)
+    dst = OperatorPsiBasis(O, src, restrictions, eng)
+    y = eng.empty(dst.n)
+    eng.check(eng.L.qg_apply(eng.ctx, O.handle(eng), dst.h, src.h, _ptr(x), _ptr(y), 1))
+    eng.torch.cuda.synchronize()
+    return Wavefunction(psi.nf, dst.dets_bytes(), y[:dst.n, 0].cpu().numpy())
+
+
+def OperatorPsiConserveBasis(O, psi, eng=None):
+    """O|psi> kept on the basis of psi (reference OperatorPsiConserveBasis[PreAllocated])."""
+    eng = eng or engine()
+    b, perm = Basis.from_bytes(psi.nf, psi.det, eng)
+    x = _upload(eng, b, perm, psi.val)
+    y = eng.empty(b.n)
+    eng.check(eng.L.qg_apply(eng.ctx, O.handle(eng), b.h, b.h, _ptr(x), _ptr(y), 1))
+    yh = y[:b.n, 0].cpu().numpy()
+    return Wavefunction(psi.nf, psi.det, yh[perm])
+
+
+def PsiOperatorPsi(O, psi, eng=None):
+    eng = eng or engine()
+    b, perm = Basis.from_bytes(psi.nf, psi.det, eng)
+    x = _upload(eng, b, perm, psi.val)
+    out = np.zeros(2)
+    eng.check(eng.L.qg_expectation(eng.ctx, O.handle(eng), b.h, _ptr(x), 1, _ptr(out)))
+    return complex(out[0], out[1])
+
+
+def count_nnz(O, basis, eng=None):
+    """Non-zero (row, term) connections of O on a basis (sources inside the basis)."""
+    eng = eng or engine()
+    n = C.c_int64()
+    eng.check(eng.L.qg_count_nnz(eng.ctx, O.handle(eng), basis.h, C.byref(n)))
+    return n.value
+
+
+def closure(O, seed_bytes, nf, restrictions=None, max_rounds=-1, eng=None):
+    eng = eng or engine()
+    seed, _ = Basis.from_bytes(nf, seed_bytes, eng)
+    res = _Res(nf, parse_restrictions(restrictions))
+    h = C.c_void_p()
+    rounds = C.c_int32()
+    eng.check(eng.L.qg_basis_closure(eng.ctx, O.handle(eng), seed.h, res.ptr(), max_rounds, C.byref(h),
+                                     C.byref(rounds)))
+    return Basis(eng, h, nf)
+
+
+# ----------------------------------------------------------------------------- Lanczos + spectra
+
+def lanczos_block(H, basis, x, ntri, eps, gamma, eng=None, krylov=None):
+    """Batched Lanczos on a device basis: x is an (n, nvec) complex CUDA tensor."""
+    eng = eng or engine()
+    nvec = x.shape[1]
+    a = np.zeros(nvec * (ntri + 1))
+    b = np.zeros(nvec * ntri)
+    kp = _ptr(krylov) if krylov is not None else None
+    eng.check(eng.L.qg_lanczos_tridiag(eng.ctx, H.handle(eng), basis.h, _ptr(x), nvec, ntri, eps, gamma, _ptr(a),
+                                       _ptr(b), kp))
+    return a.reshape(nvec, ntri + 1), b.reshape(nvec, ntri)
+
+
+def LanczosTriDiagonalize(H, psi, NTri=200, epsilon=DEFAULTS["Epsilon"], Gamma=None, restrictions=None, eng=None):
+    """Reference LanczosTriDiagonalize[Restricted] (Core/Lanczos.cpp:5228/:5274): returns (a, b)
+    with a[0] = 0 and b[0] = |psi|.  The Krylov space lives on the closure of psi's
+    determinants under H (within the restrictions)."""
+    eng = eng or engine()
+    gamma = epsilon if Gamma is None else Gamma
+    basis = closure(H, psi.det, psi.nf, restrictions, -1, eng)
+    src, perm = Basis.from_bytes(psi.nf, psi.det, eng)
+    xs = _upload(eng, src, perm, psi.val)
+    x = eng.empty(basis.n)
+    eng.check(eng.L.qg_basis_map(eng.ctx, src.h, _ptr(xs), basis.h, _ptr(x), 1))
+    a, b = lanczos_block(H, basis, x, NTri, epsilon, gamma, eng)
+    return a[0], b[0]
+
+
+def TriDiagonalMatrixToSpectrum(E0, a, b, Emin, Emax, NE, Gamma, eng=None):
+    """G(w) for w = Emin + k dE + E0, k = 0..NE (Core/Spectral.cpp:1433); a, b may hold several
+    spectra as rows."""
+    eng = eng or engine()
+    a = np.ascontiguousarray(np.atleast_2d(a), dtype=np.float64)
+    b = np.ascontiguousarray(np.atleast_2d(b), dtype=np.float64)
+    ns, ntri = b.shape
+    e0 = np.ascontiguousarray(np.broadcast_to(np.asarray(E0, dtype=np.float64), (ns,)))
+    g = np.zeros(2 * ns * (NE + 1))
+    de = (Emax - Emin) / NE
+    eng.check(eng.L.qg_cf_spectra(eng.ctx, ns, ntri, _ptr(a), _ptr(b), _ptr(e0), Emin, de, NE, Gamma, _ptr(g)))
+    G = g[0::2] + 1j * g[1::2]
+    return G.reshape(ns, NE + 1)
+
+
+def _opts(options):
+    o = dict(DEFAULTS)
+    if options:
+        items = options.items() if isinstance(options, dict) else options
+        for k, v in items:
+            k = {"epsilon": "Epsilon", "restrictions": "Restrictions", "zero": "Zero"}.get(k, k)
+            o[k] = v
+    return o
+
+
+class Spectra:
+    """CreateSpectra's result: G_s(w) on NE+1 points per spectrum (SpectraType, Core/StructDef.cpp:986)."""
+
+    def __init__(self, G, Emin, Emax, NE, Gamma):
+        self.G, self.Emin, self.Emax, self.NE, self.Gamma = G, Emin, Emax, NE, Gamma
+
+    @property
+    def energies(self):
+        return self.Emin + np.arange(self.NE + 1) * (self.Emax - self.Emin) / self.NE
+
+
+def CreateSpectra(H, T, psi, options=None, eng=None, batched=True):
+    """Reference CreateSpectra, Lanczos branch (LuaInterface/ssp.cpp:2586-2720): spectra of all
+    (T, psi) pairs, ordered iT*Npsi + ipsi.  Returns (Spectra, [(a, b) shifted by -E0]).
+    batched=True runs all pairs as one multi-vector Lanczos on the union basis."""
+    eng = eng or engine()
+    o = _opts(options)
+    Ts = T if isinstance(T, (list, tuple)) else [T]
+    psis = psi if isinstance(psi, (list, tuple)) else [psi]
+    ntri, eps = int(o["NTri"]), float(o["Epsilon"])
+    R = parse_restrictions(o.get("Restrictions"))
+    E0 = [PsiOperatorPsi(H, p, eng).real for p in psis] if o.get("E0") is None else [float(o["E0"])] * len(psis)
+    Tpsi = []
+    for t in Ts:
+        for p in psis:
+            Tpsi.append(OperatorPsi(t, p, R, eng))
+    e0 = np.array([E0[i % len(psis)] for i in range(len(Tpsi))])
+    gamma = float(o["Gamma"])
+    groups = [list(range(len(Tpsi)))] if batched else [[i] for i in range(len(Tpsi))]
+    A = np.zeros((len(Tpsi), ntri + 1))
+    B = np.zeros((len(Tpsi), ntri))
+    for grp in groups:
+        seed = np.concatenate([Tpsi[i].det for i in grp])
+        basis = closure(H, seed, H.nf, R, -1, eng)
+        x = eng.empty(basis.n, len(grp))
+        for c, i in enumerate(grp):
+            src, perm = Basis.from_bytes(H.nf, Tpsi[i].det, eng)
+            xs = _upload(eng, src, perm, Tpsi[i].val)
+            col = eng.empty(basis.n)
+            eng.check(eng.L.qg_basis_map(eng.ctx, src.h, _ptr(xs), basis.h, _ptr(col), 1))
+            x[:, c] = col[:, 0]
+        a, b = lanczos_block(H, basis, x.contiguous(), ntri, eps, max(gamma, eps), eng)
+        A[grp] = a
+        B[grp] = b
+    # pole range -> default Emin/Emax/Gamma (ssp.cpp:2655-2689) when not given
+    emin, emax = o["Emin"], o["Emax"]
+    if emin is None or emax is None or gamma == 0:
+        from numpy.linalg import eigvalsh
+        lo, hi = np.inf, -np.inf
+        for s in range(len(Tpsi)):
+            Tm = np.diag(A[s, 1:]) + np.diag(B[s, 1:], 1) + np.diag(B[s, 1:], -1)
+            w = eigvalsh(Tm)
+            lo, hi = min(lo, w[0] - e0[s]), max(hi, w[-1] - e0[s])
+        if emin is None:
+            emin = lo - 0.125 * (hi - lo)
+        if emax is None:
+            emax = hi + 0.125 * (hi - lo)
+        if gamma == 0:
+            gamma = 10 * (emax - emin) / o["NE"]
+    NE = int(o["NE"])
+    G = TriDiagonalMatrixToSpectrum(e0, A, B, emin, emax, NE, gamma, eng)
+    tri = [(np.r_[0.0, A[s, 1:] - e0[s]], B[s].copy()) for s in range(len(Tpsi))]
+    return Spectra(G, emin, emax, NE, gamma), tri
+
+
+# ----------------------------------------------------------------------------- eigensystem
+
+def enumerate_restricted(nf, restrictions):
+    """All determinants that satisfy occupation windows on disjoint masks (the complete basis
+    the reference builds for small systems, Core/BlockLanczos.cpp:102)."""
+    import itertools
+    masks = [[i for i, ch in enumerate(m) if ch == "1"] for m, _, _ in restrictions]
+    covered = set(i for m in masks for i in m)
+    free = [i for i in range(nf) if i not in covered]
+    seen = set()
+    for a in masks:
+        if seen & set(a):
+            raise ValueError("overlapping restriction masks: enumerate by closure instead")
+        seen |= set(a)
+    choices = []
+    for (m, lo, hi), idx in zip(restrictions, masks):
+        opts = []
+        for k in range(lo, min(hi, len(idx)) + 1):
+            opts.extend(itertools.combinations(idx, k))
+        choices.append(opts)
+    free_opts = [c for k in range(len(free) + 1) for c in itertools.combinations(free, k)] if free else [()]
+    rows = []
+    for combo in itertools.product(*choices, free_opts):
+        s = np.zeros(nf, dtype=np.uint8)
+        for part in combo:
+            for i in part:
+                s[i] = 1
+        rows.append(s)
+    bits = np.zeros((len(rows), nword(nf) * 8), dtype=np.uint8)
+    if rows:
+        bits[:, :nf] = np.array(rows)
+    return np.packbits(bits, axis=1, bitorder="big")
+
+
+def Eigensystem(H, StartRestrictions, Npsi, options=None, eng=None, seed=12345):
+    """Lowest Npsi eigenstates of a Hermitian H (reference Eigensystem -> BlockGroundState,
+    LuaInterface/ssp.cpp:4039, Core/BlockLanczos.cpp:5782).  The basis is the complete set of
+    determinants allowed by the restrictions (or their closure under H); the eigenproblem on it
+    is solved by restarted block Lanczos on the device.  Returns (list of Wavefunction, energies)."""
+    eng = eng or engine()
+    o = _opts(options)
+    R = parse_restrictions(StartRestrictions)
+    dets = enumerate_restricted(H.nf, R)
+    basis, _ = Basis.from_bytes(H.nf, dets, eng)
+    basis = closure(H, basis.dets_bytes(), H.nf, R, -1, eng)
+    n = basis.n
+    rng = np.random.default_rng(seed)
+    x0 = rng.standard_normal((n, Npsi)) + 1j * rng.standard_normal((n, Npsi))
+    x = eng.torch.from_numpy(x0).to("cuda:%d" % eng.device).contiguous()
+    en = np.zeros(Npsi)
+    it = C.c_int32()
+    K = int(min(max(4 * Npsi, 64), 256, n))
+    tol = float(o["Zero"])
+    eng.check(eng.L.qg_block_groundstate(eng.ctx, H.handle(eng), basis.h, Npsi, _ptr(x), _ptr(en), tol, K, 200,
+                                         C.byref(it)))
+    X = x.cpu().numpy()
+    db = basis.dets_bytes()
+    out = [Wavefunction(H.nf, db, X[:, k]) for k in range(Npsi)]
+    return out, en

@@ -1,0 +1,669 @@
+// Determinant bases on the device: conversion from the reference byte layout, sorting,
+// the lookup hash, and basis growth (targets of an operator, closure, union) through an
+// open-addressing hash with atomicCAS insert.
+//
+// The reference stores a basis as blocked byte arrays with a chained hash
+// (Core/StructDef.cpp:188-206, Core/Hash.cpp:163) and grows it one element at a time under
+// an OpenMP critical section (ComplexWaveFunctionAddElementOMPMiniFlush,
+// Core/ComplexWaveFunctionArithmetic.cpp:453-473).  Here a basis is a sorted array of W-word
+// keys plus an open-addressing table (linear probing, load <= 1/2) mapping key -> row.
+#include <cub/cub.cuh>
+
+#include <algorithm>
+#include <cstring>
+
+#include "qgpu_internal.cuh"
+
+// ------------------------------------------------------------------ small device pieces
+
+__device__ __forceinline__ void qg_cas128(unsigned long long *addr, unsigned long long clo,
+                                          unsigned long long chi, unsigned long long nlo,
+                                          unsigned long long nhi, unsigned long long &olo,
+                                          unsigned long long &ohi) {
+  asm volatile(
+      "{\n\t.reg .b128 c, n, o;\n\t"
+      "mov.b128 c, {%2, %3};\n\t"
+      "mov.b128 n, {%4, %5};\n\t"
+      "atom.global.cas.b128 o, [%6], c, n;\n\t"
+      "mov.b128 {%0, %1}, o;\n\t}"
+      : "=l"(olo), "=l"(ohi)
+      : "l"(clo), "l"(chi), "l"(nlo), "l"(nhi), "l"(addr)
+      : "memory");
+}
+
+// Insert a key into the set; returns 1 if this call inserted it, 0 if it was present,
+// -1 if the probe limit was hit.
+template <int W>
+__device__ __forceinline__ int qg_set_insert(Slot<W> *slots, uint64_t hmask, const Key<W> &k) {
+  uint64_t h = qg_hash<W>(k) & hmask;
+  for (int p = 0; p < QG_PROBE_LIMIT; p++) {
+    unsigned long long *a = reinterpret_cast<unsigned long long *>(slots + h);
+    if (W == 1) {
+      unsigned long long old = atomicCAS(a, QG_EMPTY_WORD, (unsigned long long)k.w[0]);
+      if (old == QG_EMPTY_WORD) return 1;
+      if (old == k.w[0]) return 0;
+    } else {
+      // fast path: a plain read that already shows the key or an occupied slot
+      unsigned long long olo, ohi;
+      qg_cas128(a, QG_EMPTY_WORD, QG_EMPTY_WORD, k.w[0], k.w[1], olo, ohi);
+      if (olo == QG_EMPTY_WORD && ohi == QG_EMPTY_WORD) return 1;
+      if (olo == k.w[0] && ohi == k.w[1]) return 0;
+    }
+    h = (h + 1) & hmask;
+  }
+  return -1;
+}
+
+template <int W>
+__global__ void k_slots_clear(Slot<W> *slots, int64_t n) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  Slot<W> s;
+  for (int j = 0; j < W; j++) s.k[j] = QG_EMPTY_WORD;
+  s.idx = QG_NO_INDEX;
+  for (int j = 0; j < 2 * W - 1; j++) s.pad[j] = 0;
+  slots[i] = s;
+}
+
+// Unique keys -> table rows.  Keys are distinct, so claiming the slot's index word is enough.
+template <int W>
+__global__ void k_hash_build(Slot<W> *slots, uint64_t hmask, const Key<W> *keys, int64_t n, unsigned int *err) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  Key<W> k = keys[i];
+  uint64_t h = qg_hash<W>(k) & hmask;
+  for (int p = 0; p < QG_PROBE_LIMIT; p++) {
+    uint32_t old = atomicCAS(&slots[h].idx, QG_NO_INDEX, (uint32_t)i);
+    if (old == QG_NO_INDEX) {
+      for (int j = 0; j < W; j++) slots[h].k[j] = k.w[j];
+      return;
+    }
+    h = (h + 1) & hmask;
+  }
+  atomicOr(err, QG_DEVERR_PROBE);
+}
+
+// Reference bytes (orbital i in byte i>>3, mask 128>>(i&7)) -> key (orbital i at bit nf-1-i).
+template <int W>
+__global__ void k_bytes_to_keys(const uint8_t *bytes, int nf, int nword, int64_t n, Key<W> *keys) {
+  int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  Key<W> k;
+  for (int j = 0; j < W; j++) k.w[j] = 0;
+  const uint8_t *b = bytes + r * nword;
+  for (int i = 0; i < nf; i++) {
+    if (b[i >> 3] & (128 >> (i & 7))) {
+      int p = nf - 1 - i;
+      k.w[p >> 6] |= 1ull << (p & 63);
+    }
+  }
+  keys[r] = k;
+}
+
+template <int W>
+__global__ void k_keys_to_bytes(const Key<W> *keys, int nf, int nword, int64_t n, uint8_t *bytes) {
+  int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  Key<W> k = keys[r];
+  uint8_t *b = bytes + r * nword;
+  for (int j = 0; j < nword; j++) b[j] = 0;
+  for (int i = 0; i < nf; i++) {
+    int p = nf - 1 - i;
+    if ((k.w[p >> 6] >> (p & 63)) & 1ull) b[i >> 3] |= (uint8_t)(128 >> (i & 7));
+  }
+}
+
+template <int W>
+__global__ void k_extract_word(const Key<W> *keys, const uint32_t *idx, int64_t n, int w, uint64_t *out) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  out[i] = keys[idx ? idx[i] : i].w[w];
+}
+
+__global__ void k_iota(uint32_t *v, int64_t n) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) v[i] = (uint32_t)i;
+}
+
+template <int W>
+__global__ void k_gather_keys(const Key<W> *in, const uint32_t *idx, int64_t n, Key<W> *out, uint32_t *flag) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  Key<W> k = in[idx[i]];
+  out[i] = k;
+  uint32_t f = 1;
+  if (i > 0) f = qg_eq<W>(k, in[idx[i - 1]]) ? 0u : 1u;
+  flag[i] = f;
+}
+
+template <int W>
+__global__ void k_compact_unique(const Key<W> *sorted, const uint32_t *flag, const uint32_t *pos_incl,
+                                 const uint32_t *idx, int64_t n, Key<W> *uniq, int64_t *perm) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uint32_t u = pos_incl[i] - 1;
+  if (flag[i]) uniq[u] = sorted[i];
+  if (perm) perm[idx[i]] = (int64_t)u;
+}
+
+static inline unsigned grid_for(int64_t n, int bs = 256) { return (unsigned)((n + bs - 1) / bs); }
+
+static int64_t hcap_for(int64_t n) {
+  int64_t c = 64;
+  while (c < 2 * n) c <<= 1;
+  return c;
+}
+
+template <int W>
+static qg_status build_hash_t(qg_basis b) {
+  qg_context ctx = b->ctx;
+  int64_t hcap = hcap_for(b->n);
+  if (b->d_slots && b->hcap != hcap) {
+    cudaFree(b->d_slots);
+    b->d_slots = nullptr;
+  }
+  if (!b->d_slots) {
+    cudaError_t e = cudaMalloc(&b->d_slots, hcap * sizeof(Slot<W>));
+    if (e != cudaSuccess) return qg_cuda_fail(ctx, e, "hash table");
+  }
+  b->hcap = hcap;
+  k_slots_clear<W><<<grid_for(hcap), 256, 0, ctx->stream>>>((Slot<W> *)b->d_slots, hcap);
+  ctx->launches++;
+  if (b->n)
+    k_hash_build<W><<<grid_for(b->n), 256, 0, ctx->stream>>>((Slot<W> *)b->d_slots, (uint64_t)(hcap - 1),
+                                                             (const Key<W> *)b->d_keys, b->n, ctx->d_err);
+  ctx->launches++;
+  return qg_check_launch(ctx, "hash build");
+}
+
+qg_status qg_basis_build_hash(qg_basis b) { return b->W == 1 ? build_hash_t<1>(b) : build_hash_t<2>(b); }
+
+// Sort device keys, merge duplicates, build the basis.  d_perm (optional) receives for each
+// input key its row in the basis.
+template <int W>
+static qg_status from_keys_t(qg_context ctx, int nf, void *d_keys_in, int64_t n, qg_basis *out, int64_t *d_perm) {
+  cudaStream_t s = ctx->stream;
+  qg_basis b = new qg_basis_s();
+  b->ctx = ctx;
+  b->nf = nf;
+  b->W = W;
+  if (n > (int64_t)0xFFFFFFF0) {
+    delete b;
+    ctx->last_error = "basis larger than 2^32 determinants";
+    return QG_ERR_ARG;
+  }
+  const Key<W> *keys = (const Key<W> *)d_keys_in;
+  uint32_t *idx = nullptr, *idx2 = nullptr, *flag = nullptr, *pos = nullptr;
+  uint64_t *w = nullptr, *w2 = nullptr;
+  Key<W> *sorted = nullptr;
+  void *tmp = nullptr;
+  size_t tmpb = 0, need = 0;
+  cudaError_t e = cudaSuccess;
+  int64_t nn = std::max<int64_t>(n, 1);
+#define ALLOC(p, bytes) \
+  if (e == cudaSuccess) e = cudaMalloc((void **)&p, bytes)
+  ALLOC(idx, nn * 4);
+  ALLOC(idx2, nn * 4);
+  ALLOC(flag, nn * 4);
+  ALLOC(pos, nn * 4);
+  ALLOC(w, nn * 8);
+  ALLOC(w2, nn * 8);
+  ALLOC(sorted, nn * sizeof(Key<W>));
+  if (e == cudaSuccess) {
+    cub::DeviceRadixSort::SortPairs(nullptr, need, w, w2, idx, idx2, (int)nn, 0, 64, s);
+    tmpb = need;
+    cub::DeviceScan::InclusiveSum(nullptr, need, flag, pos, (int)nn, s);
+    tmpb = std::max(tmpb, need);
+    ALLOC(tmp, tmpb);
+  }
+#undef ALLOC
+  int64_t nuniq = 0;
+  if (e == cudaSuccess && n > 0) {
+    k_iota<<<grid_for(n), 256, 0, s>>>(idx, n);
+    ctx->launches++;
+    // LSD over words: low word first, then (stable) the higher ones
+    for (int wd = 0; wd < W; wd++) {
+      int lo_bit = 64 * wd, hi_bit = std::min(nf, 64 * (wd + 1));
+      if (hi_bit <= lo_bit) continue;
+      k_extract_word<W><<<grid_for(n), 256, 0, s>>>(keys, idx, n, wd, w);
+      ctx->launches++;
+      size_t tb = tmpb;
+      e = cub::DeviceRadixSort::SortPairs(tmp, tb, w, w2, idx, idx2, (int)n, 0, hi_bit - lo_bit, s);
+      ctx->launches += 4;
+      if (e != cudaSuccess) break;
+      std::swap(idx, idx2);
+    }
+    if (e == cudaSuccess) {
+      k_gather_keys<W><<<grid_for(n), 256, 0, s>>>(keys, idx, n, sorted, flag);
+      ctx->launches++;
+      size_t tb = tmpb;
+      e = cub::DeviceScan::InclusiveSum(tmp, tb, flag, pos, (int)n, s);
+      ctx->launches += 2;
+    }
+    if (e == cudaSuccess) {
+      uint32_t last = 0;
+      e = cudaMemcpyAsync(&last, pos + (n - 1), 4, cudaMemcpyDeviceToHost, s);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+      nuniq = last;
+    }
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_keys, std::max<int64_t>(nuniq, 1) * sizeof(Key<W>));
+    if (e == cudaSuccess) {
+      k_compact_unique<W><<<grid_for(n), 256, 0, s>>>(sorted, flag, pos, idx, n, (Key<W> *)b->d_keys, d_perm);
+      ctx->launches++;
+    }
+  } else if (e == cudaSuccess) {
+    e = cudaMalloc(&b->d_keys, sizeof(Key<W>));
+  }
+  cudaStreamSynchronize(s);
+  cudaFree(idx);
+  cudaFree(idx2);
+  cudaFree(flag);
+  cudaFree(pos);
+  cudaFree(w);
+  cudaFree(w2);
+  cudaFree(sorted);
+  cudaFree(tmp);
+  if (e != cudaSuccess) {
+    qg_basis_destroy(b);
+    return qg_cuda_fail(ctx, e, "basis sort");
+  }
+  b->n = nuniq;
+  qg_status st = qg_basis_build_hash(b);
+  if (st != QG_OK) {
+    qg_basis_destroy(b);
+    return st;
+  }
+  *out = b;
+  return QG_OK;
+}
+
+qg_status qg_basis_from_device_keys(qg_context ctx, int nf, int W, void *d_keys, int64_t n, qg_basis *out,
+                                    int64_t *d_perm) {
+  return W == 1 ? from_keys_t<1>(ctx, nf, d_keys, n, out, d_perm) : from_keys_t<2>(ctx, nf, d_keys, n, out, d_perm);
+}
+
+extern "C" qg_status qg_basis_create(qg_context ctx, int32_t nf, int64_t n, const uint8_t *dets_host, qg_basis *basis,
+                                     int64_t *perm_host) {
+  if (!ctx || !basis || nf <= 0 || nf > 127 || n < 0 || (n > 0 && !dets_host)) {
+    if (ctx) ctx->last_error = "qg_basis_create: bad argument (need 0 < nf <= 127)";
+    return QG_ERR_ARG;
+  }
+  int W = qg_words_for(nf), nword = (nf + 7) / 8;
+  cudaStream_t s = ctx->stream;
+  uint8_t *d_bytes = nullptr;
+  void *d_keys = nullptr;
+  int64_t *d_perm = nullptr;
+  int64_t nn = std::max<int64_t>(n, 1);
+  QG_CUDA(ctx, cudaMalloc(&d_bytes, nn * nword));
+  QG_CUDA(ctx, cudaMalloc(&d_keys, nn * 8 * W));
+  if (perm_host) QG_CUDA(ctx, cudaMalloc(&d_perm, nn * 8));
+  if (n) QG_CUDA(ctx, cudaMemcpyAsync(d_bytes, dets_host, n * nword, cudaMemcpyHostToDevice, s));
+  if (n) {
+    if (W == 1)
+      k_bytes_to_keys<1><<<grid_for(n), 256, 0, s>>>(d_bytes, nf, nword, n, (Key<1> *)d_keys);
+    else
+      k_bytes_to_keys<2><<<grid_for(n), 256, 0, s>>>(d_bytes, nf, nword, n, (Key<2> *)d_keys);
+    ctx->launches++;
+  }
+  qg_status st = qg_basis_from_device_keys(ctx, nf, W, d_keys, n, basis, d_perm);
+  if (st == QG_OK && perm_host && n) {
+    cudaError_t e = cudaMemcpyAsync(perm_host, d_perm, n * 8, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) st = qg_cuda_fail(ctx, e, "perm copy");
+  }
+  cudaStreamSynchronize(s);
+  cudaFree(d_bytes);
+  cudaFree(d_keys);
+  cudaFree(d_perm);
+  if (st == QG_OK) st = qg_check_device_error(ctx, "qg_basis_create");
+  return st;
+}
+
+extern "C" qg_status qg_basis_destroy(qg_basis b) {
+  if (!b) return QG_OK;
+  cudaFree(b->d_keys);
+  cudaFree(b->d_slots);
+  delete b;
+  return QG_OK;
+}
+
+extern "C" int64_t qg_basis_size(qg_basis b) { return b ? b->n : -1; }
+
+extern "C" qg_status qg_basis_get_dets(qg_basis b, uint8_t *dets_host) {
+  if (!b || (!dets_host && b->n)) return QG_ERR_ARG;
+  qg_context ctx = b->ctx;
+  int nword = (b->nf + 7) / 8;
+  if (!b->n) return QG_OK;
+  uint8_t *d = nullptr;
+  QG_CUDA(ctx, cudaMalloc(&d, b->n * nword));
+  if (b->W == 1)
+    k_keys_to_bytes<1><<<grid_for(b->n), 256, 0, ctx->stream>>>((const Key<1> *)b->d_keys, b->nf, nword, b->n, d);
+  else
+    k_keys_to_bytes<2><<<grid_for(b->n), 256, 0, ctx->stream>>>((const Key<2> *)b->d_keys, b->nf, nword, b->n, d);
+  ctx->launches++;
+  cudaError_t e = cudaMemcpyAsync(dets_host, d, b->n * nword, cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  cudaFree(d);
+  if (e != cudaSuccess) return qg_cuda_fail(ctx, e, "qg_basis_get_dets");
+  return QG_OK;
+}
+
+template <int W>
+__global__ void k_find(const Slot<W> *slots, uint64_t hmask, const Key<W> *q, int64_t n, int64_t *out,
+                       unsigned int *err) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  out[i] = qg_lookup<W>(slots, hmask, q[i], err);
+}
+
+extern "C" qg_status qg_basis_find(qg_basis b, int64_t n, const uint8_t *dets_host, int64_t *index_host) {
+  if (!b || n < 0 || (n && (!dets_host || !index_host))) return QG_ERR_ARG;
+  if (!n) return QG_OK;
+  qg_context ctx = b->ctx;
+  cudaStream_t s = ctx->stream;
+  int nword = (b->nf + 7) / 8;
+  uint8_t *d_bytes = nullptr;
+  void *d_keys = nullptr;
+  int64_t *d_out = nullptr;
+  QG_CUDA(ctx, cudaMalloc(&d_bytes, n * nword));
+  QG_CUDA(ctx, cudaMalloc(&d_keys, n * 8 * b->W));
+  QG_CUDA(ctx, cudaMalloc(&d_out, n * 8));
+  QG_CUDA(ctx, cudaMemcpyAsync(d_bytes, dets_host, n * nword, cudaMemcpyHostToDevice, s));
+  if (b->W == 1) {
+    k_bytes_to_keys<1><<<grid_for(n), 256, 0, s>>>(d_bytes, b->nf, nword, n, (Key<1> *)d_keys);
+    k_find<1><<<grid_for(n), 256, 0, s>>>((const Slot<1> *)b->d_slots, b->hcap - 1, (const Key<1> *)d_keys, n, d_out,
+                                          ctx->d_err);
+  } else {
+    k_bytes_to_keys<2><<<grid_for(n), 256, 0, s>>>(d_bytes, b->nf, nword, n, (Key<2> *)d_keys);
+    k_find<2><<<grid_for(n), 256, 0, s>>>((const Slot<2> *)b->d_slots, b->hcap - 1, (const Key<2> *)d_keys, n, d_out,
+                                          ctx->d_err);
+  }
+  ctx->launches += 2;
+  cudaError_t e = cudaMemcpyAsync(index_host, d_out, n * 8, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  cudaFree(d_bytes);
+  cudaFree(d_keys);
+  cudaFree(d_out);
+  if (e != cudaSuccess) return qg_cuda_fail(ctx, e, "qg_basis_find");
+  return qg_check_device_error(ctx, "qg_basis_find");
+}
+
+// ------------------------------------------------------------------ growth
+
+// Expand the rows [r0, r1) of a key list through the forward (push) table: each applicable
+// term's target that passes the restrictions is inserted into the set; new keys are appended
+// to the list.  Lane per source determinant; groups are tested per lane.
+template <int W>
+__global__ void k_expand(const Key<W> *src, int64_t r0, int64_t r1, const GroupDev<W> *__restrict__ groups, int ngroups,
+                         const TermDev<W> *__restrict__ terms, int nres, const uint64_t *__restrict__ rmask,
+                         const int32_t *__restrict__ rmin, const int32_t *__restrict__ rmax, Slot<W> *slots,
+                         uint64_t hmask, Key<W> *list, unsigned long long *count, unsigned long long limit,
+                         unsigned int *err) {
+  int64_t r = r0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= r1) return;
+  Key<W> d = src[r];
+  for (int g = 0; g < ngroups; g++) {
+    GroupDev<W> G = groups[g];
+    bool ok = true;
+#pragma unroll
+    for (int i = 0; i < W; i++) ok &= (d.w[i] & G.need1[i]) == G.need1[i];
+    if (!ok) continue;
+    for (int t = G.begin; t < G.end; t++) {
+      const TermDev<W> &T = terms[t];
+      bool app = true, moved = false;
+#pragma unroll
+      for (int i = 0; i < W; i++) {
+        app &= (d.w[i] & T.need0[i]) == 0;
+        moved |= T.flip[i] != 0;
+      }
+      if (!app) continue;
+      Key<W> tg;
+#pragma unroll
+      for (int i = 0; i < W; i++) tg.w[i] = d.w[i] ^ T.flip[i];
+      bool keep = true;
+      for (int q = 0; q < nres && keep; q++) {
+        int c = 0;
+#pragma unroll
+        for (int i = 0; i < W; i++) c += __popcll(tg.w[i] & rmask[q * W + i]);
+        keep = (c >= rmin[q]) && (c <= rmax[q]);
+      }
+      if (!keep) continue;
+      (void)moved;
+      if (*(volatile unsigned long long *)count >= limit) {
+        atomicOr(err, QG_DEVERR_TABLE_FULL);
+        return;
+      }
+      int ins = qg_set_insert<W>(slots, hmask, tg);
+      if (ins < 0) {
+        atomicOr(err, QG_DEVERR_PROBE);
+        return;
+      }
+      if (ins == 1) {
+        unsigned long long pos = atomicAdd(count, 1ull);
+        if (pos < limit) {
+          list[pos] = tg;
+        } else {
+          atomicOr(err, QG_DEVERR_TABLE_FULL);
+        }
+      }
+    }
+  }
+}
+
+template <int W>
+__global__ void k_set_insert_list(Slot<W> *slots, uint64_t hmask, const Key<W> *list, int64_t n, unsigned int *err) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (qg_set_insert<W>(slots, hmask, list[i]) < 0) atomicOr(err, QG_DEVERR_PROBE);
+}
+
+namespace {
+
+struct Restrictions {
+  std::vector<uint64_t> mask;
+  std::vector<int32_t> mn, mx;
+  int n = 0;
+};
+
+// reference byte masks -> device key masks
+bool convert_restrictions(int nf, int W, const qg_restrictions *res, Restrictions &out) {
+  out.n = 0;
+  if (!res || res->n <= 0) return true;
+  if (!res->masks || !res->min || !res->max) return false;
+  int nword = (nf + 7) / 8;
+  out.n = res->n;
+  out.mask.assign((size_t)res->n * W, 0);
+  for (int q = 0; q < res->n; q++) {
+    for (int i = 0; i < nf; i++) {
+      if (res->masks[q * nword + (i >> 3)] & (128 >> (i & 7))) {
+        int p = nf - 1 - i;
+        out.mask[q * W + (p >> 6)] |= 1ull << (p & 63);
+      }
+    }
+    out.mn.push_back(res->min[q]);
+    out.mx.push_back(res->max[q]);
+  }
+  return true;
+}
+
+}  // namespace
+
+// Grow a key set through the push table.  Starts from `seed_keys` (n_seed keys, inserted
+// first when include_seed) and expands for up to max_rounds rounds (-1: until no new key).
+// When include_seed is false only one round is made and the result is the target set.
+template <int W>
+static qg_status grow_t(qg_context ctx, qg_operator op, const Key<W> *seed_keys, int64_t n_seed, bool include_seed,
+                        const qg_restrictions *res, int max_rounds, qg_basis *out, int *rounds_done) {
+  cudaStream_t s = ctx->stream;
+  Restrictions R;
+  if (!convert_restrictions(op->nf, W, res, R)) return QG_ERR_ARG;
+  uint64_t *d_rmask = nullptr;
+  int32_t *d_rmin = nullptr, *d_rmax = nullptr;
+  if (R.n) {
+    QG_CUDA(ctx, cudaMalloc(&d_rmask, R.mask.size() * 8));
+    QG_CUDA(ctx, cudaMalloc(&d_rmin, R.n * 4));
+    QG_CUDA(ctx, cudaMalloc(&d_rmax, R.n * 4));
+    QG_CUDA(ctx, cudaMemcpy(d_rmask, R.mask.data(), R.mask.size() * 8, cudaMemcpyHostToDevice));
+    QG_CUDA(ctx, cudaMemcpy(d_rmin, R.mn.data(), R.n * 4, cudaMemcpyHostToDevice));
+    QG_CUDA(ctx, cudaMemcpy(d_rmax, R.mx.data(), R.n * 4, cudaMemcpyHostToDevice));
+  }
+  // list capacity; the set has 2*cap slots.  An expansion stops inserting once the list is
+  // full, and the threads already past that check can overshoot by at most the number of
+  // resident threads (well under 2^20), so the set stays below 2/3 load.
+  int64_t cap = 1 << 20;
+  while (cap < 4 * (n_seed + 1)) cap <<= 1;
+  Key<W> *list = nullptr;
+  Slot<W> *slots = nullptr;
+  unsigned long long *d_count = nullptr;
+  qg_status st = QG_OK;
+  cudaError_t e = cudaMalloc(&d_count, 8);
+  auto alloc_table = [&](int64_t c) -> cudaError_t {
+    cudaFree(slots);
+    slots = nullptr;
+    cudaError_t ee = cudaMalloc(&slots, 2 * c * sizeof(Slot<W>));
+    if (ee != cudaSuccess) return ee;
+    k_slots_clear<W><<<grid_for(2 * c), 256, 0, s>>>(slots, 2 * c);
+    ctx->launches++;
+    return cudaGetLastError();
+  };
+  if (e == cudaSuccess) e = cudaMalloc(&list, cap * sizeof(Key<W>));
+  if (e == cudaSuccess) e = alloc_table(cap);
+  unsigned long long count = 0;
+  if (e == cudaSuccess && include_seed && n_seed) {
+    // seed keys are unique (a basis): copy them to the list and the set
+    e = cudaMemcpyAsync(list, seed_keys, n_seed * sizeof(Key<W>), cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess) {
+      k_set_insert_list<W><<<grid_for(n_seed), 256, 0, s>>>(slots, (uint64_t)(2 * cap - 1), list, n_seed, ctx->d_err);
+      ctx->launches++;
+    }
+    count = n_seed;
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_count, &count, 8, cudaMemcpyHostToDevice, s);
+  int rounds = 0;
+  int64_t f0 = 0, f1 = include_seed ? count : 0;
+  const Key<W> *front = include_seed ? list : seed_keys;
+  if (!include_seed) {
+    f1 = n_seed;
+    max_rounds = 1;
+  }
+  while (e == cudaSuccess && st == QG_OK && f1 > f0 && (max_rounds < 0 || rounds < max_rounds)) {
+    unsigned int zero = 0;
+    e = cudaMemcpyAsync(ctx->d_err, &zero, 4, cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) break;
+    k_expand<W><<<grid_for(f1 - f0), 256, 0, s>>>(
+        front, f0, f1, (const GroupDev<W> *)op->push.d_groups, op->push.ngroups, (const TermDev<W> *)op->push.d_terms,
+        R.n, d_rmask, d_rmin, d_rmax, slots, (uint64_t)(2 * cap - 1), list, d_count, (unsigned long long)cap,
+        ctx->d_err);
+    ctx->launches++;
+    unsigned int herr = 0;
+    e = cudaMemcpyAsync(&count, d_count, 8, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&herr, ctx->d_err, 4, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) break;
+    if (herr & QG_DEVERR_PROBE) {
+      st = QG_ERR_TIMEOUT;
+      ctx->last_error = "hash probe limit reached during basis growth";
+      break;
+    }
+    if ((herr & QG_DEVERR_TABLE_FULL) || count > (unsigned long long)cap) {
+      // grow: keep the keys that made it into the list, rebuild the set, redo the round
+      int64_t kept = std::min<int64_t>((int64_t)count, cap);
+      int64_t ncap = cap;
+      while (ncap < 2 * (int64_t)count + 1024) ncap <<= 1;
+      Key<W> *nlist = nullptr;
+      e = cudaMalloc(&nlist, ncap * sizeof(Key<W>));
+      if (e != cudaSuccess) break;
+      e = cudaMemcpyAsync(nlist, list, kept * sizeof(Key<W>), cudaMemcpyDeviceToDevice, s);
+      if (e != cudaSuccess) break;
+      cudaStreamSynchronize(s);
+      cudaFree(list);
+      list = nlist;
+      if (include_seed) front = list;
+      cap = ncap;
+      e = alloc_table(cap);
+      if (e != cudaSuccess) break;
+      k_set_insert_list<W><<<grid_for(kept), 256, 0, s>>>(slots, (uint64_t)(2 * cap - 1), list, kept, ctx->d_err);
+      ctx->launches++;
+      count = kept;
+      e = cudaMemcpyAsync(d_count, &count, 8, cudaMemcpyHostToDevice, s);
+      continue;  // same frontier again
+    }
+    rounds++;
+    if (include_seed) {
+      f0 = f1;
+      f1 = (int64_t)count;
+    } else {
+      break;
+    }
+  }
+  if (e != cudaSuccess && st == QG_OK) st = qg_cuda_fail(ctx, e, "basis growth");
+  if (st == QG_OK) st = qg_basis_from_device_keys(ctx, op->nf, W, list, (int64_t)count, out, nullptr);
+  cudaStreamSynchronize(s);
+  cudaFree(list);
+  cudaFree(slots);
+  cudaFree(d_count);
+  cudaFree(d_rmask);
+  cudaFree(d_rmin);
+  cudaFree(d_rmax);
+  if (rounds_done) *rounds_done = rounds;
+  return st;
+}
+
+extern "C" qg_status qg_operator_psi_basis(qg_context ctx, qg_operator op, qg_basis in, const qg_restrictions *res,
+                                           qg_basis *out) {
+  if (!ctx || !op || !in || !out || op->nf != in->nf) return QG_ERR_ARG;
+  if (op->W == 1) return grow_t<1>(ctx, op, (const Key<1> *)in->d_keys, in->n, false, res, 1, out, nullptr);
+  return grow_t<2>(ctx, op, (const Key<2> *)in->d_keys, in->n, false, res, 1, out, nullptr);
+}
+
+extern "C" qg_status qg_basis_closure(qg_context ctx, qg_operator op, qg_basis seed, const qg_restrictions *res,
+                                      int32_t max_rounds, qg_basis *closed, int32_t *rounds_done) {
+  if (!ctx || !op || !seed || !closed || op->nf != seed->nf) return QG_ERR_ARG;
+  int r = 0;
+  qg_status st;
+  if (op->W == 1)
+    st = grow_t<1>(ctx, op, (const Key<1> *)seed->d_keys, seed->n, true, res, max_rounds, closed, &r);
+  else
+    st = grow_t<2>(ctx, op, (const Key<2> *)seed->d_keys, seed->n, true, res, max_rounds, closed, &r);
+  if (rounds_done) *rounds_done = r;
+  return st;
+}
+
+extern "C" qg_status qg_basis_union(qg_context ctx, qg_basis a, qg_basis b, qg_basis *out) {
+  if (!ctx || !a || !b || !out || a->nf != b->nf) return QG_ERR_ARG;
+  int W = a->W;
+  void *d = nullptr;
+  int64_t n = a->n + b->n;
+  QG_CUDA(ctx, cudaMalloc(&d, std::max<int64_t>(n, 1) * 8 * W));
+  QG_CUDA(ctx, cudaMemcpyAsync(d, a->d_keys, a->n * 8 * W, cudaMemcpyDeviceToDevice, ctx->stream));
+  QG_CUDA(ctx, cudaMemcpyAsync((char *)d + a->n * 8 * W, b->d_keys, b->n * 8 * W, cudaMemcpyDeviceToDevice, ctx->stream));
+  qg_status st = qg_basis_from_device_keys(ctx, a->nf, W, d, n, out, nullptr);
+  cudaStreamSynchronize(ctx->stream);
+  cudaFree(d);
+  return st;
+}
+
+template <int W>
+__global__ void k_map(const Key<W> *dst_keys, int64_t n, const Slot<W> *src_slots, uint64_t hmask, const double2 *x,
+                      double2 *y, int nvec, unsigned int *err) {
+  int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  int64_t j = qg_lookup<W>(src_slots, hmask, dst_keys[r], err);
+  for (int k = 0; k < nvec; k++) y[r * nvec + k] = (j >= 0) ? x[j * nvec + k] : make_double2(0.0, 0.0);
+}
+
+extern "C" qg_status qg_basis_map(qg_context ctx, qg_basis src, const double *x_dev, qg_basis dst, double *y_dev,
+                                  int32_t nvec) {
+  if (!ctx || !src || !dst || src->nf != dst->nf || nvec <= 0) return QG_ERR_ARG;
+  if (!dst->n) return QG_OK;
+  if (src->W == 1)
+    k_map<1><<<grid_for(dst->n), 256, 0, ctx->stream>>>((const Key<1> *)dst->d_keys, dst->n, (const Slot<1> *)src->d_slots,
+                                                        src->hcap - 1, (const double2 *)x_dev, (double2 *)y_dev, nvec,
+                                                        ctx->d_err);
+  else
+    k_map<2><<<grid_for(dst->n), 256, 0, ctx->stream>>>((const Key<2> *)dst->d_keys, dst->n, (const Slot<2> *)src->d_slots,
+                                                        src->hcap - 1, (const double2 *)x_dev, (double2 *)y_dev, nvec,
+                                                        ctx->d_err);
+  ctx->launches++;
+  return qg_check_launch(ctx, "qg_basis_map");
+}

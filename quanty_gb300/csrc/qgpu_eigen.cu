@@ -1,0 +1,385 @@
+// Lowest eigenpairs of a Hermitian operator on a fixed basis: restarted block Lanczos with
+// full (twice repeated) reorthogonalisation and Rayleigh-Ritz restarts.
+//
+// The reference's solver (BlockLanczosGroundStateConserveBasisKrylovComplex,
+// Core/BlockLanczos.cpp:5350-5606) grows a block Krylov space with fixed-basis H*psi
+// (:5489-5496), reorthogonalises twice against all Krylov vectors (:5498-5527), diagonalises
+// the projected matrix with zheevd (:5530) and restarts from the Ritz vectors (:5554-5573)
+// until the variance <H^2> - <H>^2 of every vector is below "Zero".  The same structure here:
+// H*psi is the pull kernel, the Gram products and updates run as memory-bound kernels over
+// the n x K Krylov block (row-major, K columns), and the projected matrix (K <= a few
+// hundred) is diagonalised on the host by cyclic Jacobi rotations.
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <vector>
+
+#include "qgpu_internal.cuh"
+
+typedef std::complex<double> cd;
+
+// C[i][j] partial = sum_rows conj(A[r][a0+i]) * B[r][b0+j]; thread per (i, j), gridDim.y row chunks
+__global__ void k_gram_partial(const double2 *__restrict__ A, int lda, int a0, int ka, const double2 *__restrict__ B,
+                               int ldb, int b0, int kb, int64_t n, int64_t chunk, double2 *part) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= ka * kb) return;
+  int i = q % ka, j = q / ka;
+  int64_t r0 = blockIdx.y * chunk, r1 = r0 + chunk;
+  if (r1 > n) r1 = n;
+  double sr = 0, si = 0;
+  for (int64_t r = r0; r < r1; r++) {
+    double2 a = A[r * lda + a0 + i], b = B[r * ldb + b0 + j];
+    sr += a.x * b.x + a.y * b.y;
+    si += a.x * b.y - a.y * b.x;
+  }
+  part[(int64_t)blockIdx.y * ka * kb + q] = make_double2(sr, si);
+}
+
+__global__ void k_gram_reduce(const double2 *part, int nchunk, int m, double2 *out) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= m) return;
+  double sr = 0, si = 0;
+  for (int c = 0; c < nchunk; c++) {
+    sr += part[(int64_t)c * m + q].x;
+    si += part[(int64_t)c * m + q].y;
+  }
+  out[q] = make_double2(sr, si);
+}
+
+// B[r][b0+j] -= sum_i A[r][a0+i] C[i*kb + j]
+__global__ void k_sub_mul(const double2 *__restrict__ A, int lda, int a0, int ka, const double2 *__restrict__ C,
+                          double2 *B, int ldb, int b0, int kb, int64_t n) {
+  int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= n * kb) return;
+  int64_t r = t / kb;
+  int j = (int)(t % kb);
+  double2 acc = B[r * ldb + b0 + j];
+  for (int i = 0; i < ka; i++) {
+    double2 a = A[r * lda + a0 + i], c = C[i * kb + j];
+    acc.x -= a.x * c.x - a.y * c.y;
+    acc.y -= a.x * c.y + a.y * c.x;
+  }
+  B[r * ldb + b0 + j] = acc;
+}
+
+// X[r][j] = sum_i A[r][i] Y[i*kb + j]
+__global__ void k_combine(const double2 *__restrict__ A, int lda, int ka, const double2 *__restrict__ Y, double2 *X,
+                          int ldx, int kb, int64_t n) {
+  int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= n * kb) return;
+  int64_t r = t / kb;
+  int j = (int)(t % kb);
+  double2 acc = make_double2(0, 0);
+  for (int i = 0; i < ka; i++) {
+    double2 a = A[r * lda + i], y = Y[i * kb + j];
+    acc.x += a.x * y.x - a.y * y.y;
+    acc.y += a.x * y.y + a.y * y.x;
+  }
+  X[r * ldx + j] = acc;
+}
+
+__global__ void k_scale_col(double2 *B, int ldb, int col, int64_t n, double s) {
+  int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  double2 v = B[r * ldb + col];
+  B[r * ldb + col] = make_double2(v.x * s, v.y * s);
+}
+
+__global__ void k_copy_cols(const double2 *src, int lds, int s0, double2 *dst, int ldd, int d0, int k, int64_t n) {
+  int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= n * k) return;
+  int64_t r = t / k;
+  int j = (int)(t % k);
+  dst[r * ldd + d0 + j] = src[r * lds + s0 + j];
+}
+
+namespace {
+
+struct Gram {
+  qg_context ctx;
+  int64_t n;
+  double2 *part = nullptr, *out = nullptr;
+  int64_t cap = 0;
+  int nchunk = 1;
+  int64_t chunk = 1;
+  qg_status init(qg_context c, int64_t nn, int maxm) {
+    ctx = c;
+    n = nn;
+    chunk = std::max<int64_t>(4096, (nn + 1023) / 1024);
+    nchunk = (int)((nn + chunk - 1) / chunk);
+    if (nchunk < 1) nchunk = 1;
+    cap = maxm;
+    QG_CUDA(ctx, cudaMalloc(&part, (size_t)nchunk * maxm * 16));
+    QG_CUDA(ctx, cudaMalloc(&out, (size_t)maxm * 16));
+    return QG_OK;
+  }
+  void release() {
+    cudaFree(part);
+    cudaFree(out);
+  }
+  // out (device) and host = A[:, a0:a0+ka]^dag B[:, b0:b0+kb]
+  qg_status run(const double2 *A, int lda, int a0, int ka, const double2 *B, int ldb, int b0, int kb,
+                std::vector<cd> *host) {
+    int m = ka * kb;
+    if (m > cap || m <= 0) return QG_ERR_ARG;
+    dim3 g((m + 127) / 128, nchunk);
+    k_gram_partial<<<g, 128, 0, ctx->stream>>>(A, lda, a0, ka, B, ldb, b0, kb, n, chunk, part);
+    k_gram_reduce<<<(m + 127) / 128, 128, 0, ctx->stream>>>(part, nchunk, m, out);
+    ctx->launches += 2;
+    if (host) {
+      host->resize(m);
+      QG_CUDA(ctx, cudaMemcpyAsync(host->data(), out, m * 16, cudaMemcpyDeviceToHost, ctx->stream));
+      QG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    }
+    return qg_check_launch(ctx, "gram");
+  }
+};
+
+// Cyclic Jacobi for a Hermitian matrix (row-major, k x k).  On return w ascending and the
+// columns of V the eigenvectors.
+void jacobi_eigh(int k, std::vector<cd> A, std::vector<double> &w, std::vector<cd> &V) {
+  V.assign((size_t)k * k, cd(0, 0));
+  for (int i = 0; i < k; i++) V[(size_t)i * k + i] = 1.0;
+  auto at = [&](int i, int j) -> cd & { return A[(size_t)i * k + j]; };
+  double norm = 0;
+  for (auto &z : A) norm += std::norm(z);
+  norm = std::sqrt(norm);
+  for (int sweep = 0; sweep < 100; sweep++) {
+    double off = 0;
+    for (int i = 0; i < k; i++)
+      for (int j = i + 1; j < k; j++) off += std::norm(at(i, j));
+    if (std::sqrt(off) <= 1e-15 * (norm > 0 ? norm : 1.0)) break;
+    for (int p = 0; p < k; p++) {
+      for (int q = p + 1; q < k; q++) {
+        cd c = at(p, q);
+        double ac = std::abs(c);
+        if (ac == 0.0) continue;
+        double a = at(p, p).real(), b = at(q, q).real();
+        double th = 0.5 * std::atan2(2 * ac, a - b);
+        double C = std::cos(th), S = std::sin(th);
+        cd ph = c / ac;       // e^{i phi}
+        cd phc = std::conj(ph);
+        // U = D R with D = diag(1, e^{-i phi}), R = [[C, -S], [S, C]]
+        // columns: A <- A U
+        for (int r = 0; r < k; r++) {
+          cd xp = at(r, p), xq = at(r, q) * phc;
+          at(r, p) = xp * C + xq * S;
+          at(r, q) = -xp * S + xq * C;
+          cd vp = V[(size_t)r * k + p], vq = V[(size_t)r * k + q] * phc;
+          V[(size_t)r * k + p] = vp * C + vq * S;
+          V[(size_t)r * k + q] = -vp * S + vq * C;
+        }
+        // rows: A <- U^dag A
+        for (int cc = 0; cc < k; cc++) {
+          cd xp = at(p, cc), xq = at(q, cc) * ph;
+          at(p, cc) = xp * C + xq * S;
+          at(q, cc) = -xp * S + xq * C;
+        }
+        at(p, q) = 0;
+        at(q, p) = 0;
+        at(p, p) = at(p, p).real();
+        at(q, q) = at(q, q).real();
+      }
+    }
+  }
+  // sort ascending
+  std::vector<int> idx(k);
+  for (int i = 0; i < k; i++) idx[i] = i;
+  std::sort(idx.begin(), idx.end(), [&](int x, int y) { return at(x, x).real() < at(y, y).real(); });
+  std::vector<cd> V2((size_t)k * k);
+  w.resize(k);
+  for (int j = 0; j < k; j++) {
+    w[j] = at(idx[j], idx[j]).real();
+    for (int r = 0; r < k; r++) V2[(size_t)r * k + j] = V[(size_t)r * k + idx[j]];
+  }
+  V.swap(V2);
+}
+
+}  // namespace
+
+extern "C" qg_status qg_block_groundstate(qg_context ctx, qg_operator op, qg_basis b, int32_t p, double *x_dev,
+                                          double *energies_host, double tol, int32_t max_krylov,
+                                          int32_t max_restarts, int32_t *iterations) {
+  if (!ctx || !op || !b || !x_dev || !energies_host || p <= 0 || op->nf != b->nf) return QG_ERR_ARG;
+  int64_t n = b->n;
+  if (n < p) {
+    ctx->last_error = "qg_block_groundstate: basis smaller than the number of states";
+    return QG_ERR_ARG;
+  }
+  int K = max_krylov > 0 ? max_krylov : 128;
+  if (K < 2 * p) K = 2 * p;
+  if (K > n) K = (int)n;
+  K = (K / p) * p;
+  if (K < p) K = p;
+  cudaStream_t s = ctx->stream;
+  double2 *V = nullptr, *W = nullptr, *Cd = nullptr;
+  size_t vb = (size_t)n * K * 16, wb = (size_t)n * p * 16;
+  cudaError_t e = cudaMalloc(&V, vb);
+  if (e == cudaSuccess) e = cudaMalloc(&W, wb);
+  if (e == cudaSuccess) e = cudaMalloc(&Cd, (size_t)K * std::max(K, p) * 16);
+  if (e != cudaSuccess) {
+    cudaFree(V);
+    cudaFree(W);
+    cudaFree(Cd);
+    ctx->last_error = "qg_block_groundstate: out of device memory";
+    return QG_ERR_OOM;
+  }
+  Gram G;
+  qg_status st = G.init(ctx, n, K * std::max(K, p));
+  double2 *X = (double2 *)x_dev;
+  auto grid = [](int64_t t) { return (unsigned)((t + 255) / 256); };
+  std::vector<double> theta(p, 0.0);
+  int it = 0;
+  bool converged = false;
+  std::vector<cd> c, T;
+  for (int restart = 0; restart <= max_restarts && st == QG_OK && !converged; restart++) {
+    // V[:, 0:p] = X, orthonormalised (modified Gram-Schmidt, twice)
+    k_copy_cols<<<grid(n * p), 256, 0, s>>>(X, p, 0, V, K, 0, p, n);
+    ctx->launches++;
+    int k = 0;  // orthonormal columns in V
+    T.assign((size_t)K * K, cd(0, 0));
+    auto orth_block = [&](int c0, int cnt, std::vector<cd> *coef) -> int {
+      // orthonormalise V[:, c0:c0+cnt] against V[:, 0:c0] and among themselves; returns how
+      // many columns survived (kept contiguous from c0); coef (cnt x cnt upper) gets R.
+      int kept = 0;
+      for (int j = 0; j < cnt && st == QG_OK; j++) {
+        int col = c0 + kept;
+        if (col != c0 + j) {
+          k_copy_cols<<<grid(n), 256, 0, s>>>(V, K, c0 + j, V, K, col, 1, n);
+          ctx->launches++;
+        }
+        double nrm0 = 0;
+        {
+          std::vector<cd> h;
+          st = G.run(V, K, col, 1, V, K, col, 1, &h);
+          nrm0 = std::sqrt(std::max(0.0, h[0].real()));
+        }
+        for (int pass = 0; pass < 2 && st == QG_OK && col > 0; pass++) {
+          std::vector<cd> h;
+          st = G.run(V, K, 0, col, V, K, col, 1, &h);
+          if (st != QG_OK) break;
+          k_sub_mul<<<grid(n), 256, 0, s>>>(V, K, 0, col, G.out, V, K, col, 1, n);
+          ctx->launches++;
+          if (coef && pass == 0) {
+            for (int i = 0; i < col; i++) (*coef)[(size_t)i * cnt + j] += h[i];
+          } else if (coef) {
+            for (int i = 0; i < col; i++) (*coef)[(size_t)i * cnt + j] += h[i];
+          }
+        }
+        std::vector<cd> h;
+        if (st == QG_OK) st = G.run(V, K, col, 1, V, K, col, 1, &h);
+        if (st != QG_OK) break;
+        double nrm = std::sqrt(std::max(0.0, h[0].real()));
+        if (nrm <= 1e-10 * std::max(nrm0, 1e-300) || nrm == 0.0) continue;  // deflate
+        k_scale_col<<<grid(n), 256, 0, s>>>(V, K, col, n, 1.0 / nrm);
+        ctx->launches++;
+        if (coef) (*coef)[(size_t)col * cnt + j] = nrm;
+        kept++;
+      }
+      return kept;
+    };
+    k = orth_block(0, p, nullptr);
+    if (st != QG_OK) break;
+    if (k == 0) {
+      ctx->last_error = "qg_block_groundstate: start vectors are zero";
+      st = QG_ERR_ARG;
+      break;
+    }
+    int j0 = 0, bs = k;
+    bool invariant = false;
+    while (st == QG_OK) {
+      // W = H V[:, j0:j0+bs]
+      st = qg_apply_strided(ctx, op, b, b, (const double *)(V + j0), K, (double *)W, p, bs, nullptr);
+      it++;
+      if (st != QG_OK) break;
+      // T[0:k, j0:j0+bs] = V^dag W (twice, the second pass corrects), W -= V C
+      for (int pass = 0; pass < 2 && st == QG_OK; pass++) {
+        st = G.run(V, K, 0, k, W, p, 0, bs, &c);
+        if (st != QG_OK) break;
+        for (int i = 0; i < k; i++)
+          for (int j = 0; j < bs; j++) T[(size_t)i * K + j0 + j] += c[(size_t)i * bs + j];
+        k_sub_mul<<<grid(n * bs), 256, 0, s>>>(V, K, 0, k, G.out, W, p, 0, bs, n);
+        ctx->launches++;
+      }
+      if (st != QG_OK || k + bs > K) break;
+      // append W as new columns and orthonormalise them
+      k_copy_cols<<<grid(n * bs), 256, 0, s>>>(W, p, 0, V, K, k, bs, n);
+      ctx->launches++;
+      std::vector<cd> R((size_t)(k + bs) * bs, cd(0, 0));
+      int kept = orth_block(k, bs, &R);
+      if (st != QG_OK) break;
+      // H V_j has components R on the new columns (and small corrections on old ones)
+      for (int i = 0; i < kept; i++)
+        for (int j = 0; j < bs; j++) T[(size_t)(k + i) * K + j0 + j] += R[(size_t)(k + i) * bs + j];
+      for (int i = 0; i < k; i++)
+        for (int j = 0; j < bs; j++) T[(size_t)i * K + j0 + j] += R[(size_t)i * bs + j];
+      if (kept == 0) {
+        invariant = true;
+        break;
+      }
+      j0 = k;
+      k += kept;
+      bs = kept;
+      if (k + bs > K) {
+        // last block: its projections are needed for the Rayleigh quotient
+        st = qg_apply_strided(ctx, op, b, b, (const double *)(V + j0), K, (double *)W, p, bs, nullptr);
+        it++;
+        if (st == QG_OK) st = G.run(V, K, 0, k, W, p, 0, bs, &c);
+        if (st == QG_OK)
+          for (int i = 0; i < k; i++)
+            for (int j = 0; j < bs; j++) T[(size_t)i * K + j0 + j] = c[(size_t)i * bs + j];
+        break;
+      }
+    }
+    if (st != QG_OK) break;
+    (void)invariant;
+    // projected matrix: Hermitian part of the k x k leading block
+    std::vector<cd> M((size_t)k * k);
+    for (int i = 0; i < k; i++)
+      for (int j = 0; j < k; j++) {
+        cd a = T[(size_t)i * K + j], bb = std::conj(T[(size_t)j * K + i]);
+        // entries above the computed block columns are only known through symmetry
+        M[(size_t)i * k + j] = (a == cd(0, 0)) ? bb : ((bb == cd(0, 0)) ? a : 0.5 * (a + bb));
+      }
+    std::vector<double> w;
+    std::vector<cd> Y;
+    jacobi_eigh(k, M, w, Y);
+    std::vector<cd> Yp((size_t)k * p);
+    for (int i = 0; i < k; i++)
+      for (int j = 0; j < p; j++) Yp[(size_t)i * p + j] = Y[(size_t)i * k + j];
+    e = cudaMemcpyAsync(Cd, Yp.data(), Yp.size() * 16, cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) {
+      st = qg_cuda_fail(ctx, e, "ritz upload");
+      break;
+    }
+    k_combine<<<grid(n * p), 256, 0, s>>>(V, K, k, Cd, X, p, p, n);
+    ctx->launches++;
+    for (int j = 0; j < p; j++) theta[j] = w[j];
+    // convergence: variance |H x|^2 - theta^2 per vector
+    st = qg_apply_strided(ctx, op, b, b, (const double *)X, p, (double *)W, p, p, nullptr);
+    it++;
+    if (st != QG_OK) break;
+    std::vector<cd> hh;
+    double worst = 0;
+    for (int j = 0; j < p && st == QG_OK; j++) {
+      st = G.run(W, p, j, 1, W, p, j, 1, &hh);
+      if (st != QG_OK) break;
+      double var = hh[0].real() - theta[j] * theta[j];
+      worst = std::max(worst, std::fabs(var));
+    }
+    if (worst < tol) converged = true;
+  }
+  G.release();
+  cudaStreamSynchronize(s);
+  cudaFree(V);
+  cudaFree(W);
+  cudaFree(Cd);
+  for (int j = 0; j < p; j++) energies_host[j] = theta[j];
+  if (iterations) *iterations = it;
+  if (st == QG_OK) st = qg_check_device_error(ctx, "qg_block_groundstate");
+  if (st == QG_OK && !converged) {
+    ctx->last_error = "qg_block_groundstate: not converged within the restart limit";
+    return QG_ERR_TIMEOUT;
+  }
+  return st;
+}

@@ -1,0 +1,404 @@
+// Vector algebra, the Lanczos tridiagonalisation driver and the all-frequency continued
+// fraction.
+//
+// Lanczos follows the reference's three-term recursion without reorthogonalisation and its
+// truncation schedule (LanczosTriDiagonalizeCC, Core/Lanczos.cpp:2169-2263):
+//   b0 = |v0|, v0 /= b0, drop |v0_r| <= eps;  w = H v0;  a1 = <v0|w>
+//   i = 1..ntri-1:  v_i = w - a_i v_{i-1};  b_i = |v_i|;  v_i /= b_i;  drop |v_i,r| <= eps/err;
+//                   err *= b_i^2/(b_i^2 + 4 gamma^2);  w = H v_i;  a_{i+1} = <v_i|w>;
+//                   w -= b_i v_{i-1}
+// On a basis that is closed under H, "drop" is zeroing and the growing-basis bookkeeping of
+// the reference (union axpy, rehash) has no numerical effect.  Per step two kernels run: an
+// axpy with the norm partials, and the fused H*psi whose gather applies the 1/b_i scale and
+// the truncation on the fly, writes the stored Krylov vector, forms <v_i|H v_i> partials and
+// the three-term update in its epilogue.  Two single-block kernels finish the reductions so
+// the scalars stay on the device; the host reads a and b once at the end.
+#include <cmath>
+#include <vector>
+
+#include "qgpu_internal.cuh"
+
+static const int RBLK = 256;
+
+static inline int partial_blocks(qg_context ctx, int64_t n) {
+  int64_t b = (n + RBLK - 1) / RBLK;
+  int64_t cap = 4LL * ctx->num_sms;
+  if (b > cap) b = cap;
+  if (b < 1) b = 1;
+  return (int)b;
+}
+
+// per-vector partial sums of conj(x) y (or |x|^2 when y == nullptr) over rows
+__global__ void k_dot_partial(int64_t n, int nvec, const double2 *__restrict__ x, const double2 *__restrict__ y,
+                              double2 *part) {
+  extern __shared__ double2 sh[];
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int k = 0; k < nvec; k++) {
+    double2 s = make_double2(0.0, 0.0);
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+      double2 a = x[r * nvec + k];
+      if (y) {
+        double2 b = y[r * nvec + k];
+        s.x += a.x * b.x + a.y * b.y;
+        s.y += a.x * b.y - a.y * b.x;
+      } else {
+        s.x += a.x * a.x + a.y * a.y;
+      }
+    }
+    for (int o = 16; o; o >>= 1) {
+      s.x += __shfl_xor_sync(0xffffffffu, s.x, o);
+      s.y += __shfl_xor_sync(0xffffffffu, s.y, o);
+    }
+    if (lane == 0) sh[wid] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double2 t = make_double2(0.0, 0.0);
+      for (int w = 0; w < nw; w++) {
+        t.x += sh[w].x;
+        t.y += sh[w].y;
+      }
+      part[blockIdx.x * nvec + k] = t;
+    }
+    __syncthreads();
+  }
+}
+
+// sum nblk partials per vector (single block); out[k] = sum
+__global__ void k_reduce_partials(const double2 *part, int nblk, int nvec, double2 *out) {
+  __shared__ double2 sh[32];
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int k = 0; k < nvec; k++) {
+    double2 s = make_double2(0.0, 0.0);
+    for (int b = threadIdx.x; b < nblk; b += blockDim.x) {
+      s.x += part[b * nvec + k].x;
+      s.y += part[b * nvec + k].y;
+    }
+    for (int o = 16; o; o >>= 1) {
+      s.x += __shfl_xor_sync(0xffffffffu, s.x, o);
+      s.y += __shfl_xor_sync(0xffffffffu, s.y, o);
+    }
+    if (lane == 0) sh[wid] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double2 t = make_double2(0.0, 0.0);
+      for (int w = 0; w < nw; w++) {
+        t.x += sh[w].x;
+        t.y += sh[w].y;
+      }
+      out[k] = t;
+    }
+    __syncthreads();
+  }
+}
+
+qg_status qg_dot_dev(qg_context ctx, int64_t n, int nvec, const double *x, const double *y, double *out_dev) {
+  int P = partial_blocks(ctx, n);
+  QG_TRY(qg_ensure_scratch(ctx, (size_t)P * nvec * 16));
+  k_dot_partial<<<P, RBLK, (RBLK / 32) * sizeof(double2), ctx->stream>>>(n, nvec, (const double2 *)x,
+                                                                        (const double2 *)y, (double2 *)ctx->d_scratch);
+  k_reduce_partials<<<1, 256, 0, ctx->stream>>>((const double2 *)ctx->d_scratch, P, nvec, (double2 *)out_dev);
+  ctx->launches += 2;
+  return qg_check_launch(ctx, "dot");
+}
+
+static qg_status dot_to_host(qg_context ctx, int64_t n, int nvec, const double *x, const double *y, double *host) {
+  double2 *d = nullptr;
+  QG_CUDA(ctx, cudaMalloc(&d, nvec * 16));
+  qg_status st = qg_dot_dev(ctx, n, nvec, x, y, (double *)d);
+  cudaError_t e = cudaSuccess;
+  if (st == QG_OK) e = cudaMemcpyAsync(host, d, nvec * 16, cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  cudaFree(d);
+  if (st != QG_OK) return st;
+  if (e != cudaSuccess) return qg_cuda_fail(ctx, e, "dot copy");
+  return QG_OK;
+}
+
+extern "C" qg_status qg_dot(qg_context ctx, int64_t n, int32_t nvec, const double *x, const double *y, double *dot_host) {
+  if (!ctx || n < 0 || nvec <= 0 || !dot_host || (n && (!x || !y))) return QG_ERR_ARG;
+  return dot_to_host(ctx, n, nvec, x, y, dot_host);
+}
+
+extern "C" qg_status qg_norm(qg_context ctx, int64_t n, int32_t nvec, const double *x, double *norm_host) {
+  if (!ctx || n < 0 || nvec <= 0 || !norm_host || (n && !x)) return QG_ERR_ARG;
+  std::vector<double> t(2 * nvec);
+  QG_TRY(dot_to_host(ctx, n, nvec, x, nullptr, t.data()));
+  for (int k = 0; k < nvec; k++) norm_host[k] = std::sqrt(t[2 * k]);
+  return QG_OK;
+}
+
+__global__ void k_axpy(int64_t n, int nvec, const double2 *__restrict__ alpha, const double2 *__restrict__ x,
+                       double2 *__restrict__ y) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n * nvec) return;
+  int k = (int)(i % nvec);
+  double2 a = alpha[k], xv = x[i], yv = y[i];
+  yv.x += a.x * xv.x - a.y * xv.y;
+  yv.y += a.x * xv.y + a.y * xv.x;
+  y[i] = yv;
+}
+
+extern "C" qg_status qg_axpy(qg_context ctx, int64_t n, int32_t nvec, const double *alpha_host, const double *x,
+                             double *y) {
+  if (!ctx || n < 0 || nvec <= 0 || !alpha_host || (n && (!x || !y))) return QG_ERR_ARG;
+  if (!n) return QG_OK;
+  double2 *d = nullptr;
+  QG_CUDA(ctx, cudaMalloc(&d, nvec * 16));
+  QG_CUDA(ctx, cudaMemcpyAsync(d, alpha_host, nvec * 16, cudaMemcpyHostToDevice, ctx->stream));
+  int64_t tot = n * nvec;
+  k_axpy<<<(unsigned)((tot + 255) / 256), 256, 0, ctx->stream>>>(n, nvec, d, (const double2 *)x, (double2 *)y);
+  ctx->launches++;
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  cudaFree(d);
+  if (e != cudaSuccess) return qg_cuda_fail(ctx, e, "qg_axpy");
+  return qg_check_launch(ctx, "qg_axpy");
+}
+
+extern "C" qg_status qg_expectation(qg_context ctx, qg_operator op, qg_basis b, const double *x, int32_t nvec,
+                                    double *val_host) {
+  if (!ctx || !op || !b || nvec <= 0 || !val_host || op->nf != b->nf) return QG_ERR_ARG;
+  if (!b->n) {
+    for (int k = 0; k < 2 * nvec; k++) val_host[k] = 0;
+    return QG_OK;
+  }
+  double *y = nullptr;
+  QG_CUDA(ctx, cudaMalloc(&y, b->n * nvec * 16));
+  qg_status st = qg_apply_launch(ctx, op, b, b, x, y, nvec, nullptr);
+  if (st == QG_OK) st = dot_to_host(ctx, b->n, nvec, x, y, val_host);
+  cudaFree(y);
+  return st;
+}
+
+// ------------------------------------------------------------------ Lanczos
+
+// v = w - a_k v_prev (a from the previous dot), norm partials of v
+__global__ void k_lanczos_axpy_norm(int64_t n, int nvec, const double2 *__restrict__ w, const double2 *__restrict__ vp,
+                                    const double *__restrict__ a, double2 *__restrict__ v, double2 *part) {
+  extern __shared__ double2 sh[];
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int k = 0; k < nvec; k++) {
+    double ak = a[k];
+    double s = 0.0;
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+      double2 wv = w[r * nvec + k], pv = vp[r * nvec + k];
+      double2 o = make_double2(wv.x - ak * pv.x, wv.y - ak * pv.y);
+      v[r * nvec + k] = o;
+      s += o.x * o.x + o.y * o.y;
+    }
+    for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) sh[wid].x = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0;
+      for (int w2 = 0; w2 < nw; w2++) t += sh[w2].x;
+      part[blockIdx.x * nvec + k] = make_double2(t, 0.0);
+    }
+    __syncthreads();
+  }
+}
+
+// a[k] <- Re(sum of dot partials); also stores a into the history
+__global__ void k_fin_a(const double2 *part, int nblk, int nvec, double *a_now, double *a_hist, int stride, int col) {
+  __shared__ double sh[32];
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int k = 0; k < nvec; k++) {
+    double s = 0;
+    for (int b = threadIdx.x; b < nblk; b += blockDim.x) s += part[b * nvec + k].x;
+    for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) sh[wid] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0;
+      for (int w = 0; w < nw; w++) t += sh[w];
+      a_now[k] = t;
+      a_hist[k * stride + col] = t;
+    }
+    __syncthreads();
+  }
+}
+
+// b = sqrt(sum of norm partials); scale = 1/b (0 for an empty vector); truncation threshold
+// (eps/err)^2 with the err before this step's update; err *= b^2/(b^2+4 gamma^2)
+__global__ void k_fin_b(const double2 *part, int nblk, int nvec, double *b_now, double *b_hist, int stride, int col,
+                        double *scale, double *thr2, double *err, double eps, double gamma, int first) {
+  __shared__ double sh[32];
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int k = 0; k < nvec; k++) {
+    double s = 0;
+    for (int b = threadIdx.x; b < nblk; b += blockDim.x) s += part[b * nvec + k].x;
+    for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) sh[wid] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0;
+      for (int w = 0; w < nw; w++) t += sh[w];
+      double b = sqrt(t);
+      b_now[k] = b;
+      b_hist[k * stride + col] = b;
+      scale[k] = (b > 0.0) ? 1.0 / b : 0.0;
+      double e = first ? 1.0 : err[k];
+      double th = eps / e;
+      thr2[k] = th * th;
+      if (!first) err[k] = e * (b * b / (b * b + 4 * gamma * gamma));
+      else err[k] = 1.0;
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void k_zero(double *p, int64_t n) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) p[i] = 0.0;
+}
+
+__global__ void k_copy_col(const double2 *src, double2 *dst, int64_t n) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = src[i];
+}
+
+extern "C" qg_status qg_lanczos_tridiag(qg_context ctx, qg_operator op, qg_basis b, const double *v0_dev, int32_t nvec,
+                                        int32_t ntri, double eps, double gamma, double *a_host, double *b_host,
+                                        double *krylov_dev) {
+  if (!ctx || !op || !b || !v0_dev || nvec <= 0 || ntri <= 0 || !a_host || !b_host || op->nf != b->nf) {
+    if (ctx) ctx->last_error = "qg_lanczos_tridiag: bad argument";
+    return QG_ERR_ARG;
+  }
+  cudaStream_t s = ctx->stream;
+  int64_t n = b->n;
+  int64_t len = n * nvec;  // complex entries per block vector
+  int P = partial_blocks(ctx, n);
+  int Papply = (int)((n + 255) / 256);
+  if (Papply < 1) Papply = 1;
+  // device state
+  double2 *vp = nullptr, *vc = nullptr, *w = nullptr, *w2 = nullptr, *vraw = nullptr, *zero = nullptr;
+  double2 *npart = nullptr, *dpart = nullptr;
+  double *scal = nullptr;  // a_now, b_now, scale, thr2, err, zero_beta, a_hist, b_hist
+  size_t vb = std::max<int64_t>(len, 1) * 16;
+  cudaError_t e = cudaSuccess;
+#define ALLOC(p, bytes) \
+  if (e == cudaSuccess) e = cudaMalloc((void **)&p, bytes)
+  ALLOC(vp, vb);
+  ALLOC(vc, vb);
+  ALLOC(w, vb);
+  ALLOC(w2, vb);
+  ALLOC(vraw, vb);
+  ALLOC(zero, vb);
+  ALLOC(npart, (size_t)P * nvec * 16);
+  ALLOC(dpart, (size_t)Papply * nvec * 16);
+  size_t nscal = 6 * (size_t)nvec + (size_t)nvec * (ntri + 1) + (size_t)nvec * ntri;
+  ALLOC(scal, nscal * 8);
+#undef ALLOC
+  if (e != cudaSuccess) {
+    cudaFree(vp); cudaFree(vc); cudaFree(w); cudaFree(w2); cudaFree(vraw); cudaFree(zero);
+    cudaFree(npart); cudaFree(dpart); cudaFree(scal);
+    ctx->last_error = "qg_lanczos_tridiag: out of device memory";
+    return QG_ERR_OOM;
+  }
+  double *a_now = scal, *b_now = scal + nvec, *scale = scal + 2 * nvec, *thr2 = scal + 3 * nvec,
+         *err = scal + 4 * nvec, *zb = scal + 5 * nvec;
+  double *a_hist = scal + 6 * nvec, *b_hist = a_hist + (size_t)nvec * (ntri + 1);
+  qg_status st = QG_OK;
+  k_zero<<<(unsigned)((nscal + 255) / 256), 256, 0, s>>>(scal, (int64_t)nscal);
+  cudaMemsetAsync(zero, 0, vb, s);
+  ctx->launches++;
+  // step 0: b0 = |v0|, scale, threshold eps (err = 1)
+  k_dot_partial<<<P, RBLK, (RBLK / 32) * sizeof(double2), s>>>(n, nvec, (const double2 *)v0_dev, nullptr, npart);
+  k_fin_b<<<1, 256, 0, s>>>(npart, P, nvec, b_now, b_hist, ntri, 0, scale, thr2, err, eps, gamma, 1);
+  ctx->launches += 2;
+  ApplyFuse fz;
+  fz.src_scale = scale;
+  fz.thr2 = thr2;
+  fz.own_out = vc;
+  fz.prev = zero;
+  fz.beta = zb;
+  fz.dot_part = dpart;
+  st = qg_apply_launch(ctx, op, b, b, v0_dev, (double *)w, nvec, &fz);
+  if (st == QG_OK && krylov_dev)
+    e = cudaMemcpyAsync(krylov_dev, vc, len * 16, cudaMemcpyDeviceToDevice, s);
+  if (st == QG_OK) {
+    k_fin_a<<<1, 256, 0, s>>>(dpart, Papply, nvec, a_now, a_hist, ntri + 1, 1);
+    ctx->launches++;
+  }
+  for (int i = 1; i < ntri && st == QG_OK && e == cudaSuccess; i++) {
+    std::swap(vp, vc);  // vp = v_{i-1}
+    k_lanczos_axpy_norm<<<P, RBLK, (RBLK / 32) * sizeof(double2), s>>>(n, nvec, w, vp, a_now, vraw, npart);
+    k_fin_b<<<1, 256, 0, s>>>(npart, P, nvec, b_now, b_hist, ntri, i, scale, thr2, err, eps, gamma, 0);
+    ctx->launches += 2;
+    fz.own_out = vc;
+    fz.prev = vp;
+    fz.beta = b_now;
+    st = qg_apply_launch(ctx, op, b, b, (const double *)vraw, (double *)w2, nvec, &fz);
+    std::swap(w, w2);
+    if (st == QG_OK && krylov_dev)
+      e = cudaMemcpyAsync(krylov_dev + 2 * (size_t)i * len, vc, len * 16, cudaMemcpyDeviceToDevice, s);
+    k_fin_a<<<1, 256, 0, s>>>(dpart, Papply, nvec, a_now, a_hist, ntri + 1, i + 1);
+    ctx->launches++;
+  }
+  if (st == QG_OK && e == cudaSuccess) {
+    e = cudaMemcpyAsync(a_host, a_hist, (size_t)nvec * (ntri + 1) * 8, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(b_host, b_hist, (size_t)nvec * ntri * 8, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  }
+  if (e != cudaSuccess && st == QG_OK) st = qg_cuda_fail(ctx, e, "qg_lanczos_tridiag");
+  cudaStreamSynchronize(s);
+  cudaFree(vp); cudaFree(vc); cudaFree(w); cudaFree(w2); cudaFree(vraw); cudaFree(zero);
+  cudaFree(npart); cudaFree(dpart); cudaFree(scal);
+  if (st == QG_OK) {
+    for (int k = 0; k < nvec; k++) a_host[k * (ntri + 1)] = 0.0;
+    st = qg_check_device_error(ctx, "qg_lanczos_tridiag");
+  }
+  return st;
+}
+
+// ------------------------------------------------------------------ continued fraction
+
+// One thread per (spectrum, frequency); the recursion runs from the bottom of the chain as
+// TriDiagonalMatrixToSpectrum does (Core/Spectral.cpp:1444-1458).
+__global__ void k_cf(int nspec, int ntri, const double *__restrict__ a, const double *__restrict__ b,
+                     const double *__restrict__ e0, double emin, double de, int ne, double gamma, double2 *g) {
+  int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  int64_t np = (int64_t)ne + 1;
+  if (t >= (int64_t)nspec * np) return;
+  int s = (int)(t / np);
+  int k = (int)(t % np);
+  const double *as = a + (size_t)s * (ntri + 1);
+  const double *bs = b + (size_t)s * ntri;
+  double hg = gamma * 0.5;
+  double w = (double)k * de + emin + e0[s];
+  double dn = w - as[ntri];
+  double den = hg * hg + dn * dn;
+  double vr = dn / den, vi = -hg / den;
+  for (int j = (ntri > 1 ? ntri : 1) - 1; j >= 1; j--) {
+    double b2 = bs[j] * bs[j];
+    double zr = w - as[j] - vr * b2, zi = hg - vi * b2;
+    den = zi * zi + zr * zr;
+    vr = zr / den;
+    vi = (vi * b2 - hg) / den;
+  }
+  double b02 = bs[0] * bs[0];
+  g[t] = make_double2(as[0] + vr * b02, vi * b02);
+}
+
+extern "C" qg_status qg_cf_spectra(qg_context ctx, int32_t nspec, int32_t ntri, const double *a_host,
+                                   const double *b_host, const double *e0_host, double emin, double de, int32_t ne,
+                                   double gamma, double *g_host) {
+  if (!ctx || nspec <= 0 || ntri <= 0 || ne < 0 || !a_host || !b_host || !e0_host || !g_host) return QG_ERR_ARG;
+  cudaStream_t s = ctx->stream;
+  double *d = nullptr;
+  size_t na = (size_t)nspec * (ntri + 1), nb = (size_t)nspec * ntri, ng = (size_t)nspec * (ne + 1);
+  QG_CUDA(ctx, cudaMalloc(&d, (na + nb + nspec) * 8 + ng * 16));
+  double *da = d, *db = d + na, *de0 = db + nb;
+  double2 *dg = (double2 *)(de0 + nspec);
+  cudaError_t e = cudaMemcpyAsync(da, a_host, na * 8, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(db, b_host, nb * 8, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(de0, e0_host, nspec * 8, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) {
+    k_cf<<<(unsigned)((ng + 127) / 128), 128, 0, s>>>(nspec, ntri, da, db, de0, emin, de, ne, gamma, dg);
+    ctx->launches++;
+    e = cudaMemcpyAsync(g_host, dg, ng * 16, cudaMemcpyDeviceToHost, s);
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  cudaFree(d);
+  if (e != cudaSuccess) return qg_cuda_fail(ctx, e, "qg_cf_spectra");
+  return qg_check_launch(ctx, "qg_cf_spectra");
+}

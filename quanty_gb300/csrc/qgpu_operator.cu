@@ -1,0 +1,273 @@
+// Operator upload: ladder strings -> canonical masks -> grouped device term tables.
+//
+// The reference keeps an operator as strings of ladder codes per length
+// (OperatorFixedLengthType, Core/StructDef.cpp:223-236) and evaluates each string on each
+// determinant with a byte loop (OperatorCr/OperatorAn/OperatorLader,
+// Core/OperatorWaveFunction.cpp:7-115).  Here each string is evaluated once, symbolically,
+// into the masks described in qgpu_internal.cuh, strings with identical action are merged,
+// and two tables are uploaded:
+//   push: forward action grouped by need1 -- a source determinant emits its targets
+//         (basis closure);
+//   pull: adjoint action grouped by need1 -- a row determinant finds its sources
+//         (H*psi without atomics: y_i = sum_t V_t <i|t|j> x_j and <i|t|j> = sign(t^dag, i)).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <tuple>
+
+#include "qgpu_internal.cuh"
+
+namespace {
+
+struct Masks {
+  uint64_t n1[QG_MAXW] = {0, 0}, n0[QG_MAXW] = {0, 0}, fl[QG_MAXW] = {0, 0}, sg[QG_MAXW] = {0, 0};
+  bool operator<(const Masks &o) const {
+    for (int i = 0; i < QG_MAXW; i++) {
+      if (n1[i] != o.n1[i]) return n1[i] < o.n1[i];
+      if (n0[i] != o.n0[i]) return n0[i] < o.n0[i];
+      if (fl[i] != o.fl[i]) return fl[i] < o.fl[i];
+      if (sg[i] != o.sg[i]) return sg[i] < o.sg[i];
+    }
+    return false;
+  }
+};
+
+inline void setbit(uint64_t *m, int p) { m[p >> 6] |= 1ull << (p & 63); }
+inline int parity_and(const uint64_t *a, const uint64_t *b) {
+  int c = 0;
+  for (int i = 0; i < QG_MAXW; i++) c += __builtin_popcountll(a[i] & b[i]);
+  return c & 1;
+}
+inline int devbit(int nf, int orb) { return nf - 1 - orb; }
+
+// Symbolic evaluation of one ladder string (o[0] acts first).  Returns false if the string
+// vanishes on every determinant.  sign = (-1)^(parity(d & sg) + c).
+bool digest(int nf, int len, const uint16_t *o, Masks &m, int &c) {
+  std::vector<int> init(nf, -1), tog(nf, 0);
+  c = 0;
+  for (int t = 0; t < len; t++) {
+    int q = o[t] & 0x7FFF;
+    bool cr = (o[t] & 0x8000) != 0;
+    if (q >= nf) return false;
+    int cur_needed = cr ? 0 : 1;  // occupation required before this step
+    if (init[q] < 0) {
+      init[q] = cur_needed ^ tog[q];
+    } else if ((init[q] ^ tog[q]) != cur_needed) {
+      return false;
+    }
+    // parity of occupied orbitals j < q in the intermediate determinant
+    //   = parity(d & below(q)) ^ parity(toggled-so-far & below(q))
+    int tp = 0;
+    for (int j = 0; j < q; j++) tp ^= tog[j];
+    c ^= tp;
+    tog[q] ^= 1;
+  }
+  // rebuild sg as the xor of the below-sets of all steps: orbital j is in it iff an odd
+  // number of steps act on an orbital above j
+  std::memset(m.sg, 0, sizeof(m.sg));
+  std::vector<int> cnt(nf + 1, 0);
+  for (int t = 0; t < len; t++) cnt[(o[t] & 0x7FFF)]++;
+  int above = 0;  // number of steps on orbitals > j, mod 2
+  for (int j = nf - 1; j >= 0; j--) {
+    if (above & 1) setbit(m.sg, devbit(nf, j));
+    above += cnt[j];
+  }
+  for (int q = 0; q < nf; q++) {
+    if (init[q] == 1) setbit(m.n1, devbit(nf, q));
+    if (init[q] == 0) setbit(m.n0, devbit(nf, q));
+    if (tog[q]) setbit(m.fl, devbit(nf, q));
+  }
+  // canonical form: sign bits on orbitals whose value is fixed on the domain fold into c
+  uint64_t fixed[QG_MAXW];
+  for (int i = 0; i < QG_MAXW; i++) fixed[i] = m.n1[i] | m.n0[i];
+  c ^= parity_and(m.sg, m.n1);
+  for (int i = 0; i < QG_MAXW; i++) m.sg[i] &= ~fixed[i];
+  return true;
+}
+
+// Adjoint action: applicable on d' = d ^ fl; needs swap on flipped bits; same sg;
+// const changes by parity(fl & sg).
+Masks adjoint(const Masks &m, int &cflip) {
+  Masks a;
+  for (int i = 0; i < QG_MAXW; i++) {
+    a.n1[i] = (m.n1[i] & ~m.fl[i]) | (m.n0[i] & m.fl[i]);
+    a.n0[i] = (m.n0[i] & ~m.fl[i]) | (m.n1[i] & m.fl[i]);
+    a.fl[i] = m.fl[i];
+    a.sg[i] = m.sg[i];
+  }
+  cflip = parity_and(m.fl, m.sg);
+  // re-canonicalise: sg has no bits on n1|n0 of m; on the adjoint domain the fixed bits are
+  // the same set, so sg stays canonical.
+  return a;
+}
+
+struct Entry {
+  Masks m;
+  double re, im;
+};
+
+template <int W>
+void build_table(qg_context ctx, const std::vector<Entry> &terms, HostTable &tab, qg_status &st) {
+  // group by need1
+  std::map<std::vector<uint64_t>, std::vector<int>> groups;
+  for (int t = 0; t < (int)terms.size(); t++) {
+    std::vector<uint64_t> key(terms[t].m.n1, terms[t].m.n1 + W);
+    groups[key].push_back(t);
+  }
+  std::vector<GroupDev<W>> g;
+  std::vector<TermDev<W>> tt;
+  for (auto &kv : groups) {
+    GroupDev<W> gd;
+    std::memset(&gd, 0, sizeof(gd));
+    for (int i = 0; i < W; i++) gd.need1[i] = kv.first[i];
+    gd.begin = (int)tt.size();
+    gd.diag = 1;
+    // diagonal terms first inside a group
+    std::vector<int> idx = kv.second;
+    std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) {
+      bool da = true, db = true;
+      for (int i = 0; i < W; i++) {
+        da &= terms[a].m.fl[i] == 0;
+        db &= terms[b].m.fl[i] == 0;
+      }
+      return da && !db;
+    });
+    for (int t : idx) {
+      TermDev<W> td;
+      std::memset(&td, 0, sizeof(td));
+      bool d = true;
+      for (int i = 0; i < W; i++) {
+        td.need0[i] = terms[t].m.n0[i];
+        td.flip[i] = terms[t].m.fl[i];
+        td.sgn[i] = terms[t].m.sg[i];
+        d &= td.flip[i] == 0;
+      }
+      if (!d) gd.diag = 0;
+      td.vre = terms[t].re;
+      td.vim = terms[t].im;
+      tt.push_back(td);
+    }
+    gd.end = (int)tt.size();
+    g.push_back(gd);
+  }
+  tab.ngroups = (int)g.size();
+  tab.nterms = (int)tt.size();
+  size_t gb = std::max<size_t>(1, g.size()) * sizeof(GroupDev<W>);
+  size_t tb = std::max<size_t>(1, tt.size()) * sizeof(TermDev<W>);
+  cudaError_t e = cudaMalloc(&tab.d_groups, gb);
+  if (e == cudaSuccess) e = cudaMalloc(&tab.d_terms, tb);
+  if (e == cudaSuccess && !g.empty())
+    e = cudaMemcpy(tab.d_groups, g.data(), g.size() * sizeof(GroupDev<W>), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && !tt.empty())
+    e = cudaMemcpy(tab.d_terms, tt.data(), tt.size() * sizeof(TermDev<W>), cudaMemcpyHostToDevice);
+  st = (e == cudaSuccess) ? QG_OK : qg_cuda_fail(ctx, e, "operator table upload");
+}
+
+}  // namespace
+
+extern "C" qg_status qg_operator_create(qg_context ctx, int32_t nf, int32_t nterms, const int32_t *term_len,
+                                        const uint16_t *ops, const double *v_re, const double *v_im,
+                                        qg_operator *out) {
+  if (!ctx || !out || nf <= 0 || nf > 127 || nterms < 0) {
+    if (ctx) ctx->last_error = "qg_operator_create: need 0 < nf <= 127";
+    return QG_ERR_ARG;
+  }
+  if (nterms > 0 && (!term_len || !v_re)) return QG_ERR_ARG;
+  // digest and merge strings with identical action (the reference merges equal strings
+  // through its operator hash, Core/OperatorArithmetic.cpp:322)
+  std::map<Masks, std::pair<double, double>> merged;
+  std::vector<Masks> order;
+  int64_t off = 0;
+  int maxlen = 0;
+  for (int t = 0; t < nterms; t++) {
+    int len = term_len[t];
+    if (len < 0 || len > 64) {
+      ctx->last_error = "qg_operator_create: ladder string length out of range";
+      return QG_ERR_ARG;
+    }
+    maxlen = std::max(maxlen, len);
+    Masks m;
+    int c = 0;
+    bool ok = digest(nf, len, ops + off, m, c);
+    off += len;
+    if (!ok) continue;
+    double s = c ? -1.0 : 1.0;
+    double re = s * v_re[t], im = s * (v_im ? v_im[t] : 0.0);
+    auto it = merged.find(m);
+    if (it == merged.end()) {
+      merged[m] = {re, im};
+      order.push_back(m);
+    } else {
+      it->second.first += re;
+      it->second.second += im;
+    }
+  }
+  std::vector<Entry> fwd, pull;
+  double vmax = 0;
+  for (auto &m : order) {
+    auto v = merged[m];
+    if (v.first == 0.0 && v.second == 0.0) continue;
+    fwd.push_back({m, v.first, v.second});
+    vmax = std::max(vmax, std::hypot(v.first, v.second));
+    int cf = 0;
+    Masks a = adjoint(m, cf);
+    pull.push_back({a, v.first * (cf ? -1.0 : 1.0), v.second * (cf ? -1.0 : 1.0)});
+  }
+  // Hermiticity: the adjoint of every term must be a term with the conjugate value
+  int herm = 1;
+  {
+    std::map<Masks, std::pair<double, double>> fm;
+    for (auto &e : fwd) fm[e.m] = {e.re, e.im};
+    for (auto &e : pull) {
+      auto it = fm.find(e.m);
+      double er = e.re, ei = -e.im;  // conj of the value of the adjoint term
+      double gr = 0, gi = 0;
+      if (it != fm.end()) {
+        gr = it->second.first;
+        gi = it->second.second;
+      }
+      if (std::hypot(gr - er, gi - ei) > 1e-12 * std::max(1.0, vmax)) herm = 0;
+    }
+  }
+  qg_operator op = new qg_operator_s();
+  op->ctx = ctx;
+  op->nf = nf;
+  op->W = qg_words_for(nf);
+  op->nterms_in = nterms;
+  op->nterms = (int)fwd.size();
+  op->hermitian = herm;
+  op->max_len = maxlen;
+  qg_status st = QG_OK;
+  if (op->W == 1) {
+    build_table<1>(ctx, pull, op->pull, st);
+    if (st == QG_OK) build_table<1>(ctx, fwd, op->push, st);
+  } else {
+    build_table<2>(ctx, pull, op->pull, st);
+    if (st == QG_OK) build_table<2>(ctx, fwd, op->push, st);
+  }
+  if (st != QG_OK) {
+    qg_operator_destroy(op);
+    return st;
+  }
+  *out = op;
+  return QG_OK;
+}
+
+extern "C" qg_status qg_operator_destroy(qg_operator op) {
+  if (!op) return QG_OK;
+  cudaFree(op->pull.d_groups);
+  cudaFree(op->pull.d_terms);
+  cudaFree(op->push.d_groups);
+  cudaFree(op->push.d_terms);
+  delete op;
+  return QG_OK;
+}
+
+extern "C" qg_status qg_operator_info(qg_operator op, int32_t *nterms, int32_t *ngroups, int32_t *hermitian) {
+  if (!op) return QG_ERR_ARG;
+  if (nterms) *nterms = op->nterms;
+  if (ngroups) *ngroups = op->pull.ngroups;
+  if (hermitian) *hermitian = op->hermitian;
+  return QG_OK;
+}

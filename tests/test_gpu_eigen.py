@@ -1,0 +1,36 @@
+"""Eigensystem on the GPU: restarted block Lanczos against the Mathematica eigenvalues of
+TestScripts/Eigensystem.Quanty and the reference's ground energies (1e-10 eV)."""
+import numpy as np
+import pytest
+
+from conftest import golden
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def api():
+    from quanty_gb300 import build
+    build.build()
+    from quanty_gb300 import api
+    return api
+
+
+def test_fshell_atom_eigenvalues(api):
+    g = golden("fshell_eigen.json")
+    H = api.Operator.from_fixture(g["H"])
+    psis, E = api.Eigensystem(H, [14, 0, ["11111111111111", 6, 6]], 10, {"Zero": 1e-14})
+    assert np.max(np.abs(E - np.array(g["expected_mathematica"]))) < 1e-10
+    # eigenvectors: <psi|H|psi> = E and orthonormal
+    for p, e in zip(psis, E):
+        assert abs(p.norm() - 1) < 1e-10
+        assert abs(api.PsiOperatorPsi(H, p).real - e) < 1e-10
+
+
+@pytest.mark.parametrize("fx,key", [("c0_xas.json", "energies_dense"), ("c1_lf.json", "energies_krylov")])
+def test_ground_energies(api, fx, key):
+    g = golden(fx)
+    H = api.Operator.from_fixture(g["H"])
+    R = [len(g["restrictions"][0][0]), 0] + [list(r) for r in g["restrictions"]]
+    psis, E = api.Eigensystem(H, R, 3, {"Zero": 1e-14})
+    assert np.max(np.abs(E - np.array(g[key]))) < 1e-10, (E, g[key])

@@ -1,0 +1,166 @@
+"""H*psi on the GPU against the reference fixtures and the CPU oracle (bit-exact determinant
+sets and signs, amplitudes to 1e-12 relative)."""
+import math
+
+import numpy as np
+import pytest
+
+from conftest import golden
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-12  # amplitudes, relative to the largest
+
+
+def rel_err(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    if a.size == 0 and b.size == 0:
+        return 0.0
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+@pytest.fixture(scope="module")
+def api():
+    from quanty_gb300 import build
+    build.build()
+    from quanty_gb300 import api
+    return api
+
+
+CASES = [c["name"] for c in golden("hpsi_cases.json")["cases"]]
+
+
+def _case(name):
+    return next(c for c in golden("hpsi_cases.json")["cases"] if c["name"] == name)
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_operator_psi_matches_reference(api, case):
+    c = _case(case)
+    H = api.Operator.from_fixture(c["H"])
+    psi = api.Wavefunction.from_fixture(c["psi"])
+    if H.nf > 127:
+        with pytest.raises(api.qgpu.QGError) as e:
+            api.OperatorPsi(H, psi)
+        assert e.value.status == 4
+        return
+    for key, res in (("Hpsi", None), ("Hpsir", c["restrictions"])):
+        out = api.OperatorPsi(H, psi, res)
+        ref = api.Wavefunction.from_fixture(c[key])
+        assert sorted(map(bytes, out.det)) == sorted(map(bytes, ref.det))  # bit-exact set
+        rd = ref.as_dict()
+        want = np.array([rd[bytes(r)] for r in out.det])
+        assert rel_err(out.val, want) < TOL, key
+
+
+@pytest.mark.parametrize("case", [n for n in CASES if _case(n)["H"]["nf"] <= 127])
+def test_conserve_basis_matches_reference(api, case):
+    c = _case(case)
+    H = api.Operator.from_fixture(c["H"])
+    psi = api.Wavefunction.from_fixture(c["psi"])
+    y = api.OperatorPsiConserveBasis(H, psi)
+    rd = api.Wavefunction.from_fixture(c["Hpsi"]).as_dict()
+    want = np.array([rd.get(bytes(r), 0.0) for r in psi.det])
+    assert rel_err(y.val, want) < TOL
+
+
+def _random_operator(api, nf, n2, n4, rng, complex_values=True):
+    terms = []
+    for _ in range(n2):
+        i, j = rng.choice(nf, 2, replace=False)
+        terms.append(([int(j), int(i) | api.CREATION], complex(rng.normal(), rng.normal() if complex_values else 0)))
+    for _ in range(n4):
+        i, j, k, l = rng.choice(nf, 4, replace=False)
+        terms.append(([int(l), int(k), int(j) | api.CREATION, int(i) | api.CREATION],
+                      complex(rng.normal(), rng.normal() if complex_values else 0)))
+    terms.append(([], 0.3))
+    return api.Operator(nf, terms)
+
+
+@pytest.mark.parametrize("nf,nel", [(20, 10), (64, 12), (86, 43), (127, 60)])
+def test_apply_matches_oracle_on_closed_sets(api, oracle_mod, nf, nel):
+    """Seeded random operators on bases grown by the device closure; the oracle's push-form
+    H*psi (reference ConserveBasis semantics) on the same basis and amplitudes."""
+    O = oracle_mod
+    rng = np.random.default_rng(nf)
+    H = _random_operator(api, nf, 3 * nf, 2 * nf, rng)
+    occ = rng.choice(nf, nel, replace=False)
+    s = ["0"] * nf
+    for i in occ:
+        s[i] = "1"
+    b = api.closure(H, api.dets_to_bytes(["".join(s)], nf), nf, None, 2)
+    dets = b.dets_bytes()
+    assert len(dets) > 100
+    x = rng.normal(size=len(dets)) + 1j * rng.normal(size=len(dets))
+    psi = api.Wavefunction(nf, dets, x)
+    y = api.OperatorPsiConserveBasis(H, psi)
+    op = O.Op({"nf": nf, "terms": [[list(t[0]), t[1].real, t[1].imag] for t in H.terms]})
+    want = O.apply_conserve(op, O.WF(nf, dets, x))
+    assert rel_err(y.val, want) < TOL
+    # the device's connection count equals the oracle's
+    assert api.count_nnz(H, b) == O.count_nnz(op, O.WF(nf, dets, x))
+
+
+def test_multivector_apply_equals_single(api):
+    import torch
+    rng = np.random.default_rng(5)
+    nf = 30
+    H = _random_operator(api, nf, 60, 60, rng)
+    b = api.closure(H, api.dets_to_bytes(["1" * 8 + "0" * 22], nf), nf, None, 2)
+    eng = api.engine()
+    n = b.n
+    X = torch.from_numpy(rng.normal(size=(n, 11)) + 1j * rng.normal(size=(n, 11))).cuda()
+    Y = eng.empty(n, 11)
+    eng.check(eng.L.qg_apply(eng.ctx, H.handle(), b.h, b.h, api._ptr(X), api._ptr(Y), 11))
+    for k in (0, 5, 10):
+        xk = X[:, k].contiguous()
+        yk = eng.empty(n)
+        eng.check(eng.L.qg_apply(eng.ctx, H.handle(), b.h, b.h, api._ptr(xk), api._ptr(yk), 1))
+        assert torch.equal(Y[:, k], yk[:, 0])  # same rows, same order of summation
+
+
+def test_edge_cases(api):
+    H = api.NewOperator(4, 0, [[0, -1, 0.5], [1, -0.0, 0.5]])
+    empty = api.Wavefunction(4, np.zeros((0, 1), np.uint8), [])
+    out = api.OperatorPsi(H, empty)
+    assert out.N == 0
+    none = api.Operator(4, [])
+    psi = api.NewWavefunction(4, 0, [["1100", 1.0], ["1010", 0.5j]])
+    assert api.OperatorPsi(none, psi).N == 0
+    # duplicate determinants merge (the reference adds into the existing element)
+    dup = api.NewWavefunction(4, 0, [["1010", 1.0], ["1010", 2.0]])
+    out = api.OperatorPsi(H, dup)
+    d = dict(zip(out.dets(), out.val))
+    assert abs(d["0110"] - 1.5) < 1e-15
+    # one orbital, and the widest supported determinant
+    one = api.NewOperator(1, 0, [[0, -0.0, 2.0]])
+    r = api.OperatorPsi(one, api.NewWavefunction(1, 0, [["1", 1.0]]))
+    assert r.dets() == ["1"] and abs(r.val[0] - 2.0) < 1e-15
+    wide = api.NewOperator(127, 0, [[126, -0.0, 1.0]])
+    r = api.OperatorPsi(wide, api.NewWavefunction(127, 0, [["1" + "0" * 126, 1.0]]))
+    assert r.dets() == ["0" * 126 + "1"]
+    # more orbitals than supported: a clear argument error
+    with pytest.raises(api.qgpu.QGError):
+        api.OperatorPsi(api.NewOperator(128, 0, [[127, -0.0, 1.0]]), api.NewWavefunction(128, 0, [["1" + "0" * 127, 1.0]]))
+
+
+def test_closure_counts_and_table_growth(api):
+    """Hopping on 30 orbitals with 7 electrons reaches all C(30,7) = 2,035,800 determinants;
+    this passes the 2^20 initial table capacity, so the grow-and-retry path runs."""
+    nf, nel = 30, 7
+    terms = []
+    for i in range(nf - 1):
+        terms.append(([i + 1, i | api.CREATION], 1.0))
+        terms.append(([i, (i + 1) | api.CREATION], 1.0))
+    H = api.Operator(nf, terms)
+    b = api.closure(H, api.dets_to_bytes(["1" * nel + "0" * (nf - nel)], nf), nf)
+    assert b.n == math.comb(nf, nel)
+    # restricted: at most 2 electrons in the last 10 orbitals
+    R = [("0" * 20 + "1" * 10, 0, 2)]
+    br = api.closure(H, api.dets_to_bytes(["1" * nel + "0" * (nf - nel)], nf), nf, R)
+    want = sum(math.comb(10, k) * math.comb(20, nel - k) for k in range(0, 3))
+    assert br.n == want
+    # sorted, unique, and every determinant finds itself
+    d = b.dets_bytes()
+    idx = b.find(d[:5000])
+    assert np.array_equal(idx, np.arange(5000))

@@ -1,0 +1,92 @@
+"""Lanczos tridiagonalisation and continued-fraction spectra on the GPU against the reference:
+the golden response functions of TestScripts/CreateSpectra.Quanty (1e-12 at its omega list)
+and the XAS spectra of the 16- and 26-orbital cases (1e-8 relative)."""
+import math
+
+import numpy as np
+import pytest
+
+from conftest import golden
+
+pytestmark = pytest.mark.gpu
+EPS_DEFAULT = math.sqrt(np.finfo(float).eps) / 100
+SPEC_TOL = 1e-8
+
+
+@pytest.fixture(scope="module")
+def api():
+    from quanty_gb300 import build
+    build.build()
+    from quanty_gb300 import api
+    return api
+
+
+def spec_err(G, ref):
+    return float(np.max(np.abs(G - ref)) / np.max(np.abs(ref)))
+
+
+def test_chain_golden_response_functions(api):
+    g = golden("chain_spectra.json")
+    for c in g["combos"]:
+        H = api.Operator.from_fixture(g[c["H"]])
+        T = api.Operator.from_fixture(g[c["T"]])
+        psi = api.Wavefunction.from_fixture(g[c["psi"]])
+        E0 = api.PsiOperatorPsi(H, psi).real
+        Tpsi = api.OperatorPsi(T, psi)
+        a, b = api.LanczosTriDiagonalize(H, Tpsi, 200, EPS_DEFAULT, EPS_DEFAULT)
+        a_sh = np.r_[0.0, a[1:] - E0]
+        ref = c["ref_tri"]
+        assert np.allclose(a_sh[1:12], ref["a"][1:12], atol=1e-10)
+        assert np.allclose(b[:12], ref["b"][:12], atol=1e-10)
+        got = [api.TriDiagonalMatrixToSpectrum(0.0, a_sh, b, w, w + 1.0, 1, g["gamma"])[0, 0] for w in g["omega"]]
+        gold = [complex(*z) for z in c["golden_G"]]
+        assert max(abs(x - y) for x, y in zip(got, gold)) < g["threshold"], (c["H"], c["T"], c["psi"])
+
+
+@pytest.mark.parametrize("fx,eps_key", [("c0_xas.json", "eps0"), ("c0_xas.json", "epsdefault"), ("c1_lf.json", "eps0")])
+@pytest.mark.parametrize("batched", [True, False])
+def test_xas_spectra_match_reference(api, fx, eps_key, batched):
+    g = golden(fx)
+    HX = api.Operator.from_fixture(g["HX"])
+    Ts = [api.Operator.from_fixture(g[t]) for t in ("Tx", "Ty", "Tz")]
+    psis = [api.Wavefunction.from_fixture(p) for p in g["psi"]]
+    o = dict(g["spectra_opts"])
+    if eps_key == "eps0":
+        o["Epsilon"] = 0.0
+    else:
+        o.pop("Epsilon", None)
+    S, tri = api.CreateSpectra(HX, Ts, psis, o, batched=batched)
+    ref = g["spec_" + eps_key]
+    for s in range(9):
+        R = np.array(ref["re"][s]) + 1j * np.array(ref["im"][s])
+        assert spec_err(S.G[s], R) < SPEC_TOL, (fx, eps_key, s, spec_err(S.G[s], R))
+        rt = g["tri_" + eps_key][s]
+        assert abs(tri[s][1][0] - rt["b"][0]) < 1e-12
+        assert abs(tri[s][0][1] - rt["a"][1]) < 1e-10
+
+
+def test_cf_kernel_matches_oracle(api, oracle_mod):
+    rng = np.random.default_rng(3)
+    ntri, ns, ne = 150, 7, 777
+    a = np.c_[np.zeros(ns), rng.normal(size=(ns, ntri))]
+    b = np.abs(rng.normal(size=(ns, ntri))) + 0.1
+    e0 = rng.normal(size=ns)
+    G = api.TriDiagonalMatrixToSpectrum(e0, a, b, -7.0, 9.0, ne, 0.37)
+    for s in range(ns):
+        want = oracle_mod.cf_spectrum(a[s], b[s], e0[s], -7.0, 16.0 / ne, ne, 0.37)
+        assert spec_err(G[s], want) < 1e-13
+
+
+def test_lanczos_matches_oracle_coefficients(api, oracle_mod):
+    """The device recursion follows the oracle's (reference) recursion step by step while the
+    Krylov space is far from exhausted."""
+    O = oracle_mod
+    g = golden("c1_lf.json")
+    HX = api.Operator.from_fixture(g["HX"])
+    T = api.Operator.from_fixture(g["Tz"])
+    psi = api.Wavefunction.from_fixture(g["psi"][0])
+    Tpsi = api.OperatorPsi(T, psi)
+    a, b = api.LanczosTriDiagonalize(HX, Tpsi, 40, 0.0, 0.5)
+    ao, bo = O.lanczos_tridiag(O.Op(g["HX"]), O.WF(26, Tpsi.det, Tpsi.val), 40, 0.0, 0.5)
+    assert np.allclose(a[:20], ao[:20], atol=1e-10)
+    assert np.allclose(b[:20], bo[:20], atol=1e-10)
