@@ -47,8 +47,11 @@ class Engine:
         h = C.c_void_p()
         self.check(self.L.qg_init(device, C.byref(h)), ctx=None)
         self.ctx = h
-        stream = torch.cuda.current_stream(device).cuda_stream
-        self.check(self.L.qg_set_stream(self.ctx, C.c_void_p(stream)))
+        # one explicit stream shared by torch (buffers, events) and the library; it becomes
+        # torch's current stream so tensors and CUDA events are ordered with the kernels
+        self.stream = torch.cuda.Stream(device)
+        torch.cuda.set_stream(self.stream)
+        self.check(self.L.qg_set_stream(self.ctx, C.c_void_p(self.stream.cuda_stream)))
 
     def check(self, st, ctx="self"):
         if st != 0:
@@ -534,7 +537,7 @@ def Eigensystem(H, StartRestrictions, Npsi, options=None, eng=None, seed=12345):
     x = eng.torch.from_numpy(x0).to("cuda:%d" % eng.device).contiguous()
     en = np.zeros(Npsi)
     it = C.c_int32()
-    K = int(min(max(4 * Npsi, 64), 256, n))
+    K = int(min(max(8 * Npsi, 128), 256, n))
     tol = float(o["Zero"])
     eng.check(eng.L.qg_block_groundstate(eng.ctx, H.handle(eng), basis.h, Npsi, _ptr(x), _ptr(en), tol, K, 200,
                                          C.byref(it)))

@@ -355,17 +355,28 @@ extern "C" qg_status qg_block_groundstate(qg_context ctx, qg_operator op, qg_bas
     k_combine<<<grid(n * p), 256, 0, s>>>(V, K, k, Cd, X, p, p, n);
     ctx->launches++;
     for (int j = 0; j < p; j++) theta[j] = w[j];
-    // convergence: variance |H x|^2 - theta^2 per vector
+    // convergence: variance <(H - theta)^2> = |H x - theta x|^2 per vector, formed from the
+    // residual itself (no cancellation between <H^2> and <H>^2)
     st = qg_apply_strided(ctx, op, b, b, (const double *)X, p, (double *)W, p, p, nullptr);
     it++;
     if (st != QG_OK) break;
+    {
+      std::vector<cd> th((size_t)p * p, cd(0, 0));
+      for (int j = 0; j < p; j++) th[(size_t)j * p + j] = theta[j];
+      e = cudaMemcpyAsync(Cd, th.data(), th.size() * 16, cudaMemcpyHostToDevice, s);
+      if (e != cudaSuccess) {
+        st = qg_cuda_fail(ctx, e, "residual");
+        break;
+      }
+      k_sub_mul<<<grid(n * p), 256, 0, s>>>(X, p, 0, p, Cd, W, p, 0, p, n);
+      ctx->launches++;
+    }
     std::vector<cd> hh;
     double worst = 0;
     for (int j = 0; j < p && st == QG_OK; j++) {
       st = G.run(W, p, j, 1, W, p, j, 1, &hh);
       if (st != QG_OK) break;
-      double var = hh[0].real() - theta[j] * theta[j];
-      worst = std::max(worst, std::fabs(var));
+      worst = std::max(worst, std::fabs(hh[0].real()));
     }
     if (worst < tol) converged = true;
   }
