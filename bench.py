@@ -37,6 +37,8 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--shells", type=int, default=7)
+    p.add_argument("--hole-max", type=int, default=3)
+    p.add_argument("--particle-max", type=int, default=2)
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
     return p.parse_args()
@@ -111,9 +113,10 @@ def profiled_traffic():
     return float(m.group(1)) if m else None
 
 
-def build_workload(api, shells):
+def build_workload(api, args):
     from quanty_gb300 import workloads
-    H, R, seed, info = workloads.anderson_impurity(nshell=shells)
+    H, R, seed, info = workloads.anderson_impurity(nshell=args.shells, hole_max=args.hole_max,
+                                                   particle_max=args.particle_max)
     eng = api.engine()
     basis = api.closure(H, api.dets_to_bytes([seed], H.nf), H.nf, R, -1, eng)
     return H, R, basis, info
@@ -156,8 +159,9 @@ def run_reference(args):
     O.build()
     from quanty_gb300 import workloads
     # the basis comes from the same closure rules, enumerated on the host without a GPU
-    H, R, seed, info = workloads.anderson_impurity(nshell=args.shells)
-    dets = workloads.anderson_sector_bytes(info, H.nf)
+    H, R, seed, info = workloads.anderson_impurity(nshell=args.shells, hole_max=args.hole_max,
+                                                   particle_max=args.particle_max)
+    dets = workloads.anderson_sector_bytes(info, H.nf, hole_max=args.hole_max, particle_max=args.particle_max)
     n = len(dets)
     rng = np.random.default_rng(0)
     x = rng.normal(size=n) + 1j * rng.normal(size=n)
@@ -213,7 +217,7 @@ def main():
     api._engine = api.Engine(local)
     eng = api.engine()
     t_setup = time.perf_counter()
-    H, R, basis, info = build_workload(api, args.shells)
+    H, R, basis, info = build_workload(api, args)
     n = basis.n
     t_setup = time.perf_counter() - t_setup
     nterms = H.info()["nterms"]

@@ -23,7 +23,7 @@ __global__ void k_gram_partial(const double2 *__restrict__ A, int lda, int a0, i
                                int ldb, int b0, int kb, int64_t n, int64_t chunk, double2 *part) {
   int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= ka * kb) return;
-  int i = q % ka, j = q / ka;
+  int i = q / kb, j = q % kb;  // row-major C[i * kb + j], the layout every consumer reads
   int64_t r0 = blockIdx.y * chunk, r1 = r0 + chunk;
   if (r1 > n) r1 = n;
   double sr = 0, si = 0;

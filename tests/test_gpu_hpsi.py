@@ -65,13 +65,22 @@ def test_conserve_basis_matches_reference(api, case):
 
 
 def _random_operator(api, nf, n2, n4, rng, complex_values=True):
-    terms = []
-    for _ in range(n2):
-        i, j = rng.choice(nf, 2, replace=False)
-        terms.append(([int(j), int(i) | api.CREATION], complex(rng.normal(), rng.normal() if complex_values else 0)))
-    for _ in range(n4):
-        i, j, k, l = rng.choice(nf, 4, replace=False)
-        terms.append(([int(l), int(k), int(j) | api.CREATION, int(i) | api.CREATION],
+    """Distinct actions only (no two strings that the device would merge), so connection
+    counts compare one to one with the oracle's per-string loop."""
+    terms, seen = [], set()
+    while len(terms) < n2:
+        i, j = (int(v) for v in rng.choice(nf, 2, replace=False))
+        if (i, j) in seen:
+            continue
+        seen.add((i, j))
+        terms.append(([j, i | api.CREATION], complex(rng.normal(), rng.normal() if complex_values else 0)))
+    while len(terms) < n2 + n4:
+        i, j, k, l = (int(v) for v in rng.choice(nf, 4, replace=False))
+        key = (min(i, j), max(i, j), min(k, l), max(k, l))
+        if key in seen:
+            continue
+        seen.add(key)
+        terms.append(([l, k, j | api.CREATION, i | api.CREATION],
                       complex(rng.normal(), rng.normal() if complex_values else 0)))
     terms.append(([], 0.3))
     return api.Operator(nf, terms)
