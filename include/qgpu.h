@@ -141,8 +141,10 @@ qg_status qg_apply(qg_context ctx, qg_operator op, qg_basis basis_dst, qg_basis 
 qg_status qg_apply_host(qg_context ctx, qg_operator op, qg_basis basis_dst, qg_basis basis_src,
                         const double *x_host, double *y_host, int32_t nvec);
 
-/* Number of non-zero (row, term) connections of qg_apply(op, b, b) (sources inside b). */
+/* Number of non-zero (row, term) connections of qg_apply(op, b, b) (sources inside b), and
+ * the same count without the diagonal (flip == 0) connections. */
 qg_status qg_count_nnz(qg_context ctx, qg_operator op, qg_basis basis, int64_t *nnz);
+qg_status qg_count_nnz_offdiag(qg_context ctx, qg_operator op, qg_basis basis, int64_t *nnz);
 
 /* <psi|op|psi> for nvec vectors on one basis, complex result per vector (host out)
  * (PsiOperatorPsi / PsiHermitianOperatorPsi, Core/OperatorWaveFunction.cpp:5680, :5710). */

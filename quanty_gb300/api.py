@@ -348,11 +348,13 @@ def PsiOperatorPsi(O, psi, eng=None):
     return complex(out[0], out[1])
 
 
-def count_nnz(O, basis, eng=None):
-    """Non-zero (row, term) connections of O on a basis (sources inside the basis)."""
+def count_nnz(O, basis, eng=None, offdiag=False):
+    """Non-zero (row, term) connections of O on a basis (sources inside the basis); with
+    offdiag=True only those that change the determinant."""
     eng = eng or engine()
     n = C.c_int64()
-    eng.check(eng.L.qg_count_nnz(eng.ctx, O.handle(eng), basis.h, C.byref(n)))
+    f = eng.L.qg_count_nnz_offdiag if offdiag else eng.L.qg_count_nnz
+    eng.check(f(eng.ctx, O.handle(eng), basis.h, C.byref(n)))
     return n.value
 
 

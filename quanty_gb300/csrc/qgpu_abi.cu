@@ -27,6 +27,10 @@ qg_status qg_check_device_error(qg_context ctx, const char *what) {
   if (e == cudaSuccess) e = cudaMemcpyAsync(ctx->d_err, &zero, 4, cudaMemcpyHostToDevice, ctx->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) return qg_cuda_fail(ctx, e, what);
+  if (h & QG_DEVERR_TIMEOUT) {
+    ctx->last_error = std::string(what) + ": bounded wait on a bulk copy gave up";
+    return QG_ERR_TIMEOUT;
+  }
   if (h & QG_DEVERR_PROBE) {
     ctx->last_error = std::string(what) + ": hash probe limit reached";
     return QG_ERR_TIMEOUT;

@@ -31,56 +31,54 @@ __device__ __forceinline__ void qg_cas128(unsigned long long *addr, unsigned lon
       : "memory");
 }
 
-// Insert a key into the set; returns 1 if this call inserted it, 0 if it was present,
-// -1 if the probe limit was hit.
+// Insert a key into the set; returns 1 if this call inserted it, 0 if it was present, -1 if the probe limit was hit.  The slot index
+// is stored to *slot_out.
 template <int W>
-__device__ __forceinline__ int qg_set_insert(Slot<W> *slots, uint64_t hmask, const Key<W> &k) {
+__device__ __forceinline__ int qg_set_insert(Slot *slots, uint64_t hmask, const Key<W> &k, int64_t *slot_out) {
   uint64_t h = qg_hash<W>(k) & hmask;
+  uint64_t k1 = (W == 1) ? 0ull : k.w[W - 1];
   for (int p = 0; p < QG_PROBE_LIMIT; p++) {
     unsigned long long *a = reinterpret_cast<unsigned long long *>(slots + h);
-    if (W == 1) {
-      unsigned long long old = atomicCAS(a, QG_EMPTY_WORD, (unsigned long long)k.w[0]);
-      if (old == QG_EMPTY_WORD) return 1;
-      if (old == k.w[0]) return 0;
-    } else {
-      // fast path: a plain read that already shows the key or an occupied slot
-      unsigned long long olo, ohi;
-      qg_cas128(a, QG_EMPTY_WORD, QG_EMPTY_WORD, k.w[0], k.w[1], olo, ohi);
-      if (olo == QG_EMPTY_WORD && ohi == QG_EMPTY_WORD) return 1;
-      if (olo == k.w[0] && ohi == k.w[1]) return 0;
+    unsigned long long olo, ohi;
+    qg_cas128(a, QG_EMPTY_WORD, QG_EMPTY_WORD, k.w[0], k1, olo, ohi);
+    if (olo == QG_EMPTY_WORD && ohi == QG_EMPTY_WORD) {
+      *slot_out = (int64_t)h;
+      return 1;
+    }
+    if (olo == k.w[0] && ohi == k1) {
+      *slot_out = (int64_t)h;
+      return 0;
     }
     h = (h + 1) & hmask;
   }
   return -1;
 }
 
-template <int W>
-__global__ void k_slots_clear(Slot<W> *slots, int64_t n) {
+__global__ void k_slots_clear(Slot *slots, uint32_t *slot_row, int64_t n) {
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
-  Slot<W> s;
-  for (int j = 0; j < W; j++) s.k[j] = QG_EMPTY_WORD;
-  s.idx = QG_NO_INDEX;
-  for (int j = 0; j < 2 * W - 1; j++) s.pad[j] = 0;
+  Slot s;
+  s.k[0] = QG_EMPTY_WORD;
+  s.k[1] = QG_EMPTY_WORD;
+  s.vre = 0.0;
+  s.vim = 0.0;
   slots[i] = s;
+  if (slot_row) slot_row[i] = QG_NO_INDEX;
 }
 
-// Unique keys -> table rows.  Keys are distinct, so claiming the slot's index word is enough.
+// Unique keys -> table rows (full-key CAS claims the slot), plus both index maps.
 template <int W>
-__global__ void k_hash_build(Slot<W> *slots, uint64_t hmask, const Key<W> *keys, int64_t n, unsigned int *err) {
+__global__ void k_hash_build(Slot *slots, uint32_t *slot_row, uint32_t *row_slot, uint64_t hmask, const Key<W> *keys,
+                             int64_t n, unsigned int *err) {
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
-  Key<W> k = keys[i];
-  uint64_t h = qg_hash<W>(k) & hmask;
-  for (int p = 0; p < QG_PROBE_LIMIT; p++) {
-    uint32_t old = atomicCAS(&slots[h].idx, QG_NO_INDEX, (uint32_t)i);
-    if (old == QG_NO_INDEX) {
-      for (int j = 0; j < W; j++) slots[h].k[j] = k.w[j];
-      return;
-    }
-    h = (h + 1) & hmask;
+  int64_t h = -1;
+  if (qg_set_insert<W>(slots, hmask, keys[i], &h) < 0) {
+    atomicOr(err, QG_DEVERR_PROBE);
+    return;
   }
-  atomicOr(err, QG_DEVERR_PROBE);
+  slot_row[h] = (uint32_t)i;
+  row_slot[i] = (uint32_t)h;
 }
 
 // Reference bytes (orbital i in byte i>>3, mask 128>>(i&7)) -> key (orbital i at bit nf-1-i).
@@ -160,19 +158,26 @@ static qg_status build_hash_t(qg_basis b) {
   int64_t hcap = hcap_for(b->n);
   if (b->d_slots && b->hcap != hcap) {
     cudaFree(b->d_slots);
+    cudaFree(b->d_slot_row);
     b->d_slots = nullptr;
+    b->d_slot_row = nullptr;
   }
+  cudaError_t e = cudaSuccess;
   if (!b->d_slots) {
-    cudaError_t e = cudaMalloc(&b->d_slots, hcap * sizeof(Slot<W>));
-    if (e != cudaSuccess) return qg_cuda_fail(ctx, e, "hash table");
+    e = cudaMalloc(&b->d_slots, hcap * sizeof(Slot));
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_slot_row, hcap * sizeof(uint32_t));
   }
+  if (e == cudaSuccess && !b->d_row_slot) e = cudaMalloc(&b->d_row_slot, std::max<int64_t>(b->n, 1) * sizeof(uint32_t));
+  if (e != cudaSuccess) return qg_cuda_fail(ctx, e, "hash table");
   b->hcap = hcap;
-  k_slots_clear<W><<<grid_for(hcap), 256, 0, ctx->stream>>>((Slot<W> *)b->d_slots, hcap);
+  k_slots_clear<<<grid_for(hcap), 256, 0, ctx->stream>>>(b->d_slots, b->d_slot_row, hcap);
   ctx->launches++;
-  if (b->n)
-    k_hash_build<W><<<grid_for(b->n), 256, 0, ctx->stream>>>((Slot<W> *)b->d_slots, (uint64_t)(hcap - 1),
-                                                             (const Key<W> *)b->d_keys, b->n, ctx->d_err);
-  ctx->launches++;
+  if (b->n) {
+    k_hash_build<W><<<grid_for(b->n), 256, 0, ctx->stream>>>(b->d_slots, b->d_slot_row, b->d_row_slot,
+                                                             (uint64_t)(hcap - 1), (const Key<W> *)b->d_keys, b->n,
+                                                             ctx->d_err);
+    ctx->launches++;
+  }
   return qg_check_launch(ctx, "hash build");
 }
 
@@ -323,7 +328,33 @@ extern "C" qg_status qg_basis_destroy(qg_basis b) {
   if (!b) return QG_OK;
   cudaFree(b->d_keys);
   cudaFree(b->d_slots);
+  cudaFree(b->d_slot_row);
+  cudaFree(b->d_row_slot);
+  cudaFree(b->d_rmask);
+  cudaFree(b->d_rmin);
+  cudaFree(b->d_rmax);
+  for (auto &d : b->diag) cudaFree(d.d_diag);
   delete b;
+  return QG_OK;
+}
+
+qg_status qg_basis_set_windows(qg_basis b, int nres, const uint64_t *mask_host, const int32_t *min_host,
+                               const int32_t *max_host) {
+  qg_context ctx = b->ctx;
+  cudaFree(b->d_rmask);
+  cudaFree(b->d_rmin);
+  cudaFree(b->d_rmax);
+  b->d_rmask = nullptr;
+  b->d_rmin = b->d_rmax = nullptr;
+  b->nres = 0;
+  if (nres <= 0) return QG_OK;
+  QG_CUDA(ctx, cudaMalloc(&b->d_rmask, (size_t)nres * b->W * 8));
+  QG_CUDA(ctx, cudaMalloc(&b->d_rmin, nres * 4));
+  QG_CUDA(ctx, cudaMalloc(&b->d_rmax, nres * 4));
+  QG_CUDA(ctx, cudaMemcpy(b->d_rmask, mask_host, (size_t)nres * b->W * 8, cudaMemcpyHostToDevice));
+  QG_CUDA(ctx, cudaMemcpy(b->d_rmin, min_host, nres * 4, cudaMemcpyHostToDevice));
+  QG_CUDA(ctx, cudaMemcpy(b->d_rmax, max_host, nres * 4, cudaMemcpyHostToDevice));
+  b->nres = nres;
   return QG_OK;
 }
 
@@ -349,11 +380,11 @@ extern "C" qg_status qg_basis_get_dets(qg_basis b, uint8_t *dets_host) {
 }
 
 template <int W>
-__global__ void k_find(const Slot<W> *slots, uint64_t hmask, const Key<W> *q, int64_t n, int64_t *out,
-                       unsigned int *err) {
+__global__ void k_find(const Slot *slots, const uint32_t *slot_row, uint64_t hmask, const Key<W> *q, int64_t n,
+                       int64_t *out, unsigned int *err) {
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
-  out[i] = qg_lookup<W>(slots, hmask, q[i], err);
+  out[i] = qg_lookup<W>(slots, slot_row, hmask, q[i], err);
 }
 
 extern "C" qg_status qg_basis_find(qg_basis b, int64_t n, const uint8_t *dets_host, int64_t *index_host) {
@@ -371,11 +402,11 @@ extern "C" qg_status qg_basis_find(qg_basis b, int64_t n, const uint8_t *dets_ho
   QG_CUDA(ctx, cudaMemcpyAsync(d_bytes, dets_host, n * nword, cudaMemcpyHostToDevice, s));
   if (b->W == 1) {
     k_bytes_to_keys<1><<<grid_for(n), 256, 0, s>>>(d_bytes, b->nf, nword, n, (Key<1> *)d_keys);
-    k_find<1><<<grid_for(n), 256, 0, s>>>((const Slot<1> *)b->d_slots, b->hcap - 1, (const Key<1> *)d_keys, n, d_out,
+    k_find<1><<<grid_for(n), 256, 0, s>>>(b->d_slots, b->d_slot_row, b->hcap - 1, (const Key<1> *)d_keys, n, d_out,
                                           ctx->d_err);
   } else {
     k_bytes_to_keys<2><<<grid_for(n), 256, 0, s>>>(d_bytes, b->nf, nword, n, (Key<2> *)d_keys);
-    k_find<2><<<grid_for(n), 256, 0, s>>>((const Slot<2> *)b->d_slots, b->hcap - 1, (const Key<2> *)d_keys, n, d_out,
+    k_find<2><<<grid_for(n), 256, 0, s>>>(b->d_slots, b->d_slot_row, b->hcap - 1, (const Key<2> *)d_keys, n, d_out,
                                           ctx->d_err);
   }
   ctx->launches += 2;
@@ -396,7 +427,7 @@ extern "C" qg_status qg_basis_find(qg_basis b, int64_t n, const uint8_t *dets_ho
 template <int W>
 __global__ void k_expand(const Key<W> *src, int64_t r0, int64_t r1, const GroupDev<W> *__restrict__ groups, int ngroups,
                          const TermDev<W> *__restrict__ terms, int nres, const uint64_t *__restrict__ rmask,
-                         const int32_t *__restrict__ rmin, const int32_t *__restrict__ rmax, Slot<W> *slots,
+                         const int32_t *__restrict__ rmin, const int32_t *__restrict__ rmax, Slot *slots,
                          uint64_t hmask, Key<W> *list, unsigned long long *count, unsigned long long limit,
                          unsigned int *err) {
   int64_t r = r0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -433,7 +464,8 @@ __global__ void k_expand(const Key<W> *src, int64_t r0, int64_t r1, const GroupD
         atomicOr(err, QG_DEVERR_TABLE_FULL);
         return;
       }
-      int ins = qg_set_insert<W>(slots, hmask, tg);
+      int64_t hs;
+      int ins = qg_set_insert<W>(slots, hmask, tg, &hs);
       if (ins < 0) {
         atomicOr(err, QG_DEVERR_PROBE);
         return;
@@ -451,10 +483,27 @@ __global__ void k_expand(const Key<W> *src, int64_t r0, int64_t r1, const GroupD
 }
 
 template <int W>
-__global__ void k_set_insert_list(Slot<W> *slots, uint64_t hmask, const Key<W> *list, int64_t n, unsigned int *err) {
+__global__ void k_count_outside(const Key<W> *keys, int64_t n, int nres, const uint64_t *rmask, const int32_t *rmin,
+                                const int32_t *rmax, unsigned long long *bad) {
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
-  if (qg_set_insert<W>(slots, hmask, list[i]) < 0) atomicOr(err, QG_DEVERR_PROBE);
+  Key<W> k = keys[i];
+  for (int q = 0; q < nres; q++) {
+    int c = 0;
+    for (int j = 0; j < W; j++) c += __popcll(k.w[j] & rmask[q * W + j]);
+    if (c < rmin[q] || c > rmax[q]) {
+      atomicAdd(bad, 1ull);
+      return;
+    }
+  }
+}
+
+template <int W>
+__global__ void k_set_insert_list(Slot *slots, uint64_t hmask, const Key<W> *list, int64_t n, unsigned int *err) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int64_t h;
+  if (qg_set_insert<W>(slots, hmask, list[i], &h) < 0) atomicOr(err, QG_DEVERR_PROBE);
 }
 
 namespace {
@@ -513,16 +562,16 @@ static qg_status grow_t(qg_context ctx, qg_operator op, const Key<W> *seed_keys,
   int64_t cap = 1 << 20;
   while (cap < 4 * (n_seed + 1)) cap <<= 1;
   Key<W> *list = nullptr;
-  Slot<W> *slots = nullptr;
+  Slot *slots = nullptr;
   unsigned long long *d_count = nullptr;
   qg_status st = QG_OK;
   cudaError_t e = cudaMalloc(&d_count, 8);
   auto alloc_table = [&](int64_t c) -> cudaError_t {
     cudaFree(slots);
     slots = nullptr;
-    cudaError_t ee = cudaMalloc(&slots, 2 * c * sizeof(Slot<W>));
+    cudaError_t ee = cudaMalloc(&slots, 2 * c * sizeof(Slot));
     if (ee != cudaSuccess) return ee;
-    k_slots_clear<W><<<grid_for(2 * c), 256, 0, s>>>(slots, 2 * c);
+    k_slots_clear<<<grid_for(2 * c), 256, 0, s>>>(slots, nullptr, 2 * c);
     ctx->launches++;
     return cudaGetLastError();
   };
@@ -598,6 +647,27 @@ static qg_status grow_t(qg_context ctx, qg_operator op, const Key<W> *seed_keys,
   }
   if (e != cudaSuccess && st == QG_OK) st = qg_cuda_fail(ctx, e, "basis growth");
   if (st == QG_OK) st = qg_basis_from_device_keys(ctx, op->nf, W, list, (int64_t)count, out, nullptr);
+  // the grown basis satisfies the windows when its seeds do (targets are filtered): record
+  // them so H*psi skips sources that cannot be in it
+  if (st == QG_OK && R.n) {
+    bool seeds_ok = true;
+    if (include_seed && n_seed) {
+      unsigned long long *d_bad = nullptr;
+      unsigned long long bad = 0;
+      if (cudaMalloc(&d_bad, 8) == cudaSuccess) {
+        cudaMemsetAsync(d_bad, 0, 8, s);
+        k_count_outside<W><<<grid_for(n_seed), 256, 0, s>>>(seed_keys, n_seed, R.n, d_rmask, d_rmin, d_rmax, d_bad);
+        ctx->launches++;
+        cudaMemcpyAsync(&bad, d_bad, 8, cudaMemcpyDeviceToHost, s);
+        cudaStreamSynchronize(s);
+        cudaFree(d_bad);
+        seeds_ok = (bad == 0);
+      } else {
+        seeds_ok = false;
+      }
+    }
+    if (seeds_ok) st = qg_basis_set_windows(*out, R.n, R.mask.data(), R.mn.data(), R.mx.data());
+  }
   cudaStreamSynchronize(s);
   cudaFree(list);
   cudaFree(slots);
@@ -644,11 +714,11 @@ extern "C" qg_status qg_basis_union(qg_context ctx, qg_basis a, qg_basis b, qg_b
 }
 
 template <int W>
-__global__ void k_map(const Key<W> *dst_keys, int64_t n, const Slot<W> *src_slots, uint64_t hmask, const double2 *x,
-                      double2 *y, int nvec, unsigned int *err) {
+__global__ void k_map(const Key<W> *dst_keys, int64_t n, const Slot *src_slots, const uint32_t *src_slot_row,
+                      uint64_t hmask, const double2 *x, double2 *y, int nvec, unsigned int *err) {
   int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (r >= n) return;
-  int64_t j = qg_lookup<W>(src_slots, hmask, dst_keys[r], err);
+  int64_t j = qg_lookup<W>(src_slots, src_slot_row, hmask, dst_keys[r], err);
   for (int k = 0; k < nvec; k++) y[r * nvec + k] = (j >= 0) ? x[j * nvec + k] : make_double2(0.0, 0.0);
 }
 
@@ -657,12 +727,12 @@ extern "C" qg_status qg_basis_map(qg_context ctx, qg_basis src, const double *x_
   if (!ctx || !src || !dst || src->nf != dst->nf || nvec <= 0) return QG_ERR_ARG;
   if (!dst->n) return QG_OK;
   if (src->W == 1)
-    k_map<1><<<grid_for(dst->n), 256, 0, ctx->stream>>>((const Key<1> *)dst->d_keys, dst->n, (const Slot<1> *)src->d_slots,
-                                                        src->hcap - 1, (const double2 *)x_dev, (double2 *)y_dev, nvec,
+    k_map<1><<<grid_for(dst->n), 256, 0, ctx->stream>>>((const Key<1> *)dst->d_keys, dst->n, src->d_slots,
+                                                        src->d_slot_row, src->hcap - 1, (const double2 *)x_dev, (double2 *)y_dev, nvec,
                                                         ctx->d_err);
   else
-    k_map<2><<<grid_for(dst->n), 256, 0, ctx->stream>>>((const Key<2> *)dst->d_keys, dst->n, (const Slot<2> *)src->d_slots,
-                                                        src->hcap - 1, (const double2 *)x_dev, (double2 *)y_dev, nvec,
+    k_map<2><<<grid_for(dst->n), 256, 0, ctx->stream>>>((const Key<2> *)dst->d_keys, dst->n, src->d_slots,
+                                                        src->d_slot_row, src->hcap - 1, (const double2 *)x_dev, (double2 *)y_dev, nvec,
                                                         ctx->d_err);
   ctx->launches++;
   return qg_check_launch(ctx, "qg_basis_map");

@@ -31,36 +31,46 @@
 #define QG_DEVERR_PROBE 1u      // a hash probe exceeded QG_PROBE_LIMIT
 #define QG_DEVERR_TABLE_FULL 2u // an insert found the table over its load limit
 #define QG_DEVERR_OVERFLOW 4u   // an output list overflowed its capacity
+#define QG_DEVERR_TIMEOUT 8u    // a bounded wait on an asynchronous copy gave up
 
 template <int W>
 struct __align__(8 * W) Key {
   uint64_t w[W];
 };
 
-// Per-term masks for W words and the signed value.
+// Per-term masks for W words and the signed value, padded to a multiple of 16 bytes so a
+// table can be moved with one bulk copy.
 template <int W>
-struct TermDev {
+struct __align__(16) TermDev {
   uint64_t need0[W];
   uint64_t flip[W];
   uint64_t sgn[W];
+  uint64_t pad[W == 1 ? 1 : 0];
+  double vre, vim;
+};
+template <>
+struct __align__(16) TermDev<2> {
+  uint64_t need0[2];
+  uint64_t flip[2];
+  uint64_t sgn[2];
   double vre, vim;
 };
 
-// Terms sharing one need1 mask; terms[begin, end).
+// Terms sharing one need1 mask; terms[begin, end).  32 bytes.
 template <int W>
-struct GroupDev {
-  uint64_t need1[W];
+struct __align__(16) GroupDev {
+  uint64_t need1[2];  // words >= W are zero
   int32_t begin, end;
   int32_t diag;  // all terms of the group have flip == 0
   int32_t pad;
 };
 
-// Hash slot: key + basis index.  W=1: 16 bytes, W=2: 32 bytes (one DRAM sector).
-template <int W>
-struct __align__(16 * W) Slot {
-  uint64_t k[W];
-  uint32_t idx;
-  uint32_t pad[2 * W - 1];
+// Hash slot, one 32-byte DRAM sector: the key and the current source amplitude (written by
+// the pack step that precedes an H*psi), so a connection costs one sector.  The row a slot
+// belongs to is kept in a separate array.  For W = 1 the second key word is zero.
+struct __align__(32) Slot {
+  uint64_t k[2];
+  double vre, vim;
 };
 
 struct qg_context_s {
@@ -79,10 +89,12 @@ struct qg_context_s {
   size_t io_bytes = 0;
 };
 
+// A term table in one device allocation: ngroups GroupDev followed by nterms TermDev.
 struct HostTable {
-  // device arrays
-  void *d_groups = nullptr;
-  void *d_terms = nullptr;
+  void *d_blob = nullptr;
+  void *d_groups = nullptr;  // = d_blob
+  void *d_terms = nullptr;   // = d_blob + ngroups * sizeof(GroupDev)
+  size_t bytes = 0;          // multiple of 16
   int ngroups = 0, nterms = 0;
 };
 
@@ -91,18 +103,34 @@ struct qg_operator_s {
   int nf = 0, W = 1;
   int nterms_in = 0, nterms = 0;
   int hermitian = 0;
-  HostTable pull;  // adjoint strings grouped by need1: rows gather their sources
-  HostTable push;  // forward strings grouped by need1: sources emit their targets
+  HostTable pull;      // adjoint action grouped by need1: rows gather their sources
+  HostTable pull_off;  // the same without diagonal terms (diagonal precomputed per basis)
+  HostTable diag;      // diagonal terms only (flip == 0)
+  HostTable push;      // forward action grouped by need1: sources emit their targets
   int max_len = 0;
+  uint64_t uid = 0;    // unique per operator, keys the per-basis diagonal cache
+};
+
+struct DiagCache {
+  uint64_t op_uid;
+  double *d_diag;  // complex per row
 };
 
 struct qg_basis_s {
   qg_context ctx = nullptr;
   int nf = 0, W = 1;
   int64_t n = 0;
-  void *d_keys = nullptr;   // Key<W>[n], sorted ascending
-  void *d_slots = nullptr;  // Slot<W>[hcap]
-  int64_t hcap = 0;         // power of two, >= 2n
+  void *d_keys = nullptr;         // Key<W>[n], sorted ascending
+  Slot *d_slots = nullptr;        // [hcap]
+  uint32_t *d_slot_row = nullptr; // [hcap] row of the slot's key
+  uint32_t *d_row_slot = nullptr; // [n] slot of the row's key
+  int64_t hcap = 0;               // power of two, >= 2n
+  // occupation windows every determinant of the basis satisfies (the closure's
+  // restrictions): a source outside them cannot be in the basis, so no lookup is made
+  int nres = 0;
+  uint64_t *d_rmask = nullptr;    // [nres][W]
+  int32_t *d_rmin = nullptr, *d_rmax = nullptr;
+  std::vector<DiagCache> diag;
 };
 
 // ------------------------------------------------------------------ device helpers
@@ -141,31 +169,27 @@ __host__ __device__ inline bool qg_less(const Key<W> &a, const Key<W> &b) {
   return false;
 }
 
-// Look up a key; returns the basis index or -1.  Probes are bounded.
+// Find the slot of a key; returns the slot index or -1.  Probes are bounded.
 template <int W>
-__device__ __forceinline__ int64_t qg_lookup(const Slot<W> *__restrict__ slots, uint64_t hmask,
-                                             const Key<W> &k, unsigned int *err) {
+__device__ __forceinline__ int64_t qg_find_slot(const Slot *__restrict__ slots, uint64_t hmask, const Key<W> &k,
+                                                unsigned int *err) {
   uint64_t h = qg_hash<W>(k) & hmask;
   for (int p = 0; p < QG_PROBE_LIMIT; p++) {
-    const Slot<W> *s = slots + h;
-    Key<W> sk;
-    if (W == 1) {
-      ulonglong2 v = __ldg(reinterpret_cast<const ulonglong2 *>(s));
-      sk.w[0] = v.x;
-      if (sk.w[0] == k.w[0]) return (int64_t)(uint32_t)v.y;
-      if (sk.w[0] == QG_EMPTY_WORD) return -1;
-    } else {
-      ulonglong2 v = __ldg(reinterpret_cast<const ulonglong2 *>(s));
-      if (v.x == k.w[0] && v.y == k.w[1]) {
-        uint32_t idx = __ldg(reinterpret_cast<const uint32_t *>(s) + 4);
-        return (int64_t)idx;
-      }
-      if (v.x == QG_EMPTY_WORD && v.y == QG_EMPTY_WORD) return -1;
-    }
+    ulonglong2 v = __ldg(reinterpret_cast<const ulonglong2 *>(slots + h));
+    if (v.x == k.w[0] && (W == 1 || v.y == k.w[W - 1])) return (int64_t)h;
+    if (v.x == QG_EMPTY_WORD) return -1;
     h = (h + 1) & hmask;
   }
   atomicOr(err, QG_DEVERR_PROBE);
   return -1;
+}
+
+// Row of a key, or -1.
+template <int W>
+__device__ __forceinline__ int64_t qg_lookup(const Slot *__restrict__ slots, const uint32_t *__restrict__ slot_row,
+                                             uint64_t hmask, const Key<W> &k, unsigned int *err) {
+  int64_t h = qg_find_slot<W>(slots, hmask, k, err);
+  return h < 0 ? -1 : (int64_t)__ldg(slot_row + h);
 }
 
 template <int W>
@@ -202,26 +226,30 @@ inline int qg_words_for(int nf) { return nf / 64 + 1; }  // nf <= 63 -> 1, <= 12
 qg_status qg_basis_from_device_keys(qg_context ctx, int nf, int W, void *d_keys_unsorted, int64_t n,
                                     qg_basis *out, int64_t *d_perm /* optional, size n */);
 qg_status qg_basis_build_hash(qg_basis b);
+qg_status qg_basis_set_windows(qg_basis b, int nres, const uint64_t *mask_host, const int32_t *min_host,
+                               const int32_t *max_host);
+// diagonal of op on the basis (cached per operator), device pointer or nullptr on failure
+double *qg_basis_diag(qg_basis b, qg_operator op, qg_status *st);
 
 // Epilogue options for the fused Lanczos step (see qgpu_krylov.cu):
-//   src_scale:  x is used as x * src_scale[k] with entries |x*scale| <= thr[k] read as zero
-//               (normalisation and truncation of the Krylov vector folded into the gather);
-//   own_out:    row r of the scaled/truncated x written back (the stored Krylov vector);
 //   prev/beta:  y = H x - beta[k] * prev;
-//   dot:        per-block partial sums of conj(x_r) * (H x)_r written to dot_part.
+//   dot_part:   per-block partial sums of conj(x_r) * (H x)_r.
 struct ApplyFuse {
-  const double *src_scale = nullptr;  // [nvec]
-  const double *thr2 = nullptr;       // [nvec] squared truncation threshold, after scaling
-  double2 *own_out = nullptr;
   const double2 *prev = nullptr;
   const double *beta = nullptr;  // [nvec]
   double2 *dot_part = nullptr;   // [gridDim.x * nvec]
 };
 qg_status qg_apply_launch(qg_context ctx, qg_operator op, qg_basis dst, qg_basis src, const double *x, double *y,
                           int nvec, const ApplyFuse *fz);
-// x row stride xs, y row stride ys (complex entries), nvec columns from the given pointers
+// x row stride xs, y row stride ys (complex entries), nvec columns from the given pointers.
+// x_packed: for nvec == 1 the caller has already written x into the source basis' slots.
 qg_status qg_apply_strided(qg_context ctx, qg_operator op, qg_basis dst, qg_basis src, const double *x, int xs,
-                           double *y, int ys, int nvec, const ApplyFuse *fz);
+                           double *y, int ys, int nvec, const ApplyFuse *fz, bool x_packed = false);
+// write x (one column, stride xs) into the slots of basis b; with scale/thr2 (device, one
+// value each) the entries are scaled and truncated first and also stored to own_out
+qg_status qg_pack(qg_context ctx, qg_basis b, const double *x, int xs, const double *scale, const double *thr2,
+                  double *own_out);
+int qg_apply_grid(qg_basis dst);
 
 // reductions (qgpu_krylov.cu)
 qg_status qg_dot_dev(qg_context ctx, int64_t n, int nvec, const double *x, const double *y, double *out_dev);

@@ -246,6 +246,20 @@ __global__ void k_fin_b(const double2 *part, int nblk, int nvec, double *b_now, 
   }
 }
 
+// v_out = truncate(v_in * scale) per vector (the reference keeps |a|^2 > (eps/err)^2)
+__global__ void k_scale_trunc(int64_t n, int nvec, const double2 *__restrict__ vin, const double *__restrict__ scale,
+                              const double *__restrict__ thr2, double2 *__restrict__ vout) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n * nvec) return;
+  int k = (int)(i % nvec);
+  double2 v = vin[i];
+  double sc = scale[k];
+  v.x *= sc;
+  v.y *= sc;
+  if (!(v.x * v.x + v.y * v.y > thr2[k])) v = make_double2(0.0, 0.0);
+  vout[i] = v;
+}
+
 __global__ void k_zero(double *p, int64_t n) {
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i < n) p[i] = 0.0;
@@ -267,8 +281,7 @@ extern "C" qg_status qg_lanczos_tridiag(qg_context ctx, qg_operator op, qg_basis
   int64_t n = b->n;
   int64_t len = n * nvec;  // complex entries per block vector
   int P = partial_blocks(ctx, n);
-  int Papply = (int)((n + 255) / 256);
-  if (Papply < 1) Papply = 1;
+  int Papply = qg_apply_grid(b);
   // device state
   double2 *vp = nullptr, *vc = nullptr, *w = nullptr, *w2 = nullptr, *vraw = nullptr, *zero = nullptr;
   double2 *npart = nullptr, *dpart = nullptr;
@@ -301,18 +314,25 @@ extern "C" qg_status qg_lanczos_tridiag(qg_context ctx, qg_operator op, qg_basis
   k_zero<<<(unsigned)((nscal + 255) / 256), 256, 0, s>>>(scal, (int64_t)nscal);
   cudaMemsetAsync(zero, 0, vb, s);
   ctx->launches++;
+  // the normalised, truncated Krylov vector vc from a raw vector: for one vector the same
+  // kernel also writes it into the basis' hash slots for the gather
+  auto normalise = [&](const double2 *raw) -> qg_status {
+    if (nvec == 1) return qg_pack(ctx, b, (const double *)raw, 1, scale, thr2, (double *)vc);
+    k_scale_trunc<<<(unsigned)((len + 255) / 256), 256, 0, s>>>(n, nvec, raw, scale, thr2, vc);
+    ctx->launches++;
+    return qg_check_launch(ctx, "scale");
+  };
   // step 0: b0 = |v0|, scale, threshold eps (err = 1)
   k_dot_partial<<<P, RBLK, (RBLK / 32) * sizeof(double2), s>>>(n, nvec, (const double2 *)v0_dev, nullptr, npart);
   k_fin_b<<<1, 256, 0, s>>>(npart, P, nvec, b_now, b_hist, ntri, 0, scale, thr2, err, eps, gamma, 1);
   ctx->launches += 2;
   ApplyFuse fz;
-  fz.src_scale = scale;
-  fz.thr2 = thr2;
-  fz.own_out = vc;
   fz.prev = zero;
   fz.beta = zb;
   fz.dot_part = dpart;
-  st = qg_apply_launch(ctx, op, b, b, v0_dev, (double *)w, nvec, &fz);
+  st = normalise((const double2 *)v0_dev);
+  if (st == QG_OK)
+    st = qg_apply_strided(ctx, op, b, b, (const double *)vc, nvec, (double *)w, nvec, nvec, &fz, nvec == 1);
   if (st == QG_OK && krylov_dev)
     e = cudaMemcpyAsync(krylov_dev, vc, len * 16, cudaMemcpyDeviceToDevice, s);
   if (st == QG_OK) {
@@ -324,10 +344,11 @@ extern "C" qg_status qg_lanczos_tridiag(qg_context ctx, qg_operator op, qg_basis
     k_lanczos_axpy_norm<<<P, RBLK, (RBLK / 32) * sizeof(double2), s>>>(n, nvec, w, vp, a_now, vraw, npart);
     k_fin_b<<<1, 256, 0, s>>>(npart, P, nvec, b_now, b_hist, ntri, i, scale, thr2, err, eps, gamma, 0);
     ctx->launches += 2;
-    fz.own_out = vc;
+    st = normalise(vraw);
+    if (st != QG_OK) break;
     fz.prev = vp;
     fz.beta = b_now;
-    st = qg_apply_launch(ctx, op, b, b, (const double *)vraw, (double *)w2, nvec, &fz);
+    st = qg_apply_strided(ctx, op, b, b, (const double *)vc, nvec, (double *)w2, nvec, nvec, &fz, nvec == 1);
     std::swap(w, w2);
     if (st == QG_OK && krylov_dev)
       e = cudaMemcpyAsync(krylov_dev + 2 * (size_t)i * len, vc, len * 16, cudaMemcpyDeviceToDevice, s);

@@ -109,7 +109,7 @@ struct Entry {
 
 template <int W>
 void build_table(qg_context ctx, const std::vector<Entry> &terms, HostTable &tab, qg_status &st) {
-  // group by need1
+  // group by need1; inside a group diagonal terms first
   std::map<std::vector<uint64_t>, std::vector<int>> groups;
   for (int t = 0; t < (int)terms.size(); t++) {
     std::vector<uint64_t> key(terms[t].m.n1, terms[t].m.n1 + W);
@@ -123,7 +123,6 @@ void build_table(qg_context ctx, const std::vector<Entry> &terms, HostTable &tab
     for (int i = 0; i < W; i++) gd.need1[i] = kv.first[i];
     gd.begin = (int)tt.size();
     gd.diag = 1;
-    // diagonal terms first inside a group
     std::vector<int> idx = kv.second;
     std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) {
       bool da = true, db = true;
@@ -153,16 +152,19 @@ void build_table(qg_context ctx, const std::vector<Entry> &terms, HostTable &tab
   }
   tab.ngroups = (int)g.size();
   tab.nterms = (int)tt.size();
-  size_t gb = std::max<size_t>(1, g.size()) * sizeof(GroupDev<W>);
-  size_t tb = std::max<size_t>(1, tt.size()) * sizeof(TermDev<W>);
-  cudaError_t e = cudaMalloc(&tab.d_groups, gb);
-  if (e == cudaSuccess) e = cudaMalloc(&tab.d_terms, tb);
-  if (e == cudaSuccess && !g.empty())
-    e = cudaMemcpy(tab.d_groups, g.data(), g.size() * sizeof(GroupDev<W>), cudaMemcpyHostToDevice);
-  if (e == cudaSuccess && !tt.empty())
-    e = cudaMemcpy(tab.d_terms, tt.data(), tt.size() * sizeof(TermDev<W>), cudaMemcpyHostToDevice);
+  size_t gb = g.size() * sizeof(GroupDev<W>), tb = tt.size() * sizeof(TermDev<W>);
+  tab.bytes = gb + tb;
+  std::vector<unsigned char> blob(std::max<size_t>(tab.bytes, 16), 0);
+  if (gb) std::memcpy(blob.data(), g.data(), gb);
+  if (tb) std::memcpy(blob.data() + gb, tt.data(), tb);
+  cudaError_t e = cudaMalloc(&tab.d_blob, blob.size());
+  if (e == cudaSuccess) e = cudaMemcpy(tab.d_blob, blob.data(), blob.size(), cudaMemcpyHostToDevice);
+  tab.d_groups = tab.d_blob;
+  tab.d_terms = (unsigned char *)tab.d_blob + gb;
   st = (e == cudaSuccess) ? QG_OK : qg_cuda_fail(ctx, e, "operator table upload");
 }
+
+bool is_diag(const Entry &e) { return e.m.fl[0] == 0 && e.m.fl[1] == 0; }
 
 }  // namespace
 
@@ -238,12 +240,20 @@ extern "C" qg_status qg_operator_create(qg_context ctx, int32_t nf, int32_t nter
   op->nterms = (int)fwd.size();
   op->hermitian = herm;
   op->max_len = maxlen;
+  static uint64_t next_uid = 1;
+  op->uid = next_uid++;
+  std::vector<Entry> pull_off, diag;
+  for (auto &e : pull) (is_diag(e) ? diag : pull_off).push_back(e);
   qg_status st = QG_OK;
   if (op->W == 1) {
     build_table<1>(ctx, pull, op->pull, st);
+    if (st == QG_OK) build_table<1>(ctx, pull_off, op->pull_off, st);
+    if (st == QG_OK) build_table<1>(ctx, diag, op->diag, st);
     if (st == QG_OK) build_table<1>(ctx, fwd, op->push, st);
   } else {
     build_table<2>(ctx, pull, op->pull, st);
+    if (st == QG_OK) build_table<2>(ctx, pull_off, op->pull_off, st);
+    if (st == QG_OK) build_table<2>(ctx, diag, op->diag, st);
     if (st == QG_OK) build_table<2>(ctx, fwd, op->push, st);
   }
   if (st != QG_OK) {
@@ -256,10 +266,10 @@ extern "C" qg_status qg_operator_create(qg_context ctx, int32_t nf, int32_t nter
 
 extern "C" qg_status qg_operator_destroy(qg_operator op) {
   if (!op) return QG_OK;
-  cudaFree(op->pull.d_groups);
-  cudaFree(op->pull.d_terms);
-  cudaFree(op->push.d_groups);
-  cudaFree(op->push.d_terms);
+  cudaFree(op->pull.d_blob);
+  cudaFree(op->pull_off.d_blob);
+  cudaFree(op->diag.d_blob);
+  cudaFree(op->push.d_blob);
   delete op;
   return QG_OK;
 }

@@ -55,6 +55,7 @@ def load(path=LIB_PATH):
         "qg_apply": (C.c_int, [P, P, P, P, P, P, I32]),
         "qg_apply_host": (C.c_int, [P, P, P, P, P, P, I32]),
         "qg_count_nnz": (C.c_int, [P, P, P, P]),
+        "qg_count_nnz_offdiag": (C.c_int, [P, P, P, P]),
         "qg_expectation": (C.c_int, [P, P, P, P, I32, P]),
         "qg_dot": (C.c_int, [P, I64, I32, P, P, P]),
         "qg_norm": (C.c_int, [P, I64, I32, P, P]),
