@@ -194,6 +194,38 @@ qg_status qg_block_groundstate(qg_context ctx, qg_operator op, qg_basis basis, i
                                double *x_dev, double *energies_host, double tol, int32_t max_krylov,
                                int32_t max_restarts, int32_t *iterations);
 
+/* Lanczos that keeps its Krylov vectors, with the reference's full modified Gram-Schmidt
+ * reorthogonalisation and orthogonality test (LanczosTriDiagonalizeKrylovCC,
+ * Core/Lanczos.cpp:3705-3858).  One start vector; krylov_dev receives ntri * n complex values
+ * (vector-major); a_host ntri+1, b_host ntri. */
+qg_status qg_lanczos_krylov(qg_context ctx, qg_operator op, qg_basis basis, const double *v0_dev, int32_t ntri,
+                            double eps, double *a_host, double *b_host, double *krylov_dev);
+
+/* Settings of a resonant spectrum (ConvergenceSettingsType fields NTri1, NTri2, epsilon,
+ * Emin1..Gamma2, restrictions1/2, Core/StructDef.cpp:252; energies E0_1/E0_2).  Emin/Emax set
+ * to +-DBL_MAX and Gamma to 0 are resolved as the reference does and written back; NE1 and NE2
+ * must be given (> 0). */
+typedef struct {
+  int32_t ntri1, ntri2;
+  double epsilon;
+  double emin1, emax1;
+  int32_t ne1;
+  double gamma1;
+  double emin2, emax2;
+  int32_t ne2;
+  double gamma2;
+  double energy1, energy2; /* DBL_MAX: <psi|H|psi> / <psi|psi> */
+  const qg_restrictions *res1, *res2;
+} qg_rixs_settings;
+
+/* <psi|T1^dag G1^dag T2^dag G2 T2 G1 T1|psi> (ResonantSpectra, Core/ResonantSpectra.cpp:6):
+ * Krylov-projected G1 = 1/(w1 + E1 - H1 + i Gamma1/2) on T1|psi>, then for every incident
+ * energy and every T2 a Lanczos of H2 and the continued fraction.  g_host receives
+ * nt2 * (ne1+1) spectra of ne2+1 complex points, spectrum i*(ne1+1) + p. */
+qg_status qg_resonant_spectra(qg_context ctx, qg_operator H1, qg_operator H2, qg_operator T1,
+                              const qg_operator *T2, int32_t nt2, qg_basis psi_basis, const double *psi_dev,
+                              qg_rixs_settings *settings, double *g_host);
+
 #ifdef __cplusplus
 }
 #endif

@@ -45,6 +45,7 @@ def lib():
         L.qo_count_nnz.argtypes = [I, P, P, P, P, I64, I64]
         L.qo_lanczos_tridiag.argtypes = [I, P, P, P, P, P, P, I, D, D, I, P, P, P, P, P]
         L.qo_cf_spectrum.argtypes = [I, P, P, D, D, D, I, D, P, P]
+        L.qo_lanczos_krylov.argtypes = [I, P, P, P, P, P, P, I, D, I, P, P, P, P, P, P]
         L.qo_ladder.restype = I
         L.qo_ladder.argtypes = [P, P, I]
         L.qo_num_threads.restype = I
@@ -187,6 +188,75 @@ def lanczos_tridiag(op, psi, ntri, eps, gamma, restrictions=None):
     lib().qo_lanczos_tridiag(*op.args(), h, ntri, eps, gamma, *r.args(), _p(a), _p(b))
     lib().qo_wf_free(h)
     return a, b
+
+
+def lanczos_krylov(op, psi, ntri, eps, restrictions=None):
+    """Reference LanczosTriDiagonalizeKrylov (full reorthogonalisation, keeps the vectors):
+    returns a (ntri+1), b (ntri) and the list of Krylov vectors (WF)."""
+    r = Restr(psi.nf, restrictions)
+    a = np.zeros(ntri + 1)
+    b = np.zeros(ntri)
+    handles = (C.c_void_p * ntri)()
+    h = psi.handle()
+    lib().qo_lanczos_krylov(*op.args(), h, ntri, eps, *r.args(), _p(a), _p(b), C.cast(handles, C.c_void_p))
+    lib().qo_wf_free(h)
+    K = [WF.from_handle(psi.nf, handles[i]) for i in range(ntri)]
+    return a, b, K
+
+
+def expectation(op, psi):
+    """<psi|O|psi> with the growing-basis H*psi and the hashed dot (PsiOperatorPsi)."""
+    d = operator_psi(op, psi).as_dict()
+    return complex(sum(np.conj(v) * d.get(bytes(r), 0.0) for r, v in zip(psi.det, psi.val)))
+
+
+def linear_combination(nf, vecs, coef):
+    """sum_i coef_i vecs_i on the union basis (WaveFunctionAddComplexMultipliedUnionBasis)."""
+    acc = {}
+    order = []
+    for v, c in zip(vecs, coef):
+        for r, x in zip(v.det, v.val):
+            k = bytes(r)
+            if k not in acc:
+                acc[k] = 0j
+                order.append(r)
+            acc[k] += c * x
+    if not order:
+        return WF(nf, np.zeros((0, nword(nf)), np.uint8), [])
+    return WF(nf, np.array(order), [acc[bytes(r)] for r in order])
+
+
+def resonant_spectra(H1, H2, T1, T2s, psi, o):
+    """Reference ResonantSpectra (Core/ResonantSpectra.cpp:6-283): Krylov-projected resolvent of
+    H1 on T1|psi>, then for every incident energy and every T2 a Lanczos of H2.  o holds
+    NTri1, NTri2, Epsilon, Emin1, Emax1, NE1, Gamma1, Emin2, Emax2, NE2, Gamma2,
+    Restrictions1/2.  Returns (G [NT2*(NE1+1), NE2+1], emin2, emax2, gamma2); spectrum index
+    i*(NE1+1) + p."""
+    eps = o["Epsilon"]
+    n2 = float(np.real(np.vdot(psi.val, psi.val)))
+    e1 = expectation(H1, psi).real / (n2 if n2 > np.finfo(float).eps else 1.0)
+    e2 = expectation(H2, psi).real / (n2 if n2 > np.finfo(float).eps else 1.0)
+    Tpsi = operator_psi(T1, psi, o.get("Restrictions1"))
+    N1 = o["NTri1"]
+    a, b, K = lanczos_krylov(H1, Tpsi, N1, eps, o.get("Restrictions1"))
+    M = np.diag(a[1:N1 + 1]) + np.diag(b[1:N1], 1) + np.diag(b[1:N1], -1)
+    ev, Z = np.linalg.eigh(M)
+    emin1, emax1, ne1, g1 = o["Emin1"], o["Emax1"], o["NE1"], o["Gamma1"]
+    res = []
+    for p in range(ne1 + 1):
+        w = emin1 + (emax1 - emin1) * p / ne1 + e1
+        inv = 1.0 / (w - ev + 0.5j * g1)
+        c = b[0] * (Z * (inv * Z[0, :])[None, :]).sum(axis=1)
+        res.append(linear_combination(psi.nf, K, c))
+    tri = []
+    for T2 in T2s:
+        for p in range(ne1 + 1):
+            TG = operator_psi(T2, res[p], o.get("Restrictions2"))
+            tri.append(lanczos_tridiag(H2, TG, o["NTri2"], eps, np.sqrt(np.finfo(float).eps) + o["Gamma2"],
+                                       o.get("Restrictions2")))
+    emin2, emax2, ne2, g2 = o["Emin2"], o["Emax2"], o["NE2"], o["Gamma2"]
+    G = np.array([cf_spectrum(a2, b2, e2, emin2, (emax2 - emin2) / ne2, ne2, g2) for a2, b2 in tri])
+    return G
 
 
 def cf_spectrum(a, b, e0, emin, de, ne, gamma):

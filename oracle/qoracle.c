@@ -507,3 +507,57 @@ uint8_t *qo_enumerate(int nf, int nel, int nres, const uint8_t *masks, const int
 }
 
 void qo_free(void *p) { free(p); }
+
+/* ------------------------------------------------------------------ Krylov-basis Lanczos */
+
+/* Lanczos that keeps its Krylov vectors (LanczosTriDiagonalizeKrylovCC and the restricted
+ * variant, Core/Lanczos.cpp:3705-3858): every new vector H K_{i-1} is orthogonalised against
+ * all earlier ones by modified Gram-Schmidt in reverse order (a_i from the overlap with
+ * K_{i-1}), normalised (zeroed when b_i < 100*DBL_MIN), zeroed when the summed squared
+ * overlaps after normalisation exceed eps, and truncated at eps/err with
+ * err *= b^2/(b^2 + DBL_MIN + DBL_EPSILON a^2).  a[ntri] = <K_{ntri-1}|H|K_{ntri-1}>.
+ * K receives ntri handles (caller frees them). */
+void qo_lanczos_krylov(int nterms, const int *len, const int64_t *off, const uint16_t *ops, const double *vre,
+                       const double *vim, const qo_wf *psi, int ntri, double eps, int nres, const uint8_t *masks,
+                       const int *mn, const int *mx, double *a, double *b, qo_wf **K)
+{
+  double err = 1.0;
+  int i, j;
+  K[0] = qo_wf_copy(psi);
+  a[0] = 0;
+  b[0] = qo_norm(K[0]);
+  qo_scale(K[0], b[0] < 100 * DBL_MIN ? 0.0 : 1.0 / b[0]);
+  qo_truncate(K[0], eps / err);
+  for (i = 1; i < ntri; i++) {
+    double temp = 0;
+    K[i] = qo_operator_psi(nterms, len, off, ops, vre, vim, K[i - 1], nres, masks, mn, mx);
+    for (j = i; j > 0;) {
+      double dr, di;
+      j--;
+      qo_dot(K[j], K[i], &dr, &di);
+      if (j == i - 1) a[i] = dr;
+      qo_axpy_union(K[i], K[j], -dr, -di);
+    }
+    b[i] = qo_norm(K[i]);
+    qo_scale(K[i], b[i] < 100 * DBL_MIN ? 0.0 : 1.0 / b[i]);
+    for (j = i; j > 0;) {
+      double dr, di;
+      j--;
+      qo_dot(K[j], K[i], &dr, &di);
+      temp += dr * dr + di * di;
+      if (temp > eps) {
+        qo_scale(K[i], 0.0);
+        break;
+      }
+    }
+    err *= b[i] * b[i] / (b[i] * b[i] + DBL_MIN + DBL_EPSILON * a[i] * a[i]);
+    qo_truncate(K[i], eps / err);
+  }
+  {
+    qo_wf *hk = qo_operator_psi(nterms, len, off, ops, vre, vim, K[ntri - 1], nres, masks, mn, mx);
+    double dr, di;
+    qo_dot(K[ntri - 1], hk, &dr, &di);
+    a[ntri] = dr;
+    qo_wf_free(hk);
+  }
+}

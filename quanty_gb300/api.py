@@ -547,3 +547,40 @@ def Eigensystem(H, StartRestrictions, Npsi, options=None, eng=None, seed=12345):
     db = basis.dets_bytes()
     out = [Wavefunction(H.nf, db, X[:, k]) for k in range(Npsi)]
     return out, en
+
+
+# ----------------------------------------------------------------------------- RIXS
+
+def CreateResonantSpectra(H1, H2, T1, T2, psi, options=None, eng=None):
+    """Reference CreateResonantSpectra, sparse branch (LuaInterface/ssp.cpp:3090 ->
+    ResonantSpectra, Core/ResonantSpectra.cpp:6): returns (G [NT2*(NE1+1), NE2+1], settings)
+    with spectrum index iT2*(NE1+1) + p and the resolved energy ranges in settings."""
+    eng = eng or engine()
+    o = _opts(options)
+    T2s = T2 if isinstance(T2, (list, tuple)) else [T2]
+    big = np.finfo(float).max
+    st = qgpu.RixsSettings()
+    st.ntri1, st.ntri2 = int(o["NTri1"]), int(o["NTri2"])
+    st.epsilon = float(o["Epsilon"])
+    st.emin1 = float(o.get("Emin1", big)) if o.get("Emin1") is not None else big
+    st.emax1 = float(o.get("Emax1", -big)) if o.get("Emax1") is not None else -big
+    st.ne1 = int(o.get("NE1", 1000))
+    st.gamma1 = float(o.get("Gamma1", 0.0))
+    st.emin2 = float(o.get("Emin2", big)) if o.get("Emin2") is not None else big
+    st.emax2 = float(o.get("Emax2", -big)) if o.get("Emax2") is not None else -big
+    st.ne2 = int(o.get("NE2", 1000))
+    st.gamma2 = float(o.get("Gamma2", 0.0))
+    st.energy1 = float(o["E0_1"]) if o.get("E0_1") is not None else big
+    st.energy2 = float(o["E0_2"]) if o.get("E0_2") is not None else big
+    r1 = _Res(H1.nf, parse_restrictions(o.get("Restrictions1")))
+    r2 = _Res(H1.nf, parse_restrictions(o.get("Restrictions2")))
+    st.res1 = C.cast(C.pointer(r1.r), C.c_void_p) if r1.r.n else None
+    st.res2 = C.cast(C.pointer(r2.r), C.c_void_p) if r2.r.n else None
+    b, perm = Basis.from_bytes(psi.nf, psi.det, eng)
+    x = _upload(eng, b, perm, psi.val)
+    t2h = (C.c_void_p * len(T2s))(*[t.handle(eng) for t in T2s])
+    g = np.zeros(2 * len(T2s) * (st.ne1 + 1) * (st.ne2 + 1))
+    eng.check(eng.L.qg_resonant_spectra(eng.ctx, H1.handle(eng), H2.handle(eng), T1.handle(eng),
+                                        C.cast(t2h, C.c_void_p), len(T2s), b.h, _ptr(x), C.byref(st), _ptr(g)))
+    G = (g[0::2] + 1j * g[1::2]).reshape(len(T2s) * (st.ne1 + 1), st.ne2 + 1)
+    return G, {k: getattr(st, k) for k, _ in st._fields_ if not k.startswith("res")}

@@ -197,6 +197,11 @@ void jacobi_eigh(int k, std::vector<cd> A, std::vector<double> &w, std::vector<c
 
 }  // namespace
 
+void qg_host_eigh(int k, const std::vector<std::complex<double>> &A, std::vector<double> &w,
+                  std::vector<std::complex<double>> &V) {
+  jacobi_eigh(k, A, w, V);
+}
+
 extern "C" qg_status qg_block_groundstate(qg_context ctx, qg_operator op, qg_basis b, int32_t p, double *x_dev,
                                           double *energies_host, double tol, int32_t max_krylov,
                                           int32_t max_restarts, int32_t *iterations) {
@@ -332,7 +337,6 @@ extern "C" qg_status qg_block_groundstate(qg_context ctx, qg_operator op, qg_bas
       }
     }
     if (st != QG_OK) break;
-    (void)invariant;
     // projected matrix: Hermitian part of the k x k leading block
     std::vector<cd> M((size_t)k * k);
     for (int i = 0; i < k; i++)

@@ -251,5 +251,12 @@ qg_status qg_pack(qg_context ctx, qg_basis b, const double *x, int xs, const dou
                   double *own_out);
 int qg_apply_grid(qg_basis dst);
 
+// Hermitian eigenproblem of a small host matrix (row-major k x k): ascending values, columns of
+// V the eigenvectors (cyclic Jacobi, qgpu_eigen.cu)
+#include <complex>
+void qg_host_eigh(int k, const std::vector<std::complex<double>> &A, std::vector<double> &w,
+                  std::vector<std::complex<double>> &V);
+int qg_partial_blocks(qg_context ctx, int64_t n);
+
 // reductions (qgpu_krylov.cu)
 qg_status qg_dot_dev(qg_context ctx, int64_t n, int nvec, const double *x, const double *y, double *out_dev);

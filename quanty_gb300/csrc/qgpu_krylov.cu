@@ -20,7 +20,9 @@
 
 static const int RBLK = 256;
 
-static inline int partial_blocks(qg_context ctx, int64_t n) {
+int qg_partial_blocks(qg_context ctx, int64_t n);
+static inline int partial_blocks(qg_context ctx, int64_t n) { return qg_partial_blocks(ctx, n); }
+int qg_partial_blocks(qg_context ctx, int64_t n) {
   int64_t b = (n + RBLK - 1) / RBLK;
   int64_t cap = 4LL * ctx->num_sms;
   if (b > cap) b = cap;

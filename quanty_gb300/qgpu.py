@@ -63,6 +63,8 @@ def load(path=LIB_PATH):
         "qg_lanczos_tridiag": (C.c_int, [P, P, P, P, I32, I32, D, D, P, P, P]),
         "qg_cf_spectra": (C.c_int, [P, I32, I32, P, P, P, D, D, I32, D, P]),
         "qg_block_groundstate": (C.c_int, [P, P, P, I32, P, P, D, I32, I32, P]),
+        "qg_lanczos_krylov": (C.c_int, [P, P, P, P, I32, D, P, P, P]),
+        "qg_resonant_spectra": (C.c_int, [P, P, P, P, P, I32, P, P, P, P]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -81,3 +83,10 @@ def header_symbols(path=HEADER):
 
 class Restrictions(C.Structure):
     _fields_ = [("n", C.c_int32), ("masks", C.c_void_p), ("min", C.c_void_p), ("max", C.c_void_p)]
+
+
+class RixsSettings(C.Structure):
+    _fields_ = [("ntri1", C.c_int32), ("ntri2", C.c_int32), ("epsilon", C.c_double),
+                ("emin1", C.c_double), ("emax1", C.c_double), ("ne1", C.c_int32), ("gamma1", C.c_double),
+                ("emin2", C.c_double), ("emax2", C.c_double), ("ne2", C.c_int32), ("gamma2", C.c_double),
+                ("energy1", C.c_double), ("energy2", C.c_double), ("res1", C.c_void_p), ("res2", C.c_void_p)]

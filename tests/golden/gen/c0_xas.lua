@@ -56,4 +56,10 @@ io.put("dump", "Tyd")
 Sr = CreateResonantSpectra(HX, H, Tx, Tyd, psiList[1],
   {{"Emin1", -5}, {"Emax1", 15}, {"NE1", 4}, {"Gamma1", 0.8}, {"Emin2", -2}, {"Emax2", 8}, {"NE2", 256}, {"Gamma2", 0.3}, {"DenseBorder", 0}, {"Epsilon", 0}})
 Sr.Print({{"file", "dump/rixs.dat"}})
+-- the same at the default epsilon (the Krylov-basis Lanczos of the intermediate states zeroes
+-- a new vector whose squared overlaps with the earlier ones exceed epsilon, so epsilon 0
+-- keeps one Krylov vector)
+Sd = CreateResonantSpectra(HX, H, Tx, Tyd, psiList[1],
+  {{"Emin1", -5}, {"Emax1", 15}, {"NE1", 4}, {"Gamma1", 0.8}, {"Emin2", -2}, {"Emax2", 8}, {"NE2", 256}, {"Gamma2", 0.3}, {"DenseBorder", 0}})
+Sd.Print({{"file", "dump/rixs_default.dat"}})
 print("c0_xas done")

@@ -144,6 +144,7 @@ def gen_c0():
     out["rixs_opts"] = {"Emin1": -5, "Emax1": 15, "NE1": 4, "Gamma1": 0.8, "Emin2": -2, "Emax2": 8,
                         "NE2": 256, "Gamma2": 0.3, "Epsilon": 0}
     out["rixs"] = spectra(work, "rixs.dat")
+    out["rixs_default"] = spectra(work, "rixs_default.dat")
     save("c0_xas.json", out)
 
 

@@ -90,3 +90,18 @@ def test_lanczos_matches_oracle_coefficients(api, oracle_mod):
     ao, bo = O.lanczos_tridiag(O.Op(g["HX"]), O.WF(26, Tpsi.det, Tpsi.val), 40, 0.0, 0.5)
     assert np.allclose(a[:20], ao[:20], atol=1e-10)
     assert np.allclose(b[:20], bo[:20], atol=1e-10)
+
+
+@pytest.mark.parametrize("key,eps", [("rixs", 0.0), ("rixs_default", EPS_DEFAULT)])
+def test_rixs_matches_reference(api, key, eps):
+    """CreateResonantSpectra on the d8 case: all incident energies and final-state Lanczos runs
+    batched, against the reference's RIXS spectra (1e-8)."""
+    g = golden("c0_xas.json")
+    o = dict(g["rixs_opts"], Epsilon=eps, NTri1=100, NTri2=100)
+    G, st = api.CreateResonantSpectra(api.Operator.from_fixture(g["HX"]), api.Operator.from_fixture(g["H"]),
+                                      api.Operator.from_fixture(g["Tx"]), [api.Operator.from_fixture(g["Tyd"])],
+                                      api.Wavefunction.from_fixture(g["psi"][0]), o)
+    ref = g[key]
+    R = np.array(ref["re"]) + 1j * np.array(ref["im"])
+    assert G.shape == R.shape
+    assert spec_err(G, R) < SPEC_TOL, spec_err(G, R)

@@ -163,3 +163,17 @@ def _sector(O, g):
                 s[i] = "1"
         dets.append("".join(s))
     return O.WF(nf, O.dets_to_bytes(dets, nf), np.ones(len(dets)))
+
+
+@pytest.mark.parametrize("key,eps", [("rixs", 0.0), ("rixs_default", EPS_DEFAULT)])
+def test_rixs_matches_reference(oracle_mod, key, eps):
+    """CreateResonantSpectra (Core/ResonantSpectra.cpp:6): Krylov-projected intermediate-state
+    resolvent and per-incident-energy Lanczos, against the reference's spectra."""
+    O = oracle_mod
+    g = golden("c0_xas.json")
+    o = dict(g["rixs_opts"], Epsilon=eps, NTri1=100, NTri2=100)
+    G = O.resonant_spectra(O.Op(g["HX"]), O.Op(g["H"]), O.Op(g["Tx"]), [O.Op(g["Tyd"])],
+                           O.WF.from_fixture(g["psi"][0]), o)
+    ref = g[key]
+    R = np.array(ref["re"]) + 1j * np.array(ref["im"])
+    assert rel_err(G, R) < 1e-8
