@@ -20,7 +20,10 @@
 // warp-uniform.  The term table (groups + terms, one allocation) is staged into shared
 // memory with bulk asynchronous copies (cp.async.bulk, completion on an mbarrier with a
 // bounded wait) when it fits; otherwise it is read through the read-only cache.
+#include <cub/cub.cuh>
+
 #include <algorithm>
+#include <map>
 
 #include "qgpu_internal.cuh"
 
@@ -96,12 +99,65 @@ __device__ __forceinline__ bool in_windows(const Key<W> &s, const SrcView &v) {
   return true;
 }
 
+// Local decomposition view (see OpBasisCache): rows of one local configuration form a block;
+// entry e of block b moves a row to block ent[e].tblock at the same offset when the blocks
+// list the same remaining (non-local) configurations, which a key comparison verifies.
+struct LocalView {
+  int on;
+  int lo;          // device bit of the lowest local orbital
+  uint32_t lmask;  // (1 << H) - 1
+  const int32_t *cfg;
+  const uint32_t *bstart, *eoff;
+  const LocalEntry *ent;
+};
+
+template <int W>
+__device__ __forceinline__ uint32_t get_local(const Key<W> &d, int lo, uint32_t lmask) {
+  if (W == 1) return (uint32_t)(d.w[0] >> lo) & lmask;
+  if (lo >= 64) return (uint32_t)(d.w[W - 1] >> (lo - 64)) & lmask;
+  uint64_t v = (d.w[0] >> lo) | (lo ? (d.w[W - 1] << (64 - lo)) : 0ull);
+  return (uint32_t)v & lmask;
+}
+
+template <int W>
+__device__ __forceinline__ Key<W> set_local(const Key<W> &d, int lo, uint32_t lmask, uint32_t c) {
+  Key<W> o = d;
+  if (W == 1) {
+    o.w[0] = (d.w[0] & ~((uint64_t)lmask << lo)) | ((uint64_t)c << lo);
+  } else if (lo >= 64) {
+    o.w[W - 1] = (d.w[W - 1] & ~((uint64_t)lmask << (lo - 64))) | ((uint64_t)c << (lo - 64));
+  } else {
+    o.w[0] = (d.w[0] & ~((uint64_t)lmask << lo)) | ((uint64_t)c << lo);
+    if (lo) o.w[W - 1] = (d.w[W - 1] & ~((uint64_t)lmask >> (64 - lo))) | ((uint64_t)c >> (64 - lo));
+  }
+  return o;
+}
+
+// Window bits of a row: bit 5q + (D + 2) is set when moving D in [-2, 2] electrons into window
+// q keeps it inside [min_q, max_q]; a source the row reaches by a term whose window changes
+// are D_q passes iff all its bits (the term's wreq) are set.
+template <int W>
+__device__ __forceinline__ uint64_t window_bits(const Key<W> &d, const SrcView &v) {
+  uint64_t ok = 0;
+  for (int q = 0; q < v.nres; q++) {
+    int c = 0;
+#pragma unroll
+    for (int i = 0; i < W; i++) c += __popcll(d.w[i] & __ldg(v.rmask + q * W + i));
+    int lo = __ldg(v.rmin + q), hi = __ldg(v.rmax + q);
+#pragma unroll
+    for (int D = -2; D <= 2; D++)
+      if (c + D >= lo && c + D <= hi) ok |= 1ull << (5 * q + D + 2);
+  }
+  return ok;
+}
+
 template <int W, int NV, bool FUSE, bool SMEM>
 __global__ void __launch_bounds__(256) k_apply(const Key<W> *__restrict__ rows, int64_t n_rows,
                                                const unsigned char *__restrict__ gtab, uint32_t tab_bytes,
                                                int ngroups, const double2 *__restrict__ diag, SrcView src,
                                                int packed, int same_basis, const double2 *__restrict__ x, int xs,
                                                double2 *__restrict__ y, int ys, int vec0, ApplyFuse fz,
+                                               LocalView lv, const uint64_t *__restrict__ wreq,
                                                unsigned int *err) {
   extern __shared__ __align__(128) unsigned char s_tab[];
   __shared__ __align__(8) unsigned long long s_bar;
@@ -125,6 +181,43 @@ __global__ void __launch_bounds__(256) k_apply(const Key<W> *__restrict__ rows, 
         double2 xv = x[r * xs + vec0 + k];
         acc[k].x = dg.x * xv.x - dg.y * xv.y;
         acc[k].y = dg.x * xv.y + dg.y * xv.x;
+      }
+    }
+    uint64_t okm = 0;
+    if (wreq && src.nres) okm = window_bits<W>(d, src);
+    if (lv.on) {
+      // local moves: targets in another block at the same offset (coalesced), else probed
+      int b = __ldg(lv.cfg + get_local<W>(d, lv.lo, lv.lmask));
+      uint32_t rs = __ldg(lv.bstart + b);
+      int64_t off = r - (int64_t)rs;
+      uint32_t e1 = __ldg(lv.eoff + b + 1);
+      for (uint32_t e = __ldg(lv.eoff + b); e < e1; e++) {
+        const LocalEntry *E = lv.ent + e;
+        uint32_t tbk = __ldg(&E->tblock);
+        Key<W> s = set_local<W>(d, lv.lo, lv.lmask, __ldg(&E->target));
+        int64_t j = (int64_t)__ldg(lv.bstart + tbk) + off;
+        int64_t h = -1;
+        bool hit = false;
+        if (j < (int64_t)__ldg(lv.bstart + tbk + 1)) {
+          Key<W> kj = rows[j];
+          hit = qg_eq<W>(kj, s);
+        }
+        if (!hit) {
+          if (src.nres) {
+            uint64_t req = __ldg(&E->wreq);
+            if (wreq ? ((okm & req) != req) : !in_windows<W>(s, src)) continue;
+          }
+          h = qg_find_slot<W>(src.slots, src.hmask, s, err);
+          if (h < 0) continue;
+          j = (int64_t)__ldg(src.slot_row + h);
+        }
+        double vr = __ldg(&E->vre), vi = __ldg(&E->vim);
+#pragma unroll
+        for (int k = 0; k < NV; k++) {
+          double2 xv = __ldg(x + j * xs + vec0 + k);
+          acc[k].x = fma(vr, xv.x, fma(-vi, xv.y, acc[k].x));
+          acc[k].y = fma(vr, xv.y, fma(vi, xv.x, acc[k].y));
+        }
       }
     }
     for (int g = 0; g < ngroups; g++) {
@@ -152,7 +245,14 @@ __global__ void __launch_bounds__(256) k_apply(const Key<W> *__restrict__ rows, 
         if (dg && same_basis) {
           j = r;
         } else {
-          if (src.nres && !in_windows<W>(s, src)) continue;
+          if (src.nres) {
+            if (wreq) {
+              uint64_t req = __ldg(wreq + t);
+              if ((okm & req) != req) continue;
+            } else if (!in_windows<W>(s, src)) {
+              continue;
+            }
+          }
           h = qg_find_slot<W>(src.slots, src.hmask, s, err);
           if (h < 0) continue;
           if (!(NV == 1 && packed)) j = (int64_t)__ldg(src.slot_row + h);
@@ -223,7 +323,8 @@ int qg_apply_grid(qg_basis dst) { return (int)std::max<int64_t>(1, (dst->n + 255
 
 template <int W, int NV, bool FUSE, bool SMEM>
 static void launch_apply_t(qg_context ctx, const HostTable &tab, const double2 *diag, qg_basis dst, qg_basis src,
-                           int packed, const double2 *x, int xs, double2 *y, int ys, int vec0, const ApplyFuse &fz) {
+                           int packed, const double2 *x, int xs, double2 *y, int ys, int vec0, const ApplyFuse &fz,
+                           const LocalView &lv, const uint64_t *wreq) {
   size_t smem = SMEM ? tab.bytes : 0;
   if (SMEM) {
     static bool attr_done = false;
@@ -236,27 +337,28 @@ static void launch_apply_t(qg_context ctx, const HostTable &tab, const double2 *
              src->d_rmax};
   k_apply<W, NV, FUSE, SMEM><<<qg_apply_grid(dst), 256, smem, ctx->stream>>>(
       (const Key<W> *)dst->d_keys, dst->n, (const unsigned char *)tab.d_blob, (uint32_t)tab.bytes, tab.ngroups, diag, sv,
-      packed, dst == src, x, xs, y, ys, vec0, fz, ctx->d_err);
+      packed, dst == src, x, xs, y, ys, vec0, fz, lv, wreq, ctx->d_err);
   ctx->launches++;
 }
 
 template <int W, bool FUSE, bool SMEM>
 static void launch_apply_w(qg_context ctx, const HostTable &tab, const double2 *diag, qg_basis dst, qg_basis src,
-                           int packed, const double2 *x, int xs, double2 *y, int ys, int nvec, const ApplyFuse &fz) {
+                           int packed, const double2 *x, int xs, double2 *y, int ys, int nvec, const ApplyFuse &fz,
+                           const LocalView &lv, const uint64_t *wreq) {
   int v = 0;
   while (v < nvec) {
     int left = nvec - v;
     if (left >= 8) {
-      launch_apply_t<W, 8, FUSE, SMEM>(ctx, tab, diag, dst, src, 0, x, xs, y, ys, v, fz);
+      launch_apply_t<W, 8, FUSE, SMEM>(ctx, tab, diag, dst, src, 0, x, xs, y, ys, v, fz, lv, wreq);
       v += 8;
     } else if (left >= 4) {
-      launch_apply_t<W, 4, FUSE, SMEM>(ctx, tab, diag, dst, src, 0, x, xs, y, ys, v, fz);
+      launch_apply_t<W, 4, FUSE, SMEM>(ctx, tab, diag, dst, src, 0, x, xs, y, ys, v, fz, lv, wreq);
       v += 4;
     } else if (left >= 2) {
-      launch_apply_t<W, 2, FUSE, SMEM>(ctx, tab, diag, dst, src, 0, x, xs, y, ys, v, fz);
+      launch_apply_t<W, 2, FUSE, SMEM>(ctx, tab, diag, dst, src, 0, x, xs, y, ys, v, fz, lv, wreq);
       v += 2;
     } else {
-      launch_apply_t<W, 1, FUSE, SMEM>(ctx, tab, diag, dst, src, packed, x, xs, y, ys, v, fz);
+      launch_apply_t<W, 1, FUSE, SMEM>(ctx, tab, diag, dst, src, packed, x, xs, y, ys, v, fz, lv, wreq);
       v += 1;
     }
   }
@@ -264,11 +366,12 @@ static void launch_apply_w(qg_context ctx, const HostTable &tab, const double2 *
 
 template <int W, bool FUSE>
 static void launch_apply_s(qg_context ctx, const HostTable &tab, const double2 *diag, qg_basis dst, qg_basis src,
-                           int packed, const double2 *x, int xs, double2 *y, int ys, int nvec, const ApplyFuse &fz) {
+                           int packed, const double2 *x, int xs, double2 *y, int ys, int nvec, const ApplyFuse &fz,
+                           const LocalView &lv, const uint64_t *wreq) {
   if (tab.bytes <= QG_SMEM_TABLE_MAX)
-    launch_apply_w<W, FUSE, true>(ctx, tab, diag, dst, src, packed, x, xs, y, ys, nvec, fz);
+    launch_apply_w<W, FUSE, true>(ctx, tab, diag, dst, src, packed, x, xs, y, ys, nvec, fz, lv, wreq);
   else
-    launch_apply_w<W, FUSE, false>(ctx, tab, diag, dst, src, packed, x, xs, y, ys, nvec, fz);
+    launch_apply_w<W, FUSE, false>(ctx, tab, diag, dst, src, packed, x, xs, y, ys, nvec, fz, lv, wreq);
 }
 
 // ------------------------------------------------------------------ pack
@@ -342,13 +445,200 @@ __global__ void k_diag(const Key<W> *__restrict__ rows, int64_t n, const GroupDe
   diag[r] = acc;
 }
 
-double *qg_basis_diag(qg_basis b, qg_operator op, qg_status *st) {
+template <int W>
+__global__ void k_local_cfg(const Key<W> *keys, int64_t n, int lo, uint32_t lmask, uint32_t *cfg, uint32_t *flag) {
+  int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  uint32_t c = get_local<W>(keys[r], lo, lmask);
+  cfg[r] = c;
+  flag[r] = (r == 0) ? 1u : (get_local<W>(keys[r - 1], lo, lmask) != c ? 1u : 0u);
+}
+
+__global__ void k_block_scatter(const uint32_t *cfg, const uint32_t *flag, const uint32_t *pos, int64_t n,
+                                uint32_t *bstart, uint32_t *bcfg) {
+  int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  if (flag[r]) {
+    bstart[pos[r] - 1] = (uint32_t)r;
+    bcfg[pos[r] - 1] = cfg[r];
+  }
+}
+
+void qg_cache_free(OpBasisCache &c) {
+  cudaFree(c.d_diag);
+  cudaFree(c.d_wreq);
+  cudaFree(c.d_bstart);
+  cudaFree(c.d_cfg);
+  cudaFree(c.d_eoff);
+  cudaFree(c.d_ent);
+  c = OpBasisCache();
+}
+
+namespace {
+
+inline int popc2(const uint64_t *a, const uint64_t *b, const uint64_t *c, int W) {
+  int n = 0;
+  for (int i = 0; i < W; i++) n += __builtin_popcountll(a[i] & b[i] & c[i]);
+  return n;
+}
+
+// window bits a move needs: D_q = (bits turned on) - (bits turned off) inside window q;
+// returns false when some |D_q| > 2 (the encoding cannot express it)
+bool move_bits(const qg_basis b, const uint64_t *on, const uint64_t *offb, uint64_t &req) {
+  req = 0;
+  uint64_t ones[2] = {~0ull, ~0ull};
+  for (int q = 0; q < b->nres; q++) {
+    const uint64_t *m = &b->h_rmask[(size_t)q * b->W];
+    int D = popc2(on, m, ones, b->W) - popc2(offb, m, ones, b->W);
+    if (D == 0) continue;
+    if (D < -2 || D > 2) return false;
+    req |= 1ull << (5 * q + D + 2);
+  }
+  return true;
+}
+
+// local-bit masks (bits lo.. of a W-word key) -> H-bit integer
+uint32_t to_local(const uint64_t *m, int lo, int W) {
+  if (W == 1) return (uint32_t)(m[0] >> lo);
+  if (lo >= 64) return (uint32_t)(m[1] >> (lo - 64));
+  return (uint32_t)((m[0] >> lo) | (lo ? (m[1] << (64 - lo)) : 0ull));
+}
+
+void from_local(uint32_t c, int lo, int W, uint64_t *out) {
+  out[0] = out[1] = 0;
+  if (W == 1) {
+    out[0] = (uint64_t)c << lo;
+  } else if (lo >= 64) {
+    out[1] = (uint64_t)c << (lo - 64);
+  } else {
+    out[0] = (uint64_t)c << lo;
+    if (lo) out[1] = (uint64_t)c >> (64 - lo);
+  }
+}
+
+}  // namespace
+
+static qg_status build_local(qg_basis bs, qg_operator op, OpBasisCache &c) {
+  qg_context ctx = bs->ctx;
+  cudaStream_t s = ctx->stream;
+  int64_t n = bs->n;
+  int H = op->H, lo = bs->nf - H, W = bs->W;
+  uint32_t lmask = (H >= 32) ? 0xFFFFFFFFu : ((1u << H) - 1);
+  uint32_t *cfg = nullptr, *flag = nullptr, *pos = nullptr, *bst = nullptr, *bcf = nullptr;
+  void *tmp = nullptr;
+  size_t tb = 0;
+  cudaError_t e = cudaMalloc(&cfg, n * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&flag, n * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&pos, n * 4);
+  if (e == cudaSuccess) e = cub::DeviceScan::InclusiveSum(nullptr, tb, flag, pos, (int)n, s);
+  if (e == cudaSuccess) e = cudaMalloc(&tmp, tb);
+  if (e == cudaSuccess) {
+    if (W == 1)
+      k_local_cfg<1><<<grid_for(n, 256), 256, 0, s>>>((const Key<1> *)bs->d_keys, n, lo, lmask, cfg, flag);
+    else
+      k_local_cfg<2><<<grid_for(n, 256), 256, 0, s>>>((const Key<2> *)bs->d_keys, n, lo, lmask, cfg, flag);
+    ctx->launches++;
+    e = cub::DeviceScan::InclusiveSum(tmp, tb, flag, pos, (int)n, s);
+    ctx->launches += 2;
+  }
+  uint32_t nb = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&nb, pos + n - 1, 4, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e == cudaSuccess) e = cudaMalloc(&bst, (size_t)(nb + 1) * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&bcf, (size_t)nb * 4 + 4);
+  if (e == cudaSuccess) {
+    k_block_scatter<<<grid_for(n, 256), 256, 0, s>>>(cfg, flag, pos, n, bst, bcf);
+    ctx->launches++;
+  }
+  std::vector<uint32_t> hstart(nb + 1), hcfg(nb);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(hstart.data(), bst, (size_t)nb * 4, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(hcfg.data(), bcf, (size_t)nb * 4, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  cudaFree(cfg);
+  cudaFree(flag);
+  cudaFree(pos);
+  cudaFree(tmp);
+  cudaFree(bcf);
+  if (e != cudaSuccess) {
+    cudaFree(bst);
+    return qg_cuda_fail(ctx, e, "local blocks");
+  }
+  hstart[nb] = (uint32_t)n;
+  // configuration -> block
+  std::vector<int32_t> table((size_t)1 << H, -1);
+  for (uint32_t k = 0; k < nb; k++) table[hcfg[k]] = (int32_t)k;
+  // local terms in H-bit form
+  struct LT {
+    uint32_t n1, n0, fl, sg;
+    double re, im;
+  };
+  std::vector<LT> lt;
+  for (auto &t : op->local_off)
+    lt.push_back({to_local(t.n1, lo, W), to_local(t.n0, lo, W), to_local(t.fl, lo, W), to_local(t.sg, lo, W), t.re,
+                  t.im});
+  std::vector<uint32_t> eoff(nb + 1, 0);
+  std::vector<LocalEntry> ent;
+  bool exact = true;
+  for (uint32_t k = 0; k < nb; k++) {
+    uint32_t cc = hcfg[k];
+    std::map<uint32_t, std::pair<double, double>> acc;
+    for (auto &t : lt) {
+      if ((cc & t.n1) != t.n1 || (cc & t.n0)) continue;
+      uint32_t tg = cc ^ t.fl;
+      double sg = (__builtin_popcount(cc & t.sg) & 1) ? -1.0 : 1.0;
+      auto &v = acc[tg];
+      v.first += sg * t.re;
+      v.second += sg * t.im;
+    }
+    eoff[k] = (uint32_t)ent.size();
+    for (auto &kv : acc) {
+      int32_t tbk = table[kv.first];
+      if (tbk < 0 || (kv.second.first == 0.0 && kv.second.second == 0.0)) continue;
+      LocalEntry le;
+      le.tblock = (uint32_t)tbk;
+      le.target = kv.first;
+      le.vre = kv.second.first;
+      le.vim = kv.second.second;
+      le.wreq = 0;
+      if (bs->nres) {
+        uint64_t on[2], offb[2];
+        from_local(kv.first & ~cc, lo, W, on);
+        from_local(cc & ~kv.first, lo, W, offb);
+        exact &= move_bits(bs, on, offb, le.wreq);
+      }
+      ent.push_back(le);
+    }
+  }
+  eoff[nb] = (uint32_t)ent.size();
+  c.nblocks = (int)nb;
+  c.nent = (int64_t)ent.size();
+  c.d_bstart = bst;
+  e = cudaMemcpy(bst + nb, &hstart[nb], 4, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMalloc(&c.d_cfg, table.size() * 4);
+  if (e == cudaSuccess) e = cudaMemcpy(c.d_cfg, table.data(), table.size() * 4, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMalloc(&c.d_eoff, eoff.size() * 4);
+  if (e == cudaSuccess) e = cudaMemcpy(c.d_eoff, eoff.data(), eoff.size() * 4, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMalloc(&c.d_ent, std::max<size_t>(ent.size(), 1) * sizeof(LocalEntry));
+  if (e == cudaSuccess && !ent.empty())
+    e = cudaMemcpy(c.d_ent, ent.data(), ent.size() * sizeof(LocalEntry), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return qg_cuda_fail(ctx, e, "local entries");
+  if (!exact) c.wreq_exact = false;
+  return QG_OK;
+}
+
+OpBasisCache *qg_basis_cache(qg_basis b, qg_operator op, qg_status *st) {
   *st = QG_OK;
-  for (auto &c : b->diag)
-    if (c.op_uid == op->uid) return c.d_diag;
+  for (auto &c : b->caches)
+    if (c.op_uid == op->uid) return &c;
   qg_context ctx = b->ctx;
-  double *d = nullptr;
-  cudaError_t e = cudaMalloc(&d, std::max<int64_t>(b->n, 1) * 16);
+  if (b->caches.size() >= 4) {  // small cache: drop the oldest
+    cudaStreamSynchronize(ctx->stream);
+    qg_cache_free(b->caches.front());
+    b->caches.erase(b->caches.begin());
+  }
+  OpBasisCache c;
+  c.op_uid = op->uid;
+  cudaError_t e = cudaMalloc(&c.d_diag, std::max<int64_t>(b->n, 1) * 16);
   if (e != cudaSuccess) {
     *st = qg_cuda_fail(ctx, e, "diagonal");
     return nullptr;
@@ -357,21 +647,47 @@ double *qg_basis_diag(qg_basis b, qg_operator op, qg_status *st) {
     if (op->W == 1)
       k_diag<1><<<grid_for(b->n, 256), 256, 0, ctx->stream>>>((const Key<1> *)b->d_keys, b->n,
                                                               (const GroupDev<1> *)op->diag.d_groups, op->diag.ngroups,
-                                                              (const TermDev<1> *)op->diag.d_terms, (double2 *)d);
+                                                              (const TermDev<1> *)op->diag.d_terms, (double2 *)c.d_diag);
     else
       k_diag<2><<<grid_for(b->n, 256), 256, 0, ctx->stream>>>((const Key<2> *)b->d_keys, b->n,
                                                               (const GroupDev<2> *)op->diag.d_groups, op->diag.ngroups,
-                                                              (const TermDev<2> *)op->diag.d_terms, (double2 *)d);
+                                                              (const TermDev<2> *)op->diag.d_terms, (double2 *)c.d_diag);
     ctx->launches++;
   }
-  if (b->diag.size() >= 4) {  // small cache: drop the oldest
-    cudaStreamSynchronize(ctx->stream);
-    cudaFree(b->diag.front().d_diag);
-    b->diag.erase(b->diag.begin());
+  // window bits of the non-local terms (encoding: 5 bits per window, moves of up to 2)
+  c.wreq_exact = b->nres > 0 && b->nres <= 12;
+  if (c.wreq_exact) {
+    std::vector<uint64_t> wr(std::max<size_t>(op->nl_host.size(), 1), 0);
+    for (size_t t = 0; t < op->nl_host.size() && c.wreq_exact; t++) {
+      const HostTerm &h = op->nl_host[t];
+      uint64_t on[2] = {h.fl[0] & h.n0[0], h.fl[1] & h.n0[1]}, offb[2] = {h.fl[0] & h.n1[0], h.fl[1] & h.n1[1]};
+      c.wreq_exact = move_bits(b, on, offb, wr[t]);
+    }
+    if (c.wreq_exact) {
+      e = cudaMalloc(&c.d_wreq, wr.size() * 8);
+      if (e == cudaSuccess) e = cudaMemcpy(c.d_wreq, wr.data(), wr.size() * 8, cudaMemcpyHostToDevice);
+      if (e != cudaSuccess) {
+        qg_cache_free(c);
+        *st = qg_cuda_fail(ctx, e, "window bits");
+        return nullptr;
+      }
+    }
   }
-  b->diag.push_back({op->uid, d});
-  *st = qg_check_launch(ctx, "diagonal");
-  return d;
+  if (op->H > 0 && b->n > 0) {
+    bool keep_exact = c.wreq_exact;
+    *st = build_local(b, op, c);
+    if (*st != QG_OK) {
+      qg_cache_free(c);
+      return nullptr;
+    }
+    if (keep_exact && !c.wreq_exact) {  // a local move outside the encoding: full checks
+      cudaFree(c.d_wreq);
+      c.d_wreq = nullptr;
+    }
+  }
+  b->caches.push_back(c);
+  *st = qg_check_launch(ctx, "operator-basis cache");
+  return &b->caches.back();
 }
 
 // ------------------------------------------------------------------ entry points
@@ -384,10 +700,26 @@ qg_status qg_apply_strided(qg_context ctx, qg_operator op, qg_basis dst, qg_basi
   qg_status st = QG_OK;
   const double2 *diag = nullptr;
   const HostTable *tab = &op->pull;
+  const uint64_t *wreq = nullptr;
+  LocalView lv{};
+  lv.on = 0;
   if (dst == src) {
-    diag = (const double2 *)qg_basis_diag(dst, op, &st);
+    OpBasisCache *c = qg_basis_cache(dst, op, &st);
     if (st != QG_OK) return st;
-    tab = &op->pull_off;
+    diag = (const double2 *)c->d_diag;
+    if (op->H > 0) {
+      tab = &op->pull_nl;
+      lv.on = 1;
+      lv.lo = dst->nf - op->H;
+      lv.lmask = (1u << op->H) - 1;
+      lv.cfg = c->d_cfg;
+      lv.bstart = c->d_bstart;
+      lv.eoff = c->d_eoff;
+      lv.ent = c->d_ent;
+    } else {
+      tab = &op->pull_off;
+    }
+    if (c->wreq_exact && c->d_wreq && tab == &op->pull_nl) wreq = c->d_wreq;
   }
   int packed = 0;
   if (nvec == 1) {
@@ -397,14 +729,14 @@ qg_status qg_apply_strided(qg_context ctx, qg_operator op, qg_basis dst, qg_basi
   const ApplyFuse &f = fz ? *fz : none;
   if (op->W == 1) {
     if (fz)
-      launch_apply_s<1, true>(ctx, *tab, diag, dst, src, packed, x2, xs, y2, ys, nvec, f);
+      launch_apply_s<1, true>(ctx, *tab, diag, dst, src, packed, x2, xs, y2, ys, nvec, f, lv, wreq);
     else
-      launch_apply_s<1, false>(ctx, *tab, diag, dst, src, packed, x2, xs, y2, ys, nvec, f);
+      launch_apply_s<1, false>(ctx, *tab, diag, dst, src, packed, x2, xs, y2, ys, nvec, f, lv, wreq);
   } else {
     if (fz)
-      launch_apply_s<2, true>(ctx, *tab, diag, dst, src, packed, x2, xs, y2, ys, nvec, f);
+      launch_apply_s<2, true>(ctx, *tab, diag, dst, src, packed, x2, xs, y2, ys, nvec, f, lv, wreq);
     else
-      launch_apply_s<2, false>(ctx, *tab, diag, dst, src, packed, x2, xs, y2, ys, nvec, f);
+      launch_apply_s<2, false>(ctx, *tab, diag, dst, src, packed, x2, xs, y2, ys, nvec, f, lv, wreq);
   }
   return qg_check_launch(ctx, "qg_apply");
 }

@@ -333,7 +333,7 @@ extern "C" qg_status qg_basis_destroy(qg_basis b) {
   cudaFree(b->d_rmask);
   cudaFree(b->d_rmin);
   cudaFree(b->d_rmax);
-  for (auto &d : b->diag) cudaFree(d.d_diag);
+  for (auto &c : b->caches) qg_cache_free(c);
   delete b;
   return QG_OK;
 }
@@ -355,6 +355,9 @@ qg_status qg_basis_set_windows(qg_basis b, int nres, const uint64_t *mask_host, 
   QG_CUDA(ctx, cudaMemcpy(b->d_rmin, min_host, nres * 4, cudaMemcpyHostToDevice));
   QG_CUDA(ctx, cudaMemcpy(b->d_rmax, max_host, nres * 4, cudaMemcpyHostToDevice));
   b->nres = nres;
+  b->h_rmask.assign(mask_host, mask_host + (size_t)nres * b->W);
+  b->h_rmin.assign(min_host, min_host + nres);
+  b->h_rmax.assign(max_host, max_host + nres);
   return QG_OK;
 }
 

@@ -98,6 +98,12 @@ struct HostTable {
   int ngroups = 0, nterms = 0;
 };
 
+// A digested term on the host (canonical masks in device bit positions, signed value).
+struct HostTerm {
+  uint64_t n1[2], n0[2], fl[2], sg[2];
+  double re, im;
+};
+
 struct qg_operator_s {
   qg_context ctx = nullptr;
   int nf = 0, W = 1;
@@ -108,12 +114,36 @@ struct qg_operator_s {
   HostTable diag;      // diagonal terms only (flip == 0)
   HostTable push;      // forward action grouped by need1: sources emit their targets
   int max_len = 0;
-  uint64_t uid = 0;    // unique per operator, keys the per-basis diagonal cache
+  uint64_t uid = 0;    // unique per operator, keys the per-basis caches
+  // local decomposition: the H leading orbitals (device bits nf-H .. nf-1) hold every
+  // many-body term; off-diagonal terms confined to them are precomputed per local
+  // configuration of a basis; the rest (pull_nl, host copy nl_host in table order) is scanned
+  int H = 0;
+  std::vector<HostTerm> local_off;
+  HostTable pull_nl;
+  std::vector<HostTerm> nl_host;
 };
 
-struct DiagCache {
-  uint64_t op_uid;
-  double *d_diag;  // complex per row
+// Per-(operator, basis) precomputed data for the same-basis H*psi.
+struct LocalEntry {
+  uint32_t tblock;   // block of the target local configuration
+  uint32_t target;   // target local configuration
+  uint64_t wreq;     // window bits the target needs (see qgpu_apply.cu)
+  double vre, vim;   // merged, signed coefficient
+};
+
+struct OpBasisCache {
+  uint64_t op_uid = 0;
+  double *d_diag = nullptr;       // complex per row: all diagonal terms
+  uint64_t *d_wreq = nullptr;     // per term of op->pull_nl: window bits its source needs
+  bool wreq_exact = false;        // every term's window change fits the bit encoding
+  // local blocks (op->H > 0): rows sharing a local configuration are contiguous
+  int nblocks = 0;
+  uint32_t *d_bstart = nullptr;   // [nblocks + 1]
+  int32_t *d_cfg = nullptr;       // [2^H] local configuration -> block, -1 if absent
+  uint32_t *d_eoff = nullptr;     // [nblocks + 1]
+  LocalEntry *d_ent = nullptr;
+  int64_t nent = 0;
 };
 
 struct qg_basis_s {
@@ -130,7 +160,9 @@ struct qg_basis_s {
   int nres = 0;
   uint64_t *d_rmask = nullptr;    // [nres][W]
   int32_t *d_rmin = nullptr, *d_rmax = nullptr;
-  std::vector<DiagCache> diag;
+  std::vector<uint64_t> h_rmask;
+  std::vector<int32_t> h_rmin, h_rmax;
+  std::vector<OpBasisCache> caches;
 };
 
 // ------------------------------------------------------------------ device helpers
@@ -228,8 +260,9 @@ qg_status qg_basis_from_device_keys(qg_context ctx, int nf, int W, void *d_keys_
 qg_status qg_basis_build_hash(qg_basis b);
 qg_status qg_basis_set_windows(qg_basis b, int nres, const uint64_t *mask_host, const int32_t *min_host,
                                const int32_t *max_host);
-// diagonal of op on the basis (cached per operator), device pointer or nullptr on failure
-double *qg_basis_diag(qg_basis b, qg_operator op, qg_status *st);
+// per-(operator, basis) cache (diagonal, window bits, local blocks); nullptr on failure
+OpBasisCache *qg_basis_cache(qg_basis b, qg_operator op, qg_status *st);
+void qg_cache_free(OpBasisCache &c);
 
 // Epilogue options for the fused Lanczos step (see qgpu_krylov.cu):
 //   prev/beta:  y = H x - beta[k] * prev;

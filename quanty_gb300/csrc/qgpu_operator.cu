@@ -108,7 +108,8 @@ struct Entry {
 };
 
 template <int W>
-void build_table(qg_context ctx, const std::vector<Entry> &terms, HostTable &tab, qg_status &st) {
+void build_table(qg_context ctx, const std::vector<Entry> &terms, HostTable &tab, qg_status &st,
+                 std::vector<HostTerm> *order = nullptr) {
   // group by need1; inside a group diagonal terms first
   std::map<std::vector<uint64_t>, std::vector<int>> groups;
   for (int t = 0; t < (int)terms.size(); t++) {
@@ -146,6 +147,18 @@ void build_table(qg_context ctx, const std::vector<Entry> &terms, HostTable &tab
       td.vre = terms[t].re;
       td.vim = terms[t].im;
       tt.push_back(td);
+      if (order) {
+        HostTerm h;
+        for (int i = 0; i < 2; i++) {
+          h.n1[i] = terms[t].m.n1[i];
+          h.n0[i] = terms[t].m.n0[i];
+          h.fl[i] = terms[t].m.fl[i];
+          h.sg[i] = terms[t].m.sg[i];
+        }
+        h.re = terms[t].re;
+        h.im = terms[t].im;
+        order->push_back(h);
+      }
     }
     gd.end = (int)tt.size();
     g.push_back(gd);
@@ -244,15 +257,60 @@ extern "C" qg_status qg_operator_create(qg_context ctx, int32_t nf, int32_t nter
   op->uid = next_uid++;
   std::vector<Entry> pull_off, diag;
   for (auto &e : pull) (is_diag(e) ? diag : pull_off).push_back(e);
+  // local prefix: the leading orbitals that hold every term acting on three or more orbitals
+  int minbit = nf;
+  for (auto &e : fwd) {
+    int cnt = 0;
+    for (int i = 0; i < 2; i++) cnt += __builtin_popcountll(e.m.n1[i] | e.m.n0[i] | e.m.fl[i]);
+    if (cnt < 3) continue;
+    for (int p = 0; p < nf; p++) {
+      uint64_t bit = 1ull << (p & 63);
+      uint64_t any = e.m.n1[p >> 6] | e.m.n0[p >> 6] | e.m.fl[p >> 6];
+      if (any & bit) {
+        minbit = std::min(minbit, p);
+        break;
+      }
+    }
+  }
+  int H = (minbit < nf) ? nf - minbit : 0;
+  if (H > 20) H = 0;
+  std::vector<Entry> nonlocal;
+  if (H > 0) {
+    uint64_t lm[2] = {0, 0};
+    for (int p = nf - H; p < nf; p++) lm[p >> 6] |= 1ull << (p & 63);
+    for (auto &e : pull_off) {
+      bool inside = true;
+      for (int i = 0; i < 2; i++) inside &= ((e.m.n1[i] | e.m.n0[i] | e.m.fl[i] | e.m.sg[i]) & ~lm[i]) == 0;
+      if (inside) {
+        HostTerm h;
+        for (int i = 0; i < 2; i++) {
+          h.n1[i] = e.m.n1[i];
+          h.n0[i] = e.m.n0[i];
+          h.fl[i] = e.m.fl[i];
+          h.sg[i] = e.m.sg[i];
+        }
+        h.re = e.re;
+        h.im = e.im;
+        op->local_off.push_back(h);
+      } else {
+        nonlocal.push_back(e);
+      }
+    }
+  } else {
+    nonlocal = pull_off;
+  }
+  op->H = H;
   qg_status st = QG_OK;
   if (op->W == 1) {
     build_table<1>(ctx, pull, op->pull, st);
     if (st == QG_OK) build_table<1>(ctx, pull_off, op->pull_off, st);
+    if (st == QG_OK) build_table<1>(ctx, nonlocal, op->pull_nl, st, &op->nl_host);
     if (st == QG_OK) build_table<1>(ctx, diag, op->diag, st);
     if (st == QG_OK) build_table<1>(ctx, fwd, op->push, st);
   } else {
     build_table<2>(ctx, pull, op->pull, st);
     if (st == QG_OK) build_table<2>(ctx, pull_off, op->pull_off, st);
+    if (st == QG_OK) build_table<2>(ctx, nonlocal, op->pull_nl, st, &op->nl_host);
     if (st == QG_OK) build_table<2>(ctx, diag, op->diag, st);
     if (st == QG_OK) build_table<2>(ctx, fwd, op->push, st);
   }
@@ -269,6 +327,7 @@ extern "C" qg_status qg_operator_destroy(qg_operator op) {
   cudaFree(op->pull.d_blob);
   cudaFree(op->pull_off.d_blob);
   cudaFree(op->diag.d_blob);
+  cudaFree(op->pull_nl.d_blob);
   cudaFree(op->push.d_blob);
   delete op;
   return QG_OK;

@@ -173,3 +173,25 @@ def test_closure_counts_and_table_growth(api):
     d = b.dets_bytes()
     idx = b.find(d[:5000])
     assert np.array_equal(idx, np.arange(5000))
+
+
+@pytest.mark.parametrize("nshell,hmax,pmax", [(2, 2, 2), (3, 2, 1)])
+def test_anderson_impurity_apply_matches_oracle(api, oracle_mod, nshell, hmax, pmax):
+    """The benchmark Hamiltonian's structure at a size the oracle handles: impurity terms take
+    the local-block path, hybridisation the scanned path with window bits, the diagonal is
+    cached; every amplitude equals the oracle's push-form H*psi on the same basis."""
+    from quanty_gb300 import workloads
+    O = oracle_mod
+    H, R, seed, info = workloads.anderson_impurity(nshell=nshell, hole_max=hmax, particle_max=pmax)
+    b = api.closure(H, api.dets_to_bytes([seed], H.nf), H.nf, R)
+    assert b.n == info["sector_determinants"]
+    dets = b.dets_bytes()
+    rng = np.random.default_rng(nshell)
+    x = rng.normal(size=len(dets)) + 1j * rng.normal(size=len(dets))
+    y = api.OperatorPsiConserveBasis(H, api.Wavefunction(H.nf, dets, x))
+    op = O.Op({"nf": H.nf, "terms": [[list(t[0]), t[1].real, t[1].imag] for t in H.terms]})
+    want = O.apply_conserve(op, O.WF(H.nf, dets, x))
+    assert rel_err(y.val, want) < TOL
+    # the same on a basis given as plain determinants (no windows, no closure): full checks
+    y2 = api.OperatorPsiConserveBasis(H, api.Wavefunction(H.nf, dets[::-1].copy(), x[::-1].copy()))
+    assert rel_err(y2.val[::-1], want) < TOL
