@@ -41,6 +41,7 @@ def lib():
         L.qo_operator_psi.restype = P
         L.qo_operator_psi.argtypes = [I, P, P, P, P, P, P, I, P, P, P]
         L.qo_apply_conserve.argtypes = [I, P, P, P, P, P, P, I64, I64, P]
+        L.qo_apply_conserve_strided.argtypes = [I, P, P, P, P, P, P, I64, I64, I64, P]
         L.qo_count_nnz.restype = I64
         L.qo_count_nnz.argtypes = [I, P, P, P, P, I64, I64]
         L.qo_lanczos_tridiag.argtypes = [I, P, P, P, P, P, P, I, D, D, I, P, P, P, P, P]

@@ -246,14 +246,26 @@ qo_wf *qo_operator_psi(int nterms, const int *len, const int64_t *off, const uin
  * OpenMP over source determinants with atomic adds, as the reference.
  * Sources are rows [row0, row1) of x; y (length x->n, interleaved re/im) is overwritten
  * with zeros first. */
+void qo_apply_conserve_strided(int nterms, const int *len, const int64_t *off, const uint16_t *ops,
+                               const double *vre, const double *vim, const qo_wf *x, int64_t row0,
+                               int64_t row1, int64_t stride, double *y);
 void qo_apply_conserve(int nterms, const int *len, const int64_t *off, const uint16_t *ops,
                        const double *vre, const double *vim, const qo_wf *x, int64_t row0,
                        int64_t row1, double *y)
 {
-  int64_t i;
+  qo_apply_conserve_strided(nterms, len, off, ops, vre, vim, x, row0, row1, 1, y);
+}
+
+/* the same over the source rows row0, row0+stride, ... < row1 (a spread sample) */
+void qo_apply_conserve_strided(int nterms, const int *len, const int64_t *off, const uint16_t *ops,
+                               const double *vre, const double *vim, const qo_wf *x, int64_t row0,
+                               int64_t row1, int64_t stride, double *y)
+{
+  int64_t i, cnt = (row1 - row0 + stride - 1) / stride;
   for (i = 0; i < 2 * x->n; i++) y[i] = 0.0;
 #pragma omp parallel for schedule(dynamic, 64)
-  for (i = row0; i < row1; i++) {
+  for (int64_t c = 0; c < cnt; c++) {
+    int64_t i = row0 + c * stride;
     uint8_t tmp[64];
     const uint8_t *src = x->det + i * x->nword;
     double xr = x->re[i], xi = x->im[i];

@@ -36,9 +36,24 @@ def atomic():
     return {k: Operator(16, [(t[0], complex(t[1], t[2])) for t in d[k]], name=k) for k in ("H", "HX", "Tx", "Ty", "Tz")}
 
 
-def number_pair(i, j):
-    """n_i n_j as a ladder string (c_j acts first)."""
-    return [j, j | CREATION, i, i | CREATION]
+def number_pair(i, j, value):
+    """n_i n_j (i != j) in the normal order the reference stores two-body terms in:
+    c^dag_a c^dag_b c_a c_b with a > b (ladder codes [b, a, b^dag, a^dag], the rightmost
+    acting first) and value -U, since n_a n_b = -c^dag_a c^dag_b c_a c_b."""
+    a, b = max(i, j), min(i, j)
+    return [b, a, b | CREATION, a | CREATION], -value
+
+
+def merged(terms):
+    """Sum the values of identical ladder strings (the reference's operator addition)."""
+    acc, order = {}, []
+    for ops, v in terms:
+        k = tuple(ops)
+        if k not in acc:
+            acc[k] = 0j
+            order.append(k)
+        acc[k] += v
+    return [(list(k), acc[k]) for k in order if acc[k] != 0]
 
 
 def anderson_impurity(nshell=7, seed=0, udd=7.5, upd=8.5, half_width=2.0, v2_total=4.0, hole_max=3,
@@ -51,10 +66,10 @@ def anderson_impurity(nshell=7, seed=0, udd=7.5, upd=8.5, half_width=2.0, v2_tot
     p_orb = list(range(0, 6))
     for a in range(10):
         for b in range(a + 1, 10):
-            terms.append((number_pair(d_orb[a], d_orb[b]), udd))
+            terms.append(number_pair(d_orb[a], d_orb[b], udd))
     for p in p_orb:
         for d in d_orb:
-            terms.append((number_pair(p, d), upd))
+            terms.append(number_pair(p, d, upd))
     rng = np.random.default_rng(seed)
     eps = np.sort(rng.uniform(-5.0, 5.0, nshell))
     x = -half_width + 2 * half_width * (np.arange(nshell) + 0.5) / nshell
@@ -77,7 +92,7 @@ def anderson_impurity(nshell=7, seed=0, udd=7.5, upd=8.5, half_width=2.0, v2_tot
             terms.append(([d_orb[b], d_orb[a] | CREATION], v))
             if a != b:
                 terms.append(([d_orb[a], d_orb[b] | CREATION], v.conjugate()))
-    H = Operator(nf, terms, name="AndersonImpurity")
+    H = Operator(nf, merged(terms), name="AndersonImpurity")
     filled = [k for k in range(nshell) if eps[k] < 0]
     empty = [k for k in range(nshell) if eps[k] >= 0]
 
