@@ -64,7 +64,18 @@ class Engine:
         return int(self.L.qg_launch_count(self.ctx))
 
     def empty(self, n, nvec=1):
-        return self.torch.zeros((max(n, 1), nvec), dtype=self.torch.complex128, device="cuda:%d" % self.device)
+        with self.torch.cuda.stream(self.stream):
+            return self.torch.zeros((max(n, 1), nvec), dtype=self.torch.complex128, device="cuda:%d" % self.device)
+
+    def on_stream(self):
+        """Context manager: torch work ordered with this engine's kernels."""
+        return self.torch.cuda.stream(self.stream)
+
+    def to_host(self, t):
+        """Copy a device tensor to numpy after this engine's queued work."""
+        self.stream.synchronize()
+        with self.on_stream():
+            return t.cpu().numpy()
 
     def close(self):
         if getattr(self, "ctx", None):
@@ -300,7 +311,8 @@ def _upload(eng, basis, perm, values, nvec=1):
     v = np.zeros((max(n, 1), nvec), dtype=np.complex128)
     vals = np.asarray(values).reshape(len(perm), nvec)
     np.add.at(v, perm, vals)
-    return torch.from_numpy(v).to("cuda:%d" % eng.device)
+    with eng.on_stream():
+        return torch.from_numpy(v).to("cuda:%d" % eng.device)
 
 
 # ----------------------------------------------------------------------------- H * psi
@@ -324,8 +336,7 @@ def OperatorPsi(O, psi, restrictions=None, eng=None):
     dst = OperatorPsiBasis(O, src, restrictions, eng)
     y = eng.empty(dst.n)
     eng.check(eng.L.qg_apply(eng.ctx, O.handle(eng), dst.h, src.h, _ptr(x), _ptr(y), 1))
-    eng.torch.cuda.synchronize()
-    return Wavefunction(psi.nf, dst.dets_bytes(), y[:dst.n, 0].cpu().numpy())
+    return Wavefunction(psi.nf, dst.dets_bytes(), eng.to_host(y[:dst.n, 0]))
 
 
 def OperatorPsiConserveBasis(O, psi, eng=None):
@@ -335,7 +346,7 @@ def OperatorPsiConserveBasis(O, psi, eng=None):
     x = _upload(eng, b, perm, psi.val)
     y = eng.empty(b.n)
     eng.check(eng.L.qg_apply(eng.ctx, O.handle(eng), b.h, b.h, _ptr(x), _ptr(y), 1))
-    yh = y[:b.n, 0].cpu().numpy()
+    yh = eng.to_host(y[:b.n, 0])
     return Wavefunction(psi.nf, psi.det, yh[perm])
 
 
@@ -463,8 +474,11 @@ def CreateSpectra(H, T, psi, options=None, eng=None, batched=True):
             xs = _upload(eng, src, perm, Tpsi[i].val)
             col = eng.empty(basis.n)
             eng.check(eng.L.qg_basis_map(eng.ctx, src.h, _ptr(xs), basis.h, _ptr(col), 1))
-            x[:, c] = col[:, 0]
-        a, b = lanczos_block(H, basis, x.contiguous(), ntri, eps, max(gamma, eps), eng)
+            with eng.on_stream():
+                x[:, c] = col[:, 0]
+        with eng.on_stream():
+            x = x.contiguous()
+        a, b = lanczos_block(H, basis, x, ntri, eps, max(gamma, eps), eng)
         A[grp] = a
         B[grp] = b
     # pole range -> default Emin/Emax/Gamma (ssp.cpp:2655-2689) when not given
@@ -536,14 +550,15 @@ def Eigensystem(H, StartRestrictions, Npsi, options=None, eng=None, seed=12345):
     n = basis.n
     rng = np.random.default_rng(seed)
     x0 = rng.standard_normal((n, Npsi)) + 1j * rng.standard_normal((n, Npsi))
-    x = eng.torch.from_numpy(x0).to("cuda:%d" % eng.device).contiguous()
+    with eng.on_stream():
+        x = eng.torch.from_numpy(x0).to("cuda:%d" % eng.device).contiguous()
     en = np.zeros(Npsi)
     it = C.c_int32()
     K = int(min(max(8 * Npsi, 128), 256, n))
     tol = float(o["Zero"])
     eng.check(eng.L.qg_block_groundstate(eng.ctx, H.handle(eng), basis.h, Npsi, _ptr(x), _ptr(en), tol, K, 200,
                                          C.byref(it)))
-    X = x.cpu().numpy()
+    X = eng.to_host(x)
     db = basis.dets_bytes()
     out = [Wavefunction(H.nf, db, X[:, k]) for k in range(Npsi)]
     return out, en

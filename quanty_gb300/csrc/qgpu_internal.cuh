@@ -87,6 +87,7 @@ struct qg_context_s {
   int num_sms = 148;
   double *d_io = nullptr;             // staging for host-buffer entry points
   size_t io_bytes = 0;
+  bool use_graphs = true;             // capture Lanczos step sequences into CUDA graphs
 };
 
 // A term table in one device allocation: ngroups GroupDev followed by nterms TermDev.

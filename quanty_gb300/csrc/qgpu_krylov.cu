@@ -341,22 +341,55 @@ extern "C" qg_status qg_lanczos_tridiag(qg_context ctx, qg_operator op, qg_basis
     k_fin_a<<<1, 256, 0, s>>>(dpart, Papply, nvec, a_now, a_hist, ntri + 1, 1);
     ctx->launches++;
   }
-  for (int i = 1; i < ntri && st == QG_OK && e == cudaSuccess; i++) {
+  // steps 1 .. ntri-1: every scalar stays on the device, so the whole sequence is captured
+  // into one CUDA graph and launched once (falling back to direct launches if capture fails)
+  auto step = [&](int i) -> qg_status {
     std::swap(vp, vc);  // vp = v_{i-1}
     k_lanczos_axpy_norm<<<P, RBLK, (RBLK / 32) * sizeof(double2), s>>>(n, nvec, w, vp, a_now, vraw, npart);
     k_fin_b<<<1, 256, 0, s>>>(npart, P, nvec, b_now, b_hist, ntri, i, scale, thr2, err, eps, gamma, 0);
     ctx->launches += 2;
-    st = normalise(vraw);
-    if (st != QG_OK) break;
+    qg_status sst = normalise(vraw);
+    if (sst != QG_OK) return sst;
     fz.prev = vp;
     fz.beta = b_now;
-    st = qg_apply_strided(ctx, op, b, b, (const double *)vc, nvec, (double *)w2, nvec, nvec, &fz, nvec == 1);
+    sst = qg_apply_strided(ctx, op, b, b, (const double *)vc, nvec, (double *)w2, nvec, nvec, &fz, nvec == 1);
     std::swap(w, w2);
-    if (st == QG_OK && krylov_dev)
-      e = cudaMemcpyAsync(krylov_dev + 2 * (size_t)i * len, vc, len * 16, cudaMemcpyDeviceToDevice, s);
+    if (sst == QG_OK && krylov_dev) {
+      cudaError_t ce = cudaMemcpyAsync(krylov_dev + 2 * (size_t)i * len, vc, len * 16, cudaMemcpyDeviceToDevice, s);
+      if (ce != cudaSuccess) return qg_cuda_fail(ctx, ce, "krylov copy");
+    }
     k_fin_a<<<1, 256, 0, s>>>(dpart, Papply, nvec, a_now, a_hist, ntri + 1, i + 1);
     ctx->launches++;
+    return sst;
+  };
+  bool graphed = false;
+  if (st == QG_OK && e == cudaSuccess && ntri > 2 && ctx->use_graphs) {
+    double2 *sv[6] = {vp, vc, w, w2, vraw, zero};
+    int64_t l0 = ctx->launches;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    qg_status cst = QG_OK;
+    if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+      for (int i = 1; i < ntri && cst == QG_OK; i++) cst = step(i);
+      cudaError_t ee = cudaStreamEndCapture(s, &graph);
+      if (ee == cudaSuccess && cst == QG_OK && cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess &&
+          cudaGraphLaunch(exec, s) == cudaSuccess) {
+        graphed = true;
+      }
+    }
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    if (!graphed) {
+      cudaGetLastError();
+      // restore the buffer roles and redo the steps directly
+      vp = sv[0];
+      vc = sv[1];
+      w = sv[2];
+      w2 = sv[3];
+      ctx->launches = l0;
+    }
   }
+  for (int i = 1; !graphed && i < ntri && st == QG_OK && e == cudaSuccess; i++) st = step(i);
   if (st == QG_OK && e == cudaSuccess) {
     e = cudaMemcpyAsync(a_host, a_hist, (size_t)nvec * (ntri + 1) * 8, cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(b_host, b_hist, (size_t)nvec * ntri * 8, cudaMemcpyDeviceToHost, s);
