@@ -163,6 +163,17 @@ qg_status qg_norm(qg_context ctx, int64_t n, int32_t nvec, const double *x_dev, 
 qg_status qg_axpy(qg_context ctx, int64_t n, int32_t nvec, const double *alpha_host, const double *x_dev,
                   double *y_dev);
 
+/* qg_dot for callers that cannot allocate device memory (no counterpart in the reference,
+ * which has no GPU): per-vector <x_k|y_k> of nvec vectors of n complex entries (device
+ * pointers) into out_dev (nvec complex values, device memory), on the given CUDA stream
+ * (NULL = legacy default stream).  It calls no cudaMalloc/cudaFree: the block partial sums
+ * live in a fixed device array inside the library (1 MiB per device), so nvec is limited to
+ * 64 (larger values return QG_ERR_ARG).  The first call on a device looks up that array's
+ * address and should come before any stream capture.  All calls on a device share the
+ * array: calls that may overlap on the GPU race and must be ordered by the caller. */
+qg_status qg_dot_noalloc(int64_t n, int32_t nvec, const double *x_dev, const double *y_dev, double *out_dev,
+                         void *stream);
+
 /* ------------------------------------------------------------------ Krylov drivers */
 
 /* Three-term Lanczos tridiagonalisation of op from nvec starting vectors at once (all on

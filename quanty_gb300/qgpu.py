@@ -58,6 +58,7 @@ def load(path=LIB_PATH):
         "qg_count_nnz_offdiag": (C.c_int, [P, P, P, P]),
         "qg_expectation": (C.c_int, [P, P, P, P, I32, P]),
         "qg_dot": (C.c_int, [P, I64, I32, P, P, P]),
+        "qg_dot_noalloc": (C.c_int, [I64, I32, P, P, P, P]),
         "qg_norm": (C.c_int, [P, I64, I32, P, P]),
         "qg_axpy": (C.c_int, [P, I64, I32, P, P, P]),
         "qg_lanczos_tridiag": (C.c_int, [P, P, P, P, I32, I32, D, D, P, P, P]),
