@@ -135,6 +135,15 @@ qg_status qg_basis_map(qg_context ctx, qg_basis src, const double *x_dev, qg_bas
 qg_status qg_apply(qg_context ctx, qg_operator op, qg_basis basis_dst, qg_basis basis_src,
                    const double *x_dev, double *y_dev, int32_t nvec);
 
+/* Autotuning of the multi-vector apply (no counterpart in the reference, whose loops handle one
+ * vector at a time): the first apply of an operator with nvec >= 2 vectors on a basis (as
+ * its own source and target, outside stream capture) times each number of vectors handled per
+ * kernel pass (8, 4, 2, 1) and keeps the fastest for that (operator, basis, nvec).  The result
+ * is bitwise the same for every choice.  qg_set_autotune(ctx, 0) turns the timing off (passes
+ * of 8 vectors); qg_apply_chunk reports the choice in force (0 while none has been made). */
+qg_status qg_set_autotune(qg_context ctx, int32_t on);
+qg_status qg_apply_chunk(qg_context ctx, qg_operator op, qg_basis basis, int32_t nvec, int32_t *chunk);
+
 /* qg_apply with host buffers: copies x_host to the device, applies, copies y back (the
  * reference's calling convention, where psi and Opsi live in host memory).  Device staging
  * buffers are kept in the context between calls; pinned host buffers give full copy speed. */

@@ -372,6 +372,20 @@ def count_nnz(O, basis, eng=None, offdiag=False):
 def closure(O, seed_bytes, nf, restrictions=None, max_rounds=-1, eng=None):
     eng = eng or engine()
     seed, _ = Basis.from_bytes(nf, seed_bytes, eng)
+    return closure_of(O, seed, restrictions, max_rounds, eng)
+
+
+def basis_union(a, b, eng=None):
+    eng = eng or engine()
+    h = C.c_void_p()
+    eng.check(eng.L.qg_basis_union(eng.ctx, a.h, b.h, C.byref(h)))
+    return Basis(eng, h, a.nf)
+
+
+def closure_of(O, seed, restrictions=None, max_rounds=-1, eng=None):
+    """Closure of a device basis under O (within the restrictions)."""
+    eng = eng or engine()
+    nf = seed.nf
     res = _Res(nf, parse_restrictions(restrictions))
     h = C.c_void_p()
     rounds = C.c_int32()
@@ -443,6 +457,50 @@ class Spectra:
     @property
     def energies(self):
         return self.Emin + np.arange(self.NE + 1) * (self.Emax - self.Emin) / self.NE
+
+
+def CreateSpectraResident(H, T, basis, X, E0, options=None, eng=None, batched=True, max_vectors=None):
+    """The batched form of CreateSpectra for initial states held on the device: X is an
+    (n, npsi) complex CUDA tensor on `basis`, E0 their energies.  The final-state basis is the
+    closure under H of the targets of every T (within the Restrictions option); all (T, psi)
+    pairs, ordered iT*npsi + ipsi, then run as one multi-vector Lanczos (batched=True, or
+    groups of `max_vectors`) or one Lanczos per pair (batched=False, the plain path).
+    Returns (Spectra, A, B) with the raw Lanczos coefficients A (a_0..a_NTri) and B."""
+    eng = eng or engine()
+    o = _opts(options)
+    Ts = T if isinstance(T, (list, tuple)) else [T]
+    R = parse_restrictions(o.get("Restrictions"))
+    ntri, eps, gamma = int(o["NTri"]), float(o["Epsilon"]), float(o["Gamma"])
+    npsi = X.shape[1]
+    bt = None
+    for t in Ts:
+        tb = OperatorPsiBasis(t, basis, R, eng)
+        bt = tb if bt is None else basis_union(bt, tb, eng)
+    bf = closure_of(H, bt, R, -1, eng)
+    nvec = len(Ts) * npsi
+    Y = eng.empty(bf.n, nvec)
+    Xc = X.contiguous()
+    for j, t in enumerate(Ts):
+        yj = eng.empty(bf.n, npsi)
+        eng.check(eng.L.qg_apply(eng.ctx, t.handle(eng), bf.h, basis.h, _ptr(Xc), _ptr(yj), npsi))
+        with eng.on_stream():
+            Y[:, j * npsi:(j + 1) * npsi] = yj
+    step = nvec if batched else 1
+    if batched and max_vectors:
+        step = int(max_vectors)
+    A = np.zeros((nvec, ntri + 1))
+    B = np.zeros((nvec, ntri))
+    for c0 in range(0, nvec, step):
+        c1 = min(nvec, c0 + step)
+        with eng.on_stream():
+            x = Y[:, c0:c1].contiguous()
+        a, b = lanczos_block(H, bf, x, ntri, eps, max(gamma, eps), eng)
+        A[c0:c1] = a
+        B[c0:c1] = b
+    e0 = np.array([E0[i % npsi] for i in range(nvec)], dtype=np.float64)
+    NE = int(o["NE"])
+    G = TriDiagonalMatrixToSpectrum(e0, A, B, o["Emin"], o["Emax"], NE, gamma, eng)
+    return Spectra(G, o["Emin"], o["Emax"], NE, gamma), A, B
 
 
 def CreateSpectra(H, T, psi, options=None, eng=None, batched=True):
@@ -542,11 +600,22 @@ def Eigensystem(H, StartRestrictions, Npsi, options=None, eng=None, seed=12345):
     determinants allowed by the restrictions (or their closure under H); the eigenproblem on it
     is solved by restarted block Lanczos on the device.  Returns (list of Wavefunction, energies)."""
     eng = eng or engine()
-    o = _opts(options)
     R = parse_restrictions(StartRestrictions)
     dets = enumerate_restricted(H.nf, R)
     basis, _ = Basis.from_bytes(H.nf, dets, eng)
-    basis = closure(H, basis.dets_bytes(), H.nf, R, -1, eng)
+    basis = closure_of(H, basis, R, -1, eng)
+    x, en = EigensystemOnBasis(H, basis, Npsi, options, eng, seed)
+    X = eng.to_host(x)
+    db = basis.dets_bytes()
+    out = [Wavefunction(H.nf, db, X[:, k]) for k in range(Npsi)]
+    return out, en
+
+
+def EigensystemOnBasis(H, basis, Npsi, options=None, eng=None, seed=12345):
+    """Lowest Npsi eigenpairs of H on a device basis, kept on the device: returns
+    ((n, Npsi) complex CUDA tensor, energies)."""
+    eng = eng or engine()
+    o = _opts(options)
     n = basis.n
     rng = np.random.default_rng(seed)
     x0 = rng.standard_normal((n, Npsi)) + 1j * rng.standard_normal((n, Npsi))
@@ -554,14 +623,14 @@ def Eigensystem(H, StartRestrictions, Npsi, options=None, eng=None, seed=12345):
         x = eng.torch.from_numpy(x0).to("cuda:%d" % eng.device).contiguous()
     en = np.zeros(Npsi)
     it = C.c_int32()
-    K = int(min(max(8 * Npsi, 128), 256, n))
+    # Krylov space up to Npsi + NKrylovMax vectors (grown per restart from Npsi + 100), within
+    # half of the free device memory
+    free = eng.torch.cuda.mem_get_info(eng.device)[0]
+    K = int(min(Npsi + int(o["NKrylovMax"]), n, max(2 * Npsi, free // (2 * 16 * max(n, 1)))))
     tol = float(o["Zero"])
     eng.check(eng.L.qg_block_groundstate(eng.ctx, H.handle(eng), basis.h, Npsi, _ptr(x), _ptr(en), tol, K, 200,
                                          C.byref(it)))
-    X = eng.to_host(x)
-    db = basis.dets_bytes()
-    out = [Wavefunction(H.nf, db, X[:, k]) for k in range(Npsi)]
-    return out, en
+    return x, en
 
 
 # ----------------------------------------------------------------------------- RIXS

@@ -1,0 +1,263 @@
+"""The two added forms of the spectra path, measured beside the H*psi headline.
+
+* ``batched``: a 6-shell discretised-bath impurity (76 spin-orbitals, 2p + 3d + 6 bath shells
+  of 10; at most 1 hole in the filled bath shells, at most 2 particles in the empty ones:
+  1,701,795 ground-sector determinants).  The 16 lowest states (restarted block Lanczos),
+  Boltzmann weights at 300 K, then the XAS of all 16 states x 3 dipole polarisations
+  (Tx, Ty, Tz; 2p -> 3d) as ONE 48-vector Lanczos on the common core-excited basis, against
+  the plain path (one closure + one single-vector Lanczos per spectrum, as a one-job-at-a-time
+  caller runs it), timed on a sample of the 48 spectra.  Then the RIXS of the lowest state:
+  64 incident energies over 16 eV (Gamma1 = 0.4 eV) x 3 emission polarisations, all 192
+  second-stage recursions in one batched Lanczos.
+* ``served``: a Poisson stream of Eigensystem and CreateSpectra jobs on discretised-bath
+  impurities with seeded random charge-transfer energy (1-6 eV), hybridisation (0.5-3 eV) and
+  1-6 bath shells, sizes log-uniform up to ``--max-det`` determinants, 150-1000 Lanczos steps
+  and 1024-4096 frequencies; served by ``serve.Server`` (4 slots, HBM-budget admission,
+  3-polarisation batched Lanczos) against ``serve.run_plain`` (one job at a time, one
+  Lanczos per spectrum) on the same stream.  p50/p99 latencies and spectra/s for both.
+
+Both print one JSON line.
+"""
+import json
+import math
+import time
+
+import numpy as np
+
+KT_300K = 8.617333262e-5 * 300.0  # eV
+
+
+def _xas_ops(api, workloads, nf):
+    at = workloads.atomic()
+    return [api.Operator(nf, at[k].terms, name=k) for k in ("Tx", "Ty", "Tz")]
+
+
+def _sync(eng):
+    eng.stream.synchronize()
+
+
+def batched(args):
+    from . import api, workloads
+    eng = api.engine()
+    nshell, hm, pm = 6, 1, 2
+    H, R, seed, info = workloads.anderson_impurity(nshell=nshell, hole_max=hm, particle_max=pm)
+    _, Rx, _, _ = workloads.anderson_impurity(nshell=nshell, hole_max=hm, particle_max=pm, core_holes=1)
+    Ts = _xas_ops(api, workloads, H.nf)
+    nstates = int(args.states)
+    t0 = time.perf_counter()
+    basis = api.closure(H, api.dets_to_bytes([seed], H.nf), H.nf, R, -1, eng)
+    X, E = api.EigensystemOnBasis(H, basis, nstates, None, eng)  # the reference's default Zero
+    _sync(eng)
+    t_eigen = time.perf_counter() - t0
+    w = np.exp(-(E - E.min()) / KT_300K)
+    w /= w.sum()
+    ntri = int(args.ntri)
+    o = {"NTri": ntri, "NE": 2048, "Emin": -20.0, "Emax": 20.0, "Gamma": 0.5, "Restrictions": Rx}
+    nspec = len(Ts) * nstates
+
+    def run_batched():
+        return api.CreateSpectraResident(H, Ts, basis, X, E, o, eng, batched=True)
+
+    S, A, B = run_batched()  # warm-up: graphs, caches
+    _sync(eng)
+    reps = max(1, int(args.steps))
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        S, A, B = run_batched()
+    _sync(eng)
+    t_batched = (time.perf_counter() - t0) / reps
+    xas = np.array([(w[:, None] * S.G[j * nstates:(j + 1) * nstates]).sum(0) for j in range(len(Ts))])
+
+    # plain path on a sample of the pairs: closure + T psi + one Lanczos + CF per spectrum
+    sample = [(j, i) for i in range(min(2, nstates)) for j in range(len(Ts))]
+    with eng.on_stream():
+        cols = [X[:, i:i + 1].contiguous() for i in range(nstates)]
+    api.CreateSpectraResident(H, [Ts[0]], basis, cols[0], [E[0]], o, eng, batched=False)  # warm
+    _sync(eng)
+    t0 = time.perf_counter()
+    diff = 0.0
+    for j, i in sample:
+        Sp, _, _ = api.CreateSpectraResident(H, [Ts[j]], basis, cols[i], [E[i]], o, eng, batched=False)
+        g = S.G[j * nstates + i]
+        diff = max(diff, float(np.max(np.abs(Sp.G[0] - g)) / np.max(np.abs(g))))
+    _sync(eng)
+    t_plain = (time.perf_counter() - t0) / len(sample)
+
+    # the Lanczos stage alone: one 48-vector recursion against single-vector recursions
+    eps = float(api.DEFAULTS["Epsilon"])
+    bf, Y = _final_vectors(api, H, Ts, basis, X, Rx, eng)
+    t_lz_b = _lanczos_seconds(api, H, bf, Y, ntri, eps, eng)
+    with eng.on_stream():
+        y1 = [Y[:, c:c + 1].contiguous() for c in (0, nstates)]
+    t_lz_p = sum(_lanczos_seconds(api, H, bf, y, ntri, eps, eng) for y in y1) / len(y1)
+    n_final = bf.n
+    del Y, y1, bf
+
+    rixs = None
+    if not args.no_rixs:
+        psi0 = api.Wavefunction(H.nf, basis.dets_bytes(), eng.to_host(X[:, 0]))
+        ro = {"NTri1": ntri // 2, "NTri2": ntri // 2, "Epsilon": o.get("Epsilon", api.DEFAULTS["Epsilon"]),
+              "Emin1": -8.0, "Emax1": 8.0, "NE1": 63, "Gamma1": 0.4,
+              "Emin2": -2.0, "Emax2": 10.0, "NE2": 1024, "Gamma2": 0.1,
+              "Restrictions1": Rx, "Restrictions2": R}
+        G, _ = api.CreateResonantSpectra(H, H, Ts[2], Ts, psi0, ro, eng)  # warm
+        _sync(eng)
+        t0 = time.perf_counter()
+        G, st = api.CreateResonantSpectra(H, H, Ts[2], Ts, psi0, ro, eng)
+        _sync(eng)
+        t_rixs = time.perf_counter() - t0
+        rixs = {"incident_energies": 64, "emission_polarisations": 3, "spectra": int(G.shape[0]),
+                "ntri1": ro["NTri1"], "ntri2": ro["NTri2"], "ne2": 1024, "seconds": t_rixs,
+                "spectra_per_s": G.shape[0] / t_rixs, "finite": bool(np.all(np.isfinite(G)))}
+
+    line = {
+        "metric": "batched CreateSpectra spectra/s",
+        "value": nspec / t_batched,
+        "unit": "spectra/s",
+        "mode": "batched",
+        "n_gpus": 1,
+        "steps": reps,
+        "higher_is_better": True,
+        "dtype": "c128",
+        "data": "synthetic (seeded impurity Hamiltonian)",
+        "config": {"workload": "impurity_76so_6shell_xas_16states_x3pol", "ground_determinants": basis.n,
+                   "core_excited_determinants": int(n_final),
+                   "ntri": ntri, "ne": 2048, "vectors_per_launch": nspec, "temperature_K": 300},
+        "batched": {"seconds": t_batched, "spectra": nspec, "spectra_per_s": nspec / t_batched},
+        "plain": {"seconds_per_spectrum": t_plain, "spectra_per_s": 1.0 / t_plain, "sample": len(sample)},
+        "speedup_vs_plain": (nspec / t_batched) * t_plain,
+        "max_rel_diff_batched_vs_plain": diff,
+        "lanczos_only": {"batched_seconds": t_lz_b, "plain_seconds_per_vector": t_lz_p,
+                         "speedup": nspec * t_lz_p / t_lz_b},
+        "eigensystem_seconds": t_eigen,
+        "energies_eV": [float(e) for e in E],
+        "boltzmann_weights": [float(x) for x in w],
+        "xas_peak": float(np.max(-xas.imag)),
+        "rixs": rixs,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def _final_vectors(api, H, Ts, basis, X, R, eng):
+    """Common core-excited basis and the (n, len(Ts) * npsi) block of T psi on it."""
+    bt = None
+    for t in Ts:
+        tb = api.OperatorPsiBasis(t, basis, R, eng)
+        bt = tb if bt is None else api.basis_union(bt, tb, eng)
+    bf = api.closure_of(H, bt, R, -1, eng)
+    npsi = X.shape[1]
+    Y = eng.empty(bf.n, len(Ts) * npsi)
+    for j, t in enumerate(Ts):
+        yj = eng.empty(bf.n, npsi)
+        eng.check(eng.L.qg_apply(eng.ctx, t.handle(eng), bf.h, basis.h, api._ptr(X), api._ptr(yj), npsi))
+        with eng.on_stream():
+            Y[:, j * npsi:(j + 1) * npsi] = yj
+    return bf, Y
+
+
+def _lanczos_seconds(api, H, bf, Y, ntri, eps, eng, reps=1):
+    api.lanczos_block(H, bf, Y, ntri, eps, eps, eng)  # warm (graph capture)
+    _sync(eng)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        api.lanczos_block(H, bf, Y, ntri, eps, eps, eng)
+    _sync(eng)
+    return (time.perf_counter() - t0) / reps
+
+
+# ----------------------------------------------------------------------------- served
+
+def make_stream(njobs, seed=0, max_det=2e6, min_det=1e3, eigen_frac=0.25):
+    """Seeded mixed jobs: (kind, params) with target sizes log-uniform in [min_det, max_det]."""
+    from . import workloads
+    rng = np.random.default_rng(seed)
+    out = []
+    for j in range(njobs):
+        target = math.exp(rng.uniform(math.log(min_det), math.log(max_det)))
+        nshell = int(rng.integers(1, 7))
+        delta = float(rng.uniform(1.0, 6.0))
+        v = float(rng.uniform(0.5, 3.0))
+        bath_seed = int(rng.integers(0, 1 << 30))
+        eps = np.sort(np.random.default_rng(bath_seed).uniform(-5.0, 5.0, nshell))
+        nfill = int((eps < 0).sum())
+        best = None
+        for hm in range(0, 4):
+            for pm in range(0, 4):
+                n = workloads.sector_size(nfill, nshell - nfill, hole_max=hm, particle_max=pm)
+                d = abs(math.log(n) - math.log(target))
+                if best is None or d < best[0]:
+                    best = (d, hm, pm, n)
+        kind = "eigen" if rng.random() < eigen_frac else "spectra"
+        out.append({"kind": kind, "nshell": nshell, "delta": delta, "v": v, "seed": bath_seed,
+                    "hole_max": best[1], "particle_max": best[2], "sector": best[3],
+                    "ntri": int(rng.integers(150, 1001)), "ne": int(rng.integers(1024, 4097))})
+    return out
+
+
+def build_job(api, serve, workloads, p):
+    H, R, seed, info = workloads.anderson_impurity(nshell=p["nshell"], seed=p["seed"], delta=p["delta"],
+                                                   v2_total=p["v"] ** 2, hole_max=p["hole_max"],
+                                                   particle_max=p["particle_max"])
+    seed_b = api.dets_to_bytes([seed], H.nf)
+    if p["kind"] == "eigen":
+        return serve.EigenJob(H, R, 2, None, n_det_hint=p["sector"], seed_dets=seed_b)
+    _, Rx, _, _ = workloads.anderson_impurity(nshell=p["nshell"], seed=p["seed"], delta=p["delta"],
+                                              v2_total=p["v"] ** 2, hole_max=p["hole_max"],
+                                              particle_max=p["particle_max"], core_holes=1)
+    Ts = _xas_ops(api, workloads, H.nf)
+    psi = api.Wavefunction(H.nf, seed_b, np.ones(1, dtype=np.complex128))
+    o = {"NTri": p["ntri"], "NE": p["ne"], "Emin": -20.0, "Emax": 20.0, "Gamma": 0.5, "Restrictions": Rx}
+    return serve.SpectraJob(H, Ts, [psi], o, n_det_hint=6 * p["sector"])
+
+
+def served(args):
+    from . import api, serve, workloads
+    params = make_stream(int(args.jobs), seed=0, max_det=float(args.max_det))
+    jobs = [build_job(api, serve, workloads, p) for p in params]
+    nspec = sum(j.nspec for j in jobs)
+    rate = float(args.rate)
+    # warm-up: one small job of each kind through both paths (builds, graphs)
+    warm = sorted(range(len(jobs)), key=lambda k: params[k]["sector"])[:2]
+    eng = api.engine()
+    for k in warm:
+        jobs[k].run(eng)
+    _sync(eng)
+    res_s, lat_s, wall_s = serve.run_stream(jobs, rate, slots=int(args.slots), seed=1)
+    res_p, lat_p, wall_p = serve.run_plain(jobs, rate, seed=1, eng=eng)
+    diff = 0.0
+    for a, b in zip(res_s, res_p):
+        if "G" in a:
+            diff = max(diff, float(np.max(np.abs(a["G"] - b["G"])) / np.max(np.abs(b["G"]))))
+        else:
+            diff = max(diff, float(np.max(np.abs(a["energies"] - b["energies"]))))
+    sizes = [p["sector"] * (6 if p["kind"] == "spectra" else 1) for p in params]
+    line = {
+        "metric": "served CreateSpectra/Eigensystem spectra/s",
+        "value": nspec / wall_s,
+        "unit": "spectra/s",
+        "mode": "served",
+        "n_gpus": 1,
+        "higher_is_better": True,
+        "dtype": "c128",
+        "data": "synthetic (seeded impurity Hamiltonians, Poisson arrivals)",
+        "config": {"workload": "poisson_stream_mixed_impurity_jobs", "jobs": len(jobs), "rate_per_s": rate,
+                   "slots": int(args.slots), "spectra": nspec,
+                   "eigen_jobs": sum(p["kind"] == "eigen" for p in params),
+                   "max_det": float(args.max_det), "determinants_min": int(min(sizes)),
+                   "determinants_max": int(max(sizes))},
+        "served": {"wall_s": wall_s, "spectra_per_s": nspec / wall_s, "jobs_per_s": len(jobs) / wall_s,
+                   "p50_s": float(np.percentile(lat_s, 50)), "p99_s": float(np.percentile(lat_s, 99))},
+        "plain": {"wall_s": wall_p, "spectra_per_s": nspec / wall_p, "jobs_per_s": len(jobs) / wall_p,
+                  "p50_s": float(np.percentile(lat_p, 50)), "p99_s": float(np.percentile(lat_p, 99))},
+        "speedup_vs_plain": wall_p / wall_s,
+        "max_diff_served_vs_plain": diff,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main(args):
+    if args.mode == "batched":
+        return batched(args)
+    return served(args)

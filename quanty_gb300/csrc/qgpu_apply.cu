@@ -151,6 +151,27 @@ __device__ __forceinline__ uint64_t window_bits(const Key<W> &d, const SrcView &
   return ok;
 }
 
+// FP64 arithmetic on this GPU issues at 2 FMA per clock per SM, and the apply kernel spends
+// most of its issue slots there, so FP64 work per connection is kept minimal: the parity sign
+// is an integer flip of the sign bits, and a term with a real value (every hopping, Coulomb
+// and one-body real term) costs two FMAs per vector instead of four.  A zero imaginary part
+// contributes fma(-0, x, acc) == acc exactly, so both forms give the same bits.
+__device__ __forceinline__ double qg_flip_sign(double v, int par) {
+  return __longlong_as_double(__double_as_longlong(v) ^ ((long long)(par & 1) << 63));
+}
+
+__device__ __forceinline__ bool qg_is_nonzero(double v) { return (__double_as_longlong(v) << 1) != 0; }
+
+// acc += (vr + i vi) xv, in the operation order of the complex form
+__device__ __forceinline__ void qg_cmac(double2 &acc, double vr, double vi, bool cplx, double2 xv) {
+  if (cplx) {
+    acc.x = fma(-vi, xv.y, acc.x);
+    acc.y = fma(vi, xv.x, acc.y);
+  }
+  acc.x = fma(vr, xv.x, acc.x);
+  acc.y = fma(vr, xv.y, acc.y);
+}
+
 template <int W, int NV, bool FUSE, bool SMEM>
 __global__ void __launch_bounds__(256) k_apply(const Key<W> *__restrict__ rows, int64_t n_rows,
                                                const unsigned char *__restrict__ gtab, uint32_t tab_bytes,
@@ -176,11 +197,20 @@ __global__ void __launch_bounds__(256) k_apply(const Key<W> *__restrict__ rows, 
     Key<W> d = rows[r];
     if (diag) {
       double2 dg = diag[r];
+      if (qg_is_nonzero(dg.y)) {
 #pragma unroll
-      for (int k = 0; k < NV; k++) {
-        double2 xv = x[r * xs + vec0 + k];
-        acc[k].x = dg.x * xv.x - dg.y * xv.y;
-        acc[k].y = dg.x * xv.y + dg.y * xv.x;
+        for (int k = 0; k < NV; k++) {
+          double2 xv = x[r * xs + vec0 + k];
+          acc[k].x = dg.x * xv.x - dg.y * xv.y;
+          acc[k].y = dg.x * xv.y + dg.y * xv.x;
+        }
+      } else {  // Hermitian operators: real diagonal
+#pragma unroll
+        for (int k = 0; k < NV; k++) {
+          double2 xv = x[r * xs + vec0 + k];
+          acc[k].x = dg.x * xv.x;
+          acc[k].y = dg.x * xv.y;
+        }
       }
     }
     uint64_t okm = 0;
@@ -212,12 +242,9 @@ __global__ void __launch_bounds__(256) k_apply(const Key<W> *__restrict__ rows, 
           j = (int64_t)__ldg(src.slot_row + h);
         }
         double vr = __ldg(&E->vre), vi = __ldg(&E->vim);
+        bool cplx = qg_is_nonzero(vi);
 #pragma unroll
-        for (int k = 0; k < NV; k++) {
-          double2 xv = __ldg(x + j * xs + vec0 + k);
-          acc[k].x = fma(vr, xv.x, fma(-vi, xv.y, acc[k].x));
-          acc[k].y = fma(vr, xv.y, fma(vi, xv.x, acc[k].y));
-        }
+        for (int k = 0; k < NV; k++) qg_cmac(acc[k], vr, vi, cplx, __ldg(x + j * xs + vec0 + k));
       }
     }
     for (int g = 0; g < ngroups; g++) {
@@ -260,11 +287,10 @@ __global__ void __launch_bounds__(256) k_apply(const Key<W> *__restrict__ rows, 
         int par = 0;
 #pragma unroll
         for (int i = 0; i < W; i++) par += __popcll(d.w[i] & T.sgn[i]);
-        double vr = T.vre, vi = T.vim;
-        if (par & 1) {
-          vr = -vr;
-          vi = -vi;
-        }
+        double vi = T.vim;
+        bool cplx = qg_is_nonzero(vi);
+        double vr = qg_flip_sign(T.vre, par);
+        vi = qg_flip_sign(vi, par);
 #pragma unroll
         for (int k = 0; k < NV; k++) {
           double2 xv;
@@ -272,8 +298,7 @@ __global__ void __launch_bounds__(256) k_apply(const Key<W> *__restrict__ rows, 
             xv = __ldg(reinterpret_cast<const double2 *>(src.slots + h) + 1);
           else
             xv = __ldg(x + j * xs + vec0 + k);
-          acc[k].x = fma(vr, xv.x, fma(-vi, xv.y, acc[k].x));
-          acc[k].y = fma(vr, xv.y, fma(vi, xv.x, acc[k].y));
+          qg_cmac(acc[k], vr, vi, cplx, xv);
         }
       }
     }
@@ -344,10 +369,10 @@ static void launch_apply_t(qg_context ctx, const HostTable &tab, const double2 *
 template <int W, bool FUSE, bool SMEM>
 static void launch_apply_w(qg_context ctx, const HostTable &tab, const double2 *diag, qg_basis dst, qg_basis src,
                            int packed, const double2 *x, int xs, double2 *y, int ys, int nvec, const ApplyFuse &fz,
-                           const LocalView &lv, const uint64_t *wreq) {
+                           const LocalView &lv, const uint64_t *wreq, int chunk) {
   int v = 0;
   while (v < nvec) {
-    int left = nvec - v;
+    int left = std::min(nvec - v, chunk);
     if (left >= 8) {
       launch_apply_t<W, 8, FUSE, SMEM>(ctx, tab, diag, dst, src, 0, x, xs, y, ys, v, fz, lv, wreq);
       v += 8;
@@ -367,11 +392,11 @@ static void launch_apply_w(qg_context ctx, const HostTable &tab, const double2 *
 template <int W, bool FUSE>
 static void launch_apply_s(qg_context ctx, const HostTable &tab, const double2 *diag, qg_basis dst, qg_basis src,
                            int packed, const double2 *x, int xs, double2 *y, int ys, int nvec, const ApplyFuse &fz,
-                           const LocalView &lv, const uint64_t *wreq) {
+                           const LocalView &lv, const uint64_t *wreq, int chunk) {
   if (tab.bytes <= QG_SMEM_TABLE_MAX)
-    launch_apply_w<W, FUSE, true>(ctx, tab, diag, dst, src, packed, x, xs, y, ys, nvec, fz, lv, wreq);
+    launch_apply_w<W, FUSE, true>(ctx, tab, diag, dst, src, packed, x, xs, y, ys, nvec, fz, lv, wreq, chunk);
   else
-    launch_apply_w<W, FUSE, false>(ctx, tab, diag, dst, src, packed, x, xs, y, ys, nvec, fz, lv, wreq);
+    launch_apply_w<W, FUSE, false>(ctx, tab, diag, dst, src, packed, x, xs, y, ys, nvec, fz, lv, wreq, chunk);
 }
 
 // ------------------------------------------------------------------ pack
@@ -692,8 +717,78 @@ OpBasisCache *qg_basis_cache(qg_basis b, qg_operator op, qg_status *st) {
 
 // ------------------------------------------------------------------ entry points
 
+static int tuned_chunk(const OpBasisCache *c, int nvec) {
+  if (c)
+    for (auto &p : c->chunk)
+      if (p.first == nvec) return p.second;
+  return 0;
+}
+
+static qg_status apply_chunked(qg_context ctx, qg_operator op, qg_basis dst, qg_basis src, const double *x, int xs,
+                               double *y, int ys, int nvec, const ApplyFuse *fz, bool x_packed, int chunk);
+
+// The autotuner: the first multi-vector apply of an operator on a basis (outside stream
+// capture) times one plain apply per candidate number of vectors per pass (8, 4, 2, 1) and
+// keeps the fastest for that vector count.  The candidates compute bitwise the same result
+// (each vector's sum runs in the same order), so the choice changes only the speed.
+static qg_status autotune(qg_context ctx, qg_operator op, qg_basis b, OpBasisCache *c, const double *x, int xs,
+                          double *y, int ys, int nvec) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(ctx->stream, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) {
+    cudaGetLastError();
+    return QG_OK;
+  }
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+    if (e0) cudaEventDestroy(e0);
+    cudaGetLastError();
+    return QG_OK;  // untuned: the default chunk stays
+  }
+  int best = 8;
+  float best_ms = 0;
+  const int cand[4] = {8, 4, 2, 1};
+  qg_status st = QG_OK;
+  for (int i = 0; i < 4 && st == QG_OK; i++) {
+    int ch = cand[i];
+    if (ch > nvec && ch != 8) continue;
+    if (i == 0) st = apply_chunked(ctx, op, b, b, x, xs, y, ys, nvec, nullptr, false, ch);  // warm
+    cudaEventRecord(e0, ctx->stream);
+    if (st == QG_OK) st = apply_chunked(ctx, op, b, b, x, xs, y, ys, nvec, nullptr, false, ch);
+    cudaEventRecord(e1, ctx->stream);
+    float ms = 0;
+    if (st == QG_OK && cudaEventSynchronize(e1) == cudaSuccess && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess) {
+      if (i == 0 || ms < best_ms) {
+        best = ch;
+        best_ms = ms;
+      }
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaGetLastError();
+  if (st == QG_OK) c->chunk.push_back({nvec, best});
+  return st;
+}
+
 qg_status qg_apply_strided(qg_context ctx, qg_operator op, qg_basis dst, qg_basis src, const double *x, int xs,
                            double *y, int ys, int nvec, const ApplyFuse *fz, bool x_packed) {
+  int chunk = 8;
+  if (dst == src && nvec >= 2) {
+    qg_status st = QG_OK;
+    OpBasisCache *c = qg_basis_cache(dst, op, &st);
+    if (st != QG_OK) return st;
+    chunk = tuned_chunk(c, nvec);
+    if (!chunk && ctx->autotune) {
+      QG_TRY(autotune(ctx, op, dst, c, x, xs, y, ys, nvec));
+      chunk = tuned_chunk(c, nvec);
+    }
+    if (!chunk) chunk = 8;
+  }
+  return apply_chunked(ctx, op, dst, src, x, xs, y, ys, nvec, fz, x_packed, chunk);
+}
+
+static qg_status apply_chunked(qg_context ctx, qg_operator op, qg_basis dst, qg_basis src, const double *x, int xs,
+                               double *y, int ys, int nvec, const ApplyFuse *fz, bool x_packed, int chunk) {
   ApplyFuse none;
   const double2 *x2 = (const double2 *)x;
   double2 *y2 = (double2 *)y;
@@ -729,14 +824,14 @@ qg_status qg_apply_strided(qg_context ctx, qg_operator op, qg_basis dst, qg_basi
   const ApplyFuse &f = fz ? *fz : none;
   if (op->W == 1) {
     if (fz)
-      launch_apply_s<1, true>(ctx, *tab, diag, dst, src, packed, x2, xs, y2, ys, nvec, f, lv, wreq);
+      launch_apply_s<1, true>(ctx, *tab, diag, dst, src, packed, x2, xs, y2, ys, nvec, f, lv, wreq, chunk);
     else
-      launch_apply_s<1, false>(ctx, *tab, diag, dst, src, packed, x2, xs, y2, ys, nvec, f, lv, wreq);
+      launch_apply_s<1, false>(ctx, *tab, diag, dst, src, packed, x2, xs, y2, ys, nvec, f, lv, wreq, chunk);
   } else {
     if (fz)
-      launch_apply_s<2, true>(ctx, *tab, diag, dst, src, packed, x2, xs, y2, ys, nvec, f, lv, wreq);
+      launch_apply_s<2, true>(ctx, *tab, diag, dst, src, packed, x2, xs, y2, ys, nvec, f, lv, wreq, chunk);
     else
-      launch_apply_s<2, false>(ctx, *tab, diag, dst, src, packed, x2, xs, y2, ys, nvec, f, lv, wreq);
+      launch_apply_s<2, false>(ctx, *tab, diag, dst, src, packed, x2, xs, y2, ys, nvec, f, lv, wreq, chunk);
   }
   return qg_check_launch(ctx, "qg_apply");
 }
@@ -843,6 +938,20 @@ static qg_status count_nnz(qg_context ctx, qg_operator op, qg_basis b, int offdi
 extern "C" qg_status qg_count_nnz(qg_context ctx, qg_operator op, qg_basis b, int64_t *nnz) {
   if (!ctx || !op || !b || !nnz || op->nf != b->nf) return QG_ERR_ARG;
   return count_nnz(ctx, op, b, 0, nnz);
+}
+
+extern "C" qg_status qg_set_autotune(qg_context ctx, int32_t on) {
+  if (!ctx) return QG_ERR_ARG;
+  ctx->autotune = on != 0;
+  return QG_OK;
+}
+
+extern "C" qg_status qg_apply_chunk(qg_context ctx, qg_operator op, qg_basis b, int32_t nvec, int32_t *chunk) {
+  if (!ctx || !op || !b || !chunk || nvec <= 0) return QG_ERR_ARG;
+  *chunk = 0;
+  for (auto &c : b->caches)
+    if (c.op_uid == op->uid) *chunk = tuned_chunk(&c, nvec);
+  return QG_OK;
 }
 
 extern "C" qg_status qg_count_nnz_offdiag(qg_context ctx, qg_operator op, qg_basis b, int64_t *nnz) {

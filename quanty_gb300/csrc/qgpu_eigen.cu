@@ -237,7 +237,11 @@ extern "C" qg_status qg_block_groundstate(qg_context ctx, qg_operator op, qg_bas
   int it = 0;
   bool converged = false;
   std::vector<cd> c, T;
+  // Krylov dimension per restart: starts at p + 100 and grows by p + 10 per restart up to K
+  // (the reference's NKrylovStart / NKrylovStep schedule, Core/BlockLanczos.cpp:5130, :5311)
+  int Kcur = std::min(K, std::max(2 * p, ((p + 100) / p) * p));
   for (int restart = 0; restart <= max_restarts && st == QG_OK && !converged; restart++) {
+    if (restart > 0) Kcur = std::min(K, ((Kcur + p + 10) / p) * p);
     // V[:, 0:p] = X, orthonormalised (modified Gram-Schmidt, twice)
     k_copy_cols<<<grid(n * p), 256, 0, s>>>(X, p, 0, V, K, 0, p, n);
     ctx->launches++;
@@ -306,7 +310,7 @@ extern "C" qg_status qg_block_groundstate(qg_context ctx, qg_operator op, qg_bas
         k_sub_mul<<<grid(n * bs), 256, 0, s>>>(V, K, 0, k, G.out, W, p, 0, bs, n);
         ctx->launches++;
       }
-      if (st != QG_OK || k + bs > K) break;
+      if (st != QG_OK || k + bs > Kcur) break;
       // append W as new columns and orthonormalise them
       k_copy_cols<<<grid(n * bs), 256, 0, s>>>(W, p, 0, V, K, k, bs, n);
       ctx->launches++;
@@ -325,7 +329,7 @@ extern "C" qg_status qg_block_groundstate(qg_context ctx, qg_operator op, qg_bas
       j0 = k;
       k += kept;
       bs = kept;
-      if (k + bs > K) {
+      if (k + bs > Kcur) {
         // last block: its projections are needed for the Rayleigh quotient
         st = qg_apply_strided(ctx, op, b, b, (const double *)(V + j0), K, (double *)W, p, bs, nullptr);
         it++;

@@ -88,6 +88,7 @@ struct qg_context_s {
   double *d_io = nullptr;             // staging for host-buffer entry points
   size_t io_bytes = 0;
   bool use_graphs = true;             // capture Lanczos step sequences into CUDA graphs
+  bool autotune = true;               // time the vectors-per-pass choices of multi-vector applies
 };
 
 // A term table in one device allocation: ngroups GroupDev followed by nterms TermDev.
@@ -145,6 +146,8 @@ struct OpBasisCache {
   uint32_t *d_eoff = nullptr;     // [nblocks + 1]
   LocalEntry *d_ent = nullptr;
   int64_t nent = 0;
+  // autotuned vectors per pass of the apply kernel, per number of vectors (pairs nvec, chunk)
+  std::vector<std::pair<int, int>> chunk;
 };
 
 struct qg_basis_s {

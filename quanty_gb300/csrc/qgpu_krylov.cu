@@ -65,6 +65,43 @@ __global__ void k_dot_partial(int64_t n, int nvec, const double2 *__restrict__ x
   }
 }
 
+// Several vectors (rows hold nvec consecutive entries): the per-vector loops above would read
+// every row once per vector, a sector at a time.  Here thread t of a block of T = m * nvec
+// threads always sees entries of vector t % nvec while the block walks the flat array in
+// coalesced strides of T; partial sums per vector are then combined through shared memory
+// in a fixed order.
+static int flat_threads(int nvec) {
+  if (nvec <= 256) return nvec * (256 / nvec);
+  return nvec <= 1024 ? nvec : 0;
+}
+
+__global__ void k_dot_partial_flat(int64_t len, int nvec, const double2 *__restrict__ x,
+                                   const double2 *__restrict__ y, double2 *part) {
+  extern __shared__ double2 sh[];
+  int tid = threadIdx.x, T = blockDim.x;
+  double2 s = make_double2(0.0, 0.0);
+  for (int64_t i = blockIdx.x * (int64_t)T + tid; i < len; i += (int64_t)gridDim.x * T) {
+    double2 a = x[i];
+    if (y) {
+      double2 b = y[i];
+      s.x += a.x * b.x + a.y * b.y;
+      s.y += a.x * b.y - a.y * b.x;
+    } else {
+      s.x += a.x * a.x + a.y * a.y;
+    }
+  }
+  sh[tid] = s;
+  __syncthreads();
+  if (tid < nvec) {
+    double2 t = make_double2(0.0, 0.0);
+    for (int j = tid; j < T; j += nvec) {
+      t.x += sh[j].x;
+      t.y += sh[j].y;
+    }
+    part[blockIdx.x * nvec + tid] = t;
+  }
+}
+
 // sum nblk partials per vector (single block); out[k] = sum
 __global__ void k_reduce_partials(const double2 *part, int nblk, int nvec, double2 *out) {
   __shared__ double2 sh[32];
@@ -93,11 +130,19 @@ __global__ void k_reduce_partials(const double2 *part, int nblk, int nvec, doubl
   }
 }
 
+static void launch_dot_partial(int P, int64_t n, int nvec, const double2 *x, const double2 *y, double2 *part,
+                               cudaStream_t s) {
+  int T = nvec > 1 ? flat_threads(nvec) : 0;
+  if (T)
+    k_dot_partial_flat<<<P, T, T * sizeof(double2), s>>>(n * nvec, nvec, x, y, part);
+  else
+    k_dot_partial<<<P, RBLK, (RBLK / 32) * sizeof(double2), s>>>(n, nvec, x, y, part);
+}
+
 qg_status qg_dot_dev(qg_context ctx, int64_t n, int nvec, const double *x, const double *y, double *out_dev) {
   int P = partial_blocks(ctx, n);
   QG_TRY(qg_ensure_scratch(ctx, (size_t)P * nvec * 16));
-  k_dot_partial<<<P, RBLK, (RBLK / 32) * sizeof(double2), ctx->stream>>>(n, nvec, (const double2 *)x,
-                                                                        (const double2 *)y, (double2 *)ctx->d_scratch);
+  launch_dot_partial(P, n, nvec, (const double2 *)x, (const double2 *)y, (double2 *)ctx->d_scratch, ctx->stream);
   k_reduce_partials<<<1, 256, 0, ctx->stream>>>((const double2 *)ctx->d_scratch, P, nvec, (double2 *)out_dev);
   ctx->launches += 2;
   return qg_check_launch(ctx, "dot");
@@ -196,6 +241,29 @@ __global__ void k_lanczos_axpy_norm(int64_t n, int nvec, const double2 *__restri
       part[blockIdx.x * nvec + k] = make_double2(t, 0.0);
     }
     __syncthreads();
+  }
+}
+
+// the same for several vectors, in the flat layout of k_dot_partial_flat
+__global__ void k_lanczos_axpy_norm_flat(int64_t len, int nvec, const double2 *__restrict__ w,
+                                         const double2 *__restrict__ vp, const double *__restrict__ a,
+                                         double2 *__restrict__ v, double2 *part) {
+  extern __shared__ double2 sh[];
+  int tid = threadIdx.x, T = blockDim.x;
+  double ak = a[tid % nvec];
+  double s = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)T + tid; i < len; i += (int64_t)gridDim.x * T) {
+    double2 wv = w[i], pv = vp[i];
+    double2 o = make_double2(wv.x - ak * pv.x, wv.y - ak * pv.y);
+    v[i] = o;
+    s += o.x * o.x + o.y * o.y;
+  }
+  sh[tid].x = s;
+  __syncthreads();
+  if (tid < nvec) {
+    double t = 0;
+    for (int j = tid; j < T; j += nvec) t += sh[j].x;
+    part[blockIdx.x * nvec + tid] = make_double2(t, 0.0);
   }
 }
 
@@ -325,7 +393,7 @@ extern "C" qg_status qg_lanczos_tridiag(qg_context ctx, qg_operator op, qg_basis
     return qg_check_launch(ctx, "scale");
   };
   // step 0: b0 = |v0|, scale, threshold eps (err = 1)
-  k_dot_partial<<<P, RBLK, (RBLK / 32) * sizeof(double2), s>>>(n, nvec, (const double2 *)v0_dev, nullptr, npart);
+  launch_dot_partial(P, n, nvec, (const double2 *)v0_dev, nullptr, npart, s);
   k_fin_b<<<1, 256, 0, s>>>(npart, P, nvec, b_now, b_hist, ntri, 0, scale, thr2, err, eps, gamma, 1);
   ctx->launches += 2;
   ApplyFuse fz;
@@ -345,7 +413,11 @@ extern "C" qg_status qg_lanczos_tridiag(qg_context ctx, qg_operator op, qg_basis
   // into one CUDA graph and launched once (falling back to direct launches if capture fails)
   auto step = [&](int i) -> qg_status {
     std::swap(vp, vc);  // vp = v_{i-1}
-    k_lanczos_axpy_norm<<<P, RBLK, (RBLK / 32) * sizeof(double2), s>>>(n, nvec, w, vp, a_now, vraw, npart);
+    int T = nvec > 1 ? flat_threads(nvec) : 0;
+    if (T)
+      k_lanczos_axpy_norm_flat<<<P, T, T * sizeof(double2), s>>>(len, nvec, w, vp, a_now, vraw, npart);
+    else
+      k_lanczos_axpy_norm<<<P, RBLK, (RBLK / 32) * sizeof(double2), s>>>(n, nvec, w, vp, a_now, vraw, npart);
     k_fin_b<<<1, 256, 0, s>>>(npart, P, nvec, b_now, b_hist, ntri, i, scale, thr2, err, eps, gamma, 0);
     ctx->launches += 2;
     qg_status sst = normalise(vraw);

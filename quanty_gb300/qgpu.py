@@ -56,6 +56,8 @@ def load(path=LIB_PATH):
         "qg_apply_host": (C.c_int, [P, P, P, P, P, P, I32]),
         "qg_count_nnz": (C.c_int, [P, P, P, P]),
         "qg_count_nnz_offdiag": (C.c_int, [P, P, P, P]),
+        "qg_set_autotune": (C.c_int, [P, I32]),
+        "qg_apply_chunk": (C.c_int, [P, P, P, I32, P]),
         "qg_expectation": (C.c_int, [P, P, P, P, I32, P]),
         "qg_dot": (C.c_int, [P, I64, I32, P, P, P]),
         "qg_dot_noalloc": (C.c_int, [I64, I32, P, P, P, P]),

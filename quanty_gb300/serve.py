@@ -1,0 +1,196 @@
+"""Serving form: a request loop for CreateSpectra / Eigensystem jobs.
+
+Jobs of mixed Hilbert-space sizes arrive over time.  The server keeps ``slots`` workers, each
+with its own context and CUDA stream (``api.Engine``) and its own host thread, so the kernels
+of different jobs overlap on the device.  A job is admitted when a slot is free and its
+estimated device footprint fits into the HBM budget next to the jobs already running; it
+keeps its Krylov state on the device until it finishes.  Every job computes exactly what it
+would compute alone (its own context and stream, deterministic kernels), so results in the
+mix equal results alone.
+
+    srv = Server(slots=4, hbm_budget=200e9)
+    fut = srv.submit(SpectraJob(H, [T], [psi], {"NTri": 200, "NE": 2048, ...}))
+    result = fut.result()
+    srv.close()
+"""
+import threading
+import time
+from collections import deque
+from concurrent.futures import Future
+
+import numpy as np
+
+from . import api
+
+
+def _footprint(n_det, nvec, ntri=0, krylov=False):
+    """Device bytes a job holds at its peak (basis, lookup table, Lanczos state)."""
+    keys = 16 * n_det
+    table = 32 * 2 * n_det + 8 * 2 * n_det
+    vectors = 16 * n_det * nvec * 7
+    kry = 16 * n_det * ntri if krylov else 0
+    return int(keys + table + vectors + kry + (64 << 20))
+
+
+class SpectraJob:
+    """CreateSpectra(H, T, psi, options) (LuaInterface/ssp.cpp:1906)."""
+
+    def __init__(self, H, T, psi, options=None, n_det_hint=None, batched=True):
+        self.H, self.T, self.psi, self.options, self.batched = H, T, psi, options or {}, batched
+        self.n_det_hint = n_det_hint
+        self.nspec = len(T) * len(psi)
+
+    def footprint(self):
+        n = self.n_det_hint or max(p.N for p in self.psi) * 8
+        return _footprint(n, self.nspec)
+
+    def run(self, eng):
+        S, tri = api.CreateSpectra(self.H, self.T, self.psi, self.options, eng=eng, batched=self.batched)
+        return {"G": S.G, "tri": tri, "Emin": S.Emin, "Emax": S.Emax, "Gamma": S.Gamma}
+
+
+class EigenJob:
+    """Eigensystem(H, restrictions, Npsi, options) (LuaInterface/ssp.cpp:4039)."""
+
+    def __init__(self, H, restrictions, npsi, options=None, n_det_hint=None, seed_dets=None):
+        self.H, self.R, self.npsi, self.options = H, restrictions, npsi, options or {}
+        self.n_det_hint = n_det_hint
+        self.seed_dets = seed_dets  # basis = closure of these determinants (overlapping masks)
+        self.nspec = 0
+
+    def footprint(self):
+        n = self.n_det_hint or 10000
+        return _footprint(n, self.npsi, ntri=max(8 * self.npsi, 128), krylov=True)
+
+    def run(self, eng):
+        if self.seed_dets is None:
+            psis, E = api.Eigensystem(self.H, self.R, self.npsi, self.options, eng=eng)
+            return {"energies": E, "psi": psis}
+        basis = api.closure(self.H, self.seed_dets, self.H.nf, self.R, -1, eng)
+        x, E = api.EigensystemOnBasis(self.H, basis, self.npsi, self.options, eng)
+        return {"energies": E, "n": basis.n}
+
+
+class Server:
+    """Continuous batching over a fixed set of device slots with HBM-budget admission."""
+
+    def __init__(self, slots=4, hbm_budget=None, device=0):
+        import torch
+        self.torch = torch
+        if hbm_budget is None:
+            free, total = torch.cuda.mem_get_info(device)
+            hbm_budget = int(0.8 * free)
+        self.budget = int(hbm_budget)
+        self.in_use = 0
+        self.queue = deque()
+        self.cv = threading.Condition()
+        self.closed = False
+        prev = torch.cuda.current_stream(device)
+        self.engines = [api.Engine(device) for _ in range(slots)]
+        torch.cuda.set_stream(prev)  # the engines' streams are used only by their workers
+        self.records = []
+        self.threads = [threading.Thread(target=self._worker, args=(e,), daemon=True) for e in self.engines]
+        for t in self.threads:
+            t.start()
+
+    def submit(self, job, arrival=None):
+        fut = Future()
+        rec = {"arrival": arrival if arrival is not None else time.perf_counter(), "job": job, "future": fut}
+        with self.cv:
+            self.queue.append(rec)
+            self.cv.notify_all()
+        return fut
+
+    def _admit(self):
+        """Oldest job whose footprint fits; a job larger than the whole budget runs alone."""
+        for i, rec in enumerate(self.queue):
+            need = rec["job"].footprint()
+            if self.in_use + need <= self.budget or (self.in_use == 0 and need > self.budget):
+                del self.queue[i]
+                self.in_use += need
+                rec["need"] = need
+                return rec
+            break  # first-come first-served: do not overtake a waiting job
+        return None
+
+    def _worker(self, eng):
+        self.torch.cuda.set_stream(eng.stream)
+        while True:
+            with self.cv:
+                rec = None
+                while not self.closed:
+                    rec = self._admit()
+                    if rec is not None:
+                        break
+                    self.cv.wait(0.05)
+                if rec is None:
+                    return
+            rec["start"] = time.perf_counter()
+            try:
+                out = rec["job"].run(eng)
+                self.torch.cuda.current_stream().synchronize()
+                rec["end"] = time.perf_counter()
+                rec["future"].set_result(out)
+            except Exception as exc:  # reported through the future
+                rec["end"] = time.perf_counter()
+                rec["future"].set_exception(exc)
+            with self.cv:
+                self.in_use -= rec["need"]
+                self.records.append(rec)
+                self.cv.notify_all()
+
+    def close(self):
+        with self.cv:
+            self.closed = True
+            self.cv.notify_all()
+        for t in self.threads:
+            t.join()
+        for e in self.engines:
+            e.close()
+
+    def latencies(self):
+        return np.array([r["end"] - r["arrival"] for r in self.records])
+
+
+def run_stream(jobs, rate, slots=4, hbm_budget=None, seed=0, server=None):
+    """Submit jobs at Poisson arrival times (mean `rate` per second); wait for all.
+    Returns (results in submission order, latencies, wall seconds)."""
+    rng = np.random.default_rng(seed)
+    gaps = rng.exponential(1.0 / rate, len(jobs))
+    srv = server or Server(slots=slots, hbm_budget=hbm_budget)
+    t0 = time.perf_counter()
+    futs = []
+    for gap, job in zip(gaps, jobs):
+        target = time.perf_counter() + gap
+        while time.perf_counter() < target:
+            time.sleep(min(0.001, max(0.0, target - time.perf_counter())))
+        futs.append(srv.submit(job, arrival=time.perf_counter()))
+    results = [f.result() for f in futs]
+    wall = time.perf_counter() - t0
+    lat = np.array([r["end"] - r["arrival"] for r in sorted(srv.records, key=lambda r: r["arrival"])])
+    if server is None:
+        srv.close()
+    return results, lat, wall
+
+
+def run_plain(jobs, rate, seed=0, eng=None):
+    """The same stream served one job at a time on one context with one Lanczos per spectrum
+    (the plain GPU path).  Returns (results, latencies, wall seconds)."""
+    rng = np.random.default_rng(seed)
+    gaps = rng.exponential(1.0 / rate, len(jobs))
+    arrivals = np.cumsum(gaps)
+    eng = eng or api.engine()
+    t0 = time.perf_counter()
+    results, lat = [], []
+    for a, job in zip(arrivals, jobs):
+        now = time.perf_counter() - t0
+        if now < a:
+            time.sleep(a - now)
+        if isinstance(job, SpectraJob):
+            plain = SpectraJob(job.H, job.T, job.psi, job.options, job.n_det_hint, batched=False)
+            results.append(plain.run(eng))
+        else:
+            results.append(job.run(eng))
+        eng.torch.cuda.current_stream().synchronize()
+        lat.append(time.perf_counter() - t0 - a)
+    return results, np.array(lat), time.perf_counter() - t0

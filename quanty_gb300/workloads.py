@@ -36,6 +36,15 @@ def atomic():
     return {k: Operator(16, [(t[0], complex(t[1], t[2])) for t in d[k]], name=k) for k in ("H", "HX", "Tx", "Ty", "Tz")}
 
 
+def ligand_field():
+    """The 26-orbital ligand-field ion (2p 0-5, 3d 6-15, ligand 16-25) as the reference builds it
+    (data/ligand_field_26.json): H, HX, Tx, Ty, Tz and the ground-state restrictions."""
+    with open(os.path.join(HERE, "data", "ligand_field_26.json")) as f:
+        d = json.load(f)
+    ops = {k: Operator(26, [(t[0], complex(t[1], t[2])) for t in d[k]], name=k) for k in ("H", "HX", "Tx", "Ty", "Tz")}
+    return ops, [tuple(r) for r in d["restrictions"]]
+
+
 def number_pair(i, j, value):
     """n_i n_j (i != j) in the normal order the reference stores two-body terms in:
     c^dag_a c^dag_b c_a c_b with a > b (ladder codes [b, a, b^dag, a^dag], the rightmost
@@ -57,13 +66,16 @@ def merged(terms):
 
 
 def anderson_impurity(nshell=7, seed=0, udd=7.5, upd=8.5, half_width=2.0, v2_total=4.0, hole_max=3,
-                      particle_max=2, field=0.01):
+                      particle_max=2, field=0.01, delta=0.0, core_holes=0):
     """Returns (H, restrictions, seed determinant, info dict)."""
     nf = 16 + 10 * nshell
     at = _load()
     terms = [(list(t[0]), complex(t[1], t[2])) for t in at["HX"]]
     d_orb = list(range(6, 16))
     p_orb = list(range(0, 6))
+    if delta:  # charge-transfer shift of the 3d level
+        for d in d_orb:
+            terms.append(([d, d | CREATION], float(delta)))
     for a in range(10):
         for b in range(a + 1, 10):
             terms.append(number_pair(d_orb[a], d_orb[b], udd))
@@ -102,7 +114,7 @@ def anderson_impurity(nshell=7, seed=0, udd=7.5, upd=8.5, half_width=2.0, v2_tot
             s[o] = "1"
         return "".join(s)
 
-    R = [(mask(p_orb), 6, 6)]
+    R = [(mask(p_orb), 6 - core_holes, 6)]
     for k in filled:
         R.append((mask(range(16 + 10 * k, 26 + 10 * k)), 8, 10))
     for k in empty:

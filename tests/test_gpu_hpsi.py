@@ -128,6 +128,34 @@ def test_multivector_apply_equals_single(api):
         assert torch.equal(Y[:, k], yk[:, 0])  # same rows, same order of summation
 
 
+def test_autotuned_chunk_gives_the_same_bits(api):
+    """The autotuner picks the vectors per kernel pass; every choice sums in the same order."""
+    import ctypes
+    import torch
+    rng = np.random.default_rng(6)
+    nf = 30
+    H = _random_operator(api, nf, 60, 60, rng)
+    seed = api.dets_to_bytes(["1" * 8 + "0" * 22], nf)
+    eng = api.engine()
+    b1 = api.closure(H, seed, nf, None, 2)
+    b2 = api.closure(H, seed, nf, None, 2)
+    n = b1.n
+    X = torch.from_numpy(rng.normal(size=(n, 13)) + 1j * rng.normal(size=(n, 13))).cuda()
+    Y1, Y2 = eng.empty(n, 13), eng.empty(n, 13)
+    ch = ctypes.c_int32()
+    try:
+        eng.check(eng.L.qg_apply(eng.ctx, H.handle(), b1.h, b1.h, api._ptr(X), api._ptr(Y1), 13))
+        eng.check(eng.L.qg_apply_chunk(eng.ctx, H.handle(), b1.h, 13, ctypes.byref(ch)))
+        assert ch.value in (1, 2, 4, 8)
+        eng.check(eng.L.qg_set_autotune(eng.ctx, 0))
+        eng.check(eng.L.qg_apply(eng.ctx, H.handle(), b2.h, b2.h, api._ptr(X), api._ptr(Y2), 13))
+        eng.check(eng.L.qg_apply_chunk(eng.ctx, H.handle(), b2.h, 13, ctypes.byref(ch)))
+        assert ch.value == 0  # untuned: passes of 8 vectors
+    finally:
+        eng.check(eng.L.qg_set_autotune(eng.ctx, 1))
+    assert torch.equal(Y1, Y2)
+
+
 def test_edge_cases(api):
     H = api.NewOperator(4, 0, [[0, -1, 0.5], [1, -0.0, 0.5]])
     empty = api.Wavefunction(4, np.zeros((0, 1), np.uint8), [])

@@ -1,0 +1,49 @@
+"""Admission logic of the serving loop, without a GPU: first come first served, a job waits
+while the HBM budget is taken, a job larger than the whole budget runs alone."""
+import collections
+import threading
+
+from quanty_gb300 import serve
+
+
+class FakeJob:
+    def __init__(self, need):
+        self.need = need
+
+    def footprint(self):
+        return self.need
+
+
+def server(budget):
+    s = serve.Server.__new__(serve.Server)
+    s.budget = budget
+    s.in_use = 0
+    s.queue = collections.deque()
+    s.cv = threading.Condition()
+    return s
+
+
+def test_fifo_and_budget():
+    s = server(100)
+    for need in (40, 50, 30, 10):
+        s.queue.append({"job": FakeJob(need)})
+    a = s._admit()
+    b = s._admit()
+    assert (a["need"], b["need"]) == (40, 50) and s.in_use == 90
+    assert s._admit() is None          # 30 does not fit next to 90, and 10 may not overtake it
+    s.in_use -= 40
+    assert s._admit()["need"] == 30
+    assert s._admit()["need"] == 10
+
+
+def test_oversized_job_runs_alone():
+    s = server(100)
+    s.queue.append({"job": FakeJob(500)})
+    s.in_use = 10
+    assert s._admit() is None
+    s.in_use = 0
+    assert s._admit()["need"] == 500
+
+
+def test_footprint_grows_with_size():
+    assert serve._footprint(10 ** 6, 4) > serve._footprint(10 ** 5, 4) > 0
