@@ -15,6 +15,7 @@ sources are not there).  With N > 1 every rank runs an independent replica (the 
 shard); rank 0 prints the line.
 """
 import argparse
+import ctypes as C
 import json
 import os
 import re
@@ -50,6 +51,7 @@ def parse():
     p.add_argument("--max-det", type=float, default=2e6)
     p.add_argument("--rate", type=float, default=50.0)
     p.add_argument("--slots", type=int, default=4)
+    p.add_argument("--restarts", type=int, default=20)
     return p.parse_args()
 
 
@@ -265,6 +267,11 @@ def main():
     nterms = H.info()["nterms"]
     nnz = api.count_nnz(H, basis)
     nnz_off = api.count_nnz(H, basis, offdiag=True)
+    # connections through the hash table: one-body moves that change a bath orbital (the rest
+    # of the off-diagonal connections are local moves at a predicted offset, coalesced)
+    hop_terms = [(o, v) for o, v in H.terms
+                 if len(o) == 2 and (o[0] & 0x7FFF) != (o[1] & 0x7FFF) and max(o[0] & 0x7FFF, o[1] & 0x7FFF) >= 16]
+    nnz_hop = api.count_nnz(api.Operator(H.nf, hop_terms), basis) if hop_terms else 0
     # CPU baseline in a background thread (ctypes releases the GIL) while the GPU is timed
     cpu = {}
     cpu_thread = None
@@ -344,13 +351,21 @@ def main():
     alg_bytes_off = n * (W + 16 + 16) + nnz_off * 16 + term_bytes
     peak, peak_kind = measured_peak()
     achieved = alg_bytes / (ms * 1e-3) / 1e9
+    # two-ceiling model of the same launch: coalesced bytes at the copy bandwidth, hash-probed
+    # (random 32-byte sector) reads and the pack step's scattered writes at the random-sector
+    # gather bandwidth measured here
+    gbs = C.c_double(0.0)
+    eng.check(eng.L.qg_gather_bandwidth(eng.ctx, 4 << 30, C.byref(gbs)))
+    coalesced = n * (16 + 4 + 16 + 16 + 16) + (nnz_off - nnz_hop) * 16 + term_bytes
+    random_sectors = n + nnz_hop
+    t_bound = coalesced / (peak * 1e9) + random_sectors * 32 / (gbs.value * 1e9)
     achieved_off = alg_bytes_off / (ms * 1e-3) / 1e9
     line = {
         "metric": "H·ψ det·terms/s", "value": value, "unit": "Gdet·terms/s", "n_gpus": world, "steps": args.steps,
         "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "c128", "data": "synthetic",
         "config": {"workload": "anderson_impurity_86so_hpsi", "n_det": n, "n_terms": nterms, "nnz": nnz,
-                   "nnz_offdiag": nnz_off,
+                   "nnz_offdiag": nnz_off, "nnz_hash_probed": nnz_hop,
                    "det_words_bits": 128, "l2": "inputs larger than L2 (x, y %d MB each)" % (n * 16 // 2**20),
                    "setup_s": round(t_setup, 2), "parallelism": "replicas" if world > 1 else "single"},
         "e2e": {"value": e2e_val, "unit": "Gdet·terms/s", "h2d_bytes_per_step": n * 16, "d2h_bytes_per_step": n * 16,
@@ -358,7 +373,10 @@ def main():
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": profiled_traffic(), "peak_source": peak_kind,
                      "algorithmic_bytes_per_launch": alg_bytes,
-                     "achieved_offdiagonal_only": achieved_off, "frac_offdiagonal_only": achieved_off / peak},
+                     "achieved_offdiagonal_only": achieved_off, "frac_offdiagonal_only": achieved_off / peak,
+                     "two_ceiling": {"coalesced_bytes": coalesced, "random_sectors": random_sectors,
+                                     "gather_peak_gbs": gbs.value, "bound_ms": t_bound * 1e3,
+                                     "frac": t_bound * 1e3 / ms}},
         "cpu_baseline": cpu or None,
         "clocks": clk,
         "gpu_launches": launches,

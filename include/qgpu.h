@@ -135,6 +135,18 @@ qg_status qg_basis_map(qg_context ctx, qg_basis src, const double *x_dev, qg_bas
 qg_status qg_apply(qg_context ctx, qg_operator op, qg_basis basis_dst, qg_basis basis_src,
                    const double *x_dev, double *y_dev, int32_t nvec);
 
+/* Random-sector gather bandwidth of the device in GB/s (no counterpart in the reference):
+ * reads of 32-byte sectors at unrelated addresses spread over a buffer of `bytes` (>= 1 MiB,
+ * allocated and freed here).  The ceiling for hash-probed gathers, measured for the roofline. */
+qg_status qg_gather_bandwidth(qg_context ctx, int64_t bytes, double *gbs);
+
+/* Eigenpairs of a small dense Hermitian matrix on the host: a is k x k row-major with
+ * interleaved (re, im); w receives all k eigenvalues ascending, v (k x nv row-major,
+ * interleaved) the eigenvectors of the lowest nv as columns.  Householder reduction, implicit
+ * QL.  Replaces the reference's zheevd calls on projected matrices (Core/BlockLanczos.cpp:5530).
+ * No device work. */
+qg_status qg_hermitian_eigh(int32_t k, const double *a, double *w, double *v, int32_t nv);
+
 /* Autotuning of the multi-vector apply (no counterpart in the reference, whose loops handle one
  * vector at a time): the first apply of an operator with nvec >= 2 vectors on a basis (as
  * its own source and target, outside stream capture) times each number of vectors handled per
@@ -209,7 +221,10 @@ qg_status qg_cf_spectra(qg_context ctx, int32_t nspec, int32_t ntri, const doubl
  * Lanczos with full reorthogonalisation (BlockLanczosGroundStateConserveBasis,
  * Core/BlockLanczos.cpp:5707, its Krylov solver :5350).  x_dev holds nvec start vectors
  * on input (n * nvec) and the eigenvectors on output; energies_host nvec doubles.
- * tol is the reference's "Zero" (variance convergence), max_krylov its NKrylovMax. */
+ * tol is the reference's "Zero" (variance convergence); max_krylov caps the Krylov space,
+ * which starts at nvec + 100 vectors and grows by nvec + 10 per restart (NKrylovStart,
+ * NKrylovStep).  For nvec > 3 up to min(nvec/2, 8) guard vectors join the block; only the
+ * nvec wanted states must converge. */
 qg_status qg_block_groundstate(qg_context ctx, qg_operator op, qg_basis basis, int32_t nvec,
                                double *x_dev, double *energies_host, double tol, int32_t max_krylov,
                                int32_t max_restarts, int32_t *iterations);

@@ -611,9 +611,11 @@ def Eigensystem(H, StartRestrictions, Npsi, options=None, eng=None, seed=12345):
     return out, en
 
 
-def EigensystemOnBasis(H, basis, Npsi, options=None, eng=None, seed=12345):
+def EigensystemOnBasis(H, basis, Npsi, options=None, eng=None, seed=12345, max_restarts=200, status=None):
     """Lowest Npsi eigenpairs of H on a device basis, kept on the device: returns
-    ((n, Npsi) complex CUDA tensor, energies)."""
+    ((n, Npsi) complex CUDA tensor, energies).  With a dict `status`, a restart limit reached
+    before convergence returns the current Ritz pairs and sets status["converged"] = False
+    (otherwise it raises)."""
     eng = eng or engine()
     o = _opts(options)
     n = basis.n
@@ -628,8 +630,15 @@ def EigensystemOnBasis(H, basis, Npsi, options=None, eng=None, seed=12345):
     free = eng.torch.cuda.mem_get_info(eng.device)[0]
     K = int(min(Npsi + int(o["NKrylovMax"]), n, max(2 * Npsi, free // (2 * 16 * max(n, 1)))))
     tol = float(o["Zero"])
-    eng.check(eng.L.qg_block_groundstate(eng.ctx, H.handle(eng), basis.h, Npsi, _ptr(x), _ptr(en), tol, K, 200,
-                                         C.byref(it)))
+    st = eng.L.qg_block_groundstate(eng.ctx, H.handle(eng), basis.h, Npsi, _ptr(x), _ptr(en), tol, K,
+                                    int(max_restarts), C.byref(it))
+    if status is not None:
+        status["converged"] = st == 0
+        status["applies"] = it.value
+        status["krylov_max"] = K
+        if st == qgpu.QG_ERR_TIMEOUT:
+            st = 0
+    eng.check(st)
     return x, en
 
 

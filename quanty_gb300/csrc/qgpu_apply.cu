@@ -24,6 +24,7 @@
 
 #include <algorithm>
 #include <map>
+#include <tuple>
 
 #include "qgpu_internal.cuh"
 
@@ -175,8 +176,9 @@ __device__ __forceinline__ void qg_cmac(double2 &acc, double vr, double vi, bool
 template <int W, int NV, bool FUSE, bool SMEM>
 __global__ void __launch_bounds__(256) k_apply(const Key<W> *__restrict__ rows, int64_t n_rows,
                                                const unsigned char *__restrict__ gtab, uint32_t tab_bytes,
-                                               int ngroups, const double2 *__restrict__ diag, SrcView src,
-                                               int packed, int same_basis, const double2 *__restrict__ x, int xs,
+                                               int ngroups, int nhop, uint64_t hop0, uint64_t hop1,
+                                               const double2 *__restrict__ diag, SrcView src, int packed,
+                                               int same_basis, const double2 *__restrict__ x, int xs,
                                                double2 *__restrict__ y, int ys, int vec0, ApplyFuse fz,
                                                LocalView lv, const uint64_t *__restrict__ wreq,
                                                unsigned int *err) {
@@ -216,30 +218,34 @@ __global__ void __launch_bounds__(256) k_apply(const Key<W> *__restrict__ rows, 
     uint64_t okm = 0;
     if (wreq && src.nres) okm = window_bits<W>(d, src);
     if (lv.on) {
-      // local moves: targets in another block at the same offset (coalesced), else probed
+      // local moves: the target sits in another block at the same offset; when the two blocks
+      // list the same non-local configurations (flag bit 31 of tblock) that is certain,
+      // otherwise a key comparison checks it and a miss falls back to the hash table
       int b = __ldg(lv.cfg + get_local<W>(d, lv.lo, lv.lmask));
       uint32_t rs = __ldg(lv.bstart + b);
       int64_t off = r - (int64_t)rs;
       uint32_t e1 = __ldg(lv.eoff + b + 1);
       for (uint32_t e = __ldg(lv.eoff + b); e < e1; e++) {
         const LocalEntry *E = lv.ent + e;
-        uint32_t tbk = __ldg(&E->tblock);
-        Key<W> s = set_local<W>(d, lv.lo, lv.lmask, __ldg(&E->target));
+        uint32_t tbr = __ldg(&E->tblock);
+        uint32_t tbk = tbr & 0x7FFFFFFFu;
         int64_t j = (int64_t)__ldg(lv.bstart + tbk) + off;
-        int64_t h = -1;
-        bool hit = false;
-        if (j < (int64_t)__ldg(lv.bstart + tbk + 1)) {
-          Key<W> kj = rows[j];
-          hit = qg_eq<W>(kj, s);
-        }
-        if (!hit) {
-          if (src.nres) {
-            uint64_t req = __ldg(&E->wreq);
-            if (wreq ? ((okm & req) != req) : !in_windows<W>(s, src)) continue;
+        if (!(tbr >> 31)) {
+          Key<W> s = set_local<W>(d, lv.lo, lv.lmask, __ldg(&E->target));
+          bool hit = false;
+          if (j < (int64_t)__ldg(lv.bstart + tbk + 1)) {
+            Key<W> kj = rows[j];
+            hit = qg_eq<W>(kj, s);
           }
-          h = qg_find_slot<W>(src.slots, src.hmask, s, err);
-          if (h < 0) continue;
-          j = (int64_t)__ldg(src.slot_row + h);
+          if (!hit) {
+            if (src.nres) {
+              uint64_t req = __ldg(&E->wreq);
+              if (wreq ? ((okm & req) != req) : !in_windows<W>(s, src)) continue;
+            }
+            int64_t h = qg_find_slot<W>(src.slots, src.hmask, s, err);
+            if (h < 0) continue;
+            j = (int64_t)__ldg(src.slot_row + h);
+          }
         }
         double vr = __ldg(&E->vre), vi = __ldg(&E->vim);
         bool cplx = qg_is_nonzero(vi);
@@ -247,7 +253,82 @@ __global__ void __launch_bounds__(256) k_apply(const Key<W> *__restrict__ rows, 
         for (int k = 0; k < NV; k++) qg_cmac(acc[k], vr, vi, cplx, __ldg(x + j * xs + vec0 + k));
       }
     }
-    for (int g = 0; g < ngroups; g++) {
+    // one term of the table: source = row ^ flip, looked up, accumulated with its sign
+    auto term = [&](int t, bool known_applicable) {
+      const TermDev<W> &T = terms[t];
+      if (!known_applicable) {
+        bool app = true;
+#pragma unroll
+        for (int i = 0; i < W; i++) app &= (d.w[i] & T.need0[i]) == 0;
+        if (!app) return;
+      }
+      Key<W> s;
+      bool dg = true;
+#pragma unroll
+      for (int i = 0; i < W; i++) {
+        uint64_t fl = T.flip[i];
+        s.w[i] = d.w[i] ^ fl;
+        dg &= fl == 0;
+      }
+      int64_t h = -1, j = -1;
+      if (dg && same_basis) {
+        j = r;
+      } else {
+        if (src.nres) {
+          if (wreq) {
+            uint64_t req = __ldg(wreq + t);
+            if ((okm & req) != req) return;
+          } else if (!in_windows<W>(s, src)) {
+            return;
+          }
+        }
+        h = qg_find_slot<W>(src.slots, src.hmask, s, err);
+        if (h < 0) return;
+        if (!(NV == 1 && packed)) j = (int64_t)__ldg(src.slot_row + h);
+      }
+      int par = 0;
+#pragma unroll
+      for (int i = 0; i < W; i++) par += __popcll(d.w[i] & T.sgn[i]);
+      double vi = T.vim;
+      bool cplx = qg_is_nonzero(vi);
+      double vr = qg_flip_sign(T.vre, par);
+      vi = qg_flip_sign(vi, par);
+#pragma unroll
+      for (int k = 0; k < NV; k++) {
+        double2 xv;
+        if (NV == 1 && packed && h >= 0)
+          xv = __ldg(reinterpret_cast<const double2 *>(src.slots + h) + 1);
+        else
+          xv = __ldg(x + j * xs + vec0 + k);
+        qg_cmac(acc[k], vr, vi, cplx, xv);
+      }
+    };
+    // hop groups: each occupied orbital p with one-body moves, then each empty target q of it
+    int gbase = 0;
+#pragma unroll
+    for (int i = 0; i < W; i++) {
+      uint64_t hm = i == 0 ? hop0 : hop1;
+      uint64_t m = d.w[i] & hm;
+      while (m) {
+        int bp = __ffsll((long long)m) - 1;
+        m &= m - 1;
+        const GroupDev<W> &G = groups[gbase + __popcll(hm & ((1ull << bp) - 1))];
+        int tq = G.begin;
+#pragma unroll
+        for (int i2 = 0; i2 < W; i2++) {
+          uint64_t qm = G.qmask[i2];
+          uint64_t c = qm & ~d.w[i2];
+          while (c) {
+            int bq = __ffsll((long long)c) - 1;
+            c &= c - 1;
+            term(tq + __popcll(qm & ((1ull << bq) - 1)), true);
+          }
+          tq += __popcll(qm);
+        }
+      }
+      gbase += __popcll(hm);
+    }
+    for (int g = nhop; g < ngroups; g++) {
       bool ok = true;
 #pragma unroll
       for (int i = 0; i < W; i++) {
@@ -256,51 +337,7 @@ __global__ void __launch_bounds__(256) k_apply(const Key<W> *__restrict__ rows, 
       }
       if (!ok) continue;
       int tb = groups[g].begin, te = groups[g].end;
-      for (int t = tb; t < te; t++) {
-        const TermDev<W> &T = terms[t];
-        bool app = true, dg = true;
-        Key<W> s;
-#pragma unroll
-        for (int i = 0; i < W; i++) {
-          app &= (d.w[i] & T.need0[i]) == 0;
-          uint64_t fl = T.flip[i];
-          s.w[i] = d.w[i] ^ fl;
-          dg &= fl == 0;
-        }
-        if (!app) continue;
-        int64_t h = -1, j = -1;
-        if (dg && same_basis) {
-          j = r;
-        } else {
-          if (src.nres) {
-            if (wreq) {
-              uint64_t req = __ldg(wreq + t);
-              if ((okm & req) != req) continue;
-            } else if (!in_windows<W>(s, src)) {
-              continue;
-            }
-          }
-          h = qg_find_slot<W>(src.slots, src.hmask, s, err);
-          if (h < 0) continue;
-          if (!(NV == 1 && packed)) j = (int64_t)__ldg(src.slot_row + h);
-        }
-        int par = 0;
-#pragma unroll
-        for (int i = 0; i < W; i++) par += __popcll(d.w[i] & T.sgn[i]);
-        double vi = T.vim;
-        bool cplx = qg_is_nonzero(vi);
-        double vr = qg_flip_sign(T.vre, par);
-        vi = qg_flip_sign(vi, par);
-#pragma unroll
-        for (int k = 0; k < NV; k++) {
-          double2 xv;
-          if (NV == 1 && packed && h >= 0)
-            xv = __ldg(reinterpret_cast<const double2 *>(src.slots + h) + 1);
-          else
-            xv = __ldg(x + j * xs + vec0 + k);
-          qg_cmac(acc[k], vr, vi, cplx, xv);
-        }
-      }
+      for (int t = tb; t < te; t++) term(t, false);
     }
   }
   if (!FUSE) {
@@ -361,8 +398,9 @@ static void launch_apply_t(qg_context ctx, const HostTable &tab, const double2 *
   SrcView sv{src->d_slots, src->d_slot_row, (uint64_t)(src->hcap - 1), src->nres, src->d_rmask, src->d_rmin,
              src->d_rmax};
   k_apply<W, NV, FUSE, SMEM><<<qg_apply_grid(dst), 256, smem, ctx->stream>>>(
-      (const Key<W> *)dst->d_keys, dst->n, (const unsigned char *)tab.d_blob, (uint32_t)tab.bytes, tab.ngroups, diag, sv,
-      packed, dst == src, x, xs, y, ys, vec0, fz, lv, wreq, ctx->d_err);
+      (const Key<W> *)dst->d_keys, dst->n, (const unsigned char *)tab.d_blob, (uint32_t)tab.bytes, tab.ngroups,
+      tab.nhop, tab.hopmask[0], tab.hopmask[1], diag, sv, packed, dst == src, x, xs, y, ys, vec0, fz, lv, wreq,
+      ctx->d_err);
   ctx->launches++;
 }
 
@@ -489,6 +527,40 @@ __global__ void k_block_scatter(const uint32_t *cfg, const uint32_t *flag, const
   }
 }
 
+// Block classes: two blocks whose rows list the same non-local configurations (same count,
+// same sorted non-local parts) align row by row, so a local move between them needs no check.
+// A per-block fingerprint (two sums of mixed non-local parts) proposes the classes; an exact
+// row-by-row comparison with the class representative confirms each member.
+
+template <int W>
+__device__ __forceinline__ Key<W> nonlocal_part(const Key<W> &d, int lo, uint32_t lmask) {
+  return set_local<W>(d, lo, lmask, 0u);
+}
+
+template <int W>
+__global__ void k_block_fp(const Key<W> *keys, int64_t n, int lo, uint32_t lmask, const uint32_t *pos,
+                           unsigned long long *fp) {
+  int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  Key<W> k = nonlocal_part<W>(keys[r], lo, lmask);
+  uint64_t a = k.w[0], b = W == 2 ? k.w[W - 1] : 0x9e3779b97f4a7c15ull;
+  uint32_t blk = pos[r] - 1;
+  atomicAdd(fp + 2 * (size_t)blk, (unsigned long long)qg_mix64(a ^ qg_mix64(b + 0x632be59bd9b4e019ull)));
+  atomicAdd(fp + 2 * (size_t)blk + 1, (unsigned long long)qg_mix64(b ^ qg_mix64(a + 0x8cb92ba72f3d8dd7ull)));
+}
+
+template <int W>
+__global__ void k_block_verify(const Key<W> *keys, int64_t n, int lo, uint32_t lmask, const uint32_t *pos,
+                               const uint32_t *bstart, const uint32_t *rep, uint32_t *mismatch) {
+  int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  uint32_t blk = pos[r] - 1, rp = rep[blk];
+  if (rp == blk) return;
+  int64_t j = (int64_t)bstart[rp] + (r - (int64_t)bstart[blk]);
+  Key<W> a = nonlocal_part<W>(keys[r], lo, lmask), b = nonlocal_part<W>(keys[j], lo, lmask);
+  if (!qg_eq<W>(a, b)) mismatch[blk] = 1u;
+}
+
 void qg_cache_free(OpBasisCache &c) {
   cudaFree(c.d_diag);
   cudaFree(c.d_wreq);
@@ -579,6 +651,57 @@ static qg_status build_local(qg_basis bs, qg_operator op, OpBasisCache &c) {
   if (e == cudaSuccess) e = cudaMemcpyAsync(hstart.data(), bst, (size_t)nb * 4, cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(hcfg.data(), bcf, (size_t)nb * 4, cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  hstart[nb] = (uint32_t)n;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(bst + nb, &hstart[nb], 4, cudaMemcpyHostToDevice, s);
+  // block classes (rows of blocks in one class align)
+  std::vector<uint32_t> cls(nb);
+  for (uint32_t k = 0; k < nb; k++) cls[k] = k;
+  {
+    unsigned long long *fp = nullptr;
+    uint32_t *rep = nullptr, *mis = nullptr;
+    if (e == cudaSuccess) e = cudaMalloc(&fp, (size_t)nb * 16 + 16);
+    if (e == cudaSuccess) e = cudaMalloc(&rep, (size_t)nb * 4 + 4);
+    if (e == cudaSuccess) e = cudaMalloc(&mis, (size_t)nb * 4 + 4);
+    if (e == cudaSuccess) e = cudaMemsetAsync(fp, 0, (size_t)nb * 16 + 16, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(mis, 0, (size_t)nb * 4 + 4, s);
+    if (e == cudaSuccess) {
+      if (W == 1)
+        k_block_fp<1><<<grid_for(n, 256), 256, 0, s>>>((const Key<1> *)bs->d_keys, n, lo, lmask, pos, fp);
+      else
+        k_block_fp<2><<<grid_for(n, 256), 256, 0, s>>>((const Key<2> *)bs->d_keys, n, lo, lmask, pos, fp);
+      ctx->launches++;
+    }
+    std::vector<unsigned long long> hfp((size_t)2 * nb);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hfp.data(), fp, (size_t)nb * 16, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    std::vector<uint32_t> hrep(nb);
+    if (e == cudaSuccess) {
+      std::map<std::tuple<uint32_t, unsigned long long, unsigned long long>, uint32_t> first;
+      for (uint32_t k = 0; k < nb; k++) {
+        auto key = std::make_tuple(hstart[k + 1] - hstart[k], hfp[2 * k], hfp[2 * k + 1]);
+        auto it = first.find(key);
+        hrep[k] = it == first.end() ? (first[key] = k) : it->second;
+      }
+      e = cudaMemcpyAsync(rep, hrep.data(), (size_t)nb * 4, cudaMemcpyHostToDevice, s);
+    }
+    if (e == cudaSuccess) {
+      if (W == 1)
+        k_block_verify<1><<<grid_for(n, 256), 256, 0, s>>>((const Key<1> *)bs->d_keys, n, lo, lmask, pos, bst, rep,
+                                                           mis);
+      else
+        k_block_verify<2><<<grid_for(n, 256), 256, 0, s>>>((const Key<2> *)bs->d_keys, n, lo, lmask, pos, bst, rep,
+                                                           mis);
+      ctx->launches++;
+    }
+    std::vector<uint32_t> hmis(nb);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hmis.data(), mis, (size_t)nb * 4, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e == cudaSuccess)
+      for (uint32_t k = 0; k < nb; k++) cls[k] = hmis[k] ? k : hrep[k];
+    cudaFree(fp);
+    cudaFree(rep);
+    cudaFree(mis);
+  }
   cudaFree(cfg);
   cudaFree(flag);
   cudaFree(pos);
@@ -588,7 +711,6 @@ static qg_status build_local(qg_basis bs, qg_operator op, OpBasisCache &c) {
     cudaFree(bst);
     return qg_cuda_fail(ctx, e, "local blocks");
   }
-  hstart[nb] = (uint32_t)n;
   // configuration -> block
   std::vector<int32_t> table((size_t)1 << H, -1);
   for (uint32_t k = 0; k < nb; k++) table[hcfg[k]] = (int32_t)k;
@@ -620,7 +742,7 @@ static qg_status build_local(qg_basis bs, qg_operator op, OpBasisCache &c) {
       int32_t tbk = table[kv.first];
       if (tbk < 0 || (kv.second.first == 0.0 && kv.second.second == 0.0)) continue;
       LocalEntry le;
-      le.tblock = (uint32_t)tbk;
+      le.tblock = (uint32_t)tbk | (cls[k] == cls[tbk] ? 0x80000000u : 0u);
       le.target = kv.first;
       le.vre = kv.second.first;
       le.vim = kv.second.second;
@@ -638,8 +760,7 @@ static qg_status build_local(qg_basis bs, qg_operator op, OpBasisCache &c) {
   c.nblocks = (int)nb;
   c.nent = (int64_t)ent.size();
   c.d_bstart = bst;
-  e = cudaMemcpy(bst + nb, &hstart[nb], 4, cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = cudaMalloc(&c.d_cfg, table.size() * 4);
+  e = cudaMalloc(&c.d_cfg, table.size() * 4);
   if (e == cudaSuccess) e = cudaMemcpy(c.d_cfg, table.data(), table.size() * 4, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMalloc(&c.d_eoff, eoff.size() * 4);
   if (e == cudaSuccess) e = cudaMemcpy(c.d_eoff, eoff.data(), eoff.size() * 4, cudaMemcpyHostToDevice);

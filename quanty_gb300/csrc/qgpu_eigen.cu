@@ -8,8 +8,15 @@
 // until the variance <H^2> - <H>^2 of every vector is below "Zero".  The same structure here:
 // H*psi is the pull kernel, the Gram products and updates run as memory-bound kernels over
 // the n x K Krylov block (row-major, K columns), and the projected matrix (K <= a few
-// hundred) is diagonalised on the host by cyclic Jacobi rotations.
+// hundred) is diagonalised on the host: Householder reduction to a real tridiagonal matrix,
+// implicit QL with Wilkinson shifts, then the wanted eigenvectors transformed back.
+//
+// Block size: when more than three states are wanted, a few guard vectors join the block
+// (up to half the wanted count, at most 8) and only the wanted states are tested for
+// convergence, so a cluster of nearly degenerate states straddling the last wanted one does
+// not stall the restarts.
 #include <algorithm>
+#include <cfloat>
 #include <cmath>
 #include <complex>
 #include <vector>
@@ -85,6 +92,18 @@ __global__ void k_scale_col(double2 *B, int ldb, int col, int64_t n, double s) {
   B[r * ldb + col] = make_double2(v.x * s, v.y * s);
 }
 
+// deterministic pseudo-random fill of columns c0 .. c0+k-1 (guard vectors)
+__global__ void k_fill_cols(double2 *B, int ldb, int c0, int k, int64_t n, uint64_t salt) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n * k) return;
+  int64_t r = i / k;
+  int c = (int)(i % k);
+  uint64_t h = qg_mix64((uint64_t)i * 0x9e3779b97f4a7c15ull + salt);
+  double a = (double)(h >> 11) * (1.0 / 9007199254740992.0) - 0.5;
+  double b = (double)(qg_mix64(h) >> 11) * (1.0 / 9007199254740992.0) - 0.5;
+  B[r * ldb + c0 + c] = make_double2(a, b);
+}
+
 __global__ void k_copy_cols(const double2 *src, int lds, int s0, double2 *dst, int ldd, int d0, int k, int64_t n) {
   int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (t >= n * k) return;
@@ -135,104 +154,54 @@ struct Gram {
   }
 };
 
-// Cyclic Jacobi for a Hermitian matrix (row-major, k x k).  On return w ascending and the
-// columns of V the eigenvectors.
-void jacobi_eigh(int k, std::vector<cd> A, std::vector<double> &w, std::vector<cd> &V) {
-  V.assign((size_t)k * k, cd(0, 0));
-  for (int i = 0; i < k; i++) V[(size_t)i * k + i] = 1.0;
-  auto at = [&](int i, int j) -> cd & { return A[(size_t)i * k + j]; };
-  double norm = 0;
-  for (auto &z : A) norm += std::norm(z);
-  norm = std::sqrt(norm);
-  for (int sweep = 0; sweep < 100; sweep++) {
-    double off = 0;
-    for (int i = 0; i < k; i++)
-      for (int j = i + 1; j < k; j++) off += std::norm(at(i, j));
-    if (std::sqrt(off) <= 1e-15 * (norm > 0 ? norm : 1.0)) break;
-    for (int p = 0; p < k; p++) {
-      for (int q = p + 1; q < k; q++) {
-        cd c = at(p, q);
-        double ac = std::abs(c);
-        if (ac == 0.0) continue;
-        double a = at(p, p).real(), b = at(q, q).real();
-        double th = 0.5 * std::atan2(2 * ac, a - b);
-        double C = std::cos(th), S = std::sin(th);
-        cd ph = c / ac;       // e^{i phi}
-        cd phc = std::conj(ph);
-        // U = D R with D = diag(1, e^{-i phi}), R = [[C, -S], [S, C]]
-        // columns: A <- A U
-        for (int r = 0; r < k; r++) {
-          cd xp = at(r, p), xq = at(r, q) * phc;
-          at(r, p) = xp * C + xq * S;
-          at(r, q) = -xp * S + xq * C;
-          cd vp = V[(size_t)r * k + p], vq = V[(size_t)r * k + q] * phc;
-          V[(size_t)r * k + p] = vp * C + vq * S;
-          V[(size_t)r * k + q] = -vp * S + vq * C;
-        }
-        // rows: A <- U^dag A
-        for (int cc = 0; cc < k; cc++) {
-          cd xp = at(p, cc), xq = at(q, cc) * ph;
-          at(p, cc) = xp * C + xq * S;
-          at(q, cc) = -xp * S + xq * C;
-        }
-        at(p, q) = 0;
-        at(q, p) = 0;
-        at(p, p) = at(p, p).real();
-        at(q, q) = at(q, q).real();
-      }
-    }
-  }
-  // sort ascending
-  std::vector<int> idx(k);
-  for (int i = 0; i < k; i++) idx[i] = i;
-  std::sort(idx.begin(), idx.end(), [&](int x, int y) { return at(x, x).real() < at(y, y).real(); });
-  std::vector<cd> V2((size_t)k * k);
-  w.resize(k);
-  for (int j = 0; j < k; j++) {
-    w[j] = at(idx[j], idx[j]).real();
-    for (int r = 0; r < k; r++) V2[(size_t)r * k + j] = V[(size_t)r * k + idx[j]];
-  }
-  V.swap(V2);
-}
-
 }  // namespace
 
 void qg_host_eigh(int k, const std::vector<std::complex<double>> &A, std::vector<double> &w,
                   std::vector<std::complex<double>> &V) {
-  jacobi_eigh(k, A, w, V);
+  hermitian_eigh(k, A, w, V, k);
 }
 
-extern "C" qg_status qg_block_groundstate(qg_context ctx, qg_operator op, qg_basis b, int32_t p, double *x_dev,
+extern "C" qg_status qg_block_groundstate(qg_context ctx, qg_operator op, qg_basis b, int32_t nwant, double *x_dev,
                                           double *energies_host, double tol, int32_t max_krylov,
                                           int32_t max_restarts, int32_t *iterations) {
-  if (!ctx || !op || !b || !x_dev || !energies_host || p <= 0 || op->nf != b->nf) return QG_ERR_ARG;
+  if (!ctx || !op || !b || !x_dev || !energies_host || nwant <= 0 || op->nf != b->nf) return QG_ERR_ARG;
   int64_t n = b->n;
-  if (n < p) {
+  if (n < nwant) {
     ctx->last_error = "qg_block_groundstate: basis smaller than the number of states";
     return QG_ERR_ARG;
   }
+  int guard = nwant > 3 ? std::min(nwant / 2, 8) : 0;
+  int p = (int)std::min<int64_t>(nwant + guard, n);
   int K = max_krylov > 0 ? max_krylov : 128;
   if (K < 2 * p) K = 2 * p;
   if (K > n) K = (int)n;
   K = (K / p) * p;
   if (K < p) K = p;
   cudaStream_t s = ctx->stream;
-  double2 *V = nullptr, *W = nullptr, *Cd = nullptr;
+  double2 *V = nullptr, *W = nullptr, *Cd = nullptr, *X = nullptr;
   size_t vb = (size_t)n * K * 16, wb = (size_t)n * p * 16;
   cudaError_t e = cudaMalloc(&V, vb);
   if (e == cudaSuccess) e = cudaMalloc(&W, wb);
+  if (e == cudaSuccess) e = cudaMalloc(&X, wb);
   if (e == cudaSuccess) e = cudaMalloc(&Cd, (size_t)K * std::max(K, p) * 16);
   if (e != cudaSuccess) {
     cudaFree(V);
     cudaFree(W);
+    cudaFree(X);
     cudaFree(Cd);
     ctx->last_error = "qg_block_groundstate: out of device memory";
     return QG_ERR_OOM;
   }
+  auto grid = [](int64_t t) { return (unsigned)((t + 255) / 256); };
+  // the block: the caller's start vectors, then the guard vectors
+  k_copy_cols<<<grid(n * nwant), 256, 0, s>>>((const double2 *)x_dev, nwant, 0, X, p, 0, nwant, n);
+  ctx->launches++;
+  if (p > nwant) {
+    k_fill_cols<<<grid(n * (p - nwant)), 256, 0, s>>>(X, p, nwant, p - nwant, n, 0x5eedull);
+    ctx->launches++;
+  }
   Gram G;
   qg_status st = G.init(ctx, n, K * std::max(K, p));
-  double2 *X = (double2 *)x_dev;
-  auto grid = [](int64_t t) { return (unsigned)((t + 255) / 256); };
   std::vector<double> theta(p, 0.0);
   int it = 0;
   bool converged = false;
@@ -350,11 +319,8 @@ extern "C" qg_status qg_block_groundstate(qg_context ctx, qg_operator op, qg_bas
         M[(size_t)i * k + j] = (a == cd(0, 0)) ? bb : ((bb == cd(0, 0)) ? a : 0.5 * (a + bb));
       }
     std::vector<double> w;
-    std::vector<cd> Y;
-    jacobi_eigh(k, M, w, Y);
-    std::vector<cd> Yp((size_t)k * p);
-    for (int i = 0; i < k; i++)
-      for (int j = 0; j < p; j++) Yp[(size_t)i * p + j] = Y[(size_t)i * k + j];
+    std::vector<cd> Yp;
+    hermitian_eigh(k, M, w, Yp, p);
     e = cudaMemcpyAsync(Cd, Yp.data(), Yp.size() * 16, cudaMemcpyHostToDevice, s);
     if (e != cudaSuccess) {
       st = qg_cuda_fail(ctx, e, "ritz upload");
@@ -381,7 +347,7 @@ extern "C" qg_status qg_block_groundstate(qg_context ctx, qg_operator op, qg_bas
     }
     std::vector<cd> hh;
     double worst = 0;
-    for (int j = 0; j < p && st == QG_OK; j++) {
+    for (int j = 0; j < nwant && st == QG_OK; j++) {
       st = G.run(W, p, j, 1, W, p, j, 1, &hh);
       if (st != QG_OK) break;
       worst = std::max(worst, std::fabs(hh[0].real()));
@@ -389,11 +355,16 @@ extern "C" qg_status qg_block_groundstate(qg_context ctx, qg_operator op, qg_bas
     if (worst < tol) converged = true;
   }
   G.release();
+  if (st == QG_OK) {
+    k_copy_cols<<<grid(n * nwant), 256, 0, s>>>(X, p, 0, (double2 *)x_dev, nwant, 0, nwant, n);
+    ctx->launches++;
+  }
   cudaStreamSynchronize(s);
   cudaFree(V);
   cudaFree(W);
+  cudaFree(X);
   cudaFree(Cd);
-  for (int j = 0; j < p; j++) energies_host[j] = theta[j];
+  for (int j = 0; j < nwant; j++) energies_host[j] = theta[j];
   if (iterations) *iterations = it;
   if (st == QG_OK) st = qg_check_device_error(ctx, "qg_block_groundstate");
   if (st == QG_OK && !converged) {

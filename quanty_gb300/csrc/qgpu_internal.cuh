@@ -56,13 +56,18 @@ struct __align__(16) TermDev<2> {
   double vre, vim;
 };
 
-// Terms sharing one need1 mask; terms[begin, end).  32 bytes.
+// Terms sharing one need1 mask; terms[begin, end).  48 bytes.
+// A hop group holds one-body moves only: need1 is one orbital p, every term empties p and
+// fills one orbital q (need0 = {q}, flip = {p, q}), the terms in ascending order of q; qmask
+// is the set of those q.  Such a group's applicable terms are the set bits of qmask & ~row,
+// so no term is tested.
 template <int W>
 struct __align__(16) GroupDev {
   uint64_t need1[2];  // words >= W are zero
   int32_t begin, end;
   int32_t diag;  // all terms of the group have flip == 0
-  int32_t pad;
+  int32_t hop;   // a hop group (see above)
+  uint64_t qmask[2];
 };
 
 // Hash slot, one 32-byte DRAM sector: the key and the current source amplitude (written by
@@ -92,12 +97,16 @@ struct qg_context_s {
 };
 
 // A term table in one device allocation: ngroups GroupDev followed by nterms TermDev.
+// Hop groups come first, in ascending order of their orbital p (word 0 bits, then word 1);
+// hopmask holds those orbitals, so the hop group of an occupied p is found by a popcount.
 struct HostTable {
   void *d_blob = nullptr;
   void *d_groups = nullptr;  // = d_blob
   void *d_terms = nullptr;   // = d_blob + ngroups * sizeof(GroupDev)
   size_t bytes = 0;          // multiple of 16
   int ngroups = 0, nterms = 0;
+  int nhop = 0;              // leading hop groups
+  uint64_t hopmask[2] = {0, 0};
 };
 
 // A digested term on the host (canonical masks in device bit positions, signed value).
@@ -128,7 +137,8 @@ struct qg_operator_s {
 
 // Per-(operator, basis) precomputed data for the same-basis H*psi.
 struct LocalEntry {
-  uint32_t tblock;   // block of the target local configuration
+  uint32_t tblock;   // block of the target local configuration; bit 31: both blocks list the
+                     // same non-local configurations, so the target row is at the same offset
   uint32_t target;   // target local configuration
   uint64_t wreq;     // window bits the target needs (see qgpu_apply.cu)
   double vre, vim;   // merged, signed coefficient
@@ -291,6 +301,10 @@ int qg_apply_grid(qg_basis dst);
 // Hermitian eigenproblem of a small host matrix (row-major k x k): ascending values, columns of
 // V the eigenvectors (cyclic Jacobi, qgpu_eigen.cu)
 #include <complex>
+// Householder + implicit QL (qgpu_hosteig.cu): all eigenvalues ascending, the lowest nv
+// eigenvectors as the columns of V (row-major, k x nv); A row-major k x k.
+void hermitian_eigh(int k, std::vector<std::complex<double>> A, std::vector<double> &w,
+                    std::vector<std::complex<double>> &V, int nv);
 void qg_host_eigh(int k, const std::vector<std::complex<double>> &A, std::vector<double> &w,
                   std::vector<std::complex<double>> &V);
 int qg_partial_blocks(qg_context ctx, int64_t n);

@@ -116,15 +116,57 @@ void build_table(qg_context ctx, const std::vector<Entry> &terms, HostTable &tab
     std::vector<uint64_t> key(terms[t].m.n1, terms[t].m.n1 + W);
     groups[key].push_back(t);
   }
+  // hop groups (one-body moves out of a single orbital p) first, by p; then the rest
+  auto popc2 = [&](const uint64_t *m) {
+    int c = 0;
+    for (int i = 0; i < W; i++) c += __builtin_popcountll(m[i]);
+    return c;
+  };
+  auto bitpos = [&](const uint64_t *m) {  // position of the lowest set bit, word-major
+    for (int i = 0; i < W; i++)
+      if (m[i]) return 64 * i + __builtin_ctzll(m[i]);
+    return -1;
+  };
+  auto is_hop = [&](const std::vector<int> &idx) {
+    uint64_t qs[2] = {0, 0};
+    for (int t : idx)
+      for (int i = 0; i < W; i++) qs[i] |= terms[t].m.n0[i];
+    if (popc2(qs) != (int)idx.size()) return false;  // one term per target orbital q
+    for (int t : idx) {
+      const Masks &m = terms[t].m;
+      if (popc2(m.n1) != 1 || popc2(m.fl) != 2 || popc2(m.n0) != 1) return false;
+      for (int i = 0; i < W; i++)
+        if ((m.fl[i] & m.n1[i]) != m.n1[i] || (m.fl[i] & ~m.n1[i]) != m.n0[i]) return false;
+    }
+    return !idx.empty();
+  };
+  std::vector<std::pair<std::vector<uint64_t>, std::vector<int>>> order_g;
+  std::vector<std::pair<std::vector<uint64_t>, std::vector<int>>> rest_g;
+  for (auto &kv : groups) (is_hop(kv.second) ? order_g : rest_g).push_back(kv);
+  std::sort(order_g.begin(), order_g.end(),
+            [&](const auto &a, const auto &b) { return bitpos(a.first.data()) < bitpos(b.first.data()); });
+  tab.nhop = (int)order_g.size();
+  tab.hopmask[0] = tab.hopmask[1] = 0;
+  for (auto &kv : order_g)
+    for (int i = 0; i < W; i++) tab.hopmask[i] |= kv.first[i];
+  for (auto &kv : order_g) {
+    std::vector<int> &idx = kv.second;
+    std::sort(idx.begin(), idx.end(), [&](int a, int b) { return bitpos(terms[a].m.n0) < bitpos(terms[b].m.n0); });
+  }
+  for (auto &kv : rest_g) order_g.push_back(kv);
   std::vector<GroupDev<W>> g;
   std::vector<TermDev<W>> tt;
-  for (auto &kv : groups) {
+  for (auto &kv : order_g) {
     GroupDev<W> gd;
     std::memset(&gd, 0, sizeof(gd));
     for (int i = 0; i < W; i++) gd.need1[i] = kv.first[i];
     gd.begin = (int)tt.size();
     gd.diag = 1;
+    gd.hop = (int)g.size() < tab.nhop;
     std::vector<int> idx = kv.second;
+    if (gd.hop)
+      for (int t : idx)
+        for (int i = 0; i < W; i++) gd.qmask[i] |= terms[t].m.n0[i];
     std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) {
       bool da = true, db = true;
       for (int i = 0; i < W; i++) {

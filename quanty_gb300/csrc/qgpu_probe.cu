@@ -1,0 +1,52 @@
+// Random-sector gather bandwidth of the device: the ceiling of a gather whose addresses are
+// unrelated (hash-table probes), as opposed to the streaming copy bandwidth.  The H*psi
+// roofline charges its hash-probed connections against this figure.
+#include "qgpu_internal.cuh"
+
+// each thread reads four 32-byte sectors at independent pseudo-random positions
+__global__ void k_gather_probe(const double2 *__restrict__ a, uint64_t mask, int64_t n, double *out, uint64_t salt) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double s = 0;
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    uint64_t j = qg_mix64((uint64_t)i * 4 + k + salt) & mask;
+    double2 v0 = __ldg(a + 2 * j), v1 = __ldg(a + 2 * j + 1);
+    s += v0.x + v1.y;
+  }
+  if (s != 0.0) out[0] = s;  // the buffer is zero: never taken, keeps the loads
+}
+
+extern "C" qg_status qg_gather_bandwidth(qg_context ctx, int64_t bytes, double *gbs) {
+  if (!ctx || !gbs || bytes < (1 << 20)) return QG_ERR_ARG;
+  uint64_t nsec = 1;
+  while (nsec * 2 * 32 <= (uint64_t)bytes) nsec *= 2;
+  double2 *a = nullptr;
+  double *out = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaStream_t s = ctx->stream;
+  cudaError_t e = cudaMalloc(&a, nsec * 32);
+  if (e == cudaSuccess) e = cudaMalloc(&out, 8);
+  if (e == cudaSuccess) e = cudaMemsetAsync(a, 0, nsec * 32, s);
+  if (e == cudaSuccess) e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  float ms = 0;
+  int64_t nthr = (int64_t)(nsec / 4);  // 4 sectors per thread: one pass reads nsec sectors
+  unsigned grid = (unsigned)((nthr + 255) / 256);
+  if (e == cudaSuccess) {
+    k_gather_probe<<<grid, 256, 0, s>>>(a, nsec - 1, nthr, out, 1);  // warm
+    cudaEventRecord(e0, s);
+    for (int r = 0; r < 3; r++) k_gather_probe<<<grid, 256, 0, s>>>(a, nsec - 1, nthr, out, 2 + r);
+    cudaEventRecord(e1, s);
+    ctx->launches += 4;
+    e = cudaEventSynchronize(e1);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaFree(a);
+  cudaFree(out);
+  if (e != cudaSuccess) return qg_cuda_fail(ctx, e, "qg_gather_bandwidth");
+  *gbs = (double)nthr * 4 * 32 * 3 / (ms * 1e-3) / 1e9;
+  return QG_OK;
+}

@@ -10,6 +10,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libqgpu.so")
 HEADER = os.path.join(os.path.dirname(HERE), "include", "qgpu.h")
 
+QG_ERR_TIMEOUT = 3
 STATUS = {0: "QG_OK", 1: "QG_ERR_OOM", 2: "QG_ERR_TABLE_FULL", 3: "QG_ERR_TIMEOUT", 4: "QG_ERR_ARG",
           5: "QG_ERR_CUDA", 6: "QG_ERR_NOT_HERMITIAN"}
 
@@ -57,6 +58,8 @@ def load(path=LIB_PATH):
         "qg_count_nnz": (C.c_int, [P, P, P, P]),
         "qg_count_nnz_offdiag": (C.c_int, [P, P, P, P]),
         "qg_set_autotune": (C.c_int, [P, I32]),
+        "qg_hermitian_eigh": (C.c_int, [I32, P, P, P, I32]),
+        "qg_gather_bandwidth": (C.c_int, [P, I64, P]),
         "qg_apply_chunk": (C.c_int, [P, P, P, I32, P]),
         "qg_expectation": (C.c_int, [P, P, P, P, I32, P]),
         "qg_dot": (C.c_int, [P, I64, I32, P, P, P]),
