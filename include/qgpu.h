@@ -150,11 +150,15 @@ qg_status qg_hermitian_eigh(int32_t k, const double *a, double *w, double *v, in
 /* Autotuning of the multi-vector apply (no counterpart in the reference, whose loops handle one
  * vector at a time): the first apply of an operator with nvec >= 2 vectors on a basis (as
  * its own source and target, outside stream capture) times each number of vectors handled per
- * kernel pass (8, 4, 2, 1) and keeps the fastest for that (operator, basis, nvec).  The result
- * is bitwise the same for every choice.  qg_set_autotune(ctx, 0) turns the timing off (passes
- * of 8 vectors); qg_apply_chunk reports the choice in force (0 while none has been made). */
+ * kernel pass and keeps the fastest for that (operator, basis, nvec): a thread per row carrying
+ * 8, 4, 2 or 1 vectors per pass, or (nvec >= 16) a warp per row with its lanes over 32 or 64
+ * vectors per pass (chunk -32, -64).  Every choice sums each vector's connections in the same
+ * order, so the result is bitwise the same.  qg_set_autotune(ctx, 0) turns the timing off
+ * (passes of 8 vectors); qg_apply_chunk reports the choice in force (0 while none has been
+ * made); qg_apply_set_chunk pins one. */
 qg_status qg_set_autotune(qg_context ctx, int32_t on);
 qg_status qg_apply_chunk(qg_context ctx, qg_operator op, qg_basis basis, int32_t nvec, int32_t *chunk);
+qg_status qg_apply_set_chunk(qg_context ctx, qg_operator op, qg_basis basis, int32_t nvec, int32_t chunk);
 
 /* qg_apply with host buffers: copies x_host to the device, applies, copies y back (the
  * reference's calling convention, where psi and Opsi live in host memory).  Device staging

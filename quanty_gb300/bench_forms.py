@@ -111,7 +111,36 @@ def batched(args):
     t_lz_p = sum(_lanczos_seconds(api, H, bf, y, ntri, eps, eng) for y in y1) / len(y1)
     _log("lanczos only: batched %.2f s, plain %.3f s per vector" % (t_lz_b, t_lz_p))
     n_final = bf.n
-    del Y, y1, bf
+    # every vector layout of the multi-vector apply, timed on the 48-vector block
+    import ctypes
+    ch = ctypes.c_int32()
+    eng.check(eng.L.qg_apply_chunk(eng.ctx, H.handle(eng), bf.h, nspec, ctypes.byref(ch)))
+    tuned = ch.value
+    layouts = {}
+    Z = eng.empty(bf.n, nspec)
+    torch = eng.torch
+    for c in (1, 2, 4, 8, -32, -64):
+        eng.check(eng.L.qg_apply_set_chunk(eng.ctx, H.handle(eng), bf.h, nspec, c))
+        eng.check(eng.L.qg_apply(eng.ctx, H.handle(eng), bf.h, bf.h, api._ptr(Y), api._ptr(Z), nspec))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(eng.stream)
+        for _ in range(3):
+            eng.check(eng.L.qg_apply(eng.ctx, H.handle(eng), bf.h, bf.h, api._ptr(Y), api._ptr(Z), nspec))
+        e1.record(eng.stream)
+        e1.synchronize()
+        layouts[str(c)] = e0.elapsed_time(e1) / 3
+    eng.check(eng.L.qg_apply_set_chunk(eng.ctx, H.handle(eng), bf.h, nspec, tuned if tuned else 8))
+    z1 = eng.empty(bf.n, 1)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    eng.check(eng.L.qg_apply(eng.ctx, H.handle(eng), bf.h, bf.h, api._ptr(y1[0]), api._ptr(z1), 1))
+    e0.record(eng.stream)
+    for _ in range(3):
+        eng.check(eng.L.qg_apply(eng.ctx, H.handle(eng), bf.h, bf.h, api._ptr(y1[0]), api._ptr(z1), 1))
+    e1.record(eng.stream)
+    e1.synchronize()
+    single_ms = e0.elapsed_time(e1) / 3
+    _log("apply ms for 48 vectors by layout %s (autotuned %d); one vector %.3f ms" % (layouts, tuned, single_ms))
+    del Y, y1, bf, Z, z1
 
     rixs = None
     if not args.no_rixs:
@@ -150,6 +179,7 @@ def batched(args):
         "max_rel_diff_batched_vs_plain": diff,
         "lanczos_only": {"batched_seconds": t_lz_b, "plain_seconds_per_vector": t_lz_p,
                          "speedup": nspec * t_lz_p / t_lz_b},
+        "apply_ms_by_layout": layouts, "apply_ms_one_vector": single_ms, "autotuned_layout": tuned,
         "eigensystem": {"seconds": t_eigen, "converged": est["converged"], "max_variance": res,
                         "block_applies": est["applies"], "krylov_max": est["krylov_max"]},
         "energies_eV": [float(e) for e in E],

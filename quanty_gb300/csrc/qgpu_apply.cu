@@ -381,6 +381,237 @@ __global__ void __launch_bounds__(256) k_apply(const Key<W> *__restrict__ rows, 
   if (SMEM && pending) mbar_wait_bounded(smem_addr(&s_bar), 0);  // never leave with a copy in flight
 }
 
+// ------------------------------------------------------------------ warp-per-row, lanes over vectors
+//
+// For many vectors (nvec >= 32) one warp takes one row at a time: its 32 lanes share the
+// row's work out (local moves, terms of the table: one per lane per round), and every lane
+// that found a connection appends (source row, signed value) to a per-warp list in shared
+// memory in lane order (ballot + prefix popcount, so the order is fixed).  The list is then
+// applied with lanes over vectors: lane l owns vectors vec0 + l + 32 m, so the amplitudes of
+// one source row are one coalesced read and every FP64 lane is busy.  The list order is the
+// thread-per-row kernel's order (diagonal, local moves in entry order, terms in table order),
+// so each vector's sum runs in the same order and the output is bitwise the same.
+#define QG_WARP_LIST 128
+
+template <int W, int VPL, bool FUSE, bool SMEM>
+__global__ void __launch_bounds__(256) k_apply_warp(const Key<W> *__restrict__ rows, int64_t n_rows,
+                                                    const unsigned char *__restrict__ gtab, uint32_t tab_bytes,
+                                                    int ngroups, int nterms, uint32_t tgrp_off,
+                                                    const double2 *__restrict__ diag, SrcView src,
+                                                    const double2 *__restrict__ x, int xs, double2 *__restrict__ y,
+                                                    int ys, int vec0, int nv, ApplyFuse fz, LocalView lv,
+                                                    const uint64_t *__restrict__ wreq, unsigned int *err) {
+  extern __shared__ __align__(128) unsigned char s_tab[];
+  __shared__ __align__(8) unsigned long long s_bar;
+  __shared__ uint32_t s_j[8][QG_WARP_LIST];
+  __shared__ double s_vr[8][QG_WARP_LIST], s_vi[8][QG_WARP_LIST];
+  bool pending = false;
+  const unsigned char *tab = gtab;
+  if (SMEM) tab = stage_table(gtab, tab_bytes, s_tab, &s_bar, err, pending);
+  const GroupDev<W> *groups = reinterpret_cast<const GroupDev<W> *>(tab);
+  const TermDev<W> *terms = reinterpret_cast<const TermDev<W> *>(tab + (size_t)ngroups * sizeof(GroupDev<W>));
+  const uint32_t *tgrp = reinterpret_cast<const uint32_t *>(tab + tgrp_off);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const unsigned FULL = 0xffffffffu;
+  uint32_t *lj = s_j[wid];
+  double *lvr = s_vr[wid], *lvi = s_vi[wid];
+  double2 dsum[VPL];
+#pragma unroll
+  for (int m = 0; m < VPL; m++) dsum[m] = make_double2(0.0, 0.0);
+  const int64_t base = (int64_t)blockIdx.x * 256 + wid * 32;
+  for (int it = 0; it < 32; it++) {
+    const int64_t r = base + it;
+    if (r >= n_rows) break;  // uniform across the warp
+    const Key<W> d = rows[r];
+    double2 acc[VPL];
+    double2 dg = diag ? diag[r] : make_double2(0.0, 0.0);
+    bool dgc = qg_is_nonzero(dg.y);
+#pragma unroll
+    for (int m = 0; m < VPL; m++) {
+      int k = lane + 32 * m;
+      acc[m] = make_double2(0.0, 0.0);
+      if (diag && k < nv) {
+        double2 xv = x[r * xs + vec0 + k];
+        if (dgc) {
+          acc[m].x = dg.x * xv.x - dg.y * xv.y;
+          acc[m].y = dg.x * xv.y + dg.y * xv.x;
+        } else {
+          acc[m].x = dg.x * xv.x;
+          acc[m].y = dg.x * xv.y;
+        }
+      }
+    }
+    int cnt = 0;
+    auto flush = [&]() {
+      __syncwarp();
+      for (int c = 0; c < cnt; c++) {
+        int64_t j = lj[c];
+        double vr = lvr[c], vi = lvi[c];
+        bool cplx = qg_is_nonzero(vi);
+#pragma unroll
+        for (int m = 0; m < VPL; m++) {
+          int k = lane + 32 * m;
+          if (k < nv) qg_cmac(acc[m], vr, vi, cplx, __ldg(x + j * xs + vec0 + k));
+        }
+      }
+      __syncwarp();
+      cnt = 0;
+    };
+    auto append = [&](bool has, int64_t j, double vr, double vi) {
+      unsigned msk = __ballot_sync(FULL, has);
+      if (!msk) return;
+      if (cnt + 32 > QG_WARP_LIST) flush();
+      if (has) {
+        int pos = cnt + __popc(msk & ((1u << lane) - 1u));
+        lj[pos] = (uint32_t)j;
+        lvr[pos] = vr;
+        lvi[pos] = vi;
+      }
+      cnt += __popc(msk);
+    };
+    // window bits of the row, one window per lane
+    uint64_t okm = 0;
+    if (wreq && src.nres) {
+      uint64_t mine = 0;
+      if (lane < src.nres) {
+        int c = 0;
+#pragma unroll
+        for (int i = 0; i < W; i++) c += __popcll(d.w[i] & __ldg(src.rmask + lane * W + i));
+        int lo = __ldg(src.rmin + lane), hi = __ldg(src.rmax + lane);
+#pragma unroll
+        for (int D = -2; D <= 2; D++)
+          if (c + D >= lo && c + D <= hi) mine |= 1ull << (5 * lane + D + 2);
+      }
+      uint32_t a = __reduce_or_sync(FULL, (uint32_t)mine), b = __reduce_or_sync(FULL, (uint32_t)(mine >> 32));
+      okm = (uint64_t)a | ((uint64_t)b << 32);
+    }
+    if (lv.on) {
+      int b = __ldg(lv.cfg + get_local<W>(d, lv.lo, lv.lmask));
+      int64_t off = r - (int64_t)__ldg(lv.bstart + b);
+      uint32_t e0 = __ldg(lv.eoff + b), e1 = __ldg(lv.eoff + b + 1);
+      for (uint32_t e = e0; e < e1; e += 32) {
+        uint32_t ee = e + lane;
+        bool has = false;
+        int64_t j = 0;
+        double vr = 0.0, vi = 0.0;
+        if (ee < e1) {
+          const LocalEntry *E = lv.ent + ee;
+          uint32_t tbr = __ldg(&E->tblock);
+          uint32_t tbk = tbr & 0x7FFFFFFFu;
+          j = (int64_t)__ldg(lv.bstart + tbk) + off;
+          if (tbr >> 31) {
+            has = true;
+          } else {
+            Key<W> s = set_local<W>(d, lv.lo, lv.lmask, __ldg(&E->target));
+            if (j < (int64_t)__ldg(lv.bstart + tbk + 1)) has = qg_eq<W>(rows[j], s);
+            if (!has) {
+              bool ok = true;
+              if (src.nres) {
+                uint64_t req = __ldg(&E->wreq);
+                ok = wreq ? ((okm & req) == req) : in_windows<W>(s, src);
+              }
+              if (ok) {
+                int64_t h = qg_find_slot<W>(src.slots, src.hmask, s, err);
+                if (h >= 0) {
+                  j = (int64_t)__ldg(src.slot_row + h);
+                  has = true;
+                }
+              }
+            }
+          }
+          if (has) {
+            vr = __ldg(&E->vre);
+            vi = __ldg(&E->vim);
+          }
+        }
+        append(has, j, vr, vi);
+      }
+    }
+    // table terms, one per lane per round, in table order
+    for (int t0 = 0; t0 < nterms; t0 += 32) {
+      int t = t0 + lane;
+      bool has = false;
+      int64_t j = 0;
+      double vr = 0.0, vi = 0.0;
+      if (t < nterms) {
+        const GroupDev<W> &G = groups[tgrp[t]];
+        const TermDev<W> &T = terms[t];
+        bool app = true, dgt = true;
+        Key<W> s;
+#pragma unroll
+        for (int i = 0; i < W; i++) {
+          app &= (d.w[i] & G.need1[i]) == G.need1[i];
+          app &= (d.w[i] & T.need0[i]) == 0;
+          s.w[i] = d.w[i] ^ T.flip[i];
+          dgt &= T.flip[i] == 0;
+        }
+        if (app) {
+          if (dgt) {
+            j = r;
+            has = true;
+          } else {
+            bool ok = true;
+            if (src.nres) {
+              if (wreq) {
+                uint64_t req = __ldg(wreq + t);
+                ok = (okm & req) == req;
+              } else {
+                ok = in_windows<W>(s, src);
+              }
+            }
+            if (ok) {
+              int64_t h = qg_find_slot<W>(src.slots, src.hmask, s, err);
+              if (h >= 0) {
+                j = (int64_t)__ldg(src.slot_row + h);
+                has = true;
+              }
+            }
+          }
+          if (has) {
+            int par = 0;
+#pragma unroll
+            for (int i = 0; i < W; i++) par += __popcll(d.w[i] & T.sgn[i]);
+            vr = qg_flip_sign(T.vre, par);
+            vi = qg_flip_sign(T.vim, par);
+          }
+        }
+      }
+      append(has, j, vr, vi);
+    }
+    flush();
+#pragma unroll
+    for (int m = 0; m < VPL; m++) {
+      int k = lane + 32 * m;
+      if (k >= nv) continue;
+      if (!FUSE) {
+        y[r * ys + vec0 + k] = acc[m];
+      } else {
+        double2 xv = x[r * xs + vec0 + k];
+        dsum[m].x += xv.x * acc[m].x + xv.y * acc[m].y;
+        dsum[m].y += xv.x * acc[m].y - xv.y * acc[m].x;
+        double2 pv = fz.prev[r * ys + vec0 + k];
+        double be = fz.beta[vec0 + k];
+        y[r * ys + vec0 + k] = make_double2(acc[m].x - be * pv.x, acc[m].y - be * pv.y);
+      }
+    }
+  }
+  if (FUSE) {
+    __shared__ double2 red[8][32 * VPL];
+#pragma unroll
+    for (int m = 0; m < VPL; m++) red[wid][lane + 32 * m] = dsum[m];
+    __syncthreads();
+    for (int k = threadIdx.x; k < nv && k < 32 * VPL; k += blockDim.x) {
+      double2 sacc = make_double2(0.0, 0.0);
+      for (int w = 0; w < 8; w++) {
+        sacc.x += red[w][k].x;
+        sacc.y += red[w][k].y;
+      }
+      fz.dot_part[blockIdx.x * ys + vec0 + k] = sacc;
+    }
+  }
+  if (SMEM && pending) mbar_wait_bounded(smem_addr(&s_bar), 0);
+}
+
 int qg_apply_grid(qg_basis dst) { return (int)std::max<int64_t>(1, (dst->n + 255) / 256); }
 
 template <int W, int NV, bool FUSE, bool SMEM>
@@ -404,10 +635,44 @@ static void launch_apply_t(qg_context ctx, const HostTable &tab, const double2 *
   ctx->launches++;
 }
 
+template <int W, int VPL, bool FUSE, bool SMEM>
+static void launch_apply_warp_t(qg_context ctx, const HostTable &tab, const double2 *diag, qg_basis dst,
+                                qg_basis src, const double2 *x, int xs, double2 *y, int ys, int vec0, int nv,
+                                const ApplyFuse &fz, const LocalView &lv, const uint64_t *wreq) {
+  size_t smem = SMEM ? tab.bytes : 0;
+  if (SMEM) {
+    static bool attr_done = false;
+    if (!attr_done) {
+      cudaFuncSetAttribute(k_apply_warp<W, VPL, FUSE, SMEM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           QG_SMEM_TABLE_MAX);
+      attr_done = true;
+    }
+  }
+  SrcView sv{src->d_slots, src->d_slot_row, (uint64_t)(src->hcap - 1), src->nres, src->d_rmask, src->d_rmin,
+             src->d_rmax};
+  k_apply_warp<W, VPL, FUSE, SMEM><<<qg_apply_grid(dst), 256, smem, ctx->stream>>>(
+      (const Key<W> *)dst->d_keys, dst->n, (const unsigned char *)tab.d_blob, (uint32_t)tab.bytes, tab.ngroups,
+      tab.nterms, (uint32_t)tab.tgrp_off, diag, sv, x, xs, y, ys, vec0, nv, fz, lv, wreq, ctx->d_err);
+  ctx->launches++;
+}
+
 template <int W, bool FUSE, bool SMEM>
 static void launch_apply_w(qg_context ctx, const HostTable &tab, const double2 *diag, qg_basis dst, qg_basis src,
                            int packed, const double2 *x, int xs, double2 *y, int ys, int nvec, const ApplyFuse &fz,
                            const LocalView &lv, const uint64_t *wreq, int chunk) {
+  if (chunk < 0 && dst == src) {
+    // warp per row with lanes over vectors: passes of 32 or 64 vectors
+    int per = -chunk;
+    for (int v = 0; v < nvec; v += per) {
+      int nv = std::min(per, nvec - v);
+      if (per > 32)
+        launch_apply_warp_t<W, 2, FUSE, SMEM>(ctx, tab, diag, dst, src, x, xs, y, ys, v, nv, fz, lv, wreq);
+      else
+        launch_apply_warp_t<W, 1, FUSE, SMEM>(ctx, tab, diag, dst, src, x, xs, y, ys, v, nv, fz, lv, wreq);
+    }
+    return;
+  }
+  if (chunk < 0) chunk = 8;
   int v = 0;
   while (v < nvec) {
     int left = std::min(nvec - v, chunk);
@@ -867,11 +1132,13 @@ static qg_status autotune(qg_context ctx, qg_operator op, qg_basis b, OpBasisCac
   }
   int best = 8;
   float best_ms = 0;
-  const int cand[4] = {8, 4, 2, 1};
+  // thread per row with 8, 4, 2 or 1 vectors per pass; warp per row with 32 or 64
+  const int cand[6] = {8, 4, 2, 1, -32, -64};
   qg_status st = QG_OK;
-  for (int i = 0; i < 4 && st == QG_OK; i++) {
+  for (int i = 0; i < 6 && st == QG_OK; i++) {
     int ch = cand[i];
     if (ch > nvec && ch != 8) continue;
+    if (ch < 0 && (nvec < 16 || (ch == -64 && nvec <= 32))) continue;
     if (i == 0) st = apply_chunked(ctx, op, b, b, x, xs, y, ys, nvec, nullptr, false, ch);  // warm
     cudaEventRecord(e0, ctx->stream);
     if (st == QG_OK) st = apply_chunked(ctx, op, b, b, x, xs, y, ys, nvec, nullptr, false, ch);
@@ -1064,6 +1331,21 @@ extern "C" qg_status qg_count_nnz(qg_context ctx, qg_operator op, qg_basis b, in
 extern "C" qg_status qg_set_autotune(qg_context ctx, int32_t on) {
   if (!ctx) return QG_ERR_ARG;
   ctx->autotune = on != 0;
+  return QG_OK;
+}
+
+extern "C" qg_status qg_apply_set_chunk(qg_context ctx, qg_operator op, qg_basis b, int32_t nvec, int32_t chunk) {
+  if (!ctx || !op || !b || nvec <= 0) return QG_ERR_ARG;
+  if (!(chunk == 1 || chunk == 2 || chunk == 4 || chunk == 8 || chunk == -32 || chunk == -64)) return QG_ERR_ARG;
+  qg_status st = QG_OK;
+  OpBasisCache *c = qg_basis_cache(b, op, &st);
+  if (st != QG_OK) return st;
+  for (auto &p : c->chunk)
+    if (p.first == nvec) {
+      p.second = chunk;
+      return QG_OK;
+    }
+  c->chunk.push_back({nvec, chunk});
   return QG_OK;
 }
 

@@ -107,6 +107,7 @@ struct HostTable {
   int ngroups = 0, nterms = 0;
   int nhop = 0;              // leading hop groups
   uint64_t hopmask[2] = {0, 0};
+  size_t tgrp_off = 0;       // byte offset of the uint32 group index of each term (after the terms)
 };
 
 // A digested term on the host (canonical masks in device bit positions, signed value).
@@ -216,6 +217,20 @@ __host__ __device__ inline bool qg_less(const Key<W> &a, const Key<W> &b) {
 }
 
 // Find the slot of a key; returns the slot index or -1.  Probes are bounded.
+// linear probe for key k starting at slot h
+template <int W>
+__device__ __forceinline__ int64_t qg_find_slot_at(const Slot *__restrict__ slots, uint64_t hmask, const Key<W> &k,
+                                                   uint64_t h, unsigned int *err) {
+  for (int p = 0; p < QG_PROBE_LIMIT; p++) {
+    ulonglong2 v = __ldg(reinterpret_cast<const ulonglong2 *>(slots + h));
+    if (v.x == k.w[0] && (W == 1 || v.y == k.w[W - 1])) return (int64_t)h;
+    if (v.x == QG_EMPTY_WORD) return -1;
+    h = (h + 1) & hmask;
+  }
+  atomicOr(err, QG_DEVERR_PROBE);
+  return -1;
+}
+
 template <int W>
 __device__ __forceinline__ int64_t qg_find_slot(const Slot *__restrict__ slots, uint64_t hmask, const Key<W> &k,
                                                 unsigned int *err) {

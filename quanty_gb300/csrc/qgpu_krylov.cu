@@ -382,8 +382,17 @@ extern "C" qg_status qg_lanczos_tridiag(qg_context ctx, qg_operator op, qg_basis
   double *a_hist = scal + 6 * nvec, *b_hist = a_hist + (size_t)nvec * (ntri + 1);
   qg_status st = QG_OK;
   k_zero<<<(unsigned)((nscal + 255) / 256), 256, 0, s>>>(scal, (int64_t)nscal);
-  cudaMemsetAsync(zero, 0, vb, s);
   ctx->launches++;
+  qg_status st0 = qg_check_launch(ctx, "lanczos state");
+  if (st0 == QG_OK) {
+    cudaError_t me = cudaMemsetAsync(zero, 0, vb, s);
+    if (me != cudaSuccess) st0 = qg_cuda_fail(ctx, me, "lanczos zero vector");
+  }
+  if (st0 != QG_OK) {
+    cudaFree(vp); cudaFree(vc); cudaFree(w); cudaFree(w2); cudaFree(vraw); cudaFree(zero);
+    cudaFree(npart); cudaFree(dpart); cudaFree(scal);
+    return st0;
+  }
   // the normalised, truncated Krylov vector vc from a raw vector: for one vector the same
   // kernel also writes it into the basis' hash slots for the gather
   auto normalise = [&](const double2 *raw) -> qg_status {
@@ -396,11 +405,12 @@ extern "C" qg_status qg_lanczos_tridiag(qg_context ctx, qg_operator op, qg_basis
   launch_dot_partial(P, n, nvec, (const double2 *)v0_dev, nullptr, npart, s);
   k_fin_b<<<1, 256, 0, s>>>(npart, P, nvec, b_now, b_hist, ntri, 0, scale, thr2, err, eps, gamma, 1);
   ctx->launches += 2;
+  st = qg_check_launch(ctx, "lanczos start norm");
   ApplyFuse fz;
   fz.prev = zero;
   fz.beta = zb;
   fz.dot_part = dpart;
-  st = normalise((const double2 *)v0_dev);
+  if (st == QG_OK) st = normalise((const double2 *)v0_dev);
   if (st == QG_OK)
     st = qg_apply_strided(ctx, op, b, b, (const double *)vc, nvec, (double *)w, nvec, nvec, &fz, nvec == 1);
   if (st == QG_OK && krylov_dev)

@@ -207,11 +207,18 @@ void build_table(qg_context ctx, const std::vector<Entry> &terms, HostTable &tab
   }
   tab.ngroups = (int)g.size();
   tab.nterms = (int)tt.size();
+  // group index of every term (for kernels that hand terms, not groups, to threads)
+  std::vector<uint32_t> tg(tt.size());
+  for (int k = 0; k < (int)g.size(); k++)
+    for (int t = g[k].begin; t < g[k].end; t++) tg[t] = (uint32_t)k;
   size_t gb = g.size() * sizeof(GroupDev<W>), tb = tt.size() * sizeof(TermDev<W>);
-  tab.bytes = gb + tb;
+  size_t tgb = (tg.size() * 4 + 15) / 16 * 16;
+  tab.tgrp_off = gb + tb;
+  tab.bytes = gb + tb + tgb;
   std::vector<unsigned char> blob(std::max<size_t>(tab.bytes, 16), 0);
   if (gb) std::memcpy(blob.data(), g.data(), gb);
   if (tb) std::memcpy(blob.data() + gb, tt.data(), tb);
+  if (!tg.empty()) std::memcpy(blob.data() + gb + tb, tg.data(), tg.size() * 4);
   cudaError_t e = cudaMalloc(&tab.d_blob, blob.size());
   if (e == cudaSuccess) e = cudaMemcpy(tab.d_blob, blob.data(), blob.size(), cudaMemcpyHostToDevice);
   tab.d_groups = tab.d_blob;

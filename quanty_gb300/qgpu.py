@@ -61,6 +61,7 @@ def load(path=LIB_PATH):
         "qg_hermitian_eigh": (C.c_int, [I32, P, P, P, I32]),
         "qg_gather_bandwidth": (C.c_int, [P, I64, P]),
         "qg_apply_chunk": (C.c_int, [P, P, P, I32, P]),
+        "qg_apply_set_chunk": (C.c_int, [P, P, P, I32, I32]),
         "qg_expectation": (C.c_int, [P, P, P, P, I32, P]),
         "qg_dot": (C.c_int, [P, I64, I32, P, P, P]),
         "qg_dot_noalloc": (C.c_int, [I64, I32, P, P, P, P]),

@@ -156,6 +156,65 @@ def test_autotuned_chunk_gives_the_same_bits(api):
     assert torch.equal(Y1, Y2)
 
 
+@pytest.mark.parametrize("model", ["random", "anderson"])
+def test_every_vector_layout_gives_the_same_bits(api, model):
+    """Thread-per-row passes of 1/2/4/8 vectors and warp-per-row passes of 32/64 vectors
+    (lanes over vectors) sum every vector's connections in the same order."""
+    import ctypes
+    import torch
+    from quanty_gb300 import workloads
+    eng = api.engine()
+    rng = np.random.default_rng(8)
+    if model == "random":
+        nf = 30
+        H = _random_operator(api, nf, 60, 60, rng)
+        seed = api.dets_to_bytes(["1" * 8 + "0" * 22], nf)
+        R = None
+    else:
+        H, R, s0, info = workloads.anderson_impurity(nshell=2, hole_max=2, particle_max=2)
+        nf = H.nf
+        seed = api.dets_to_bytes([s0], nf)
+    nvec = 40
+    out = {}
+    for chunk in (1, 2, 8, -32, -64):
+        b = api.closure(H, seed, nf, R, 3 if model == "random" else -1)
+        if chunk == 1:
+            X = torch.from_numpy(rng.normal(size=(b.n, nvec)) + 1j * rng.normal(size=(b.n, nvec))).cuda()
+        Y = eng.empty(b.n, nvec)
+        eng.check(eng.L.qg_apply_set_chunk(eng.ctx, H.handle(), b.h, nvec, chunk))
+        eng.check(eng.L.qg_apply(eng.ctx, H.handle(), b.h, b.h, api._ptr(X), api._ptr(Y), nvec))
+        ch = ctypes.c_int32()
+        eng.check(eng.L.qg_apply_chunk(eng.ctx, H.handle(), b.h, nvec, ctypes.byref(ch)))
+        assert ch.value == chunk
+        out[chunk] = Y
+    for chunk, Y in out.items():
+        assert torch.equal(Y, out[1]), chunk
+
+
+def test_batched_lanczos_with_warp_layout_matches_single(api):
+    import torch
+    from quanty_gb300 import workloads
+    eng = api.engine()
+    H, R, s0, info = workloads.anderson_impurity(nshell=2, hole_max=2, particle_max=2)
+    b = api.closure(H, api.dets_to_bytes([s0], H.nf), H.nf, R)
+    rng = np.random.default_rng(9)
+    nvec = 36
+    X = torch.from_numpy(rng.normal(size=(b.n, nvec)) + 1j * rng.normal(size=(b.n, nvec))).cuda()
+    eng.check(eng.L.qg_apply_set_chunk(eng.ctx, H.handle(), b.h, nvec, -64))
+    A, B = api.lanczos_block(H, b, X.clone(), 20, 0.0, 0.0, eng)
+    for k in (0, 17, 35):
+        a, bb = api.lanczos_block(H, b, X[:, k:k + 1].contiguous(), 20, 0.0, 0.0, eng)
+        # the block's inner products are reduced in another order; without reorthogonalisation
+        # such last-bit differences grow about tenfold per step once orthogonality is lost
+        # (here after ~20 steps on a basis of a few thousand determinants), so the chains are
+        # compared over their first 20 steps
+        assert np.max(np.abs(A[k] - a[0])) < 1e-10 * np.max(np.abs(a[0]))
+        assert np.max(np.abs(B[k] - bb[0])) < 1e-10 * np.max(np.abs(bb[0]))
+        g1 = api.TriDiagonalMatrixToSpectrum(0.0, A[k], B[k], -20.0, 20.0, 400, 0.5, eng)
+        g0 = api.TriDiagonalMatrixToSpectrum(0.0, a[0], bb[0], -20.0, 20.0, 400, 0.5, eng)
+        assert np.max(np.abs(g1 - g0)) < 1e-8 * np.max(np.abs(g0))
+
+
 def test_edge_cases(api):
     H = api.NewOperator(4, 0, [[0, -1, 0.5], [1, -0.0, 0.5]])
     empty = api.Wavefunction(4, np.zeros((0, 1), np.uint8), [])
