@@ -165,6 +165,12 @@ class Operator:
     def __add__(self, other):
         return Operator(self.nf, self.terms + other.terms)
 
+    def dagger(self):
+        """Conjugate transpose (the reference's ConjugateTranspose): each ladder string reversed
+        with creation and annihilation exchanged, each value conjugated."""
+        return Operator(self.nf, [(tuple(o ^ CREATION for o in reversed(ops)), complex(v).conjugate())
+                                  for ops, v in self.terms], name=self.name + "^dag")
+
     def __mul__(self, other):
         if isinstance(other, Wavefunction):
             return OperatorPsi(self, other)

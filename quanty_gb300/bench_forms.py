@@ -149,10 +149,11 @@ def batched(args):
               "Emin1": -8.0, "Emax1": 8.0, "NE1": 63, "Gamma1": 0.4,
               "Emin2": -2.0, "Emax2": 10.0, "NE2": 1024, "Gamma2": 0.1,
               "Restrictions1": Rx, "Restrictions2": R}
-        G, _ = api.CreateResonantSpectra(H, H, Ts[2], Ts, psi0, ro, eng)  # warm
+        Te = [t.dagger() for t in Ts]  # emission: 3d -> 2p
+        G, _ = api.CreateResonantSpectra(H, H, Ts[2], Te, psi0, ro, eng)  # warm
         _sync(eng)
         t0 = time.perf_counter()
-        G, st = api.CreateResonantSpectra(H, H, Ts[2], Ts, psi0, ro, eng)
+        G, st = api.CreateResonantSpectra(H, H, Ts[2], Te, psi0, ro, eng)
         _sync(eng)
         t_rixs = time.perf_counter() - t0
         _log("rixs: %d spectra in %.2f s" % (G.shape[0], t_rixs))
@@ -309,7 +310,64 @@ def served(args):
     return 0
 
 
+def layouts(args):
+    """The multi-vector apply alone: 48 random vectors on the core-excited basis of the
+    impurity with `--shells` bath shells (at most 1 hole, 2 particles); every vector layout
+    timed with CUDA events, or (with --layout) only that one, twice (a profiling target)."""
+    import ctypes
+    from . import api, workloads
+    eng = api.engine()
+    torch = eng.torch
+    nshell = int(args.shells)
+    H, R, seed, info = workloads.anderson_impurity(nshell=nshell, hole_max=1, particle_max=2)
+    _, Rx, _, _ = workloads.anderson_impurity(nshell=nshell, hole_max=1, particle_max=2, core_holes=1)
+    T = _xas_ops(api, workloads, H.nf)[2]
+    b0 = api.closure(H, api.dets_to_bytes([seed], H.nf), H.nf, R, -1, eng)
+    bf = api.closure_of(H, api.OperatorPsiBasis(T, b0, Rx, eng), Rx, -1, eng)
+    n, nvec = bf.n, 48
+    rng = np.random.default_rng(0)
+    with eng.on_stream():
+        X = torch.from_numpy(rng.normal(size=(n, nvec)) + 1j * rng.normal(size=(n, nvec))).to(
+            "cuda:%d" % eng.device)
+    Y = eng.empty(n, nvec)
+    eng.check(eng.L.qg_set_autotune(eng.ctx, 0))
+
+    def run(c, reps):
+        eng.check(eng.L.qg_apply_set_chunk(eng.ctx, H.handle(eng), bf.h, nvec, c))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(eng.stream)
+        for _ in range(reps):
+            eng.check(eng.L.qg_apply(eng.ctx, H.handle(eng), bf.h, bf.h, api._ptr(X), api._ptr(Y), nvec))
+        e1.record(eng.stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    if args.layout is not None:
+        run(int(args.layout), 2)
+        print(json.dumps({"mode": "layouts", "layout": int(args.layout), "n": n}))
+        return 0
+    out = {}
+    for c in (1, 2, 4, 8, -32, -64):
+        run(c, 1)
+        out[str(c)] = run(c, 3)
+    x1 = X[:, :1].contiguous()
+    y1 = eng.empty(n, 1)
+    eng.check(eng.L.qg_apply(eng.ctx, H.handle(eng), bf.h, bf.h, api._ptr(x1), api._ptr(y1), 1))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(eng.stream)
+    for _ in range(3):
+        eng.check(eng.L.qg_apply(eng.ctx, H.handle(eng), bf.h, bf.h, api._ptr(x1), api._ptr(y1), 1))
+    e1.record(eng.stream)
+    e1.synchronize()
+    nnz_off = api.count_nnz(H, bf, offdiag=True)
+    print(json.dumps({"mode": "layouts", "n": n, "nvec": nvec, "nnz_offdiag": nnz_off, "apply_ms": out,
+                      "one_vector_ms": e0.elapsed_time(e1) / 3}))
+    return 0
+
+
 def main(args):
     if args.mode == "batched":
         return batched(args)
+    if args.mode == "layouts":
+        return layouts(args)
     return served(args)

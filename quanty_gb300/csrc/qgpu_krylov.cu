@@ -349,6 +349,11 @@ extern "C" qg_status qg_lanczos_tridiag(qg_context ctx, qg_operator op, qg_basis
   }
   cudaStream_t s = ctx->stream;
   int64_t n = b->n;
+  if (n == 0) {  // an empty start vector: every coefficient is zero (the spectrum vanishes)
+    for (int64_t k = 0; k < (int64_t)nvec * (ntri + 1); k++) a_host[k] = 0.0;
+    for (int64_t k = 0; k < (int64_t)nvec * ntri; k++) b_host[k] = 0.0;
+    return QG_OK;
+  }
   int64_t len = n * nvec;  // complex entries per block vector
   int P = partial_blocks(ctx, n);
   int Papply = qg_apply_grid(b);
