@@ -53,6 +53,7 @@ def parse():
     p.add_argument("--rate", type=float, default=50.0)
     p.add_argument("--slots", type=int, default=4)
     p.add_argument("--restarts", type=int, default=20)
+    p.add_argument("--policy", default="sjf", choices=["fifo", "sjf"])
     return p.parse_args()
 
 
@@ -179,7 +180,7 @@ def xas_spectra_rate(api):
     ops, R = workloads.ligand_field()
     eng = api.engine()
     psis, E = api.Eigensystem(ops["H"], [26, 0] + [list(r) for r in R], 3, {"Zero": 1e-12}, eng=eng)
-    o = {"Emin": -10, "Emax": 20, "NE": 2048, "Gamma": 0.5, "NTri": 200, "Epsilon": 0.0}
+    o = {"Emin": -10, "Emax": 20, "NE": 2048, "Gamma": 0.5, "NTri": 200, "Epsilon": 0.0, "Method": "Lanczos"}
     Ts = [ops["Tx"], ops["Ty"], ops["Tz"]]
     out = {}
     for mode in (True, False):

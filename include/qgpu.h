@@ -135,6 +135,20 @@ qg_status qg_basis_map(qg_context ctx, qg_basis src, const double *x_dev, qg_bas
 qg_status qg_apply(qg_context ctx, qg_operator op, qg_basis basis_dst, qg_basis basis_src,
                    const double *x_dev, double *y_dev, int32_t nvec);
 
+/* ------------------------------------------------------------------ dense path (small bases) */
+
+/* op as a dense matrix on a basis (OperatorToDeterminantMatrix, Core/MatrixOperator.cpp:1149):
+ * m_host receives n x n complex values row-major interleaved, m[r][c] = <r|op|c>.  n <= 16384;
+ * the reference takes this path below DenseBorder = 1513 determinants. */
+qg_status qg_operator_dense(qg_context ctx, qg_operator op, qg_basis basis, double *m_host);
+
+/* Spectra from lists of poles (ListOfPolesToSpectrum, Core/Spectral.cpp:1516, Gamma > 0):
+ * G_s(w) = sum_k b[s][k] / (w - a[s][k] + i gamma/2) at w = emin + k*de + e0[s], k = 0..ne;
+ * a_host, b_host nspec x npole row-major; g_host nspec*(ne+1) complex (interleaved). */
+qg_status qg_poles_spectra(qg_context ctx, int32_t nspec, int32_t npole, const double *a_host,
+                           const double *b_host, const double *e0_host, double emin, double de,
+                           int32_t ne, double gamma, double *g_host);
+
 /* Random-sector gather bandwidth of the device in GB/s (no counterpart in the reference):
  * reads of 32-byte sectors at unrelated addresses spread over a buffer of `bytes` (>= 1 MiB,
  * allocated and freed here).  The ceiling for hash-probed gathers, measured for the roofline. */

@@ -270,6 +270,22 @@ def cf_spectrum(a, b, e0, emin, de, ne, gamma):
     return gre + 1j * gim
 
 
+def poles_spectrum(a, b, e0, emin, de, ne, gamma):
+    """Sum of Lorentzians on NE+1 points (reference ListOfPolesToSpectrum, Core/Spectral.cpp:1516,
+    Gamma > 0 branch :1576-1588): G(w) = sum_k b_k (w - a_k - i gamma/2) / ((gamma/2)^2 + (w - a_k)^2)
+    at w = emin + k de + e0, summed in pole order."""
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    out = np.zeros(ne + 1, dtype=np.complex128)
+    hg = gamma / 2.0
+    for k in range(ne + 1):
+        w = k * de + emin + e0
+        d = w - a
+        den = hg * hg + d * d
+        out[k] = complex(np.sum(b * d / den), np.sum(b * (-hg) / den))
+    return out
+
+
 def closure(op, seed, restrictions=None, max_rounds=10000):
     """All determinants reachable from the seed determinants under repeated H (within the
     restrictions); the seed comes first, then targets in discovery order."""

@@ -230,6 +230,21 @@ class Wavefunction:
     def as_dict(self):
         return {bytes(r): v for r, v in zip(self.det, self.val)}
 
+    def put(self, var=None, complex_values=None, name="Wave Function", nbitskey=16):
+        """The reference's io.put text of this wavefunction (get_put.cpp:588-634)."""
+        from .quanty_text import format_wavefunction
+        wf = {"nf": self.nf, "nb": 0, "dets": self.dets(), "re": list(self.val.real), "im": list(self.val.imag),
+              "name": name, "nbitskey": nbitskey}
+        if complex_values is not None:
+            wf["complex"] = bool(complex_values)
+        return format_wavefunction(wf, var)
+
+    @classmethod
+    def from_put(cls, text):
+        from .quanty_text import parse_wavefunction
+        d = parse_wavefunction(text)
+        return cls(d["nf"], dets_to_bytes(d["dets"], d["nf"]), np.array(d["re"]) + 1j * np.array(d["im"]))
+
     def norm(self):
         return float(np.linalg.norm(self.val))
 
@@ -455,14 +470,112 @@ def _opts(options):
 
 
 class Spectra:
-    """CreateSpectra's result: G_s(w) on NE+1 points per spectrum (SpectraType, Core/StructDef.cpp:986)."""
+    """CreateSpectra's result: G_s(w) on NE+1 points per spectrum (SpectraType, Core/StructDef.cpp:986),
+    with the pole range the energy window defaults were taken from."""
 
-    def __init__(self, G, Emin, Emax, NE, Gamma):
-        self.G, self.Emin, self.Emax, self.NE, self.Gamma = G, Emin, Emax, NE, Gamma
+    def __init__(self, G, Emin, Emax, NE, Gamma, EminPole=float("nan"), EmaxPole=float("nan")):
+        self.G, self.Emin, self.Emax, self.NE, self.Gamma = np.atleast_2d(G), Emin, Emax, NE, Gamma
+        self.EminPole, self.EmaxPole = EminPole, EmaxPole
 
     @property
     def energies(self):
         return self.Emin + np.arange(self.NE + 1) * (self.Emax - self.Emin) / self.NE
+
+    def Print(self, file=None):
+        """The reference's spectra file (Spectra.Print, StreamPrintSpectra IO/StreamPrint.cpp:4):
+        three header lines of window, pole range and (dE, Gamma) per spectrum, a column header,
+        then one line per frequency.  Returns the text; writes it to `file` when given."""
+        ns = self.G.shape[0]
+        de = (self.Emax - self.Emin) / self.NE
+        out = ["#Spectra: %i\n" % ns]
+        out.append("Emin______Emax     " + "".join(" %22.15E %22.15E" % (self.Emin, self.Emax) for _ in range(ns)) + "\n")
+        out.append("EminPole__EmaxPole " + "".join(" %22.15E %22.15E" % (self.EminPole, self.EmaxPole)
+                                                   for _ in range(ns)) + "\n")
+        out.append("dE________Gamma    " + "".join(" %22.15E %22.15E" % (de, self.Gamma) for _ in range(ns)) + "\n")
+        hdr = "Energy             "
+        for i in range(ns):
+            w = len(str(i))
+            hdr += "  Re[%s]%s Im[%s]%s" % (i, " " * (18 - w), i, " " * (17 - w))
+        out.append(hdr + "\n")
+        for j in range(self.NE + 1):
+            row = "%19.12E" % (de * j + self.Emin)
+            row += "".join(" %22.15E %22.15E" % (self.G[i, j].real, self.G[i, j].imag) for i in range(ns))
+            out.append(row + "\n")
+        text = "".join(out)
+        if file is not None:
+            with open(file, "w") as f:
+                f.write(text)
+        return text
+
+    @classmethod
+    def from_text(cls, text):
+        """Read a spectra file written by Print (or by the reference)."""
+        lines = text.splitlines()
+        ns = int(lines[0].split(":")[1])
+        emin, emax = (float(t) for t in lines[1].split()[1:3])
+        pmin, pmax = (float(t) for t in lines[2].split()[1:3])
+        de, gamma = (float(t) for t in lines[3].split()[1:3])
+        rows = [[float(t) for t in ln.split()] for ln in lines[5:] if ln.strip()]
+        G = np.array([[r[1 + 2 * i] + 1j * r[2 + 2 * i] for r in rows] for i in range(ns)])
+        return cls(G, emin, emax, len(rows) - 1, gamma, pmin, pmax)
+
+
+# ----------------------------------------------------------------------------- dense path
+
+def OperatorToDeterminantMatrix(O, basis, eng=None):
+    """O as a dense matrix on a device basis (Core/MatrixOperator.cpp:1149): M[r, c] = <r|O|c>."""
+    eng = eng or engine()
+    n = basis.n
+    m = np.zeros((max(n, 1), max(n, 1)), dtype=np.complex128)
+    eng.check(eng.L.qg_operator_dense(eng.ctx, O.handle(eng), basis.h, _ptr(m)))
+    return m[:n, :n]
+
+
+def hermitian_eigh(M, nvec=None, eng=None):
+    """All eigenvalues (ascending) and the lowest nvec eigenvectors (columns) of a Hermitian
+    matrix, by the library's host Householder + QL solver."""
+    eng = eng or engine()
+    k = M.shape[0]
+    nv = k if nvec is None else int(nvec)
+    a = np.ascontiguousarray(M, dtype=np.complex128)
+    w = np.zeros(k)
+    v = np.zeros((k, max(nv, 1)), dtype=np.complex128)
+    eng.check(eng.L.qg_hermitian_eigh(k, _ptr(a), _ptr(w), _ptr(v), nv))
+    return w, v[:, :nv]
+
+
+def ListOfPolesToSpectrum(E0, poles, weights, Emin, Emax, NE, Gamma, eng=None):
+    """G(w) = sum_k b_k / (w - a_k + i Gamma/2) at w = Emin + k dE + E0 (Core/Spectral.cpp:1516);
+    poles and weights may hold several spectra as rows."""
+    eng = eng or engine()
+    b = np.ascontiguousarray(np.atleast_2d(weights), dtype=np.float64)
+    ns, npole = b.shape
+    a = np.ascontiguousarray(np.broadcast_to(np.atleast_2d(np.asarray(poles, dtype=np.float64)), (ns, npole)))
+    e0 = np.ascontiguousarray(np.broadcast_to(np.asarray(E0, dtype=np.float64), (ns,)))
+    g = np.zeros(2 * ns * (NE + 1))
+    eng.check(eng.L.qg_poles_spectra(eng.ctx, ns, npole, _ptr(a), _ptr(b), _ptr(e0), float(Emin),
+                                     (Emax - Emin) / NE, int(NE), float(Gamma), _ptr(g)))
+    return (g[0::2] + 1j * g[1::2]).reshape(ns, NE + 1)
+
+
+def _spectra_dense(H, Tpsi, e0, o, basis, eng):
+    """CreateSpectra's dense branch (LuaInterface/ssp.cpp:2347-2460): the eigensystem of H on
+    the union basis, poles at its eigenvalues with weights |<E_k|T psi>|^2."""
+    n = basis.n
+    w, V = hermitian_eigh(OperatorToDeterminantMatrix(H, basis, eng), n, eng)
+    X = np.zeros((n, len(Tpsi)), dtype=np.complex128)
+    for s, t in enumerate(Tpsi):
+        if t.N:
+            rows = basis.find(t.det)
+            np.add.at(X[:, s], rows, t.val)
+    Wt = np.abs(V.conj().T @ X) ** 2  # (pole, spectrum)
+    lo = min(w[0] - e for e in e0)
+    hi = max(w[-1] - e for e in e0)
+    NE = int(o["NE"])
+    emin, emax, gamma = _default_window(lo, hi, o["Emin"], o["Emax"], float(o["Gamma"]), NE)
+    G = ListOfPolesToSpectrum(np.asarray(e0), np.tile(w, (len(Tpsi), 1)), Wt.T, emin, emax, NE, gamma, eng)
+    poles = [(w - e0[s], Wt[:, s].copy()) for s in range(len(Tpsi))]
+    return Spectra(G, emin, emax, NE, gamma, lo, hi), poles
 
 
 def CreateSpectraResident(H, T, basis, X, E0, options=None, eng=None, batched=True, max_vectors=None):
@@ -510,9 +623,11 @@ def CreateSpectraResident(H, T, basis, X, E0, options=None, eng=None, batched=Tr
 
 
 def CreateSpectra(H, T, psi, options=None, eng=None, batched=True):
-    """Reference CreateSpectra, Lanczos branch (LuaInterface/ssp.cpp:2586-2720): spectra of all
-    (T, psi) pairs, ordered iT*Npsi + ipsi.  Returns (Spectra, [(a, b) shifted by -E0]).
-    batched=True runs all pairs as one multi-vector Lanczos on the union basis."""
+    """Reference CreateSpectra (LuaInterface/ssp.cpp:1906): spectra of all (T, psi) pairs,
+    ordered iT*Npsi + ipsi.  Lanczos branch (:2586-2720): returns (Spectra, [(a, b) shifted by
+    -E0]); batched=True runs all pairs as one multi-vector Lanczos on the union basis.  Dense
+    branch (:2347-2460; Method "Dense", or a union basis within DenseBorder unless Method is
+    "Lanczos"): returns (Spectra, [(poles - E0, weights)])."""
     eng = eng or engine()
     o = _opts(options)
     Ts = T if isinstance(T, (list, tuple)) else [T]
@@ -525,6 +640,14 @@ def CreateSpectra(H, T, psi, options=None, eng=None, batched=True):
         for p in psis:
             Tpsi.append(OperatorPsi(t, p, R, eng))
     e0 = np.array([E0[i % len(psis)] for i in range(len(Tpsi))])
+    # dense branch (ssp.cpp:2262-2319): Method "Dense", or the union basis of all T psi closed
+    # under H within DenseBorder determinants (unless Method is "Lanczos")
+    method = str(o.get("Method") or "").lower()
+    if method != "lanczos":
+        seed = np.concatenate([t.det for t in Tpsi if t.N] or [np.zeros((0, nword(H.nf)), np.uint8)])
+        ub = closure(H, seed, H.nf, R, -1, eng) if len(seed) else None
+        if ub is not None and (method == "dense" or ub.n <= int(o["DenseBorder"])):
+            return _spectra_dense(H, Tpsi, e0, o, ub, eng)
     gamma = float(o["Gamma"])
     groups = [list(range(len(Tpsi)))] if batched else [[i] for i in range(len(Tpsi))]
     A = np.zeros((len(Tpsi), ntri + 1))
@@ -545,25 +668,44 @@ def CreateSpectra(H, T, psi, options=None, eng=None, batched=True):
         a, b = lanczos_block(H, basis, x, ntri, eps, max(gamma, eps), eng)
         A[grp] = a
         B[grp] = b
-    # pole range -> default Emin/Emax/Gamma (ssp.cpp:2655-2689) when not given
-    emin, emax = o["Emin"], o["Emax"]
-    if emin is None or emax is None or gamma == 0:
-        from numpy.linalg import eigvalsh
-        lo, hi = np.inf, -np.inf
-        for s in range(len(Tpsi)):
-            Tm = np.diag(A[s, 1:]) + np.diag(B[s, 1:], 1) + np.diag(B[s, 1:], -1)
-            w = eigvalsh(Tm)
-            lo, hi = min(lo, w[0] - e0[s]), max(hi, w[-1] - e0[s])
-        if emin is None:
-            emin = lo - 0.125 * (hi - lo)
-        if emax is None:
-            emax = hi + 0.125 * (hi - lo)
-        if gamma == 0:
-            gamma = 10 * (emax - emin) / o["NE"]
-    NE = int(o["NE"])
+    # pole range from the eigenvalues of every tridiagonal matrix, and from it the default
+    # Emin/Emax/Gamma (ssp.cpp:2651-2684)
+    lo, hi = np.inf, -np.inf
+    for s in range(len(Tpsi)):
+        m = ntri
+        for k in range(1, ntri):  # a chain that ended early (b = 0) is shorter
+            if B[s, k] == 0.0:
+                m = k
+                break
+        Tm = np.diag(A[s, 1:m + 1]) + np.diag(B[s, 1:m], 1) + np.diag(B[s, 1:m], -1)
+        w = np.linalg.eigvalsh(Tm)
+        lo, hi = min(lo, w[0] - e0[s]), max(hi, w[-1] - e0[s])
+    emin, emax, NE = o["Emin"], o["Emax"], int(o["NE"])
+    emin, emax, gamma = _default_window(lo, hi, emin, emax, gamma, NE)
     G = TriDiagonalMatrixToSpectrum(e0, A, B, emin, emax, NE, gamma, eng)
     tri = [(np.r_[0.0, A[s, 1:] - e0[s]], B[s].copy()) for s in range(len(Tpsi))]
-    return Spectra(G, emin, emax, NE, gamma), tri
+    return Spectra(G, emin, emax, NE, gamma, lo, hi), tri
+
+
+def _default_window(lo, hi, emin, emax, gamma, NE):
+    """Emin/Emax/Gamma not given: from the pole range [lo, hi] (ssp.cpp:2664-2684)."""
+    if lo == hi:
+        if lo == 0:
+            emin = -1.0 if emin is None else emin
+            emax = 1.0 if emax is None else emax
+        elif lo < 0:
+            emin = 2.125 * lo if emin is None else emin
+            emax = -0.125 * lo if emax is None else emax
+        else:
+            emin = -0.125 * lo if emin is None else emin
+            emax = 2.125 * lo if emax is None else emax
+    if emin is None:
+        emin = lo - 0.125 * (hi - lo)
+    if emax is None:
+        emax = hi + 0.125 * (hi - lo)
+    if gamma == 0:
+        gamma = 10 * (emax - emin) / NE
+    return emin, emax, gamma
 
 
 # ----------------------------------------------------------------------------- eigensystem
@@ -610,6 +752,11 @@ def Eigensystem(H, StartRestrictions, Npsi, options=None, eng=None, seed=12345):
     dets = enumerate_restricted(H.nf, R)
     basis, _ = Basis.from_bytes(H.nf, dets, eng)
     basis = closure_of(H, basis, R, -1, eng)
+    if basis.n <= int(_opts(options)["DenseBorder"]):
+        # dense branch (BlockLanczosGroundStateConserveBasisDense, Core/BlockLanczos.cpp:370)
+        w, V = hermitian_eigh(OperatorToDeterminantMatrix(H, basis, eng), min(Npsi, basis.n), eng)
+        db = basis.dets_bytes()
+        return [Wavefunction(H.nf, db, V[:, k]) for k in range(V.shape[1])], w[:V.shape[1]]
     x, en = EigensystemOnBasis(H, basis, Npsi, options, eng, seed)
     X = eng.to_host(x)
     db = basis.dets_bytes()

@@ -276,7 +276,7 @@ def served(args):
     for k in warm:
         jobs[k].run(eng)
     _sync(eng)
-    res_s, lat_s, wall_s = serve.run_stream(jobs, rate, slots=int(args.slots), seed=1)
+    res_s, lat_s, wall_s = serve.run_stream(jobs, rate, slots=int(args.slots), seed=1, policy=args.policy)
     res_p, lat_p, wall_p = serve.run_plain(jobs, rate, seed=1, eng=eng)
     diff = 0.0
     for a, b in zip(res_s, res_p):
@@ -295,7 +295,7 @@ def served(args):
         "dtype": "c128",
         "data": "synthetic (seeded impurity Hamiltonians, Poisson arrivals)",
         "config": {"workload": "poisson_stream_mixed_impurity_jobs", "jobs": len(jobs), "rate_per_s": rate,
-                   "slots": int(args.slots), "spectra": nspec,
+                   "slots": int(args.slots), "policy": args.policy, "spectra": nspec,
                    "eigen_jobs": sum(p["kind"] == "eigen" for p in params),
                    "max_det": float(args.max_det), "determinants_min": int(min(sizes)),
                    "determinants_max": int(max(sizes))},

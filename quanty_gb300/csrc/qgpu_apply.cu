@@ -32,6 +32,10 @@ static inline unsigned grid_for(int64_t n, int bs) { return (unsigned)((n + bs -
 
 #define QG_SMEM_TABLE_MAX (96 * 1024)
 #define QG_MBAR_SPIN_LIMIT (1 << 24)
+#ifndef QG_LOCAL_UNROLL
+#define QG_LOCAL_UNROLL 1
+#endif
+static constexpr int kLocalUnroll = QG_LOCAL_UNROLL;  // local moves unrolled per iteration
 
 __device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -110,6 +114,7 @@ struct LocalView {
   const int32_t *cfg;
   const uint32_t *bstart, *eoff;
   const LocalEntry *ent;
+  const uint32_t *etarget;
 };
 
 template <int W>
@@ -225,15 +230,15 @@ __global__ void __launch_bounds__(256) k_apply(const Key<W> *__restrict__ rows, 
       uint32_t rs = __ldg(lv.bstart + b);
       int64_t off = r - (int64_t)rs;
       uint32_t e1 = __ldg(lv.eoff + b + 1);
+#pragma unroll (kLocalUnroll)
       for (uint32_t e = __ldg(lv.eoff + b); e < e1; e++) {
         const LocalEntry *E = lv.ent + e;
-        uint32_t tbr = __ldg(&E->tblock);
-        uint32_t tbk = tbr & 0x7FFFFFFFu;
-        int64_t j = (int64_t)__ldg(lv.bstart + tbk) + off;
-        if (!(tbr >> 31)) {
-          Key<W> s = set_local<W>(d, lv.lo, lv.lmask, __ldg(&E->target));
+        uint32_t te = __ldg(&E->tend);
+        int64_t j = (int64_t)__ldg(&E->tstart) + off;
+        if (!(te >> 31)) {
+          Key<W> s = set_local<W>(d, lv.lo, lv.lmask, __ldg(lv.etarget + e));
           bool hit = false;
-          if (j < (int64_t)__ldg(lv.bstart + tbk + 1)) {
+          if (j < (int64_t)(te & 0x7FFFFFFFu)) {
             Key<W> kj = rows[j];
             hit = qg_eq<W>(kj, s);
           }
@@ -496,14 +501,13 @@ __global__ void __launch_bounds__(256) k_apply_warp(const Key<W> *__restrict__ r
         double vr = 0.0, vi = 0.0;
         if (ee < e1) {
           const LocalEntry *E = lv.ent + ee;
-          uint32_t tbr = __ldg(&E->tblock);
-          uint32_t tbk = tbr & 0x7FFFFFFFu;
-          j = (int64_t)__ldg(lv.bstart + tbk) + off;
-          if (tbr >> 31) {
+          uint32_t te = __ldg(&E->tend);
+          j = (int64_t)__ldg(&E->tstart) + off;
+          if (te >> 31) {
             has = true;
           } else {
-            Key<W> s = set_local<W>(d, lv.lo, lv.lmask, __ldg(&E->target));
-            if (j < (int64_t)__ldg(lv.bstart + tbk + 1)) has = qg_eq<W>(rows[j], s);
+            Key<W> s = set_local<W>(d, lv.lo, lv.lmask, __ldg(lv.etarget + ee));
+            if (j < (int64_t)(te & 0x7FFFFFFFu)) has = qg_eq<W>(rows[j], s);
             if (!has) {
               bool ok = true;
               if (src.nres) {
@@ -833,6 +837,7 @@ void qg_cache_free(OpBasisCache &c) {
   cudaFree(c.d_cfg);
   cudaFree(c.d_eoff);
   cudaFree(c.d_ent);
+  cudaFree(c.d_ent_target);
   c = OpBasisCache();
 }
 
@@ -990,6 +995,7 @@ static qg_status build_local(qg_basis bs, qg_operator op, OpBasisCache &c) {
                   t.im});
   std::vector<uint32_t> eoff(nb + 1, 0);
   std::vector<LocalEntry> ent;
+  std::vector<uint32_t> etarget;
   bool exact = true;
   for (uint32_t k = 0; k < nb; k++) {
     uint32_t cc = hcfg[k];
@@ -1007,8 +1013,9 @@ static qg_status build_local(qg_basis bs, qg_operator op, OpBasisCache &c) {
       int32_t tbk = table[kv.first];
       if (tbk < 0 || (kv.second.first == 0.0 && kv.second.second == 0.0)) continue;
       LocalEntry le;
-      le.tblock = (uint32_t)tbk | (cls[k] == cls[tbk] ? 0x80000000u : 0u);
-      le.target = kv.first;
+      le.tstart = hstart[tbk];
+      le.tend = hstart[tbk + 1] | (cls[k] == cls[tbk] ? 0x80000000u : 0u);
+      etarget.push_back(kv.first);
       le.vre = kv.second.first;
       le.vim = kv.second.second;
       le.wreq = 0;
@@ -1032,6 +1039,9 @@ static qg_status build_local(qg_basis bs, qg_operator op, OpBasisCache &c) {
   if (e == cudaSuccess) e = cudaMalloc(&c.d_ent, std::max<size_t>(ent.size(), 1) * sizeof(LocalEntry));
   if (e == cudaSuccess && !ent.empty())
     e = cudaMemcpy(c.d_ent, ent.data(), ent.size() * sizeof(LocalEntry), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMalloc(&c.d_ent_target, std::max<size_t>(etarget.size(), 1) * 4);
+  if (e == cudaSuccess && !etarget.empty())
+    e = cudaMemcpy(c.d_ent_target, etarget.data(), etarget.size() * 4, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return qg_cuda_fail(ctx, e, "local entries");
   if (!exact) c.wreq_exact = false;
   return QG_OK;
@@ -1199,6 +1209,7 @@ static qg_status apply_chunked(qg_context ctx, qg_operator op, qg_basis dst, qg_
       lv.bstart = c->d_bstart;
       lv.eoff = c->d_eoff;
       lv.ent = c->d_ent;
+      lv.etarget = c->d_ent_target;
     } else {
       tab = &op->pull_off;
     }

@@ -138,9 +138,9 @@ struct qg_operator_s {
 
 // Per-(operator, basis) precomputed data for the same-basis H*psi.
 struct LocalEntry {
-  uint32_t tblock;   // block of the target local configuration; bit 31: both blocks list the
-                     // same non-local configurations, so the target row is at the same offset
-  uint32_t target;   // target local configuration
+  uint32_t tstart;   // first row of the target local configuration's block
+  uint32_t tend;     // one past its last row; bit 31: both blocks list the same non-local
+                     // configurations, so the target row is at the same offset
   uint64_t wreq;     // window bits the target needs (see qgpu_apply.cu)
   double vre, vim;   // merged, signed coefficient
 };
@@ -156,6 +156,7 @@ struct OpBasisCache {
   int32_t *d_cfg = nullptr;       // [2^H] local configuration -> block, -1 if absent
   uint32_t *d_eoff = nullptr;     // [nblocks + 1]
   LocalEntry *d_ent = nullptr;
+  uint32_t *d_ent_target = nullptr;  // target local configuration of each entry
   int64_t nent = 0;
   // autotuned vectors per pass of the apply kernel, per number of vectors (pairs nvec, chunk)
   std::vector<std::pair<int, int>> chunk;

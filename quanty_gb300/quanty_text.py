@@ -81,19 +81,47 @@ def parse_operator(text):
 
 
 def parse_wavefunction(text):
-    """Parse one ``NewWavefunction(...)`` record into ``{"nf", "nb", "dets", "re", "im"}``."""
+    """Parse one ``NewWavefunction(...)`` record into ``{"nf", "nb", "dets", "re", "im"}``
+    (plus ``complex``, ``name`` and ``nbitskey`` when the record states them)."""
     nf, nb, start = _header(text, "NewWavefunction")
     body = _body(text, start)
     dets, re_, im = [], [], []
+    cplx = False
     for m in re.finditer(r'\{\s*"([01 0-9A-F]*)"\s*,([^{}]*)\}', body):
         d = m.group(1).strip()
         if nb:
             raise ValueError("bosonic determinants are not supported")
+        cplx |= "I" in m.group(2)
         v = _parse_value(m.group(2))
         dets.append(d[:nf])
         re_.append(v[0])
         im.append(v[1])
-    return {"nf": nf, "nb": nb, "dets": dets, "re": re_, "im": im}
+    out = {"nf": nf, "nb": nb, "dets": dets, "re": re_, "im": im, "complex": cplx}
+    m = re.search(r'\{"Name",\s*"((?:[^"\\]|\\.)*)"\}', text)
+    if m:
+        out["name"] = m.group(1)
+    m = re.search(r'\{"NBitsKey",\s*(\d+)\}', text)
+    if m:
+        out["nbitskey"] = int(m.group(1))
+    return out
+
+
+def format_wavefunction(wf, var=None):
+    """The ``io.put`` text of a wavefunction (LuaInterface/lua_extensions/get_put.cpp:588-634):
+    one ``{"0101...", value}`` line per determinant in the stored order, values ``%23.16E`` and,
+    for a complex wavefunction, ``re +/- I * |im|`` on every line; then the name and NBitsKey.
+    ``wf`` is a dict as returned by :func:`parse_wavefunction` (``complex``, ``name`` and
+    ``nbitskey`` default to any non-zero imaginary part, "Wave Function" and 16)."""
+    cplx = wf.get("complex", any(v != 0.0 for v in wf["im"]))
+    lines = []
+    for d, vr, vi in zip(wf["dets"], wf["re"], wf["im"]):
+        val = "%23.16E" % vr
+        if cplx:
+            val += (" - I * " if vi < 0 else " + I * ") + "%23.16E" % abs(vi)
+        lines.append('{"%s",%s}' % (d, val))
+    text = "NewWavefunction( %d, %d,{\n%s},\n{{\"Name\",\"%s\"},{\"NBitsKey\",%d}})" % (
+        wf["nf"], wf.get("nb", 0), ",\n".join(lines), wf.get("name", "Wave Function"), wf.get("nbitskey", 16))
+    return text if var is None else "%s = %s" % (var, text)
 
 
 def format_operator(op, name="O"):

@@ -74,9 +74,12 @@ class EigenJob:
 class Server:
     """Continuous batching over a fixed set of device slots with HBM-budget admission."""
 
-    def __init__(self, slots=4, hbm_budget=None, device=0):
+    def __init__(self, slots=4, hbm_budget=None, device=0, policy="fifo"):
         import torch
         self.torch = torch
+        if policy not in ("fifo", "sjf"):
+            raise ValueError("policy is 'fifo' or 'sjf'")
+        self.policy = policy
         if hbm_budget is None:
             free, total = torch.cuda.mem_get_info(device)
             hbm_budget = int(0.8 * free)
@@ -102,15 +105,22 @@ class Server:
         return fut
 
     def _admit(self):
-        """Oldest job whose footprint fits; a job larger than the whole budget runs alone."""
-        for i, rec in enumerate(self.queue):
-            need = rec["job"].footprint()
-            if self.in_use + need <= self.budget or (self.in_use == 0 and need > self.budget):
-                del self.queue[i]
-                self.in_use += need
-                rec["need"] = need
-                return rec
-            break  # first-come first-served: do not overtake a waiting job
+        """fifo: the oldest job, when its footprint fits.  sjf: the waiting job with the smallest
+        footprint (the oldest among equals), when it fits.  A job larger than the whole budget
+        runs alone."""
+        if not self.queue:
+            return None
+        if getattr(self, "policy", "fifo") == "sjf":
+            i = min(range(len(self.queue)), key=lambda k: (self.queue[k]["job"].footprint(), k))
+        else:
+            i = 0  # first-come first-served: do not overtake a waiting job
+        rec = self.queue[i]
+        need = rec["job"].footprint()
+        if self.in_use + need <= self.budget or (self.in_use == 0 and need > self.budget):
+            del self.queue[i]
+            self.in_use += need
+            rec["need"] = need
+            return rec
         return None
 
     def _worker(self, eng):
@@ -152,12 +162,12 @@ class Server:
         return np.array([r["end"] - r["arrival"] for r in self.records])
 
 
-def run_stream(jobs, rate, slots=4, hbm_budget=None, seed=0, server=None):
+def run_stream(jobs, rate, slots=4, hbm_budget=None, seed=0, server=None, policy="fifo"):
     """Submit jobs at Poisson arrival times (mean `rate` per second); wait for all.
     Returns (results in submission order, latencies, wall seconds)."""
     rng = np.random.default_rng(seed)
     gaps = rng.exponential(1.0 / rate, len(jobs))
-    srv = server or Server(slots=slots, hbm_budget=hbm_budget)
+    srv = server or Server(slots=slots, hbm_budget=hbm_budget, policy=policy)
     t0 = time.perf_counter()
     futs = []
     for gap, job in zip(gaps, jobs):

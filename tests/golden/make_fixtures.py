@@ -257,9 +257,21 @@ def gen_fshell():
     save("fshell_eigen.json", out)
 
 
+def gen_print():
+    """Spectra.Print files of the reference, kept as text (the byte layout of spectra files)."""
+    work = run(open(os.path.join(HERE, "gen", "print_fmt.lua")).read(), "print_fmt.lua")
+    out = {"source": "tests/golden/gen/print_fmt.lua", "HX": op(work, "HX"), "Tz": op(work, "Tz"),
+           "psi": [wf(work, "psi1"), wf(work, "psi2")]}
+    for k in ("lanczos", "defaults", "dense"):
+        out["print_" + k] = open(os.path.join(work, "dump", "print_%s.dat" % k)).read()
+    for k in ("psi1", "psi2", "Tz"):
+        out["put_" + k] = open(os.path.join(work, "dump", fname(k))).read()
+    save("print_fmt.json", out)
+
+
 if __name__ == "__main__":
     if not os.path.exists(QUANTY):
         sys.exit("build the reference first: oracle/build_ref.sh")
-    which = sys.argv[1:] or ["hpsi", "c0", "c1", "chain", "fshell"]
+    which = sys.argv[1:] or ["hpsi", "c0", "c1", "chain", "fshell", "print"]
     for w in which:
         globals()["gen_" + w]()

@@ -32,5 +32,18 @@ def test_ground_energies(api, fx, key):
     g = golden(fx)
     H = api.Operator.from_fixture(g["H"])
     R = [len(g["restrictions"][0][0]), 0] + [list(r) for r in g["restrictions"]]
-    psis, E = api.Eigensystem(H, R, 3, {"Zero": 1e-14})
+    psis, E = api.Eigensystem(H, R, 3, {"Zero": 1e-14, "DenseBorder": 0})  # block Lanczos
     assert np.max(np.abs(E - np.array(g[key]))) < 1e-10, (E, g[key])
+
+
+@pytest.mark.parametrize("fx", ["c0_xas.json", "c1_lf.json"])
+def test_dense_eigensystem(api, fx):
+    """Bases within DenseBorder take the dense branch (BlockLanczosGroundStateConserveBasisDense,
+    Core/BlockLanczos.cpp:370): the reference's dense energies to 1e-10 eV."""
+    g = golden(fx)
+    H = api.Operator.from_fixture(g["H"])
+    R = [H.nf, 0] + [list(r) for r in g["restrictions"]]
+    psis, E = api.Eigensystem(H, R, 3, {"DenseBorder": 100000})
+    assert np.max(np.abs(np.array(E) - np.array(g["energies_dense"]))) < 1e-10
+    for p, e in zip(psis, E):
+        assert abs(api.PsiOperatorPsi(H, p).real / p.norm() ** 2 - e) < 1e-10

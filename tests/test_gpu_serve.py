@@ -32,7 +32,8 @@ def _jobs(api, serve, workloads):
     for k in range(3):
         psi = api.Wavefunction(H.nf, dets, rng.normal(size=len(dets)) + 1j * rng.normal(size=len(dets)))
         T = api.Operator(H.nf, [([6 + k], 1.0), ([7 + k], 0.5)])
-        o = {"Emin": -15, "Emax": 15, "NE": 1024, "Gamma": 0.4, "NTri": 150, "Restrictions": R}
+        o = {"Emin": -15, "Emax": 15, "NE": 1024, "Gamma": 0.4, "NTri": 150, "Restrictions": R,
+             "Method": "Lanczos"}
         jobs.append(serve.SpectraJob(H, [T], [psi], o, n_det_hint=info["sector_determinants"]))
     jobs.append(serve.EigenJob(api.Operator.from_fixture(g1["H"]),
                                [26, 0] + [list(r) for r in g1["restrictions"]], 3, {"Zero": 1e-14},

@@ -51,6 +51,7 @@ def test_xas_spectra_match_reference(api, fx, eps_key, batched):
     Ts = [api.Operator.from_fixture(g[t]) for t in ("Tx", "Ty", "Tz")]
     psis = [api.Wavefunction.from_fixture(p) for p in g["psi"]]
     o = dict(g["spectra_opts"])
+    o["Method"] = "Lanczos"
     if eps_key == "eps0":
         o["Epsilon"] = 0.0
     else:
@@ -119,3 +120,52 @@ def test_rixs_with_empty_final_basis_gives_zero(api):
          "Restrictions2": [16, 0, ["1111110000000000", 6, 6]]}
     G, st = api.CreateResonantSpectra(HX, HX, Ts[2], Ts, psi, o)  # T2 = absorption again: 2p4
     assert G.shape == (3 * 5, 51) and np.all(G == 0)
+
+
+def test_dense_spectra_match_reference(api):
+    """The dense branch (Method Dense): poles of H on the union basis, against the reference's
+    dense spectra of the same call (1e-8 relative)."""
+    g = golden("c0_xas.json")
+    HX = api.Operator.from_fixture(g["HX"])
+    Ts = [api.Operator.from_fixture(g[t]) for t in ("Tx", "Ty", "Tz")]
+    psis = [api.Wavefunction.from_fixture(p) for p in g["psi"]]
+    o = dict(g["spectra_opts"])
+    o["Method"] = "Dense"
+    S, poles = api.CreateSpectra(HX, Ts, psis, o)
+    ref = g["spec_dense"]
+    for s in range(9):
+        R = np.array(ref["re"][s]) + 1j * np.array(ref["im"][s])
+        assert spec_err(S.G[s], R) < SPEC_TOL, (s, spec_err(S.G[s], R))
+    # the same call through Lanczos at epsilon 0 (exact on this basis)
+    o["Method"] = "Lanczos"
+    o["Epsilon"] = 0.0
+    SL, _ = api.CreateSpectra(HX, Ts, psis, o)
+    assert spec_err(S.G, SL.G) < SPEC_TOL
+    # default options choose the dense branch on this small basis
+    S2, poles2 = api.CreateSpectra(HX, Ts, psis, dict(g["spectra_opts"]))
+    assert np.array_equal(S2.G, S.G) and len(poles2[0]) == 2
+
+
+def test_operator_dense_matches_oracle(api, oracle_mod):
+    g = golden("c0_xas.json")
+    HX = api.Operator.from_fixture(g["HX"])
+    psi = api.Wavefunction.from_fixture(g["psi"][0])
+    b = api.closure(HX, psi.det, HX.nf)
+    M = api.OperatorToDeterminantMatrix(HX, b)
+    dets = b.dets_bytes()
+    op = oracle_mod.Op({"nf": HX.nf, "terms": [[list(t[0]), t[1].real, t[1].imag] for t in HX.terms]})
+    want = oracle_mod.dense_matrix(op, oracle_mod.WF(HX.nf, dets, np.zeros(len(dets))))
+    assert np.max(np.abs(M - want)) < 1e-13 * np.max(np.abs(want))
+    assert np.max(np.abs(M - M.conj().T)) < 1e-13 * np.max(np.abs(M))
+
+
+def test_poles_kernel_matches_oracle(api, oracle_mod):
+    rng = np.random.default_rng(4)
+    ns, npole, ne = 5, 300, 901
+    a = rng.normal(size=(ns, npole)) * 4
+    b = np.abs(rng.normal(size=(ns, npole)))
+    e0 = rng.normal(size=ns)
+    G = api.ListOfPolesToSpectrum(e0, a, b, -9.0, 11.0, ne, 0.42)
+    for s in range(ns):
+        want = oracle_mod.poles_spectrum(a[s], b[s], e0[s], -9.0, 20.0 / ne, ne, 0.42)
+        assert spec_err(G[s], want) < 1e-13

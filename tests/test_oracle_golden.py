@@ -136,6 +136,38 @@ def test_xas_spectra_match_reference(oracle_mod, fx):
             k += 1
 
 
+def test_dense_spectra_match_reference(oracle_mod):
+    """The dense branch restated (CreateSpectra, LuaInterface/ssp.cpp:2347-2460): H on the
+    union basis of all T psi closed under H, its eigensystem, poles weighted by |<E_k|T psi>|^2
+    (Core/BasicMath/BasicMath_CompactMatrixVector.cpp:3990), summed Lorentzians
+    (Core/Spectral.cpp:1576-1588); against the reference's dense spectra of the same call."""
+    O = oracle_mod
+    g = golden("c0_xas.json")
+    HX = O.Op(g["HX"])
+    opts = g["spectra_opts"]
+    emin, emax, ne, gamma = opts["Emin"], opts["Emax"], opts["NE"], opts["Gamma"]
+    psis = [O.WF.from_fixture(p) for p in g["psi"]]
+    Tpsi, E0 = [], []
+    for T in ("Tx", "Ty", "Tz"):
+        Top = O.Op(g[T])
+        for psi in psis:
+            Tpsi.append(O.operator_psi(Top, psi))
+            E0.append(_expectation(O, HX, psi))
+    seed = O.linear_combination(HX.nf, Tpsi, [1.0] * len(Tpsi))
+    basis = O.closure(HX, seed)
+    M = O.dense_matrix(HX, basis)
+    w, V = np.linalg.eigh(M)
+    index = {bytes(r): i for i, r in enumerate(basis.det)}
+    for k, tp in enumerate(Tpsi):
+        x = np.zeros(len(basis.val), dtype=np.complex128)
+        for r, v in zip(tp.det, tp.val):
+            x[index[bytes(r)]] += v
+        weights = np.abs(V.conj().T @ x) ** 2
+        G = O.poles_spectrum(w, weights, E0[k], emin, (emax - emin) / ne, ne, gamma)
+        ref = np.array(g["spec_dense"]["re"][k]) + 1j * np.array(g["spec_dense"]["im"][k])
+        assert rel_err(G, ref) < 1e-8, (k, rel_err(G, ref))
+
+
 def test_ground_energies_match_reference(oracle_mod):
     O = oracle_mod
     for fx in ("c0_xas.json", "c1_lf.json"):

@@ -1,0 +1,51 @@
+"""Output formats, byte for byte against files the reference wrote (tests/golden/gen/print_fmt.lua):
+spectra files (Spectra.Print, IO/StreamPrint.cpp:4) and io.put wavefunction records
+(LuaInterface/lua_extensions/get_put.cpp:588-634).  Host code only."""
+import numpy as np
+import pytest
+
+from conftest import golden
+
+
+@pytest.mark.parametrize("key", ["print_lanczos", "print_defaults", "print_dense"])
+def test_spectra_file_round_trip_is_byte_identical(key):
+    from quanty_gb300 import api
+    text = golden("print_fmt.json")[key]
+    S = api.Spectra.from_text(text)
+    assert S.Print() == text
+
+
+def test_spectra_file_layout_for_many_spectra():
+    from quanty_gb300 import api
+    G = np.arange(12 * 5, dtype=float).reshape(12, 5) * (1 - 0.5j)
+    text = api.Spectra(G, -1.0, 3.0, 4, 0.1, -0.5, 2.5).Print()
+    lines = text.splitlines()
+    assert lines[0] == "#Spectra: 12"
+    assert lines[4].startswith("Energy               Re[0]                  Im[0]                ")
+    assert "  Re[10]                 Im[10]               " in lines[4]
+    assert len(lines) == 5 + 5
+    assert all(len(ln) == 19 + 12 * 46 for ln in lines[5:])
+    S = api.Spectra.from_text(text)
+    assert np.array_equal(S.G, G) and S.Emin == -1.0 and S.Gamma == 0.1 and S.EmaxPole == 2.5
+
+
+@pytest.mark.parametrize("key", ["put_psi1", "put_psi2"])
+def test_wavefunction_put_round_trip_is_byte_identical(key):
+    from quanty_gb300 import api, quanty_text
+    text = golden("print_fmt.json")[key]
+    var = key[4:]
+    d = quanty_text.parse_wavefunction(text)
+    assert quanty_text.format_wavefunction(d, var) == text
+    psi = api.Wavefunction.from_put(text)
+    assert psi.put(var, complex_values=d["complex"], nbitskey=d["nbitskey"]) == text
+
+
+def test_complex_wavefunction_text():
+    from quanty_gb300 import api
+    psi = api.NewWavefunction(4, 0, [["1100", 0.5 - 0.25j], ["0011", -1.0]])
+    t = psi.put("psi")
+    assert t.startswith("psi = NewWavefunction( 4, 0,{\n")
+    assert '{"1100", 5.0000000000000000E-01 - I *  2.5000000000000000E-01}' in t
+    assert '{"0011",-1.0000000000000000E+00 + I *  0.0000000000000000E+00}' in t
+    back = api.Wavefunction.from_put(t)
+    assert np.array_equal(back.val, psi.val) and back.dets() == psi.dets()

@@ -14,8 +14,9 @@ class FakeJob:
         return self.need
 
 
-def server(budget):
+def server(budget, policy="fifo"):
     s = serve.Server.__new__(serve.Server)
+    s.policy = policy
     s.budget = budget
     s.in_use = 0
     s.queue = collections.deque()
@@ -47,3 +48,15 @@ def test_oversized_job_runs_alone():
 
 def test_footprint_grows_with_size():
     assert serve._footprint(10 ** 6, 4) > serve._footprint(10 ** 5, 4) > 0
+
+
+def test_shortest_job_first():
+    s = server(100, "sjf")
+    for need in (60, 30, 50, 10):
+        s.queue.append({"job": FakeJob(need)})
+    assert s._admit()["need"] == 10
+    assert s._admit()["need"] == 30
+    assert s._admit()["need"] == 50   # 90 in use
+    assert s._admit() is None          # 60 does not fit
+    s.in_use = 0
+    assert s._admit()["need"] == 60
