@@ -578,6 +578,65 @@ def _spectra_dense(H, Tpsi, e0, o, basis, eng):
     return Spectra(G, emin, emax, NE, gamma, lo, hi), poles
 
 
+def _spectra_tensor(H, Tpsi, E0, o, R, method, eng):
+    """CreateSpectra with Tensor = true (ssp.cpp:2480-2530, :2753-2800): the m x m matrix
+    G_ij(w) = <T_i psi| (w + E0 - H + i Gamma/2)^-1 |T_j psi>, spectrum i*m + j, one energy
+    shift E0 (the first state's).  Dense branch: poles of H on the union basis with weights
+    conj(c_ki) c_kj, c_ki = <E_k|T_i psi> (BasicMath_CompactMatrixVector.cpp:4064,
+    BasicMath_BlockTypeConversion.cpp:588).  Lanczos branch: the m diagonal elements and, per
+    pair, the spectra of T_i psi + T_j psi and T_i psi + i T_j psi, all m^2 chains as one
+    batched Lanczos; the off-diagonal elements follow by polarisation,
+    G_ij = (S - i T) / 2 and G_ji = (S + i T) / 2 with S = G(u_i + u_j) - G_ii - G_jj and
+    T = G(u_i + i u_j) - G_ii - G_jj.  At a converged chain length this is the reference's
+    block-Lanczos result."""
+    m = len(Tpsi)
+    NE, gamma, ntri, eps = int(o["NE"]), float(o["Gamma"]), int(o["NTri"]), float(o["Epsilon"])
+    seed = np.concatenate([t.det for t in Tpsi if t.N] or [np.zeros((0, nword(H.nf)), np.uint8)])
+    if not len(seed):
+        raise ValueError("CreateSpectra: every T psi is empty")
+    ub = closure(H, seed, H.nf, R, -1, eng)
+    n = ub.n
+    X = np.zeros((n, m), dtype=np.complex128)
+    for s, t in enumerate(Tpsi):
+        if t.N:
+            np.add.at(X[:, s], ub.find(t.det), t.val)
+    if method == "dense" or (method != "lanczos" and n <= int(o["DenseBorder"])):
+        w, V = hermitian_eigh(OperatorToDeterminantMatrix(H, ub, eng), n, eng)
+        Cm = V.conj().T @ X  # (pole, vector)
+        lo, hi = w[0] - E0, w[-1] - E0
+        emin, emax, gamma = _default_window(lo, hi, o["Emin"], o["Emax"], gamma, NE)
+        Wt = (Cm.conj()[:, :, None] * Cm[:, None, :]).reshape(n, m * m).T  # (i*m + j, pole)
+        poles = w - E0
+        G = (ListOfPolesToSpectrum(0.0, poles, Wt.real.copy(), emin, emax, NE, gamma, eng)
+             + 1j * ListOfPolesToSpectrum(0.0, poles, Wt.imag.copy(), emin, emax, NE, gamma, eng))
+        return Spectra(G, emin, emax, NE, gamma, lo, hi), {"poles": poles, "weights": Wt}
+    pairs = [(i, j) for i in range(m) for j in range(i + 1, m)]
+    Z = np.zeros((n, m + 2 * len(pairs)), dtype=np.complex128)
+    Z[:, :m] = X
+    for p, (i, j) in enumerate(pairs):
+        Z[:, m + 2 * p] = X[:, i] + X[:, j]
+        Z[:, m + 2 * p + 1] = X[:, i] + 1j * X[:, j]
+    with eng.on_stream():
+        z = eng.torch.from_numpy(Z).to("cuda:%d" % eng.device).contiguous()
+    A, B = lanczos_block(H, ub, z, ntri, eps, max(gamma, eps), eng)
+    lo, hi = np.inf, -np.inf
+    for c in range(m):
+        k = next((q for q in range(1, ntri) if B[c, q] == 0.0), ntri)
+        ev = np.linalg.eigvalsh(np.diag(A[c, 1:k + 1]) + np.diag(B[c, 1:k], 1) + np.diag(B[c, 1:k], -1))
+        lo, hi = min(lo, ev[0] - E0), max(hi, ev[-1] - E0)
+    emin, emax, gamma = _default_window(lo, hi, o["Emin"], o["Emax"], gamma, NE)
+    D = TriDiagonalMatrixToSpectrum(np.full(Z.shape[1], E0), A, B, emin, emax, NE, gamma, eng)
+    G = np.zeros((m * m, NE + 1), dtype=np.complex128)
+    for i in range(m):
+        G[i * m + i] = D[i]
+    for p, (i, j) in enumerate(pairs):
+        S_ = D[m + 2 * p] - D[i] - D[j]
+        T_ = D[m + 2 * p + 1] - D[i] - D[j]
+        G[i * m + j] = 0.5 * (S_ - 1j * T_)
+        G[j * m + i] = 0.5 * (S_ + 1j * T_)
+    return Spectra(G, emin, emax, NE, gamma, lo, hi), {"a": A, "b": B}
+
+
 def CreateSpectraResident(H, T, basis, X, E0, options=None, eng=None, batched=True, max_vectors=None):
     """The batched form of CreateSpectra for initial states held on the device: X is an
     (n, npsi) complex CUDA tensor on `basis`, E0 their energies.  The final-state basis is the
@@ -643,6 +702,8 @@ def CreateSpectra(H, T, psi, options=None, eng=None, batched=True):
     # dense branch (ssp.cpp:2262-2319): Method "Dense", or the union basis of all T psi closed
     # under H within DenseBorder determinants (unless Method is "Lanczos")
     method = str(o.get("Method") or "").lower()
+    if o.get("Tensor"):
+        return _spectra_tensor(H, Tpsi, float(E0[0]), o, R, method, eng)
     if method != "lanczos":
         seed = np.concatenate([t.det for t in Tpsi if t.N] or [np.zeros((0, nword(H.nf)), np.uint8)])
         ub = closure(H, seed, H.nf, R, -1, eng) if len(seed) else None

@@ -36,6 +36,9 @@ static inline unsigned grid_for(int64_t n, int bs) { return (unsigned)((n + bs -
 #define QG_LOCAL_UNROLL 1
 #endif
 static constexpr int kLocalUnroll = QG_LOCAL_UNROLL;  // local moves unrolled per iteration
+#ifndef QG_APPLY_MIN_BLOCKS
+#define QG_APPLY_MIN_BLOCKS 6  // resident blocks asked of the single-vector apply (caps registers)
+#endif
 
 __device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -179,7 +182,7 @@ __device__ __forceinline__ void qg_cmac(double2 &acc, double vr, double vi, bool
 }
 
 template <int W, int NV, bool FUSE, bool SMEM>
-__global__ void __launch_bounds__(256) k_apply(const Key<W> *__restrict__ rows, int64_t n_rows,
+__global__ void __launch_bounds__(256, NV == 1 ? QG_APPLY_MIN_BLOCKS : 1) k_apply(const Key<W> *__restrict__ rows, int64_t n_rows,
                                                const unsigned char *__restrict__ gtab, uint32_t tab_bytes,
                                                int ngroups, int nhop, uint64_t hop0, uint64_t hop1,
                                                const double2 *__restrict__ diag, SrcView src, int packed,
@@ -806,16 +809,35 @@ __device__ __forceinline__ Key<W> nonlocal_part(const Key<W> &d, int lo, uint32_
   return set_local<W>(d, lo, lmask, 0u);
 }
 
+// one CTA per block of rows: the sums of two mixes of the rows' non-local parts (modulo 2^64,
+// so the order of summation does not matter)
 template <int W>
-__global__ void k_block_fp(const Key<W> *keys, int64_t n, int lo, uint32_t lmask, const uint32_t *pos,
+__global__ void k_block_fp(const Key<W> *keys, const uint32_t *bstart, int lo, uint32_t lmask,
                            unsigned long long *fp) {
-  int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (r >= n) return;
-  Key<W> k = nonlocal_part<W>(keys[r], lo, lmask);
-  uint64_t a = k.w[0], b = W == 2 ? k.w[W - 1] : 0x9e3779b97f4a7c15ull;
-  uint32_t blk = pos[r] - 1;
-  atomicAdd(fp + 2 * (size_t)blk, (unsigned long long)qg_mix64(a ^ qg_mix64(b + 0x632be59bd9b4e019ull)));
-  atomicAdd(fp + 2 * (size_t)blk + 1, (unsigned long long)qg_mix64(b ^ qg_mix64(a + 0x8cb92ba72f3d8dd7ull)));
+  __shared__ unsigned long long sa[256], sb[256];
+  int blk = blockIdx.x;
+  uint32_t r0 = bstart[blk], r1 = bstart[blk + 1];
+  unsigned long long a = 0, b = 0;
+  for (uint32_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+    Key<W> k = nonlocal_part<W>(keys[r], lo, lmask);
+    uint64_t x = k.w[0], y = W == 2 ? k.w[W - 1] : 0x9e3779b97f4a7c15ull;
+    a += qg_mix64(x ^ qg_mix64(y + 0x632be59bd9b4e019ull));
+    b += qg_mix64(y ^ qg_mix64(x + 0x8cb92ba72f3d8dd7ull));
+  }
+  sa[threadIdx.x] = a;
+  sb[threadIdx.x] = b;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) {
+      sa[threadIdx.x] += sa[threadIdx.x + o];
+      sb[threadIdx.x] += sb[threadIdx.x + o];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    fp[2 * (size_t)blk] = sa[0];
+    fp[2 * (size_t)blk + 1] = sb[0];
+  }
 }
 
 template <int W>
@@ -932,13 +954,12 @@ static qg_status build_local(qg_basis bs, qg_operator op, OpBasisCache &c) {
     if (e == cudaSuccess) e = cudaMalloc(&fp, (size_t)nb * 16 + 16);
     if (e == cudaSuccess) e = cudaMalloc(&rep, (size_t)nb * 4 + 4);
     if (e == cudaSuccess) e = cudaMalloc(&mis, (size_t)nb * 4 + 4);
-    if (e == cudaSuccess) e = cudaMemsetAsync(fp, 0, (size_t)nb * 16 + 16, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(mis, 0, (size_t)nb * 4 + 4, s);
     if (e == cudaSuccess) {
       if (W == 1)
-        k_block_fp<1><<<grid_for(n, 256), 256, 0, s>>>((const Key<1> *)bs->d_keys, n, lo, lmask, pos, fp);
+        k_block_fp<1><<<nb, 256, 0, s>>>((const Key<1> *)bs->d_keys, bst, lo, lmask, fp);
       else
-        k_block_fp<2><<<grid_for(n, 256), 256, 0, s>>>((const Key<2> *)bs->d_keys, n, lo, lmask, pos, fp);
+        k_block_fp<2><<<nb, 256, 0, s>>>((const Key<2> *)bs->d_keys, bst, lo, lmask, fp);
       ctx->launches++;
     }
     std::vector<unsigned long long> hfp((size_t)2 * nb);

@@ -269,9 +269,20 @@ def gen_print():
     save("print_fmt.json", out)
 
 
+def gen_tensor():
+    """Tensor spectra (3 x 3 dipole matrix) of the reference, dense and block-Lanczos branches."""
+    work = run(open(os.path.join(HERE, "gen", "tensor.lua")).read(), "tensor.lua")
+    out = {"source": "tests/golden/gen/tensor.lua", "psi": wf(work, "psi1")}
+    for n in ("HX", "Tx", "Ty", "Tz"):
+        out[n] = op(work, n)
+    for k in ("dense", "dense_defaults", "lanczos"):
+        out["tensor_" + k] = open(os.path.join(work, "dump", "tensor_%s.dat" % k)).read()
+    save("tensor.json", out)
+
+
 if __name__ == "__main__":
     if not os.path.exists(QUANTY):
         sys.exit("build the reference first: oracle/build_ref.sh")
-    which = sys.argv[1:] or ["hpsi", "c0", "c1", "chain", "fshell", "print"]
+    which = sys.argv[1:] or ["hpsi", "c0", "c1", "chain", "fshell", "print", "tensor"]
     for w in which:
         globals()["gen_" + w]()

@@ -209,3 +209,36 @@ def test_rixs_matches_reference(oracle_mod, key, eps):
     ref = g[key]
     R = np.array(ref["re"]) + 1j * np.array(ref["im"])
     assert rel_err(G, R) < 1e-8
+
+
+@pytest.mark.parametrize("key", ["tensor_dense", "tensor_dense_defaults"])
+def test_dense_tensor_spectra_match_reference(oracle_mod, key):
+    """Tensor spectra, dense branch restated: G_ij(w) = sum_k conj(c_ki) c_kj / (w - (E_k - E0)
+    + i Gamma/2), c_ki = <E_k|T_i psi>, spectrum i*3 + j (LuaInterface/ssp.cpp:2480-2530,
+    Core/BasicMath/BasicMath_CompactMatrixVector.cpp:4064, BasicMath_BlockTypeConversion.cpp:588)."""
+    from quanty_gb300 import api  # Spectra.from_text only (host code)
+    O = oracle_mod
+    g = golden("tensor.json")
+    HX = O.Op(g["HX"])
+    psi = O.WF.from_fixture(g["psi"])
+    E0 = _expectation(O, HX, psi)
+    Tpsi = [O.operator_psi(O.Op(g[T]), psi) for T in ("Tx", "Ty", "Tz")]
+    seed = O.linear_combination(HX.nf, Tpsi, [1.0] * 3)
+    basis = O.closure(HX, seed)
+    w, V = np.linalg.eigh(O.dense_matrix(HX, basis))
+    index = {bytes(r): i for i, r in enumerate(basis.det)}
+    X = np.zeros((len(basis.val), 3), dtype=np.complex128)
+    for s, tp in enumerate(Tpsi):
+        for r, v in zip(tp.det, tp.val):
+            X[index[bytes(r)], s] += v
+    C = V.conj().T @ X
+    ref = api.Spectra.from_text(g[key])
+    assert abs(ref.EminPole - (w[0] - E0)) < 1e-8 and abs(ref.EmaxPole - (w[-1] - E0)) < 1e-8
+    de = (ref.Emax - ref.Emin) / ref.NE
+    for i in range(3):
+        for j in range(3):
+            wt = np.conj(C[:, i]) * C[:, j]
+            G = (O.poles_spectrum(w - E0, wt.real, 0.0, ref.Emin, de, ref.NE, ref.Gamma)
+                 + 1j * O.poles_spectrum(w - E0, wt.imag, 0.0, ref.Emin, de, ref.NE, ref.Gamma))
+            R = ref.G[i * 3 + j]
+            assert np.max(np.abs(G - R)) < 1e-8 * np.max(np.abs(ref.G)), (i, j)
