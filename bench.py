@@ -137,22 +137,20 @@ def build_workload(api, args):
 
 def timed_sample(O, op, wf_handle, n, seconds):
     """Time the oracle's push-form H*psi over a spread sample of source rows (every stride-th
-    row of the basis, the full basis as lookup target), sized for about `seconds`."""
+    row of the basis, the full basis as lookup target), grown until one pass takes at least
+    half of `seconds` (or covers the basis)."""
     L = O.lib()
     y = np.zeros(2 * n)
-    S = min(n, 2000)
-    stride = max(1, n // S)
-    t0 = time.perf_counter()
-    L.qo_apply_conserve_strided(*op.args(), wf_handle, 0, n, stride, O._p(y))
-    dt = time.perf_counter() - t0
-    rows = (n + stride - 1) // stride
-    S2 = int(min(n, max(rows, rows * seconds / max(dt, 1e-6))))
-    stride = max(1, n // S2)
-    rows = (n + stride - 1) // stride
-    t0 = time.perf_counter()
-    L.qo_apply_conserve_strided(*op.args(), wf_handle, 0, n, stride, O._p(y))
-    dt = time.perf_counter() - t0
-    return rows, stride, dt
+    target = min(n, 2000)
+    while True:
+        stride = max(1, n // target)
+        rows = (n + stride - 1) // stride
+        t0 = time.perf_counter()
+        L.qo_apply_conserve_strided(*op.args(), wf_handle, 0, n, stride, O._p(y))
+        dt = time.perf_counter() - t0
+        if dt >= 0.5 * seconds or rows >= n:
+            return rows, stride, dt
+        target = int(min(n, max(2 * rows, rows * seconds / max(dt, 1e-6))))
 
 
 def cpu_baseline(api, H, basis, seconds):
@@ -269,21 +267,6 @@ def main():
     nterms = H.info()["nterms"]
     nnz = api.count_nnz(H, basis)
     nnz_off = api.count_nnz(H, basis, offdiag=True)
-    # connections through the hash table: one-body moves that change a bath orbital (the rest
-    # of the off-diagonal connections are local moves at a predicted offset, coalesced)
-    hop_terms = [(o, v) for o, v in H.terms
-                 if len(o) == 2 and (o[0] & 0x7FFF) != (o[1] & 0x7FFF) and max(o[0] & 0x7FFF, o[1] & 0x7FFF) >= 16]
-    nnz_hop = api.count_nnz(api.Operator(H.nf, hop_terms), basis) if hop_terms else 0
-    # CPU baseline in a background thread (ctypes releases the GIL) while the GPU is timed
-    cpu = {}
-    cpu_thread = None
-    if rank == 0 and not args.no_cpu_baseline:
-        def go():
-            try:
-                cpu.update(cpu_baseline(api, H, basis, args.cpu_seconds))
-            except Exception as e:  # reported, never fatal to the GPU number
-                cpu.update({"value": None, "error": str(e)})
-        cpu_thread = threading.Thread(target=go, daemon=True)
     rng = np.random.default_rng(1)
     x = torch.from_numpy(rng.normal(size=(n, 1)) + 1j * rng.normal(size=(n, 1))).cuda()
     y = eng.empty(n)
@@ -295,8 +278,10 @@ def main():
     for _ in range(max(args.warmup, 3)):
         step()
     torch.cuda.synchronize()
-    if cpu_thread is not None:
-        cpu_thread.start()
+    # connections the apply gathers through its per-row lists (the rest are local moves at a
+    # certain offset in another block of the sorted basis)
+    built, nconn = C.c_int32(0), C.c_int64(0)
+    eng.check(eng.L.qg_apply_list_info(eng.ctx, H.handle(), basis.h, C.byref(built), C.byref(nconn)))
     clocks = Clocks(local)
     clocks.start()
     if dist:
@@ -330,10 +315,15 @@ def main():
     if dist:
         dist.all_reduce(t_ms, op=dist.ReduceOp.MAX)
     ms, e2e_ms = float(t_ms[0]), float(t_ms[1])
-    if cpu_thread is not None:
-        cpu_thread.join()
     if rank != 0:
         return 0
+    # CPU baseline after the GPU timing (its threads would compete with the host-buffer copies)
+    cpu = {}
+    if not args.no_cpu_baseline:
+        try:
+            cpu = cpu_baseline(api, H, basis, args.cpu_seconds)
+        except Exception as e:  # reported, never fatal to the GPU number
+            cpu = {"value": None, "error": str(e)}
     secondary = None
     if not args.no_secondary:
         try:
@@ -343,31 +333,38 @@ def main():
     units = n * nterms * world
     value = units / (ms * 1e-3) / 1e9
     e2e_val = units / (e2e_ms * 1e-3) / 1e9
-    # algorithmic bytes of one H*psi (the survey's per-unit figure): one key, one source
+    # algorithmic bytes of one H*psi, the survey's per-unit figure: one key, one source
     # amplitude and one result per row, one 16-byte amplitude gather per non-zero connection
-    # (no cache reuse credited), the term table once.  Also reported: the same counting only
-    # the connections that change the determinant (diagonal ones reuse the row's own amplitude).
+    # (no cache reuse credited), the term table once.  The diagonal connection of a row reads
+    # the row's own amplitude, already counted once per row, so nnz counts the connections that
+    # change the determinant; the literal count with the diagonal pairs is reported beside it.
     W = 16
     term_bytes = nterms * 64
-    alg_bytes = n * (W + 16 + 16) + nnz * 16 + term_bytes
-    alg_bytes_off = n * (W + 16 + 16) + nnz_off * 16 + term_bytes
+    alg_bytes = n * (W + 16 + 16) + nnz_off * 16 + term_bytes
+    alg_bytes_lit = n * (W + 16 + 16) + nnz * 16 + term_bytes
     peak, peak_kind = measured_peak()
     achieved = alg_bytes / (ms * 1e-3) / 1e9
-    # two-ceiling model of the same launch: coalesced bytes at the copy bandwidth, hash-probed
-    # (random 32-byte sector) reads and the pack step's scattered writes at the random-sector
-    # gather bandwidth measured here
-    gbs = C.c_double(0.0)
-    eng.check(eng.L.qg_gather_bandwidth(eng.ctx, 4 << 30, C.byref(gbs)))
-    coalesced = n * (16 + 4 + 16 + 16 + 16) + (nnz_off - nnz_hop) * 16 + term_bytes
-    random_sectors = n + nnz_hop
-    t_bound = coalesced / (peak * 1e9) + random_sectors * 32 / (gbs.value * 1e9)
-    achieved_off = alg_bytes_off / (ms * 1e-3) / 1e9
+    achieved_lit = alg_bytes_lit / (ms * 1e-3) / 1e9
+    # FP64 ceiling: the exact FP64 operations of the launch (2 per real connection, 4 per
+    # complex one, 2-4 for the diagonal) against 2 FP64 lanes per SM per clock at the clock
+    # sampled under load
+    ops = C.c_int64(0)
+    eng.check(eng.L.qg_apply_fp64_ops(eng.ctx, H.handle(), basis.h, C.byref(ops)))
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    mhz = clk.get("sm_mhz") or clk.get("sm_max_mhz") or 2070.0
+    fp64_nominal = 2.0 * sms * mhz * 1e6 / 1e9  # G FP64 lane-operations per second
+    meas = C.c_double(0.0)
+    eng.check(eng.L.qg_fp64_peak(eng.ctx, C.byref(meas)))
+    fp64_peak = meas.value
+    fp64_achieved = ops.value / (ms * 1e-3) / 1e9
+    hbm_floor_ms = alg_bytes / (peak * 1e9) * 1e3
+    fp64_floor_ms = ops.value / (fp64_peak * 1e9) * 1e3
     line = {
         "metric": "H·ψ det·terms/s", "value": value, "unit": "Gdet·terms/s", "n_gpus": world, "steps": args.steps,
         "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "c128", "data": "synthetic",
         "config": {"workload": "anderson_impurity_86so_hpsi", "n_det": n, "n_terms": nterms, "nnz": nnz,
-                   "nnz_offdiag": nnz_off, "nnz_hash_probed": nnz_hop,
+                   "nnz_offdiag": nnz_off, "connection_lists": bool(built.value), "nnz_listed": nconn.value,
                    "det_words_bits": 128, "l2": "inputs larger than L2 (x, y %d MB each)" % (n * 16 // 2**20),
                    "setup_s": round(t_setup, 2), "parallelism": "replicas" if world > 1 else "single"},
         "e2e": {"value": e2e_val, "unit": "Gdet·terms/s", "h2d_bytes_per_step": n * 16, "d2h_bytes_per_step": n * 16,
@@ -375,10 +372,15 @@ def main():
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": profiled_traffic(), "peak_source": peak_kind,
                      "algorithmic_bytes_per_launch": alg_bytes,
-                     "achieved_offdiagonal_only": achieved_off, "frac_offdiagonal_only": achieved_off / peak,
-                     "two_ceiling": {"coalesced_bytes": coalesced, "random_sectors": random_sectors,
-                                     "gather_peak_gbs": gbs.value, "bound_ms": t_bound * 1e3,
-                                     "frac": t_bound * 1e3 / ms}},
+                     "achieved_survey_literal": achieved_lit, "frac_survey_literal": achieved_lit / peak,
+                     "fp64": {"ops_per_launch": ops.value, "achieved_gops": fp64_achieved,
+                              "peak_gops": fp64_peak, "frac": fp64_achieved / fp64_peak,
+                              "peak_source": "measured (independent FMA chains on every lane, qg_fp64_peak)",
+                              "nominal_gops": fp64_nominal, "frac_of_nominal": fp64_achieved / fp64_nominal,
+                              "nominal_source": "2 FP64 lanes per SM per clock x %d SMs x %.0f MHz sampled" % (sms, mhz)},
+                     "floors_ms": {"hbm": hbm_floor_ms, "fp64": fp64_floor_ms,
+                                   "frac_of_larger": max(hbm_floor_ms, fp64_floor_ms) / ms},
+                     "limiter": "fp64" if fp64_floor_ms > hbm_floor_ms else "hbm"},
         "cpu_baseline": cpu or None,
         "clocks": clk,
         "gpu_launches": launches,

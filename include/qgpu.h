@@ -154,6 +154,11 @@ qg_status qg_poles_spectra(qg_context ctx, int32_t nspec, int32_t npole, const d
  * allocated and freed here).  The ceiling for hash-probed gathers, measured for the roofline. */
 qg_status qg_gather_bandwidth(qg_context ctx, int64_t bytes, double *gbs);
 
+/* FP64 issue ceiling of the device in G lane-operations per second (no counterpart in the
+ * reference): independent FMA chains in registers on every lane of num_sms * 8 blocks, timed
+ * with events.  The measured denominator of the H*psi FP64 roofline. */
+qg_status qg_fp64_peak(qg_context ctx, double *gops);
+
 /* Eigenpairs of a small dense Hermitian matrix on the host: a is k x k row-major with
  * interleaved (re, im); w receives all k eigenvalues ascending, v (k x nv row-major,
  * interleaved) the eigenvectors of the lowest nv as columns.  Householder reduction, implicit
@@ -174,9 +179,30 @@ qg_status qg_set_autotune(qg_context ctx, int32_t on);
 qg_status qg_apply_chunk(qg_context ctx, qg_operator op, qg_basis basis, int32_t nvec, int32_t *chunk);
 qg_status qg_apply_set_chunk(qg_context ctx, qg_operator op, qg_basis basis, int32_t nvec, int32_t chunk);
 
+/* Connection lists of the same-basis apply (no counterpart in the reference, which looks every
+ * connection up in its hash on every H*psi, ComplexWaveFunctionAddElementConserveBasis,
+ * Core/ComplexWaveFunctionArithmetic.cpp:355): on the first apply of an operator on a basis
+ * (outside stream capture) the sources that need a hash lookup are resolved once into
+ * per-row lists of source rows (8 bytes per connection, 8 per row), and later applies gather
+ * by row.  The lists keep each row's summation order, so the result is bitwise the same as
+ * the hash path.  They are not built when they would take more than a quarter of the free
+ * device memory or the basis has 2^32 - 1 rows or more.  on = 0 turns them off for lists not
+ * yet built; qg_apply_list_info reports whether (op, basis) has them (built = 1) and their
+ * connection count. */
+qg_status qg_set_connection_lists(qg_context ctx, int32_t on);
+qg_status qg_apply_list_info(qg_context ctx, qg_operator op, qg_basis basis, int32_t *built, int64_t *nconn);
+
+/* FP64 operations of one single-vector same-basis apply of op on basis (no counterpart in the
+ * reference): per row 2 multiplies for a real diagonal (4 complex), per connection 2 FMAs for
+ * a real value (4 complex), counted over the connection lists (built here if needed;
+ * QG_ERR_ARG when they cannot be).  The exact work behind the apply's FP64 ceiling. */
+qg_status qg_apply_fp64_ops(qg_context ctx, qg_operator op, qg_basis basis, int64_t *ops);
+
 /* qg_apply with host buffers: copies x_host to the device, applies, copies y back (the
  * reference's calling convention, where psi and Opsi live in host memory).  Device staging
- * buffers are kept in the context between calls; pinned host buffers give full copy speed. */
+ * buffers are kept in the context between calls.  Page-locked (pinned) buffers are used in
+ * place: the SMs pull x over the host link, and the apply writes y straight into y_host, so
+ * the copy back overlaps the computation; pageable buffers are staged with copies. */
 qg_status qg_apply_host(qg_context ctx, qg_operator op, qg_basis basis_dst, qg_basis basis_src,
                         const double *x_host, double *y_host, int32_t nvec);
 

@@ -23,6 +23,7 @@
 #include <cub/cub.cuh>
 
 #include <algorithm>
+#include <cstring>
 #include <map>
 #include <tuple>
 
@@ -619,6 +620,286 @@ __global__ void __launch_bounds__(256) k_apply_warp(const Key<W> *__restrict__ r
   if (SMEM && pending) mbar_wait_bounded(smem_addr(&s_bar), 0);
 }
 
+// ------------------------------------------------------------------ connection lists
+//
+// k_apply resolves a connection that has no certain offset through the hash table on every
+// H*psi: it hashes the source key, probes (one random 32-byte sector of a table twice the
+// basis), and for several vectors reads the slot's row.  The sources do not change between
+// the H*psi calls of a Lanczos run, so k_conn resolves them once per (operator, basis), in
+// the order k_apply visits them, into per-row lists of (source row, meta); k_apply_list then
+// gathers x[source] by row.  Rows of a warp are neighbours in the sorted basis and a term
+// maps sorted sources monotonically to sorted targets, so their sources are neighbours too:
+// the gathers share sectors and stay in L2, where hashed probes scatter over the table.
+// Both kernels follow k_apply's visiting order exactly, so each row's sum is bitwise the same.
+
+// One pass over a row's connections: FILL = false counts them into cnt[r], FILL = true
+// writes them at cptr[r] (bounded by cptr[r + 1]).
+template <int W, bool FILL>
+__global__ void __launch_bounds__(256) k_conn(const Key<W> *__restrict__ rows, int64_t n_rows,
+                                              const GroupDev<W> *__restrict__ groups, const TermDev<W> *__restrict__ terms,
+                                              int ngroups, int nhop, uint64_t hop0, uint64_t hop1, SrcView src,
+                                              LocalView lv, const uint64_t *__restrict__ wreq, int64_t *cptr,
+                                              uint2 *conn, unsigned int *err) {
+  int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= n_rows) return;
+  const Key<W> d = rows[r];
+  const int64_t p0 = FILL ? cptr[r] : 0, pend = FILL ? cptr[r + 1] : 0;
+  int64_t c = 0;
+  auto emit = [&](uint32_t j, uint32_t meta) {
+    if (FILL) {
+      if (p0 + c < pend)
+        conn[p0 + c] = make_uint2(j, meta);
+      else
+        atomicOr(err, QG_DEVERR_OVERFLOW);
+    }
+    c++;
+  };
+  uint64_t okm = 0;
+  if (wreq && src.nres) okm = window_bits<W>(d, src);
+  if (lv.on) {
+    int b = __ldg(lv.cfg + get_local<W>(d, lv.lo, lv.lmask));
+    int64_t off = r - (int64_t)__ldg(lv.bstart + b);
+    uint32_t e1 = __ldg(lv.eoff + b + 1);
+    for (uint32_t e = __ldg(lv.eoff + b); e < e1; e++) {
+      const LocalEntry *E = lv.ent + e;
+      uint32_t te = __ldg(&E->tend);
+      if (te >> 31) continue;  // certain offset: no list entry
+      int64_t j = (int64_t)__ldg(&E->tstart) + off;
+      Key<W> s = set_local<W>(d, lv.lo, lv.lmask, __ldg(lv.etarget + e));
+      bool hit = false;
+      if (j < (int64_t)(te & 0x7FFFFFFFu)) hit = qg_eq<W>(rows[j], s);
+      if (!hit) {
+        if (src.nres) {
+          uint64_t req = __ldg(&E->wreq);
+          if (wreq ? ((okm & req) != req) : !in_windows<W>(s, src)) {
+            emit(QG_NO_INDEX, 0);
+            continue;
+          }
+        }
+        int64_t h = qg_find_slot<W>(src.slots, src.hmask, s, err);
+        if (h < 0) {
+          emit(QG_NO_INDEX, 0);
+          continue;
+        }
+        j = (int64_t)__ldg(src.slot_row + h);
+      }
+      emit((uint32_t)j, 0);
+    }
+  }
+  auto term = [&](int t, bool known_applicable) {
+    const TermDev<W> &T = terms[t];
+    if (!known_applicable) {
+      bool app = true;
+#pragma unroll
+      for (int i = 0; i < W; i++) app &= (d.w[i] & T.need0[i]) == 0;
+      if (!app) return;
+    }
+    Key<W> s;
+    bool dg = true;
+#pragma unroll
+    for (int i = 0; i < W; i++) {
+      uint64_t fl = T.flip[i];
+      s.w[i] = d.w[i] ^ fl;
+      dg &= fl == 0;
+    }
+    int64_t j = r;
+    if (!dg) {
+      if (src.nres) {
+        if (wreq) {
+          uint64_t req = __ldg(wreq + t);
+          if ((okm & req) != req) return;
+        } else if (!in_windows<W>(s, src)) {
+          return;
+        }
+      }
+      int64_t h = qg_find_slot<W>(src.slots, src.hmask, s, err);
+      if (h < 0) return;
+      j = (int64_t)__ldg(src.slot_row + h);
+    }
+    int par = 0;
+#pragma unroll
+    for (int i = 0; i < W; i++) par += __popcll(d.w[i] & T.sgn[i]);
+    emit((uint32_t)j, (uint32_t)t | ((uint32_t)(par & 1) << 31));
+  };
+  int gbase = 0;
+#pragma unroll
+  for (int i = 0; i < W; i++) {
+    uint64_t hm = i == 0 ? hop0 : hop1;
+    uint64_t m = d.w[i] & hm;
+    while (m) {
+      int bp = __ffsll((long long)m) - 1;
+      m &= m - 1;
+      const GroupDev<W> &G = groups[gbase + __popcll(hm & ((1ull << bp) - 1))];
+      int tq = G.begin;
+#pragma unroll
+      for (int i2 = 0; i2 < W; i2++) {
+        uint64_t qm = G.qmask[i2];
+        uint64_t cm = qm & ~d.w[i2];
+        while (cm) {
+          int bq = __ffsll((long long)cm) - 1;
+          cm &= cm - 1;
+          term(tq + __popcll(qm & ((1ull << bq) - 1)), true);
+        }
+        tq += __popcll(qm);
+      }
+    }
+    gbase += __popcll(hm);
+  }
+  for (int g = nhop; g < ngroups; g++) {
+    bool ok = true;
+#pragma unroll
+    for (int i = 0; i < W; i++) {
+      uint64_t n1 = groups[g].need1[i];
+      ok &= (d.w[i] & n1) == n1;
+    }
+    if (!ok) continue;
+    int tb = groups[g].begin, te = groups[g].end;
+    for (int t = tb; t < te; t++) term(t, false);
+  }
+  if (!FILL) cptr[r] = c;
+}
+
+// The apply over connection lists: diagonal, local moves (certain offsets inline, the others
+// from the list), then the listed table connections; the arithmetic of each connection is
+// k_apply's (qg_cmac with the parity-flipped value), in the same order.
+template <int W, int NV, bool FUSE>
+__global__ void __launch_bounds__(256, NV == 1 ? QG_APPLY_MIN_BLOCKS : 1)
+    k_apply_list(const Key<W> *__restrict__ rows, int64_t n_rows, const int64_t *__restrict__ cptr,
+                 const uint2 *__restrict__ conn, const double2 *__restrict__ coef, const double2 *__restrict__ diag,
+                 const double2 *__restrict__ x, int xs, double2 *__restrict__ y, int ys, int vec0, ApplyFuse fz,
+                 LocalView lv) {
+  int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  bool live = r < n_rows;
+  double2 acc[NV];
+#pragma unroll
+  for (int k = 0; k < NV; k++) acc[k] = make_double2(0.0, 0.0);
+  if (live) {
+    if (diag) {
+      double2 dg = diag[r];
+      if (qg_is_nonzero(dg.y)) {
+#pragma unroll
+        for (int k = 0; k < NV; k++) {
+          double2 xv = x[r * xs + vec0 + k];
+          acc[k].x = dg.x * xv.x - dg.y * xv.y;
+          acc[k].y = dg.x * xv.y + dg.y * xv.x;
+        }
+      } else {
+#pragma unroll
+        for (int k = 0; k < NV; k++) {
+          double2 xv = x[r * xs + vec0 + k];
+          acc[k].x = dg.x * xv.x;
+          acc[k].y = dg.x * xv.y;
+        }
+      }
+    }
+    int64_t p = __ldg(cptr + r);
+    const int64_t pe = __ldg(cptr + r + 1);
+    if (lv.on) {
+      const Key<W> d = rows[r];
+      int b = __ldg(lv.cfg + get_local<W>(d, lv.lo, lv.lmask));
+      int64_t off = r - (int64_t)__ldg(lv.bstart + b);
+      uint32_t e1 = __ldg(lv.eoff + b + 1);
+#pragma unroll(kLocalUnroll)
+      for (uint32_t e = __ldg(lv.eoff + b); e < e1; e++) {
+        const LocalEntry *E = lv.ent + e;
+        int64_t j;
+        if (__ldg(&E->tend) >> 31) {
+          j = (int64_t)__ldg(&E->tstart) + off;
+        } else {
+          uint32_t js = p < pe ? __ldg(&conn[p].x) : QG_NO_INDEX;
+          p++;
+          if (js == QG_NO_INDEX) continue;
+          j = js;
+        }
+        double vr = __ldg(&E->vre), vi = __ldg(&E->vim);
+        bool cplx = qg_is_nonzero(vi);
+#pragma unroll
+        for (int k = 0; k < NV; k++) qg_cmac(acc[k], vr, vi, cplx, __ldg(x + j * xs + vec0 + k));
+      }
+    }
+    for (; p < pe; p++) {
+      uint2 cn = __ldg(conn + p);
+      double2 cf = __ldg(coef + (cn.y & 0x7FFFFFFFu));
+      int par = (int)(cn.y >> 31);
+      bool cplx = qg_is_nonzero(cf.y);
+      double vr = qg_flip_sign(cf.x, par), vi = qg_flip_sign(cf.y, par);
+      int64_t j = cn.x;
+#pragma unroll
+      for (int k = 0; k < NV; k++) qg_cmac(acc[k], vr, vi, cplx, __ldg(x + j * xs + vec0 + k));
+    }
+  }
+  if (!FUSE) {
+    if (live) {
+#pragma unroll
+      for (int k = 0; k < NV; k++) y[r * ys + vec0 + k] = acc[k];
+    }
+  } else {
+    __shared__ double2 red[NV][8];
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; k++) {
+      double2 dv = make_double2(0.0, 0.0);
+      if (live) {
+        double2 xv = x[r * xs + vec0 + k];
+        dv.x = xv.x * acc[k].x + xv.y * acc[k].y;
+        dv.y = xv.x * acc[k].y - xv.y * acc[k].x;
+        double2 pv = fz.prev[r * ys + vec0 + k];
+        double be = fz.beta[vec0 + k];
+        y[r * ys + vec0 + k] = make_double2(acc[k].x - be * pv.x, acc[k].y - be * pv.y);
+      }
+#pragma unroll
+      for (int o = 16; o; o >>= 1) {
+        dv.x += __shfl_xor_sync(0xffffffffu, dv.x, o);
+        dv.y += __shfl_xor_sync(0xffffffffu, dv.y, o);
+      }
+      if (lane == 0) red[k][wid] = dv;
+    }
+    __syncthreads();
+    if (threadIdx.x < NV) {
+      int k = threadIdx.x;
+      double2 s = make_double2(0.0, 0.0);
+      for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
+        s.x += red[k][w].x;
+        s.y += red[k][w].y;
+      }
+      fz.dot_part[blockIdx.x * ys + vec0 + k] = s;
+    }
+  }
+}
+
+// FP64 operations of one single-vector k_apply_list launch, counted per row as the kernel
+// issues them: the diagonal 2 multiplies (real) or 4 (complex), each connection 2 FMAs (real
+// value) or 4 (complex).  The exact work behind the FP64 ceiling of the roofline.
+template <int W>
+__global__ void k_count_fp64(const Key<W> *__restrict__ rows, int64_t n_rows, const int64_t *__restrict__ cptr,
+                             const uint2 *__restrict__ conn, const double2 *__restrict__ coef,
+                             const double2 *__restrict__ diag, LocalView lv, unsigned long long *out) {
+  int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  unsigned long long c = 0;
+  if (r < n_rows) {
+    if (diag) c += qg_is_nonzero(diag[r].y) ? 4 : 2;
+    int64_t p = cptr[r];
+    const int64_t pe = cptr[r + 1];
+    if (lv.on) {
+      const Key<W> d = rows[r];
+      int b = lv.cfg[get_local<W>(d, lv.lo, lv.lmask)];
+      uint32_t e1 = lv.eoff[b + 1];
+      for (uint32_t e = lv.eoff[b]; e < e1; e++) {
+        const LocalEntry *E = lv.ent + e;
+        if (!(E->tend >> 31)) {
+          uint32_t js = p < pe ? conn[p].x : QG_NO_INDEX;
+          p++;
+          if (js == QG_NO_INDEX) continue;
+        }
+        c += qg_is_nonzero(E->vim) ? 4 : 2;
+      }
+    }
+    for (; p < pe; p++) c += qg_is_nonzero(coef[conn[p].y & 0x7FFFFFFFu].y) ? 4 : 2;
+  }
+  for (int o = 16; o; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+  if ((threadIdx.x & 31) == 0 && c) atomicAdd(out, c);
+}
+
 int qg_apply_grid(qg_basis dst) { return (int)std::max<int64_t>(1, (dst->n + 255) / 256); }
 
 template <int W, int NV, bool FUSE, bool SMEM>
@@ -860,6 +1141,9 @@ void qg_cache_free(OpBasisCache &c) {
   cudaFree(c.d_eoff);
   cudaFree(c.d_ent);
   cudaFree(c.d_ent_target);
+  cudaFree(c.d_cptr);
+  cudaFree(c.d_conn);
+  cudaFree(c.d_coef);
   c = OpBasisCache();
 }
 
@@ -1132,6 +1416,200 @@ OpBasisCache *qg_basis_cache(qg_basis b, qg_operator op, qg_status *st) {
   return &b->caches.back();
 }
 
+// ------------------------------------------------------------------ connection lists (host)
+
+// The table and local view the same-basis apply scans (also used by the list build).
+static void same_basis_view(qg_operator op, qg_basis b, const OpBasisCache *c, const HostTable **tab, LocalView *lv,
+                            const uint64_t **wreq) {
+  *lv = LocalView{};
+  lv->on = 0;
+  *tab = &op->pull_off;
+  *wreq = nullptr;
+  if (op->H > 0) {
+    *tab = &op->pull_nl;
+    lv->on = 1;
+    lv->lo = b->nf - op->H;
+    lv->lmask = (1u << op->H) - 1;
+    lv->cfg = c->d_cfg;
+    lv->bstart = c->d_bstart;
+    lv->eoff = c->d_eoff;
+    lv->ent = c->d_ent;
+    lv->etarget = c->d_ent_target;
+    if (c->wreq_exact && c->d_wreq) *wreq = c->d_wreq;
+  }
+}
+
+template <int W>
+__global__ void k_term_coef(const TermDev<W> *__restrict__ terms, int nterms, double2 *coef) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < nterms) coef[t] = make_double2(terms[t].vre, terms[t].vim);
+}
+
+template <int W>
+static void launch_conn(qg_context ctx, qg_basis b, const HostTable &tab, const LocalView &lv, const uint64_t *wreq,
+                        int64_t *cptr, uint2 *conn, bool fill) {
+  SrcView sv{b->d_slots, b->d_slot_row, (uint64_t)(b->hcap - 1), b->nres, b->d_rmask, b->d_rmin, b->d_rmax};
+  const GroupDev<W> *g = (const GroupDev<W> *)tab.d_groups;
+  const TermDev<W> *t = (const TermDev<W> *)tab.d_terms;
+  if (fill)
+    k_conn<W, true><<<grid_for(b->n, 256), 256, 0, ctx->stream>>>((const Key<W> *)b->d_keys, b->n, g, t, tab.ngroups,
+                                                                  tab.nhop, tab.hopmask[0], tab.hopmask[1], sv, lv,
+                                                                  wreq, cptr, conn, ctx->d_err);
+  else
+    k_conn<W, false><<<grid_for(b->n, 256), 256, 0, ctx->stream>>>((const Key<W> *)b->d_keys, b->n, g, t,
+                                                                   tab.ngroups, tab.nhop, tab.hopmask[0],
+                                                                   tab.hopmask[1], sv, lv, wreq, cptr, conn,
+                                                                   ctx->d_err);
+  ctx->launches++;
+}
+
+// Build the connection lists of (op, b) into c.  Leaves conn_state = -1 (and the apply on the
+// hash path) when the basis is too large for 32-bit rows, when the lists would take more than
+// a quarter of the free device memory, or while the stream is being captured (then it is
+// tried again on a later apply).
+static qg_status build_conn(qg_context ctx, qg_operator op, qg_basis b, OpBasisCache &c) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(ctx->stream, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) {
+    cudaGetLastError();
+    return QG_OK;
+  }
+  c.conn_state = -1;
+  const int64_t n = b->n;
+  if (n <= 0 || n >= (int64_t)QG_NO_INDEX) return QG_OK;
+  const HostTable *tab;
+  LocalView lv;
+  const uint64_t *wreq;
+  same_basis_view(op, b, &c, &tab, &lv, &wreq);
+  cudaStream_t s = ctx->stream;
+  size_t fr = 0, tot = 0;
+  if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) {
+    cudaGetLastError();
+    return QG_OK;
+  }
+  const size_t ptr_bytes = (size_t)(n + 1) * 8;
+  if (4 * 2 * ptr_bytes > fr) return QG_OK;
+  int64_t *cnt = nullptr, *cptr = nullptr;
+  void *tmp = nullptr;
+  size_t tb = 0;
+  cudaError_t e = cudaMalloc(&cnt, ptr_bytes);
+  if (e == cudaSuccess) e = cudaMalloc(&cptr, ptr_bytes);
+  if (e == cudaSuccess) e = cub::DeviceScan::ExclusiveSum(nullptr, tb, cnt, cptr, n + 1, s);
+  if (e == cudaSuccess) e = cudaMalloc(&tmp, std::max<size_t>(tb, 16));
+  if (e == cudaSuccess) e = cudaMemsetAsync(cnt + n, 0, 8, s);
+  if (e == cudaSuccess) {
+    if (b->W == 1)
+      launch_conn<1>(ctx, b, *tab, lv, wreq, cnt, nullptr, false);
+    else
+      launch_conn<2>(ctx, b, *tab, lv, wreq, cnt, nullptr, false);
+    e = cub::DeviceScan::ExclusiveSum(tmp, tb, cnt, cptr, n + 1, s);
+    ctx->launches += 2;
+  }
+  int64_t total = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&total, cptr + n, 8, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  cudaFree(cnt);
+  cudaFree(tmp);
+  if (e != cudaSuccess) {
+    cudaFree(cptr);
+    return qg_cuda_fail(ctx, e, "connection counts");
+  }
+  QG_TRY(qg_check_device_error(ctx, "connection counts"));
+  size_t conn_bytes = (size_t)std::max<int64_t>(total, 1) * sizeof(uint2);
+  if (cudaMemGetInfo(&fr, &tot) != cudaSuccess || 4 * conn_bytes > fr) {
+    cudaGetLastError();
+    cudaFree(cptr);
+    return QG_OK;
+  }
+  uint2 *conn = nullptr;
+  double2 *coef = nullptr;
+  e = cudaMalloc(&conn, conn_bytes);
+  if (e == cudaSuccess) e = cudaMalloc(&coef, (size_t)std::max(tab->nterms, 1) * 16);
+  if (e != cudaSuccess) {
+    cudaFree(cptr);
+    cudaFree(conn);
+    cudaFree(coef);
+    cudaGetLastError();
+    return QG_OK;  // no room: the hash path stays
+  }
+  if (tab->nterms > 0) {
+    if (b->W == 1)
+      k_term_coef<1><<<(tab->nterms + 255) / 256, 256, 0, s>>>((const TermDev<1> *)tab->d_terms, tab->nterms, coef);
+    else
+      k_term_coef<2><<<(tab->nterms + 255) / 256, 256, 0, s>>>((const TermDev<2> *)tab->d_terms, tab->nterms, coef);
+    ctx->launches++;
+  }
+  if (b->W == 1)
+    launch_conn<1>(ctx, b, *tab, lv, wreq, cptr, conn, true);
+  else
+    launch_conn<2>(ctx, b, *tab, lv, wreq, cptr, conn, true);
+  qg_status st = qg_check_launch(ctx, "connection lists");
+  if (st == QG_OK) {
+    e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) st = qg_cuda_fail(ctx, e, "connection lists");
+  }
+  if (st == QG_OK) st = qg_check_device_error(ctx, "connection lists");
+  if (st != QG_OK) {
+    cudaFree(cptr);
+    cudaFree(conn);
+    cudaFree(coef);
+    return st;
+  }
+  c.d_cptr = cptr;
+  c.d_conn = conn;
+  c.d_coef = coef;
+  c.nconn = total;
+  c.conn_state = 1;
+  return QG_OK;
+}
+
+static qg_status ensure_conn(qg_context ctx, qg_operator op, qg_basis b, OpBasisCache *c) {
+  if (!ctx->conn_lists || c->conn_state != 0) return QG_OK;
+  return build_conn(ctx, op, b, *c);
+}
+
+bool qg_apply_uses_lists(qg_operator op, qg_basis b) {
+  qg_context ctx = b->ctx;
+  if (!ctx->conn_lists || op->nf != b->nf || b->n <= 0) return false;
+  qg_status st = QG_OK;
+  OpBasisCache *c = qg_basis_cache(b, op, &st);
+  if (st != QG_OK || !c) return false;
+  if (ensure_conn(ctx, op, b, c) != QG_OK) return false;
+  return c->conn_state == 1;
+}
+
+template <int W, int NV, bool FUSE>
+static void launch_apply_list_t(qg_context ctx, const OpBasisCache *c, const double2 *diag, qg_basis dst,
+                                const double2 *x, int xs, double2 *y, int ys, int vec0, const ApplyFuse &fz,
+                                const LocalView &lv) {
+  k_apply_list<W, NV, FUSE><<<qg_apply_grid(dst), 256, 0, ctx->stream>>>(
+      (const Key<W> *)dst->d_keys, dst->n, c->d_cptr, c->d_conn, c->d_coef, diag, x, xs, y, ys, vec0, fz, lv);
+  ctx->launches++;
+}
+
+template <int W, bool FUSE>
+static void launch_apply_list(qg_context ctx, const OpBasisCache *c, const double2 *diag, qg_basis dst,
+                              const double2 *x, int xs, double2 *y, int ys, int nvec, const ApplyFuse &fz,
+                              const LocalView &lv, int chunk) {
+  if (chunk <= 0) chunk = 8;
+  int v = 0;
+  while (v < nvec) {
+    int left = std::min(nvec - v, chunk);
+    if (left >= 8) {
+      launch_apply_list_t<W, 8, FUSE>(ctx, c, diag, dst, x, xs, y, ys, v, fz, lv);
+      v += 8;
+    } else if (left >= 4) {
+      launch_apply_list_t<W, 4, FUSE>(ctx, c, diag, dst, x, xs, y, ys, v, fz, lv);
+      v += 4;
+    } else if (left >= 2) {
+      launch_apply_list_t<W, 2, FUSE>(ctx, c, diag, dst, x, xs, y, ys, v, fz, lv);
+      v += 2;
+    } else {
+      launch_apply_list_t<W, 1, FUSE>(ctx, c, diag, dst, x, xs, y, ys, v, fz, lv);
+      v += 1;
+    }
+  }
+}
+
 // ------------------------------------------------------------------ entry points
 
 static int tuned_chunk(const OpBasisCache *c, int nvec) {
@@ -1235,6 +1713,24 @@ static qg_status apply_chunked(qg_context ctx, qg_operator op, qg_basis dst, qg_
       tab = &op->pull_off;
     }
     if (c->wreq_exact && c->d_wreq && tab == &op->pull_nl) wreq = c->d_wreq;
+    if (chunk > 0) {  // thread per row: gather through the connection lists when built
+      QG_TRY(ensure_conn(ctx, op, dst, c));
+      if (c->conn_state == 1) {
+        const ApplyFuse &f = fz ? *fz : none;
+        if (op->W == 1) {
+          if (fz)
+            launch_apply_list<1, true>(ctx, c, diag, dst, x2, xs, y2, ys, nvec, f, lv, chunk);
+          else
+            launch_apply_list<1, false>(ctx, c, diag, dst, x2, xs, y2, ys, nvec, f, lv, chunk);
+        } else {
+          if (fz)
+            launch_apply_list<2, true>(ctx, c, diag, dst, x2, xs, y2, ys, nvec, f, lv, chunk);
+          else
+            launch_apply_list<2, false>(ctx, c, diag, dst, x2, xs, y2, ys, nvec, f, lv, chunk);
+        }
+        return qg_check_launch(ctx, "qg_apply");
+      }
+    }
   }
   int packed = 0;
   if (nvec == 1) {
@@ -1275,12 +1771,40 @@ extern "C" qg_status qg_apply(qg_context ctx, qg_operator op, qg_basis dst, qg_b
   return qg_apply_launch(ctx, op, dst, src, x_dev, y_dev, nvec, nullptr);
 }
 
+// Device address of a page-locked host buffer (cudaHostAlloc / cudaHostRegister memory is
+// mapped into the device's address space), or nullptr for pageable memory.
+static void *mapped_host(const void *p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
+// Streams a page-locked host buffer into device memory with the SMs (16-byte loads, grid
+// stride): every SM pulls over the host link at once.
+__global__ void k_pull_host(const double2 *__restrict__ src, double2 *__restrict__ dst, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    dst[i] = src[i];
+}
+
 extern "C" qg_status qg_apply_host(qg_context ctx, qg_operator op, qg_basis dst, qg_basis src, const double *x_host,
                                    double *y_host, int32_t nvec) {
   if (!ctx || !op || !dst || !src || nvec <= 0 || !x_host || !y_host || op->nf != dst->nf || op->nf != src->nf)
     return QG_ERR_ARG;
   size_t xb = (size_t)src->n * nvec * 16, yb = (size_t)dst->n * nvec * 16;
-  size_t need = xb + yb;
+  if (!dst->n) return QG_OK;
+  if (!src->n) {
+    QG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    memset(y_host, 0, yb);
+    return QG_OK;
+  }
+  // page-locked buffers: x is pulled by the SMs, y is written by the apply kernel straight
+  // into host memory (the copy back overlaps the gather); pageable ones go through staging
+  const double2 *xmap = (const double2 *)mapped_host(x_host);
+  double *ymap = (double *)mapped_host(y_host);
+  size_t need = xb + (ymap ? 0 : yb);
   if (ctx->io_bytes < need) {
     cudaStreamSynchronize(ctx->stream);
     cudaFree(ctx->d_io);
@@ -1289,11 +1813,19 @@ extern "C" qg_status qg_apply_host(qg_context ctx, qg_operator op, qg_basis dst,
     QG_CUDA(ctx, cudaMalloc(&ctx->d_io, need));
     ctx->io_bytes = need;
   }
-  double *dx = ctx->d_io, *dy = ctx->d_io + xb / 8;
-  if (xb) QG_CUDA(ctx, cudaMemcpyAsync(dx, x_host, xb, cudaMemcpyHostToDevice, ctx->stream));
+  double *dx = ctx->d_io, *dy = ymap ? ymap : ctx->d_io + xb / 8;
+  if (xmap) {
+    int64_t n2 = (int64_t)(xb / 16);
+    unsigned g = (unsigned)std::min<int64_t>((n2 + 255) / 256, (int64_t)ctx->num_sms * 8);
+    k_pull_host<<<g, 256, 0, ctx->stream>>>(xmap, (double2 *)dx, n2);
+    ctx->launches++;
+    QG_TRY(qg_check_launch(ctx, "qg_apply_host pull"));
+  } else {
+    QG_CUDA(ctx, cudaMemcpyAsync(dx, x_host, xb, cudaMemcpyHostToDevice, ctx->stream));
+  }
   qg_status st = qg_apply(ctx, op, dst, src, dx, dy, nvec);
   if (st != QG_OK) return st;
-  if (yb) QG_CUDA(ctx, cudaMemcpyAsync(y_host, dy, yb, cudaMemcpyDeviceToHost, ctx->stream));
+  if (!ymap) QG_CUDA(ctx, cudaMemcpyAsync(y_host, dy, yb, cudaMemcpyDeviceToHost, ctx->stream));
   QG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   return qg_check_device_error(ctx, "qg_apply_host");
 }
@@ -1378,6 +1910,63 @@ extern "C" qg_status qg_apply_set_chunk(qg_context ctx, qg_operator op, qg_basis
       return QG_OK;
     }
   c->chunk.push_back({nvec, chunk});
+  return QG_OK;
+}
+
+extern "C" qg_status qg_set_connection_lists(qg_context ctx, int32_t on) {
+  if (!ctx) return QG_ERR_ARG;
+  ctx->conn_lists = on != 0;
+  return QG_OK;
+}
+
+extern "C" qg_status qg_apply_list_info(qg_context ctx, qg_operator op, qg_basis b, int32_t *built, int64_t *nconn) {
+  if (!ctx || !op || !b || !built || !nconn || op->nf != b->nf) return QG_ERR_ARG;
+  *built = 0;
+  *nconn = 0;
+  for (auto &c : b->caches)
+    if (c.op_uid == op->uid && c.conn_state == 1) {
+      *built = 1;
+      *nconn = c.nconn;
+    }
+  return QG_OK;
+}
+
+extern "C" qg_status qg_apply_fp64_ops(qg_context ctx, qg_operator op, qg_basis b, int64_t *ops) {
+  if (!ctx || !op || !b || !ops || op->nf != b->nf) return QG_ERR_ARG;
+  *ops = 0;
+  if (!b->n) return QG_OK;
+  if (!qg_apply_uses_lists(op, b)) {
+    ctx->last_error = "qg_apply_fp64_ops: no connection lists for this operator and basis";
+    return QG_ERR_ARG;
+  }
+  qg_status st = QG_OK;
+  OpBasisCache *c = qg_basis_cache(b, op, &st);
+  if (st != QG_OK) return st;
+  const HostTable *tab;
+  LocalView lv;
+  const uint64_t *wreq;
+  same_basis_view(op, b, c, &tab, &lv, &wreq);
+  unsigned long long *d = nullptr;
+  QG_CUDA(ctx, cudaMalloc(&d, 8));
+  cudaError_t e = cudaMemsetAsync(d, 0, 8, ctx->stream);
+  if (e == cudaSuccess) {
+    if (b->W == 1)
+      k_count_fp64<1><<<grid_for(b->n, 256), 256, 0, ctx->stream>>>((const Key<1> *)b->d_keys, b->n, c->d_cptr,
+                                                                      c->d_conn, c->d_coef,
+                                                                      (const double2 *)c->d_diag, lv, d);
+    else
+      k_count_fp64<2><<<grid_for(b->n, 256), 256, 0, ctx->stream>>>((const Key<2> *)b->d_keys, b->n, c->d_cptr,
+                                                                      c->d_conn, c->d_coef,
+                                                                      (const double2 *)c->d_diag, lv, d);
+    ctx->launches++;
+    e = cudaGetLastError();
+  }
+  unsigned long long h = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&h, d, 8, cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  cudaFree(d);
+  if (e != cudaSuccess) return qg_cuda_fail(ctx, e, "qg_apply_fp64_ops");
+  *ops = (int64_t)h;
   return QG_OK;
 }
 

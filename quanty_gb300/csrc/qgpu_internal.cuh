@@ -94,6 +94,7 @@ struct qg_context_s {
   size_t io_bytes = 0;
   bool use_graphs = true;             // capture Lanczos step sequences into CUDA graphs
   bool autotune = true;               // time the vectors-per-pass choices of multi-vector applies
+  bool conn_lists = true;             // resolve hashed connections once per (operator, basis)
 };
 
 // A term table in one device allocation: ngroups GroupDev followed by nterms TermDev.
@@ -158,6 +159,17 @@ struct OpBasisCache {
   LocalEntry *d_ent = nullptr;
   uint32_t *d_ent_target = nullptr;  // target local configuration of each entry
   int64_t nent = 0;
+  // connection lists: per row, in the order the thread-per-row apply visits them, the
+  // connections it would otherwise resolve through the hash table (local moves without a
+  // certain offset, hit or miss; hits of the scanned table), each as (source row, meta):
+  // meta = term index in the scanned table | parity sign << 31, QG_NO_INDEX rows mark a
+  // local move whose source is absent.  Built once per (operator, basis); every later H*psi
+  // gathers x[source] by row, so neighbouring rows read neighbouring sources.
+  int conn_state = 0;             // 0 not tried, 1 built, -1 not built (size, memory, capture)
+  int64_t nconn = 0;
+  int64_t *d_cptr = nullptr;      // [n + 1] list offsets
+  uint2 *d_conn = nullptr;        // [nconn]
+  double2 *d_coef = nullptr;      // [terms of the scanned table] (vre, vim)
   // autotuned vectors per pass of the apply kernel, per number of vectors (pairs nvec, chunk)
   std::vector<std::pair<int, int>> chunk;
 };
@@ -313,6 +325,9 @@ qg_status qg_apply_strided(qg_context ctx, qg_operator op, qg_basis dst, qg_basi
 qg_status qg_pack(qg_context ctx, qg_basis b, const double *x, int xs, const double *scale, const double *thr2,
                   double *own_out);
 int qg_apply_grid(qg_basis dst);
+// True when the same-basis apply of op on b gathers through connection lists (builds the
+// per-(operator, basis) cache first), so a caller need not pack x into the hash slots.
+bool qg_apply_uses_lists(qg_operator op, qg_basis b);
 
 // Hermitian eigenproblem of a small host matrix (row-major k x k): ascending values, columns of
 // V the eigenvectors (cyclic Jacobi, qgpu_eigen.cu)

@@ -400,8 +400,10 @@ extern "C" qg_status qg_lanczos_tridiag(qg_context ctx, qg_operator op, qg_basis
   }
   // the normalised, truncated Krylov vector vc from a raw vector: for one vector the same
   // kernel also writes it into the basis' hash slots for the gather
+  // (with connection lists the apply gathers from vc itself and the slots are not needed)
+  const bool pack1 = nvec == 1 && !qg_apply_uses_lists(op, b);
   auto normalise = [&](const double2 *raw) -> qg_status {
-    if (nvec == 1) return qg_pack(ctx, b, (const double *)raw, 1, scale, thr2, (double *)vc);
+    if (pack1) return qg_pack(ctx, b, (const double *)raw, 1, scale, thr2, (double *)vc);
     k_scale_trunc<<<(unsigned)((len + 255) / 256), 256, 0, s>>>(n, nvec, raw, scale, thr2, vc);
     ctx->launches++;
     return qg_check_launch(ctx, "scale");
@@ -417,7 +419,7 @@ extern "C" qg_status qg_lanczos_tridiag(qg_context ctx, qg_operator op, qg_basis
   fz.dot_part = dpart;
   if (st == QG_OK) st = normalise((const double2 *)v0_dev);
   if (st == QG_OK)
-    st = qg_apply_strided(ctx, op, b, b, (const double *)vc, nvec, (double *)w, nvec, nvec, &fz, nvec == 1);
+    st = qg_apply_strided(ctx, op, b, b, (const double *)vc, nvec, (double *)w, nvec, nvec, &fz, pack1);
   if (st == QG_OK && krylov_dev)
     e = cudaMemcpyAsync(krylov_dev, vc, len * 16, cudaMemcpyDeviceToDevice, s);
   if (st == QG_OK) {
@@ -439,7 +441,7 @@ extern "C" qg_status qg_lanczos_tridiag(qg_context ctx, qg_operator op, qg_basis
     if (sst != QG_OK) return sst;
     fz.prev = vp;
     fz.beta = b_now;
-    sst = qg_apply_strided(ctx, op, b, b, (const double *)vc, nvec, (double *)w2, nvec, nvec, &fz, nvec == 1);
+    sst = qg_apply_strided(ctx, op, b, b, (const double *)vc, nvec, (double *)w2, nvec, nvec, &fz, pack1);
     std::swap(w, w2);
     if (sst == QG_OK && krylov_dev) {
       cudaError_t ce = cudaMemcpyAsync(krylov_dev + 2 * (size_t)i * len, vc, len * 16, cudaMemcpyDeviceToDevice, s);

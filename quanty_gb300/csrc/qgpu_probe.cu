@@ -50,3 +50,47 @@ extern "C" qg_status qg_gather_bandwidth(qg_context ctx, int64_t bytes, double *
   *gbs = (double)nthr * 4 * 32 * 3 / (ms * 1e-3) / 1e9;
   return QG_OK;
 }
+
+// FP64 issue ceiling of the device: every thread runs 8 independent FMA chains in registers,
+// all lanes active, no memory traffic.  The H*psi kernel's FP64 work is charged against it.
+__global__ void k_fp64_probe(int iters, double m, double c, double *out) {
+  double a[8];
+#pragma unroll
+  for (int k = 0; k < 8; k++) a[k] = 1.0 + 1e-3 * (threadIdx.x + k);
+  for (int it = 0; it < iters; it++) {
+#pragma unroll
+    for (int k = 0; k < 8; k++) a[k] = fma(a[k], m, c);
+  }
+  double s = 0;
+#pragma unroll
+  for (int k = 0; k < 8; k++) s += a[k];
+  if (s == -1.0) out[0] = s;  // never taken (the chains stay positive), keeps the work
+}
+
+extern "C" qg_status qg_fp64_peak(qg_context ctx, double *gops) {
+  if (!ctx || !gops) return QG_ERR_ARG;
+  double *out = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaStream_t s = ctx->stream;
+  cudaError_t e = cudaMalloc(&out, 8);
+  if (e == cudaSuccess) e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  const int iters = 4096, bs = 256;
+  const unsigned grid = (unsigned)ctx->num_sms * 8;
+  float ms = 0;
+  if (e == cudaSuccess) {
+    k_fp64_probe<<<grid, bs, 0, s>>>(iters, 0.9999999, 1e-9, out);  // warm
+    cudaEventRecord(e0, s);
+    for (int r = 0; r < 3; r++) k_fp64_probe<<<grid, bs, 0, s>>>(iters, 0.9999999, 1e-9, out);
+    cudaEventRecord(e1, s);
+    ctx->launches += 4;
+    e = cudaEventSynchronize(e1);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaFree(out);
+  if (e != cudaSuccess) return qg_cuda_fail(ctx, e, "qg_fp64_peak");
+  *gops = (double)grid * bs * iters * 8 * 3 / (ms * 1e-3) / 1e9;
+  return QG_OK;
+}

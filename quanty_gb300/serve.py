@@ -24,12 +24,14 @@ from . import api
 
 
 def _footprint(n_det, nvec, ntri=0, krylov=False):
-    """Device bytes a job holds at its peak (basis, lookup table, Lanczos state)."""
+    """Device bytes a job holds at its peak (basis, lookup table, connection lists with up to
+    12 hashed connections per row, Lanczos state)."""
     keys = 16 * n_det
     table = 32 * 2 * n_det + 8 * 2 * n_det
+    lists = 8 * n_det + 8 * 12 * n_det
     vectors = 16 * n_det * nvec * 7
     kry = 16 * n_det * ntri if krylov else 0
-    return int(keys + table + vectors + kry + (64 << 20))
+    return int(keys + table + lists + vectors + kry + (64 << 20))
 
 
 class SpectraJob:

@@ -282,3 +282,46 @@ def test_anderson_impurity_apply_matches_oracle(api, oracle_mod, nshell, hmax, p
     # the same on a basis given as plain determinants (no windows, no closure): full checks
     y2 = api.OperatorPsiConserveBasis(H, api.Wavefunction(H.nf, dets[::-1].copy(), x[::-1].copy()))
     assert rel_err(y2.val[::-1], want) < TOL
+
+
+@pytest.mark.parametrize("model", ["random", "anderson"])
+def test_connection_lists_give_the_same_bits(api, model):
+    """The apply over per-row connection lists (sources resolved once per operator and basis)
+    sums every row's connections in the hash path's order: outputs are bitwise equal, for one
+    vector, several vectors and a Lanczos chain."""
+    import ctypes
+    import torch
+    from quanty_gb300 import workloads
+    eng = api.engine()
+    rng = np.random.default_rng(12)
+    if model == "random":
+        nf = 30
+        H = _random_operator(api, nf, 60, 60, rng)
+        seed, R, depth = api.dets_to_bytes(["1" * 8 + "0" * 22], nf), None, 3
+    else:
+        H, R, s0, info = workloads.anderson_impurity(nshell=2, hole_max=2, particle_max=2)
+        nf, seed, depth = H.nf, api.dets_to_bytes([s0], H.nf), -1
+    out = {}
+    try:
+        for on in (0, 1):
+            eng.check(eng.L.qg_set_connection_lists(eng.ctx, on))
+            b = api.closure(H, seed, nf, R, depth)
+            if on == 0:
+                X = torch.from_numpy(rng.normal(size=(b.n, 5)) + 1j * rng.normal(size=(b.n, 5))).cuda()
+            x1 = X[:, :1].contiguous()
+            y1, y5 = eng.empty(b.n), eng.empty(b.n, 5)
+            eng.check(eng.L.qg_apply(eng.ctx, H.handle(), b.h, b.h, api._ptr(x1), api._ptr(y1), 1))
+            eng.check(eng.L.qg_apply_set_chunk(eng.ctx, H.handle(), b.h, 5, 4))
+            eng.check(eng.L.qg_apply(eng.ctx, H.handle(), b.h, b.h, api._ptr(X), api._ptr(y5), 5))
+            built, nconn = ctypes.c_int32(), ctypes.c_int64()
+            eng.check(eng.L.qg_apply_list_info(eng.ctx, H.handle(), b.h, ctypes.byref(built), ctypes.byref(nconn)))
+            assert built.value == on
+            if on:
+                assert nconn.value > 0
+            a, bb = api.lanczos_block(H, b, x1.clone(), 30, 0.0, 0.0, eng)
+            out[on] = (y1, y5, a, bb)
+    finally:
+        eng.check(eng.L.qg_set_connection_lists(eng.ctx, 1))
+    assert torch.equal(out[0][0], out[1][0])
+    assert torch.equal(out[0][1], out[1][1])
+    assert np.array_equal(out[0][2], out[1][2]) and np.array_equal(out[0][3], out[1][3])
