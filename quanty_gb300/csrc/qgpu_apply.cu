@@ -762,6 +762,19 @@ __global__ void __launch_bounds__(256) k_conn(const Key<W> *__restrict__ rows, i
 // The apply over connection lists: diagonal, local moves (certain offsets inline, the others
 // from the list), then the listed table connections; the arithmetic of each connection is
 // k_apply's (qg_cmac with the parity-flipped value), in the same order.
+//
+// Rows of a warp share their local moves (one block of the sorted basis) but not the lengths
+// of their lists, so a warp would run its list loop as long as its longest row with the other
+// lanes idle -- on FP64 issue, the kernel's limit.  With REGROUP the block's 256 rows are
+// dealt out again after the local moves, sorted by the length of what is left of their lists
+// (a counting sort in shared memory), so each warp continues 32 rows of about equal length.
+// Each row keeps its accumulator and its order of summation, so the output is bitwise the
+// same; the fused epilogue's dot partials are reduced in the original row order.
+#ifndef QG_LIST_REGROUP
+#define QG_LIST_REGROUP 1
+#endif
+#define QG_REGROUP_BUCKETS 64
+
 template <int W, int NV, bool FUSE>
 __global__ void __launch_bounds__(256, NV == 1 ? QG_APPLY_MIN_BLOCKS : 1)
     k_apply_list(const Key<W> *__restrict__ rows, int64_t n_rows, const int64_t *__restrict__ cptr,
@@ -773,6 +786,7 @@ __global__ void __launch_bounds__(256, NV == 1 ? QG_APPLY_MIN_BLOCKS : 1)
   double2 acc[NV];
 #pragma unroll
   for (int k = 0; k < NV; k++) acc[k] = make_double2(0.0, 0.0);
+  int64_t p = 0, pe = 0;
   if (live) {
     if (diag) {
       double2 dg = diag[r];
@@ -792,8 +806,8 @@ __global__ void __launch_bounds__(256, NV == 1 ? QG_APPLY_MIN_BLOCKS : 1)
         }
       }
     }
-    int64_t p = __ldg(cptr + r);
-    const int64_t pe = __ldg(cptr + r + 1);
+    p = __ldg(cptr + r);
+    pe = __ldg(cptr + r + 1);
     if (lv.on) {
       const Key<W> d = rows[r];
       int b = __ldg(lv.cfg + get_local<W>(d, lv.lo, lv.lmask));
@@ -817,6 +831,49 @@ __global__ void __launch_bounds__(256, NV == 1 ? QG_APPLY_MIN_BLOCKS : 1)
         for (int k = 0; k < NV; k++) qg_cmac(acc[k], vr, vi, cplx, __ldg(x + j * xs + vec0 + k));
       }
     }
+  }
+  int me = threadIdx.x;  // the block position of the row this thread finishes
+  __shared__ double2 s_acc[QG_LIST_REGROUP ? NV : 1][QG_LIST_REGROUP ? 256 : 1];  // also the dot partials
+  if (QG_LIST_REGROUP) {
+    __shared__ int s_cnt[QG_REGROUP_BUCKETS];
+    __shared__ int64_t s_p[256], s_pe[256];
+    __shared__ int s_me[256];
+    if (threadIdx.x < QG_REGROUP_BUCKETS) s_cnt[threadIdx.x] = 0;
+    __syncthreads();
+    int64_t left = live && pe > p ? pe - p : 0;
+    int bucket = (int)(left < QG_REGROUP_BUCKETS - 1 ? left : QG_REGROUP_BUCKETS - 1);
+    atomicAdd(&s_cnt[bucket], 1);
+    __syncthreads();
+    if (threadIdx.x < 32) {  // exclusive scan of the bucket counts, longest lists first
+      int lane = threadIdx.x;
+      int c0 = s_cnt[QG_REGROUP_BUCKETS - 1 - 2 * lane], c1 = s_cnt[QG_REGROUP_BUCKETS - 2 - 2 * lane];
+      int v = c0 + c1, incl = v;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        int t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+      }
+      int excl = incl - v;
+      s_cnt[QG_REGROUP_BUCKETS - 1 - 2 * lane] = excl;
+      s_cnt[QG_REGROUP_BUCKETS - 2 - 2 * lane] = excl + c0;
+    }
+    __syncthreads();
+    int slot = atomicAdd(&s_cnt[bucket], 1);
+    s_p[slot] = p;
+    s_pe[slot] = live ? pe : p;
+    s_me[slot] = threadIdx.x;
+#pragma unroll
+    for (int k = 0; k < NV; k++) s_acc[k][slot] = acc[k];
+    __syncthreads();
+    p = s_p[threadIdx.x];
+    pe = s_pe[threadIdx.x];
+    me = s_me[threadIdx.x];
+#pragma unroll
+    for (int k = 0; k < NV; k++) acc[k] = s_acc[k][threadIdx.x];
+    r = blockIdx.x * (int64_t)blockDim.x + me;
+    live = r < n_rows;
+  }
+  if (live) {
     for (; p < pe; p++) {
       uint2 cn = __ldg(conn + p);
       double2 cf = __ldg(coef + (cn.y & 0x7FFFFFFFu));
@@ -836,6 +893,7 @@ __global__ void __launch_bounds__(256, NV == 1 ? QG_APPLY_MIN_BLOCKS : 1)
   } else {
     __shared__ double2 red[NV][8];
     int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    double2 dvs[NV];
 #pragma unroll
     for (int k = 0; k < NV; k++) {
       double2 dv = make_double2(0.0, 0.0);
@@ -847,6 +905,19 @@ __global__ void __launch_bounds__(256, NV == 1 ? QG_APPLY_MIN_BLOCKS : 1)
         double be = fz.beta[vec0 + k];
         y[r * ys + vec0 + k] = make_double2(acc[k].x - be * pv.x, acc[k].y - be * pv.y);
       }
+      dvs[k] = dv;
+    }
+    if (QG_LIST_REGROUP) {  // back to the original row order for the reduction
+      __syncthreads();  // every regrouped accumulator has been read
+#pragma unroll
+      for (int k = 0; k < NV; k++) s_acc[k][me] = dvs[k];
+      __syncthreads();
+#pragma unroll
+      for (int k = 0; k < NV; k++) dvs[k] = s_acc[k][threadIdx.x];
+    }
+#pragma unroll
+    for (int k = 0; k < NV; k++) {
+      double2 dv = dvs[k];
 #pragma unroll
       for (int o = 16; o; o >>= 1) {
         dv.x += __shfl_xor_sync(0xffffffffu, dv.x, o);
