@@ -1853,11 +1853,19 @@ static void *mapped_host(const void *p) {
   return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
 }
 
-// Streams a page-locked host buffer into device memory with the SMs (16-byte loads, grid
-// stride): every SM pulls over the host link at once.
+// Streams a page-locked host buffer into device memory with the SMs: every SM pulls over the
+// host link at once, each thread with four 16-byte loads in flight before its stores.
 __global__ void k_pull_host(const double2 *__restrict__ src, double2 *__restrict__ dst, int64_t n) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    dst[i] = src[i];
+  const int64_t T = (int64_t)gridDim.x * blockDim.x;
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  for (; i + 3 * T < n; i += 4 * T) {
+    double2 v0 = src[i], v1 = src[i + T], v2 = src[i + 2 * T], v3 = src[i + 3 * T];
+    dst[i] = v0;
+    dst[i + T] = v1;
+    dst[i + 2 * T] = v2;
+    dst[i + 3 * T] = v3;
+  }
+  for (; i < n; i += T) dst[i] = src[i];
 }
 
 extern "C" qg_status qg_apply_host(qg_context ctx, qg_operator op, qg_basis dst, qg_basis src, const double *x_host,

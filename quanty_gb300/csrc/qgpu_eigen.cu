@@ -6,9 +6,10 @@
 // (:5489-5496), reorthogonalises twice against all Krylov vectors (:5498-5527), diagonalises
 // the projected matrix with zheevd (:5530) and restarts from the Ritz vectors (:5554-5573)
 // until the variance <H^2> - <H>^2 of every vector is below "Zero".  The same structure here:
-// H*psi is the pull kernel, the Gram products and updates run as memory-bound kernels over
-// the n x K Krylov block (row-major, K columns), and the projected matrix (K <= a few
-// hundred) is diagonalised on the host: Householder reduction to a real tridiagonal matrix,
+// H*psi is the pull kernel, the Gram products and updates of whole blocks are plain complex
+// GEMMs over the n x K Krylov block (row-major, K columns; cuBLAS, qgpu_blas.cu), single
+// columns use the partial-sum kernels below, and the projected matrix (K <= a few hundred)
+// is diagonalised on the host: Householder reduction to a real tridiagonal matrix,
 // implicit QL with Wilkinson shifts, then the wanted eigenvectors transformed back.
 //
 // Block size: when more than three states are wanted, a few guard vectors join the block
@@ -42,6 +43,83 @@ __global__ void k_gram_partial(const double2 *__restrict__ A, int lda, int a0, i
   part[(int64_t)blockIdx.y * ka * kb + q] = make_double2(sr, si);
 }
 
+// Gram products against ONE column b (kb = 1): part[blk][i] = sum over the block's rows of
+// conj(A[r][a0+i]) b[r].  With ka <= 8 a thread takes whole rows and keeps the ka sums in
+// registers; with more columns a warp takes a row and its lanes take the columns (coalesced
+// reads of the row).  Grid-stride over rows with many blocks, so the reduction is wide rather
+// than a long serial walk per thread; sums are combined in a fixed order.
+template <int KMAX>
+__global__ void k_gram_col_rows(const double2 *__restrict__ A, int lda, int a0, int ka, const double2 *__restrict__ B,
+                                int ldb, int b0, int64_t n, double2 *part) {
+  __shared__ double2 sh[8][KMAX];
+  double2 acc[KMAX];
+#pragma unroll
+  for (int i = 0; i < KMAX; i++) acc[i] = make_double2(0.0, 0.0);
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    double2 b = B[r * ldb + b0];
+#pragma unroll
+    for (int i = 0; i < KMAX; i++) {
+      if (i < ka) {
+        double2 a = A[r * lda + a0 + i];
+        acc[i].x += a.x * b.x + a.y * b.y;
+        acc[i].y += a.x * b.y - a.y * b.x;
+      }
+    }
+  }
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int i = 0; i < KMAX; i++) {
+    double2 v = acc[i];
+    for (int o = 16; o; o >>= 1) {
+      v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+      v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+    }
+    if (lane == 0) sh[wid][i] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < ka) {
+    double2 t = make_double2(0.0, 0.0);
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
+      t.x += sh[w][threadIdx.x].x;
+      t.y += sh[w][threadIdx.x].y;
+    }
+    part[(int64_t)blockIdx.x * ka + threadIdx.x] = t;
+  }
+}
+
+#define QG_GRAM_LANE_COLS 8  // columns per lane: ka <= 256
+__global__ void k_gram_col_lanes(const double2 *__restrict__ A, int lda, int a0, int ka,
+                                 const double2 *__restrict__ B, int ldb, int b0, int64_t n, double2 *part) {
+  __shared__ double2 sh[8][32 * QG_GRAM_LANE_COLS];
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  double2 acc[QG_GRAM_LANE_COLS];
+#pragma unroll
+  for (int m = 0; m < QG_GRAM_LANE_COLS; m++) acc[m] = make_double2(0.0, 0.0);
+  for (int64_t r = (int64_t)blockIdx.x * nw + wid; r < n; r += (int64_t)gridDim.x * nw) {
+    double2 b = B[r * ldb + b0];
+#pragma unroll
+    for (int m = 0; m < QG_GRAM_LANE_COLS; m++) {
+      int i = lane + 32 * m;
+      if (i < ka) {
+        double2 a = A[r * lda + a0 + i];
+        acc[m].x += a.x * b.x + a.y * b.y;
+        acc[m].y += a.x * b.y - a.y * b.x;
+      }
+    }
+  }
+#pragma unroll
+  for (int m = 0; m < QG_GRAM_LANE_COLS; m++) sh[wid][lane + 32 * m] = acc[m];
+  __syncthreads();
+  for (int i = threadIdx.x; i < ka; i += blockDim.x) {
+    double2 t = make_double2(0.0, 0.0);
+    for (int w = 0; w < nw; w++) {
+      t.x += sh[w][i].x;
+      t.y += sh[w][i].y;
+    }
+    part[(int64_t)blockIdx.x * ka + i] = t;
+  }
+}
+
 __global__ void k_gram_reduce(const double2 *part, int nchunk, int m, double2 *out) {
   int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= m) return;
@@ -67,22 +145,6 @@ __global__ void k_sub_mul(const double2 *__restrict__ A, int lda, int a0, int ka
     acc.y -= a.x * c.y + a.y * c.x;
   }
   B[r * ldb + b0 + j] = acc;
-}
-
-// X[r][j] = sum_i A[r][i] Y[i*kb + j]
-__global__ void k_combine(const double2 *__restrict__ A, int lda, int ka, const double2 *__restrict__ Y, double2 *X,
-                          int ldx, int kb, int64_t n) {
-  int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (t >= n * kb) return;
-  int64_t r = t / kb;
-  int j = (int)(t % kb);
-  double2 acc = make_double2(0, 0);
-  for (int i = 0; i < ka; i++) {
-    double2 a = A[r * lda + i], y = Y[i * kb + j];
-    acc.x += a.x * y.x - a.y * y.y;
-    acc.y += a.x * y.y + a.y * y.x;
-  }
-  X[r * ldx + j] = acc;
 }
 
 __global__ void k_scale_col(double2 *B, int ldb, int col, int64_t n, double s) {
@@ -121,14 +183,16 @@ struct Gram {
   int64_t cap = 0;
   int nchunk = 1;
   int64_t chunk = 1;
+  int nblk = 1;  // blocks of the one-column Gram kernels
   qg_status init(qg_context c, int64_t nn, int maxm) {
     ctx = c;
     n = nn;
     chunk = std::max<int64_t>(4096, (nn + 1023) / 1024);
     nchunk = (int)((nn + chunk - 1) / chunk);
     if (nchunk < 1) nchunk = 1;
+    nblk = (int)std::max<int64_t>(1, std::min<int64_t>(4LL * c->num_sms, (nn + 255) / 256));
     cap = maxm;
-    QG_CUDA(ctx, cudaMalloc(&part, (size_t)nchunk * maxm * 16));
+    QG_CUDA(ctx, cudaMalloc(&part, (size_t)std::max(nchunk * (int64_t)maxm, (int64_t)nblk * 32 * QG_GRAM_LANE_COLS) * 16));
     QG_CUDA(ctx, cudaMalloc(&out, (size_t)maxm * 16));
     return QG_OK;
   }
@@ -141,10 +205,21 @@ struct Gram {
                 std::vector<cd> *host) {
     int m = ka * kb;
     if (m > cap || m <= 0) return QG_ERR_ARG;
-    dim3 g((m + 127) / 128, nchunk);
-    k_gram_partial<<<g, 128, 0, ctx->stream>>>(A, lda, a0, ka, B, ldb, b0, kb, n, chunk, part);
-    k_gram_reduce<<<(m + 127) / 128, 128, 0, ctx->stream>>>(part, nchunk, m, out);
-    ctx->launches += 2;
+    if (kb > 1) {  // a block against a block: a plain GEMM (cuBLAS)
+      QG_TRY(qg_zgemm_ahb(ctx, A + a0, lda, ka, B + b0, ldb, kb, n, out));
+    } else if (ka <= 32 * QG_GRAM_LANE_COLS) {  // one column: wide partial sums, fixed-order reduction
+      if (ka <= 8)
+        k_gram_col_rows<8><<<nblk, 256, 0, ctx->stream>>>(A, lda, a0, ka, B, ldb, b0, n, part);
+      else
+        k_gram_col_lanes<<<nblk, 256, 0, ctx->stream>>>(A, lda, a0, ka, B, ldb, b0, n, part);
+      k_gram_reduce<<<(m + 127) / 128, 128, 0, ctx->stream>>>(part, nblk, m, out);
+      ctx->launches += 2;
+    } else {
+      dim3 g((m + 127) / 128, nchunk);
+      k_gram_partial<<<g, 128, 0, ctx->stream>>>(A, lda, a0, ka, B, ldb, b0, kb, n, chunk, part);
+      k_gram_reduce<<<(m + 127) / 128, 128, 0, ctx->stream>>>(part, nchunk, m, out);
+      ctx->launches += 2;
+    }
     if (host) {
       host->resize(m);
       QG_CUDA(ctx, cudaMemcpyAsync(host->data(), out, m * 16, cudaMemcpyDeviceToHost, ctx->stream));
@@ -217,8 +292,11 @@ extern "C" qg_status qg_block_groundstate(qg_context ctx, qg_operator op, qg_bas
     int k = 0;  // orthonormal columns in V
     T.assign((size_t)K * K, cd(0, 0));
     auto orth_block = [&](int c0, int cnt, std::vector<cd> *coef) -> int {
-      // orthonormalise V[:, c0:c0+cnt] against V[:, 0:c0] and among themselves; returns how
-      // many columns survived (kept contiguous from c0); coef (cnt x cnt upper) gets R.
+      // orthonormalise V[:, c0:c0+cnt] among themselves (modified Gram-Schmidt, twice);
+      // returns how many columns survived (kept contiguous from c0); coef gets R.  The block
+      // has already been projected twice against V[:, 0:c0] as a whole, so a column is
+      // projected against the old columns again only when the in-block passes cancelled most
+      // of it (norm below a tenth of its start: "twice is enough" no longer holds for it).
       int kept = 0;
       for (int j = 0; j < cnt && st == QG_OK; j++) {
         int col = c0 + kept;
@@ -232,22 +310,29 @@ extern "C" qg_status qg_block_groundstate(qg_context ctx, qg_operator op, qg_bas
           st = G.run(V, K, col, 1, V, K, col, 1, &h);
           nrm0 = std::sqrt(std::max(0.0, h[0].real()));
         }
-        for (int pass = 0; pass < 2 && st == QG_OK && col > 0; pass++) {
-          std::vector<cd> h;
-          st = G.run(V, K, 0, col, V, K, col, 1, &h);
-          if (st != QG_OK) break;
-          k_sub_mul<<<grid(n), 256, 0, s>>>(V, K, 0, col, G.out, V, K, col, 1, n);
-          ctx->launches++;
-          if (coef && pass == 0) {
-            for (int i = 0; i < col; i++) (*coef)[(size_t)i * cnt + j] += h[i];
-          } else if (coef) {
-            for (int i = 0; i < col; i++) (*coef)[(size_t)i * cnt + j] += h[i];
+        // project v_col against columns lo .. col-1, twice
+        auto project = [&](int lo) {
+          for (int pass = 0; pass < 2 && st == QG_OK && col > lo; pass++) {
+            std::vector<cd> h;
+            st = G.run(V, K, lo, col - lo, V, K, col, 1, &h);
+            if (st != QG_OK) break;
+            k_sub_mul<<<grid(n), 256, 0, s>>>(V, K, lo, col - lo, G.out, V, K, col, 1, n);
+            ctx->launches++;
+            if (coef)
+              for (int i = lo; i < col; i++) (*coef)[(size_t)i * cnt + j] += h[i - lo];
           }
-        }
+        };
+        project(c0);
         std::vector<cd> h;
         if (st == QG_OK) st = G.run(V, K, col, 1, V, K, col, 1, &h);
         if (st != QG_OK) break;
         double nrm = std::sqrt(std::max(0.0, h[0].real()));
+        if (c0 > 0 && nrm < 0.1 * nrm0) {
+          project(0);
+          if (st == QG_OK) st = G.run(V, K, col, 1, V, K, col, 1, &h);
+          if (st != QG_OK) break;
+          nrm = std::sqrt(std::max(0.0, h[0].real()));
+        }
         if (nrm <= 1e-10 * std::max(nrm0, 1e-300) || nrm == 0.0) continue;  // deflate
         k_scale_col<<<grid(n), 256, 0, s>>>(V, K, col, n, 1.0 / nrm);
         ctx->launches++;
@@ -276,8 +361,7 @@ extern "C" qg_status qg_block_groundstate(qg_context ctx, qg_operator op, qg_bas
         if (st != QG_OK) break;
         for (int i = 0; i < k; i++)
           for (int j = 0; j < bs; j++) T[(size_t)i * K + j0 + j] += c[(size_t)i * bs + j];
-        k_sub_mul<<<grid(n * bs), 256, 0, s>>>(V, K, 0, k, G.out, W, p, 0, bs, n);
-        ctx->launches++;
+        st = qg_zgemm_acc(ctx, V, K, k, G.out, W, p, bs, n, -1.0, 1.0);
       }
       if (st != QG_OK || k + bs > Kcur) break;
       // append W as new columns and orthonormalise them
@@ -326,8 +410,8 @@ extern "C" qg_status qg_block_groundstate(qg_context ctx, qg_operator op, qg_bas
       st = qg_cuda_fail(ctx, e, "ritz upload");
       break;
     }
-    k_combine<<<grid(n * p), 256, 0, s>>>(V, K, k, Cd, X, p, p, n);
-    ctx->launches++;
+    st = qg_zgemm_acc(ctx, V, K, k, Cd, X, p, p, n, 1.0, 0.0);
+    if (st != QG_OK) break;
     for (int j = 0; j < p; j++) theta[j] = w[j];
     // convergence: variance <(H - theta)^2> = |H x - theta x|^2 per vector, formed from the
     // residual itself (no cancellation between <H^2> and <H>^2)
@@ -342,8 +426,8 @@ extern "C" qg_status qg_block_groundstate(qg_context ctx, qg_operator op, qg_bas
         st = qg_cuda_fail(ctx, e, "residual");
         break;
       }
-      k_sub_mul<<<grid(n * p), 256, 0, s>>>(X, p, 0, p, Cd, W, p, 0, p, n);
-      ctx->launches++;
+      st = qg_zgemm_acc(ctx, X, p, p, Cd, W, p, p, n, -1.0, 1.0);
+      if (st != QG_OK) break;
     }
     std::vector<cd> hh;
     double worst = 0;

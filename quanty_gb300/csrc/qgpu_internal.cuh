@@ -95,6 +95,7 @@ struct qg_context_s {
   bool use_graphs = true;             // capture Lanczos step sequences into CUDA graphs
   bool autotune = true;               // time the vectors-per-pass choices of multi-vector applies
   bool conn_lists = true;             // resolve hashed connections once per (operator, basis)
+  void *blas = nullptr;               // cuBLAS handle of the dense block products (created on first use)
 };
 
 // A term table in one device allocation: ngroups GroupDev followed by nterms TermDev.
@@ -339,6 +340,14 @@ void hermitian_eigh(int k, std::vector<std::complex<double>> A, std::vector<doub
 void qg_host_eigh(int k, const std::vector<std::complex<double>> &A, std::vector<double> &w,
                   std::vector<std::complex<double>> &V);
 int qg_partial_blocks(qg_context ctx, int64_t n);
+
+// dense complex block products (qgpu_blas.cu, cuBLAS); row-major n x k blocks
+//   C (ka x kb row-major) = A^H B;   X = beta X + alpha A M  (M ka x kb row-major)
+qg_status qg_zgemm_ahb(qg_context ctx, const double2 *A, int lda, int ka, const double2 *B, int ldb, int kb,
+                       int64_t n, double2 *C);
+qg_status qg_zgemm_acc(qg_context ctx, const double2 *A, int lda, int ka, const double2 *M, double2 *X, int ldx,
+                       int kb, int64_t n, double alpha, double beta);
+void qg_blas_release(qg_context ctx);
 
 // reductions (qgpu_krylov.cu)
 qg_status qg_dot_dev(qg_context ctx, int64_t n, int nvec, const double *x, const double *y, double *out_dev);
