@@ -87,18 +87,19 @@ __global__ void k_gram_col_rows(const double2 *__restrict__ A, int lda, int a0, 
   }
 }
 
-#define QG_GRAM_LANE_COLS 8  // columns per lane: ka <= 256
+#define QG_GRAM_LANE_COLS 8  // columns per lane at most: ka <= 256
+template <int M>
 __global__ void k_gram_col_lanes(const double2 *__restrict__ A, int lda, int a0, int ka,
                                  const double2 *__restrict__ B, int ldb, int b0, int64_t n, double2 *part) {
-  __shared__ double2 sh[8][32 * QG_GRAM_LANE_COLS];
+  __shared__ double2 sh[8][32 * M];
   int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  double2 acc[QG_GRAM_LANE_COLS];
+  double2 acc[M];
 #pragma unroll
-  for (int m = 0; m < QG_GRAM_LANE_COLS; m++) acc[m] = make_double2(0.0, 0.0);
+  for (int m = 0; m < M; m++) acc[m] = make_double2(0.0, 0.0);
   for (int64_t r = (int64_t)blockIdx.x * nw + wid; r < n; r += (int64_t)gridDim.x * nw) {
     double2 b = B[r * ldb + b0];
 #pragma unroll
-    for (int m = 0; m < QG_GRAM_LANE_COLS; m++) {
+    for (int m = 0; m < M; m++) {
       int i = lane + 32 * m;
       if (i < ka) {
         double2 a = A[r * lda + a0 + i];
@@ -108,7 +109,7 @@ __global__ void k_gram_col_lanes(const double2 *__restrict__ A, int lda, int a0,
     }
   }
 #pragma unroll
-  for (int m = 0; m < QG_GRAM_LANE_COLS; m++) sh[wid][lane + 32 * m] = acc[m];
+  for (int m = 0; m < M; m++) sh[wid][lane + 32 * m] = acc[m];
   __syncthreads();
   for (int i = threadIdx.x; i < ka; i += blockDim.x) {
     double2 t = make_double2(0.0, 0.0);
@@ -129,6 +130,22 @@ __global__ void k_gram_reduce(const double2 *part, int nchunk, int m, double2 *o
     si += part[(int64_t)c * m + q].y;
   }
   out[q] = make_double2(sr, si);
+}
+
+// the same with a warp per output: lanes stride over the partials, then a shuffle tree
+__global__ void k_gram_reduce_warp(const double2 *part, int nchunk, int m, double2 *out) {
+  int q = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (q >= m) return;
+  double sr = 0, si = 0;
+  for (int c = lane; c < nchunk; c += 32) {
+    sr += part[(int64_t)c * m + q].x;
+    si += part[(int64_t)c * m + q].y;
+  }
+  for (int o = 16; o; o >>= 1) {
+    sr += __shfl_xor_sync(0xffffffffu, sr, o);
+    si += __shfl_xor_sync(0xffffffffu, si, o);
+  }
+  if (lane == 0) out[q] = make_double2(sr, si);
 }
 
 // B[r][b0+j] -= sum_i A[r][a0+i] C[i*kb + j]
@@ -208,11 +225,22 @@ struct Gram {
     if (kb > 1) {  // a block against a block: a plain GEMM (cuBLAS)
       QG_TRY(qg_zgemm_ahb(ctx, A + a0, lda, ka, B + b0, ldb, kb, n, out));
     } else if (ka <= 32 * QG_GRAM_LANE_COLS) {  // one column: wide partial sums, fixed-order reduction
-      if (ka <= 8)
-        k_gram_col_rows<8><<<nblk, 256, 0, ctx->stream>>>(A, lda, a0, ka, B, ldb, b0, n, part);
+      cudaStream_t s = ctx->stream;
+      if (ka == 1)
+        k_gram_col_rows<1><<<nblk, 256, 0, s>>>(A, lda, a0, ka, B, ldb, b0, n, part);
+      else if (ka <= 4)
+        k_gram_col_rows<4><<<nblk, 256, 0, s>>>(A, lda, a0, ka, B, ldb, b0, n, part);
+      else if (ka <= 8)
+        k_gram_col_rows<8><<<nblk, 256, 0, s>>>(A, lda, a0, ka, B, ldb, b0, n, part);
+      else if (ka <= 32)
+        k_gram_col_lanes<1><<<nblk, 256, 0, s>>>(A, lda, a0, ka, B, ldb, b0, n, part);
+      else if (ka <= 64)
+        k_gram_col_lanes<2><<<nblk, 256, 0, s>>>(A, lda, a0, ka, B, ldb, b0, n, part);
+      else if (ka <= 128)
+        k_gram_col_lanes<4><<<nblk, 256, 0, s>>>(A, lda, a0, ka, B, ldb, b0, n, part);
       else
-        k_gram_col_lanes<<<nblk, 256, 0, ctx->stream>>>(A, lda, a0, ka, B, ldb, b0, n, part);
-      k_gram_reduce<<<(m + 127) / 128, 128, 0, ctx->stream>>>(part, nblk, m, out);
+        k_gram_col_lanes<8><<<nblk, 256, 0, s>>>(A, lda, a0, ka, B, ldb, b0, n, part);
+      k_gram_reduce_warp<<<(m + 7) / 8, 256, 0, s>>>(part, nblk, m, out);
       ctx->launches += 2;
     } else {
       dim3 g((m + 127) / 128, nchunk);
