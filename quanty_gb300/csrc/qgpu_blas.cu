@@ -65,3 +65,21 @@ qg_status qg_zgemm_acc(qg_context ctx, const double2 *A, int lda, int ka, const 
   if (s != CUBLAS_STATUS_SUCCESS) return blas_fail(ctx, s, "block update");
   return QG_OK;
 }
+
+// out (n x np, row-major) = sum_i K_i C[i][:]: the vectors K_i (vector-major, K[i * n + r],
+// i < ntri) combined with C (ntri x np, row-major).  Transposed: out^T = C^T K^T.
+qg_status qg_zgemm_combine(qg_context ctx, const double2 *K, int64_t n, int ntri, const double2 *C, int np,
+                           double2 *out) {
+  if (n <= 0 || np <= 0) return QG_OK;
+  if (ntri <= 0) {
+    QG_CUDA(ctx, cudaMemsetAsync(out, 0, (size_t)n * np * 16, ctx->stream));
+    return QG_OK;
+  }
+  cublasHandle_t h;
+  QG_TRY(blas_handle(ctx, &h));
+  const cuDoubleComplex one = make_cuDoubleComplex(1.0, 0.0), zero = make_cuDoubleComplex(0.0, 0.0);
+  cublasStatus_t s = cublasZgemm_64(h, CUBLAS_OP_N, CUBLAS_OP_T, np, n, ntri, &one, (const cuDoubleComplex *)C, np,
+                                    (const cuDoubleComplex *)K, n, &zero, (cuDoubleComplex *)out, np);
+  if (s != CUBLAS_STATUS_SUCCESS) return blas_fail(ctx, s, "Krylov combination");
+  return QG_OK;
+}

@@ -347,6 +347,9 @@ qg_status qg_zgemm_ahb(qg_context ctx, const double2 *A, int lda, int ka, const 
                        int64_t n, double2 *C);
 qg_status qg_zgemm_acc(qg_context ctx, const double2 *A, int lda, int ka, const double2 *M, double2 *X, int ldx,
                        int kb, int64_t n, double alpha, double beta);
+// out (n x np row-major) = sum_i K_i C[i][:], K vector-major (K[i * n + r])
+qg_status qg_zgemm_combine(qg_context ctx, const double2 *K, int64_t n, int ntri, const double2 *C, int np,
+                           double2 *out);
 void qg_blas_release(qg_context ctx);
 
 // reductions (qgpu_krylov.cu)

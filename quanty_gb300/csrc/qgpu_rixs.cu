@@ -116,20 +116,6 @@ __global__ void k_trunc_vec(int64_t n, double2 *v, const double *mult, const dou
 }
 
 // out[r][p] = sum_i K_i[r] C[i][p] (K vector-major, C row-major ntri x np)
-__global__ void k_krylov_combine(const double2 *K, int64_t n, int ntri, const double2 *C, int np, double2 *out) {
-  int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (t >= n * np) return;
-  int64_t r = t / np;
-  int p = (int)(t % np);
-  double2 acc = make_double2(0, 0);
-  for (int i = 0; i < ntri; i++) {
-    double2 k = K[(int64_t)i * n + r], c = C[i * np + p];
-    acc.x += k.x * c.x - k.y * c.y;
-    acc.y += k.x * c.y + k.y * c.x;
-  }
-  out[t] = acc;
-}
-
 // ------------------------------------------------------------------ Krylov-basis Lanczos
 
 // Lanczos keeping the Krylov vectors, the reference's LanczosTriDiagonalizeKrylovCC: modified
@@ -326,8 +312,7 @@ extern "C" qg_status qg_resonant_spectra(qg_context ctx, qg_operator H1, qg_oper
     if ((e = cudaMalloc(&Cd, C.size() * 16)) != cudaSuccess) break;
     if ((e = cudaMemcpyAsync(Cd, C.data(), C.size() * 16, cudaMemcpyHostToDevice, s)) != cudaSuccess) break;
     if ((e = cudaMalloc(&gt, (size_t)std::max<int64_t>(n1, 1) * np * 16)) != cudaSuccess) break;
-    k_krylov_combine<<<gridn(n1 * np), 256, 0, s>>>((const double2 *)K, n1, nt, Cd, np, (double2 *)gt);
-    ctx->launches++;
+    if ((st = qg_zgemm_combine(ctx, (const double2 *)K, n1, nt, Cd, np, (double2 *)gt)) != QG_OK) break;
     // T2 targets of all operators, their closure under H2: the common final-state basis
     for (int j = 0; j < nt2 && st == QG_OK; j++) {
       qg_basis tj = nullptr;
