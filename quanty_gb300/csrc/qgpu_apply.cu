@@ -781,6 +781,7 @@ __global__ void __launch_bounds__(256, NV == 1 ? QG_APPLY_MIN_BLOCKS : 1)
                  const uint2 *__restrict__ conn, const double2 *__restrict__ coef, const double2 *__restrict__ diag,
                  const double2 *__restrict__ x, int xs, double2 *__restrict__ y, int ys, int vec0, ApplyFuse fz,
                  LocalView lv) {
+  vec0 += blockIdx.y * NV;  // passes of NV vectors side by side (gridDim.y of them)
   int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   bool live = r < n_rows;
   double2 acc[NV];
@@ -1650,13 +1651,17 @@ bool qg_apply_uses_lists(qg_operator op, qg_basis b) {
 
 template <int W, int NV, bool FUSE>
 static void launch_apply_list_t(qg_context ctx, const OpBasisCache *c, const double2 *diag, qg_basis dst,
-                                const double2 *x, int xs, double2 *y, int ys, int vec0, const ApplyFuse &fz,
-                                const LocalView &lv) {
-  k_apply_list<W, NV, FUSE><<<qg_apply_grid(dst), 256, 0, ctx->stream>>>(
+                                const double2 *x, int xs, double2 *y, int ys, int vec0, int npass,
+                                const ApplyFuse &fz, const LocalView &lv) {
+  dim3 grid((unsigned)qg_apply_grid(dst), (unsigned)npass);
+  k_apply_list<W, NV, FUSE><<<grid, 256, 0, ctx->stream>>>(
       (const Key<W> *)dst->d_keys, dst->n, c->d_cptr, c->d_conn, c->d_coef, diag, x, xs, y, ys, vec0, fz, lv);
   ctx->launches++;
 }
 
+// Passes of 8, 4, 2 or 1 vectors (at most `chunk` per pass, the same passes as the hash
+// path); all passes of one width run as one launch with a pass per blockIdx.y, so a small
+// basis still spreads its vectors over the SMs.
 template <int W, bool FUSE>
 static void launch_apply_list(qg_context ctx, const OpBasisCache *c, const double2 *diag, qg_basis dst,
                               const double2 *x, int xs, double2 *y, int ys, int nvec, const ApplyFuse &fz,
@@ -1665,19 +1670,17 @@ static void launch_apply_list(qg_context ctx, const OpBasisCache *c, const doubl
   int v = 0;
   while (v < nvec) {
     int left = std::min(nvec - v, chunk);
-    if (left >= 8) {
-      launch_apply_list_t<W, 8, FUSE>(ctx, c, diag, dst, x, xs, y, ys, v, fz, lv);
-      v += 8;
-    } else if (left >= 4) {
-      launch_apply_list_t<W, 4, FUSE>(ctx, c, diag, dst, x, xs, y, ys, v, fz, lv);
-      v += 4;
-    } else if (left >= 2) {
-      launch_apply_list_t<W, 2, FUSE>(ctx, c, diag, dst, x, xs, y, ys, v, fz, lv);
-      v += 2;
-    } else {
-      launch_apply_list_t<W, 1, FUSE>(ctx, c, diag, dst, x, xs, y, ys, v, fz, lv);
-      v += 1;
-    }
+    int per = left >= 8 ? 8 : left >= 4 ? 4 : left >= 2 ? 2 : 1;
+    int np = std::min((nvec - v) / per, 65535);
+    if (per == 8)
+      launch_apply_list_t<W, 8, FUSE>(ctx, c, diag, dst, x, xs, y, ys, v, np, fz, lv);
+    else if (per == 4)
+      launch_apply_list_t<W, 4, FUSE>(ctx, c, diag, dst, x, xs, y, ys, v, np, fz, lv);
+    else if (per == 2)
+      launch_apply_list_t<W, 2, FUSE>(ctx, c, diag, dst, x, xs, y, ys, v, np, fz, lv);
+    else
+      launch_apply_list_t<W, 1, FUSE>(ctx, c, diag, dst, x, xs, y, ys, v, np, fz, lv);
+    v += per * np;
   }
 }
 
