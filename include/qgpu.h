@@ -82,6 +82,21 @@ qg_status qg_operator_destroy(qg_operator op);
  * Core/OperatorArithmetic.cpp:6517; 1 = Hermitian within 1e-12 relative). */
 qg_status qg_operator_info(qg_operator op, int32_t *nterms, int32_t *ngroups, int32_t *hermitian);
 
+/* Parameter scans: H = sum_k p_k O_k over already uploaded operators (all on the same nf),
+ * the reference's operator sum and scalar product (OperatorAdd, Core/OperatorArithmetic.cpp:5674,
+ * after NormalOrderOperator, :1607), kept on the device so that a scan does not rebuild it.
+ * The sum operator holds the union of the components' terms -- zero values included, so its
+ * structure does not depend on the coefficients -- and each term's contribution per
+ * component.  qg_operator_set_coefficients(op, p) recomputes the values in place (ordered on
+ * the context's stream after the work already queued); bases keep their per-operator caches
+ * (local blocks, connection lists) and only refresh the values on their next use.  A term
+ * whose value is zero reaches no determinant in basis growth (the reference holds no zero
+ * terms).  coef_im may be NULL (real coefficients).  The components may be destroyed
+ * afterwards; set_coefficients returns QG_ERR_ARG for an operator that is not a sum. */
+qg_status qg_operator_create_sum(qg_context ctx, int32_t ncomp, const qg_operator *components,
+                                 const double *coef_re, const double *coef_im, qg_operator *op);
+qg_status qg_operator_set_coefficients(qg_operator op, const double *coef_re, const double *coef_im);
+
 /* ------------------------------------------------------------------ bases */
 
 /* Build a basis from n determinants (reference byte layout, n * ceil(nf/8) bytes, host

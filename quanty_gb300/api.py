@@ -187,6 +187,53 @@ class Operator:
                 pass
 
 
+class OperatorSum(Operator):
+    """H = sum_k p_k O_k kept on the device for parameter scans.  A Quanty scan rebuilds H with
+    OperatorAdd (Core/OperatorArithmetic.cpp:5674) for every parameter set; here the union of
+    the components' terms is uploaded once and ``set_coefficients`` rewrites only the values,
+    so every basis keeps its local blocks and connection lists and refreshes only the values.
+    ``terms`` always holds the current sum as plain ladder strings."""
+
+    def __init__(self, components, coefficients, name="OperatorSum"):
+        self.components = list(components)
+        if not self.components or any(c.nf != self.components[0].nf for c in self.components):
+            raise ValueError("OperatorSum: components must exist and share nf")
+        self.coefficients = np.asarray(coefficients, dtype=np.complex128).reshape(-1)
+        if len(self.coefficients) != len(self.components):
+            raise ValueError("OperatorSum: one coefficient per component")
+        super().__init__(self.components[0].nf, self._sum_terms(), name)
+
+    def _sum_terms(self):
+        return [(o, complex(v) * complex(p)) for comp, p in zip(self.components, self.coefficients)
+                for o, v in comp.terms]
+
+    def _coef_arrays(self):
+        return (np.ascontiguousarray(self.coefficients.real), np.ascontiguousarray(self.coefficients.imag))
+
+    def handle(self, eng=None):
+        eng = eng or engine()
+        key = id(eng)
+        if key not in self._handles:
+            hs = np.array([c.handle(eng).value for c in self.components], dtype=np.uint64)
+            re, im = self._coef_arrays()
+            h = C.c_void_p()
+            eng.check(eng.L.qg_operator_create_sum(eng.ctx, len(self.components), _ptr(hs), _ptr(re), _ptr(im),
+                                                   C.byref(h)))
+            self._handles[key] = (eng, h, (hs, re, im))
+        return self._handles[key][1]
+
+    def set_coefficients(self, coefficients):
+        c = np.asarray(coefficients, dtype=np.complex128).reshape(-1)
+        if len(c) != len(self.components):
+            raise ValueError("OperatorSum: one coefficient per component")
+        self.coefficients = c
+        self.terms = [(tuple(int(o) for o in ops), complex(v)) for ops, v in self._sum_terms()]
+        re, im = self._coef_arrays()
+        for eng, h, _ in self._handles.values():
+            eng.check(eng.L.qg_operator_set_coefficients(h, _ptr(re), _ptr(im)))
+        return self
+
+
 def NewOperator(nf, nb, terms):
     """Lua-style constructor: each term is ``[i1, i2, ..., value]`` with a non-negative index
     for a creation and a negative index (or -0.0) for an annihilation operator, leftmost factor

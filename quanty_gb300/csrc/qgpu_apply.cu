@@ -1388,7 +1388,7 @@ static qg_status build_local(qg_basis bs, qg_operator op, OpBasisCache &c) {
     eoff[k] = (uint32_t)ent.size();
     for (auto &kv : acc) {
       int32_t tbk = table[kv.first];
-      if (tbk < 0 || (kv.second.first == 0.0 && kv.second.second == 0.0)) continue;
+      if (tbk < 0 || (!op->keep_zero && kv.second.first == 0.0 && kv.second.second == 0.0)) continue;
       LocalEntry le;
       le.tstart = hstart[tbk];
       le.tend = hstart[tbk + 1] | (cls[k] == cls[tbk] ? 0x80000000u : 0u);
@@ -1408,6 +1408,10 @@ static qg_status build_local(qg_basis bs, qg_operator op, OpBasisCache &c) {
   eoff[nb] = (uint32_t)ent.size();
   c.nblocks = (int)nb;
   c.nent = (int64_t)ent.size();
+  c.h_bcfg = hcfg;
+  c.h_eoff = eoff;
+  c.h_etarget = etarget;
+  c.h_ent = ent;
   c.d_bstart = bst;
   e = cudaMalloc(&c.d_cfg, table.size() * 4);
   if (e == cudaSuccess) e = cudaMemcpy(c.d_cfg, table.data(), table.size() * 4, cudaMemcpyHostToDevice);
@@ -1424,10 +1428,90 @@ static qg_status build_local(qg_basis bs, qg_operator op, OpBasisCache &c) {
   return QG_OK;
 }
 
+// New values of a sum operator's local entries on the blocks of a cache (same entries, same
+// order: the entry set of a sum operator does not depend on its values).
+static qg_status refresh_local(qg_basis bs, qg_operator op, OpBasisCache &c) {
+  if (c.nent == 0) return QG_OK;
+  int H = op->H, lo = bs->nf - H, W = bs->W;
+  struct LT {
+    uint32_t n1, n0, fl, sg;
+    double re, im;
+  };
+  std::vector<LT> lt;
+  for (auto &t : op->local_off)
+    lt.push_back({to_local(t.n1, lo, W), to_local(t.n0, lo, W), to_local(t.fl, lo, W), to_local(t.sg, lo, W), t.re,
+                  t.im});
+  for (size_t k = 0; k + 1 < c.h_eoff.size(); k++) {
+    uint32_t cc = c.h_bcfg[k];
+    std::map<uint32_t, std::pair<double, double>> acc;
+    for (auto &t : lt) {
+      if ((cc & t.n1) != t.n1 || (cc & t.n0)) continue;
+      double sg = (__builtin_popcount(cc & t.sg) & 1) ? -1.0 : 1.0;
+      auto &v = acc[cc ^ t.fl];
+      v.first += sg * t.re;
+      v.second += sg * t.im;
+    }
+    for (uint32_t e = c.h_eoff[k]; e < c.h_eoff[k + 1]; e++) {
+      auto &v = acc[c.h_etarget[e]];
+      c.h_ent[e].vre = v.first;
+      c.h_ent[e].vim = v.second;
+    }
+  }
+  QG_CUDA(bs->ctx, cudaMemcpyAsync(c.d_ent, c.h_ent.data(), c.h_ent.size() * sizeof(LocalEntry),
+                                   cudaMemcpyHostToDevice, bs->ctx->stream));
+  return QG_OK;
+}
+
+static void launch_diag(qg_context ctx, qg_operator op, qg_basis b, double *d_diag);
+template <int W>
+__global__ void k_term_coef(const TermDev<W> *__restrict__ terms, int nterms, double2 *coef);
+
+// A sum operator was rescaled since this cache was built: recompute what depends on values
+// (the diagonal, the local entries' values, the list coefficients); the structure -- blocks,
+// entries, window bits, connection lists -- stays.
+static qg_status refresh_values(qg_basis b, qg_operator op, OpBasisCache &c) {
+  qg_context ctx = b->ctx;
+  if (b->n) launch_diag(ctx, op, b, c.d_diag);
+  if (op->H > 0) QG_TRY(refresh_local(b, op, c));
+  if (c.conn_state == 1) {
+    const HostTable &tab = op->H > 0 ? op->pull_nl : op->pull_off;
+    if (tab.nterms > 0) {
+      if (b->W == 1)
+        k_term_coef<1><<<(tab.nterms + 255) / 256, 256, 0, ctx->stream>>>((const TermDev<1> *)tab.d_terms, tab.nterms,
+                                                                          c.d_coef);
+      else
+        k_term_coef<2><<<(tab.nterms + 255) / 256, 256, 0, ctx->stream>>>((const TermDev<2> *)tab.d_terms, tab.nterms,
+                                                                          c.d_coef);
+      ctx->launches++;
+    }
+  }
+  c.op_version = op->version;
+  return qg_check_launch(ctx, "value refresh");
+}
+
+// the diagonal of op on every row of b (all flip == 0 terms), into d_diag
+static void launch_diag(qg_context ctx, qg_operator op, qg_basis b, double *d_diag) {
+  if (op->W == 1)
+    k_diag<1><<<grid_for(b->n, 256), 256, 0, ctx->stream>>>((const Key<1> *)b->d_keys, b->n,
+                                                            (const GroupDev<1> *)op->diag.d_groups, op->diag.ngroups,
+                                                            (const TermDev<1> *)op->diag.d_terms, (double2 *)d_diag);
+  else
+    k_diag<2><<<grid_for(b->n, 256), 256, 0, ctx->stream>>>((const Key<2> *)b->d_keys, b->n,
+                                                            (const GroupDev<2> *)op->diag.d_groups, op->diag.ngroups,
+                                                            (const TermDev<2> *)op->diag.d_terms, (double2 *)d_diag);
+  ctx->launches++;
+}
+
 OpBasisCache *qg_basis_cache(qg_basis b, qg_operator op, qg_status *st) {
   *st = QG_OK;
   for (auto &c : b->caches)
-    if (c.op_uid == op->uid) return &c;
+    if (c.op_uid == op->uid) {
+      if (c.op_version != op->version) {
+        *st = refresh_values(b, op, c);
+        if (*st != QG_OK) return nullptr;
+      }
+      return &c;
+    }
   qg_context ctx = b->ctx;
   if (b->caches.size() >= 4) {  // small cache: drop the oldest
     cudaStreamSynchronize(ctx->stream);
@@ -1436,22 +1520,13 @@ OpBasisCache *qg_basis_cache(qg_basis b, qg_operator op, qg_status *st) {
   }
   OpBasisCache c;
   c.op_uid = op->uid;
+  c.op_version = op->version;
   cudaError_t e = cudaMalloc(&c.d_diag, std::max<int64_t>(b->n, 1) * 16);
   if (e != cudaSuccess) {
     *st = qg_cuda_fail(ctx, e, "diagonal");
     return nullptr;
   }
-  if (b->n) {
-    if (op->W == 1)
-      k_diag<1><<<grid_for(b->n, 256), 256, 0, ctx->stream>>>((const Key<1> *)b->d_keys, b->n,
-                                                              (const GroupDev<1> *)op->diag.d_groups, op->diag.ngroups,
-                                                              (const TermDev<1> *)op->diag.d_terms, (double2 *)c.d_diag);
-    else
-      k_diag<2><<<grid_for(b->n, 256), 256, 0, ctx->stream>>>((const Key<2> *)b->d_keys, b->n,
-                                                              (const GroupDev<2> *)op->diag.d_groups, op->diag.ngroups,
-                                                              (const TermDev<2> *)op->diag.d_terms, (double2 *)c.d_diag);
-    ctx->launches++;
-  }
+  if (b->n) launch_diag(ctx, op, b, c.d_diag);
   // window bits of the non-local terms (encoding: 5 bits per window, moves of up to 2)
   c.wreq_exact = b->nres > 0 && b->nres <= 12;
   if (c.wreq_exact) {

@@ -450,7 +450,9 @@ __global__ void k_expand(const Key<W> *src, int64_t r0, int64_t r1, const GroupD
         app &= (d.w[i] & T.need0[i]) == 0;
         moved |= T.flip[i] != 0;
       }
-      if (!app) continue;
+      // a term whose value is zero (a sum operator's component scaled to 0) reaches nothing,
+      // as in the reference, whose operators hold no zero terms
+      if (!app || (T.vre == 0.0 && T.vim == 0.0)) continue;
       Key<W> tg;
 #pragma unroll
       for (int i = 0; i < W; i++) tg.w[i] = d.w[i] ^ T.flip[i];

@@ -110,12 +110,17 @@ struct HostTable {
   int nhop = 0;              // leading hop groups
   uint64_t hopmask[2] = {0, 0};
   size_t tgrp_off = 0;       // byte offset of the uint32 group index of each term (after the terms)
+  // host copy of the blob and, per term slot, the forward term it came from and the sign
+  // its value carries (adjoint tables): what a rescale of a sum operator patches
+  std::vector<unsigned char> h_blob;
+  std::vector<std::pair<int, int>> slot_src;
 };
 
 // A digested term on the host (canonical masks in device bit positions, signed value).
 struct HostTerm {
   uint64_t n1[2], n0[2], fl[2], sg[2];
   double re, im;
+  int src = -1, sgn = 1;  // forward term it came from, sign its value carries
 };
 
 struct qg_operator_s {
@@ -136,6 +141,16 @@ struct qg_operator_s {
   std::vector<HostTerm> local_off;
   HostTable pull_nl;
   std::vector<HostTerm> nl_host;
+  // forward terms in creation order (masks and values)
+  std::vector<HostTerm> fwd_host;
+  // sum operators (parameter scans, qg_operator_create_sum): the union of the components'
+  // terms, zero values kept, so the structure never depends on the coefficients; comp holds
+  // each term's contribution per component ([ncomp][fwd] complex); a rescale rewrites the
+  // values and bumps `version`, and per-basis caches refresh their values when they see it
+  int ncomp = 0;
+  bool keep_zero = false;
+  std::vector<double> comp_re, comp_im;
+  uint64_t version = 0;
 };
 
 // Per-(operator, basis) precomputed data for the same-basis H*psi.
@@ -149,6 +164,10 @@ struct LocalEntry {
 
 struct OpBasisCache {
   uint64_t op_uid = 0;
+  uint64_t op_version = 0;        // the operator's value version the cached values belong to
+  // host copies for a value refresh (sum operators): configuration of each block, entries
+  std::vector<uint32_t> h_bcfg, h_eoff, h_etarget;
+  std::vector<LocalEntry> h_ent;
   double *d_diag = nullptr;       // complex per row: all diagonal terms
   uint64_t *d_wreq = nullptr;     // per term of op->pull_nl: window bits its source needs
   bool wreq_exact = false;        // every term's window change fits the bit encoding

@@ -105,6 +105,8 @@ Masks adjoint(const Masks &m, int &cflip) {
 struct Entry {
   Masks m;
   double re, im;
+  int src = -1;  // forward term it came from
+  int sgn = 1;   // sign its value carries relative to that term's value
 };
 
 template <int W>
@@ -189,6 +191,7 @@ void build_table(qg_context ctx, const std::vector<Entry> &terms, HostTable &tab
       td.vre = terms[t].re;
       td.vim = terms[t].im;
       tt.push_back(td);
+      tab.slot_src.push_back({terms[t].src, terms[t].sgn});
       if (order) {
         HostTerm h;
         for (int i = 0; i < 2; i++) {
@@ -199,6 +202,8 @@ void build_table(qg_context ctx, const std::vector<Entry> &terms, HostTable &tab
         }
         h.re = terms[t].re;
         h.im = terms[t].im;
+        h.src = terms[t].src;
+        h.sgn = terms[t].sgn;
         order->push_back(h);
       }
     }
@@ -221,6 +226,7 @@ void build_table(qg_context ctx, const std::vector<Entry> &terms, HostTable &tab
   if (!tg.empty()) std::memcpy(blob.data() + gb + tb, tg.data(), tg.size() * 4);
   cudaError_t e = cudaMalloc(&tab.d_blob, blob.size());
   if (e == cudaSuccess) e = cudaMemcpy(tab.d_blob, blob.data(), blob.size(), cudaMemcpyHostToDevice);
+  tab.h_blob = std::move(blob);
   tab.d_groups = tab.d_blob;
   tab.d_terms = (unsigned char *)tab.d_blob + gb;
   st = (e == cudaSuccess) ? QG_OK : qg_cuda_fail(ctx, e, "operator table upload");
@@ -229,6 +235,155 @@ void build_table(qg_context ctx, const std::vector<Entry> &terms, HostTable &tab
 bool is_diag(const Entry &e) { return e.m.fl[0] == 0 && e.m.fl[1] == 0; }
 
 }  // namespace
+
+namespace {
+
+// Forward terms (zero values dropped unless keep_zero) and their adjoints, with provenance.
+void forward_and_adjoint(const std::vector<Masks> &order, const std::vector<std::pair<double, double>> &vals,
+                         bool keep_zero, std::vector<Entry> &fwd, std::vector<Entry> &pull) {
+  for (size_t t = 0; t < order.size(); t++) {
+    const auto &v = vals[t];
+    if (!keep_zero && v.first == 0.0 && v.second == 0.0) continue;
+    Entry f;
+    f.m = order[t];
+    f.re = v.first;
+    f.im = v.second;
+    f.src = (int)t;
+    fwd.push_back(f);
+    int cf = 0;
+    Entry a;
+    a.m = adjoint(order[t], cf);
+    a.sgn = cf ? -1 : 1;
+    a.re = v.first * a.sgn;
+    a.im = v.second * a.sgn;
+    a.src = (int)t;
+    pull.push_back(a);
+  }
+}
+
+// Hermiticity: the adjoint of every term must be a term with the conjugate value.
+int hermitian_of(const std::vector<Entry> &fwd, const std::vector<Entry> &pull) {
+  double vmax = 0;
+  for (auto &e : fwd) vmax = std::max(vmax, std::hypot(e.re, e.im));
+  std::map<Masks, std::pair<double, double>> fm;
+  for (auto &e : fwd) fm[e.m] = {e.re, e.im};
+  for (auto &e : pull) {
+    auto it = fm.find(e.m);
+    double er = e.re, ei = -e.im;  // conj of the value of the adjoint term
+    double gr = 0, gi = 0;
+    if (it != fm.end()) {
+      gr = it->second.first;
+      gi = it->second.second;
+    }
+    if (std::hypot(gr - er, gi - ei) > 1e-12 * std::max(1.0, vmax)) return 0;
+  }
+  return 1;
+}
+
+}  // namespace
+
+// An operator from merged forward terms (masks in creation order and their values).  With
+// keep_zero, zero-valued terms stay in every table (sum operators: the structure must not
+// depend on the coefficients).
+static qg_status make_operator(qg_context ctx, int nf, int nterms, int maxlen, const std::vector<Masks> &order,
+                               const std::vector<std::pair<double, double>> &vals, bool keep_zero,
+                               qg_operator *out) {
+  std::vector<Entry> fwd, pull;
+  forward_and_adjoint(order, vals, keep_zero, fwd, pull);
+  int herm = hermitian_of(fwd, pull);
+  qg_operator op = new qg_operator_s();
+  op->ctx = ctx;
+  op->nf = nf;
+  op->W = qg_words_for(nf);
+  op->nterms_in = nterms;
+  op->nterms = (int)fwd.size();
+  op->hermitian = herm;
+  op->max_len = maxlen;
+  static uint64_t next_uid = 1;
+  op->uid = next_uid++;
+  op->keep_zero = keep_zero;
+  op->fwd_host.resize(order.size());
+  for (size_t t = 0; t < order.size(); t++) {
+    HostTerm &h = op->fwd_host[t];
+    for (int i = 0; i < 2; i++) {
+      h.n1[i] = order[t].n1[i];
+      h.n0[i] = order[t].n0[i];
+      h.fl[i] = order[t].fl[i];
+      h.sg[i] = order[t].sg[i];
+    }
+    h.re = vals[t].first;
+    h.im = vals[t].second;
+    h.src = (int)t;
+  }
+  std::vector<Entry> pull_off, diag;
+  for (auto &e : pull) (is_diag(e) ? diag : pull_off).push_back(e);
+  // local prefix: the leading orbitals that hold every term acting on three or more orbitals
+  int minbit = nf;
+  for (auto &e : fwd) {
+    int cnt = 0;
+    for (int i = 0; i < 2; i++) cnt += __builtin_popcountll(e.m.n1[i] | e.m.n0[i] | e.m.fl[i]);
+    if (cnt < 3) continue;
+    for (int p = 0; p < nf; p++) {
+      uint64_t bit = 1ull << (p & 63);
+      uint64_t any = e.m.n1[p >> 6] | e.m.n0[p >> 6] | e.m.fl[p >> 6];
+      if (any & bit) {
+        minbit = std::min(minbit, p);
+        break;
+      }
+    }
+  }
+  int H = (minbit < nf) ? nf - minbit : 0;
+  if (H > 20) H = 0;
+  std::vector<Entry> nonlocal;
+  if (H > 0) {
+    uint64_t lm[2] = {0, 0};
+    for (int p = nf - H; p < nf; p++) lm[p >> 6] |= 1ull << (p & 63);
+    for (auto &e : pull_off) {
+      bool inside = true;
+      for (int i = 0; i < 2; i++) inside &= ((e.m.n1[i] | e.m.n0[i] | e.m.fl[i] | e.m.sg[i]) & ~lm[i]) == 0;
+      if (inside) {
+        HostTerm h;
+        for (int i = 0; i < 2; i++) {
+          h.n1[i] = e.m.n1[i];
+          h.n0[i] = e.m.n0[i];
+          h.fl[i] = e.m.fl[i];
+          h.sg[i] = e.m.sg[i];
+        }
+        h.re = e.re;
+        h.im = e.im;
+        h.src = e.src;
+        h.sgn = e.sgn;
+        op->local_off.push_back(h);
+      } else {
+        nonlocal.push_back(e);
+      }
+    }
+  } else {
+    nonlocal = pull_off;
+  }
+  op->H = H;
+  qg_status st = QG_OK;
+  if (op->W == 1) {
+    build_table<1>(ctx, pull, op->pull, st);
+    if (st == QG_OK) build_table<1>(ctx, pull_off, op->pull_off, st);
+    if (st == QG_OK) build_table<1>(ctx, nonlocal, op->pull_nl, st, &op->nl_host);
+    if (st == QG_OK) build_table<1>(ctx, diag, op->diag, st);
+    if (st == QG_OK) build_table<1>(ctx, fwd, op->push, st);
+  } else {
+    build_table<2>(ctx, pull, op->pull, st);
+    if (st == QG_OK) build_table<2>(ctx, pull_off, op->pull_off, st);
+    if (st == QG_OK) build_table<2>(ctx, nonlocal, op->pull_nl, st, &op->nl_host);
+    if (st == QG_OK) build_table<2>(ctx, diag, op->diag, st);
+    if (st == QG_OK) build_table<2>(ctx, fwd, op->push, st);
+  }
+  if (st != QG_OK) {
+    qg_operator_destroy(op);
+    return st;
+  }
+  *out = op;
+  return QG_OK;
+}
+
 
 extern "C" qg_status qg_operator_create(qg_context ctx, int32_t nf, int32_t nterms, const int32_t *term_len,
                                         const uint16_t *ops, const double *v_re, const double *v_im,
@@ -267,108 +422,10 @@ extern "C" qg_status qg_operator_create(qg_context ctx, int32_t nf, int32_t nter
       it->second.second += im;
     }
   }
-  std::vector<Entry> fwd, pull;
-  double vmax = 0;
-  for (auto &m : order) {
-    auto v = merged[m];
-    if (v.first == 0.0 && v.second == 0.0) continue;
-    fwd.push_back({m, v.first, v.second});
-    vmax = std::max(vmax, std::hypot(v.first, v.second));
-    int cf = 0;
-    Masks a = adjoint(m, cf);
-    pull.push_back({a, v.first * (cf ? -1.0 : 1.0), v.second * (cf ? -1.0 : 1.0)});
-  }
-  // Hermiticity: the adjoint of every term must be a term with the conjugate value
-  int herm = 1;
-  {
-    std::map<Masks, std::pair<double, double>> fm;
-    for (auto &e : fwd) fm[e.m] = {e.re, e.im};
-    for (auto &e : pull) {
-      auto it = fm.find(e.m);
-      double er = e.re, ei = -e.im;  // conj of the value of the adjoint term
-      double gr = 0, gi = 0;
-      if (it != fm.end()) {
-        gr = it->second.first;
-        gi = it->second.second;
-      }
-      if (std::hypot(gr - er, gi - ei) > 1e-12 * std::max(1.0, vmax)) herm = 0;
-    }
-  }
-  qg_operator op = new qg_operator_s();
-  op->ctx = ctx;
-  op->nf = nf;
-  op->W = qg_words_for(nf);
-  op->nterms_in = nterms;
-  op->nterms = (int)fwd.size();
-  op->hermitian = herm;
-  op->max_len = maxlen;
-  static uint64_t next_uid = 1;
-  op->uid = next_uid++;
-  std::vector<Entry> pull_off, diag;
-  for (auto &e : pull) (is_diag(e) ? diag : pull_off).push_back(e);
-  // local prefix: the leading orbitals that hold every term acting on three or more orbitals
-  int minbit = nf;
-  for (auto &e : fwd) {
-    int cnt = 0;
-    for (int i = 0; i < 2; i++) cnt += __builtin_popcountll(e.m.n1[i] | e.m.n0[i] | e.m.fl[i]);
-    if (cnt < 3) continue;
-    for (int p = 0; p < nf; p++) {
-      uint64_t bit = 1ull << (p & 63);
-      uint64_t any = e.m.n1[p >> 6] | e.m.n0[p >> 6] | e.m.fl[p >> 6];
-      if (any & bit) {
-        minbit = std::min(minbit, p);
-        break;
-      }
-    }
-  }
-  int H = (minbit < nf) ? nf - minbit : 0;
-  if (H > 20) H = 0;
-  std::vector<Entry> nonlocal;
-  if (H > 0) {
-    uint64_t lm[2] = {0, 0};
-    for (int p = nf - H; p < nf; p++) lm[p >> 6] |= 1ull << (p & 63);
-    for (auto &e : pull_off) {
-      bool inside = true;
-      for (int i = 0; i < 2; i++) inside &= ((e.m.n1[i] | e.m.n0[i] | e.m.fl[i] | e.m.sg[i]) & ~lm[i]) == 0;
-      if (inside) {
-        HostTerm h;
-        for (int i = 0; i < 2; i++) {
-          h.n1[i] = e.m.n1[i];
-          h.n0[i] = e.m.n0[i];
-          h.fl[i] = e.m.fl[i];
-          h.sg[i] = e.m.sg[i];
-        }
-        h.re = e.re;
-        h.im = e.im;
-        op->local_off.push_back(h);
-      } else {
-        nonlocal.push_back(e);
-      }
-    }
-  } else {
-    nonlocal = pull_off;
-  }
-  op->H = H;
-  qg_status st = QG_OK;
-  if (op->W == 1) {
-    build_table<1>(ctx, pull, op->pull, st);
-    if (st == QG_OK) build_table<1>(ctx, pull_off, op->pull_off, st);
-    if (st == QG_OK) build_table<1>(ctx, nonlocal, op->pull_nl, st, &op->nl_host);
-    if (st == QG_OK) build_table<1>(ctx, diag, op->diag, st);
-    if (st == QG_OK) build_table<1>(ctx, fwd, op->push, st);
-  } else {
-    build_table<2>(ctx, pull, op->pull, st);
-    if (st == QG_OK) build_table<2>(ctx, pull_off, op->pull_off, st);
-    if (st == QG_OK) build_table<2>(ctx, nonlocal, op->pull_nl, st, &op->nl_host);
-    if (st == QG_OK) build_table<2>(ctx, diag, op->diag, st);
-    if (st == QG_OK) build_table<2>(ctx, fwd, op->push, st);
-  }
-  if (st != QG_OK) {
-    qg_operator_destroy(op);
-    return st;
-  }
-  *out = op;
-  return QG_OK;
+  std::vector<std::pair<double, double>> vals;
+  vals.reserve(order.size());
+  for (auto &m : order) vals.push_back(merged[m]);
+  return make_operator(ctx, nf, nterms, maxlen, order, vals, false, out);
 }
 
 extern "C" qg_status qg_operator_destroy(qg_operator op) {
@@ -387,5 +444,143 @@ extern "C" qg_status qg_operator_info(qg_operator op, int32_t *nterms, int32_t *
   if (nterms) *nterms = op->nterms;
   if (ngroups) *ngroups = op->pull.ngroups;
   if (hermitian) *hermitian = op->hermitian;
+  return QG_OK;
+}
+
+// ------------------------------------------------------------------ parameter scans
+
+namespace {
+
+// Rewrite the values of every term slot of a table from the forward values, and upload the
+// blob on the context's stream (ordered after the work already queued that reads it).
+template <int W>
+qg_status patch_table(qg_context ctx, HostTable &tab, const std::vector<HostTerm> &fwd) {
+  if (tab.slot_src.empty()) return QG_OK;
+  size_t base = (size_t)tab.ngroups * sizeof(GroupDev<W>);
+  for (size_t t = 0; t < tab.slot_src.size(); t++) {
+    TermDev<W> td;
+    unsigned char *at = tab.h_blob.data() + base + t * sizeof(TermDev<W>);
+    std::memcpy(&td, at, sizeof(td));
+    const HostTerm &f = fwd[tab.slot_src[t].first];
+    td.vre = tab.slot_src[t].second * f.re;
+    td.vim = tab.slot_src[t].second * f.im;
+    std::memcpy(at, &td, sizeof(td));
+  }
+  QG_CUDA(ctx, cudaMemcpyAsync(tab.d_blob, tab.h_blob.data(), tab.h_blob.size(), cudaMemcpyHostToDevice, ctx->stream));
+  return QG_OK;
+}
+
+}  // namespace
+
+extern "C" qg_status qg_operator_create_sum(qg_context ctx, int32_t ncomp, const qg_operator *comps,
+                                            const double *coef_re, const double *coef_im, qg_operator *out) {
+  if (!ctx || !out || ncomp <= 0 || !comps || !coef_re) return QG_ERR_ARG;
+  for (int k = 0; k < ncomp; k++)
+    if (!comps[k] || comps[k]->nf != comps[0]->nf) {
+      ctx->last_error = "qg_operator_create_sum: components must exist and share nf";
+      return QG_ERR_ARG;
+    }
+  int nf = comps[0]->nf, maxlen = 0, nin = 0;
+  // union of the components' forward terms, each term's contribution per component
+  std::map<Masks, int> index;
+  std::vector<Masks> order;
+  std::vector<std::vector<std::pair<int, std::pair<double, double>>>> contrib(ncomp);
+  for (int k = 0; k < ncomp; k++) {
+    maxlen = std::max(maxlen, comps[k]->max_len);
+    nin += comps[k]->nterms_in;
+    for (const HostTerm &h : comps[k]->fwd_host) {
+      if (!comps[k]->keep_zero && h.re == 0.0 && h.im == 0.0) continue;  // cancelled in the component
+      Masks m;
+      for (int i = 0; i < 2; i++) {
+        m.n1[i] = h.n1[i];
+        m.n0[i] = h.n0[i];
+        m.fl[i] = h.fl[i];
+        m.sg[i] = h.sg[i];
+      }
+      auto it = index.find(m);
+      int id;
+      if (it == index.end()) {
+        id = (int)order.size();
+        index[m] = id;
+        order.push_back(m);
+      } else {
+        id = it->second;
+      }
+      contrib[k].push_back({id, {h.re, h.im}});
+    }
+  }
+  size_t nu = order.size();
+  std::vector<double> cre((size_t)ncomp * nu, 0.0), cim((size_t)ncomp * nu, 0.0);
+  for (int k = 0; k < ncomp; k++)
+    for (auto &c : contrib[k]) {
+      cre[(size_t)k * nu + c.first] += c.second.first;
+      cim[(size_t)k * nu + c.first] += c.second.second;
+    }
+  std::vector<std::pair<double, double>> vals(nu, {0.0, 0.0});
+  for (int k = 0; k < ncomp; k++) {
+    double pr = coef_re[k], pi = coef_im ? coef_im[k] : 0.0;
+    for (size_t t = 0; t < nu; t++) {
+      double ar = cre[(size_t)k * nu + t], ai = cim[(size_t)k * nu + t];
+      vals[t].first += pr * ar - pi * ai;
+      vals[t].second += pr * ai + pi * ar;
+    }
+  }
+  QG_TRY(make_operator(ctx, nf, nin, maxlen, order, vals, true, out));
+  (*out)->ncomp = ncomp;
+  (*out)->comp_re = std::move(cre);
+  (*out)->comp_im = std::move(cim);
+  return QG_OK;
+}
+
+extern "C" qg_status qg_operator_set_coefficients(qg_operator op, const double *coef_re, const double *coef_im) {
+  if (!op || !coef_re || op->ncomp <= 0) {
+    if (op) op->ctx->last_error = "qg_operator_set_coefficients: not a sum operator";
+    return QG_ERR_ARG;
+  }
+  qg_context ctx = op->ctx;
+  size_t nu = op->fwd_host.size();
+  for (size_t t = 0; t < nu; t++) {
+    double vr = 0.0, vi = 0.0;
+    for (int k = 0; k < op->ncomp; k++) {
+      double pr = coef_re[k], pi = coef_im ? coef_im[k] : 0.0;
+      double ar = op->comp_re[(size_t)k * nu + t], ai = op->comp_im[(size_t)k * nu + t];
+      vr += pr * ar - pi * ai;
+      vi += pr * ai + pi * ar;
+    }
+    op->fwd_host[t].re = vr;
+    op->fwd_host[t].im = vi;
+  }
+  for (HostTerm &h : op->local_off) {
+    h.re = h.sgn * op->fwd_host[h.src].re;
+    h.im = h.sgn * op->fwd_host[h.src].im;
+  }
+  for (HostTerm &h : op->nl_host) {
+    h.re = h.sgn * op->fwd_host[h.src].re;
+    h.im = h.sgn * op->fwd_host[h.src].im;
+  }
+  HostTable *tabs[5] = {&op->pull, &op->pull_off, &op->diag, &op->pull_nl, &op->push};
+  for (HostTable *t : tabs) {
+    if (op->W == 1)
+      QG_TRY(patch_table<1>(ctx, *t, op->fwd_host));
+    else
+      QG_TRY(patch_table<2>(ctx, *t, op->fwd_host));
+  }
+  // Hermiticity of the new values
+  std::vector<Masks> order(nu);
+  std::vector<std::pair<double, double>> vals(nu);
+  for (size_t t = 0; t < nu; t++) {
+    const HostTerm &h = op->fwd_host[t];
+    for (int i = 0; i < 2; i++) {
+      order[t].n1[i] = h.n1[i];
+      order[t].n0[i] = h.n0[i];
+      order[t].fl[i] = h.fl[i];
+      order[t].sg[i] = h.sg[i];
+    }
+    vals[t] = {h.re, h.im};
+  }
+  std::vector<Entry> fwd, pull;
+  forward_and_adjoint(order, vals, false, fwd, pull);
+  op->hermitian = hermitian_of(fwd, pull);
+  op->version++;
   return QG_OK;
 }

@@ -44,6 +44,8 @@ def load(path=LIB_PATH):
         "qg_operator_create": (C.c_int, [P, I32, I32, P, P, P, P, PP]),
         "qg_operator_destroy": (C.c_int, [P]),
         "qg_operator_info": (C.c_int, [P, P, P, P]),
+        "qg_operator_create_sum": (C.c_int, [P, I32, P, P, P, PP]),
+        "qg_operator_set_coefficients": (C.c_int, [P, P, P]),
         "qg_basis_create": (C.c_int, [P, I32, I64, P, PP, P]),
         "qg_basis_destroy": (C.c_int, [P]),
         "qg_basis_size": (I64, [P]),
