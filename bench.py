@@ -230,7 +230,7 @@ def run_reference(args):
     line = {"impl": "reference", "metric": "H·ψ det·terms/s", "value": val, "unit": "Gdet·terms/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
-            "data": "synthetic", "config": {"workload": "anderson_impurity_86so_hpsi", "n_det": n,
+            "data": "synthetic", "config": {"workload": "anderson_impurity_%dso_hpsi" % H.nf, "n_det": n,
                                            "n_terms": op.nterms},
             "cpu_baseline": {"value": val, "unit": "Gdet·terms/s", "cores": O.num_threads(), "kind": "port",
                              "sample": "every %d-th of %d source determinants (%d rows) per step" % (stride, n, S2)},
@@ -246,14 +246,9 @@ def main():
     if args.mode != "hpsi":
         from quanty_gb300 import bench_forms
         return bench_forms.main(args)
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
     import torch
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
+    from quanty_gb300 import replicas
+    world, rank, local = replicas.init("nccl")
     torch.cuda.set_device(local)
     from quanty_gb300 import build
     build.build()
@@ -284,8 +279,7 @@ def main():
     eng.check(eng.L.qg_apply_list_info(eng.ctx, H.handle(), basis.h, C.byref(built), C.byref(nconn)))
     clocks = Clocks(local)
     clocks.start()
-    if dist:
-        dist.barrier()
+    replicas.barrier()
     torch.cuda.synchronize()
     l0 = eng.launches()
     ev0 = torch.cuda.Event(enable_timing=True)
@@ -295,8 +289,7 @@ def main():
         step()
     ev1.record(stream)
     torch.cuda.synchronize()
-    if dist:
-        dist.barrier()
+    replicas.barrier()
     ms = ev0.elapsed_time(ev1) / args.steps
     launches = eng.launches() - l0
     # e2e: the host-buffer entry point, pinned host memory, copies inside the timed region
@@ -311,10 +304,7 @@ def main():
         eng.check(eng.L.qg_apply_host(eng.ctx, H.handle(), basis.h, basis.h, api._ptr(xh), api._ptr(yh), 1))
     e2e_s = (time.perf_counter() - t0) / args.steps
     clk = clocks.stop()
-    t_ms = torch.tensor([ms, e2e_s * 1e3], device="cuda")
-    if dist:
-        dist.all_reduce(t_ms, op=dist.ReduceOp.MAX)
-    ms, e2e_ms = float(t_ms[0]), float(t_ms[1])
+    ms, e2e_ms = replicas.max_over_ranks([ms, e2e_s * 1e3], device="cuda")
     if rank != 0:
         return 0
     # CPU baseline after the GPU timing (its threads would compete with the host-buffer copies)
@@ -330,9 +320,8 @@ def main():
             secondary = xas_spectra_rate(api)
         except Exception as e:  # reported, never fatal to the headline number
             secondary = {"error": str(e)}
-    units = n * nterms * world
-    value = units / (ms * 1e-3) / 1e9
-    e2e_val = units / (e2e_ms * 1e-3) / 1e9
+    value = replicas.aggregate_rate(n * nterms, world, ms * 1e-3) / 1e9
+    e2e_val = replicas.aggregate_rate(n * nterms, world, e2e_ms * 1e-3) / 1e9
     # algorithmic bytes of one H*psi, the survey's per-unit figure: one key, one source
     # amplitude and one result per row, one 16-byte amplitude gather per non-zero connection
     # (no cache reuse credited), the term table once.  The diagonal connection of a row reads
@@ -363,7 +352,7 @@ def main():
         "metric": "H·ψ det·terms/s", "value": value, "unit": "Gdet·terms/s", "n_gpus": world, "steps": args.steps,
         "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "c128", "data": "synthetic",
-        "config": {"workload": "anderson_impurity_86so_hpsi", "n_det": n, "n_terms": nterms, "nnz": nnz,
+        "config": {"workload": "anderson_impurity_%dso_hpsi" % H.nf, "n_det": n, "n_terms": nterms, "nnz": nnz,
                    "nnz_offdiag": nnz_off, "connection_lists": bool(built.value), "nnz_listed": nconn.value,
                    "det_words_bits": 128, "l2": "inputs larger than L2 (x, y %d MB each)" % (n * 16 // 2**20),
                    "setup_s": round(t_setup, 2), "parallelism": "replicas" if world > 1 else "single"},
