@@ -23,6 +23,7 @@
 #include <cub/cub.cuh>
 
 #include <algorithm>
+#include <cstddef>
 #include <cstring>
 #include <map>
 #include <tuple>
@@ -770,6 +771,10 @@ __global__ void __launch_bounds__(256) k_conn(const Key<W> *__restrict__ rows, i
 // (a counting sort in shared memory), so each warp continues 32 rows of about equal length.
 // Each row keeps its accumulator and its order of summation, so the output is bitwise the
 // same; the fused epilogue's dot partials are reduced in the original row order.
+// the list kernel reads (tstart, tend) and (vre, vim) of a LocalEntry as vector loads
+static_assert(sizeof(LocalEntry) == 32 && offsetof(LocalEntry, tend) == 4 && offsetof(LocalEntry, vre) == 16 &&
+                  offsetof(LocalEntry, vim) == 24,
+              "LocalEntry layout");
 #ifndef QG_LIST_REGROUP
 #define QG_LIST_REGROUP 1
 #endif
@@ -817,19 +822,21 @@ __global__ void __launch_bounds__(256, NV == 1 ? QG_APPLY_MIN_BLOCKS : 1)
 #pragma unroll(kLocalUnroll)
       for (uint32_t e = __ldg(lv.eoff + b); e < e1; e++) {
         const LocalEntry *E = lv.ent + e;
+        // (tstart, tend) and (vre, vim) as two vector loads (entries are 32-byte aligned)
+        const uint2 tt = __ldg(reinterpret_cast<const uint2 *>(&E->tstart));
         int64_t j;
-        if (__ldg(&E->tend) >> 31) {
-          j = (int64_t)__ldg(&E->tstart) + off;
+        if (tt.y >> 31) {
+          j = (int64_t)tt.x + off;
         } else {
           uint32_t js = p < pe ? __ldg(&conn[p].x) : QG_NO_INDEX;
           p++;
           if (js == QG_NO_INDEX) continue;
           j = js;
         }
-        double vr = __ldg(&E->vre), vi = __ldg(&E->vim);
-        bool cplx = qg_is_nonzero(vi);
+        const double2 v = __ldg(reinterpret_cast<const double2 *>(&E->vre));
+        bool cplx = qg_is_nonzero(v.y);
 #pragma unroll
-        for (int k = 0; k < NV; k++) qg_cmac(acc[k], vr, vi, cplx, __ldg(x + j * xs + vec0 + k));
+        for (int k = 0; k < NV; k++) qg_cmac(acc[k], v.x, v.y, cplx, __ldg(x + j * xs + vec0 + k));
       }
     }
   }
