@@ -325,3 +325,61 @@ def test_connection_lists_give_the_same_bits(api, model):
     assert torch.equal(out[0][0], out[1][0])
     assert torch.equal(out[0][1], out[1][1])
     assert np.array_equal(out[0][2], out[1][2]) and np.array_equal(out[0][3], out[1][3])
+
+
+def test_host_buffer_entry_point_matches_device_apply(api):
+    """qg_apply_host (the reference's calling convention, psi and Opsi in host memory) gives
+    the device apply's bits: page-locked buffers used in place, pageable ones staged; one and
+    several vectors; on one basis and between bases; an empty source basis gives zeros."""
+    import torch
+    rng = np.random.default_rng(21)
+    nf = 30
+    H = _random_operator(api, nf, 60, 60, rng)
+    T = api.Operator(nf, [([i, (i + 7) % nf | api.CREATION], 0.5 + 0.1j * i) for i in range(nf)])
+    eng = api.engine()
+    b = api.closure(H, api.dets_to_bytes(["1" * 8 + "0" * 22], nf), nf, None, 2)
+    bt = api.OperatorPsiBasis(T, b)
+    for dst, src, op in ((b, b, H), (bt, b, T)):
+        for nvec in (1, 3):
+            X = torch.from_numpy(rng.normal(size=(src.n, nvec)) + 1j * rng.normal(size=(src.n, nvec)))
+            Yd = eng.empty(dst.n, nvec)
+            Xd = X.cuda()
+            eng.check(eng.L.qg_apply(eng.ctx, op.handle(), dst.h, src.h, api._ptr(Xd), api._ptr(Yd), nvec))
+            torch.cuda.synchronize()
+            want = Yd.cpu()
+            for pinned in (True, False):
+                xh = X.clone().pin_memory() if pinned else X.clone()
+                yh = torch.zeros((dst.n, nvec), dtype=torch.complex128)
+                if pinned:
+                    yh = yh.pin_memory()
+                for _ in range(2):  # twice: the staging buffers are reused
+                    eng.check(eng.L.qg_apply_host(eng.ctx, op.handle(), dst.h, src.h, api._ptr(xh), api._ptr(yh),
+                                                  nvec))
+                    assert torch.equal(yh, want), (pinned, nvec, dst is b)
+    empty = api.Basis.from_bytes(nf, np.zeros((0, api.nword(nf)), np.uint8), eng)[0]
+    yh = torch.ones((b.n, 1), dtype=torch.complex128)
+    xh = torch.zeros((1, 1), dtype=torch.complex128)
+    eng.check(eng.L.qg_apply_host(eng.ctx, T.handle(), b.h, empty.h, api._ptr(xh), api._ptr(yh), 1))
+    assert torch.count_nonzero(yh) == 0
+
+
+@pytest.mark.parametrize("complex_values", [False, True])
+def test_fp64_operation_count(api, complex_values):
+    """qg_apply_fp64_ops counts what the list kernel issues: 2 multiplies per row for a real
+    diagonal, 2 FMAs per real connection, 4 per complex one (distinct random actions, no
+    local block decomposition, so connections and list entries coincide)."""
+    import ctypes
+    rng = np.random.default_rng(31)
+    nf = 30
+    H = _random_operator(api, nf, 60, 60, rng, complex_values=complex_values)
+    b = api.closure(H, api.dets_to_bytes(["1" * 8 + "0" * 22], nf), nf, None, 2)
+    eng = api.engine()
+    ops = ctypes.c_int64()
+    eng.check(eng.L.qg_apply_fp64_ops(eng.ctx, H.handle(), b.h, ctypes.byref(ops)))
+    nnz_off = api.count_nnz(H, b, offdiag=True)
+    assert ops.value == 2 * b.n + (4 if complex_values else 2) * nnz_off
+    peak = ctypes.c_double()
+    eng.check(eng.L.qg_fp64_peak(eng.ctx, ctypes.byref(peak)))
+    import torch
+    nominal = 2 * torch.cuda.get_device_properties(0).multi_processor_count * 2.07  # G lane-ops/s at 2.07 GHz
+    assert 0.3 * nominal < peak.value < 1.1 * nominal
