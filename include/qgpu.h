@@ -185,7 +185,7 @@ qg_status qg_hermitian_eigh(int32_t k, const double *a, double *w, double *v, in
  * vector at a time): the first apply of an operator with nvec >= 2 vectors on a basis (as
  * its own source and target, outside stream capture) times each number of vectors handled per
  * kernel pass and keeps the fastest for that (operator, basis, nvec): a thread per row carrying
- * 8, 4, 2 or 1 vectors per pass, or (nvec >= 16) a warp per row with its lanes over 32 or 64
+ * 8, 4, 3, 2 or 1 vectors per pass, or (nvec >= 16) a warp per row with its lanes over 32 or 64
  * vectors per pass (chunk -32, -64).  Every choice sums each vector's connections in the same
  * order, so the result is bitwise the same.  qg_set_autotune(ctx, 0) turns the timing off
  * (passes of 8 vectors); qg_apply_chunk reports the choice in force (0 while none has been

@@ -757,12 +757,25 @@ def CreateSpectra(H, T, psi, options=None, eng=None, batched=True):
         if ub is not None and (method == "dense" or ub.n <= int(o["DenseBorder"])):
             return _spectra_dense(H, Tpsi, e0, o, ub, eng)
     gamma = float(o["Gamma"])
-    groups = [list(range(len(Tpsi)))] if batched else [[i] for i in range(len(Tpsi))]
+    # An empty T psi has a zero spectrum (all coefficients zero) and takes no vector.  Batched,
+    # the other pairs share one multi-vector Lanczos per closed basis: a pair joins a group when
+    # all its determinants lie in the group's basis (the closure of the group's first pair), so
+    # pairs in different symmetry sectors do not run on each other's determinants.
+    live = [i for i in range(len(Tpsi)) if Tpsi[i].N > 0]
+    groups = []
+    if batched:
+        while live:
+            b0 = closure(H, Tpsi[live[0]].det, H.nf, R, -1, eng)
+            members = [i for i in live if i == live[0] or bool(np.all(b0.find(Tpsi[i].det) >= 0))]
+            groups.append((members, b0))
+            live = [i for i in live if i not in members]
+    else:
+        groups = [([i], None) for i in live]
     A = np.zeros((len(Tpsi), ntri + 1))
     B = np.zeros((len(Tpsi), ntri))
-    for grp in groups:
-        seed = np.concatenate([Tpsi[i].det for i in grp])
-        basis = closure(H, seed, H.nf, R, -1, eng)
+    for grp, basis in groups:
+        if basis is None:
+            basis = closure(H, Tpsi[grp[0]].det, H.nf, R, -1, eng)
         x = eng.empty(basis.n, len(grp))
         for c, i in enumerate(grp):
             src, perm = Basis.from_bytes(H.nf, Tpsi[i].det, eng)

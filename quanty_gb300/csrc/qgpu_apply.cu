@@ -1741,9 +1741,10 @@ static void launch_apply_list_t(qg_context ctx, const OpBasisCache *c, const dou
   ctx->launches++;
 }
 
-// Passes of 8, 4, 2 or 1 vectors (at most `chunk` per pass, the same passes as the hash
-// path); all passes of one width run as one launch with a pass per blockIdx.y, so a small
-// basis still spreads its vectors over the SMs.
+// Passes of 8, 4, 3, 2 or 1 vectors (at most `chunk` per pass); all passes of one width run as
+// one launch with a pass per blockIdx.y, so a small basis still spreads its vectors over the
+// SMs.  Three vectors (the x, y, z polarisations) get a width of their own: as 2 + 1 passes
+// each pass would gather 32 or 16 of every 48 bytes of a row.
 template <int W, bool FUSE>
 static void launch_apply_list(qg_context ctx, const OpBasisCache *c, const double2 *diag, qg_basis dst,
                               const double2 *x, int xs, double2 *y, int ys, int nvec, const ApplyFuse &fz,
@@ -1752,12 +1753,14 @@ static void launch_apply_list(qg_context ctx, const OpBasisCache *c, const doubl
   int v = 0;
   while (v < nvec) {
     int left = std::min(nvec - v, chunk);
-    int per = left >= 8 ? 8 : left >= 4 ? 4 : left >= 2 ? 2 : 1;
+    int per = left >= 8 ? 8 : left >= 4 ? 4 : left == 3 ? 3 : left >= 2 ? 2 : 1;
     int np = std::min((nvec - v) / per, 65535);
     if (per == 8)
       launch_apply_list_t<W, 8, FUSE>(ctx, c, diag, dst, x, xs, y, ys, v, np, fz, lv);
     else if (per == 4)
       launch_apply_list_t<W, 4, FUSE>(ctx, c, diag, dst, x, xs, y, ys, v, np, fz, lv);
+    else if (per == 3)
+      launch_apply_list_t<W, 3, FUSE>(ctx, c, diag, dst, x, xs, y, ys, v, np, fz, lv);
     else if (per == 2)
       launch_apply_list_t<W, 2, FUSE>(ctx, c, diag, dst, x, xs, y, ys, v, np, fz, lv);
     else
@@ -1779,7 +1782,7 @@ static qg_status apply_chunked(qg_context ctx, qg_operator op, qg_basis dst, qg_
                                double *y, int ys, int nvec, const ApplyFuse *fz, bool x_packed, int chunk);
 
 // The autotuner: the first multi-vector apply of an operator on a basis (outside stream
-// capture) times one plain apply per candidate number of vectors per pass (8, 4, 2, 1) and
+// capture) times one plain apply per candidate number of vectors per pass (8, 4, 3, 2, 1) and
 // keeps the fastest for that vector count.  The candidates compute bitwise the same result
 // (each vector's sum runs in the same order), so the choice changes only the speed.
 static qg_status autotune(qg_context ctx, qg_operator op, qg_basis b, OpBasisCache *c, const double *x, int xs,
@@ -1797,10 +1800,10 @@ static qg_status autotune(qg_context ctx, qg_operator op, qg_basis b, OpBasisCac
   }
   int best = 8;
   float best_ms = 0;
-  // thread per row with 8, 4, 2 or 1 vectors per pass; warp per row with 32 or 64
-  const int cand[6] = {8, 4, 2, 1, -32, -64};
+  // thread per row with 8, 4, 3, 2 or 1 vectors per pass; warp per row with 32 or 64
+  const int cand[7] = {8, 4, 3, 2, 1, -32, -64};
   qg_status st = QG_OK;
-  for (int i = 0; i < 6 && st == QG_OK; i++) {
+  for (int i = 0; i < 7 && st == QG_OK; i++) {
     int ch = cand[i];
     if (ch > nvec && ch != 8) continue;
     if (ch < 0 && (nvec < 16 || (ch == -64 && nvec <= 32))) continue;
@@ -2057,7 +2060,8 @@ extern "C" qg_status qg_set_autotune(qg_context ctx, int32_t on) {
 
 extern "C" qg_status qg_apply_set_chunk(qg_context ctx, qg_operator op, qg_basis b, int32_t nvec, int32_t chunk) {
   if (!ctx || !op || !b || nvec <= 0) return QG_ERR_ARG;
-  if (!(chunk == 1 || chunk == 2 || chunk == 4 || chunk == 8 || chunk == -32 || chunk == -64)) return QG_ERR_ARG;
+  if (!(chunk == 1 || chunk == 2 || chunk == 3 || chunk == 4 || chunk == 8 || chunk == -32 || chunk == -64))
+    return QG_ERR_ARG;
   qg_status st = QG_OK;
   OpBasisCache *c = qg_basis_cache(b, op, &st);
   if (st != QG_OK) return st;
