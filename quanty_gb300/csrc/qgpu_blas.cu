@@ -41,7 +41,7 @@ qg_status qg_zgemm_ahb(qg_context ctx, const double2 *A, int lda, int ka, const 
     QG_CUDA(ctx, cudaMemsetAsync(C, 0, (size_t)ka * kb * 16, ctx->stream));
     return QG_OK;
   }
-  cublasHandle_t h;
+  cublasHandle_t h = nullptr;
   QG_TRY(blas_handle(ctx, &h));
   const cuDoubleComplex one = make_cuDoubleComplex(1.0, 0.0), zero = make_cuDoubleComplex(0.0, 0.0);
   cublasStatus_t s = cublasZgemm_64(h, CUBLAS_OP_N, CUBLAS_OP_C, kb, ka, n, &one, (const cuDoubleComplex *)B, ldb,
@@ -56,7 +56,7 @@ qg_status qg_zgemm_acc(qg_context ctx, const double2 *A, int lda, int ka, const 
                        int kb, int64_t n, double alpha, double beta) {
   if (kb <= 0 || n <= 0) return QG_OK;
   if (ka <= 0) return beta == 1.0 ? QG_OK : QG_ERR_ARG;  // no terms (the solver never asks to rescale)
-  cublasHandle_t h;
+  cublasHandle_t h = nullptr;
   QG_TRY(blas_handle(ctx, &h));
   const cuDoubleComplex a = make_cuDoubleComplex(alpha, 0.0), b = make_cuDoubleComplex(beta, 0.0);
   cublasStatus_t s;
@@ -75,7 +75,7 @@ qg_status qg_zgemm_combine(qg_context ctx, const double2 *K, int64_t n, int ntri
     QG_CUDA(ctx, cudaMemsetAsync(out, 0, (size_t)n * np * 16, ctx->stream));
     return QG_OK;
   }
-  cublasHandle_t h;
+  cublasHandle_t h = nullptr;
   QG_TRY(blas_handle(ctx, &h));
   const cuDoubleComplex one = make_cuDoubleComplex(1.0, 0.0), zero = make_cuDoubleComplex(0.0, 0.0);
   cublasStatus_t s = cublasZgemm_64(h, CUBLAS_OP_N, CUBLAS_OP_T, np, n, ntri, &one, (const cuDoubleComplex *)C, np,

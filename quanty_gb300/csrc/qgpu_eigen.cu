@@ -377,7 +377,6 @@ extern "C" qg_status qg_block_groundstate(qg_context ctx, qg_operator op, qg_bas
       break;
     }
     int j0 = 0, bs = k;
-    bool invariant = false;
     while (st == QG_OK) {
       // W = H V[:, j0:j0+bs]
       st = qg_apply_strided(ctx, op, b, b, (const double *)(V + j0), K, (double *)W, p, bs, nullptr);
@@ -403,10 +402,7 @@ extern "C" qg_status qg_block_groundstate(qg_context ctx, qg_operator op, qg_bas
         for (int j = 0; j < bs; j++) T[(size_t)(k + i) * K + j0 + j] += R[(size_t)(k + i) * bs + j];
       for (int i = 0; i < k; i++)
         for (int j = 0; j < bs; j++) T[(size_t)i * K + j0 + j] += R[(size_t)i * bs + j];
-      if (kept == 0) {
-        invariant = true;
-        break;
-      }
+      if (kept == 0) break;  // the block Krylov space is invariant: the projection is exact
       j0 = k;
       k += kept;
       bs = kept;
