@@ -669,8 +669,8 @@ def _spectra_tensor(H, Tpsi, E0, o, R, method, eng):
     lo, hi = np.inf, -np.inf
     for c in range(m):
         k = next((q for q in range(1, ntri) if B[c, q] == 0.0), ntri)
-        ev = np.linalg.eigvalsh(np.diag(A[c, 1:k + 1]) + np.diag(B[c, 1:k], 1) + np.diag(B[c, 1:k], -1))
-        lo, hi = min(lo, ev[0] - E0), max(hi, ev[-1] - E0)
+        w0, w1 = _tri_extremes(A[c, 1:k + 1], B[c, 1:k])
+        lo, hi = min(lo, w0 - E0), max(hi, w1 - E0)
     emin, emax, gamma = _default_window(lo, hi, o["Emin"], o["Emax"], gamma, NE)
     D = TriDiagonalMatrixToSpectrum(np.full(Z.shape[1], E0), A, B, emin, emax, NE, gamma, eng)
     G = np.zeros((m * m, NE + 1), dtype=np.complex128)
@@ -731,15 +731,23 @@ def CreateSpectraResident(H, T, basis, X, E0, options=None, eng=None, batched=Tr
 def CreateSpectra(H, T, psi, options=None, eng=None, batched=True):
     """Reference CreateSpectra (LuaInterface/ssp.cpp:1906): spectra of all (T, psi) pairs,
     ordered iT*Npsi + ipsi.  Lanczos branch (:2586-2720): returns (Spectra, [(a, b) shifted by
-    -E0]); batched=True runs all pairs as one multi-vector Lanczos on the union basis.  Dense
-    branch (:2347-2460; Method "Dense", or a union basis within DenseBorder unless Method is
-    "Lanczos"): returns (Spectra, [(poles - E0, weights)])."""
+    -E0]); batched=True runs all pairs as one multi-vector Lanczos with every step on the
+    device.  Dense branch (:2347-2460; Method "Dense", or a union basis within DenseBorder
+    unless Method is "Lanczos"): returns (Spectra, [(poles - E0, weights)])."""
     eng = eng or engine()
     o = _opts(options)
     Ts = T if isinstance(T, (list, tuple)) else [T]
     psis = psi if isinstance(psi, (list, tuple)) else [psi]
     ntri, eps = int(o["NTri"]), float(o["Epsilon"])
     R = parse_restrictions(o.get("Restrictions"))
+    method = str(o.get("Method") or "").lower()
+    gamma = float(o["Gamma"])
+    if batched and not o.get("Tensor") and method != "dense":
+        got = _batched_lanczos_device(H, Ts, psis, o, R, eng)
+        if got is not None:
+            A, B, E0 = got
+            e0 = np.array([E0[i % len(psis)] for i in range(len(Ts) * len(psis))])
+            return _lanczos_spectra(A, B, e0, o, gamma, ntri, eng)
     E0 = [PsiOperatorPsi(H, p, eng).real for p in psis] if o.get("E0") is None else [float(o["E0"])] * len(psis)
     Tpsi = []
     for t in Ts:
@@ -748,7 +756,6 @@ def CreateSpectra(H, T, psi, options=None, eng=None, batched=True):
     e0 = np.array([E0[i % len(psis)] for i in range(len(Tpsi))])
     # dense branch (ssp.cpp:2262-2319): Method "Dense", or the union basis of all T psi closed
     # under H within DenseBorder determinants (unless Method is "Lanczos")
-    method = str(o.get("Method") or "").lower()
     if o.get("Tensor"):
         return _spectra_tensor(H, Tpsi, float(E0[0]), o, R, method, eng)
     if method != "lanczos":
@@ -756,56 +763,118 @@ def CreateSpectra(H, T, psi, options=None, eng=None, batched=True):
         ub = closure(H, seed, H.nf, R, -1, eng) if len(seed) else None
         if ub is not None and (method == "dense" or ub.n <= int(o["DenseBorder"])):
             return _spectra_dense(H, Tpsi, e0, o, ub, eng)
-    gamma = float(o["Gamma"])
-    # An empty T psi has a zero spectrum (all coefficients zero) and takes no vector.  Batched,
-    # the other pairs share one multi-vector Lanczos per closed basis: a pair joins a group when
-    # all its determinants lie in the group's basis (the closure of the group's first pair), so
-    # pairs in different symmetry sectors do not run on each other's determinants.
-    live = [i for i in range(len(Tpsi)) if Tpsi[i].N > 0]
-    groups = []
-    if batched:
-        while live:
-            b0 = closure(H, Tpsi[live[0]].det, H.nf, R, -1, eng)
-            members = [i for i in live if i == live[0] or bool(np.all(b0.find(Tpsi[i].det) >= 0))]
-            groups.append((members, b0))
-            live = [i for i in live if i not in members]
-    else:
-        groups = [([i], None) for i in live]
+    # the plain path: one Lanczos per pair on the closure of its own T psi, as the reference
+    # runs them; an empty T psi has a zero spectrum (all coefficients zero)
     A = np.zeros((len(Tpsi), ntri + 1))
     B = np.zeros((len(Tpsi), ntri))
-    for grp, basis in groups:
-        if basis is None:
-            basis = closure(H, Tpsi[grp[0]].det, H.nf, R, -1, eng)
-        x = eng.empty(basis.n, len(grp))
-        for c, i in enumerate(grp):
-            src, perm = Basis.from_bytes(H.nf, Tpsi[i].det, eng)
-            xs = _upload(eng, src, perm, Tpsi[i].val)
-            col = eng.empty(basis.n)
-            eng.check(eng.L.qg_basis_map(eng.ctx, src.h, _ptr(xs), basis.h, _ptr(col), 1))
-            with eng.on_stream():
-                x[:, c] = col[:, 0]
-        with eng.on_stream():
-            x = x.contiguous()
+    for i in range(len(Tpsi)):
+        if Tpsi[i].N == 0:
+            continue
+        basis = closure(H, Tpsi[i].det, H.nf, R, -1, eng)
+        src, perm = Basis.from_bytes(H.nf, Tpsi[i].det, eng)
+        xs = _upload(eng, src, perm, Tpsi[i].val)
+        x = eng.empty(basis.n)
+        eng.check(eng.L.qg_basis_map(eng.ctx, src.h, _ptr(xs), basis.h, _ptr(x), 1))
         a, b = lanczos_block(H, basis, x, ntri, eps, max(gamma, eps), eng)
-        A[grp] = a
-        B[grp] = b
-    # pole range from the eigenvalues of every tridiagonal matrix, and from it the default
-    # Emin/Emax/Gamma (ssp.cpp:2651-2684)
+        A[i] = a[0]
+        B[i] = b[0]
+    return _lanczos_spectra(A, B, e0, o, gamma, ntri, eng)
+
+
+def _batched_lanczos_device(H, Ts, psis, o, R, eng):
+    """The batched Lanczos branch with every step on the device: the initial states on one
+    basis, their energies as one multi-vector expectation value, each T applied to all of them
+    at once straight into the final basis (the closure under H of every T's targets, within
+    the restrictions), the empty (T, psi) pairs left out, one multi-vector Lanczos for the
+    rest.  Returns (A, B, E0), or None when the dense branch applies (a final basis within
+    DenseBorder and Method not "Lanczos")."""
+    torch = eng.torch
+    nf, npsi = H.nf, len(psis)
+    ntri, eps, gamma = int(o["NTri"]), float(o["Epsilon"]), float(o["Gamma"])
+    method = str(o.get("Method") or "").lower()
+    dets = np.concatenate([p.det for p in psis])
+    b0, perm = Basis.from_bytes(nf, dets, eng)
+    X = np.zeros((max(b0.n, 1), npsi), dtype=np.complex128)
+    off = 0
+    for j, p in enumerate(psis):
+        np.add.at(X[:, j], perm[off:off + p.N], np.asarray(p.val, dtype=np.complex128))
+        off += p.N
+    with eng.on_stream():
+        Xd = torch.from_numpy(X).to("cuda:%d" % eng.device)
+    if o.get("E0") is None:
+        out = np.zeros(2 * npsi)
+        eng.check(eng.L.qg_expectation(eng.ctx, H.handle(eng), b0.h, _ptr(Xd), npsi, _ptr(out)))
+        E0 = [float(out[2 * j]) for j in range(npsi)]
+    else:
+        E0 = [float(o["E0"])] * npsi
+    bt = None
+    for t in Ts:
+        tb = OperatorPsiBasis(t, b0, R, eng)
+        bt = tb if bt is None else basis_union(bt, tb, eng)
+    bf = closure_of(H, bt, R, -1, eng)
+    if method != "lanczos" and 0 < bf.n <= int(o["DenseBorder"]):
+        return None
+    nvec = len(Ts) * npsi
+    A = np.zeros((nvec, ntri + 1))
+    B = np.zeros((nvec, ntri))
+    if bf.n == 0:
+        return A, B, E0
+    Y = eng.empty(bf.n, nvec)
+    for j, t in enumerate(Ts):
+        yj = eng.empty(bf.n, npsi)
+        eng.check(eng.L.qg_apply(eng.ctx, t.handle(eng), bf.h, b0.h, _ptr(Xd), _ptr(yj), npsi))
+        with eng.on_stream():
+            Y[:, j * npsi:(j + 1) * npsi] = yj
+    norms = np.zeros(nvec)
+    eng.check(eng.L.qg_norm(eng.ctx, bf.n, nvec, _ptr(Y), _ptr(norms)))
+    live = [i for i in range(nvec) if norms[i] > 0.0]
+    if live:
+        with eng.on_stream():
+            x = Y[:, live].contiguous()
+        a, b = lanczos_block(H, bf, x, ntri, eps, max(gamma, eps), eng)
+        A[live] = a
+        B[live] = b
+    return A, B, E0
+
+
+def _lanczos_spectra(A, B, e0, o, gamma, ntri, eng):
+    """Spectra of the Lanczos branch from the coefficients: pole range from the extreme
+    eigenvalues of every tridiagonal matrix, the default Emin/Emax/Gamma from it
+    (ssp.cpp:2651-2684), all spectra at all frequencies in one kernel."""
     lo, hi = np.inf, -np.inf
-    for s in range(len(Tpsi)):
+    for s in range(A.shape[0]):
         m = ntri
         for k in range(1, ntri):  # a chain that ended early (b = 0) is shorter
             if B[s, k] == 0.0:
                 m = k
                 break
-        Tm = np.diag(A[s, 1:m + 1]) + np.diag(B[s, 1:m], 1) + np.diag(B[s, 1:m], -1)
-        w = np.linalg.eigvalsh(Tm)
-        lo, hi = min(lo, w[0] - e0[s]), max(hi, w[-1] - e0[s])
+        w0, w1 = _tri_extremes(A[s, 1:m + 1], B[s, 1:m])
+        lo, hi = min(lo, w0 - e0[s]), max(hi, w1 - e0[s])
     emin, emax, NE = o["Emin"], o["Emax"], int(o["NE"])
     emin, emax, gamma = _default_window(lo, hi, emin, emax, gamma, NE)
     G = TriDiagonalMatrixToSpectrum(e0, A, B, emin, emax, NE, gamma, eng)
-    tri = [(np.r_[0.0, A[s, 1:] - e0[s]], B[s].copy()) for s in range(len(Tpsi))]
+    tri = [(np.r_[0.0, A[s, 1:] - e0[s]], B[s].copy()) for s in range(A.shape[0])]
     return Spectra(G, emin, emax, NE, gamma, lo, hi), tri
+
+
+def _tri_extremes(a, b):
+    """Lowest and highest eigenvalue of the symmetric tridiagonal matrix with diagonal a and
+    off-diagonal b, as CreateSpectra takes them for the pole range (LuaInterface/ssp.cpp:2651-2663,
+    TriDiagonalMatrixToEigenvalues, Core/BasicMath/BasicMath_MatrixTypeConversion.cpp:1538):
+    LAPACK bisection for the two wanted eigenvalues, O(m) each, not a dense eigensolve."""
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    m = len(a)
+    if m == 1:
+        return float(a[0]), float(a[0])
+    try:
+        from scipy.linalg import eigvalsh_tridiagonal
+        lo = eigvalsh_tridiagonal(a, b, select="i", select_range=(0, 0))[0]
+        hi = eigvalsh_tridiagonal(a, b, select="i", select_range=(m - 1, m - 1))[0]
+        return float(lo), float(hi)
+    except ImportError:
+        w = np.linalg.eigvalsh(np.diag(a) + np.diag(b, 1) + np.diag(b, -1))
+        return float(w[0]), float(w[-1])
 
 
 def _default_window(lo, hi, emin, emax, gamma, NE):
