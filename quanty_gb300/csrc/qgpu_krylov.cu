@@ -267,23 +267,54 @@ __global__ void k_lanczos_axpy_norm_flat(int64_t len, int nvec, const double2 *_
   }
 }
 
+// Sum of the .x parts of vector k's partials, in a fixed order: with at least as many vectors
+// as warps, or few partials, a warp per vector (lanes over the partials, a shuffle tree);
+// otherwise (few vectors over many partials) the whole block per vector (threads over the
+// partials, shuffles, then the warps' sums in order).  Returns the sum on lane 0 (warp form)
+// or thread 0 (block form).
+__device__ __forceinline__ bool fin_warp_form(int nvec, int nblk) {
+  return nvec >= (int)(blockDim.x >> 5) || nblk <= 2048;
+}
+
+__device__ double fin_sum_block(const double2 *part, int nblk, int nvec, int k, double *sh) {
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  double s = 0;
+  for (int b = threadIdx.x; b < nblk; b += blockDim.x) s += part[b * nvec + k].x;
+  for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) sh[wid] = s;
+  __syncthreads();
+  double t = 0;
+  if (threadIdx.x == 0)
+    for (int w = 0; w < nw; w++) t += sh[w];
+  __syncthreads();
+  return t;
+}
+
+__device__ __forceinline__ double fin_sum_warp(const double2 *part, int nblk, int nvec, int k) {
+  int lane = threadIdx.x & 31;
+  double s = 0;
+  for (int b = lane; b < nblk; b += 32) s += part[b * nvec + k].x;
+  for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  return s;
+}
+
 // a[k] <- Re(sum of dot partials); also stores a into the history
 __global__ void k_fin_a(const double2 *part, int nblk, int nvec, double *a_now, double *a_hist, int stride, int col) {
   __shared__ double sh[32];
-  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  for (int k = 0; k < nvec; k++) {
-    double s = 0;
-    for (int b = threadIdx.x; b < nblk; b += blockDim.x) s += part[b * nvec + k].x;
-    for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if (lane == 0) sh[wid] = s;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      double t = 0;
-      for (int w = 0; w < nw; w++) t += sh[w];
-      a_now[k] = t;
-      a_hist[k * stride + col] = t;
+  auto store = [&](int k, double t) {
+    a_now[k] = t;
+    a_hist[k * stride + col] = t;
+  };
+  if (fin_warp_form(nvec, nblk)) {
+    for (int k = threadIdx.x >> 5; k < nvec; k += blockDim.x >> 5) {
+      double t = fin_sum_warp(part, nblk, nvec, k);
+      if ((threadIdx.x & 31) == 0) store(k, t);
     }
-    __syncthreads();
+  } else {
+    for (int k = 0; k < nvec; k++) {
+      double t = fin_sum_block(part, nblk, nvec, k, sh);
+      if (threadIdx.x == 0) store(k, t);
+    }
   }
 }
 
@@ -292,27 +323,27 @@ __global__ void k_fin_a(const double2 *part, int nblk, int nvec, double *a_now, 
 __global__ void k_fin_b(const double2 *part, int nblk, int nvec, double *b_now, double *b_hist, int stride, int col,
                         double *scale, double *thr2, double *err, double eps, double gamma, int first) {
   __shared__ double sh[32];
-  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  for (int k = 0; k < nvec; k++) {
-    double s = 0;
-    for (int b = threadIdx.x; b < nblk; b += blockDim.x) s += part[b * nvec + k].x;
-    for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if (lane == 0) sh[wid] = s;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      double t = 0;
-      for (int w = 0; w < nw; w++) t += sh[w];
-      double b = sqrt(t);
-      b_now[k] = b;
-      b_hist[k * stride + col] = b;
-      scale[k] = (b > 0.0) ? 1.0 / b : 0.0;
-      double e = first ? 1.0 : err[k];
-      double th = eps / e;
-      thr2[k] = th * th;
-      if (!first) err[k] = e * (b * b / (b * b + 4 * gamma * gamma));
-      else err[k] = 1.0;
+  auto store = [&](int k, double t) {
+    double b = sqrt(t);
+    b_now[k] = b;
+    b_hist[k * stride + col] = b;
+    scale[k] = (b > 0.0) ? 1.0 / b : 0.0;
+    double e = first ? 1.0 : err[k];
+    double th = eps / e;
+    thr2[k] = th * th;
+    if (!first) err[k] = e * (b * b / (b * b + 4 * gamma * gamma));
+    else err[k] = 1.0;
+  };
+  if (fin_warp_form(nvec, nblk)) {
+    for (int k = threadIdx.x >> 5; k < nvec; k += blockDim.x >> 5) {
+      double t = fin_sum_warp(part, nblk, nvec, k);
+      if ((threadIdx.x & 31) == 0) store(k, t);
     }
-    __syncthreads();
+  } else {
+    for (int k = 0; k < nvec; k++) {
+      double t = fin_sum_block(part, nblk, nvec, k, sh);
+      if (threadIdx.x == 0) store(k, t);
+    }
   }
 }
 
