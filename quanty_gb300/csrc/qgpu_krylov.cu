@@ -298,9 +298,12 @@ __device__ __forceinline__ double fin_sum_warp(const double2 *part, int nblk, in
   return s;
 }
 
-// a[k] <- Re(sum of dot partials); also stores a into the history
-__global__ void k_fin_a(const double2 *part, int nblk, int nvec, double *a_now, double *a_hist, int stride, int col) {
+// a[k] <- Re(sum of dot partials); also stores a into the history at column *step + 1 and
+// then advances the device step counter (so a captured step can be replayed)
+__global__ void k_fin_a(const double2 *part, int nblk, int nvec, double *a_now, double *a_hist, int stride,
+                        int *step) {
   __shared__ double sh[32];
+  const int col = *step + 1;
   auto store = [&](int k, double t) {
     a_now[k] = t;
     a_hist[k * stride + col] = t;
@@ -316,13 +319,18 @@ __global__ void k_fin_a(const double2 *part, int nblk, int nvec, double *a_now, 
       if (threadIdx.x == 0) store(k, t);
     }
   }
+  __syncthreads();  // every thread has read the counter
+  if (threadIdx.x == 0) *step = col;
 }
 
-// b = sqrt(sum of norm partials); scale = 1/b (0 for an empty vector); truncation threshold
-// (eps/err)^2 with the err before this step's update; err *= b^2/(b^2+4 gamma^2)
-__global__ void k_fin_b(const double2 *part, int nblk, int nvec, double *b_now, double *b_hist, int stride, int col,
-                        double *scale, double *thr2, double *err, double eps, double gamma, int first) {
+// b = sqrt(sum of norm partials) into the history at column *step; scale = 1/b (0 for an empty
+// vector); truncation threshold (eps/err)^2 with the err before this step's update;
+// err *= b^2/(b^2+4 gamma^2)
+__global__ void k_fin_b(const double2 *part, int nblk, int nvec, double *b_now, double *b_hist, int stride,
+                        const int *step, double *scale, double *thr2, double *err, double eps, double gamma,
+                        int first) {
   __shared__ double sh[32];
+  const int col = *step;
   auto store = [&](int k, double t) {
     double b = sqrt(t);
     b_now[k] = b;
@@ -404,7 +412,8 @@ extern "C" qg_status qg_lanczos_tridiag(qg_context ctx, qg_operator op, qg_basis
   ALLOC(zero, vb);
   ALLOC(npart, (size_t)P * nvec * 16);
   ALLOC(dpart, (size_t)Papply * nvec * 16);
-  size_t nscal = 6 * (size_t)nvec + (size_t)nvec * (ntri + 1) + (size_t)nvec * ntri;
+  // the scalars, then one slot for the device step counter (zeroed with them)
+  size_t nscal = 6 * (size_t)nvec + (size_t)nvec * (ntri + 1) + (size_t)nvec * ntri + 1;
   ALLOC(scal, nscal * 8);
 #undef ALLOC
   if (e != cudaSuccess) {
@@ -416,6 +425,7 @@ extern "C" qg_status qg_lanczos_tridiag(qg_context ctx, qg_operator op, qg_basis
   double *a_now = scal, *b_now = scal + nvec, *scale = scal + 2 * nvec, *thr2 = scal + 3 * nvec,
          *err = scal + 4 * nvec, *zb = scal + 5 * nvec;
   double *a_hist = scal + 6 * nvec, *b_hist = a_hist + (size_t)nvec * (ntri + 1);
+  int *step_ctr = reinterpret_cast<int *>(scal + nscal - 1);
   qg_status st = QG_OK;
   k_zero<<<(unsigned)((nscal + 255) / 256), 256, 0, s>>>(scal, (int64_t)nscal);
   ctx->launches++;
@@ -441,7 +451,7 @@ extern "C" qg_status qg_lanczos_tridiag(qg_context ctx, qg_operator op, qg_basis
   };
   // step 0: b0 = |v0|, scale, threshold eps (err = 1)
   launch_dot_partial(P, n, nvec, (const double2 *)v0_dev, nullptr, npart, s);
-  k_fin_b<<<1, 256, 0, s>>>(npart, P, nvec, b_now, b_hist, ntri, 0, scale, thr2, err, eps, gamma, 1);
+  k_fin_b<<<1, 256, 0, s>>>(npart, P, nvec, b_now, b_hist, ntri, step_ctr, scale, thr2, err, eps, gamma, 1);
   ctx->launches += 2;
   st = qg_check_launch(ctx, "lanczos start norm");
   ApplyFuse fz;
@@ -454,11 +464,10 @@ extern "C" qg_status qg_lanczos_tridiag(qg_context ctx, qg_operator op, qg_basis
   if (st == QG_OK && krylov_dev)
     e = cudaMemcpyAsync(krylov_dev, vc, len * 16, cudaMemcpyDeviceToDevice, s);
   if (st == QG_OK) {
-    k_fin_a<<<1, 256, 0, s>>>(dpart, Papply, nvec, a_now, a_hist, ntri + 1, 1);
+    k_fin_a<<<1, 256, 0, s>>>(dpart, Papply, nvec, a_now, a_hist, ntri + 1, step_ctr);
     ctx->launches++;
   }
-  // steps 1 .. ntri-1: every scalar stays on the device, so the whole sequence is captured
-  // into one CUDA graph and launched once (falling back to direct launches if capture fails)
+  // one step: every scalar stays on the device
   auto step = [&](int i) -> qg_status {
     std::swap(vp, vc);  // vp = v_{i-1}
     int T = nvec > 1 ? flat_threads(nvec) : 0;
@@ -466,7 +475,7 @@ extern "C" qg_status qg_lanczos_tridiag(qg_context ctx, qg_operator op, qg_basis
       k_lanczos_axpy_norm_flat<<<P, T, T * sizeof(double2), s>>>(len, nvec, w, vp, a_now, vraw, npart);
     else
       k_lanczos_axpy_norm<<<P, RBLK, (RBLK / 32) * sizeof(double2), s>>>(n, nvec, w, vp, a_now, vraw, npart);
-    k_fin_b<<<1, 256, 0, s>>>(npart, P, nvec, b_now, b_hist, ntri, i, scale, thr2, err, eps, gamma, 0);
+    k_fin_b<<<1, 256, 0, s>>>(npart, P, nvec, b_now, b_hist, ntri, step_ctr, scale, thr2, err, eps, gamma, 0);
     ctx->launches += 2;
     qg_status sst = normalise(vraw);
     if (sst != QG_OK) return sst;
@@ -478,10 +487,15 @@ extern "C" qg_status qg_lanczos_tridiag(qg_context ctx, qg_operator op, qg_basis
       cudaError_t ce = cudaMemcpyAsync(krylov_dev + 2 * (size_t)i * len, vc, len * 16, cudaMemcpyDeviceToDevice, s);
       if (ce != cudaSuccess) return qg_cuda_fail(ctx, ce, "krylov copy");
     }
-    k_fin_a<<<1, 256, 0, s>>>(dpart, Papply, nvec, a_now, a_hist, ntri + 1, i + 1);
+    k_fin_a<<<1, 256, 0, s>>>(dpart, Papply, nvec, a_now, a_hist, ntri + 1, step_ctr);
     ctx->launches++;
     return sst;
   };
+  // Steps 1 .. ntri-1 as CUDA graphs.  The buffer roles repeat every two steps and the step's
+  // column comes from the device counter, so without stored Krylov vectors two steps are
+  // captured once and replayed (ntri-1)/2 times (an odd last step runs directly); with stored
+  // Krylov vectors, whose copy offset depends on the step, the whole sequence is captured.
+  // If capture fails, the steps run as direct launches.
   bool graphed = false;
   if (st == QG_OK && e == cudaSuccess && ntri > 2 && ctx->use_graphs) {
     double2 *sv[6] = {vp, vc, w, w2, vraw, zero};
@@ -489,19 +503,28 @@ extern "C" qg_status qg_lanczos_tridiag(qg_context ctx, qg_operator op, qg_basis
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     qg_status cst = QG_OK;
+    const int span = krylov_dev ? ntri - 1 : 2;
     if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
-      for (int i = 1; i < ntri && cst == QG_OK; i++) cst = step(i);
+      for (int i = 1; i <= span && cst == QG_OK; i++) cst = step(i);
       cudaError_t ee = cudaStreamEndCapture(s, &graph);
-      if (ee == cudaSuccess && cst == QG_OK && cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess &&
-          cudaGraphLaunch(exec, s) == cudaSuccess) {
-        graphed = true;
+      if (ee == cudaSuccess && cst == QG_OK && cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess) graphed = true;
+    }
+    if (graphed) {
+      const int reps = krylov_dev ? 1 : (ntri - 1) / 2;
+      const int64_t per = ctx->launches - l0;  // kernels of one replay, counted while capturing
+      for (int r = 0; r < reps && st == QG_OK; r++) {
+        cudaError_t le = cudaGraphLaunch(exec, s);
+        if (le != cudaSuccess) st = qg_cuda_fail(ctx, le, "lanczos graph launch");
       }
+      ctx->launches = l0 + per * reps;
+      // the buffer roles are those before step 1 again, as for every odd step
+      if (st == QG_OK && !krylov_dev && (ntri - 1) % 2) st = step(ntri - 1);
     }
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
     if (!graphed) {
       cudaGetLastError();
-      // restore the buffer roles and redo the steps directly
+      // nothing captured ran: restore the buffer roles and run the steps directly
       vp = sv[0];
       vc = sv[1];
       w = sv[2];
