@@ -169,3 +169,24 @@ def test_poles_kernel_matches_oracle(api, oracle_mod):
     for s in range(ns):
         want = oracle_mod.poles_spectrum(a[s], b[s], e0[s], -9.0, 20.0 / ne, ne, 0.42)
         assert spec_err(G[s], want) < 1e-13
+
+
+def test_lanczos_with_stored_krylov_vectors(api):
+    """qg_lanczos_tridiag with krylov_dev: the coefficients are bitwise those of the run that
+    keeps no vectors (the same kernels; that run replays a two-step graph, this one captures
+    every step), and the stored vectors start orthonormal."""
+    import torch
+    from quanty_gb300 import workloads
+    eng = api.engine()
+    H, R, s0, info = workloads.anderson_impurity(nshell=2, hole_max=2, particle_max=2)
+    b = api.closure(H, api.dets_to_bytes([s0], H.nf), H.nf, R)
+    rng = np.random.default_rng(41)
+    x = torch.from_numpy(rng.normal(size=(b.n, 1)) + 1j * rng.normal(size=(b.n, 1))).cuda()
+    ntri = 25
+    a0, b0 = api.lanczos_block(H, b, x.clone(), ntri, 0.0, 0.0, eng)
+    K = torch.zeros((ntri, b.n), dtype=torch.complex128, device="cuda")
+    a1, b1 = api.lanczos_block(H, b, x.clone(), ntri, 0.0, 0.0, eng, krylov=K)
+    assert np.array_equal(a0, a1) and np.array_equal(b0, b1)
+    torch.cuda.synchronize()
+    G = (K[:6].conj() @ K[:6].T).cpu().numpy()
+    assert np.max(np.abs(G - np.eye(6))) < 1e-10
