@@ -49,3 +49,22 @@ def test_complex_wavefunction_text():
     assert '{"0011",-1.0000000000000000E+00 + I *  0.0000000000000000E+00}' in t
     back = api.Wavefunction.from_put(t)
     assert np.array_equal(back.val, psi.val) and back.dets() == psi.dets()
+
+
+def test_pole_range_extremes_match_dense_eigenvalues():
+    """The pole range of CreateSpectra takes the extreme eigenvalues of each tridiagonal matrix
+    by bisection; they equal a dense eigensolve's to rounding, including chains of length one
+    and two and matrices with repeated or tiny off-diagonal entries."""
+    from quanty_gb300.api import _tri_extremes
+    rng = np.random.default_rng(5)
+    cases = [(rng.normal(size=m), rng.normal(size=m - 1)) for m in (1, 2, 3, 17, 200)]
+    cases.append((np.full(50, 2.0), np.full(49, 1e-12)))
+    cases.append((np.linspace(-3, 3, 40), np.ones(39)))
+    for a, b in cases:
+        lo, hi = _tri_extremes(a, b)
+        if len(a) == 1:
+            w = a
+        else:
+            w = np.linalg.eigvalsh(np.diag(a) + np.diag(b, 1) + np.diag(b, -1))
+        scale = max(1.0, float(np.max(np.abs(w))))
+        assert abs(lo - w[0]) <= 1e-12 * scale and abs(hi - w[-1]) <= 1e-12 * scale
