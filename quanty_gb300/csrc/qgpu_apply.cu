@@ -1478,6 +1478,13 @@ __global__ void k_term_coef(const TermDev<W> *__restrict__ terms, int nterms, do
 // entries, window bits, connection lists -- stays.
 static qg_status refresh_values(qg_basis b, qg_operator op, OpBasisCache &c) {
   qg_context ctx = b->ctx;
+  // the refresh must run now, not be recorded into a graph being captured
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(ctx->stream, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) {
+    cudaGetLastError();
+    ctx->last_error = "a rescaled operator was first used on this basis under stream capture";
+    return QG_ERR_ARG;
+  }
   if (b->n) launch_diag(ctx, op, b, c.d_diag);
   if (op->H > 0) QG_TRY(refresh_local(b, op, c));
   if (c.conn_state == 1) {
