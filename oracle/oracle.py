@@ -260,6 +260,128 @@ def resonant_spectra(H1, H2, T1, T2s, psi, o):
     return G
 
 
+def _auto_range(emin, emax, ne, gamma, lo_ev, hi_ev, e_lo, e_hi):
+    """Energy-range defaults of the dense RIXS branch (Core/ResonantSpectra.cpp:472-535):
+    unset Emin/Emax (None) from the extreme eigenvalues, then NE and Gamma."""
+    if emin is None and emax is None:
+        emin = 1.1 * lo_ev - 0.1 * hi_ev - e_hi
+        emax = 1.1 * hi_ev - 0.1 * lo_ev - e_lo
+    if emin is None:
+        emin = 1.1 * lo_ev - 0.1 * emax - e_hi
+    if emax is None:
+        emax = 1.1 * hi_ev - 0.1 * emin - e_lo
+    if gamma == 0 and ne == 0:
+        ne = 1000
+        gamma = 5 * (emax - emin) / ne
+    if ne == 0:
+        ne = int(5 * (emax - emin) / gamma)
+    if gamma == 0:
+        gamma = 5 * (emax - emin) / ne
+    return emin, emax, ne, gamma
+
+
+def _on_basis(wf, index, n):
+    v = np.zeros(n, dtype=np.complex128)
+    for r, x in zip(wf.det, wf.val):
+        v[index[bytes(r)]] += x
+    return v
+
+
+def resonant_spectra_dense(H1, H2, T1s, T2s, psis, o, tensor=False, krylov_layout=False):
+    """Reference dense RIXS, ResonantSpectraDense and ResonantSpectraDenseTensor
+    (Core/ResonantSpectra.cpp:290-663, :665-1073), on the bases LuaCreateResonantSpectra builds
+    for them (LuaInterface/ssp.cpp:3300-3371): the union of the initial states, the targets of
+    every T1, their closure under H1; the targets of every T2 from there, their closure under H2.
+
+    Intermediate eigenpairs (E_m, |m>), final (E_f, |f>), A[m, j] = <m|T1 psi_j> with
+    j = iT1 + NT1 ipsi, B_k[f, m] = <f|T2_k|m>; per incident energy w_l the amplitudes
+    D_k = B_k (A / (w_l - E_m + E1_psi + i Gamma1/2)).  Non-tensor spectrum l + (NE1+1)(k + NT2 j):
+    sum_f |D_k[f, j]|^2 / (w - E_f + E2_psi + i Gamma2/2).  Tensor spectrum
+    l + (NE1+1)(j2 + NT2(i1 + NT1(n2 + NT2(m1 + NT1(r + Npsi s))))):
+    sum_f conj(D_n2[f, m1 + NT1 s]) D_j2[f, i1 + NT1 r] / (w - E_f + E2_psi0 + i Gamma2/2).
+    krylov_layout gives the index order and energy shifts of the Krylov tensor branch
+    (ResonantSpectraTensor, Core/ResonantSpectra.cpp:1204-1686: the left vector carries psi r,
+    the right psi s, both shifts from psi 0), which it equals once its Krylov spaces are complete.
+    o holds Emin1..Gamma2 (None / 0 for automatic), E0_1, E0_2 (None: <psi|H|psi>/<psi|psi>),
+    Restrictions1/2.  Returns (G [nspec, NE2+1], settings)."""
+    nf = psis[0].nf
+    R1, R2 = o.get("Restrictions1"), o.get("Restrictions2")
+    npsi, nt1, nt2 = len(psis), len(T1s), len(T2s)
+    u = linear_combination(nf, psis, [1.0] * npsi)
+    seed1 = linear_combination(nf, [operator_psi(T, u, R1) for T in T1s], [1.0] * nt1)
+    b1 = closure(H1, seed1, R1)
+    n1 = len(b1.val)
+    idx1 = {bytes(r): i for i, r in enumerate(b1.det)}
+    seed2 = linear_combination(nf, [operator_psi(T, b1, R2) for T in T2s], [1.0] * nt2)
+    b2 = closure(H2, seed2, R2)
+    n2 = len(b2.val)
+    idx2 = {bytes(r): i for i, r in enumerate(b2.det)}
+
+    def energies(H, key):
+        if o.get(key) is not None:
+            return np.full(npsi, float(o[key]))
+        out = []
+        for p in psis:
+            nn = float(np.real(np.vdot(p.val, p.val)))
+            out.append(expectation(H, p).real / (nn if nn > np.finfo(float).eps else 1.0))
+        return np.array(out)
+
+    e1, e2 = energies(H1, "E0_1"), energies(H2, "E0_2")
+    if krylov_layout:
+        e1[:], e2[:] = e1[0], e2[0]
+    X = np.zeros((n1, npsi * nt1), dtype=np.complex128)
+    for ip, p in enumerate(psis):
+        for it, T in enumerate(T1s):
+            X[:, it + nt1 * ip] = _on_basis(operator_psi(T, p, R1), idx1, n1)
+    w1, V1 = np.linalg.eigh(dense_matrix(H1, b1)) if n1 else (np.zeros(0), np.zeros((0, 0)))
+    w2, V2 = np.linalg.eigh(dense_matrix(H2, b2)) if n2 else (np.zeros(0), np.zeros((0, 0)))
+    A = V1.conj().T @ X
+    B = []
+    for T in T2s:
+        M = np.zeros((n2, n1), dtype=np.complex128)
+        for c in range(n1):
+            e = np.zeros(n1)
+            e[c] = 1.0
+            M[:, c] = _on_basis(operator_psi(T, WF(nf, b1.det, e), R2), idx2, n2)
+        B.append(V2.conj().T @ M @ V1)
+    emin1, emax1, ne1, g1 = _auto_range(o.get("Emin1"), o.get("Emax1"), o.get("NE1", 1000), o.get("Gamma1", 0.0),
+                                        w1[0], w1[-1], e1.min(), e1.max())
+    emin2, emax2, ne2, g2 = _auto_range(o.get("Emin2"), o.get("Emax2"), o.get("NE2", 1000), o.get("Gamma2", 0.0),
+                                        w2[0] if n2 else 0.0, w2[-1] if n2 else 0.0, e2.min(), e2.max())
+    np1 = ne1 + 1
+    wl = np.array([emin2 + (m / ne2) * (emax2 - emin2) for m in range(ne2 + 1)])
+    M1 = npsi * nt1
+    nspec = (M1 * nt2) ** 2 * np1 if tensor else M1 * nt2 * np1
+    G = np.zeros((nspec, ne2 + 1), dtype=np.complex128)
+    psi_of = np.arange(M1) // nt1
+    for l in range(np1):
+        wres = emin1 + (emax1 - emin1) * l / ne1
+        Cm = A / (wres - w1[:, None] + e1[psi_of][None, :] + 0.5j * g1)
+        D = [Bk @ Cm for Bk in B]
+        if not tensor:
+            for k in range(nt2):
+                for j in range(M1):
+                    lor = 1.0 / (wl[:, None] - w2[None, :] + e2[psi_of[j]] + 0.5j * g2)
+                    G[l + np1 * (k + nt2 * j)] = lor @ (np.abs(D[k][:, j]) ** 2)
+            continue
+        lor = 1.0 / (wl[:, None] - w2[None, :] + e2[0] + 0.5j * g2)
+        for r in range(npsi):
+            for s_ in range(npsi):
+                for i1 in range(nt1):
+                    for j2 in range(nt2):
+                        for m1 in range(nt1):
+                            for n2_ in range(nt2):
+                                t = l + np1 * (j2 + nt2 * (i1 + nt1 * (n2_ + nt2 * (m1 + nt1 * (r + npsi * s_)))))
+                                if krylov_layout:
+                                    left, right = D[n2_][:, m1 + nt1 * r], D[j2][:, i1 + nt1 * s_]
+                                else:
+                                    left, right = D[n2_][:, m1 + nt1 * s_], D[j2][:, i1 + nt1 * r]
+                                G[t] = lor @ (np.conj(left) * right)
+    st = {"emin1": emin1, "emax1": emax1, "ne1": ne1, "gamma1": g1,
+          "emin2": emin2, "emax2": emax2, "ne2": ne2, "gamma2": g2, "n1": n1, "n2": n2}
+    return G, st
+
+
 def cf_spectrum(a, b, e0, emin, de, ne, gamma):
     """Continued fraction on NE+1 points (reference TriDiagonalMatrixToSpectrum)."""
     a = np.ascontiguousarray(a, dtype=np.float64)

@@ -280,9 +280,23 @@ def gen_tensor():
     save("tensor.json", out)
 
 
+def gen_rixs():
+    """CreateResonantSpectra of the reference: dense branch (lists of T1, T2 and psi, automatic
+    energy ranges, tensor form) and Krylov branch (lists, tensor form)."""
+    work = run(open(os.path.join(HERE, "gen", "rixs.lua")).read(), "rixs.lua")
+    out = {"source": "tests/golden/gen/rixs.lua", "psi": [wf(work, "psi1"), wf(work, "psi2")],
+           "opts": {"Emin1": -5, "Emax1": 15, "NE1": 4, "Gamma1": 0.8, "Emin2": -2, "Emax2": 8, "NE2": 64,
+                    "Gamma2": 0.3}}
+    for n in ("H", "HX", "Tx", "Ty", "Txd", "Tyd", "Tzd"):
+        out[n] = op(work, n)
+    for k in ("dense_lists", "dense_auto", "dense_tensor", "dense_tensor_psi", "krylov_lists", "krylov_tensor"):
+        out[k] = spectra(work, k + ".dat")
+    save("rixs.json", out)
+
+
 if __name__ == "__main__":
     if not os.path.exists(QUANTY):
         sys.exit("build the reference first: oracle/build_ref.sh")
-    which = sys.argv[1:] or ["hpsi", "c0", "c1", "chain", "fshell", "print", "tensor"]
+    which = sys.argv[1:] or ["hpsi", "c0", "c1", "chain", "fshell", "print", "tensor", "rixs"]
     for w in which:
         globals()["gen_" + w]()

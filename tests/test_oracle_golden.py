@@ -242,3 +242,49 @@ def test_dense_tensor_spectra_match_reference(oracle_mod, key):
                  + 1j * O.poles_spectrum(w - E0, wt.imag, 0.0, ref.Emin, de, ref.NE, ref.Gamma))
             R = ref.G[i * 3 + j]
             assert np.max(np.abs(G - R)) < 1e-8 * np.max(np.abs(ref.G)), (i, j)
+
+
+def _rixs_inputs(O, g, t1, t2, npsi):
+    return ([O.Op(g[t]) for t in t1], [O.Op(g[t]) for t in t2],
+            [O.WF.from_fixture(p) for p in g["psi"][:npsi]])
+
+
+def _spectra_of(ref):
+    return np.array(ref["re"]) + 1j * np.array(ref["im"])
+
+
+@pytest.mark.parametrize("key,t1,t2,npsi,tensor,auto", [
+    ("dense_lists", ("Tx", "Ty"), ("Txd", "Tyd", "Tzd"), 2, False, False),
+    ("dense_auto", ("Tx",), ("Txd", "Tyd"), 1, False, True),
+    ("dense_tensor", ("Tx", "Ty"), ("Txd", "Tyd"), 1, True, False),
+    ("dense_tensor_psi", ("Tx",), ("Tyd",), 2, True, False),
+])
+def test_dense_rixs_matches_reference(oracle_mod, key, t1, t2, npsi, tensor, auto):
+    """Dense RIXS restated (ResonantSpectraDense / ResonantSpectraDenseTensor,
+    Core/ResonantSpectra.cpp:290, :665): lists of absorption and emission operators and of
+    initial states, the spectrum order of both forms, the automatic energy ranges."""
+    O = oracle_mod
+    g = golden("rixs.json")
+    T1s, T2s, psis = _rixs_inputs(O, g, t1, t2, npsi)
+    o = {"NE1": 4, "Gamma1": 0.8, "NE2": 64, "Gamma2": 0.3} if auto else dict(g["opts"])
+    G, st = O.resonant_spectra_dense(O.Op(g["HX"]), O.Op(g["H"]), T1s, T2s, psis, o, tensor=tensor)
+    ref = g[key]
+    assert G.shape == (ref["nspec"], 65)
+    assert rel_err(G, _spectra_of(ref)) < 1e-8
+    assert abs(st["emin2"] - ref["emin"]) < 1e-10 and abs(st["emax2"] - ref["emax"]) < 1e-10
+    assert abs(st["gamma2"] - ref["gamma"]) < 1e-12
+
+
+def test_krylov_rixs_lists_and_tensor_match_reference(oracle_mod):
+    """Krylov branch: lists of T1 and psi run one ResonantSpectra per (psi, T1) pair, blocks in
+    that order (LuaInterface/ssp.cpp:3401-3424); the Krylov tensor form at complete Krylov
+    spaces equals the dense tensor restatement in the Krylov branch's index order."""
+    O = oracle_mod
+    g = golden("rixs.json")
+    T1s, T2s, psis = _rixs_inputs(O, g, ("Tx", "Ty"), ("Txd", "Tyd"), 2)
+    o = dict(g["opts"], Epsilon=0.0, NTri1=100, NTri2=100)
+    G = np.concatenate([O.resonant_spectra(O.Op(g["HX"]), O.Op(g["H"]), T, T2s, p, o) for p in psis for T in T1s])
+    assert rel_err(G, _spectra_of(g["krylov_lists"])) < 1e-8
+    Gt, _ = O.resonant_spectra_dense(O.Op(g["HX"]), O.Op(g["H"]), T1s, T2s, psis[:1], dict(g["opts"]),
+                                     tensor=True, krylov_layout=True)
+    assert rel_err(Gt, _spectra_of(g["krylov_tensor"])) < 1e-8
