@@ -987,13 +987,49 @@ def EigensystemOnBasis(H, basis, Npsi, options=None, eng=None, seed=12345, max_r
 
 # ----------------------------------------------------------------------------- RIXS
 
+def _as_list(x):
+    return list(x) if isinstance(x, (list, tuple)) else [x]
+
+
 def CreateResonantSpectra(H1, H2, T1, T2, psi, options=None, eng=None):
-    """Reference CreateResonantSpectra, sparse branch (LuaInterface/ssp.cpp:3090 ->
-    ResonantSpectra, Core/ResonantSpectra.cpp:6): returns (G [NT2*(NE1+1), NE2+1], settings)
-    with spectrum index iT2*(NE1+1) + p and the resolved energy ranges in settings."""
+    """Reference CreateResonantSpectra (LuaInterface/ssp.cpp:3090-3447).  T1, T2 and psi are an
+    operator / a wavefunction or lists of them.  Returns (G [nspec, NE2+1], settings).
+
+    Branch choice as in the reference (ssp.cpp:3300-3371): the dense branch when the union of
+    the initial states, the targets of every T1, their closure under H1, the targets of every T2
+    and their closure under H2 all stay within DenseBorder (or ForceDenseMethod), else the
+    Krylov branch.  Spectrum order: dense, l + (NE1+1)(k + NT2 (iT1 + NT1 ipsi)); Krylov,
+    one block of NT2 (NE1+1) spectra (index k (NE1+1) + l) per (ipsi, iT1) pair, psi outer;
+    tensor forms, (NT1 NT2 Npsi)^2 (NE1+1) spectra (see _rixs_dense and _rixs_krylov_tensor)."""
     eng = eng or engine()
     o = _opts(options)
-    T2s = T2 if isinstance(T2, (list, tuple)) else [T2]
+    T1s, T2s, psis = _as_list(T1), _as_list(T2), _as_list(psi)
+    if not T1s or not T2s or not psis:
+        raise ValueError("CreateResonantSpectra: empty list of operators or wavefunctions")
+    for k in ("E0_1", "E0_2"):
+        if o.get(k) is None and o.get("E0") is not None:
+            o[k] = o["E0"]
+    tensor = bool(o.get("Tensor"))
+    bases = _rixs_dense_bases(H1, H2, T1s, T2s, psis, o, eng)
+    if bases is not None:
+        return _rixs_dense(H1, H2, T1s, T2s, psis, o, bases[0], bases[1], tensor, eng)
+    if tensor:
+        return _rixs_krylov_tensor(H1, H2, T1s, T2s, psis, o, eng)
+    blocks, sts = [], []
+    for p in psis:
+        for T in T1s:
+            G, st = _rixs_krylov(H1, H2, T, T2s, p, o, eng)
+            blocks.append(G)
+            sts.append(st)
+    st = dict(sts[0], method="krylov")
+    if len(sts) > 1:
+        st["blocks"] = sts
+    return np.concatenate(blocks), st
+
+
+def _rixs_krylov(H1, H2, T1, T2s, psi, o, eng):
+    """One Krylov RIXS run, ResonantSpectra (Core/ResonantSpectra.cpp:6): spectrum
+    iT2 (NE1+1) + p, every incident energy and T2 batched on the device (qg_resonant_spectra)."""
     big = np.finfo(float).max
     st = qgpu.RixsSettings()
     st.ntri1, st.ntri2 = int(o["NTri1"]), int(o["NTri2"])
@@ -1020,3 +1056,322 @@ def CreateResonantSpectra(H1, H2, T1, T2, psi, options=None, eng=None):
                                         C.cast(t2h, C.c_void_p), len(T2s), b.h, _ptr(x), C.byref(st), _ptr(g)))
     G = (g[0::2] + 1j * g[1::2]).reshape(len(T2s) * (st.ne1 + 1), st.ne2 + 1)
     return G, {k: getattr(st, k) for k, _ in st._fields_ if not k.startswith("res")}
+
+
+def _rixs_dense_bases(H1, H2, T1s, T2s, psis, o, eng):
+    """The two bases of the dense branch, or None when one of them outgrows DenseBorder
+    (LuaInterface/ssp.cpp:3300-3371): the union of the initial states; the targets of every T1
+    from it; their closure under H1 (intermediate states); the targets of every T2 from that;
+    their closure under H2 (final states), all within Restrictions1 / Restrictions2."""
+    force = bool(o.get("ForceDenseMethod"))
+    border = int(o["DenseBorder"])
+
+    def fits(n):
+        return force or n <= border
+
+    nf = H1.nf
+    if not fits(max(p.N for p in psis)):  # then their union is larger still
+        return None
+    dets = np.unique(np.concatenate([np.asarray(p.det, dtype=np.uint8).reshape(-1, nword(nf)) for p in psis]), axis=0)
+    if not fits(len(dets)):
+        return None
+    R1, R2 = o.get("Restrictions1"), o.get("Restrictions2")
+    u, _ = Basis.from_bytes(nf, dets, eng)
+    bases = []
+    for H, Ts, R in ((H1, T1s, R1), (H2, T2s, R2)):
+        bt = None
+        for T in Ts:
+            t = OperatorPsiBasis(T, u, R, eng)
+            bt = t if bt is None else basis_union(bt, t, eng)
+            if not fits(bt.n):
+                return None
+        u = closure_of(H, bt, R, -1, eng)
+        if not fits(u.n):
+            return None
+        bases.append(u)
+    return bases
+
+
+def _rixs_energies(H, psis, key, o, eng, normalise=True):
+    """E0_1 / E0_2 when given, else <psi|H|psi> (divided by <psi|psi> when that exceeds
+    DBL_EPSILON, Core/ResonantSpectra.cpp:345-373) for every initial state."""
+    if o.get(key) is not None:
+        return np.full(len(psis), float(o[key]))
+    out = []
+    for p in psis:
+        e = PsiOperatorPsi(H, p, eng).real
+        nn = float(np.real(np.vdot(p.val, p.val)))
+        out.append(e / nn if normalise and nn > DBL_EPSILON else e)
+    return np.array(out)
+
+
+def _rixs_range(emin, emax, ne, gamma, lo_ev, hi_ev, e_lo, e_hi):
+    """Energy-range defaults of the dense branch (Core/ResonantSpectra.cpp:472-535)."""
+    if emin is None and emax is None:
+        emin = 1.1 * lo_ev - 0.1 * hi_ev - e_hi
+        emax = 1.1 * hi_ev - 0.1 * lo_ev - e_lo
+    if emin is None:
+        emin = 1.1 * lo_ev - 0.1 * emax - e_hi
+    if emax is None:
+        emax = 1.1 * hi_ev - 0.1 * emin - e_lo
+    if gamma == 0 and ne == 0:
+        ne = 1000
+        gamma = 5 * (emax - emin) / ne
+    if ne == 0:
+        ne = int(5 * (emax - emin) / gamma)
+    if gamma == 0:
+        gamma = 5 * (emax - emin) / ne
+    return float(emin), float(emax), int(ne), float(gamma)
+
+
+def _apply_between(O, dst, src, X, eng):
+    """O applied to every column of the host matrix X (rows on src) into dst, one multi-vector
+    pull launch sequence on the device; returns the host matrix (dst.n x columns)."""
+    k = X.shape[1]
+    if not dst.n or not src.n or not k:
+        return np.zeros((dst.n, k), dtype=np.complex128)
+    with eng.on_stream():
+        x = eng.torch.from_numpy(np.ascontiguousarray(X, dtype=np.complex128)).to("cuda:%d" % eng.device)
+    y = eng.empty(dst.n, k)
+    eng.check(eng.L.qg_apply(eng.ctx, O.handle(eng), dst.h, src.h, _ptr(x), _ptr(y), k))
+    return eng.to_host(y[:dst.n])
+
+
+def _poles_complex(e0, poles, W, emin, emax, ne, gamma, eng):
+    """Sum of Lorentzians with complex weights: the poles kernel on the real and imaginary parts."""
+    G = ListOfPolesToSpectrum(e0, poles, np.ascontiguousarray(W.real), emin, emax, ne, gamma, eng)
+    if np.any(W.imag):
+        G = G + 1j * ListOfPolesToSpectrum(e0, poles, np.ascontiguousarray(W.imag), emin, emax, ne, gamma, eng)
+    return G
+
+
+def _rixs_dense(H1, H2, T1s, T2s, psis, o, b1, b2, tensor, eng):
+    """Dense RIXS, ResonantSpectraDense / ResonantSpectraDenseTensor (Core/ResonantSpectra.cpp:290,
+    :665).  H1 and H2 as dense matrices on their bases (device), their eigensystems (host
+    solver), A[m, j] = <m|T1 psi_j> (j = iT1 + NT1 ipsi), B_k[f, m] = <f|T2_k|m> with T2_k
+    applied to every intermediate eigenvector on the device; per incident energy w_l the
+    amplitudes D_k = B_k (A / (w_l - E_m + E1_psi + i Gamma1/2)) and the spectra as sums of
+    Lorentzians at the final eigenvalues (the poles kernel, all spectra and energies at once).
+    Non-tensor spectrum l + (NE1+1)(k + NT2 j): weights |D_k[f, j]|^2, shift E2 of psi_j.
+    Tensor spectrum l + (NE1+1)(j2 + NT2(i1 + NT1(n2 + NT2(m1 + NT1(r + Npsi s))))): weights
+    conj(D_n2[f, m1 + NT1 s]) D_j2[f, i1 + NT1 r], shift E2 of psi 0."""
+    npsi, nt1, nt2 = len(psis), len(T1s), len(T2s)
+    n1, n2 = b1.n, b2.n
+    M1 = npsi * nt1
+    R1 = o.get("Restrictions1")
+    e1 = _rixs_energies(H1, psis, "E0_1", o, eng)
+    e2 = _rixs_energies(H2, psis, "E0_2", o, eng)
+    X = np.zeros((n1, M1), dtype=np.complex128)
+    for ip, p in enumerate(psis):
+        for it, T in enumerate(T1s):
+            t = OperatorPsi(T, p, R1, eng)
+            if t.N and n1:
+                np.add.at(X[:, it + nt1 * ip], b1.find(t.det), t.val)
+    if n1:
+        w1, V1 = hermitian_eigh(OperatorToDeterminantMatrix(H1, b1, eng), n1, eng)
+    else:
+        w1, V1 = np.zeros(1), np.zeros((0, 0), dtype=np.complex128)
+    if n2:
+        w2, V2 = hermitian_eigh(OperatorToDeterminantMatrix(H2, b2, eng), n2, eng)
+    else:
+        w2, V2 = np.zeros(1), np.zeros((0, 0), dtype=np.complex128)
+    A = V1.conj().T @ X
+    B = [V2.conj().T @ _apply_between(T, b2, b1, V1, eng) for T in T2s]
+    big = None
+    emin1, emax1, ne1, g1 = _rixs_range(o.get("Emin1", big), o.get("Emax1", big), int(o.get("NE1", 1000)),
+                                        float(o.get("Gamma1", 0.0)), w1[0], w1[-1], e1.min(), e1.max())
+    emin2, emax2, ne2, g2 = _rixs_range(o.get("Emin2", big), o.get("Emax2", big), int(o.get("NE2", 1000)),
+                                        float(o.get("Gamma2", 0.0)), w2[0], w2[-1], e2.min(), e2.max())
+    np1 = ne1 + 1
+    wres = np.array([emin1 + (emax1 - emin1) * l / ne1 for l in range(np1)])
+    psi_of = np.arange(M1) // nt1
+    Cm = A[None, :, :] / (wres[:, None, None] - w1[None, :n1, None] + e1[psi_of][None, None, :] + 0.5j * g1)
+    D = np.stack([Bk @ Cm for Bk in B]) if n2 and n1 else np.zeros((nt2, np1, n2, M1), dtype=np.complex128)
+    st = {"method": "dense", "emin1": emin1, "emax1": emax1, "ne1": ne1, "gamma1": g1, "emin2": emin2,
+          "emax2": emax2, "ne2": ne2, "gamma2": g2, "energy1": e1.tolist(), "energy2": e2.tolist(),
+          "n1": n1, "n2": n2, "resonant_energies": wres.tolist()}
+    if not tensor:
+        nspec = nt2 * M1 * np1
+        if not n2:
+            return np.zeros((nspec, ne2 + 1), dtype=np.complex128), st
+        W = np.zeros((nspec, n2))
+        e0 = np.zeros(nspec)
+        for k in range(nt2):
+            for j in range(M1):
+                rows = np.arange(np1) + np1 * (k + nt2 * j)
+                W[rows] = np.abs(D[k][:, :, j]) ** 2
+                e0[rows] = e2[psi_of[j]]
+        return ListOfPolesToSpectrum(e0, w2, W, emin2, emax2, ne2, g2, eng), st
+    M = M1 * nt2
+    nspec = M * M * np1
+    G = np.zeros((nspec, ne2 + 1), dtype=np.complex128)
+    if not n2:
+        return G, st
+    lk, lc, rk, rc, base = [], [], [], [], []
+    for r in range(npsi):
+        for s_ in range(npsi):
+            for i1 in range(nt1):
+                for j2 in range(nt2):
+                    for m1 in range(nt1):
+                        for n2_ in range(nt2):
+                            base.append(np1 * (j2 + nt2 * (i1 + nt1 * (n2_ + nt2 * (m1 + nt1 * (r + npsi * s_))))))
+                            lk.append(n2_)
+                            lc.append(m1 + nt1 * s_)
+                            rk.append(j2)
+                            rc.append(i1 + nt1 * r)
+    lk, lc, rk, rc, base = (np.array(v) for v in (lk, lc, rk, rc, base))
+    step = max(1, int(2 ** 24 // max(1, M * M * n2)))  # bound the host weight block
+    for l0 in range(0, np1, step):
+        ls = np.arange(l0, min(np1, l0 + step))
+        W = np.conj(D[lk[:, None], ls[None, :], :, lc[:, None]]) * D[rk[:, None], ls[None, :], :, rc[:, None]]
+        W = W.reshape(-1, n2)  # rows (pair, l)
+        rows = (base[:, None] + ls[None, :]).reshape(-1)
+        G[rows] = _poles_complex(e2[0], w2, W, emin2, emax2, ne2, g2, eng)
+    return G, st
+
+
+def _rixs_krylov_tensor(H1, H2, T1s, T2s, psis, o, eng):
+    """Krylov tensor RIXS, the result of ResonantSpectraTensor (Core/ResonantSpectra.cpp:1204):
+    the matrix <v_a| (w + E2 - H2 + i Gamma2/2)^-1 |v_b> of the vectors
+    v_(psi, T1, T2) = T2 G1(w_l) T1 psi for every incident energy, both shifts from psi 0 (as the
+    reference).  The reference runs one block Lanczos per stage; here every T1 psi gets its own
+    three-term Lanczos with stored Krylov vectors and G1(w_l) T1 psi is that space's projected
+    resolvent, all w_l at once; the matrix elements come from one batched
+    Lanczos over every diagonal vector and, per pair, v_a + v_b and v_a + i v_b (polarisation).
+    Each chain runs as many steps as the block run has Krylov vectors (NTri blocks times the
+    block width, at most the basis size), so a complete block space means complete chains, and
+    then the result equals the block-Lanczos one; the reference's
+    index order is kept: spectrum l + (NE1+1)(j2 + NT2(i1 + NT1(n2 + NT2(m1 + NT1(r + Npsi s)))))
+    holds the element between v_(r, m1, n2) (left) and v_(s, i1, j2) (right).  Energy ranges
+    come from the extreme Krylov eigenvalues with the block branch's rules."""
+    torch = eng.torch
+    dev = "cuda:%d" % eng.device
+    npsi, nt1, nt2 = len(psis), len(T1s), len(T2s)
+    M1, nf = npsi * nt1, H1.nf
+    eps, ntri1, ntri2 = float(o["Epsilon"]), int(o["NTri1"]), int(o["NTri2"])
+    R1, R2 = o.get("Restrictions1"), o.get("Restrictions2")
+    e1 = float(_rixs_energies(H1, psis[:1], "E0_1", o, eng, normalise=False)[0])
+    e2 = float(_rixs_energies(H2, psis[:1], "E0_2", o, eng, normalise=False)[0])
+    ne1, ne2 = int(o.get("NE1", 1000)), int(o.get("NE2", 1000))
+    np1 = ne1 + 1
+    M = M1 * nt2
+    Tpsi = [OperatorPsi(T, p, R1, eng) for p in psis for T in T1s]  # j = iT1 + NT1 ipsi
+    seed = [t.det for t in Tpsi if t.N]
+    if not seed:
+        raise ValueError("CreateResonantSpectra: every T1 psi is empty")
+    b1 = closure(H1, np.concatenate(seed), nf, R1, -1, eng)
+    n1 = b1.n
+    X1 = np.zeros((n1, M1), dtype=np.complex128)
+    for j, t in enumerate(Tpsi):
+        if t.N:
+            v = np.where(np.abs(t.val) <= eps, 0.0, t.val) if eps > 0 else t.val
+            np.add.at(X1[:, j], b1.find(t.det), v)
+    # each chain gets the Krylov dimension of the reference's block run, NTri1 blocks of M1
+    # (a few steps past the basis size at most); three-term Lanczos keeping its vectors
+    L1 = max(1, min(ntri1 * M1, n1 + 16))
+    chains = []
+    for j in range(M1):
+        with eng.on_stream():
+            x = torch.from_numpy(np.ascontiguousarray(X1[:, j:j + 1])).to(dev)
+            K = torch.zeros((L1, n1, 1), dtype=torch.complex128, device=dev)
+        A1, B1 = lanczos_block(H1, b1, x, L1, eps, eps, eng, krylov=K)
+        a, b = A1[0], B1[0]
+        k = next((q for q in range(1, L1) if b[q] == 0.0), L1)
+        T = np.diag(a[1:k + 1]) + np.diag(b[1:k], 1) + np.diag(b[1:k], -1)
+        ev, Z = hermitian_eigh(T.astype(np.complex128), k, eng)
+        chains.append((K[:, :, 0], k, b[0], ev, Z.real))
+    lo = min(c[3][0] for c in chains if c[2] != 0.0) if any(c[2] != 0.0 for c in chains) else 0.0
+    hi = max(c[3][-1] for c in chains if c[2] != 0.0) if any(c[2] != 0.0 for c in chains) else 0.0
+    emin1, emax1, g1 = _default_window(lo - e1, hi - e1, o.get("Emin1"), o.get("Emax1"),
+                                       float(o.get("Gamma1", 0.0)), ne1)
+    wres = np.array([emin1 + (emax1 - emin1) * p / ne1 + e1 for p in range(np1)])
+    # G1(w_l) T1 psi_j for all l: column l + np1 j on b1
+    with eng.on_stream():
+        GT = torch.zeros((n1, M1 * np1), dtype=torch.complex128, device=dev)
+    for j, (K, k, b0, ev, Z) in enumerate(chains):
+        Cc = b0 * (Z[:, None, :] * (Z[0, :][None, None, :] / (wres[None, :, None] - ev[None, None, :] + 0.5j * g1))).sum(-1)
+        with eng.on_stream():
+            GT[:, j * np1:(j + 1) * np1] = K[:k].T @ torch.from_numpy(np.ascontiguousarray(Cc)).to(dev)
+    # final-state basis: targets of every T2, closure under H2
+    bt = None
+    for T in T2s:
+        t = OperatorPsiBasis(T, b1, R2, eng)
+        bt = t if bt is None else basis_union(bt, t, eng)
+    b2 = closure_of(H2, bt, R2, -1, eng)
+    n2 = b2.n
+    G = np.zeros((M * M * np1, ne2 + 1), dtype=np.complex128)
+    st = {"method": "krylov_tensor", "emin1": emin1, "emax1": emax1, "ne1": ne1, "gamma1": g1,
+          "energy1": e1, "energy2": e2, "n1": n1, "n2": n2, "resonant_energies": (wres - e1).tolist()}
+    if not n2:
+        st.update(emin2=o.get("Emin2"), emax2=o.get("Emax2"), ne2=ne2, gamma2=float(o.get("Gamma2", 0.0)))
+        return G, st
+    # v_a(l), a = s + NT2 j: Y[s] column l + np1 j
+    Y = []
+    for T in T2s:
+        yv = eng.empty(n2, M1 * np1)
+        eng.check(eng.L.qg_apply(eng.ctx, T.handle(eng), b2.h, b1.h, _ptr(GT), _ptr(yv), M1 * np1))
+        Y.append(yv[:n2])
+    pairs = [(a_, b_) for a_ in range(M) for b_ in range(a_ + 1, M)]
+    per_l = M + 2 * len(pairs)  # chains per incident energy: diagonals, then v_a + v_b, v_a + i v_b
+
+    def vec(l, a_):
+        s_, j = a_ % nt2, a_ // nt2
+        return Y[s_][:, l + np1 * j]
+
+    gamma_l = max(float(o.get("Gamma2", 0.0)), eps)
+    L2 = max(1, min(ntri2 * M, n2 + 16))  # the block run's Krylov dimension, NTri2 blocks of M
+    # incident energies in chunks of at most ~1 GiB of start vectors (the Lanczos holds six
+    # blocks of that size)
+    chunk = max(1, min(np1, (1 << 30) // (per_l * n2 * 16)))
+    Gm = np.zeros((np1, M, M, ne2 + 1), dtype=np.complex128)
+    emin2 = emax2 = g2 = None
+    for l0 in range(0, np1, chunk):
+        ls = range(l0, min(np1, l0 + chunk))
+        with eng.on_stream():
+            Zc = torch.empty((n2, per_l * len(ls)), dtype=torch.complex128, device=dev)
+            c = 0
+            for l in ls:
+                for a_ in range(M):
+                    Zc[:, c] = vec(l, a_)
+                    c += 1
+                for a_, b_ in pairs:
+                    Zc[:, c] = vec(l, a_) + vec(l, b_)
+                    Zc[:, c + 1] = vec(l, a_) + 1j * vec(l, b_)
+                    c += 2
+        A2, B2 = lanczos_block(H2, b2, Zc, L2, eps, gamma_l, eng)
+        if emin2 is None:
+            # ranges from the first incident energy's diagonal chains, the block branch's rules
+            lo2, hi2 = np.inf, -np.inf
+            for c in range(M):
+                if B2[c, 0] == 0.0:
+                    continue
+                k = next((q for q in range(1, L2) if B2[c, q] == 0.0), L2)
+                w0, w1_ = _tri_extremes(A2[c, 1:k + 1], B2[c, 1:k])
+                lo2, hi2 = min(lo2, w0 - e2), max(hi2, w1_ - e2)
+            if not np.isfinite(lo2):
+                lo2 = hi2 = 0.0
+            emin2, emax2, g2 = _default_window(lo2, hi2, o.get("Emin2"), o.get("Emax2"),
+                                               float(o.get("Gamma2", 0.0)), ne2)
+            st.update(emin2=emin2, emax2=emax2, ne2=ne2, gamma2=g2)
+        Dcf = TriDiagonalMatrixToSpectrum(np.full(A2.shape[0], e2), A2, B2, emin2, emax2, ne2, g2, eng)
+        for q0, l in enumerate(ls):
+            c0 = q0 * per_l
+            diag = Dcf[c0:c0 + M]
+            for a_ in range(M):
+                Gm[l, a_, a_] = diag[a_]
+            for q, (a_, b_) in enumerate(pairs):
+                S_ = Dcf[c0 + M + 2 * q] - diag[a_] - diag[b_]
+                T_ = Dcf[c0 + M + 2 * q + 1] - diag[a_] - diag[b_]
+                Gm[l, a_, b_] = 0.5 * (S_ - 1j * T_)
+                Gm[l, b_, a_] = 0.5 * (S_ + 1j * T_)
+    for r in range(npsi):
+        for s_ in range(npsi):
+            for i1 in range(nt1):
+                for j2 in range(nt2):
+                    for m1 in range(nt1):
+                        for n2_ in range(nt2):
+                            idx = j2 + nt2 * (i1 + nt1 * (n2_ + nt2 * (m1 + nt1 * (r + npsi * s_))))
+                            row = n2_ + nt2 * (m1 + nt1 * r)
+                            col = j2 + nt2 * (i1 + nt1 * s_)
+                            G[np1 * idx:np1 * (idx + 1)] = Gm[:, row, col]
+    return G, st

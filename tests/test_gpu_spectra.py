@@ -98,7 +98,7 @@ def test_rixs_matches_reference(api, key, eps):
     """CreateResonantSpectra on the d8 case: all incident energies and final-state Lanczos runs
     batched, against the reference's RIXS spectra (1e-8)."""
     g = golden("c0_xas.json")
-    o = dict(g["rixs_opts"], Epsilon=eps, NTri1=100, NTri2=100)
+    o = dict(g["rixs_opts"], Epsilon=eps, NTri1=100, NTri2=100, DenseBorder=0)
     G, st = api.CreateResonantSpectra(api.Operator.from_fixture(g["HX"]), api.Operator.from_fixture(g["H"]),
                                       api.Operator.from_fixture(g["Tx"]), [api.Operator.from_fixture(g["Tyd"])],
                                       api.Wavefunction.from_fixture(g["psi"][0]), o)
@@ -108,16 +108,17 @@ def test_rixs_matches_reference(api, key, eps):
     assert spec_err(G, R) < SPEC_TOL, spec_err(G, R)
 
 
-def test_rixs_with_empty_final_basis_gives_zero(api):
+@pytest.mark.parametrize("dense_border", [0, 1513])
+def test_rixs_with_empty_final_basis_gives_zero(api, dense_border):
     """Emission operators that lead out of the final-state restrictions: no determinant is
-    reachable, so every RIXS spectrum vanishes (no error)."""
+    reachable, so every RIXS spectrum vanishes (no error), in the Krylov and the dense branch."""
     g = golden("c0_xas.json")
     HX = api.Operator.from_fixture(g["HX"])
     Ts = [api.Operator.from_fixture(g[t]) for t in ("Tx", "Ty", "Tz")]
     psi = api.Wavefunction.from_fixture(g["psi"][0])
     o = {"NTri1": 20, "NTri2": 20, "NE1": 4, "Gamma1": 0.4, "NE2": 50, "Gamma2": 0.2,
          "Emin1": -5.0, "Emax1": 5.0, "Emin2": -2.0, "Emax2": 8.0,
-         "Restrictions2": [16, 0, ["1111110000000000", 6, 6]]}
+         "Restrictions2": [16, 0, ["1111110000000000", 6, 6]], "DenseBorder": dense_border}
     G, st = api.CreateResonantSpectra(HX, HX, Ts[2], Ts, psi, o)  # T2 = absorption again: 2p4
     assert G.shape == (3 * 5, 51) and np.all(G == 0)
 
