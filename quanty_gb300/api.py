@@ -728,19 +728,39 @@ def CreateSpectraResident(H, T, basis, X, E0, options=None, eng=None, batched=Tr
     return Spectra(G, o["Emin"], o["Emax"], NE, gamma), A, B
 
 
+def _spectra_method(o):
+    """CreateSpectra's Method and ForceDenseMethod options (LuaInterface/ssp.cpp:2029-2058):
+    "dense" (Method "Dense" or ForceDenseMethod), "lanczos" (Method "Lanczos", any size) or ""
+    (Method "Auto": dense within DenseBorder).  Contradicting or unknown choices raise, as the
+    reference's luaL_error; Method "Mesh" (the hybridisation on an energy mesh, a self-energy
+    feature) is not part of this library."""
+    m = str(o.get("Method") or "Auto")
+    force = bool(o.get("ForceDenseMethod"))
+    key = m.lower()
+    if key not in ("auto", "dense", "lanczos", "mesh"):
+        raise ValueError('CreateSpectra: unknown Method "%s", possible are "Auto", "Dense", "Lanczos" and "Mesh"' % m)
+    if key in ("lanczos", "mesh") and force:
+        raise ValueError('CreateSpectra: Method "%s" and ForceDenseMethod true contradict each other' % m)
+    if key == "mesh":
+        raise NotImplementedError('CreateSpectra: Method "Mesh" (hybridisation on an energy mesh) is not supported')
+    if force or key == "dense":
+        return "dense"
+    return "lanczos" if key == "lanczos" else ""
+
+
 def CreateSpectra(H, T, psi, options=None, eng=None, batched=True):
     """Reference CreateSpectra (LuaInterface/ssp.cpp:1906): spectra of all (T, psi) pairs,
     ordered iT*Npsi + ipsi.  Lanczos branch (:2586-2720): returns (Spectra, [(a, b) shifted by
     -E0]); batched=True runs all pairs as one multi-vector Lanczos with every step on the
     device.  Dense branch (:2347-2460; Method "Dense", or a union basis within DenseBorder
     unless Method is "Lanczos"): returns (Spectra, [(poles - E0, weights)])."""
-    eng = eng or engine()
     o = _opts(options)
+    method = _spectra_method(o)
+    eng = eng or engine()
     Ts = T if isinstance(T, (list, tuple)) else [T]
     psis = psi if isinstance(psi, (list, tuple)) else [psi]
     ntri, eps = int(o["NTri"]), float(o["Epsilon"])
     R = parse_restrictions(o.get("Restrictions"))
-    method = str(o.get("Method") or "").lower()
     gamma = float(o["Gamma"])
     if batched and not o.get("Tensor") and method != "dense":
         got = _batched_lanczos_device(H, Ts, psis, o, R, eng)
@@ -791,7 +811,7 @@ def _batched_lanczos_device(H, Ts, psis, o, R, eng):
     torch = eng.torch
     nf, npsi = H.nf, len(psis)
     ntri, eps, gamma = int(o["NTri"]), float(o["Epsilon"]), float(o["Gamma"])
-    method = str(o.get("Method") or "").lower()
+    method = _spectra_method(o)
     dets = np.concatenate([p.det for p in psis])
     b0, perm = Basis.from_bytes(nf, dets, eng)
     X = np.zeros((max(b0.n, 1), npsi), dtype=np.complex128)
@@ -932,17 +952,38 @@ def enumerate_restricted(nf, restrictions):
     return np.packbits(bits, axis=1, bitorder="big")
 
 
-def Eigensystem(H, StartRestrictions, Npsi, options=None, eng=None, seed=12345):
-    """Lowest Npsi eigenstates of a Hermitian H (reference Eigensystem -> BlockGroundState,
-    LuaInterface/ssp.cpp:4039, Core/BlockLanczos.cpp:5782).  The basis is the complete set of
-    determinants allowed by the restrictions (or their closure under H); the eigenproblem on it
-    is solved by restarted block Lanczos on the device.  Returns (list of Wavefunction, energies)."""
+def Eigensystem(H, StartRestrictions, Npsi=None, options=None, eng=None, seed=12345):
+    """Lowest eigenstates of a Hermitian H (reference Eigensystem -> BlockGroundState,
+    LuaInterface/ssp.cpp:4039-4260, Core/BlockLanczos.cpp:5782).  Two call forms, as the
+    reference: Eigensystem(H, StartRestrictions, Npsi[, options]) starts from every determinant
+    the start restrictions allow; Eigensystem(H, psi or [psi, ...][, options]) starts from the
+    given states' determinants and finds as many states as were given.  The basis then grows
+    under H within the Restrictions option, or without limit when it is absent (the reference's
+    growth loop uses only that option, BlockLanczos.cpp:5843-5884), and the eigenproblem on the
+    closed basis is solved densely (at most DenseBorder determinants, raised to Npsi when
+    options are given, BlockLanczosGroundStateConserveBasisDense) or by restarted block Lanczos
+    on the device.  Returns (list of Wavefunction, energies)."""
+    states = None
+    if isinstance(StartRestrictions, Wavefunction) or (
+            isinstance(StartRestrictions, (list, tuple)) and len(StartRestrictions)
+            and isinstance(StartRestrictions[0], Wavefunction)):
+        states = _as_list(StartRestrictions)
+        if options is None and not isinstance(Npsi, (int, np.integer)):
+            options = Npsi
+        Npsi = len(states)
+    elif Npsi is None:
+        raise ValueError("Eigensystem called with start restrictions needs the number of states")
     eng = eng or engine()
-    R = parse_restrictions(StartRestrictions)
-    dets = enumerate_restricted(H.nf, R)
-    basis, _ = Basis.from_bytes(H.nf, dets, eng)
-    basis = closure_of(H, basis, R, -1, eng)
-    if basis.n <= int(_opts(options)["DenseBorder"]):
+    o = _opts(options)
+    if options:
+        o["DenseBorder"] = max(int(o["DenseBorder"]), int(Npsi))
+    if states is None:
+        seed_dets = enumerate_restricted(H.nf, parse_restrictions(StartRestrictions))
+    else:
+        seed_dets = np.concatenate([np.asarray(p.det, dtype=np.uint8).reshape(-1, nword(H.nf)) for p in states])
+    basis, _ = Basis.from_bytes(H.nf, seed_dets, eng)
+    basis = closure_of(H, basis, o.get("Restrictions"), -1, eng)
+    if basis.n <= int(o["DenseBorder"]):
         # dense branch (BlockLanczosGroundStateConserveBasisDense, Core/BlockLanczos.cpp:370)
         w, V = hermitian_eigh(OperatorToDeterminantMatrix(H, basis, eng), min(Npsi, basis.n), eng)
         db = basis.dets_bytes()

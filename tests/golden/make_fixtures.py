@@ -294,9 +294,23 @@ def gen_rixs():
     save("rixs.json", out)
 
 
+def gen_eigen_growth():
+    """Eigensystem's basis growth beyond the start restrictions, and its confinement by the
+    Restrictions option, on the 26-orbital ligand-field ion (operators of c1_lf.lua)."""
+    head = open(os.path.join(HERE, "gen", "c1_lf.lua")).read().splitlines()[:44]
+    tail = open(os.path.join(HERE, "gen", "eigen_growth.lua")).read()
+    work = run("\n".join(head) + "\n" + tail, "eigen_growth.lua")
+    out = {"source": "tests/golden/gen/c1_lf.lua:1-44 + tests/golden/gen/eigen_growth.lua",
+           "start_restrictions": [["11111100000000000000000000", 6, 6], ["00000011111111110000000000", 8, 8],
+                                  ["00000000000000001111111111", 10, 10]]}
+    for k in ("grown", "confined", "from_states"):
+        out["energies_" + k] = reals(work, "energies_%s.txt" % k)
+    save("eigen_growth.json", out)
+
+
 if __name__ == "__main__":
     if not os.path.exists(QUANTY):
         sys.exit("build the reference first: oracle/build_ref.sh")
-    which = sys.argv[1:] or ["hpsi", "c0", "c1", "chain", "fshell", "print", "tensor", "rixs"]
+    which = sys.argv[1:] or ["hpsi", "c0", "c1", "chain", "fshell", "print", "tensor", "rixs", "eigen_growth"]
     for w in which:
         globals()["gen_" + w]()

@@ -47,3 +47,20 @@ def test_dense_eigensystem(api, fx):
     assert np.max(np.abs(np.array(E) - np.array(g["energies_dense"]))) < 1e-10
     for p, e in zip(psis, E):
         assert abs(api.PsiOperatorPsi(H, p).real / p.norm() ** 2 - e) < 1e-10
+
+
+def test_basis_grows_beyond_the_start_restrictions(api):
+    """Start restrictions that allow only d8 L10 on the ligand-field ion: without the
+    Restrictions option the basis grows under the hybridisation into d9 L9 and d10 L8, as the
+    reference's growth loop does; with it the states stay confined; the second call form starts
+    from given states and replaces them by as many eigenstates (1e-10 eV against the reference)."""
+    g = golden("eigen_growth.json")
+    H = api.Operator.from_fixture(golden("c1_lf.json")["H"])
+    Rn = [26, 0] + [list(r) for r in g["start_restrictions"]]
+    _, E = api.Eigensystem(H, Rn, 3)
+    assert np.max(np.abs(np.array(E) - np.array(g["energies_grown"]))) < 1e-10
+    psis, E = api.Eigensystem(H, Rn, 3, {"Restrictions": Rn})
+    assert np.max(np.abs(np.array(E) - np.array(g["energies_confined"]))) < 1e-10
+    out, E = api.Eigensystem(H, psis)
+    assert len(out) == 3
+    assert np.max(np.abs(np.array(E) - np.array(g["energies_from_states"]))) < 1e-10

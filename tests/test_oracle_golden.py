@@ -288,3 +288,24 @@ def test_krylov_rixs_lists_and_tensor_match_reference(oracle_mod):
     Gt, _ = O.resonant_spectra_dense(O.Op(g["HX"]), O.Op(g["H"]), T1s, T2s, psis[:1], dict(g["opts"]),
                                      tensor=True, krylov_layout=True)
     assert rel_err(Gt, _spectra_of(g["krylov_tensor"])) < 1e-8
+
+
+def test_eigensystem_growth_matches_reference(oracle_mod):
+    """Eigensystem grows the basis under H within the Restrictions option only
+    (Core/BlockLanczos.cpp:5843-5884): from the d8 L10 start determinants of the ligand-field
+    ion the unrestricted closure holds d9 L9 and d10 L8 and gives the reference's energies; the
+    closure confined to the start windows gives the confined energies."""
+    import itertools
+    O = oracle_mod
+    g = golden("eigen_growth.json")
+    H = O.Op(golden("c1_lf.json")["H"])
+    dets = []
+    for holes in itertools.combinations(range(6, 16), 2):
+        s = ["1"] * 26
+        for h in holes:
+            s[h] = "0"
+        dets.append("".join(s))
+    seed = O.WF(26, O.dets_to_bytes(dets, 26), np.ones(len(dets)))
+    for key, R in (("energies_grown", None), ("energies_confined", g["start_restrictions"])):
+        w, _ = O.exact_eigensystem(H, O.closure(H, seed, R), 3)
+        assert np.max(np.abs(w - np.array(g[key]))) < 1e-10, key

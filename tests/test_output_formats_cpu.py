@@ -68,3 +68,25 @@ def test_pole_range_extremes_match_dense_eigenvalues():
             w = np.linalg.eigvalsh(np.diag(a) + np.diag(b, 1) + np.diag(b, -1))
         scale = max(1.0, float(np.max(np.abs(w))))
         assert abs(lo - w[0]) <= 1e-12 * scale and abs(hi - w[-1]) <= 1e-12 * scale
+
+
+def test_spectra_method_options_follow_the_reference():
+    """Method / ForceDenseMethod of CreateSpectra (LuaInterface/ssp.cpp:2029-2058): Dense or
+    ForceDenseMethod force the dense branch, Lanczos forces the Krylov branch, Auto (or nothing)
+    decides by DenseBorder; contradicting or unknown choices are errors raised before any
+    device work."""
+    import pytest
+    from quanty_gb300 import api
+    m = lambda **k: api._spectra_method(api._opts(k))  # noqa: E731
+    assert m() == "" and m(Method="Auto") == "" and m(Method="auto") == ""
+    assert m(Method="Dense") == "dense" and m(ForceDenseMethod=True) == "dense"
+    assert m(Method="DENSE", ForceDenseMethod=True) == "dense"
+    assert m(Method="Lanczos") == "lanczos"
+    with pytest.raises(ValueError, match="contradict"):
+        m(Method="Lanczos", ForceDenseMethod=True)
+    with pytest.raises(ValueError, match="unknown Method"):
+        m(Method="Arnoldi")
+    with pytest.raises(NotImplementedError):
+        m(Method="Mesh")
+    with pytest.raises(ValueError, match="unknown Method"):  # checked before the GPU is needed
+        api.CreateSpectra(None, [], [], {"Method": "Arnoldi"})
