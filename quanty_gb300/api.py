@@ -1284,7 +1284,10 @@ def _rixs_krylov_tensor(H1, H2, T1s, T2s, psis, o, eng):
     then the result equals the block-Lanczos one; the reference's
     index order is kept: spectrum l + (NE1+1)(j2 + NT2(i1 + NT1(n2 + NT2(m1 + NT1(r + Npsi s)))))
     holds the element between v_(r, m1, n2) (left) and v_(s, i1, j2) (right).  Energy ranges
-    come from the extreme Krylov eigenvalues with the block branch's rules."""
+    come from the extreme Krylov eigenvalues with the block branch's rules; when the
+    second-stage block dimension (NTri2 times the block width) exceeds the final basis, the
+    reference's block matrix ends in zero blocks and its range includes their eigenvalue 0,
+    which is added here too."""
     torch = eng.torch
     dev = "cuda:%d" % eng.device
     npsi, nt1, nt2 = len(psis), len(T1s), len(T2s)
@@ -1391,6 +1394,11 @@ def _rixs_krylov_tensor(H1, H2, T1s, T2s, psis, o, eng):
                 lo2, hi2 = min(lo2, w0 - e2), max(hi2, w1_ - e2)
             if not np.isfinite(lo2):
                 lo2 = hi2 = 0.0
+            if ntri2 * M > n2:
+                # the reference's second-stage block matrix then ends in unused zero blocks,
+                # whose eigenvalue 0 enters its pole range (its Krylov-basis first stage drops
+                # them)
+                lo2, hi2 = min(lo2, -e2), max(hi2, -e2)
             emin2, emax2, g2 = _default_window(lo2, hi2, o.get("Emin2"), o.get("Emax2"),
                                                float(o.get("Gamma2", 0.0)), ne2)
             st.update(emin2=emin2, emax2=emax2, ne2=ne2, gamma2=g2)

@@ -50,4 +50,15 @@ S.Print({{"file", "dump/krylov_lists.dat"}})
 -- Krylov tensor form
 S = CreateResonantSpectra(HX, H, {Tx, Ty}, {Txd, Tyd}, psi1, opts({{"DenseBorder", 0}, {"Epsilon", 0}, {"Tensor", true}, {"NTri1", 40}, {"NTri2", 40}}))
 S.Print({{"file", "dump/krylov_tensor.dat"}})
+-- Krylov tensor form with automatic energy ranges
+S = CreateResonantSpectra(HX, H, {Tx, Ty}, {Txd}, psi1, {{"NE1", 3}, {"NE2", 48}, {"DenseBorder", 0}, {"Epsilon", 0}, {"Tensor", true}, {"NTri1", 40}, {"NTri2", 40}})
+S.Print({{"file", "dump/krylov_tensor_auto.dat"}})
+-- Krylov tensor form with two initial states
+S = CreateResonantSpectra(HX, H, {Tx}, {Tyd}, {psi1, psi2}, opts({{"DenseBorder", 0}, {"Epsilon", 0}, {"Tensor", true}, {"NTri1", 40}, {"NTri2", 40}}))
+S.Print({{"file", "dump/krylov_tensor_psi.dat"}})
+-- dense branch with given energy shifts
+S = CreateResonantSpectra(HX, H, {Tx, Ty}, {Txd}, {psi1, psi2}, opts({{"E0_1", -37.0}, {"E0_2", -17.0}}))
+S.Print({{"file", "dump/dense_shifts.dat"}})
+S = CreateResonantSpectra(HX, H, {Tx, Ty}, {Txd}, {psi1, psi2}, opts({{"E0", -30.0}}))
+S.Print({{"file", "dump/dense_e0.dat"}})
 print("rixs done")

@@ -1,0 +1,225 @@
+"""Host logic of CreateResonantSpectra and Eigensystem checked on the CPU against the
+reference's outputs: branch choice (dense below DenseBorder, Krylov otherwise), the bases of the
+dense branch, lists of operators and states, the spectrum order of every form, energy shifts,
+automatic energy ranges (including the zero eigenvalue of the reference's unused blocks in the
+Krylov tensor form) and Eigensystem's basis growth.
+
+Only the orchestration in quanty_gb300/api.py runs here: every device call it makes (bases,
+H*psi, dense operator matrices, the Lanczos recursions, the spectrum kernels) is replaced for
+the test by the oracle's CPU equivalent.  The device path itself is checked against the same
+fixtures by tests/test_gpu_rixs.py and tests/test_gpu_eigen.py."""
+import contextlib
+
+import numpy as np
+import pytest
+import torch
+
+from conftest import golden
+
+TOL = 1e-8
+
+
+def _oop(O, op):
+    return O.Op({"nf": op.nf, "terms": [[list(t[0]), t[1].real, t[1].imag] for t in op.terms]})
+
+
+class _Basis:
+    """A sorted determinant set standing in for a device basis."""
+
+    def __init__(self, O, api, nf, dets):
+        dets = np.asarray(dets, dtype=np.uint8).reshape(-1, api.nword(nf))
+        self.O, self.nf = O, nf
+        self.dets = np.unique(dets, axis=0) if len(dets) else dets
+        self.h = self
+        self.idx = {bytes(r): i for i, r in enumerate(self.dets)}
+
+    @property
+    def n(self):
+        return len(self.dets)
+
+    def find(self, d):
+        return np.array([self.idx[bytes(r)] for r in np.asarray(d).reshape(len(d), -1)], dtype=np.int64)
+
+    def dets_bytes(self):
+        return self.dets
+
+    def wf(self, v=None):
+        return self.O.WF(self.nf, self.dets, np.ones(self.n) if v is None else v)
+
+
+@pytest.fixture
+def host_api(monkeypatch, oracle_mod):
+    from quanty_gb300 import api
+    O = oracle_mod
+
+    def B(nf, dets):
+        return _Basis(O, api, nf, dets)
+
+    def apply_vec(T, dst, src, x):
+        out = np.zeros(dst.n, dtype=np.complex128)
+        if src.n:
+            w = O.operator_psi(_oop(O, T), src.wf(x))
+            for r, v in zip(w.det, w.val):
+                i = dst.idx.get(bytes(r))
+                if i is not None:
+                    out[i] += v
+        return out
+
+    class L:
+        def qg_apply(self, ctx, T, dst, src, x, y, k):
+            X, Y = x.numpy(), y.numpy()
+            for c in range(k):
+                Y[:dst.n, c] = apply_vec(T, dst, src, X[:src.n, c])
+            return 0
+
+    zeros, empty = torch.zeros, torch.empty
+
+    class Eng:
+        device, ctx = 0, None
+
+        def __init__(self):
+            self.torch, self.L = torch, L()
+
+        def check(self, st, ctx=None):
+            assert st == 0
+
+        def empty(self, n, nvec=1):
+            return zeros((max(n, 1), nvec), dtype=torch.complex128)
+
+        def on_stream(self):
+            return contextlib.nullcontext()
+
+        def to_host(self, t):
+            return t.numpy().copy()
+
+    def plain_lanczos(H, b, x, ntri, eps, gamma, eng=None, krylov=None):
+        """Three-term recursion without truncation, as the device runs it at Epsilon 0."""
+        X = x.numpy()
+        M = O.dense_matrix(_oop(O, H), b.wf())
+        A, Bv = [], []
+        for c in range(X.shape[1]):
+            v0 = X[:b.n, c]
+            a, bb = np.zeros(ntri + 1), np.zeros(ntri)
+            bb[0] = np.linalg.norm(v0)
+            v = v0 / bb[0] if bb[0] > 0 else 0 * v0
+            vp, bp = 0 * v0, 0.0
+            for i in range(ntri):
+                if krylov is not None:
+                    krylov.numpy()[i, :b.n, c] = v
+                w = M @ v
+                a[i + 1] = np.vdot(v, w).real
+                w = w - a[i + 1] * v - bp * vp
+                if i + 1 < ntri:
+                    nb = np.linalg.norm(w)
+                    bb[i + 1] = nb
+                    vp, v, bp = v, (w / nb if nb > 100 * np.finfo(float).tiny else 0 * w), nb
+            A.append(a)
+            Bv.append(bb)
+        return np.array(A), np.array(Bv)
+
+    def poles(E0, p, W, emin, emax, ne, g, eng=None):
+        W = np.atleast_2d(W)
+        P = np.broadcast_to(np.atleast_2d(p), W.shape)
+        E = np.broadcast_to(np.asarray(E0, float), (W.shape[0],))
+        return np.array([O.poles_spectrum(P[s], W[s], E[s], emin, (emax - emin) / ne, ne, g)
+                         for s in range(W.shape[0])])
+
+    def cf(E0, A, Bv, emin, emax, ne, g, eng=None):
+        E = np.broadcast_to(np.asarray(E0, float), (len(A),))
+        return np.array([O.cf_spectrum(A[s], Bv[s], E[s], emin, (emax - emin) / ne, ne, g) for s in range(len(A))])
+
+    def eigh(M, nv=None, eng=None):
+        w, v = np.linalg.eigh(0.5 * (M + M.conj().T))
+        return w, v[:, :(len(w) if nv is None else nv)]
+
+    def opsi(T, p, R=None, eng=None):
+        w = O.operator_psi(_oop(O, T), O.WF(p.nf, p.det, p.val), api.parse_restrictions(R))
+        return api.Wavefunction(p.nf, w.det, w.val)
+
+    def closure_of(H, s, R=None, m=-1, eng=None):
+        if not s.n:
+            return s
+        return B(s.nf, O.closure(_oop(O, H), s.wf(), api.parse_restrictions(R)).det)
+
+    def krylov_one(H1, H2, T, T2s, p, o, eng):
+        G = O.resonant_spectra(_oop(O, H1), _oop(O, H2), _oop(O, T), [_oop(O, t) for t in T2s],
+                               O.WF(p.nf, p.det, p.val), dict(o, Restrictions1=None, Restrictions2=None))
+        return G, {"emin2": o["Emin2"], "emax2": o["Emax2"]}
+
+    monkeypatch.setattr(torch.Tensor, "to", lambda self, *a, **k: self)
+    monkeypatch.setattr(torch, "zeros", lambda *a, **k: zeros(*a, **{x: y for x, y in k.items() if x != "device"}))
+    monkeypatch.setattr(torch, "empty", lambda *a, **k: empty(*a, **{x: y for x, y in k.items() if x != "device"}))
+    monkeypatch.setattr(api, "_engine", Eng())
+    monkeypatch.setattr(api, "_ptr", lambda a: a)
+    monkeypatch.setattr(api.Operator, "handle", lambda self, eng=None: self)
+    monkeypatch.setattr(api.Basis, "from_bytes", classmethod(lambda cls, nf, d, eng=None: (B(nf, d), None)))
+    monkeypatch.setattr(api, "OperatorPsiBasis", lambda T, b, R=None, eng=None: B(b.nf, opsi(T, api.Wavefunction(
+        b.nf, b.dets, np.ones(b.n)), R).det))
+    monkeypatch.setattr(api, "basis_union", lambda a, b, eng=None: B(a.nf, np.concatenate([a.dets, b.dets])))
+    monkeypatch.setattr(api, "closure_of", closure_of)
+    monkeypatch.setattr(api, "closure", lambda H, d, nf, R=None, m=-1, eng=None: closure_of(H, B(nf, d), R))
+    monkeypatch.setattr(api, "OperatorPsi", opsi)
+    monkeypatch.setattr(api, "PsiOperatorPsi",
+                        lambda H, p, eng=None: O.expectation(_oop(O, H), O.WF(p.nf, p.det, p.val)))
+    monkeypatch.setattr(api, "OperatorToDeterminantMatrix", lambda H, b, eng=None: O.dense_matrix(_oop(O, H), b.wf()))
+    monkeypatch.setattr(api, "hermitian_eigh", eigh)
+    monkeypatch.setattr(api, "_apply_between", lambda T, dst, src, X, eng: np.stack(
+        [apply_vec(T, dst, src, X[:, c]) for c in range(X.shape[1])], 1) if X.shape[1] else np.zeros((dst.n, 0)))
+    monkeypatch.setattr(api, "ListOfPolesToSpectrum", poles)
+    monkeypatch.setattr(api, "lanczos_block", plain_lanczos)
+    monkeypatch.setattr(api, "TriDiagonalMatrixToSpectrum", cf)
+    monkeypatch.setattr(api, "_rixs_krylov", krylov_one)
+    return api
+
+
+GRID = {"Emin1": -5, "Emax1": 15, "NE1": 4, "Gamma1": 0.8, "Emin2": -2, "Emax2": 8, "NE2": 64, "Gamma2": 0.3}
+KRYLOV = {"DenseBorder": 0, "Epsilon": 0.0}
+CASES = [
+    # key, T1, T2, number of initial states, options, branch
+    ("dense_lists", ("Tx", "Ty"), ("Txd", "Tyd", "Tzd"), 2, GRID, "dense"),
+    ("dense_auto", ("Tx",), ("Txd", "Tyd"), 1, {"NE1": 4, "Gamma1": 0.8, "NE2": 64, "Gamma2": 0.3}, "dense"),
+    ("dense_tensor", ("Tx", "Ty"), ("Txd", "Tyd"), 1, dict(GRID, Tensor=True), "dense"),
+    ("dense_tensor_psi", ("Tx",), ("Tyd",), 2, dict(GRID, Tensor=True), "dense"),
+    ("dense_shifts", ("Tx", "Ty"), ("Txd",), 2, dict(GRID, E0_1=-37.0, E0_2=-17.0), "dense"),
+    ("dense_e0", ("Tx", "Ty"), ("Txd",), 2, dict(GRID, E0=-30.0), "dense"),
+    ("krylov_lists", ("Tx", "Ty"), ("Txd", "Tyd"), 2, dict(GRID, **KRYLOV), "krylov"),
+    ("krylov_tensor", ("Tx", "Ty"), ("Txd", "Tyd"), 1, dict(GRID, Tensor=True, NTri1=40, NTri2=40, **KRYLOV),
+     "krylov_tensor"),
+    ("krylov_tensor_auto", ("Tx", "Ty"), ("Txd",), 1,
+     dict(KRYLOV, NE1=3, NE2=48, Tensor=True, NTri1=40, NTri2=40), "krylov_tensor"),
+    ("krylov_tensor_psi", ("Tx",), ("Tyd",), 2, dict(GRID, Tensor=True, NTri1=40, NTri2=40, **KRYLOV),
+     "krylov_tensor"),
+]
+
+
+@pytest.mark.parametrize("key,t1,t2,npsi,opts,branch", CASES, ids=[c[0] for c in CASES])
+def test_resonant_spectra_orchestration_matches_reference(host_api, key, t1, t2, npsi, opts, branch):
+    api = host_api
+    g = golden("rixs.json")
+    op = lambda k: api.Operator.from_fixture(g[k])  # noqa: E731
+    psis = [api.Wavefunction.from_fixture(p) for p in g["psi"][:npsi]]
+    G, st = api.CreateResonantSpectra(op("HX"), op("H"), [op(t) for t in t1], [op(t) for t in t2],
+                                      psis if npsi > 1 else psis[0], dict(opts))
+    ref = g[key]
+    R = np.array(ref["re"]) + 1j * np.array(ref["im"])
+    assert st["method"] == branch
+    assert G.shape == R.shape
+    assert np.max(np.abs(G - R)) / np.max(np.abs(R)) < TOL
+    assert abs(st["emin2"] - ref["emin"]) < 1e-10 and abs(st["emax2"] - ref["emax"]) < 1e-10
+    if "gamma2" in st:
+        assert abs(st["gamma2"] - ref["gamma"]) < 1e-10
+
+
+def test_eigensystem_growth_and_call_forms(host_api):
+    """Growth beyond the start restrictions without the Restrictions option, confinement with
+    it, and the start-state call form, against the reference's energies."""
+    api = host_api
+    g = golden("eigen_growth.json")
+    H = api.Operator.from_fixture(golden("c1_lf.json")["H"])
+    Rn = [26, 0] + [list(r) for r in g["start_restrictions"]]
+    _, E = api.Eigensystem(H, Rn, 3)
+    assert np.max(np.abs(np.array(E) - g["energies_grown"])) < 1e-10
+    psis, E = api.Eigensystem(H, Rn, 3, {"Restrictions": Rn})
+    assert np.max(np.abs(np.array(E) - g["energies_confined"])) < 1e-10
+    out, E = api.Eigensystem(H, psis)
+    assert len(out) == 3 and np.max(np.abs(np.array(E) - g["energies_from_states"])) < 1e-10
