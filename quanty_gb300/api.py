@@ -511,7 +511,8 @@ def _opts(options):
     if options:
         items = options.items() if isinstance(options, dict) else options
         for k, v in items:
-            k = {"epsilon": "Epsilon", "restrictions": "Restrictions", "zero": "Zero"}.get(k, k)
+            k = {"epsilon": "Epsilon", "restrictions": "Restrictions", "zero": "Zero",
+                 "restrictions1": "Restrictions1", "restrictions2": "Restrictions2"}.get(k, k)
             o[k] = v
     return o
 

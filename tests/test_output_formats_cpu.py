@@ -90,3 +90,13 @@ def test_spectra_method_options_follow_the_reference():
         m(Method="Mesh")
     with pytest.raises(ValueError, match="unknown Method"):  # checked before the GPU is needed
         api.CreateSpectra(None, [], [], {"Method": "Arnoldi"})
+
+
+def test_option_names_accept_the_reference_aliases():
+    """Lower-case option names the reference's option tables also accept
+    (LuaInterface/ssp.cpp:1958-1980, :3118-3125, :4063-4075)."""
+    from quanty_gb300 import api
+    o = api._opts({"epsilon": 0.0, "zero": 1e-12, "restrictions": [1], "restrictions1": [2], "restrictions2": [3]})
+    assert (o["Epsilon"], o["Zero"], o["Restrictions"], o["Restrictions1"], o["Restrictions2"]) == (0.0, 1e-12, [1], [2], [3])
+    o = api._opts([("NE", 10), ("Gamma", 0.2)])  # the ordered-pairs form of a Lua option table
+    assert o["NE"] == 10 and o["Gamma"] == 0.2 and o["NTri"] == 200
