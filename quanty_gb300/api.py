@@ -606,9 +606,10 @@ def ListOfPolesToSpectrum(E0, poles, weights, Emin, Emax, NE, Gamma, eng=None):
     return (g[0::2] + 1j * g[1::2]).reshape(ns, NE + 1)
 
 
-def _spectra_dense(H, Tpsi, e0, o, basis, eng):
+def _spectra_dense(H, Tpsi, e0, o, basis, eng, states=False):
     """CreateSpectra's dense branch (LuaInterface/ssp.cpp:2347-2460): the eigensystem of H on
-    the union basis, poles at its eigenvalues with weights |<E_k|T psi>|^2."""
+    the union basis, poles at its eigenvalues with weights |<E_k|T psi>|^2.  With states=True
+    (the KrylovBasis option, :2538-2580) the eigenstates come back as a third result."""
     n = basis.n
     w, V = hermitian_eigh(OperatorToDeterminantMatrix(H, basis, eng), n, eng)
     X = np.zeros((n, len(Tpsi)), dtype=np.complex128)
@@ -623,6 +624,9 @@ def _spectra_dense(H, Tpsi, e0, o, basis, eng):
     emin, emax, gamma = _default_window(lo, hi, o["Emin"], o["Emax"], float(o["Gamma"]), NE)
     G = ListOfPolesToSpectrum(np.asarray(e0), np.tile(w, (len(Tpsi), 1)), Wt.T, emin, emax, NE, gamma, eng)
     poles = [(w - e0[s], Wt[:, s].copy()) for s in range(len(Tpsi))]
+    if states:
+        db = basis.dets_bytes()
+        return Spectra(G, emin, emax, NE, gamma, lo, hi), poles, [Wavefunction(H.nf, db, V[:, k]) for k in range(n)]
     return Spectra(G, emin, emax, NE, gamma, lo, hi), poles
 
 
@@ -754,16 +758,22 @@ def CreateSpectra(H, T, psi, options=None, eng=None, batched=True):
     ordered iT*Npsi + ipsi.  Lanczos branch (:2586-2720): returns (Spectra, [(a, b) shifted by
     -E0]); batched=True runs all pairs as one multi-vector Lanczos with every step on the
     device.  Dense branch (:2347-2460; Method "Dense", or a union basis within DenseBorder
-    unless Method is "Lanczos"): returns (Spectra, [(poles - E0, weights)])."""
+    unless Method is "Lanczos"): returns (Spectra, [(poles - E0, weights)]).  KrylovBasis adds a
+    third result: the Lanczos branch's Krylov vectors of every pair (the reference's Krylov-basis
+    Lanczos, LanczosTriDiagonalizeKrylov, Core/Lanczos.cpp:5405; empty vectors left out; one list
+    for one pair, else a list per pair, :2729-2745), or the dense branch's eigenstates of H."""
     o = _opts(options)
     method = _spectra_method(o)
+    krylov = bool(o.get("KrylovBasis"))
+    if krylov and o.get("Tensor"):
+        raise NotImplementedError("CreateSpectra: KrylovBasis with Tensor (a block Krylov basis) is not supported")
     eng = eng or engine()
     Ts = T if isinstance(T, (list, tuple)) else [T]
     psis = psi if isinstance(psi, (list, tuple)) else [psi]
     ntri, eps = int(o["NTri"]), float(o["Epsilon"])
     R = parse_restrictions(o.get("Restrictions"))
     gamma = float(o["Gamma"])
-    if batched and not o.get("Tensor") and method != "dense":
+    if batched and not o.get("Tensor") and method != "dense" and not krylov:
         got = _batched_lanczos_device(H, Ts, psis, o, R, eng)
         if got is not None:
             A, B, E0 = got
@@ -783,11 +793,12 @@ def CreateSpectra(H, T, psi, options=None, eng=None, batched=True):
         seed = np.concatenate([t.det for t in Tpsi if t.N] or [np.zeros((0, nword(H.nf)), np.uint8)])
         ub = closure(H, seed, H.nf, R, -1, eng) if len(seed) else None
         if ub is not None and (method == "dense" or ub.n <= int(o["DenseBorder"])):
-            return _spectra_dense(H, Tpsi, e0, o, ub, eng)
+            return _spectra_dense(H, Tpsi, e0, o, ub, eng, states=krylov)
     # the plain path: one Lanczos per pair on the closure of its own T psi, as the reference
     # runs them; an empty T psi has a zero spectrum (all coefficients zero)
     A = np.zeros((len(Tpsi), ntri + 1))
     B = np.zeros((len(Tpsi), ntri))
+    vectors = [[] for _ in Tpsi]
     for i in range(len(Tpsi)):
         if Tpsi[i].N == 0:
             continue
@@ -796,10 +807,35 @@ def CreateSpectra(H, T, psi, options=None, eng=None, batched=True):
         xs = _upload(eng, src, perm, Tpsi[i].val)
         x = eng.empty(basis.n)
         eng.check(eng.L.qg_basis_map(eng.ctx, src.h, _ptr(xs), basis.h, _ptr(x), 1))
+        if krylov:
+            vectors[i], A[i], B[i] = _krylov_vectors(H, basis, x, ntri, eps, eng)
+            continue
         a, b = lanczos_block(H, basis, x, ntri, eps, max(gamma, eps), eng)
         A[i] = a[0]
         B[i] = b[0]
-    return _lanczos_spectra(A, B, e0, o, gamma, ntri, eng)
+    out = _lanczos_spectra(A, B, e0, o, gamma, ntri, eng)
+    if krylov:
+        return out + (vectors[0] if len(vectors) == 1 else vectors,)
+    return out
+
+
+def _krylov_vectors(H, basis, x, ntri, eps, eng):
+    """The reference's Krylov-basis Lanczos on the device (qg_lanczos_krylov: full
+    reorthogonalisation, orthogonality test, truncation): its non-empty vectors as
+    wavefunctions (zero amplitudes left out, as the reference's truncated vectors), a and b."""
+    with eng.on_stream():
+        K = eng.torch.zeros((ntri, basis.n), dtype=eng.torch.complex128, device="cuda:%d" % eng.device)
+    a = np.zeros(ntri + 1)
+    b = np.zeros(ntri)
+    eng.check(eng.L.qg_lanczos_krylov(eng.ctx, H.handle(eng), basis.h, _ptr(x), ntri, eps, _ptr(a), _ptr(b), _ptr(K)))
+    Kh = eng.to_host(K)
+    db = basis.dets_bytes()
+    out = []
+    for k in range(ntri):
+        nz = np.flatnonzero(Kh[k])
+        if len(nz):
+            out.append(Wavefunction(H.nf, db[nz], Kh[k][nz]))
+    return out, a, b
 
 
 def _batched_lanczos_device(H, Ts, psis, o, R, eng):

@@ -309,9 +309,26 @@ def gen_eigen_growth():
     save("eigen_growth.json", out)
 
 
+def gen_krylov_basis():
+    """CreateSpectra with KrylovBasis: the Krylov vectors of the Lanczos branch (one pair, and
+    lists at Epsilon 0) and the eigenstate energies of the dense branch."""
+    head = open(os.path.join(HERE, "gen", "rixs.lua")).read().splitlines()[:28]
+    tail = open(os.path.join(HERE, "gen", "krylov_basis.lua")).read()
+    work = run("\n".join(head) + "\n" + tail, "krylov_basis.lua")
+    out = {"source": "tests/golden/gen/rixs.lua:1-28 + tests/golden/gen/krylov_basis.lua", "Tz": op(work, "Tz")}
+    n1 = int(reals(work, "count_one.txt")[0])
+    out["krylov_one"] = [wf(work, "kone%d" % i) for i in range(1, n1 + 1)]
+    counts = [int(x) for x in reals(work, "count_lists.txt")]
+    out["krylov_lists"] = [[wf(work, "klist%dx%d" % (p, i)) for i in range(1, c + 1)] for p, c in enumerate(counts, 1)]
+    out["dense_energies"] = reals(work, "dense_energies.txt")
+    for k in ("lanczos_one", "lanczos_lists", "dense_states"):
+        out[k] = spectra(work, k + ".dat")
+    save("krylov_basis.json", out)
+
+
 if __name__ == "__main__":
     if not os.path.exists(QUANTY):
         sys.exit("build the reference first: oracle/build_ref.sh")
-    which = sys.argv[1:] or ["hpsi", "c0", "c1", "chain", "fshell", "print", "tensor", "rixs", "eigen_growth"]
+    which = sys.argv[1:] or ["hpsi", "c0", "c1", "chain", "fshell", "print", "tensor", "rixs", "eigen_growth", "krylov_basis"]
     for w in which:
         globals()["gen_" + w]()

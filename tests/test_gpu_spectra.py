@@ -191,3 +191,29 @@ def test_lanczos_with_stored_krylov_vectors(api):
     torch.cuda.synchronize()
     G = (K[:6].conj() @ K[:6].T).cpu().numpy()
     assert np.max(np.abs(G - np.eye(6))) < 1e-10
+
+
+def test_krylov_basis_option(api):
+    """CreateSpectra with KrylovBasis: the Lanczos branch returns the reference's non-empty
+    Krylov vectors (LanczosTriDiagonalizeKrylov; their count and the leading ones element by
+    element, 1e-10) with its spectra (1e-8); the dense branch returns the eigenstates of H
+    (energies 1e-10 eV)."""
+    g = golden("krylov_basis.json")
+    r = golden("rixs.json")
+    HX, Tz = api.Operator.from_fixture(r["HX"]), api.Operator.from_fixture(g["Tz"])
+    psi1 = api.Wavefunction.from_fixture(r["psi"][0])
+    o = {"NE": 32, "Emin": -10, "Emax": 20, "Gamma": 0.5}
+    ref = np.array(g["lanczos_one"]["re"]) + 1j * np.array(g["lanczos_one"]["im"])
+    S, tri, K = api.CreateSpectra(HX, Tz, psi1, dict(o, Method="Lanczos", KrylovBasis=True, NTri=80))
+    assert spec_err(S.G, ref) < SPEC_TOL
+    assert len(K) == len(g["krylov_one"])
+    for fx, k in list(zip(g["krylov_one"], K))[:12]:
+        R = api.Wavefunction.from_fixture(fx)
+        d = {bytes(x): v for x, v in zip(k.det, k.val)}
+        assert len(k.val) == len(R.val)
+        assert np.max(np.abs(np.array([d[bytes(x)] for x in R.det]) - R.val)) < 1e-10 * np.max(np.abs(R.val))
+    ref = np.array(g["dense_states"]["re"]) + 1j * np.array(g["dense_states"]["im"])
+    S, poles, K = api.CreateSpectra(HX, Tz, psi1, dict(o, Method="Dense", KrylovBasis=True))
+    assert spec_err(S.G, ref) < SPEC_TOL
+    E = np.array([api.PsiOperatorPsi(HX, k).real for k in K])
+    assert len(E) == len(g["dense_energies"]) and np.max(np.abs(E - np.array(g["dense_energies"]))) < 1e-10

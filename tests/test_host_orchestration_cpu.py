@@ -1,8 +1,9 @@
-"""Host logic of CreateResonantSpectra and Eigensystem checked on the CPU against the
-reference's outputs: branch choice (dense below DenseBorder, Krylov otherwise), the bases of the
-dense branch, lists of operators and states, the spectrum order of every form, energy shifts,
-automatic energy ranges (including the zero eigenvalue of the reference's unused blocks in the
-Krylov tensor form) and Eigensystem's basis growth.
+"""Host logic of CreateResonantSpectra, Eigensystem and CreateSpectra's KrylovBasis option
+checked on the CPU against the reference's outputs: branch choice (dense below DenseBorder,
+Krylov otherwise), the bases of the dense branch, lists of operators and states, the spectrum
+order of every form, energy shifts, automatic energy ranges (including the zero eigenvalue of
+the reference's unused blocks in the Krylov tensor form), Eigensystem's basis growth and the
+vectors KrylovBasis returns.
 
 Only the orchestration in quanty_gb300/api.py runs here: every device call it makes (bases,
 H*psi, dense operator matrices, the Lanczos recursions, the spectrum kernels) is replaced for
@@ -66,6 +67,21 @@ def host_api(monkeypatch, oracle_mod):
         return out
 
     class L:
+        def qg_basis_map(self, ctx, src, xs, dst, x, k):
+            X, Xs = x.numpy(), xs.numpy()
+            for r, d in enumerate(src.dets):
+                X[dst.idx[bytes(d)], :k] = Xs[r, :k]
+            return 0
+
+        def qg_lanczos_krylov(self, ctx, H, b, x, ntri, eps, a, bb, K):
+            aa, b2, Ks = O.lanczos_krylov(_oop(O, H), b.wf(x.numpy()[:b.n, 0]), ntri, eps)
+            a[:], bb[:] = aa, b2
+            Kn = K.numpy()
+            for i, w in enumerate(Ks):
+                for r, v in zip(w.det, w.val):
+                    Kn[i, b.idx[bytes(r)]] += v
+            return 0
+
         def qg_apply(self, ctx, T, dst, src, x, y, k):
             X, Y = x.numpy(), y.numpy()
             for c in range(k):
@@ -152,7 +168,11 @@ def host_api(monkeypatch, oracle_mod):
     monkeypatch.setattr(api, "_engine", Eng())
     monkeypatch.setattr(api, "_ptr", lambda a: a)
     monkeypatch.setattr(api.Operator, "handle", lambda self, eng=None: self)
-    monkeypatch.setattr(api.Basis, "from_bytes", classmethod(lambda cls, nf, d, eng=None: (B(nf, d), None)))
+    def from_bytes(cls, nf, d, eng=None):
+        b = B(nf, d)
+        return b, b.find(d)
+
+    monkeypatch.setattr(api.Basis, "from_bytes", classmethod(from_bytes))
     monkeypatch.setattr(api, "OperatorPsiBasis", lambda T, b, R=None, eng=None: B(b.nf, opsi(T, api.Wavefunction(
         b.nf, b.dets, np.ones(b.n)), R).det))
     monkeypatch.setattr(api, "basis_union", lambda a, b, eng=None: B(a.nf, np.concatenate([a.dets, b.dets])))
@@ -223,3 +243,47 @@ def test_eigensystem_growth_and_call_forms(host_api):
     assert np.max(np.abs(np.array(E) - g["energies_confined"])) < 1e-10
     out, E = api.Eigensystem(H, psis)
     assert len(out) == 3 and np.max(np.abs(np.array(E) - g["energies_from_states"])) < 1e-10
+
+
+def _wf_err(api, ref, got):
+    R = api.Wavefunction.from_fixture(ref)
+    d = {bytes(r): v for r, v in zip(got.det, got.val)}
+    assert len(got.val) == len(R.val)
+    v = np.array([d[bytes(r)] for r in R.det])
+    return np.max(np.abs(v - R.val)) / np.max(np.abs(R.val))
+
+
+def test_krylov_basis_option(host_api):
+    """KrylovBasis: the Lanczos branch returns the reference's Krylov vectors (the count of
+    non-empty ones, and the leading ones element by element; later ones depend on rounding
+    that the recursion amplifies) with unchanged spectra, a list per pair for several pairs
+    (at Epsilon 0 the orthogonality test keeps one vector each); the dense branch returns the
+    eigenstates of H."""
+    import math
+    api = host_api
+    g = golden("krylov_basis.json")
+    r = golden("rixs.json")
+    HX, Tx, Tz = (api.Operator.from_fixture(d) for d in (r["HX"], r["Tx"], g["Tz"]))
+    psi1, psi2 = (api.Wavefunction.from_fixture(p) for p in r["psi"])
+    o = {"NE": 32, "Emin": -10, "Emax": 20, "Gamma": 0.5}
+
+    def spec(key):
+        return np.array(g[key]["re"]) + 1j * np.array(g[key]["im"])
+
+    S, tri, K = api.CreateSpectra(HX, Tz, psi1, dict(o, Method="Lanczos", KrylovBasis=True, NTri=80))
+    assert np.max(np.abs(S.G - spec("lanczos_one"))) / np.max(np.abs(spec("lanczos_one"))) < TOL
+    assert len(K) == len(g["krylov_one"])
+    for ref, got in list(zip(g["krylov_one"], K))[:12]:
+        assert _wf_err(api, ref, got) < 1e-10
+    S, tri, K = api.CreateSpectra(HX, [Tx, Tz], [psi1, psi2],
+                                  dict(o, Method="Lanczos", KrylovBasis=True, NTri=80, Epsilon=0.0))
+    assert np.max(np.abs(S.G - spec("lanczos_lists"))) / np.max(np.abs(spec("lanczos_lists"))) < TOL
+    assert [len(k) for k in K] == [len(k) for k in g["krylov_lists"]]
+    for refs, got in zip(g["krylov_lists"], K):
+        for ref, k in zip(refs, got):
+            assert _wf_err(api, ref, k) < 1e-12
+    S, poles, K = api.CreateSpectra(HX, Tz, psi1, dict(o, Method="Dense", KrylovBasis=True))
+    assert np.max(np.abs(S.G - spec("dense_states"))) / np.max(np.abs(spec("dense_states"))) < TOL
+    E = [api.PsiOperatorPsi(HX, k).real for k in K]
+    assert len(E) == len(g["dense_energies"]) and np.max(np.abs(np.array(E) - g["dense_energies"])) < 1e-10
+    assert math.isclose(np.linalg.norm(K[0].val), 1.0, rel_tol=1e-12)

@@ -309,3 +309,23 @@ def test_eigensystem_growth_matches_reference(oracle_mod):
     for key, R in (("energies_grown", None), ("energies_confined", g["start_restrictions"])):
         w, _ = O.exact_eigensystem(H, O.closure(H, seed, R), 3)
         assert np.max(np.abs(w - np.array(g[key]))) < 1e-10, key
+
+
+def test_krylov_basis_matches_reference(oracle_mod):
+    """The Krylov-basis Lanczos (LanczosTriDiagonalizeKrylov, Core/Lanczos.cpp:5405) restated:
+    the reference's non-empty Krylov vectors of CreateSpectra's KrylovBasis option (their count,
+    the leading ones element by element) and, for the dense branch, the eigenstate energies."""
+    O = oracle_mod
+    g = golden("krylov_basis.json")
+    r = golden("rixs.json")
+    HX = O.Op(r["HX"])
+    t = O.operator_psi(O.Op(g["Tz"]), O.WF.from_fixture(r["psi"][0]))
+    a, b, K = O.lanczos_krylov(HX, t, 80, EPS_DEFAULT)
+    K = [k for k in K if len(k.val) and np.any(k.val != 0)]
+    assert len(K) == len(g["krylov_one"])
+    for ref, k in list(zip(g["krylov_one"], K))[:12]:
+        R = O.WF.from_fixture(ref)
+        d = k.as_dict()
+        assert rel_err([d[bytes(x)] for x in R.det], R.val) < 1e-10
+    w, _ = O.exact_eigensystem(HX, O.closure(HX, t), len(g["dense_energies"]))
+    assert np.max(np.abs(w - np.array(g["dense_energies"]))) < 1e-10
