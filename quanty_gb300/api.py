@@ -257,6 +257,8 @@ def NewOperator(nf, nb, terms):
 class Wavefunction:
     """Determinants (reference byte layout) with complex FP64 amplitudes."""
 
+    __array_ufunc__ = None  # numpy scalars defer to the arithmetic below
+
     def __init__(self, nf, det_bytes, values):
         self.nf = int(nf)
         self.det = np.ascontiguousarray(det_bytes, dtype=np.uint8).reshape(-1, nword(nf))
@@ -294,6 +296,77 @@ class Wavefunction:
 
     def norm(self):
         return float(np.linalg.norm(self.val))
+
+    # ------------------------------------------------------------- arithmetic (host side)
+    # The reference's Lua metamethods (LuaInterface/Wavefunction.cpp:1-440): sums on the union
+    # basis, scaling by numbers, <a|b> for two wavefunctions, O|psi> and <psi|O = O^dag|psi>.
+
+    def _keys(self):
+        return np.ascontiguousarray(self.det).view(np.dtype((np.void, self.det.shape[1]))).ravel()
+
+    def _union_add(self, other, c):
+        """self + c * other on the union basis, self's determinants first, then the new ones of
+        other in their order (WaveFunctionAddUnionBasis)."""
+        if not isinstance(other, Wavefunction):
+            return NotImplemented
+        if other.nf != self.nf:
+            raise ValueError("adding wavefunctions with %d and %d fermions" % (self.nf, other.nf))
+        dets = np.concatenate([self.det, other.det])
+        keys = np.ascontiguousarray(dets).view(np.dtype((np.void, dets.shape[1]))).ravel()
+        _, first, inv = np.unique(keys, return_index=True, return_inverse=True)
+        order = np.argsort(first, kind="stable")
+        rank = np.empty_like(order)
+        rank[order] = np.arange(len(order))
+        vals = np.zeros(len(order), dtype=np.complex128)
+        np.add.at(vals, rank[inv.ravel()], np.concatenate([self.val, c * other.val]))
+        return Wavefunction(self.nf, dets[first[order]], vals)
+
+    def dot(self, other):
+        """<self|other>, the left side conjugated (WaveFunctionDotProduct); a real number when
+        the imaginary part is below 10 (DBL_EPSILON |Re| + DBL_MIN), as the reference returns."""
+        if other.nf != self.nf:
+            raise ValueError("dot product of wavefunctions with %d and %d fermions" % (self.nf, other.nf))
+        _, ia, ib = np.intersect1d(self._keys(), other._keys(), assume_unique=True, return_indices=True)
+        d = complex(np.sum(np.conj(self.val[ia]) * other.val[ib]))
+        if abs(d.imag) < 10 * (DBL_EPSILON * abs(d.real) + np.finfo(float).tiny):
+            return d.real
+        return d
+
+    def __add__(self, other):
+        if isinstance(other, (list, tuple)):
+            return [self + o for o in other]
+        return self._union_add(other, 1.0)
+
+    def __sub__(self, other):
+        if isinstance(other, (list, tuple)):
+            return [self - o for o in other]
+        return self._union_add(other, -1.0)
+
+    def __neg__(self):
+        return Wavefunction(self.nf, self.det, -self.val)
+
+    def __mul__(self, other):
+        if isinstance(other, (list, tuple)):
+            return [self * o for o in other]
+        if isinstance(other, Wavefunction):
+            return self.dot(other)
+        if isinstance(other, Operator):
+            return OperatorPsi(other.dagger(), self)  # <psi|O as the ket O^dag|psi>
+        if isinstance(other, (int, float, complex, np.number)):
+            return Wavefunction(self.nf, self.det, self.val * other)
+        return NotImplemented
+
+    def __rmul__(self, other):
+        if isinstance(other, (list, tuple)):
+            return [o * self for o in other]
+        if isinstance(other, (int, float, complex, np.number)):
+            return Wavefunction(self.nf, self.det, other * self.val)
+        return NotImplemented
+
+    def __truediv__(self, other):
+        if isinstance(other, (int, float, complex, np.number)):
+            return Wavefunction(self.nf, self.det, self.val / other)
+        return NotImplemented
 
 
 def NewWavefunction(nf, nb, entries):

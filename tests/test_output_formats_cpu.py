@@ -100,3 +100,36 @@ def test_option_names_accept_the_reference_aliases():
     assert (o["Epsilon"], o["Zero"], o["Restrictions"], o["Restrictions1"], o["Restrictions2"]) == (0.0, 1e-12, [1], [2], [3])
     o = api._opts([("NE", 10), ("Gamma", 0.2)])  # the ordered-pairs form of a Lua option table
     assert o["NE"] == 10 and o["Gamma"] == 0.2 and o["NTri"] == 200
+
+
+def test_wavefunction_arithmetic_follows_the_reference(monkeypatch):
+    """The Lua metamethods of wavefunctions (LuaInterface/Wavefunction.cpp): sums on the union
+    basis in the reference's order (left operand's determinants first), scaling by real and
+    complex numbers, <a|b> with the left side conjugated and returned as a real number when its
+    imaginary part vanishes, <psi|O as O^dag|psi>, and the elementwise forms over lists."""
+    import numpy as np
+    from quanty_gb300 import api
+    from oracle import oracle as O
+    from conftest import golden
+    g = golden("rixs.json")
+    p1, p2 = (api.Wavefunction.from_fixture(p) for p in g["psi"])
+    t = api.Wavefunction(16, p2.det[::3], np.linspace(1, 2, len(p2.det[::3])) * 1j)
+    for a, b, c in ((p1, p2, 0.5), (p1, t, -2.0), (t, p1, 1.5 - 0.5j)):
+        s = a + c * b
+        ref = O.linear_combination(16, [O.WF(16, a.det, a.val), O.WF(16, b.det, b.val)], [1.0, c])
+        assert np.array_equal(s.det, ref.det) and np.allclose(s.val, ref.val, rtol=0, atol=1e-15)
+        d = a * b
+        want = sum(np.conj(x) * ref_b for x, ref_b in
+                   ((a.as_dict()[k], b.as_dict()[k]) for k in a.as_dict() if k in b.as_dict()))
+        assert abs(d - want) < 1e-14
+    assert isinstance(p1 * p1, float) and abs(p1 * p1 - 1) < 1e-12
+    assert isinstance(p1 * (1j * p1), complex) and abs((p1 * (1j * p1)) - 1j) < 1e-12
+    assert np.allclose((p1 - p1).val, 0) and np.allclose((-p1).val, -p1.val)
+    assert np.allclose((np.float64(2.0) * p1).val, 2 * p1.val) and np.allclose((p1 / 4).val, p1.val / 4)
+    assert [w.N for w in p1 + [p1, t]] == [p1.N, (p1 + t).N]
+    seen = {}
+    monkeypatch.setattr(api, "OperatorPsi", lambda O_, psi: seen.setdefault("call", (O_, psi)))
+    Tz = api.Operator.from_fixture(golden("krylov_basis.json")["Tz"])
+    p1 * Tz
+    O_, psi = seen["call"]
+    assert psi is p1 and O_.terms == Tz.dagger().terms
