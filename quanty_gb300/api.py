@@ -468,7 +468,11 @@ def OperatorPsiBasis(O, basis, restrictions=None, eng=None):
 
 def OperatorPsi(O, psi, restrictions=None, eng=None):
     """O|psi> with basis growth (reference OperatorPsi / OperatorPsiRestricted).  The output
-    determinants are the targets of all non-zero (determinant, term) pairs, in sorted order."""
+    determinants are the targets of all applicable (determinant, string) pairs, in sorted
+    order.  Strings whose value is zero (the constant of the common "O = 0; O = O + ..." or a
+    cancelled sum) reach their targets too, with amplitude 0, as in the reference, which
+    inserts every applicable target whatever the value; the device growth leaves them out and
+    they are added here on the host."""
     eng = eng or engine()
     if O.nf != psi.nf:
         raise ValueError("operator and wavefunction have different numbers of fermions")
@@ -477,7 +481,43 @@ def OperatorPsi(O, psi, restrictions=None, eng=None):
     dst = OperatorPsiBasis(O, src, restrictions, eng)
     y = eng.empty(dst.n)
     eng.check(eng.L.qg_apply(eng.ctx, O.handle(eng), dst.h, src.h, _ptr(x), _ptr(y), 1))
-    return Wavefunction(psi.nf, dst.dets_bytes(), eng.to_host(y[:dst.n, 0]))
+    dets, vals = dst.dets_bytes(), eng.to_host(y[:dst.n, 0])
+    extra = _zero_term_targets(O, psi.det, parse_restrictions(restrictions))
+    if len(extra):
+        both = np.concatenate([np.asarray(dets, dtype=np.uint8).reshape(-1, nword(psi.nf)), extra])
+        dets, first, inv = np.unique(both, axis=0, return_index=True, return_inverse=True)
+        v = np.zeros(len(dets), dtype=np.complex128)
+        v[inv.ravel()[:len(vals)]] = vals
+        vals = v
+    return Wavefunction(psi.nf, dets, vals)
+
+
+def _zero_term_targets(O, dets, restrictions=None):
+    """The determinants that O's zero-valued strings reach from `dets` (host ladder
+    application in the reference's byte layout, Core/OperatorWaveFunction.cpp:7-115: orbital i
+    in byte i>>3 under mask 128>>(i&7), the first code acts first, an annihilator needs the
+    orbital occupied and a creator empty), kept when they satisfy the restrictions."""
+    zero = [ops for ops, v in O.terms if v == 0]
+    dets = np.asarray(dets, dtype=np.uint8).reshape(-1, nword(O.nf))
+    if not zero or not len(dets):
+        return np.zeros((0, nword(O.nf)), dtype=np.uint8)
+    out = []
+    for ops in zero:
+        d = dets.copy()
+        ok = np.ones(len(d), dtype=bool)
+        for code in ops:
+            i = code & 0x7FFF
+            byte, mask = i >> 3, np.uint8(128 >> (i & 7))
+            occ = (d[:, byte] & mask) != 0
+            ok &= ~occ if code & CREATION else occ
+            d[:, byte] ^= mask
+        out.append(d[ok])
+    t = np.concatenate(out)
+    for m, lo, hi in restrictions or []:
+        mb = dets_to_bytes([m], O.nf)[0]
+        cnt = np.unpackbits(t & mb[None, :], axis=1).sum(axis=1)
+        t = t[(cnt >= lo) & (cnt <= hi)]
+    return np.unique(t, axis=0) if len(t) else t
 
 
 def OperatorPsiConserveBasis(O, psi, eng=None):
@@ -1317,7 +1357,12 @@ def _rixs_dense(H1, H2, T1s, T2s, psis, o, b1, b2, tensor, eng):
         for it, T in enumerate(T1s):
             t = OperatorPsi(T, p, R1, eng)
             if t.N and n1:
-                np.add.at(X[:, it + nt1 * ip], b1.find(t.det), t.val)
+                # zero-amplitude targets of zero-valued strings may lie outside the device basis
+                rows = b1.find(t.det)
+                keep = rows >= 0
+                if not np.all(t.val[~keep] == 0):
+                    raise RuntimeError("CreateResonantSpectra: T1 psi reaches outside the intermediate basis")
+                np.add.at(X[:, it + nt1 * ip], rows[keep], t.val[keep])
     if n1:
         w1, V1 = hermitian_eigh(OperatorToDeterminantMatrix(H1, b1, eng), n1, eng)
     else:

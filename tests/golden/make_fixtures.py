@@ -309,6 +309,46 @@ def gen_eigen_growth():
     save("eigen_growth.json", out)
 
 
+RIXS_ONEBODY_DRIVER = """dofile("common.lua")
+%s
+H1 = H0 + 10
+T2 = ConjugateTranspose(OppT)
+psi1, psi2, psi3, psi4, psi5, psi6 = psilist[1], psilist[2], psilist[3], psilist[4], psilist[5], psilist[6]
+Tpsi0 = OppT * psi0  -- the zero constant of "OppT = 0 + ..." reaches psi0's determinants
+for _, n in ipairs({"H0", "H1", "OppT", "T2", "psi0", "psi1", "psi2", "psi3", "psi4", "psi5", "psi6", "Tpsi0"}) do io.put("dump", n) end
+function o(border)
+  return {{"DenseBorder", border}, {"NE1", 5}, {"NE2", 200}, {"Emin1", 0}, {"Emax1", 10}, {"Gamma1", 0.1},
+          {"Emin2", -5}, {"Emax2", 15}, {"Gamma2", 0.1}, {"NTri1", 200}, {"NTri2", 200}, {"epsilon", 1E-10}}
+end
+CreateResonantSpectra(H1, H0, OppT, T2, psilist, o(10000)).Print({{"file", "dump/list_dense.dat"}})
+CreateResonantSpectra(H1, H0, OppT, T2, psilist, o(1)).Print({{"file", "dump/list_krylov.dat"}})
+CreateResonantSpectra(H1, H0, OppT, T2, psi0, o(10000)).Print({{"file", "dump/psi0_dense.dat"}})
+CreateResonantSpectra(H1, H0, OppT, T2, psi0, o(1)).Print({{"file", "dump/psi0_krylov.dat"}})
+print("rixs_onebody done")
+"""
+
+
+def gen_rixs_onebody():
+    """The one-particle RIXS model of the reference's own test (TestScripts/
+    CreateResonantSpectra.Quanty, its model lines taken at run time): a list of six one-particle
+    states and a superposition, both branches, on a coarser final-state grid."""
+    lines = open(os.path.join(REF, "TestScripts", "CreateResonantSpectra.Quanty")).read().splitlines()
+    a = next(i for i, l in enumerate(lines) if l.startswith("NF = 6"))
+    b = next(i for i in range(a, len(lines)) if lines[i].startswith("print("))
+    work = run(RIXS_ONEBODY_DRIVER % "\n".join(lines[a:b]), "rixs_onebody.lua")
+    out = {"source": "TestScripts/CreateResonantSpectra.Quanty:%d-%d" % (a + 1, b),
+           "opts": {"NE1": 5, "NE2": 200, "Emin1": 0, "Emax1": 10, "Gamma1": 0.1, "Emin2": -5, "Emax2": 15,
+                    "Gamma2": 0.1, "NTri1": 200, "NTri2": 200, "Epsilon": 1e-10}}
+    for n in ("H0", "H1", "OppT", "T2"):
+        out[n] = op(work, n)
+    out["psi0"] = wf(work, "psi0")
+    out["Tpsi0"] = wf(work, "Tpsi0")
+    out["psilist"] = [wf(work, "psi%d" % i) for i in range(1, 7)]
+    for k in ("list_dense", "list_krylov", "psi0_dense", "psi0_krylov"):
+        out[k] = spectra(work, k + ".dat")
+    save("rixs_onebody.json", out)
+
+
 def gen_krylov_basis():
     """CreateSpectra with KrylovBasis: the Krylov vectors of the Lanczos branch (one pair, and
     lists at Epsilon 0) and the eigenstate energies of the dense branch."""
@@ -329,6 +369,6 @@ def gen_krylov_basis():
 if __name__ == "__main__":
     if not os.path.exists(QUANTY):
         sys.exit("build the reference first: oracle/build_ref.sh")
-    which = sys.argv[1:] or ["hpsi", "c0", "c1", "chain", "fshell", "print", "tensor", "rixs", "eigen_growth", "krylov_basis"]
+    which = sys.argv[1:] or ["hpsi", "c0", "c1", "chain", "fshell", "print", "tensor", "rixs", "eigen_growth", "krylov_basis", "rixs_onebody"]
     for w in which:
         globals()["gen_" + w]()

@@ -39,7 +39,7 @@ class _Basis:
         return len(self.dets)
 
     def find(self, d):
-        return np.array([self.idx[bytes(r)] for r in np.asarray(d).reshape(len(d), -1)], dtype=np.int64)
+        return np.array([self.idx.get(bytes(r), -1) for r in np.asarray(d).reshape(len(d), -1)], dtype=np.int64)
 
     def dets_bytes(self):
         return self.dets
@@ -212,6 +212,25 @@ CASES = [
 ]
 
 
+ONEBODY = [("list_dense", "psilist", 10000, "dense"), ("list_krylov", "psilist", 1, "krylov"),
+           ("psi0_dense", "psi0", 10000, "dense"), ("psi0_krylov", "psi0", 1, "krylov")]
+
+
+@pytest.mark.parametrize("key,which,border,branch", ONEBODY, ids=[c[0] for c in ONEBODY])
+def test_one_particle_rixs_of_the_reference_test(host_api, key, which, border, branch):
+    """The one-particle model of TestScripts/CreateResonantSpectra.Quanty: DenseBorder 10000
+    takes the dense branch, DenseBorder 1 the Krylov branch (one run per state of the list)."""
+    api = host_api
+    g = golden("rixs_onebody.json")
+    H1, H0, T, T2 = (api.Operator.from_fixture(g[k]) for k in ("H1", "H0", "OppT", "T2"))
+    psi = ([api.Wavefunction.from_fixture(p) for p in g["psilist"]] if which == "psilist"
+           else api.Wavefunction.from_fixture(g["psi0"]))
+    G, st = api.CreateResonantSpectra(H1, H0, T, T2, psi, dict(g["opts"], DenseBorder=border))
+    R = np.array(g[key]["re"]) + 1j * np.array(g[key]["im"])
+    assert st["method"] == branch and G.shape == R.shape
+    assert np.max(np.abs(G - R)) / np.max(np.abs(R)) < TOL
+
+
 @pytest.mark.parametrize("key,t1,t2,npsi,opts,branch", CASES, ids=[c[0] for c in CASES])
 def test_resonant_spectra_orchestration_matches_reference(host_api, key, t1, t2, npsi, opts, branch):
     api = host_api
@@ -287,3 +306,64 @@ def test_krylov_basis_option(host_api):
     E = [api.PsiOperatorPsi(HX, k).real for k in K]
     assert len(E) == len(g["dense_energies"]) and np.max(np.abs(np.array(E) - g["dense_energies"])) < 1e-10
     assert math.isclose(np.linalg.norm(K[0].val), 1.0, rel_tol=1e-12)
+
+
+def test_zero_valued_strings_reach_their_targets(oracle_mod, monkeypatch):
+    """H*psi inserts the targets of zero-valued strings with amplitude 0, as the reference's
+    OperatorPsi does (the "O = 0; O = O + ..." constant, cancelled sums): the host
+    enumeration of those targets equals the oracle's, with and without restrictions, and
+    OperatorPsi merges them into the device result in sorted order."""
+    from quanty_gb300 import api
+    O = oracle_mod
+    g = golden("rixs.json")
+    g1 = golden("rixs_onebody.json")
+    HX = api.Operator.from_fixture(g["HX"])
+    psi = api.Wavefunction.from_fixture(g["psi"][0])
+    Z = api.Operator(HX.nf, [(ops, 0.0) for ops, v in HX.terms])  # every string, value zero
+    R = [("1111110000000000", 5, 6), ("0000001111111111", 8, 9)]
+    for res in (None, R):
+        got = api._zero_term_targets(Z, psi.det, res)
+        ref = O.operator_psi(O.Op({"nf": 16, "terms": [[list(t[0]), 0.0, 0.0] for t in HX.terms]}),
+                             O.WF(16, psi.det, psi.val), res)
+        assert sorted(map(bytes, got)) == sorted(map(bytes, ref.det))
+        assert np.all(ref.val == 0)
+    # the merge: a device growth without the zero-valued strings, then OperatorPsi's result
+    T = api.Operator.from_fixture(g1["OppT"])  # holds the zero constant of "OppT = 0 + ..."
+    p0 = api.Wavefunction.from_fixture(g1["psi0"])
+    nz = api.Operator(T.nf, [(o, v) for o, v in T.terms if v != 0])
+    dev = O.operator_psi(_oop(O, nz), O.WF(T.nf, p0.det, p0.val))
+    order = np.lexsort(dev.det.T[::-1])
+
+    class Dst:
+        n = len(order)
+        h = None
+
+        def dets_bytes(self):
+            return dev.det[order]
+
+    class Eng:
+        torch = torch
+
+        def check(self, st, ctx=None):
+            pass
+
+        def empty(self, n, nvec=1):
+            return torch.zeros((max(n, 1), nvec), dtype=torch.complex128)
+
+        def to_host(self, t):
+            return np.asarray(dev.val[order])
+
+    eng = Eng()
+    monkeypatch.setattr(api.Basis, "from_bytes", classmethod(lambda cls, nf, d, eng=None: (Dst(), np.arange(len(d)))))
+    monkeypatch.setattr(api, "_upload", lambda *a, **k: None)
+    monkeypatch.setattr(api, "OperatorPsiBasis", lambda *a, **k: Dst())
+    monkeypatch.setattr(api, "_ptr", lambda a: a)
+    eng.L = type("L", (), {"qg_apply": staticmethod(lambda *a: 0)})()
+    eng.ctx = None
+    monkeypatch.setattr(api.Operator, "handle", lambda self, eng=None: None)
+    out = api.OperatorPsi(T, p0, eng=eng)
+    ref = O.operator_psi(_oop(O, T), O.WF(T.nf, p0.det, p0.val))
+    assert out.N == len(ref.val) == len(order) + p0.N
+    assert [bytes(r) for r in out.det] == sorted(bytes(r) for r in ref.det)
+    d = ref.as_dict()
+    assert np.allclose([d[bytes(r)] for r in out.det], out.val, rtol=0, atol=1e-15)

@@ -329,3 +329,40 @@ def test_krylov_basis_matches_reference(oracle_mod):
         assert rel_err([d[bytes(x)] for x in R.det], R.val) < 1e-10
     w, _ = O.exact_eigensystem(HX, O.closure(HX, t), len(g["dense_energies"]))
     assert np.max(np.abs(w - np.array(g["dense_energies"]))) < 1e-10
+
+
+def test_zero_valued_strings_insert_targets_as_the_reference(oracle_mod):
+    """OperatorPsi inserts the target of every applicable string whatever its value: the zero
+    constant of "OppT = 0 + ..." (TestScripts/CreateResonantSpectra.Quanty's operator) puts
+    psi0's own determinants into OppT * psi0 with amplitude 0."""
+    O = oracle_mod
+    g = golden("rixs_onebody.json")
+    out = O.operator_psi(O.Op(g["OppT"]), O.WF.from_fixture(g["psi0"]))
+    ref = O.WF.from_fixture(g["Tpsi0"])
+    assert sorted(map(bytes, out.det)) == sorted(map(bytes, ref.det))
+    d = out.as_dict()
+    assert rel_err([d[bytes(r)] for r in ref.det], ref.val) < 1e-14
+    assert sum(1 for v in ref.val if v == 0) == len(g["psi0"]["dets"])
+
+
+def test_one_particle_rixs_of_the_reference_test(oracle_mod):
+    """The one-particle RIXS model of TestScripts/CreateResonantSpectra.Quanty (a list of six
+    one-particle states and a superposition): dense and Krylov branches restated, against the
+    reference (1e-8)."""
+    O = oracle_mod
+    g = golden("rixs_onebody.json")
+    H1, H0, T, T2 = (O.Op(g[k]) for k in ("H1", "H0", "OppT", "T2"))
+    psis = [O.WF.from_fixture(p) for p in g["psilist"]]
+    p0 = O.WF.from_fixture(g["psi0"])
+    o = dict(g["opts"])
+
+    def spec(k):
+        return np.array(g[k]["re"]) + 1j * np.array(g[k]["im"])
+
+    G, _ = O.resonant_spectra_dense(H1, H0, [T], [T2], psis, o)
+    assert rel_err(G, spec("list_dense")) < 1e-8
+    G = np.concatenate([O.resonant_spectra(H1, H0, T, [T2], p, o) for p in psis])
+    assert rel_err(G, spec("list_krylov")) < 1e-8
+    G, _ = O.resonant_spectra_dense(H1, H0, [T], [T2], [p0], o)
+    assert rel_err(G, spec("psi0_dense")) < 1e-8
+    assert rel_err(O.resonant_spectra(H1, H0, T, [T2], p0, o), spec("psi0_krylov")) < 1e-8
