@@ -492,6 +492,17 @@ def OperatorPsi(O, psi, restrictions=None, eng=None):
     return Wavefunction(psi.nf, dets, vals)
 
 
+def _targets_basis(O, src, restrictions=None, eng=None):
+    """The targets of O from a device basis as the reference's OperatorPsi reaches them: the
+    device growth, plus the targets of O's zero-valued strings (host enumeration)."""
+    tb = OperatorPsiBasis(O, src, restrictions, eng)
+    if src.n and any(v == 0 for _, v in O.terms):
+        extra = _zero_term_targets(O, src.dets_bytes(), parse_restrictions(restrictions))
+        if len(extra):
+            tb = basis_union(tb, Basis.from_bytes(O.nf, extra, eng)[0], eng)
+    return tb
+
+
 def _zero_term_targets(O, dets, restrictions=None):
     """The determinants that O's zero-valued strings reach from `dets` (host ladder
     application in the reference's byte layout, Core/OperatorWaveFunction.cpp:7-115: orbital i
@@ -979,7 +990,7 @@ def _batched_lanczos_device(H, Ts, psis, o, R, eng):
         E0 = [float(o["E0"])] * npsi
     bt = None
     for t in Ts:
-        tb = OperatorPsiBasis(t, b0, R, eng)
+        tb = _targets_basis(t, b0, R, eng)
         bt = tb if bt is None else basis_union(bt, tb, eng)
     bf = closure_of(H, bt, R, -1, eng)
     if method != "lanczos" and 0 < bf.n <= int(o["DenseBorder"]):
@@ -1272,7 +1283,7 @@ def _rixs_dense_bases(H1, H2, T1s, T2s, psis, o, eng):
     for H, Ts, R in ((H1, T1s, R1), (H2, T2s, R2)):
         bt = None
         for T in Ts:
-            t = OperatorPsiBasis(T, u, R, eng)
+            t = _targets_basis(T, u, R, eng)
             bt = t if bt is None else basis_union(bt, t, eng)
             if not fits(bt.n):
                 return None
@@ -1494,7 +1505,7 @@ def _rixs_krylov_tensor(H1, H2, T1s, T2s, psis, o, eng):
     # final-state basis: targets of every T2, closure under H2
     bt = None
     for T in T2s:
-        t = OperatorPsiBasis(T, b1, R2, eng)
+        t = _targets_basis(T, b1, R2, eng)
         bt = t if bt is None else basis_union(bt, t, eng)
     b2 = closure_of(H2, bt, R2, -1, eng)
     n2 = b2.n

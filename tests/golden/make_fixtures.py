@@ -324,6 +324,9 @@ CreateResonantSpectra(H1, H0, OppT, T2, psilist, o(10000)).Print({{"file", "dump
 CreateResonantSpectra(H1, H0, OppT, T2, psilist, o(1)).Print({{"file", "dump/list_krylov.dat"}})
 CreateResonantSpectra(H1, H0, OppT, T2, psi0, o(10000)).Print({{"file", "dump/psi0_dense.dat"}})
 CreateResonantSpectra(H1, H0, OppT, T2, psi0, o(1)).Print({{"file", "dump/psi0_krylov.dat"}})
+-- automatic energy ranges: the zero constant of OppT puts psi0's sector into the dense bases
+CreateResonantSpectra(H1, H0, OppT, T2, psi0, {{"NE1", 5}, {"Gamma1", 0.1}, {"NE2", 200}, {"Gamma2", 0.1}}).Print({{"file", "dump/psi0_dense_auto.dat"}})
+CreateSpectra(H1, OppT, psi0, {{"NE", 100}}).Print({{"file", "dump/xas_dense_auto.dat"}})
 print("rixs_onebody done")
 """
 
@@ -344,7 +347,7 @@ def gen_rixs_onebody():
     out["psi0"] = wf(work, "psi0")
     out["Tpsi0"] = wf(work, "Tpsi0")
     out["psilist"] = [wf(work, "psi%d" % i) for i in range(1, 7)]
-    for k in ("list_dense", "list_krylov", "psi0_dense", "psi0_krylov"):
+    for k in ("list_dense", "list_krylov", "psi0_dense", "psi0_krylov", "psi0_dense_auto", "xas_dense_auto"):
         out[k] = spectra(work, k + ".dat")
     save("rixs_onebody.json", out)
 

@@ -82,6 +82,14 @@ def host_api(monkeypatch, oracle_mod):
                     Kn[i, b.idx[bytes(r)]] += v
             return 0
 
+        def qg_expectation(self, ctx, H, b, x, k, out):
+            M = O.dense_matrix(_oop(O, H), b.wf())
+            X = x.numpy()[:b.n]
+            for j in range(k):
+                e = np.vdot(X[:, j], M @ X[:, j])
+                out[2 * j], out[2 * j + 1] = e.real, e.imag
+            return 0
+
         def qg_apply(self, ctx, T, dst, src, x, y, k):
             X, Y = x.numpy(), y.numpy()
             for c in range(k):
@@ -173,8 +181,12 @@ def host_api(monkeypatch, oracle_mod):
         return b, b.find(d)
 
     monkeypatch.setattr(api.Basis, "from_bytes", classmethod(from_bytes))
-    monkeypatch.setattr(api, "OperatorPsiBasis", lambda T, b, R=None, eng=None: B(b.nf, opsi(T, api.Wavefunction(
-        b.nf, b.dets, np.ones(b.n)), R).det))
+    def device_targets(T, b, R=None, eng=None):
+        # the device growth leaves zero-valued strings out
+        nz = api.Operator(T.nf, [(o, v) for o, v in T.terms if v != 0])
+        return B(b.nf, opsi(nz, api.Wavefunction(b.nf, b.dets, np.ones(b.n)), R).det)
+
+    monkeypatch.setattr(api, "OperatorPsiBasis", device_targets)
     monkeypatch.setattr(api, "basis_union", lambda a, b, eng=None: B(a.nf, np.concatenate([a.dets, b.dets])))
     monkeypatch.setattr(api, "closure_of", closure_of)
     monkeypatch.setattr(api, "closure", lambda H, d, nf, R=None, m=-1, eng=None: closure_of(H, B(nf, d), R))
@@ -214,6 +226,26 @@ CASES = [
 
 ONEBODY = [("list_dense", "psilist", 10000, "dense"), ("list_krylov", "psilist", 1, "krylov"),
            ("psi0_dense", "psi0", 10000, "dense"), ("psi0_krylov", "psi0", 1, "krylov")]
+
+
+def test_zero_valued_strings_shape_the_dense_bases(host_api):
+    """The zero constant of "OppT = 0 + ..." puts the initial states' sector into the dense
+    bases of RIXS and of CreateSpectra, so the automatic energy ranges span it (reference
+    outputs of the one-particle model)."""
+    api = host_api
+    g = golden("rixs_onebody.json")
+    H1, H0, T, T2 = (api.Operator.from_fixture(g[k]) for k in ("H1", "H0", "OppT", "T2"))
+    p0 = api.Wavefunction.from_fixture(g["psi0"])
+    G, st = api.CreateResonantSpectra(H1, H0, T, T2, p0, {"NE1": 5, "Gamma1": 0.1, "NE2": 200, "Gamma2": 0.1})
+    ref = g["psi0_dense_auto"]
+    R = np.array(ref["re"]) + 1j * np.array(ref["im"])
+    assert st["method"] == "dense" and abs(st["emin2"] - ref["emin"]) < 1e-10 and abs(st["emax2"] - ref["emax"]) < 1e-10
+    assert np.max(np.abs(G - R)) / np.max(np.abs(R)) < TOL
+    S, _ = api.CreateSpectra(H1, T, p0, {"NE": 100})
+    ref = g["xas_dense_auto"]
+    R = np.array(ref["re"]) + 1j * np.array(ref["im"])
+    assert abs(S.Emin - ref["emin"]) < 1e-10 and abs(S.Emax - ref["emax"]) < 1e-10 and abs(S.Gamma - ref["gamma"]) < 1e-10
+    assert np.max(np.abs(S.G - R)) / np.max(np.abs(R)) < TOL
 
 
 @pytest.mark.parametrize("key,which,border,branch", ONEBODY, ids=[c[0] for c in ONEBODY])
