@@ -136,6 +136,10 @@ class Operator:
         self.name = name
         self.terms = [(tuple(int(o) for o in ops), complex(v)) for ops, v in terms]
         self._handles = {}
+        # occupation windows attached to the operator (the Lua field O.Restrictions,
+        # OperatorType.Res, Core/StructDef.cpp:247): O * psi then keeps only targets inside them
+        # (OperatorPsi dispatches to OperatorPsiRestricted, Core/OperatorWaveFunction.cpp:5600)
+        self.Restrictions = None
 
     @classmethod
     def from_fixture(cls, d):
@@ -476,6 +480,8 @@ def OperatorPsi(O, psi, restrictions=None, eng=None):
     eng = eng or engine()
     if O.nf != psi.nf:
         raise ValueError("operator and wavefunction have different numbers of fermions")
+    if restrictions is None:
+        restrictions = getattr(O, "Restrictions", None)
     src, perm = Basis.from_bytes(psi.nf, psi.det, eng)
     x = _upload(eng, src, perm, psi.val)
     dst = OperatorPsiBasis(O, src, restrictions, eng)

@@ -399,3 +399,41 @@ def test_zero_valued_strings_reach_their_targets(oracle_mod, monkeypatch):
     assert [bytes(r) for r in out.det] == sorted(bytes(r) for r in ref.det)
     d = ref.as_dict()
     assert np.allclose([d[bytes(r)] for r in out.det], out.val, rtol=0, atol=1e-15)
+
+
+def test_operator_restrictions_apply_to_h_psi(monkeypatch):
+    """O.Restrictions (OperatorType.Res) makes O * psi the restricted product, as the
+    reference's OperatorPsi dispatch does; an explicit restrictions argument wins."""
+    from quanty_gb300 import api
+    seen = []
+
+    class Dst:
+        n, h = 0, None
+
+        def dets_bytes(self):
+            return np.zeros((0, 1), dtype=np.uint8)
+
+    class Eng:
+        ctx, L = None, type("L", (), {"qg_apply": staticmethod(lambda *a: 0)})()
+
+        def check(self, st, ctx=None):
+            pass
+
+        def empty(self, n, nvec=1):
+            return torch.zeros((max(n, 1), nvec), dtype=torch.complex128)
+
+        def to_host(self, t):
+            return t.numpy()
+
+    monkeypatch.setattr(api.Basis, "from_bytes", classmethod(lambda cls, nf, d, eng=None: (Dst(), np.arange(len(d)))))
+    monkeypatch.setattr(api, "_upload", lambda *a, **k: None)
+    monkeypatch.setattr(api, "OperatorPsiBasis", lambda O, b, R=None, eng=None: seen.append(R) or Dst())
+    monkeypatch.setattr(api, "_ptr", lambda a: a)
+    monkeypatch.setattr(api.Operator, "handle", lambda self, eng=None: None)
+    O = api.NewOperator(4, 0, [[0, -1, 1.0]])
+    psi = api.NewWavefunction(4, 0, [["0100", 1.0]])
+    api.OperatorPsi(O, psi, eng=Eng())
+    O.Restrictions = [4, 0, ["1100", 1, 1]]
+    api.OperatorPsi(O, psi, eng=Eng())
+    api.OperatorPsi(O, psi, [4, 0, ["1111", 1, 1]], eng=Eng())
+    assert seen == [None, [4, 0, ["1100", 1, 1]], [4, 0, ["1111", 1, 1]]]
