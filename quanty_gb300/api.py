@@ -1390,10 +1390,10 @@ def _rixs_dense(H1, H2, T1s, T2s, psis, o, b1, b2, tensor, eng):
         w2, V2 = np.zeros(1), np.zeros((0, 0), dtype=np.complex128)
     A = V1.conj().T @ X
     B = [V2.conj().T @ _apply_between(T, b2, b1, V1, eng) for T in T2s]
-    big = None
-    emin1, emax1, ne1, g1 = _rixs_range(o.get("Emin1", big), o.get("Emax1", big), int(o.get("NE1", 1000)),
+    # unset Emin/Emax (None) are derived from the extreme eigenvalues
+    emin1, emax1, ne1, g1 = _rixs_range(o.get("Emin1"), o.get("Emax1"), int(o.get("NE1", 1000)),
                                         float(o.get("Gamma1", 0.0)), w1[0], w1[-1], e1.min(), e1.max())
-    emin2, emax2, ne2, g2 = _rixs_range(o.get("Emin2", big), o.get("Emax2", big), int(o.get("NE2", 1000)),
+    emin2, emax2, ne2, g2 = _rixs_range(o.get("Emin2"), o.get("Emax2"), int(o.get("NE2", 1000)),
                                         float(o.get("Gamma2", 0.0)), w2[0], w2[-1], e2.min(), e2.max())
     np1 = ne1 + 1
     wres = np.array([emin1 + (emax1 - emin1) * l / ne1 for l in range(np1)])
