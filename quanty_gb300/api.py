@@ -1449,12 +1449,12 @@ def _rixs_krylov_tensor(H1, H2, T1s, T2s, psis, o, eng):
     v_(psi, T1, T2) = T2 G1(w_l) T1 psi for every incident energy, both shifts from psi 0 (as the
     reference).  The reference runs one block Lanczos per stage; here every T1 psi gets its own
     three-term Lanczos with stored Krylov vectors and G1(w_l) T1 psi is that space's projected
-    resolvent, all w_l at once; the matrix elements come from one batched
-    Lanczos over every diagonal vector and, per pair, v_a + v_b and v_a + i v_b (polarisation).
-    Each chain runs as many steps as the block run has Krylov vectors (NTri blocks times the
-    block width, at most the basis size), so a complete block space means complete chains, and
-    then the result equals the block-Lanczos one; the reference's
-    index order is kept: spectrum l + (NE1+1)(j2 + NT2(i1 + NT1(n2 + NT2(m1 + NT1(r + Npsi s)))))
+    resolvent, all w_l at once; the matrix elements come from one batched Lanczos over every
+    diagonal vector and, per pair, v_a + v_b and v_a + i v_b (polarisation).  Each chain runs
+    as many steps as the block run has Krylov vectors (NTri blocks times the block width, at
+    most 16 past the basis size), so a complete block space means complete chains, and then
+    the result equals the block-Lanczos one.  The reference's index order is kept: spectrum
+    l + (NE1+1)(j2 + NT2(i1 + NT1(n2 + NT2(m1 + NT1(r + Npsi s)))))
     holds the element between v_(r, m1, n2) (left) and v_(s, i1, j2) (right).  Energy ranges
     come from the extreme Krylov eigenvalues with the block branch's rules; when the
     second-stage block dimension (NTri2 times the block width) exceeds the final basis, the
@@ -1480,7 +1480,9 @@ def _rixs_krylov_tensor(H1, H2, T1s, T2s, psis, o, eng):
     X1 = np.zeros((n1, M1), dtype=np.complex128)
     for j, t in enumerate(Tpsi):
         if t.N:
-            v = np.where(np.abs(t.val) <= eps, 0.0, t.val) if eps > 0 else t.val
+            # ComplexWaveFunctionTruncateBasis (Core/ComplexWaveFunctionArithmetic.cpp:1073):
+            # keep |a|^2 > epsilon^2
+            v = np.where(t.val.real ** 2 + t.val.imag ** 2 > eps * eps, t.val, 0.0)
             np.add.at(X1[:, j], b1.find(t.det), v)
     # each chain gets the Krylov dimension of the reference's block run, NTri1 blocks of M1
     # (a few steps past the basis size at most); three-term Lanczos keeping its vectors
