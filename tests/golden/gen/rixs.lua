@@ -61,4 +61,9 @@ S = CreateResonantSpectra(HX, H, {Tx, Ty}, {Txd}, {psi1, psi2}, opts({{"E0_1", -
 S.Print({{"file", "dump/dense_shifts.dat"}})
 S = CreateResonantSpectra(HX, H, {Tx, Ty}, {Txd}, {psi1, psi2}, opts({{"E0", -30.0}}))
 S.Print({{"file", "dump/dense_e0.dat"}})
+-- final-state restrictions (four down-spin 3d electrons) in both branches
+S = CreateResonantSpectra(HX, H, {Tx, Ty}, {Txd, Tyd}, psi1, opts({{"Restrictions2", {NF, 0, {"000000 1010101010", 4, 4}}}}))
+S.Print({{"file", "dump/dense_res2.dat"}})
+S = CreateResonantSpectra(HX, H, {Tx, Ty}, {Txd, Tyd}, psi1, opts({{"Restrictions2", {NF, 0, {"000000 1010101010", 4, 4}}}, {"DenseBorder", 0}, {"Epsilon", 0}}))
+S.Print({{"file", "dump/krylov_res2.dat"}})
 print("rixs done")

@@ -167,7 +167,9 @@ def host_api(monkeypatch, oracle_mod):
 
     def krylov_one(H1, H2, T, T2s, p, o, eng):
         G = O.resonant_spectra(_oop(O, H1), _oop(O, H2), _oop(O, T), [_oop(O, t) for t in T2s],
-                               O.WF(p.nf, p.det, p.val), dict(o, Restrictions1=None, Restrictions2=None))
+                               O.WF(p.nf, p.det, p.val),
+                               dict(o, Restrictions1=api.parse_restrictions(o.get("Restrictions1")),
+                                    Restrictions2=api.parse_restrictions(o.get("Restrictions2"))))
         return G, {"emin2": o["Emin2"], "emax2": o["Emax2"]}
 
     monkeypatch.setattr(torch.Tensor, "to", lambda self, *a, **k: self)
@@ -221,6 +223,10 @@ CASES = [
      dict(KRYLOV, NE1=3, NE2=48, Tensor=True, NTri1=40, NTri2=40), "krylov_tensor"),
     ("krylov_tensor_psi", ("Tx",), ("Tyd",), 2, dict(GRID, Tensor=True, NTri1=40, NTri2=40, **KRYLOV),
      "krylov_tensor"),
+    ("dense_res2", ("Tx", "Ty"), ("Txd", "Tyd"), 1, dict(GRID, Restrictions2=[16, 0, ["000000 1010101010", 4, 4]]),
+     "dense"),
+    ("krylov_res2", ("Tx", "Ty"), ("Txd", "Tyd"), 1,
+     dict(GRID, Restrictions2=[16, 0, ["000000 1010101010", 4, 4]], **KRYLOV), "krylov"),
 ]
 
 
