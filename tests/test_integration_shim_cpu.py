@@ -39,7 +39,11 @@ def test_shim_compiles_against_the_reference(tmp_path):
         "#define QUANTY_GB300\n"
         "#include <vector>\n"
         '#include "shim_body.inc"\n' % os.path.join(REF, "LuaInterface", "main.cpp"))
+    cuda_inc = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "include")
+    if not os.path.isfile(os.path.join(cuda_inc, "cuda_runtime.h")):
+        pytest.skip("CUDA headers not found")
     r = subprocess.run(["g++", "-fsyntax-only", "-std=gnu++17", "-fopenmp", "-w", "-D", "LUA_USE_LINUX",
-                        "-DBLASunderscore", "-I", os.path.join(ROOT, "include"), str(tmp_path / "shim_check.cpp")],
+                        "-DBLASunderscore", "-I", os.path.join(ROOT, "include"), "-I", cuda_inc,
+                        str(tmp_path / "shim_check.cpp")],
                        capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stderr[-3000:]
