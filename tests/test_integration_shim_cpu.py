@@ -1,5 +1,6 @@
-"""The C++ shim that INTEGRATION.md gives a Quanty maintainer compiles against the reference's
-own types: its code block is extracted and syntax-checked together with the reference's single
+"""The C++ shim the integration guide gives a Quanty maintainer (its first C++ block) compiles
+against the reference's own types: the block is extracted and syntax-checked together with the
+reference's single
 translation unit (LuaInterface/main.cpp, which includes every source file), and each qg_*
 function it calls is declared in include/qgpu.h and exported by libqgpu.so.  Skipped where the
 reference sources or g++ are absent (the reference never travels with this repository)."""
