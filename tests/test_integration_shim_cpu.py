@@ -1,9 +1,9 @@
 """The C++ shim the integration guide gives a Quanty maintainer (its first C++ block) compiles
 against the reference's own types: the block is extracted and syntax-checked together with the
-reference's single
-translation unit (LuaInterface/main.cpp, which includes every source file), and each qg_*
-function it calls is declared in include/qgpu.h and exported by libqgpu.so.  Skipped where the
-reference sources or g++ are absent (the reference never travels with this repository)."""
+reference's single translation unit (LuaInterface/main.cpp, which includes every source file),
+and each qg_* function it calls is declared in include/qgpu.h and exported by libqgpu.so.
+Skipped where the reference sources or g++ are absent (the reference never travels with this
+repository)."""
 import os
 import re
 import shutil
