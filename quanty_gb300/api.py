@@ -1126,8 +1126,8 @@ def Eigensystem(H, StartRestrictions, Npsi=None, options=None, eng=None, seed=12
     the start restrictions allow; Eigensystem(H, psi or [psi, ...][, options]) starts from the
     given states' determinants and finds as many states as were given.  The basis then grows
     under H within the Restrictions option, or without limit when it is absent (the reference's
-    growth loop uses only that option, BlockLanczos.cpp:5843-5884), and the eigenproblem on the
-    closed basis is solved densely (at most DenseBorder determinants, raised to Npsi when
+    growth loop uses only that option, BlockLanczos.cpp:5843-5884; ExpandBasis false keeps the
+    start determinants), and the eigenproblem on that basis is solved densely (at most DenseBorder determinants, raised to Npsi when
     options are given, BlockLanczosGroundStateConserveBasisDense) or by restarted block Lanczos
     on the device.  Returns (list of Wavefunction, energies)."""
     states = None
@@ -1149,7 +1149,10 @@ def Eigensystem(H, StartRestrictions, Npsi=None, options=None, eng=None, seed=12
     else:
         seed_dets = np.concatenate([np.asarray(p.det, dtype=np.uint8).reshape(-1, nword(H.nf)) for p in states])
     basis, _ = Basis.from_bytes(H.nf, seed_dets, eng)
-    basis = closure_of(H, basis, o.get("Restrictions"), -1, eng)
+    if o.get("ExpandBasis", True):
+        basis = closure_of(H, basis, o.get("Restrictions"), -1, eng)
+    # ExpandBasis false: the eigenproblem on the start determinants as they are
+    # (BlockLanczosGroundStateConserveBasis, LuaInterface/ssp.cpp:4231-4238)
     if basis.n <= int(o["DenseBorder"]):
         # dense branch (BlockLanczosGroundStateConserveBasisDense, Core/BlockLanczos.cpp:370)
         w, V = hermitian_eigh(OperatorToDeterminantMatrix(H, basis, eng), min(Npsi, basis.n), eng)

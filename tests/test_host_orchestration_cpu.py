@@ -300,6 +300,9 @@ def test_eigensystem_growth_and_call_forms(host_api):
     assert np.max(np.abs(np.array(E) - g["energies_confined"])) < 1e-10
     out, E = api.Eigensystem(H, psis)
     assert len(out) == 3 and np.max(np.abs(np.array(E) - g["energies_from_states"])) < 1e-10
+    # ExpandBasis false: the confined states' own basis, so the confined energies again
+    out, E = api.Eigensystem(H, psis, {"ExpandBasis": False})
+    assert np.max(np.abs(np.array(E) - g["energies_confined"])) < 1e-10
 
 
 def _wf_err(api, ref, got):
