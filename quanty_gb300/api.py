@@ -878,6 +878,11 @@ def _spectra_method(o):
         raise ValueError('CreateSpectra: Method "%s" and ForceDenseMethod true contradict each other' % m)
     if key == "mesh":
         raise NotImplementedError('CreateSpectra: Method "Mesh" (hybridisation on an energy mesh) is not supported')
+    # the self-energy options (ssp.cpp:1973-1977, used with a self-energy argument, :1992-2070)
+    if (o.get("GridPoints") is not None or o.get("NTriFull") is not None or o.get("NonCrossing")
+            or int(o.get("NBathExcitations", 1)) != 1):
+        raise NotImplementedError("CreateSpectra: self-energy options (GridPoints, NTriFull, NBathExcitations, "
+                                  "NonCrossing) are not supported")
     if force or key == "dense":
         return "dense"
     return "lanczos" if key == "lanczos" else ""

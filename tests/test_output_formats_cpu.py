@@ -88,6 +88,10 @@ def test_spectra_method_options_follow_the_reference():
         m(Method="Arnoldi")
     with pytest.raises(NotImplementedError):
         m(Method="Mesh")
+    for opt in ({"GridPoints": [0.0, 1.0]}, {"NTriFull": 10}, {"NonCrossing": True}, {"NBathExcitations": 2}):
+        with pytest.raises(NotImplementedError, match="self-energy"):
+            m(**opt)
+    assert m(NBathExcitations=1, NonCrossing=False) == ""
     with pytest.raises(ValueError, match="unknown Method"):  # checked before the GPU is needed
         api.CreateSpectra(None, [], [], {"Method": "Arnoldi"})
 
