@@ -66,4 +66,12 @@ S = CreateResonantSpectra(HX, H, {Tx, Ty}, {Txd, Tyd}, psi1, opts({{"Restriction
 S.Print({{"file", "dump/dense_res2.dat"}})
 S = CreateResonantSpectra(HX, H, {Tx, Ty}, {Txd, Tyd}, psi1, opts({{"Restrictions2", {NF, 0, {"000000 1010101010", 4, 4}}}, {"DenseBorder", 0}, {"Epsilon", 0}}))
 S.Print({{"file", "dump/krylov_res2.dat"}})
+-- intermediate-state restrictions (five down-spin 3d electrons) in every branch
+R1 = {NF, 0, {"000000 1010101010", 5, 5}}
+S = CreateResonantSpectra(HX, H, {Tx, Ty}, {Txd, Tyd}, psi1, opts({{"Restrictions1", R1}}))
+S.Print({{"file", "dump/dense_res1.dat"}})
+S = CreateResonantSpectra(HX, H, {Tx, Ty}, {Txd, Tyd}, psi1, opts({{"Restrictions1", R1}, {"DenseBorder", 0}, {"Epsilon", 0}}))
+S.Print({{"file", "dump/krylov_res1.dat"}})
+S = CreateResonantSpectra(HX, H, {Tx, Ty}, {Txd, Tyd}, psi1, opts({{"Restrictions1", R1}, {"DenseBorder", 0}, {"Epsilon", 0}, {"Tensor", true}}))
+S.Print({{"file", "dump/krylov_tensor_res1.dat"}})
 print("rixs done")

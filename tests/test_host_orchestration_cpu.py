@@ -227,6 +227,12 @@ CASES = [
      "dense"),
     ("krylov_res2", ("Tx", "Ty"), ("Txd", "Tyd"), 1,
      dict(GRID, Restrictions2=[16, 0, ["000000 1010101010", 4, 4]], **KRYLOV), "krylov"),
+    ("dense_res1", ("Tx", "Ty"), ("Txd", "Tyd"), 1, dict(GRID, Restrictions1=[16, 0, ["000000 1010101010", 5, 5]]),
+     "dense"),
+    ("krylov_res1", ("Tx", "Ty"), ("Txd", "Tyd"), 1,
+     dict(GRID, Restrictions1=[16, 0, ["000000 1010101010", 5, 5]], **KRYLOV), "krylov"),
+    ("krylov_tensor_res1", ("Tx", "Ty"), ("Txd", "Tyd"), 1,
+     dict(GRID, Restrictions1=[16, 0, ["000000 1010101010", 5, 5]], Tensor=True, **KRYLOV), "krylov_tensor"),
 ]
 
 
