@@ -301,6 +301,23 @@ class Wavefunction:
     def norm(self):
         return float(np.linalg.norm(self.val))
 
+    # The Lua methods that change a wavefunction in place (LuaInterface/Wavefunction.cpp:507-556).
+
+    def Chop(self, border=10 * DBL_EPSILON):
+        """psi.Chop(): drop determinants with |a|^2 <= border^2 (WaveFunctionTruncateBasis)."""
+        keep = self.val.real ** 2 + self.val.imag ** 2 > border * border
+        self.det, self.val = np.ascontiguousarray(self.det[keep]), np.ascontiguousarray(self.val[keep])
+
+    def Conjugate(self):
+        """psi.Conjugate(): complex-conjugate every amplitude."""
+        self.val = np.conj(self.val)
+
+    def Norm(self):
+        """psi.Norm(): normalise to unit length (WaveFunctionNormalize; the Lua name)."""
+        n = self.norm()
+        if n > 0:
+            self.val = self.val / n
+
     # ------------------------------------------------------------- arithmetic (host side)
     # The reference's Lua metamethods (LuaInterface/Wavefunction.cpp:1-440): sums on the union
     # basis, scaling by numbers, <a|b> for two wavefunctions, O|psi> and <psi|O = O^dag|psi>.

@@ -137,3 +137,19 @@ def test_wavefunction_arithmetic_follows_the_reference(monkeypatch):
     p1 * Tz
     O_, psi = seen["call"]
     assert psi is p1 and O_.terms == Tz.dagger().terms
+
+
+def test_wavefunction_in_place_methods():
+    """psi.Chop(), psi.Conjugate() and psi.Norm() as the reference's Lua methods: truncation at
+    |a|^2 > border^2 (default 10 DBL_EPSILON), conjugation, normalisation."""
+    import numpy as np
+    from quanty_gb300 import api
+    psi = api.NewWavefunction(4, 0, [["1100", 1e-17], ["1010", 2j], ["0011", 1e-3]])
+    psi.Chop()
+    assert psi.dets() == ["1010", "0011"]
+    psi.Chop(1e-3)
+    assert psi.dets() == ["1010"]
+    psi.Conjugate()
+    assert psi.val[0] == -2j
+    psi.Norm()
+    assert abs(psi.norm() - 1) < 1e-15 and psi.val[0] == -1j
