@@ -5,10 +5,14 @@ same: ``NewOperator``, ``NewWavefunction``, ``OperatorPsi`` (``H*psi``,
 ``Core/OperatorWaveFunction.cpp:5598``), ``OperatorPsiConserveBasis`` (:5507/:5541),
 ``PsiOperatorPsi`` (:5680), ``LanczosTriDiagonalize`` (``Core/Lanczos.cpp:5274``),
 ``TriDiagonalMatrixToSpectrum`` (``Core/Spectral.cpp:1433``), ``CreateSpectra``
-(``LuaInterface/ssp.cpp:1906``) and ``Eigensystem`` (``LuaInterface/ssp.cpp:4039``).  Options
-take the reference's names and defaults (``InitConvergenceSettings``,
-``Core/StructDef.cpp:291-320``).  Every numerical step runs in libqgpu.so on the GPU; this module
-only converts layouts, owns handles and sequences calls.
+(``LuaInterface/ssp.cpp:1906``), ``CreateResonantSpectra`` (:3090) and ``Eigensystem``
+(``LuaInterface/ssp.cpp:4039``).  Options take the reference's names and defaults
+(``InitConvergenceSettings``, ``Core/StructDef.cpp:291-320``).  Operator applications, bases and
+closures, the Lanczos recursions, dense operator matrices and spectrum evaluations run in
+libqgpu.so on the GPU; this module converts layouts, owns handles and sequences calls, and does
+on the host only what is small by construction: products of eigenvector matrices of the dense
+branches (bases within DenseBorder), the library's host eigensolver on them, and arithmetic
+between wavefunctions the caller holds on the host.  There is no CPU path for any GPU step.
 """
 import ctypes as C
 import math
