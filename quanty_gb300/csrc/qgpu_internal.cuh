@@ -249,15 +249,18 @@ __host__ __device__ inline bool qg_less(const Key<W> &a, const Key<W> &b) {
   return false;
 }
 
-// Find the slot of a key; returns the slot index or -1.  Probes are bounded.
-// linear probe for key k starting at slot h
+// Linear probe for key k starting at slot h; returns the slot index or -1.  Probes are bounded.
+// A slot is empty when its second word is all ones: an occupied slot holds 0 there (W = 1) or
+// the key's top word, which never has all 64 bits set (at most 63 orbitals live in it since
+// nf <= 127).  The low word can be all ones for a resident key (W = 2, orbitals nf-64..nf-1
+// all occupied), so it cannot mark an empty slot.
 template <int W>
 __device__ __forceinline__ int64_t qg_find_slot_at(const Slot *__restrict__ slots, uint64_t hmask, const Key<W> &k,
                                                    uint64_t h, unsigned int *err) {
   for (int p = 0; p < QG_PROBE_LIMIT; p++) {
     ulonglong2 v = __ldg(reinterpret_cast<const ulonglong2 *>(slots + h));
     if (v.x == k.w[0] && (W == 1 || v.y == k.w[W - 1])) return (int64_t)h;
-    if (v.x == QG_EMPTY_WORD) return -1;
+    if (v.y == QG_EMPTY_WORD) return -1;  // the key's top word is never all ones (nf <= 127)
     h = (h + 1) & hmask;
   }
   atomicOr(err, QG_DEVERR_PROBE);
@@ -271,7 +274,7 @@ __device__ __forceinline__ int64_t qg_find_slot(const Slot *__restrict__ slots, 
   for (int p = 0; p < QG_PROBE_LIMIT; p++) {
     ulonglong2 v = __ldg(reinterpret_cast<const ulonglong2 *>(slots + h));
     if (v.x == k.w[0] && (W == 1 || v.y == k.w[W - 1])) return (int64_t)h;
-    if (v.x == QG_EMPTY_WORD) return -1;
+    if (v.y == QG_EMPTY_WORD) return -1;  // the key's top word is never all ones (nf <= 127)
     h = (h + 1) & hmask;
   }
   atomicOr(err, QG_DEVERR_PROBE);

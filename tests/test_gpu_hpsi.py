@@ -110,6 +110,42 @@ def test_apply_matches_oracle_on_closed_sets(api, oracle_mod, nf, nel):
     assert api.count_nnz(H, b) == O.count_nnz(op, O.WF(nf, dets, x))
 
 
+def test_apply_with_all_ones_low_key_word(api, oracle_mod):
+    """nf = 70 with orbitals 16..69 filled: a determinant with orbitals 6..15 also filled has
+    all 64 bits of its low device word set (orbitals 6..69).  Such keys sit in the hash table
+    beside the others, and lookups whose probe chains pass their slots must keep probing.
+    Growth, fixed-basis H*psi and the connection count against the oracle."""
+    O = oracle_mod
+    nf = 70
+    rng = np.random.default_rng(70)
+    terms, seen = [], set()
+    while len(terms) < 60:  # one-body moves and pair terms among orbitals 0..15
+        i, j = (int(v) for v in rng.choice(16, 2, replace=False))
+        if (i, j) not in seen:
+            seen.add((i, j))
+            terms.append(([j, i | api.CREATION], complex(rng.normal(), rng.normal())))
+    for _ in range(20):
+        i, j, k, l = (int(v) for v in rng.choice(16, 4, replace=False))
+        terms.append(([l, k, j | api.CREATION, i | api.CREATION], complex(rng.normal(), 0.0)))
+    H = api.Operator(nf, terms)
+    seed = "1" * 2 + "0" * 4 + "1" * 64  # orbitals 0, 1 and 6..69: low word all ones
+    b = api.closure(H, api.dets_to_bytes([seed], nf), nf, None, -1)
+    dets = b.dets_bytes()
+    full = [r for r in dets if all(r[i >> 3] & (128 >> (i & 7)) for i in range(6, 70))]
+    assert len(dets) == math.comb(16, 12) and len(full) == math.comb(6, 2)
+    assert (b.find(dets) == np.arange(len(dets))).all()  # every key found at its row
+    x = rng.normal(size=len(dets)) + 1j * rng.normal(size=len(dets))
+    psi = api.Wavefunction(nf, dets, x)
+    y = api.OperatorPsiConserveBasis(H, psi)
+    op = O.Op({"nf": nf, "terms": [[list(t[0]), t[1].real, t[1].imag] for t in H.terms]})
+    want = O.apply_conserve(op, O.WF(nf, dets, x))
+    assert rel_err(y.val, want) < TOL
+    assert api.count_nnz(H, b) == O.count_nnz(op, O.WF(nf, dets, x))
+    out = api.OperatorPsi(H, api.Wavefunction(nf, [dets[0]], [1.0]))
+    ref = O.operator_psi(op, O.WF(nf, [dets[0]], [1.0]))
+    assert sorted(map(bytes, out.det)) == sorted(map(bytes, ref.det))
+
+
 def test_multivector_apply_equals_single(api):
     import torch
     rng = np.random.default_rng(5)
