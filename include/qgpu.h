@@ -225,6 +225,12 @@ qg_status qg_apply_host(qg_context ctx, qg_operator op, qg_basis basis_dst, qg_b
  * the same count without the diagonal (flip == 0) connections. */
 qg_status qg_count_nnz(qg_context ctx, qg_operator op, qg_basis basis, int64_t *nnz);
 qg_status qg_count_nnz_offdiag(qg_context ctx, qg_operator op, qg_basis basis, int64_t *nnz);
+/* The same count over the rows row0, row0 + stride, ... of the basis only (offdiag != 0: without
+ * the diagonal connections), for checks on a spread sample of a large basis.  For a Hermitian
+ * term list this equals the reference's count of the pairs its push loop visits from those
+ * determinants as sources (Core/OperatorWaveFunction.cpp:784-838). */
+qg_status qg_count_nnz_rows(qg_context ctx, qg_operator op, qg_basis basis, int64_t row0, int64_t stride,
+                            int32_t offdiag, int64_t *nnz);
 
 /* <psi|op|psi> for nvec vectors on one basis, complex result per vector (host out)
  * (PsiOperatorPsi / PsiHermitianOperatorPsi, Core/OperatorWaveFunction.cpp:5680, :5710). */

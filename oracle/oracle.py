@@ -44,6 +44,9 @@ def lib():
         L.qo_apply_conserve_strided.argtypes = [I, P, P, P, P, P, P, I64, I64, I64, P]
         L.qo_count_nnz.restype = I64
         L.qo_count_nnz.argtypes = [I, P, P, P, P, I64, I64]
+        L.qo_count_nnz_strided.restype = I64
+        L.qo_apply_multi.argtypes = [I, P, P, P, P, P, P, P, I, P, P]
+        L.qo_count_nnz_strided.argtypes = [I, P, P, P, P, I64, I64, I64]
         L.qo_lanczos_tridiag.argtypes = [I, P, P, P, P, P, P, I, D, D, I, P, P, P, P, P]
         L.qo_cf_spectrum.argtypes = [I, P, P, D, D, D, I, D, P, P]
         L.qo_lanczos_krylov.argtypes = [I, P, P, P, P, P, P, I, D, I, P, P, P, P, P, P]
@@ -178,6 +181,32 @@ def count_nnz(op, psi, row0=0, row1=None):
     n = lib().qo_count_nnz(op.nterms, _p(op.len), _p(op.off), _p(op.ops), h, row0, row1)
     lib().qo_wf_free(h)
     return n
+
+
+def apply_sampled(op, handle, n, stride, row0=0):
+    """Fixed-basis H*psi from the source rows row0, row0 + stride, ... only (push form, the
+    full basis of the handle as the lookup target): equal to H applied to x with every other
+    row zeroed.  `handle` is a WF.handle() the caller frees."""
+    y = np.zeros(2 * n)
+    lib().qo_apply_conserve_strided(*op.args(), handle, row0, n, stride, _p(y))
+    return y[0::2] + 1j * y[1::2]
+
+
+def apply_multi(op, src_handle, dst_handle, n_src, n_dst, X):
+    """Push-form op X for the columns of X (n_src x nvec complex, rows in the order of the
+    src handle's determinants) into the basis of dst (the same handle: the fixed-basis
+    apply); returns n_dst x nvec."""
+    X = np.ascontiguousarray(X, dtype=np.complex128)
+    nvec = X.shape[1]
+    Y = np.zeros((n_dst, nvec), dtype=np.complex128)
+    lib().qo_apply_multi(*op.args(), src_handle, dst_handle, nvec, _p(X), _p(Y))
+    return Y
+
+
+def count_nnz_sampled(op, handle, n, stride, row0=0):
+    """Pairs (source row, term) with a non-zero sign and the target in the basis, over the
+    source rows row0, row0 + stride, ... (the pairs the push loop visits from them)."""
+    return lib().qo_count_nnz_strided(op.nterms, _p(op.len), _p(op.off), _p(op.ops), handle, row0, n, stride)
 
 
 def lanczos_tridiag(op, psi, ntri, eps, gamma, restrictions=None):

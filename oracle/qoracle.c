@@ -309,6 +309,82 @@ int64_t qo_count_nnz(int nterms, const int *len, const int64_t *off, const uint1
   return nnz;
 }
 
+/* Push-form H*psi of nvec vectors at once from the determinants of src into the basis of dst
+ * (src == dst: the fixed-basis apply), x [src.n][nvec] and y [dst.n][nvec] complex
+ * interleaved, y overwritten.  The same visits as qo_apply_conserve (every (determinant,
+ * term) pair, ladder sign, lookup of the target, contributions with |a|^2 < 100*DBL_MIN per
+ * vector dropped); the values of the determinant strings that map a source onto itself are
+ * summed per source first, so the many diagonal strings cost no atomic adds.  Used for checks
+ * of the multi-vector paths on bases of millions of determinants (BlockOperatorPsi,
+ * Core/BlockWaveFunctionArithmetic.cpp:1575, runs the reference's loop for each vector). */
+void qo_apply_multi(int nterms, const int *len, const int64_t *off, const uint16_t *ops, const double *vre,
+                    const double *vim, const qo_wf *src, const qo_wf *dst, int nvec, const double *x, double *y)
+{
+  int64_t i;
+  for (i = 0; i < 2 * dst->n * nvec; i++) y[i] = 0.0;
+#pragma omp parallel for schedule(dynamic, 64)
+  for (i = 0; i < src->n; i++) {
+    uint8_t tmp[64];
+    const uint8_t *d = src->det + i * src->nword;
+    const double *xi = x + 2 * i * nvec;
+    double dre = 0.0, dim = 0.0;
+    int t, k, has_diag = 0;
+    for (t = 0; t < nterms; t++) {
+      int ph;
+      int64_t j;
+      memcpy(tmp, d, (size_t)src->nword);
+      ph = qo_ladder(tmp, ops + off[t], len[t]);
+      if (!ph) continue;
+      if (src == dst && memcmp(tmp, d, (size_t)src->nword) == 0) {
+        dre += ph * vre[t];
+        dim += ph * vim[t];
+        has_diag = 1;
+        continue;
+      }
+      j = qo_wf_find(dst, tmp);
+      if (j < 0) continue;
+      for (k = 0; k < nvec; k++) {
+        double xr = xi[2 * k], xm = xi[2 * k + 1];
+        double ar = ph * (vre[t] * xr - vim[t] * xm), ai = ph * (vre[t] * xm + vim[t] * xr);
+        if (ar * ar + ai * ai < 100 * DBL_MIN) continue;
+#pragma omp atomic
+        y[2 * (j * nvec + k)] += ar;
+#pragma omp atomic
+        y[2 * (j * nvec + k) + 1] += ai;
+      }
+    }
+    if (has_diag) {
+      for (k = 0; k < nvec; k++) {
+        double xr = xi[2 * k], xm = xi[2 * k + 1];
+        double ar = dre * xr - dim * xm, ai = dre * xm + dim * xr;
+#pragma omp atomic
+        y[2 * (i * nvec + k)] += ar;
+#pragma omp atomic
+        y[2 * (i * nvec + k) + 1] += ai;
+      }
+    }
+  }
+}
+
+/* the same over the source rows row0, row0+stride, ... < row1 (a spread sample) */
+int64_t qo_count_nnz_strided(int nterms, const int *len, const int64_t *off, const uint16_t *ops,
+                             const qo_wf *x, int64_t row0, int64_t row1, int64_t stride)
+{
+  int64_t c, cnt = (row1 - row0 + stride - 1) / stride, nnz = 0;
+#pragma omp parallel for reduction(+ : nnz) schedule(dynamic, 64)
+  for (c = 0; c < cnt; c++) {
+    uint8_t tmp[64];
+    int64_t i = row0 + c * stride;
+    int t;
+    for (t = 0; t < nterms; t++) {
+      memcpy(tmp, x->det + i * x->nword, (size_t)x->nword);
+      if (!qo_ladder(tmp, ops + off[t], len[t])) continue;
+      if (qo_wf_find(x, tmp) >= 0) nnz++;
+    }
+  }
+  return nnz;
+}
+
 /* ------------------------------------------------------------------ vector algebra */
 
 double qo_norm(const qo_wf *a)

@@ -780,7 +780,12 @@ static_assert(sizeof(LocalEntry) == 32 && offsetof(LocalEntry, tend) == 4 && off
 #endif
 #define QG_REGROUP_BUCKETS 64
 
-template <int W, int NV, bool FUSE>
+//
+// REAL: every value of the operator is real (the diagonal, the local entries and the listed
+// coefficients), so each connection is two FMAs and no imaginary part is read or tested.  The
+// general form's per-connection test of the imaginary part compiles to predicated FMAs, which
+// hold the FP64 pipe whether or not they take effect; a real operator would pay for all four.
+template <int W, int NV, bool FUSE, bool REAL>
 __global__ void __launch_bounds__(256, NV == 1 ? QG_APPLY_MIN_BLOCKS : 1)
     k_apply_list(const Key<W> *__restrict__ rows, int64_t n_rows, const int64_t *__restrict__ cptr,
                  const uint2 *__restrict__ conn, const double2 *__restrict__ coef, const double2 *__restrict__ diag,
@@ -796,7 +801,7 @@ __global__ void __launch_bounds__(256, NV == 1 ? QG_APPLY_MIN_BLOCKS : 1)
   if (live) {
     if (diag) {
       double2 dg = diag[r];
-      if (qg_is_nonzero(dg.y)) {
+      if (!REAL && qg_is_nonzero(dg.y)) {
 #pragma unroll
         for (int k = 0; k < NV; k++) {
           double2 xv = x[r * xs + vec0 + k];
@@ -833,10 +838,16 @@ __global__ void __launch_bounds__(256, NV == 1 ? QG_APPLY_MIN_BLOCKS : 1)
           if (js == QG_NO_INDEX) continue;
           j = js;
         }
-        const double2 v = __ldg(reinterpret_cast<const double2 *>(&E->vre));
-        bool cplx = qg_is_nonzero(v.y);
+        if (REAL) {
+          const double v = __ldg(&E->vre);
 #pragma unroll
-        for (int k = 0; k < NV; k++) qg_cmac(acc[k], v.x, v.y, cplx, __ldg(x + j * xs + vec0 + k));
+          for (int k = 0; k < NV; k++) qg_cmac(acc[k], v, 0.0, false, __ldg(x + j * xs + vec0 + k));
+        } else {
+          const double2 v = __ldg(reinterpret_cast<const double2 *>(&E->vre));
+          bool cplx = qg_is_nonzero(v.y);
+#pragma unroll
+          for (int k = 0; k < NV; k++) qg_cmac(acc[k], v.x, v.y, cplx, __ldg(x + j * xs + vec0 + k));
+        }
       }
     }
   }
@@ -884,13 +895,19 @@ __global__ void __launch_bounds__(256, NV == 1 ? QG_APPLY_MIN_BLOCKS : 1)
   if (live) {
     for (; p < pe; p++) {
       uint2 cn = __ldg(conn + p);
-      double2 cf = __ldg(coef + (cn.y & 0x7FFFFFFFu));
       int par = (int)(cn.y >> 31);
-      bool cplx = qg_is_nonzero(cf.y);
-      double vr = qg_flip_sign(cf.x, par), vi = qg_flip_sign(cf.y, par);
       int64_t j = cn.x;
+      if (REAL) {
+        double vr = qg_flip_sign(__ldg(&coef[cn.y & 0x7FFFFFFFu].x), par);
 #pragma unroll
-      for (int k = 0; k < NV; k++) qg_cmac(acc[k], vr, vi, cplx, __ldg(x + j * xs + vec0 + k));
+        for (int k = 0; k < NV; k++) qg_cmac(acc[k], vr, 0.0, false, __ldg(x + j * xs + vec0 + k));
+      } else {
+        double2 cf = __ldg(coef + (cn.y & 0x7FFFFFFFu));
+        bool cplx = qg_is_nonzero(cf.y);
+        double vr = qg_flip_sign(cf.x, par), vi = qg_flip_sign(cf.y, par);
+#pragma unroll
+        for (int k = 0; k < NV; k++) qg_cmac(acc[k], vr, vi, cplx, __ldg(x + j * xs + vec0 + k));
+      }
     }
   }
   if (!FUSE) {
@@ -1741,10 +1758,14 @@ bool qg_apply_uses_lists(qg_operator op, qg_basis b) {
 template <int W, int NV, bool FUSE>
 static void launch_apply_list_t(qg_context ctx, const OpBasisCache *c, const double2 *diag, qg_basis dst,
                                 const double2 *x, int xs, double2 *y, int ys, int vec0, int npass,
-                                const ApplyFuse &fz, const LocalView &lv) {
+                                const ApplyFuse &fz, const LocalView &lv, bool real) {
   dim3 grid((unsigned)qg_apply_grid(dst), (unsigned)npass);
-  k_apply_list<W, NV, FUSE><<<grid, 256, 0, ctx->stream>>>(
-      (const Key<W> *)dst->d_keys, dst->n, c->d_cptr, c->d_conn, c->d_coef, diag, x, xs, y, ys, vec0, fz, lv);
+  if (real)
+    k_apply_list<W, NV, FUSE, true><<<grid, 256, 0, ctx->stream>>>(
+        (const Key<W> *)dst->d_keys, dst->n, c->d_cptr, c->d_conn, c->d_coef, diag, x, xs, y, ys, vec0, fz, lv);
+  else
+    k_apply_list<W, NV, FUSE, false><<<grid, 256, 0, ctx->stream>>>(
+        (const Key<W> *)dst->d_keys, dst->n, c->d_cptr, c->d_conn, c->d_coef, diag, x, xs, y, ys, vec0, fz, lv);
   ctx->launches++;
 }
 
@@ -1755,7 +1776,7 @@ static void launch_apply_list_t(qg_context ctx, const OpBasisCache *c, const dou
 template <int W, bool FUSE>
 static void launch_apply_list(qg_context ctx, const OpBasisCache *c, const double2 *diag, qg_basis dst,
                               const double2 *x, int xs, double2 *y, int ys, int nvec, const ApplyFuse &fz,
-                              const LocalView &lv, int chunk) {
+                              const LocalView &lv, int chunk, bool real) {
   if (chunk <= 0) chunk = 8;
   int v = 0;
   while (v < nvec) {
@@ -1763,20 +1784,28 @@ static void launch_apply_list(qg_context ctx, const OpBasisCache *c, const doubl
     int per = left >= 8 ? 8 : left >= 4 ? 4 : left == 3 ? 3 : left >= 2 ? 2 : 1;
     int np = std::min((nvec - v) / per, 65535);
     if (per == 8)
-      launch_apply_list_t<W, 8, FUSE>(ctx, c, diag, dst, x, xs, y, ys, v, np, fz, lv);
+      launch_apply_list_t<W, 8, FUSE>(ctx, c, diag, dst, x, xs, y, ys, v, np, fz, lv, real);
     else if (per == 4)
-      launch_apply_list_t<W, 4, FUSE>(ctx, c, diag, dst, x, xs, y, ys, v, np, fz, lv);
+      launch_apply_list_t<W, 4, FUSE>(ctx, c, diag, dst, x, xs, y, ys, v, np, fz, lv, real);
     else if (per == 3)
-      launch_apply_list_t<W, 3, FUSE>(ctx, c, diag, dst, x, xs, y, ys, v, np, fz, lv);
+      launch_apply_list_t<W, 3, FUSE>(ctx, c, diag, dst, x, xs, y, ys, v, np, fz, lv, real);
     else if (per == 2)
-      launch_apply_list_t<W, 2, FUSE>(ctx, c, diag, dst, x, xs, y, ys, v, np, fz, lv);
+      launch_apply_list_t<W, 2, FUSE>(ctx, c, diag, dst, x, xs, y, ys, v, np, fz, lv, real);
     else
-      launch_apply_list_t<W, 1, FUSE>(ctx, c, diag, dst, x, xs, y, ys, v, np, fz, lv);
+      launch_apply_list_t<W, 1, FUSE>(ctx, c, diag, dst, x, xs, y, ys, v, np, fz, lv, real);
     v += per * np;
   }
 }
 
 // ------------------------------------------------------------------ entry points
+
+// Every value of the operator is real (its current values, after any rescale of a sum
+// operator): then the diagonal, the merged local entries and the listed coefficients are real.
+static bool op_values_real(qg_operator op) {
+  for (const HostTerm &h : op->fwd_host)
+    if (h.im != 0.0) return false;
+  return true;
+}
 
 static int tuned_chunk(const OpBasisCache *c, int nvec) {
   if (c)
@@ -1883,16 +1912,17 @@ static qg_status apply_chunked(qg_context ctx, qg_operator op, qg_basis dst, qg_
       QG_TRY(ensure_conn(ctx, op, dst, c));
       if (c->conn_state == 1) {
         const ApplyFuse &f = fz ? *fz : none;
+        const bool real = op_values_real(op);
         if (op->W == 1) {
           if (fz)
-            launch_apply_list<1, true>(ctx, c, diag, dst, x2, xs, y2, ys, nvec, f, lv, chunk);
+            launch_apply_list<1, true>(ctx, c, diag, dst, x2, xs, y2, ys, nvec, f, lv, chunk, real);
           else
-            launch_apply_list<1, false>(ctx, c, diag, dst, x2, xs, y2, ys, nvec, f, lv, chunk);
+            launch_apply_list<1, false>(ctx, c, diag, dst, x2, xs, y2, ys, nvec, f, lv, chunk, real);
         } else {
           if (fz)
-            launch_apply_list<2, true>(ctx, c, diag, dst, x2, xs, y2, ys, nvec, f, lv, chunk);
+            launch_apply_list<2, true>(ctx, c, diag, dst, x2, xs, y2, ys, nvec, f, lv, chunk, real);
           else
-            launch_apply_list<2, false>(ctx, c, diag, dst, x2, xs, y2, ys, nvec, f, lv, chunk);
+            launch_apply_list<2, false>(ctx, c, diag, dst, x2, xs, y2, ys, nvec, f, lv, chunk, real);
         }
         return qg_check_launch(ctx, "qg_apply");
       }
@@ -1999,14 +2029,17 @@ extern "C" qg_status qg_apply_host(qg_context ctx, qg_operator op, qg_basis dst,
 
 // ------------------------------------------------------------------ nnz count
 
+// Connections into rows row0, row0 + stride, ... (cnt of them): per row the (row, term) pairs
+// with a non-zero sign whose source lies in the basis.
 template <int W>
-__global__ void k_count(const Key<W> *__restrict__ rows, int64_t n, const GroupDev<W> *__restrict__ groups,
-                        int ngroups, const TermDev<W> *__restrict__ terms, const Slot *__restrict__ slots,
-                        uint64_t hmask, int offdiag_only, unsigned long long *out, unsigned int *err) {
-  int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+__global__ void k_count(const Key<W> *__restrict__ rows, int64_t row0, int64_t stride, int64_t cnt,
+                        const GroupDev<W> *__restrict__ groups, int ngroups, const TermDev<W> *__restrict__ terms,
+                        const Slot *__restrict__ slots, uint64_t hmask, int offdiag_only, unsigned long long *out,
+                        unsigned int *err) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   unsigned long long c = 0;
-  if (r < n) {
-    Key<W> d = rows[r];
+  if (i < cnt) {
+    Key<W> d = rows[row0 + i * stride];
     for (int g = 0; g < ngroups; g++) {
       bool ok = true;
 #pragma unroll
@@ -2030,23 +2063,28 @@ __global__ void k_count(const Key<W> *__restrict__ rows, int64_t n, const GroupD
   if ((threadIdx.x & 31) == 0 && c) atomicAdd(out, c);
 }
 
-static qg_status count_nnz(qg_context ctx, qg_operator op, qg_basis b, int offdiag, int64_t *nnz) {
+static qg_status count_nnz(qg_context ctx, qg_operator op, qg_basis b, int offdiag, int64_t row0, int64_t stride,
+                           int64_t *nnz) {
   *nnz = 0;
-  if (!b->n) return QG_OK;
+  if (row0 >= b->n) return QG_OK;
+  const int64_t cnt = (b->n - row0 + stride - 1) / stride;
   unsigned long long *d = nullptr;
   QG_CUDA(ctx, cudaMalloc(&d, 8));
-  QG_CUDA(ctx, cudaMemsetAsync(d, 0, 8, ctx->stream));
-  if (op->W == 1)
-    k_count<1><<<grid_for(b->n, 256), 256, 0, ctx->stream>>>(
-        (const Key<1> *)b->d_keys, b->n, (const GroupDev<1> *)op->pull.d_groups, op->pull.ngroups,
-        (const TermDev<1> *)op->pull.d_terms, b->d_slots, b->hcap - 1, offdiag, d, ctx->d_err);
-  else
-    k_count<2><<<grid_for(b->n, 256), 256, 0, ctx->stream>>>(
-        (const Key<2> *)b->d_keys, b->n, (const GroupDev<2> *)op->pull.d_groups, op->pull.ngroups,
-        (const TermDev<2> *)op->pull.d_terms, b->d_slots, b->hcap - 1, offdiag, d, ctx->d_err);
-  ctx->launches++;
+  cudaError_t e = cudaMemsetAsync(d, 0, 8, ctx->stream);
+  if (e == cudaSuccess) {
+    if (op->W == 1)
+      k_count<1><<<grid_for(cnt, 256), 256, 0, ctx->stream>>>(
+          (const Key<1> *)b->d_keys, row0, stride, cnt, (const GroupDev<1> *)op->pull.d_groups, op->pull.ngroups,
+          (const TermDev<1> *)op->pull.d_terms, b->d_slots, b->hcap - 1, offdiag, d, ctx->d_err);
+    else
+      k_count<2><<<grid_for(cnt, 256), 256, 0, ctx->stream>>>(
+          (const Key<2> *)b->d_keys, row0, stride, cnt, (const GroupDev<2> *)op->pull.d_groups, op->pull.ngroups,
+          (const TermDev<2> *)op->pull.d_terms, b->d_slots, b->hcap - 1, offdiag, d, ctx->d_err);
+    ctx->launches++;
+    e = cudaGetLastError();
+  }
   unsigned long long h = 0;
-  cudaError_t e = cudaMemcpyAsync(&h, d, 8, cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&h, d, 8, cudaMemcpyDeviceToHost, ctx->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   cudaFree(d);
   if (e != cudaSuccess) return qg_cuda_fail(ctx, e, "qg_count_nnz");
@@ -2056,7 +2094,13 @@ static qg_status count_nnz(qg_context ctx, qg_operator op, qg_basis b, int offdi
 
 extern "C" qg_status qg_count_nnz(qg_context ctx, qg_operator op, qg_basis b, int64_t *nnz) {
   if (!ctx || !op || !b || !nnz || op->nf != b->nf) return QG_ERR_ARG;
-  return count_nnz(ctx, op, b, 0, nnz);
+  return count_nnz(ctx, op, b, 0, 0, 1, nnz);
+}
+
+extern "C" qg_status qg_count_nnz_rows(qg_context ctx, qg_operator op, qg_basis b, int64_t row0, int64_t stride,
+                                       int32_t offdiag, int64_t *nnz) {
+  if (!ctx || !op || !b || !nnz || op->nf != b->nf || row0 < 0 || stride < 1) return QG_ERR_ARG;
+  return count_nnz(ctx, op, b, offdiag != 0, row0, stride, nnz);
 }
 
 extern "C" qg_status qg_set_autotune(qg_context ctx, int32_t on) {
@@ -2148,5 +2192,5 @@ extern "C" qg_status qg_apply_chunk(qg_context ctx, qg_operator op, qg_basis b, 
 
 extern "C" qg_status qg_count_nnz_offdiag(qg_context ctx, qg_operator op, qg_basis b, int64_t *nnz) {
   if (!ctx || !op || !b || !nnz || op->nf != b->nf) return QG_ERR_ARG;
-  return count_nnz(ctx, op, b, 1, nnz);
+  return count_nnz(ctx, op, b, 1, 0, 1, nnz);
 }
