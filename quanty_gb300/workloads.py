@@ -8,9 +8,9 @@
   (2p, 3d, 7 bath shells of 10), 3d F0 = Udd = 7.5 plus the atomic multiplet terms, 2p-3d F0 =
   Upd = 8.5, bath energies uniform on [-5, 5] eV from seed 0, hybridisations from a 7-point
   discretisation of a semicircle density of states of half-width 2 eV (sum of V_k^2 = 4 eV^2,
-  each bath orbital coupled to the 3d orbital of the same index), and a weak random Hermitian
-  one-body field (<= 0.01 eV, seed 1) on the 3d shell that lifts the point-group symmetry so
-  the closure of one determinant is the whole sector.  Its sector: 2p6, 44
+  each bath orbital coupled to the 3d orbital of the same index), and a weak random real
+  symmetric one-body field (<= 0.01 eV, seed 1) on the 3d shell that lifts the point-group
+  symmetry so the closure of one determinant is the whole sector; every term is real.  Its sector: 2p6, 44
   electrons, at most 2 holes (particles) per filled (empty) shell, at most 3 holes in all
   filled shells together and at most 2 particles in all empty shells together: 47,481,880
   determinants.
@@ -66,7 +66,7 @@ def merged(terms):
 
 
 def anderson_impurity(nshell=7, seed=0, udd=7.5, upd=8.5, half_width=2.0, v2_total=4.0, hole_max=3,
-                      particle_max=2, field=0.01, delta=0.0, core_holes=0):
+                      particle_max=2, field=0.01, delta=0.0, core_holes=0, complex_field=False):
     """Returns (H, restrictions, seed determinant, info dict)."""
     nf = 16 + 10 * nshell
     at = _load()
@@ -94,13 +94,18 @@ def anderson_impurity(nshell=7, seed=0, udd=7.5, upd=8.5, half_width=2.0, v2_tot
             terms.append(([b, b | CREATION], float(eps[k])))
             terms.append(([b, d | CREATION], float(V[k])))
             terms.append(([d, b | CREATION], float(V[k])))
-    # a weak random Hermitian one-body field on the 3d shell (seed 0, entries up to `field`
-    # eV) breaks the point-group symmetry, so the closure of the seed determinant under H
-    # is the whole restricted sector rather than one symmetry block of it
+    # a weak random one-body field on the 3d shell (seed + 1, entries up to `field` eV) breaks
+    # the point-group symmetry, so the closure of the seed determinant under H is the whole
+    # restricted sector rather than one symmetry block of it.  It is real symmetric, like the
+    # rest of this Hamiltonian (the reference's atomic H and HX carry real values only);
+    # complex_field=True draws a complex Hermitian one instead (same connectivity, so the
+    # same sector), which makes every impurity move complex-valued.
     fr = np.random.default_rng(seed + 1)
     for a in range(10):
         for b in range(a, 10):
-            v = field * complex(fr.uniform(-1, 1), fr.uniform(-1, 1) if a != b else 0.0)
+            re = fr.uniform(-1, 1)
+            im = fr.uniform(-1, 1) if a != b else 0.0
+            v = field * complex(re, im if complex_field else 0.0)
             terms.append(([d_orb[b], d_orb[a] | CREATION], v))
             if a != b:
                 terms.append(([d_orb[a], d_orb[b] | CREATION], v.conjugate()))
