@@ -174,12 +174,15 @@ qg_status qg_gather_bandwidth(qg_context ctx, int64_t bytes, double *gbs);
  * with events.  The measured denominator of the H*psi FP64 roofline. */
 qg_status qg_fp64_peak(qg_context ctx, double *gops);
 
-/* Eigenpairs of a small dense Hermitian matrix on the host: a is k x k row-major with
- * interleaved (re, im); w receives all k eigenvalues ascending, v (k x nv row-major,
- * interleaved) the eigenvectors of the lowest nv as columns.  Householder reduction, implicit
- * QL.  Replaces the reference's zheevd calls on projected matrices (Core/BlockLanczos.cpp:5530).
- * No device work. */
-qg_status qg_hermitian_eigh(int32_t k, const double *a, double *w, double *v, int32_t nv);
+/* Eigenpairs of a dense Hermitian matrix, computed on the device (cyclic Jacobi with the
+ * round-robin ordering: every step rotates k/2 disjoint index pairs at once): a_host is k x k
+ * row-major with interleaved (re, im); w_host receives all k eigenvalues ascending, v_host
+ * (k x nv row-major, interleaved) the eigenvectors of the lowest nv as columns.  Replaces the
+ * reference's zheevd calls on dense and projected matrices (Core/BlockLanczos.cpp:5530, :370-501;
+ * HermitianCompactMatrixToListOfPoles, Core/BasicMath/BasicMath_CompactMatrixVector.cpp:3990).
+ * QG_ERR_TIMEOUT if the rotations have not converged after 60 sweeps. */
+qg_status qg_hermitian_eigh(qg_context ctx, int32_t k, const double *a_host, double *w_host, double *v_host,
+                            int32_t nv);
 
 /* Autotuning of the multi-vector apply (no counterpart in the reference, whose loops handle one
  * vector at a time): the first apply of an operator with nvec >= 2 vectors on a basis (as
@@ -252,7 +255,9 @@ qg_status qg_axpy(qg_context ctx, int64_t n, int32_t nvec, const double *alpha_h
 /* qg_dot for callers that cannot allocate device memory (no counterpart in the reference,
  * which has no GPU): per-vector <x_k|y_k> of nvec vectors of n complex entries (device
  * pointers) into out_dev (nvec complex values, device memory), on the given CUDA stream
- * (NULL = legacy default stream).  It calls no cudaMalloc/cudaFree: the block partial sums
+ * (NULL = legacy default stream).  It takes no context: it runs on the calling thread's
+ * current device (cudaGetDevice), to which the pointers and the stream must belong.  It calls
+ * no cudaMalloc/cudaFree: the block partial sums
  * live in a fixed device array inside the library (1 MiB per device), so nvec is limited to
  * 64 (larger values return QG_ERR_ARG).  The first call on a device looks up that array's
  * address and should come before any stream capture.  All calls on a device share the

@@ -732,14 +732,14 @@ def OperatorToDeterminantMatrix(O, basis, eng=None):
 
 def hermitian_eigh(M, nvec=None, eng=None):
     """All eigenvalues (ascending) and the lowest nvec eigenvectors (columns) of a Hermitian
-    matrix, by the library's host Householder + QL solver."""
+    matrix, by the library's device eigensolver (cyclic Jacobi)."""
     eng = eng or engine()
     k = M.shape[0]
     nv = k if nvec is None else int(nvec)
     a = np.ascontiguousarray(M, dtype=np.complex128)
     w = np.zeros(k)
     v = np.zeros((k, max(nv, 1)), dtype=np.complex128)
-    eng.check(eng.L.qg_hermitian_eigh(k, _ptr(a), _ptr(w), _ptr(v), nv))
+    eng.check(eng.L.qg_hermitian_eigh(eng.ctx, k, _ptr(a), _ptr(w), _ptr(v), nv))
     return w, v[:, :nv]
 
 

@@ -94,7 +94,6 @@ extern "C" qg_status qg_init(int device, qg_context *out) {
 extern "C" qg_status qg_finalize(qg_context ctx) {
   if (!ctx) return QG_OK;
   cudaStreamSynchronize(ctx->stream);
-  qg_blas_release(ctx);
   cudaFree(ctx->d_err);
   cudaFree(ctx->d_scratch);
   cudaFreeHost(ctx->h_pinned);

@@ -7,10 +7,10 @@
 // the projected matrix with zheevd (:5530) and restarts from the Ritz vectors (:5554-5573)
 // until the variance <H^2> - <H>^2 of every vector is below "Zero".  The same structure here:
 // H*psi is the pull kernel, the Gram products and updates of whole blocks are plain complex
-// GEMMs over the n x K Krylov block (row-major, K columns; cuBLAS, qgpu_blas.cu), single
+// products over the n x K Krylov block (row-major, K columns; qgpu_blocks.cu), single
 // columns use the partial-sum kernels below, and the projected matrix (K <= a few hundred)
-// is diagonalised on the host: Householder reduction to a real tridiagonal matrix,
-// implicit QL with Wilkinson shifts, then the wanted eigenvectors transformed back.
+// is diagonalised on the device (cyclic Jacobi, qgpu_jacobi.cu), its lowest eigenvectors left
+// in device memory for the Ritz combination.
 //
 // Block size: when more than three states are wanted, a few guard vectors join the block
 // (up to half the wanted count, at most 8) and only the wanted states are tested for
@@ -197,11 +197,11 @@ struct Gram {
   qg_context ctx;
   int64_t n;
   double2 *part = nullptr, *out = nullptr;
-  int64_t cap = 0;
+  int64_t cap = 0, part_elems = 0;
   int nchunk = 1;
   int64_t chunk = 1;
   int nblk = 1;  // blocks of the one-column Gram kernels
-  qg_status init(qg_context c, int64_t nn, int maxm) {
+  qg_status init(qg_context c, int64_t nn, int maxm, int kcol) {
     ctx = c;
     n = nn;
     chunk = std::max<int64_t>(4096, (nn + 1023) / 1024);
@@ -209,7 +209,11 @@ struct Gram {
     if (nchunk < 1) nchunk = 1;
     nblk = (int)std::max<int64_t>(1, std::min<int64_t>(4LL * c->num_sms, (nn + 255) / 256));
     cap = maxm;
-    QG_CUDA(ctx, cudaMalloc(&part, (size_t)std::max(nchunk * (int64_t)maxm, (int64_t)nblk * 32 * QG_GRAM_LANE_COLS) * 16));
+    // partial sums: one column against up to kcol columns (nchunk chunks, or nblk blocks of the
+    // one-column kernels), or the row-chunk tiles of a block product (qg_block_gram uses as many
+    // chunks as fit, at most the few dozen that fill the SMs)
+    part_elems = std::max<int64_t>(std::max<int64_t>(nchunk * (int64_t)kcol, (int64_t)nblk * 32 * QG_GRAM_LANE_COLS), 16 * (int64_t)maxm);
+    QG_CUDA(ctx, cudaMalloc(&part, (size_t)part_elems * 16));
     QG_CUDA(ctx, cudaMalloc(&out, (size_t)maxm * 16));
     return QG_OK;
   }
@@ -222,8 +226,8 @@ struct Gram {
                 std::vector<cd> *host) {
     int m = ka * kb;
     if (m > cap || m <= 0) return QG_ERR_ARG;
-    if (kb > 1) {  // a block against a block: a plain GEMM (cuBLAS)
-      QG_TRY(qg_zgemm_ahb(ctx, A + a0, lda, ka, B + b0, ldb, kb, n, out));
+    if (kb > 1) {  // a block against a block: tiled products, partial sums per row chunk
+      QG_TRY(qg_block_gram(ctx, A + a0, lda, ka, B + b0, ldb, kb, n, out, part, part_elems));
     } else if (ka <= 32 * QG_GRAM_LANE_COLS) {  // one column: wide partial sums, fixed-order reduction
       cudaStream_t s = ctx->stream;
       if (ka == 1)
@@ -259,11 +263,6 @@ struct Gram {
 
 }  // namespace
 
-void qg_host_eigh(int k, const std::vector<std::complex<double>> &A, std::vector<double> &w,
-                  std::vector<std::complex<double>> &V) {
-  hermitian_eigh(k, A, w, V, k);
-}
-
 extern "C" qg_status qg_block_groundstate(qg_context ctx, qg_operator op, qg_basis b, int32_t nwant, double *x_dev,
                                           double *energies_host, double tol, int32_t max_krylov,
                                           int32_t max_restarts, int32_t *iterations) {
@@ -281,17 +280,22 @@ extern "C" qg_status qg_block_groundstate(qg_context ctx, qg_operator op, qg_bas
   K = (K / p) * p;
   if (K < p) K = p;
   cudaStream_t s = ctx->stream;
-  double2 *V = nullptr, *W = nullptr, *Cd = nullptr, *X = nullptr;
+  double2 *V = nullptr, *W = nullptr, *Cd = nullptr, *X = nullptr, *Md = nullptr;
+  double *wd = nullptr;
   size_t vb = (size_t)n * K * 16, wb = (size_t)n * p * 16;
   cudaError_t e = cudaMalloc(&V, vb);
   if (e == cudaSuccess) e = cudaMalloc(&W, wb);
   if (e == cudaSuccess) e = cudaMalloc(&X, wb);
   if (e == cudaSuccess) e = cudaMalloc(&Cd, (size_t)K * std::max(K, p) * 16);
+  if (e == cudaSuccess) e = cudaMalloc(&Md, (size_t)K * K * 16);
+  if (e == cudaSuccess) e = cudaMalloc(&wd, (size_t)K * sizeof(double));
   if (e != cudaSuccess) {
     cudaFree(V);
     cudaFree(W);
     cudaFree(X);
     cudaFree(Cd);
+    cudaFree(Md);
+    cudaFree(wd);
     ctx->last_error = "qg_block_groundstate: out of device memory";
     return QG_ERR_OOM;
   }
@@ -304,7 +308,7 @@ extern "C" qg_status qg_block_groundstate(qg_context ctx, qg_operator op, qg_bas
     ctx->launches++;
   }
   Gram G;
-  qg_status st = G.init(ctx, n, K * std::max(K, p));
+  qg_status st = G.init(ctx, n, K * std::max(K, p), K);
   std::vector<double> theta(p, 0.0);
   int it = 0;
   bool converged = false;
@@ -388,7 +392,7 @@ extern "C" qg_status qg_block_groundstate(qg_context ctx, qg_operator op, qg_bas
         if (st != QG_OK) break;
         for (int i = 0; i < k; i++)
           for (int j = 0; j < bs; j++) T[(size_t)i * K + j0 + j] += c[(size_t)i * bs + j];
-        st = qg_zgemm_acc(ctx, V, K, k, G.out, W, p, bs, n, -1.0, 1.0);
+        st = qg_block_update(ctx, V, K, k, G.out, W, p, bs, n, -1.0, 1.0);
       }
       if (st != QG_OK || k + bs > Kcur) break;
       // append W as new columns and orthonormalise them
@@ -426,17 +430,38 @@ extern "C" qg_status qg_block_groundstate(qg_context ctx, qg_operator op, qg_bas
         // entries above the computed block columns are only known through symmetry
         M[(size_t)i * k + j] = (a == cd(0, 0)) ? bb : ((bb == cd(0, 0)) ? a : 0.5 * (a + bb));
       }
-    std::vector<double> w;
-    std::vector<cd> Yp;
-    hermitian_eigh(k, M, w, Yp, p);
-    e = cudaMemcpyAsync(Cd, Yp.data(), Yp.size() * 16, cudaMemcpyHostToDevice, s);
+    // Ritz pairs on the device: the lowest p eigenvectors of M straight into Cd (k x p)
+    const int nv = std::min(p, k);
+    e = cudaMemcpyAsync(Md, M.data(), M.size() * 16, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && nv < p) e = cudaMemsetAsync(Cd, 0, (size_t)k * p * 16, s);
     if (e != cudaSuccess) {
-      st = qg_cuda_fail(ctx, e, "ritz upload");
+      st = qg_cuda_fail(ctx, e, "projected matrix upload");
       break;
     }
-    st = qg_zgemm_acc(ctx, V, K, k, Cd, X, p, p, n, 1.0, 0.0);
+    st = qg_eigh_device(ctx, k, Md, wd, Cd, nv);
     if (st != QG_OK) break;
-    for (int j = 0; j < p; j++) theta[j] = w[j];
+    if (nv < p) {  // eigenvectors packed k x nv; spread them to k x p (the remaining columns stay zero)
+      std::vector<cd> Yp((size_t)k * nv), Yw((size_t)k * p, cd(0, 0));
+      e = cudaMemcpyAsync(Yp.data(), Cd, Yp.size() * 16, cudaMemcpyDeviceToHost, s);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+      for (int i = 0; i < k && e == cudaSuccess; i++)
+        for (int j = 0; j < nv; j++) Yw[(size_t)i * p + j] = Yp[(size_t)i * nv + j];
+      if (e == cudaSuccess) e = cudaMemcpyAsync(Cd, Yw.data(), Yw.size() * 16, cudaMemcpyHostToDevice, s);
+      if (e != cudaSuccess) {
+        st = qg_cuda_fail(ctx, e, "ritz vectors");
+        break;
+      }
+    }
+    st = qg_block_update(ctx, V, K, k, Cd, X, p, p, n, 1.0, 0.0);
+    if (st != QG_OK) break;
+    std::vector<double> w(nv);
+    e = cudaMemcpyAsync(w.data(), wd, (size_t)nv * sizeof(double), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+      st = qg_cuda_fail(ctx, e, "ritz values");
+      break;
+    }
+    for (int j = 0; j < p; j++) theta[j] = j < nv ? w[j] : 0.0;
     // convergence: variance <(H - theta)^2> = |H x - theta x|^2 per vector, formed from the
     // residual itself (no cancellation between <H^2> and <H>^2)
     st = qg_apply_strided(ctx, op, b, b, (const double *)X, p, (double *)W, p, p, nullptr);
@@ -450,7 +475,7 @@ extern "C" qg_status qg_block_groundstate(qg_context ctx, qg_operator op, qg_bas
         st = qg_cuda_fail(ctx, e, "residual");
         break;
       }
-      st = qg_zgemm_acc(ctx, X, p, p, Cd, W, p, p, n, -1.0, 1.0);
+      st = qg_block_update(ctx, X, p, p, Cd, W, p, p, n, -1.0, 1.0);
       if (st != QG_OK) break;
     }
     std::vector<cd> hh;
@@ -472,6 +497,8 @@ extern "C" qg_status qg_block_groundstate(qg_context ctx, qg_operator op, qg_bas
   cudaFree(W);
   cudaFree(X);
   cudaFree(Cd);
+  cudaFree(Md);
+  cudaFree(wd);
   for (int j = 0; j < nwant; j++) energies_host[j] = theta[j];
   if (iterations) *iterations = it;
   if (st == QG_OK) st = qg_check_device_error(ctx, "qg_block_groundstate");

@@ -95,7 +95,6 @@ struct qg_context_s {
   bool use_graphs = true;             // capture Lanczos step sequences into CUDA graphs
   bool autotune = true;               // time the vectors-per-pass choices of multi-vector applies
   bool conn_lists = true;             // resolve hashed connections once per (operator, basis)
-  void *blas = nullptr;               // cuBLAS handle of the dense block products (created on first use)
 };
 
 // A term table in one device allocation: ngroups GroupDev followed by nterms TermDev.
@@ -352,27 +351,23 @@ int qg_apply_grid(qg_basis dst);
 // per-(operator, basis) cache first), so a caller need not pack x into the hash slots.
 bool qg_apply_uses_lists(qg_operator op, qg_basis b);
 
-// Hermitian eigenproblem of a small host matrix (row-major k x k): ascending values, columns of
-// V the eigenvectors (cyclic Jacobi, qgpu_eigen.cu)
-#include <complex>
-// Householder + implicit QL (qgpu_hosteig.cu): all eigenvalues ascending, the lowest nv
-// eigenvectors as the columns of V (row-major, k x nv); A row-major k x k.
-void hermitian_eigh(int k, std::vector<std::complex<double>> A, std::vector<double> &w,
-                    std::vector<std::complex<double>> &V, int nv);
-void qg_host_eigh(int k, const std::vector<std::complex<double>> &A, std::vector<double> &w,
-                  std::vector<std::complex<double>> &V);
+// Hermitian eigenproblems on the device (qgpu_jacobi.cu): A (k x k row-major, device,
+// overwritten) -> eigenvalues ascending (w_dev, k) and the lowest nv eigenvectors as the columns
+// of V_dev (k x nv row-major); the host-buffer form copies in and out.
+qg_status qg_eigh_device(qg_context ctx, int k, double2 *A, double *w_dev, double2 *V_dev, int nv);
+qg_status qg_eigh_host_io(qg_context ctx, int k, const double *a_host, double *w_host, double *v_host, int nv);
 int qg_partial_blocks(qg_context ctx, int64_t n);
 
-// dense complex block products (qgpu_blas.cu, cuBLAS); row-major n x k blocks
-//   C (ka x kb row-major) = A^H B;   X = beta X + alpha A M  (M ka x kb row-major)
-qg_status qg_zgemm_ahb(qg_context ctx, const double2 *A, int lda, int ka, const double2 *B, int ldb, int kb,
-                       int64_t n, double2 *C);
-qg_status qg_zgemm_acc(qg_context ctx, const double2 *A, int lda, int ka, const double2 *M, double2 *X, int ldx,
-                       int kb, int64_t n, double alpha, double beta);
+// dense complex block products (qgpu_blocks.cu); row-major n x k blocks
+//   C (ka x kb row-major) = A^H B, with a work buffer of work_elems complex entries for the
+//   partial sums;   X = beta X + alpha A M  (M ka x kb row-major)
+qg_status qg_block_gram(qg_context ctx, const double2 *A, int lda, int ka, const double2 *B, int ldb, int kb,
+                        int64_t n, double2 *C, double2 *work, int64_t work_elems);
+qg_status qg_block_update(qg_context ctx, const double2 *A, int lda, int ka, const double2 *M, double2 *X, int ldx,
+                          int kb, int64_t n, double alpha, double beta);
 // out (n x np row-major) = sum_i K_i C[i][:], K vector-major (K[i * n + r])
-qg_status qg_zgemm_combine(qg_context ctx, const double2 *K, int64_t n, int ntri, const double2 *C, int np,
+qg_status qg_block_combine(qg_context ctx, const double2 *K, int64_t n, int ntri, const double2 *C, int np,
                            double2 *out);
-void qg_blas_release(qg_context ctx);
 
 // reductions (qgpu_krylov.cu)
 qg_status qg_dot_dev(qg_context ctx, int64_t n, int nvec, const double *x, const double *y, double *out_dev);

@@ -220,7 +220,46 @@ extern "C" qg_status qg_lanczos_krylov(qg_context ctx, qg_operator op, qg_basis 
 
 // ------------------------------------------------------------------ RIXS
 
-static void tridiag_eigen(int nt, const double *a, const double *b, std::vector<double> &ev, std::vector<cd> &Z) {
+// Lowest and highest eigenvalue of the symmetric tridiagonal matrix diag a[1..nt], off-diagonal
+// b[1..nt-1] by bisection on Sturm counts inside the Gershgorin interval: only the final-state
+// pole range is needed of the second-stage chains, not their eigenvectors.
+static int sturm_below(int nt, const double *a, const double *b, double x) {
+  int cnt = 0;
+  double d = 1.0;
+  for (int i = 0; i < nt; i++) {
+    const double off = i ? b[i] * b[i] : 0.0;
+    d = (a[i + 1] - x) - (i ? off / d : 0.0);
+    if (d == 0.0) d = -1e-300;  // a zero pivot counts as negative (the limit from below)
+    cnt += d < 0.0;
+  }
+  return cnt;
+}
+
+static void tridiag_extremes(int nt, const double *a, const double *b, double *lo, double *hi) {
+  double g0 = DBL_MAX, g1 = -DBL_MAX;
+  for (int i = 0; i < nt; i++) {
+    const double r = (i ? std::fabs(b[i]) : 0.0) + (i + 1 < nt ? std::fabs(b[i + 1]) : 0.0);
+    g0 = std::min(g0, a[i + 1] - r);
+    g1 = std::max(g1, a[i + 1] + r);
+  }
+  for (int which = 0; which < 2; which++) {
+    // the eigenvalue with (which ? nt - 1 : 0) eigenvalues below it
+    const int target = which ? nt - 1 : 0;
+    double l = g0, h = g1;
+    for (int it = 0; it < 200 && h - l > 4 * DBL_EPSILON * std::max(std::fabs(l), std::fabs(h)); it++) {
+      const double m = 0.5 * (l + h);
+      if (m <= l || m >= h) break;
+      if (sturm_below(nt, a, b, m) > target)
+        h = m;
+      else
+        l = m;
+    }
+    (which ? *hi : *lo) = 0.5 * (l + h);
+  }
+}
+
+static qg_status tridiag_eigen(qg_context ctx, int nt, const double *a, const double *b, std::vector<double> &ev,
+                               std::vector<cd> &Z) {
   // diag a[1..nt], off-diagonal b[1..nt-1] (TriDiagonalMatrixToEigensystem's matrix)
   std::vector<cd> M((size_t)nt * nt, cd(0, 0));
   for (int i = 0; i < nt; i++) {
@@ -230,7 +269,9 @@ static void tridiag_eigen(int nt, const double *a, const double *b, std::vector<
       M[(size_t)(i + 1) * nt + i] = b[i + 1];
     }
   }
-  qg_host_eigh(nt, M, ev, Z);
+  ev.assign(nt, 0.0);
+  Z.assign((size_t)nt * nt, cd(0, 0));
+  return qg_eigh_host_io(ctx, nt, (const double *)M.data(), ev.data(), (double *)Z.data(), nt);
 }
 
 extern "C" qg_status qg_resonant_spectra(qg_context ctx, qg_operator H1, qg_operator H2, qg_operator T1,
@@ -279,7 +320,7 @@ extern "C" qg_status qg_resonant_spectra(qg_context ctx, qg_operator H1, qg_oper
       break;
     std::vector<double> ev;
     std::vector<cd> Z;
-    tridiag_eigen(o->ntri1, a1.data(), b1v.data(), ev, Z);
+    if ((st = tridiag_eigen(ctx, o->ntri1, a1.data(), b1v.data(), ev, Z)) != QG_OK) break;
     int nt = o->ntri1;
     // intermediate-state energy range defaults (Core/ResonantSpectra.cpp:80-112)
     if (o->emin1 > 0.001 * DBL_MAX && o->emax1 < -0.001 * DBL_MAX) {
@@ -312,7 +353,7 @@ extern "C" qg_status qg_resonant_spectra(qg_context ctx, qg_operator H1, qg_oper
     if ((e = cudaMalloc(&Cd, C.size() * 16)) != cudaSuccess) break;
     if ((e = cudaMemcpyAsync(Cd, C.data(), C.size() * 16, cudaMemcpyHostToDevice, s)) != cudaSuccess) break;
     if ((e = cudaMalloc(&gt, (size_t)std::max<int64_t>(n1, 1) * np * 16)) != cudaSuccess) break;
-    if ((st = qg_zgemm_combine(ctx, (const double2 *)K, n1, nt, Cd, np, (double2 *)gt)) != QG_OK) break;
+    if ((st = qg_block_combine(ctx, (const double2 *)K, n1, nt, Cd, np, (double2 *)gt)) != QG_OK) break;
     // T2 targets of all operators, their closure under H2: the common final-state basis
     for (int j = 0; j < nt2 && st == QG_OK; j++) {
       qg_basis tj = nullptr;
@@ -343,11 +384,10 @@ extern "C" qg_status qg_resonant_spectra(qg_context ctx, qg_operator H1, qg_oper
     // final-state energy range from the poles (Core/ResonantSpectra.cpp:221-262)
     double lo = DBL_MAX, hi = -DBL_MAX;
     for (int c = 0; c < ncol; c++) {
-      std::vector<double> ev2;
-      std::vector<cd> Z2;
-      tridiag_eigen(o->ntri2, &a2[(size_t)c * (o->ntri2 + 1)], &b2v[(size_t)c * o->ntri2], ev2, Z2);
-      lo = std::min(lo, ev2.front() - o->energy2);
-      hi = std::max(hi, ev2.back() - o->energy2);
+      double e0, e1;
+      tridiag_extremes(o->ntri2, &a2[(size_t)c * (o->ntri2 + 1)], &b2v[(size_t)c * o->ntri2], &e0, &e1);
+      lo = std::min(lo, e0 - o->energy2);
+      hi = std::max(hi, e1 - o->energy2);
     }
     if (o->emin2 > 0.001 * DBL_MAX || o->emax2 < -0.001 * DBL_MAX) {
       if (o->emin2 > 0.001 * DBL_MAX && o->emax2 < -0.001 * DBL_MAX) {
