@@ -191,11 +191,15 @@ extern "C" qg_status qg_axpy(qg_context ctx, int64_t n, int32_t nvec, const doub
   if (!n) return QG_OK;
   double2 *d = nullptr;
   QG_CUDA(ctx, cudaMalloc(&d, nvec * 16));
-  QG_CUDA(ctx, cudaMemcpyAsync(d, alpha_host, nvec * 16, cudaMemcpyHostToDevice, ctx->stream));
-  int64_t tot = n * nvec;
-  k_axpy<<<(unsigned)((tot + 255) / 256), 256, 0, ctx->stream>>>(n, nvec, d, (const double2 *)x, (double2 *)y);
-  ctx->launches++;
-  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  // every path from here frees d
+  cudaError_t e = cudaMemcpyAsync(d, alpha_host, nvec * 16, cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess) {
+    int64_t tot = n * nvec;
+    k_axpy<<<(unsigned)((tot + 255) / 256), 256, 0, ctx->stream>>>(n, nvec, d, (const double2 *)x, (double2 *)y);
+    ctx->launches++;
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   cudaFree(d);
   if (e != cudaSuccess) return qg_cuda_fail(ctx, e, "qg_axpy");
   return qg_check_launch(ctx, "qg_axpy");

@@ -7,8 +7,9 @@
 // partial sums live in a file-scope device array of fixed size, the caller passes the inputs
 // and a device output, and nothing is allocated.
 //
-// The array's name is only a host-side stand-in for host code; the device address is obtained
-// once per device with cudaGetSymbolAddress (the first call on a device does this set-up, so
+// The call works on the calling thread's current device (cudaGetDevice): the pointers and the
+// stream must belong to it.  The array's name is only a host-side stand-in for host code; the
+// device address is obtained once per device with cudaGetSymbolAddress (the first call on a device does this set-up, so
 // that first call should come before any stream capture).  Every call on a device shares the
 // array and leaves its partial sums behind; calls that overlap on the GPU (other streams, or
 // without ordering between them) race on it.  Each call writes every partial it later reads,
@@ -24,9 +25,12 @@
 
 static __device__ __align__(256) double2 g_noalloc_partials[QG_NOALLOC_MAX_VECTORS * QG_NOALLOC_MAX_BLOCKS];
 
-// the reduction kernels of qgpu_krylov.cu
+// the reduction kernels of qgpu_krylov.cu: per vector (one vector), or over the flat row-major
+// block with a fixed vector per thread (several vectors: coalesced, every row read once)
 __global__ void k_dot_partial(int64_t n, int nvec, const double2 *__restrict__ x, const double2 *__restrict__ y,
                               double2 *part);
+__global__ void k_dot_partial_flat(int64_t len, int nvec, const double2 *__restrict__ x,
+                                   const double2 *__restrict__ y, double2 *part);
 __global__ void k_reduce_partials(const double2 *part, int nblk, int nvec, double2 *out);
 
 namespace {
@@ -77,8 +81,14 @@ extern "C" qg_status qg_dot_noalloc(int64_t n, int32_t nvec, const double *x_dev
   if (blocks > QG_NOALLOC_MAX_BLOCKS) blocks = QG_NOALLOC_MAX_BLOCKS;
   if (blocks < 1) blocks = 1;
   cudaStream_t s = (cudaStream_t)stream;
-  k_dot_partial<<<(unsigned)blocks, 256, (256 / 32) * sizeof(double2), s>>>(n, nvec, (const double2 *)x_dev,
-                                                                          (const double2 *)y_dev, part);
+  if (nvec > 1) {  // threads per block a multiple of nvec, so each thread keeps one vector
+    const int T = nvec * (256 / nvec);
+    k_dot_partial_flat<<<(unsigned)blocks, T, T * sizeof(double2), s>>>(n * nvec, nvec, (const double2 *)x_dev,
+                                                                       (const double2 *)y_dev, part);
+  } else {
+    k_dot_partial<<<(unsigned)blocks, 256, (256 / 32) * sizeof(double2), s>>>(n, nvec, (const double2 *)x_dev,
+                                                                            (const double2 *)y_dev, part);
+  }
   k_reduce_partials<<<1, 256, 0, s>>>(part, (int)blocks, nvec, (double2 *)out_dev);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? QG_OK : QG_ERR_CUDA;

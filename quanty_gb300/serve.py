@@ -34,6 +34,20 @@ def _footprint(n_det, nvec, ntri=0, krylov=False):
     return int(keys + table + lists + vectors + kry + (64 << 20))
 
 
+def _final_basis_size(H, Ts, psis, options):
+    """Determinants of CreateSpectra's final-state basis: the closure under H (within the
+    Restrictions option) of the targets of every T on every initial state."""
+    R = api.parse_restrictions((options or {}).get("Restrictions"))
+    eng = api.engine()
+    dets = np.concatenate([p.det for p in psis])
+    b0, _ = api.Basis.from_bytes(H.nf, dets, eng)
+    bt = None
+    for t in Ts:
+        tb = api.OperatorPsiBasis(t, b0, R, eng)
+        bt = tb if bt is None else api.basis_union(bt, tb, eng)
+    return max(int(api.closure_of(H, bt, R, -1, eng).n), 1)
+
+
 class SpectraJob:
     """CreateSpectra(H, T, psi, options) (LuaInterface/ssp.cpp:1906)."""
 
@@ -43,8 +57,11 @@ class SpectraJob:
         self.nspec = len(T) * len(psi)
 
     def footprint(self):
-        n = self.n_det_hint or max(p.N for p in self.psi) * 8
-        return _footprint(n, self.nspec)
+        # without a hint the final basis is measured: the closure under H of the targets of
+        # every T (what CreateSpectra builds), so admission never counts on a guessed size
+        if self.n_det_hint is None:
+            self.n_det_hint = _final_basis_size(self.H, self.T, self.psi, self.options)
+        return _footprint(self.n_det_hint, self.nspec)
 
     def run(self, eng):
         S, tri = api.CreateSpectra(self.H, self.T, self.psi, self.options, eng=eng, batched=self.batched)
