@@ -5,6 +5,7 @@
 #   quanty  the reference binary (LuaInterface/main.cpp): golden fixtures, oracle pins
 #   hpsi    oracle/ref_hpsi.cpp around the reference's translation unit: the reference's own
 #           fixed-basis H*psi timed on a given basis (the CPU arm of bench.py) and its output
+#   headers only the generated headers (BLAS name map, seed pin) other builds reuse
 #
 # Recipe: the reference is one translation unit (LuaInterface/main.cpp includes every .cpp).
 # It needs an LP64 BLAS/LAPACK; the one present on these machines is scipy's bundled OpenBLAS,
@@ -31,18 +32,19 @@ print(c[0] if c else "")
 PY
 )
 [ -n "$OB" ] || { echo "no LP64 scipy OpenBLAS found" >&2; exit 1; }
-nm -D --defined-only "$OB" | awk '$3 ~ /^scipy_/ { n = substr($3, 7); print "#define " n " " $3 }' > "$OUT/blas_names.h"
-cat > "$OUT/pin_seed.h" <<'H'
-#include <stdlib.h>
-#define srand(x) srand(12345u)
-H
-ln -sf "$OB" "$OUT/libscipyob.so"
+# written to temporary names and moved into place, so builds running side by side read whole files
+nm -D --defined-only "$OB" | awk '$3 ~ /^scipy_/ { n = substr($3, 7); print "#define " n " " $3 }' > "$OUT/blas_names.h.$$"
+mv -f "$OUT/blas_names.h.$$" "$OUT/blas_names.h"
+printf '#include <stdlib.h>\n#define srand(x) srand(12345u)\n' > "$OUT/pin_seed.h.$$"
+mv -f "$OUT/pin_seed.h.$$" "$OUT/pin_seed.h"
+ln -sfn "$OB" "$OUT/libscipyob.so.$$" && mv -fT "$OUT/libscipyob.so.$$" "$OUT/libscipyob.so"
 FLAGS=(-include "$OUT/blas_names.h" -include "$OUT/pin_seed.h" -D LUA_USE_LINUX -DBLASunderscore -O2 -fopenmp -w
        -L"$OUT" -lscipyob -Wl,-rpath,"$(dirname "$OB")")
 for t in $TARGETS; do
   case $t in
     quanty) g++ "$REF/LuaInterface/main.cpp" "${FLAGS[@]}" -o "$OUT/Quanty" & ;;
     hpsi) g++ "$HERE/ref_hpsi.cpp" -I"$REF" "${FLAGS[@]}" -o "$OUT/ref_hpsi" & ;;
+    headers) ;;  # only the BLAS name map and the seed pin (for builds made elsewhere)
     *) echo "unknown target $t" >&2; exit 2 ;;
   esac
 done

@@ -28,7 +28,11 @@ sys.path.insert(0, ROOT)
 from quanty_gb300.quanty_text import parse_operator, parse_wavefunction  # noqa: E402
 
 REF = os.environ.get("QUANTY_REFERENCE", "/root/reference")
-QUANTY = os.path.join(ROOT, "oracle", "_ref", "Quanty")
+# the binary the generators run under (another build of Quanty may be named, e.g. the one whose
+# H*psi path runs through libqgpu, to compare its outputs with the fixtures)
+QUANTY = os.environ.get("QUANTY_BINARY", os.path.join(ROOT, "oracle", "_ref", "Quanty"))
+# when a dict, generated fixtures are stored here by name instead of written to tests/golden
+SINK = None
 
 
 def run(script_text, name):
@@ -104,6 +108,9 @@ def spectra(work, f):
 
 
 def save(name, obj):
+    if SINK is not None:
+        SINK[name] = obj
+        return
     path = os.path.join(HERE, name)
     with open(path, "w") as f:
         json.dump(obj, f, separators=(",", ":"))
