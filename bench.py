@@ -161,15 +161,22 @@ PARITY_STRIDE = 32
 
 
 def cpu_baseline(api, H, basis, seconds, eng):
-    """The reference's push-form H*psi (oracle restatement, OpenMP, all host threads) on a
-    spread sample of source rows of the full basis, sized for about `seconds` of work.
+    """The CPU side of the default bench line, on the GPU machine's host cores.
 
-    The same oracle handle then checks the timed GPU path at this configuration: x zero except
-    on every PARITY_STRIDE-th row, the device apply (the benchmark's call) against the oracle's
-    push from those rows, all rows compared (amplitudes to 1e-12 relative, the set of rows
-    reached exactly), and the connection count of those rows.  Returns (baseline, parity)."""
+    Timing: the reference's own fixed-basis H*psi (oracle/_ref/ref_hpsi, when it has been built
+    from the staged reference sources) on a spread sample of source rows with the whole basis as
+    the lookup target, on all host threads and on one; beside it, as a calibration, the
+    oracle's restatement of the same loop (OpenMP, all host threads) on a sample sized for about
+    `seconds`.  Without the reference program the oracle's figure is the baseline ("port").
+
+    Parity of the timed GPU call at this configuration: x zero except on every
+    PARITY_STRIDE-th row, the device apply against the oracle's push from those rows and, with
+    the reference program, against the reference's own result; all rows compared (amplitudes
+    to 1e-12 relative, the set of rows reached exactly), and the connection count of the
+    sampled rows.  Returns (baseline, parity)."""
     import torch
     from oracle import oracle as O
+    from oracle import ref_hpsi
     O.build()
     dets = basis.dets_bytes()
     n = len(dets)
@@ -179,7 +186,7 @@ def cpu_baseline(api, H, basis, seconds, eng):
     h = O.WF(H.nf, dets, x).handle()
     try:
         rows, stride, dt = timed_sample(O, op, h, n, seconds)
-        base = {"value": rows * op.nterms / dt / 1e9, "unit": "Gdet·terms/s", "cores": O.num_threads(),
+        port = {"value": rows * op.nterms / dt / 1e9, "unit": "Gdet·terms/s", "cores": O.num_threads(),
                 "kind": "port",
                 "sample": "every %d-th of %d source determinants (%d rows), full basis as lookup target, %d terms, "
                           "%.1f s" % (stride, n, rows, op.nterms, dt)}
@@ -197,11 +204,35 @@ def cpu_baseline(api, H, basis, seconds, eng):
     finally:
         O.lib().qo_wf_free(h)
     max_rel = float(np.max(np.abs(y - want)) / np.max(np.abs(want)))
+    reached = bool(np.array_equal(y != 0, want != 0))
     parity = {"rows": int((n + PARITY_STRIDE - 1) // PARITY_STRIDE), "stride": PARITY_STRIDE, "outputs_compared": n,
-              "max_rel": max_rel, "tolerance": 1e-12, "rows_reached_equal": bool(np.array_equal(y != 0, want != 0)),
+              "max_rel": max_rel, "tolerance": 1e-12, "rows_reached_equal": reached,
               "nnz_sample": int(cnt.value), "nnz_sample_oracle": int(cnt_o),
-              "ok": bool(max_rel < 1e-12 and np.array_equal(y != 0, want != 0) and cnt.value == cnt_o),
+              "ok": bool(max_rel < 1e-12 and reached and cnt.value == cnt_o),
               "checker": "oracle push-form H*psi from the sampled source rows (OpenMP C restatement)"}
+    del want
+    base = dict(port)
+    if ref_hpsi.available():
+        threads = os.cpu_count() or 1
+        res, yref, why = reference_runs(H, dets, x, [(threads, "s%d" % PARITY_STRIDE, 1), (threads, "t%g" % seconds, 2),
+                                                     (1, "t%g" % min(seconds, 10.0), 1)], want_y=True)
+        if res:
+            r1, r2 = res[1], res[2]
+            base = {"value": r1["pairs"] / min(r1["calls"]) / 1e9, "unit": "Gdet·terms/s", "cores": threads,
+                    "kind": "reference",
+                    "sample": "reference OperatorPsiConserveBasisPreAllocated from every %d-th of %d source "
+                              "determinants (%d rows, %d terms) into the whole basis" % (r1["stride"], n, r1["sources"],
+                                                                                         op.nterms),
+                    "one_thread_value": r2["pairs"] / r2["calls"][0] / 1e9, "port": port}
+            base["port_over_reference"] = port["value"] / base["value"]
+            rel = float(np.max(np.abs(y - yref)) / np.max(np.abs(yref)))
+            same = bool(np.array_equal(y != 0, yref != 0))
+            parity["reference"] = {"max_rel": rel, "rows_reached_equal": same, "ok": bool(rel < 1e-12 and same),
+                                   "checker": "the reference's own OperatorPsiConserveBasisPreAllocated (unmodified "
+                                              "sources) from the same sampled rows"}
+            parity["ok"] = parity["ok"] and parity["reference"]["ok"]
+        else:
+            base["reference_unavailable"] = why
     return base, parity
 
 
@@ -229,12 +260,50 @@ def xas_spectra_rate(api):
             "batched": out["batched"], "plain": out["plain"], "speedup": out["batched"] / out["plain"]}
 
 
+def reference_program():
+    """The reference's own fixed-basis H*psi program (oracle/_ref/ref_hpsi), built from the
+    reference sources staged in baseline/_ref when it is missing.  Returns (module, None) or
+    (None, why it is unavailable)."""
+    from oracle import ref_hpsi
+    if ref_hpsi.available():
+        return ref_hpsi, None
+    src = os.path.join(ROOT, "baseline", "_ref")
+    if not os.path.isfile(os.path.join(src, "LuaInterface", "main.cpp")):
+        return None, "reference sources not staged in baseline/_ref"
+    r = subprocess.run([os.path.join(ROOT, "oracle", "build_ref.sh"), src, "hpsi"], capture_output=True, text=True)
+    if r.returncode != 0 or not ref_hpsi.available():
+        return None, "reference build failed: " + (r.stderr or r.stdout)[-300:].replace("\n", " ")
+    return ref_hpsi, None
+
+
+def reference_runs(H, dets, x, runs, want_y=False):
+    """The reference's OperatorPsiConserveBasisPreAllocated with the whole basis as the lookup
+    target and sources every stride-th row, for each (threads, spec, calls) of `runs` (spec
+    "t<seconds>": a stride for about that many seconds per call; "s<stride>").  Returns
+    (harness runs, y or None, None) or (None, None, why it is unavailable)."""
+    ref, why = reference_program()
+    if ref is None:
+        return None, None, why
+    import tempfile
+    fd, path = tempfile.mkstemp(prefix="ref_hpsi_in_")
+    os.close(fd)
+    try:
+        ref.write_input(path, H.nf, H.terms, dets, x)
+        res, y = ref.run(path, runs, want_y=want_y)
+        return res, y, None
+    except Exception as e:  # reported by the caller
+        return None, None, str(e)[-300:]
+    finally:
+        os.unlink(path)
+
+
 def run_reference(args):
+    """The reference arm: the reference's own fixed-basis H*psi (its unmodified sources, built
+    here) on the host cores, on the same basis and operator, each step a spread sample of
+    source rows.  Falls back to the oracle's restatement when the reference cannot be built."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
-    from oracle import oracle as O
-    O.build()
     from quanty_gb300 import workloads
     # the basis comes from the same closure rules, enumerated on the host without a GPU
     H, R, seed, info = workloads.anderson_impurity(nshell=args.shells, hole_max=args.hole_max,
@@ -243,31 +312,51 @@ def run_reference(args):
     n = len(dets)
     rng = np.random.default_rng(0)
     x = rng.normal(size=n) + 1j * rng.normal(size=n)
-    op = O.Op({"nf": H.nf, "terms": [[list(t[0]), t[1].real, t[1].imag] for t in H.terms]})
-    wf = O.WF(H.nf, dets, x)
-    h = wf.handle()
-    L = O.lib()
-    y = np.zeros(2 * n)
-    per_step = max(10.0, 60.0 / max(args.steps + args.warmup, 1))
-    rows, stride, _ = timed_sample(O, op, h, n, per_step)
-    for _ in range(args.warmup):
-        L.qo_apply_conserve_strided(*op.args(), h, 0, n, max(stride, n // 1000), O._p(y))
-    times = []
-    for _ in range(args.steps):
-        t0 = time.perf_counter()
-        L.qo_apply_conserve_strided(*op.args(), h, 0, n, stride, O._p(y))
-        times.append(time.perf_counter() - t0)
-    L.qo_wf_free(h)
-    S2 = rows
-    t = sum(times) / len(times)
-    val = S2 * op.nterms / t / 1e9
+    threads = os.cpu_count() or 1
+    per_step = max(2.0, min(10.0, 40.0 / max(args.steps + args.warmup, 1)))
+    runs, _, why = reference_runs(H, dets, x, [(threads, "t%g" % per_step, args.steps + args.warmup),
+                                              (1, "t%g" % per_step, 1)])
+    workload = "anderson_impurity_%dso_hpsi" % H.nf
+    if runs:
+        r0 = runs[0]
+        times = r0["calls"][args.warmup:] or r0["calls"]
+        t = sum(times) / len(times)
+        val = r0["pairs"] / t / 1e9
+        base = {"value": val, "unit": "Gdet·terms/s", "cores": threads, "kind": "reference",
+                "sample": "reference OperatorPsiConserveBasisPreAllocated from every %d-th of %d source determinants "
+                          "(%d rows, %d terms) into the whole basis, per step" % (r0["stride"], n, r0["sources"],
+                                                                                 len(H.terms)),
+                "basis_build_s": r0["basis_s"]}
+        if len(runs) > 1:
+            r1 = runs[1]
+            base["one_thread_value"] = r1["pairs"] / r1["calls"][0] / 1e9
+    else:
+        # the oracle's restatement of the same loop, when the reference cannot be built here
+        from oracle import oracle as O
+        O.build()
+        op = O.Op({"nf": H.nf, "terms": [[list(t_[0]), t_[1].real, t_[1].imag] for t_ in H.terms]})
+        h = O.WF(H.nf, dets, x).handle()
+        L = O.lib()
+        y = np.zeros(2 * n)
+        rows, stride, _ = timed_sample(O, op, h, n, per_step)
+        for _ in range(args.warmup):
+            L.qo_apply_conserve_strided(*op.args(), h, 0, n, max(stride, n // 1000), O._p(y))
+        times = []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            L.qo_apply_conserve_strided(*op.args(), h, 0, n, stride, O._p(y))
+            times.append(time.perf_counter() - t0)
+        L.qo_wf_free(h)
+        t = sum(times) / len(times)
+        val = rows * op.nterms / t / 1e9
+        base = {"value": val, "unit": "Gdet·terms/s", "cores": O.num_threads(), "kind": "port",
+                "sample": "every %d-th of %d source determinants (%d rows) per step" % (stride, n, rows),
+                "reference_unavailable": why}
     line = {"impl": "reference", "metric": "H·ψ det·terms/s", "value": val, "unit": "Gdet·terms/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
-            "data": "synthetic", "config": {"workload": "anderson_impurity_%dso_hpsi" % H.nf, "n_det": n,
-                                           "n_terms": op.nterms},
-            "cpu_baseline": {"value": val, "unit": "Gdet·terms/s", "cores": O.num_threads(), "kind": "port",
-                             "sample": "every %d-th of %d source determinants (%d rows) per step" % (stride, n, S2)},
+            "data": "synthetic", "config": {"workload": workload, "n_det": n, "n_terms": len(H.terms)},
+            "cpu_baseline": base,
             "e2e": {"value": val, "unit": "Gdet·terms/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
