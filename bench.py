@@ -116,6 +116,21 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
+def probe_fp64_peak(eng):
+    """The device's FP64 issue ceiling in G lane-operations/s (bench_probe.cu, built beside this
+    file by __graft_entry__.build(); independent FMA chains on every lane of 8 blocks per SM)."""
+    lib = os.path.join(ROOT, "bench_probe.so")
+    if not os.path.exists(lib):
+        import __graft_entry__
+        __graft_entry__.build()
+    L = C.CDLL(lib)
+    L.bench_fp64_peak.argtypes = [C.c_void_p, C.c_void_p]
+    out = C.c_double(0.0)
+    if L.bench_fp64_peak(eng.L.qg_get_stream(eng.ctx), C.byref(out)) != 0:
+        raise RuntimeError("bench_fp64_peak failed")
+    return out.value
+
+
 def profiled_traffic(workload):
     """DRAM bytes (read + write) per launch of the H*psi kernel on this workload, from one ncu
     capture recorded in profiles/traffic.json (None when none was recorded)."""
@@ -367,7 +382,7 @@ def main():
     if args.impl == "reference":
         return run_reference(args)
     if args.mode != "hpsi":
-        from quanty_gb300 import bench_forms
+        import bench_forms
         return bench_forms.main(args)
     import torch
     from quanty_gb300 import replicas
@@ -471,9 +486,7 @@ def main():
     sms = torch.cuda.get_device_properties(local).multi_processor_count
     mhz = clk.get("sm_mhz") or clk.get("sm_max_mhz") or 2070.0
     fp64_nominal = 2.0 * sms * mhz * 1e6 / 1e9  # G FP64 lane-operations per second
-    meas = C.c_double(0.0)
-    eng.check(eng.L.qg_fp64_peak(eng.ctx, C.byref(meas)))
-    fp64_peak = meas.value
+    fp64_peak = probe_fp64_peak(eng)
     fp64_achieved = ops.value / (ms * 1e-3) / 1e9
     hbm_floor_ms = alg_bytes / (peak * 1e9) * 1e3
     fp64_floor_ms = ops.value / (fp64_peak * 1e9) * 1e3
@@ -503,7 +516,7 @@ def main():
                      "algorithmic_bytes_per_launch": alg_bytes,
                      "fp64": {"ops_per_launch": ops.value, "achieved_gops": fp64_achieved,
                               "peak_gops": fp64_peak, "frac": fp64_achieved / fp64_peak,
-                              "peak_source": "measured (independent FMA chains on every lane, qg_fp64_peak)",
+                              "peak_source": "measured (independent FMA chains on every lane, bench_probe.cu)",
                               "nominal_gops": fp64_nominal, "frac_of_nominal": fp64_achieved / fp64_nominal,
                               "nominal_source": "2 FP64 lanes per SM per clock x %d SMs x %.0f MHz sampled" % (sms, mhz)},
                      "floors_ms": {"hbm": hbm_floor_ms, "fp64": fp64_floor_ms,

@@ -42,7 +42,7 @@ def _log(msg):
 
 
 def batched(args):
-    from . import api, workloads
+    from quanty_gb300 import api, workloads
     eng = api.engine()
     nshell, hm, pm = 6, 1, 2
     H, R, seed, info = workloads.anderson_impurity(nshell=nshell, hole_max=hm, particle_max=pm)
@@ -223,7 +223,7 @@ def _lanczos_seconds(api, H, bf, Y, ntri, eps, eng, reps=1):
 
 def make_stream(njobs, seed=0, max_det=2e6, min_det=1e3, eigen_frac=0.25):
     """Seeded mixed jobs: (kind, params) with target sizes log-uniform in [min_det, max_det]."""
-    from . import workloads
+    from quanty_gb300 import workloads
     rng = np.random.default_rng(seed)
     out = []
     for j in range(njobs):
@@ -265,7 +265,7 @@ def build_job(api, serve, workloads, p):
 
 
 def served(args):
-    from . import api, serve, workloads
+    from quanty_gb300 import api, serve, workloads
     params = make_stream(int(args.jobs), seed=0, max_det=float(args.max_det))
     jobs = [build_job(api, serve, workloads, p) for p in params]
     nspec = sum(j.nspec for j in jobs)
@@ -315,7 +315,7 @@ def layouts(args):
     impurity with `--shells` bath shells (at most 1 hole, 2 particles); every vector layout
     timed with CUDA events, or (with --layout) only that one, twice (a profiling target)."""
     import ctypes
-    from . import api, workloads
+    from quanty_gb300 import api, workloads
     eng = api.engine()
     torch = eng.torch
     nshell = int(args.shells)

@@ -164,16 +164,6 @@ qg_status qg_poles_spectra(qg_context ctx, int32_t nspec, int32_t npole, const d
                            const double *b_host, const double *e0_host, double emin, double de,
                            int32_t ne, double gamma, double *g_host);
 
-/* Random-sector gather bandwidth of the device in GB/s (no counterpart in the reference):
- * reads of 32-byte sectors at unrelated addresses spread over a buffer of `bytes` (>= 1 MiB,
- * allocated and freed here).  The ceiling for hash-probed gathers, measured for the roofline. */
-qg_status qg_gather_bandwidth(qg_context ctx, int64_t bytes, double *gbs);
-
-/* FP64 issue ceiling of the device in G lane-operations per second (no counterpart in the
- * reference): independent FMA chains in registers on every lane of num_sms * 8 blocks, timed
- * with events.  The measured denominator of the H*psi FP64 roofline. */
-qg_status qg_fp64_peak(qg_context ctx, double *gops);
-
 /* Eigenpairs of a dense Hermitian matrix, computed on the device (cyclic Jacobi with the
  * round-robin ordering: every step rotates k/2 disjoint index pairs at once): a_host is k x k
  * row-major with interleaved (re, im); w_host receives all k eigenvalues ascending, v_host

@@ -62,8 +62,6 @@ def load(path=LIB_PATH):
         "qg_count_nnz_rows": (C.c_int, [P, P, P, I64, I64, I32, P]),
         "qg_set_autotune": (C.c_int, [P, I32]),
         "qg_hermitian_eigh": (C.c_int, [P, I32, P, P, P, I32]),
-        "qg_gather_bandwidth": (C.c_int, [P, I64, P]),
-        "qg_fp64_peak": (C.c_int, [P, P]),
         "qg_operator_dense": (C.c_int, [P, P, P, P]),
         "qg_poles_spectra": (C.c_int, [P, I32, I32, P, P, P, D, D, I32, D, P]),
         "qg_apply_chunk": (C.c_int, [P, P, P, I32, P]),

@@ -414,8 +414,3 @@ def test_fp64_operation_count(api, complex_values):
     eng.check(eng.L.qg_apply_fp64_ops(eng.ctx, H.handle(), b.h, ctypes.byref(ops)))
     nnz_off = api.count_nnz(H, b, offdiag=True)
     assert ops.value == 2 * b.n + (4 if complex_values else 2) * nnz_off
-    peak = ctypes.c_double()
-    eng.check(eng.L.qg_fp64_peak(eng.ctx, ctypes.byref(peak)))
-    import torch
-    nominal = 2 * torch.cuda.get_device_properties(0).multi_processor_count * 2.07  # G lane-ops/s at 2.07 GHz
-    assert 0.3 * nominal < peak.value < 1.1 * nominal

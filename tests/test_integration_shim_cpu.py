@@ -1,45 +1,47 @@
-"""The C++ shim the integration guide gives a Quanty maintainer (its first C++ block) compiles
-against the reference's own types: the block is extracted and syntax-checked together with the
-reference's single translation unit (LuaInterface/main.cpp, which includes every source file),
-and each qg_* function it calls is declared in include/qgpu.h and exported by libqgpu.so.
-Skipped where the reference sources or g++ are absent (the reference never travels with this
-repository)."""
+"""The Quanty shim (integration/qgpu_shim.cpp) compiles against the reference's own types: it is
+syntax-checked together with the reference's single translation unit (LuaInterface/main.cpp,
+which includes every source file), and every qg_* function it calls is declared in
+include/qgpu.h.  The reference tree is located through QUANTY_REFERENCE, else the copy staged in
+baseline/_ref by oracle/stage_ref.sh; the compile check is skipped where neither exists (the
+reference never travels with this repository) or g++ is absent.  The patch script is checked
+to find every dispatcher it hooks."""
 import os
 import re
 import shutil
 import subprocess
+import sys
 
 import pytest
 
 from conftest import ROOT
 
-REF = os.environ.get("QUANTY_REFERENCE", "/root/reference")
+SHIM = os.path.join(ROOT, "integration", "qgpu_shim.cpp")
 
 
-def _shim():
-    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
-    return re.findall(r"```cpp\n(.*?)```", text, re.S)[0]
+def _reference():
+    for d in (os.environ.get("QUANTY_REFERENCE"), os.path.join(ROOT, "baseline", "_ref")):
+        if d and os.path.isfile(os.path.join(d, "LuaInterface", "main.cpp")):
+            return d
+    return None
 
 
 def test_shim_calls_only_exported_entry_points():
     from quanty_gb300 import qgpu
-    called = set(re.findall(r"\b(qg_[a-z_0-9]+)\s*\(", _shim()))
+    called = set(re.findall(r"\b(qg_[a-z_0-9]+)\s*\(", open(SHIM).read()))
     assert called, "no qg_ call found in the shim"
     declared = set(qgpu.header_symbols())
     assert called <= declared, called - declared
 
 
-@pytest.mark.skipif(not os.path.isfile(os.path.join(REF, "LuaInterface", "main.cpp")) or not shutil.which("g++"),
-                    reason="reference sources or g++ not available")
+@pytest.mark.skipif(_reference() is None or not shutil.which("g++"), reason="reference sources or g++ not available")
 def test_shim_compiles_against_the_reference(tmp_path):
-    (tmp_path / "shim_body.inc").write_text(_shim())
+    ref = _reference()
     (tmp_path / "shim_check.cpp").write_text(
         "#define main quanty_reference_main\n"
         '#include "%s"\n'
         "#undef main\n"
         "#define QUANTY_GB300\n"
-        "#include <vector>\n"
-        '#include "shim_body.inc"\n' % os.path.join(REF, "LuaInterface", "main.cpp"))
+        '#include "%s"\n' % (os.path.join(ref, "LuaInterface", "main.cpp"), SHIM))
     cuda_inc = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "include")
     if not os.path.isfile(os.path.join(cuda_inc, "cuda_runtime.h")):
         pytest.skip("CUDA headers not found")
@@ -48,3 +50,16 @@ def test_shim_compiles_against_the_reference(tmp_path):
                         str(tmp_path / "shim_check.cpp")],
                        capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stderr[-3000:]
+
+
+@pytest.mark.skipif(_reference() is None, reason="reference sources not available")
+def test_patch_finds_every_dispatcher(tmp_path):
+    sys.path.insert(0, os.path.join(ROOT, "integration"))
+    import build_quanty_gb300 as b
+    b.patch(_reference(), str(tmp_path / "src"))
+    text = open(tmp_path / "src" / "Core" / "Core.cpp").read()
+    assert text.startswith('#ifdef QUANTY_GB300\n#include "QGpu.cpp"')
+    hooked = open(tmp_path / "src" / "Core" / "OperatorWaveFunction.cpp").read() + \
+        open(tmp_path / "src" / "Core" / "Lanczos.cpp").read()
+    for _, _, call in b.HOOKS:
+        assert call in hooked, call
