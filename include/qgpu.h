@@ -296,6 +296,27 @@ qg_status qg_block_groundstate(qg_context ctx, qg_operator op, qg_basis basis, i
 qg_status qg_lanczos_krylov(qg_context ctx, qg_operator op, qg_basis basis, const double *v0_dev, int32_t ntri,
                             double eps, double *a_host, double *b_host, double *krylov_dev);
 
+/* Block Lanczos tridiagonalisation of op from m start vectors (v0_dev, n x m row-major on one
+ * basis), NTri blocks (LanczosBlockTriDiagonalize{RR,RC,CC}, Core/BlockLanczos.cpp:1647-2660, as
+ * CreateSpectra with Tensor = true calls it, LuaInterface/ssp.cpp:2753-2800): Loewdin
+ * orthonormalisation with the reference's deflation (a direction whose singular value is not
+ * above max(singular_value, 3 sqrt(DBL_EPSILON) s_max) is dropped), two projections against
+ * each of the last two blocks, entries below eps zeroed.  a_host receives (ntri + 1) blocks
+ * and b_host ntri blocks of m x m complex values (interleaved, row-major, zero beyond a
+ * deflated block's size; a_0 = 0, b_0(i, j) = <q_j|v0_i>, A_k = Q_k^H H Q_k,
+ * B_k = Q_k^H H Q_{k+1}); sizes_host (ntri + 1) the block sizes (sizes[0] = m). */
+qg_status qg_block_lanczos(qg_context ctx, qg_operator op, qg_basis basis, const double *v0_dev, int32_t m,
+                           int32_t ntri, double eps, double singular_value, double *a_host, double *b_host,
+                           int32_t *sizes_host);
+
+/* The m x m matrix of spectra of a block tridiagonal matrix by the block continued fraction
+ * (BlockTriDiagonalMatrixToSpectraWithBroadening, Core/BasicMathBlock/BasicMath_BlockTypeConversion.cpp:1636):
+ * G_ij(w) = <v0_i| (w - H + i gamma/2)^-1 |v0_j> at w = emin + k*de + e0, k = 0..ne, one thread
+ * per frequency; a_host, b_host as qg_block_lanczos returns them; m <= 8; g_host receives
+ * m*m spectra of ne+1 complex points, spectrum i*m + j. */
+qg_status qg_block_cf_spectra(qg_context ctx, int32_t m, int32_t ntri, const double *a_host, const double *b_host,
+                              double e0, double emin, double de, int32_t ne, double gamma, double *g_host);
+
 /* Settings of a resonant spectrum (ConvergenceSettingsType fields NTri1, NTri2, epsilon,
  * Emin1..Gamma2, restrictions1/2, Core/StructDef.cpp:252; energies E0_1/E0_2).  Emin/Emax set
  * to +-DBL_MAX and Gamma to 0 are resolved as the reference does and written back; NE1 and NE2

@@ -27,6 +27,7 @@ DEFAULTS = {
     "DenseBorder": 1513, "NKrylovStart": 100, "NKrylovMax": 500, "NKrylovStep": 10, "NTri": 200,
     "NTri1": 100, "NTri2": 100, "Zero": 100 * math.sqrt(DBL_EPSILON), "Epsilon": math.sqrt(DBL_EPSILON) / 100,
     "Emin": None, "Emax": None, "NE": 1000, "Gamma": 0.0, "NBitsKey": 16,
+    "SingularValue": math.sqrt(DBL_EPSILON),
 }
 
 _engine = None
@@ -781,17 +782,58 @@ def _spectra_dense(H, Tpsi, e0, o, basis, eng, states=False):
     return Spectra(G, emin, emax, NE, gamma, lo, hi), poles
 
 
+def block_lanczos(H, basis, X, ntri, eps, singular_value, eng=None):
+    """Block Lanczos on a device basis (LanczosBlockTriDiagonalize, Core/BlockLanczos.cpp:2131):
+    X is an (n, m) complex CUDA tensor of start vectors.  Returns A ((ntri+1), m, m), B (ntri, m,
+    m) complex and the block sizes (ntri + 1)."""
+    eng = eng or engine()
+    m = X.shape[1]
+    a = np.zeros((ntri + 1, m, m), dtype=np.complex128)
+    b = np.zeros((ntri, m, m), dtype=np.complex128)
+    sizes = np.zeros(ntri + 1, dtype=np.int32)
+    Xc = X.contiguous()
+    eng.check(eng.L.qg_block_lanczos(eng.ctx, H.handle(eng), basis.h, _ptr(Xc), m, ntri, float(eps),
+                                     float(singular_value), _ptr(a), _ptr(b), _ptr(sizes)))
+    return a, b, sizes
+
+
+def block_tridiagonal_dense(A, B):
+    """The Hermitian (N m) x (N m) matrix of the blocks A_1..A_N on the diagonal and B_1..B_{N-1}
+    beside it, zero rows and columns for deflated directions included, as the reference's
+    BlockTriDiagonalMatrixEigenValues sees it (Core/BasicMathBlock/BasicMath_BlockTypeConversion.cpp:1731)."""
+    N, m = A.shape[0] - 1, A.shape[1]
+    T = np.zeros((N * m, N * m), dtype=np.complex128)
+    for k in range(1, N + 1):
+        T[(k - 1) * m:k * m, (k - 1) * m:k * m] = A[k]
+        if k < N:
+            T[(k - 1) * m:k * m, k * m:(k + 1) * m] = B[k]
+            T[k * m:(k + 1) * m, (k - 1) * m:k * m] = B[k].conj().T
+    return (T + T.conj().T) / 2
+
+
+def BlockTriDiagonalMatrixToSpectra(E0, A, B, Emin, Emax, NE, Gamma, eng=None):
+    """G_ij(w) = <v0_i| (w - H + i Gamma/2)^-1 |v0_j> at w = Emin + k dE + E0 from a block
+    tridiagonal matrix by the block continued fraction (BlockTriDiagonalMatrixToSpectraWithBroadening,
+    Core/BasicMathBlock/BasicMath_BlockTypeConversion.cpp:1636): (m*m, NE+1), spectrum i*m + j."""
+    eng = eng or engine()
+    m, ntri = A.shape[1], B.shape[0]
+    a = np.ascontiguousarray(A, dtype=np.complex128)
+    b = np.ascontiguousarray(B, dtype=np.complex128)
+    g = np.zeros((m * m, NE + 1), dtype=np.complex128)
+    eng.check(eng.L.qg_block_cf_spectra(eng.ctx, m, ntri, _ptr(a), _ptr(b), float(E0), float(Emin),
+                                        (Emax - Emin) / NE, int(NE), float(Gamma), _ptr(g)))
+    return g
+
+
 def _spectra_tensor(H, Tpsi, E0, o, R, method, eng):
     """CreateSpectra with Tensor = true (ssp.cpp:2480-2530, :2753-2800): the m x m matrix
     G_ij(w) = <T_i psi| (w + E0 - H + i Gamma/2)^-1 |T_j psi>, spectrum i*m + j, one energy
     shift E0 (the first state's).  Dense branch: poles of H on the union basis with weights
     conj(c_ki) c_kj, c_ki = <E_k|T_i psi> (BasicMath_CompactMatrixVector.cpp:4064,
-    BasicMath_BlockTypeConversion.cpp:588).  Lanczos branch: the m diagonal elements and, per
-    pair, the spectra of T_i psi + T_j psi and T_i psi + i T_j psi, all m^2 chains as one
-    batched Lanczos; the off-diagonal elements follow by polarisation,
-    G_ij = (S - i T) / 2 and G_ji = (S + i T) / 2 with S = G(u_i + u_j) - G_ii - G_jj and
-    T = G(u_i + i u_j) - G_ii - G_jj.  At a converged chain length this is the reference's
-    block-Lanczos result."""
+    BasicMath_BlockTypeConversion.cpp:588).  Lanczos branch: the reference's block Lanczos on the
+    device from the m vectors T_i psi on their common basis (qg_block_lanczos, NTri blocks), the
+    pole range from the eigenvalues of the whole block tridiagonal matrix, and the spectra by the
+    block continued fraction (qg_block_cf_spectra)."""
     m = len(Tpsi)
     NE, gamma, ntri, eps = int(o["NE"]), float(o["Gamma"]), int(o["NTri"]), float(o["Epsilon"])
     seed = np.concatenate([t.det for t in Tpsi if t.N] or [np.zeros((0, nword(H.nf)), np.uint8)])
@@ -813,31 +855,15 @@ def _spectra_tensor(H, Tpsi, E0, o, R, method, eng):
         G = (ListOfPolesToSpectrum(0.0, poles, Wt.real.copy(), emin, emax, NE, gamma, eng)
              + 1j * ListOfPolesToSpectrum(0.0, poles, Wt.imag.copy(), emin, emax, NE, gamma, eng))
         return Spectra(G, emin, emax, NE, gamma, lo, hi), {"poles": poles, "weights": Wt}
-    pairs = [(i, j) for i in range(m) for j in range(i + 1, m)]
-    Z = np.zeros((n, m + 2 * len(pairs)), dtype=np.complex128)
-    Z[:, :m] = X
-    for p, (i, j) in enumerate(pairs):
-        Z[:, m + 2 * p] = X[:, i] + X[:, j]
-        Z[:, m + 2 * p + 1] = X[:, i] + 1j * X[:, j]
     with eng.on_stream():
-        z = eng.torch.from_numpy(Z).to("cuda:%d" % eng.device).contiguous()
-    A, B = lanczos_block(H, ub, z, ntri, eps, max(gamma, eps), eng)
-    lo, hi = np.inf, -np.inf
-    for c in range(m):
-        k = next((q for q in range(1, ntri) if B[c, q] == 0.0), ntri)
-        w0, w1 = _tri_extremes(A[c, 1:k + 1], B[c, 1:k])
-        lo, hi = min(lo, w0 - E0), max(hi, w1 - E0)
+        x = eng.torch.from_numpy(X).to("cuda:%d" % eng.device).contiguous()
+    sv = float(o.get("SingularValue", DEFAULTS["SingularValue"]))
+    A, B, sizes = block_lanczos(H, ub, x, ntri, eps, sv, eng)
+    val, _ = hermitian_eigh(block_tridiagonal_dense(A, B), 0, eng)
+    lo, hi = val[0] - E0, val[-1] - E0
     emin, emax, gamma = _default_window(lo, hi, o["Emin"], o["Emax"], gamma, NE)
-    D = TriDiagonalMatrixToSpectrum(np.full(Z.shape[1], E0), A, B, emin, emax, NE, gamma, eng)
-    G = np.zeros((m * m, NE + 1), dtype=np.complex128)
-    for i in range(m):
-        G[i * m + i] = D[i]
-    for p, (i, j) in enumerate(pairs):
-        S_ = D[m + 2 * p] - D[i] - D[j]
-        T_ = D[m + 2 * p + 1] - D[i] - D[j]
-        G[i * m + j] = 0.5 * (S_ - 1j * T_)
-        G[j * m + i] = 0.5 * (S_ + 1j * T_)
-    return Spectra(G, emin, emax, NE, gamma, lo, hi), {"a": A, "b": B}
+    G = BlockTriDiagonalMatrixToSpectra(E0, A, B, emin, emax, NE, gamma, eng)
+    return Spectra(G, emin, emax, NE, gamma, lo, hi), {"a": A, "b": B, "block_sizes": sizes}
 
 
 def CreateSpectraResident(H, T, basis, X, E0, options=None, eng=None, batched=True, max_vectors=None):

@@ -27,4 +27,10 @@ S = CreateSpectra(HX, {Tx, Ty, Tz}, psi1, {{"Tensor", true}, {"Method", "Dense"}
 S.Print({{"file", "dump/tensor_dense_defaults.dat"}})
 S = CreateSpectra(HX, {Tx, Ty, Tz}, psi1, {{"Tensor", true}, {"Method", "Lanczos"}, {"NE", 40}, {"Emin", -5}, {"Emax", 15}, {"Gamma", 0.6}, {"Epsilon", 0}})
 S.Print({{"file", "dump/tensor_lanczos.dat"}})
+-- block Lanczos with an incomplete Krylov space (15 and 24 Krylov vectors on the final-state
+-- basis): the result depends on the block recursion itself, not only on H
+S = CreateSpectra(HX, {Tx, Ty, Tz}, psi1, {{"Tensor", true}, {"Method", "Lanczos"}, {"NTri", 5}, {"NE", 40}, {"Emin", -5}, {"Emax", 15}, {"Gamma", 0.6}, {"Epsilon", 0}})
+S.Print({{"file", "dump/tensor_lanczos_short.dat"}})
+S = CreateSpectra(HX, {Tx, Ty, Tz}, psi1, {{"Tensor", true}, {"Method", "Lanczos"}, {"NTri", 8}, {"NE", 32}})
+S.Print({{"file", "dump/tensor_lanczos_short_auto.dat"}})
 print("tensor done")

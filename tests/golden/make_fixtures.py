@@ -282,7 +282,7 @@ def gen_tensor():
     out = {"source": "tests/golden/gen/tensor.lua", "psi": wf(work, "psi1")}
     for n in ("HX", "Tx", "Ty", "Tz"):
         out[n] = op(work, n)
-    for k in ("dense", "dense_defaults", "lanczos"):
+    for k in ("dense", "dense_defaults", "lanczos", "lanczos_short", "lanczos_short_auto"):
         out["tensor_" + k] = open(os.path.join(work, "dump", "tensor_%s.dat" % k)).read()
     save("tensor.json", out)
 
