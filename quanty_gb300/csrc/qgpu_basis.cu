@@ -426,18 +426,22 @@ extern "C" qg_status qg_basis_find(qg_basis b, int64_t n, const uint8_t *dets_ho
 
 // Expand the rows [r0, r1) of a key list through the forward (push) table: each applicable
 // term's target that passes the restrictions is inserted into the set; new keys are appended
-// to the list.  Lane per source determinant; groups are tested per lane.
+// to the list.  Lane per source determinant; groups are tested per lane.  In a closure
+// (skip_diag) the sources are members of the set already, so the terms that leave a
+// determinant unchanged -- the densities and Coulomb direct terms, most of a Hamiltonian's
+// applicable terms -- are skipped, a whole group at a time where the group holds only those.
 template <int W>
 __global__ void k_expand(const Key<W> *src, int64_t r0, int64_t r1, const GroupDev<W> *__restrict__ groups, int ngroups,
                          const TermDev<W> *__restrict__ terms, int nres, const uint64_t *__restrict__ rmask,
                          const int32_t *__restrict__ rmin, const int32_t *__restrict__ rmax, Slot *slots,
                          uint64_t hmask, Key<W> *list, unsigned long long *count, unsigned long long limit,
-                         unsigned int *err) {
+                         unsigned int *err, int skip_diag) {
   int64_t r = r0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (r >= r1) return;
   Key<W> d = src[r];
   for (int g = 0; g < ngroups; g++) {
     GroupDev<W> G = groups[g];
+    if (skip_diag && G.diag) continue;
     bool ok = true;
 #pragma unroll
     for (int i = 0; i < W; i++) ok &= (d.w[i] & G.need1[i]) == G.need1[i];
@@ -452,7 +456,7 @@ __global__ void k_expand(const Key<W> *src, int64_t r0, int64_t r1, const GroupD
       }
       // a term whose value is zero (a sum operator's component scaled to 0) reaches nothing,
       // as in the reference, whose operators hold no zero terms
-      if (!app || (T.vre == 0.0 && T.vim == 0.0)) continue;
+      if (!app || (T.vre == 0.0 && T.vim == 0.0) || (skip_diag && !moved)) continue;
       Key<W> tg;
 #pragma unroll
       for (int i = 0; i < W; i++) tg.w[i] = d.w[i] ^ T.flip[i];
@@ -464,7 +468,6 @@ __global__ void k_expand(const Key<W> *src, int64_t r0, int64_t r1, const GroupD
         keep = (c >= rmin[q]) && (c <= rmax[q]);
       }
       if (!keep) continue;
-      (void)moved;
       if (*(volatile unsigned long long *)count >= limit) {
         atomicOr(err, QG_DEVERR_TABLE_FULL);
         return;
@@ -607,7 +610,7 @@ static qg_status grow_t(qg_context ctx, qg_operator op, const Key<W> *seed_keys,
     k_expand<W><<<grid_for(f1 - f0), 256, 0, s>>>(
         front, f0, f1, (const GroupDev<W> *)op->push.d_groups, op->push.ngroups, (const TermDev<W> *)op->push.d_terms,
         R.n, d_rmask, d_rmin, d_rmax, slots, (uint64_t)(2 * cap - 1), list, d_count, (unsigned long long)cap,
-        ctx->d_err);
+        ctx->d_err, include_seed ? 1 : 0);
     ctx->launches++;
     unsigned int herr = 0;
     e = cudaMemcpyAsync(&count, d_count, 8, cudaMemcpyDeviceToHost, s);
