@@ -304,10 +304,20 @@ qg_status qg_lanczos_krylov(qg_context ctx, qg_operator op, qg_basis basis, cons
  * each of the last two blocks, entries below eps zeroed.  a_host receives (ntri + 1) blocks
  * and b_host ntri blocks of m x m complex values (interleaved, row-major, zero beyond a
  * deflated block's size; a_0 = 0, b_0(i, j) = <q_j|v0_i>, A_k = Q_k^H H Q_k,
- * B_k = Q_k^H H Q_{k+1}); sizes_host (ntri + 1) the block sizes (sizes[0] = m). */
+ * B_k = Q_k^H H Q_{k+1}); sizes_host (ntri + 1) the block sizes (sizes[0] = m).  krylov_dev
+ * (optional, ntri * m * n complex) receives the blocks Q_1 .. Q_ntri as Krylov vectors,
+ * vector (k - 1) * m + c at [((k - 1) * m + c) * n], zero beyond a block's size
+ * (LanczosBlockTriDiagonalizeKrylov, Core/BlockLanczos.cpp:3649ff). */
 qg_status qg_block_lanczos(qg_context ctx, qg_operator op, qg_basis basis, const double *v0_dev, int32_t m,
                            int32_t ntri, double eps, double singular_value, double *a_host, double *b_host,
-                           int32_t *sizes_host);
+                           int32_t *sizes_host, double *krylov_dev);
+
+/* out_dev (n x np row-major) = sum_i K_i C[i][:] for nk vectors K_i stored vector-major (K_dev,
+ * K_i at [i * n]) and C_host (nk x np row-major complex): the combination of stored Krylov
+ * vectors with the coefficients of a projected resolvent (the G1 T1 psi of RIXS,
+ * Core/ResonantSpectra.cpp:123-195, :1441-1478). */
+qg_status qg_krylov_combine(qg_context ctx, const double *K_dev, int64_t n, int32_t nk, const double *C_host,
+                            int32_t np, double *out_dev);
 
 /* The m x m matrix of spectra of a block tridiagonal matrix by the block continued fraction
  * (BlockTriDiagonalMatrixToSpectraWithBroadening, Core/BasicMathBlock/BasicMath_BlockTypeConversion.cpp:1636):

@@ -782,19 +782,29 @@ def _spectra_dense(H, Tpsi, e0, o, basis, eng, states=False):
     return Spectra(G, emin, emax, NE, gamma, lo, hi), poles
 
 
-def block_lanczos(H, basis, X, ntri, eps, singular_value, eng=None):
+def block_lanczos(H, basis, X, ntri, eps, singular_value, eng=None, krylov=None):
     """Block Lanczos on a device basis (LanczosBlockTriDiagonalize, Core/BlockLanczos.cpp:2131):
     X is an (n, m) complex CUDA tensor of start vectors.  Returns A ((ntri+1), m, m), B (ntri, m,
-    m) complex and the block sizes (ntri + 1)."""
+    m) complex and the block sizes (ntri + 1); krylov (a complex CUDA tensor of ntri * m * n
+    entries) receives the orthonormal blocks as Krylov vectors, vector-major."""
     eng = eng or engine()
     m = X.shape[1]
     a = np.zeros((ntri + 1, m, m), dtype=np.complex128)
     b = np.zeros((ntri, m, m), dtype=np.complex128)
     sizes = np.zeros(ntri + 1, dtype=np.int32)
     Xc = X.contiguous()
+    kp = _ptr(krylov) if krylov is not None else None
     eng.check(eng.L.qg_block_lanczos(eng.ctx, H.handle(eng), basis.h, _ptr(Xc), m, ntri, float(eps),
-                                     float(singular_value), _ptr(a), _ptr(b), _ptr(sizes)))
+                                     float(singular_value), _ptr(a), _ptr(b), _ptr(sizes), kp))
     return a, b, sizes
+
+
+def block_chop(A, eps):
+    """Components below eps set to zero, real and imaginary parts separately
+    (BlockTridiagonalMatrixChop, Core/BasicMathBlock/BasicMath_BlockTridiagonalMatrix.cpp:137)."""
+    re = np.where(np.abs(A.real) < eps, 0.0, A.real)
+    im = np.where(np.abs(A.imag) < eps, 0.0, A.imag)
+    return re + 1j * im
 
 
 def block_tridiagonal_dense(A, B):
@@ -1499,27 +1509,29 @@ def _rixs_dense(H1, H2, T1s, T2s, psis, o, b1, b2, tensor, eng):
 
 
 def _rixs_krylov_tensor(H1, H2, T1s, T2s, psis, o, eng):
-    """Krylov tensor RIXS, the result of ResonantSpectraTensor (Core/ResonantSpectra.cpp:1204):
-    the matrix <v_a| (w + E2 - H2 + i Gamma2/2)^-1 |v_b> of the vectors
-    v_(psi, T1, T2) = T2 G1(w_l) T1 psi for every incident energy, both shifts from psi 0 (as the
-    reference).  The reference runs one block Lanczos per stage; here every T1 psi gets its own
-    three-term Lanczos with stored Krylov vectors and G1(w_l) T1 psi is that space's projected
-    resolvent, all w_l at once; the matrix elements come from one batched Lanczos over every
-    diagonal vector and, per pair, v_a + v_b and v_a + i v_b (polarisation).  Each chain runs
-    as many steps as the block run has Krylov vectors (NTri blocks times the block width, at
-    most 16 past the basis size), so a complete block space means complete chains, and then
-    the result equals the block-Lanczos one.  The reference's index order is kept: spectrum
+    """Krylov tensor RIXS (ResonantSpectraTensor, Core/ResonantSpectra.cpp:1204-1700): the matrix
+    <v_a| (w + E2 - H2 + i Gamma2/2)^-1 |v_b> of the vectors v_(psi, T1, T2) = T2 G1(w_l) T1 psi
+    for every incident energy w_l, both shifts from psi 0, as the reference computes it:
+      1. the block of T1 psi (j = iT1 + NT1 ipsi) on one basis, entries below Epsilon dropped;
+      2. a block Lanczos of H1 from it that keeps its Krylov blocks (qg_block_lanczos), the block
+         tridiagonal matrix chopped at Epsilon and diagonalised on the device; the intermediate
+         window from its extreme eigenvalues;
+      3. G1(w_l) T1 psi_j = Q (w_l - T + i Gamma1/2)^-1 Q^H T1 psi_j for all l at once: the
+         coefficients in the Krylov basis (Q^H T1 psi_j is the first block's b_0) and the
+         combination of the stored vectors on the device (qg_krylov_combine);
+      4. T2 on all of them in one multi-vector launch per T2;
+      5. per incident energy a block Lanczos of H2 from its NT2 NT1 Npsi vectors, chopped, the
+         final window from the first energy's block eigenvalues (the reference sets it there and
+         keeps it), and the m x m spectra by the block continued fraction.
+    The reference's index order is kept: spectrum
     l + (NE1+1)(j2 + NT2(i1 + NT1(n2 + NT2(m1 + NT1(r + Npsi s)))))
-    holds the element between v_(r, m1, n2) (left) and v_(s, i1, j2) (right).  Energy ranges
-    come from the extreme Krylov eigenvalues with the block branch's rules; when the
-    second-stage block dimension (NTri2 times the block width) exceeds the final basis, the
-    reference's block matrix ends in zero blocks and its range includes their eigenvalue 0,
-    which is added here too."""
+    holds the element between v_(r, m1, n2) (left) and v_(s, i1, j2) (right)."""
     torch = eng.torch
     dev = "cuda:%d" % eng.device
     npsi, nt1, nt2 = len(psis), len(T1s), len(T2s)
     M1, nf = npsi * nt1, H1.nf
     eps, ntri1, ntri2 = float(o["Epsilon"]), int(o["NTri1"]), int(o["NTri2"])
+    sv = float(o.get("SingularValue", DEFAULTS["SingularValue"]))
     R1, R2 = o.get("Restrictions1"), o.get("Restrictions2")
     e1 = float(_rixs_energies(H1, psis[:1], "E0_1", o, eng, normalise=False)[0])
     e2 = float(_rixs_energies(H2, psis[:1], "E0_2", o, eng, normalise=False)[0])
@@ -1539,32 +1551,32 @@ def _rixs_krylov_tensor(H1, H2, T1s, T2s, psis, o, eng):
             # keep |a|^2 > epsilon^2
             v = np.where(t.val.real ** 2 + t.val.imag ** 2 > eps * eps, t.val, 0.0)
             np.add.at(X1[:, j], b1.find(t.det), v)
-    # each chain gets the Krylov dimension of the reference's block run, NTri1 blocks of M1
-    # (a few steps past the basis size at most); three-term Lanczos keeping its vectors
-    L1 = max(1, min(ntri1 * M1, n1 + 16))
-    chains = []
-    for j in range(M1):
-        with eng.on_stream():
-            x = torch.from_numpy(np.ascontiguousarray(X1[:, j:j + 1])).to(dev)
-            K = torch.zeros((L1, n1, 1), dtype=torch.complex128, device=dev)
-        A1, B1 = lanczos_block(H1, b1, x, L1, eps, eps, eng, krylov=K)
-        a, b = A1[0], B1[0]
-        k = next((q for q in range(1, L1) if b[q] == 0.0), L1)
-        T = np.diag(a[1:k + 1]) + np.diag(b[1:k], 1) + np.diag(b[1:k], -1)
-        ev, Z = hermitian_eigh(T.astype(np.complex128), k, eng)
-        chains.append((K[:, :, 0], k, b[0], ev, Z.real))
-    lo = min(c[3][0] for c in chains if c[2] != 0.0) if any(c[2] != 0.0 for c in chains) else 0.0
-    hi = max(c[3][-1] for c in chains if c[2] != 0.0) if any(c[2] != 0.0 for c in chains) else 0.0
-    emin1, emax1, g1 = _default_window(lo - e1, hi - e1, o.get("Emin1"), o.get("Emax1"),
+    nk = ntri1 * M1
+    with eng.on_stream():
+        x1 = torch.from_numpy(X1).to(dev)
+        K1 = torch.zeros((nk, n1), dtype=torch.complex128, device=dev)
+    A1, B1, sizes1 = block_lanczos(H1, b1, x1, ntri1, eps, sv, eng, krylov=K1)
+    A1, B1 = block_chop(A1, eps), block_chop(B1, eps)
+    T1m = block_tridiagonal_dense(A1, B1)
+    ev, Z = hermitian_eigh(T1m, nk, eng)
+    # the intermediate window from the Krylov directions the recursion kept: the rows of
+    # deflated directions are zero and their eigenvalue 0 stays out of it (they carry no weight
+    # of T1 psi either)
+    live = [k * M1 + c for k in range(ntri1) for c in range(int(sizes1[k + 1]))]
+    evl = hermitian_eigh(T1m[np.ix_(live, live)], 0, eng)[0] if live else np.zeros(1)
+    emin1, emax1, g1 = _default_window(evl[0] - e1, evl[-1] - e1, o.get("Emin1"), o.get("Emax1"),
                                        float(o.get("Gamma1", 0.0)), ne1)
     wres = np.array([emin1 + (emax1 - emin1) * p / ne1 + e1 for p in range(np1)])
-    # G1(w_l) T1 psi_j for all l: column l + np1 j on b1
-    with eng.on_stream():
-        GT = torch.zeros((n1, M1 * np1), dtype=torch.complex128, device=dev)
-    for j, (K, k, b0, ev, Z) in enumerate(chains):
-        Cc = b0 * (Z[:, None, :] * (Z[0, :][None, None, :] / (wres[None, :, None] - ev[None, None, :] + 0.5j * g1))).sum(-1)
-        with eng.on_stream():
-            GT[:, j * np1:(j + 1) * np1] = K[:k].T @ torch.from_numpy(np.ascontiguousarray(Cc)).to(dev)
+    # coefficients of G1(w_l) T1 psi_j in the Krylov basis, column l * M1 + j:
+    # Z diag(1 / (w_l - ev + i g1/2)) Z^H[:, first block] b_0^T
+    first = Z[:M1, :].conj().T @ B1[0].T
+    Cc = np.zeros((nk, np1 * M1), dtype=np.complex128)
+    for p in range(np1):
+        Cc[:, p * M1:(p + 1) * M1] = Z @ (first / (wres[p] - ev + 0.5j * g1)[:, None])
+    GT = eng.empty(n1, np1 * M1)
+    Cc = np.ascontiguousarray(Cc)
+    eng.check(eng.L.qg_krylov_combine(eng.ctx, _ptr(K1), n1, nk, _ptr(Cc), np1 * M1, _ptr(GT)))
+    del K1
     # final-state basis: targets of every T2, closure under H2
     bt = None
     for T in T2s:
@@ -1578,70 +1590,25 @@ def _rixs_krylov_tensor(H1, H2, T1s, T2s, psis, o, eng):
     if not n2:
         st.update(emin2=o.get("Emin2"), emax2=o.get("Emax2"), ne2=ne2, gamma2=float(o.get("Gamma2", 0.0)))
         return G, st
-    # v_a(l), a = s + NT2 j: Y[s] column l + np1 j
+    # T2_s G1(w_l) T1 psi_j: Y[s] column l * M1 + j
     Y = []
     for T in T2s:
-        yv = eng.empty(n2, M1 * np1)
-        eng.check(eng.L.qg_apply(eng.ctx, T.handle(eng), b2.h, b1.h, _ptr(GT), _ptr(yv), M1 * np1))
+        yv = eng.empty(n2, np1 * M1)
+        eng.check(eng.L.qg_apply(eng.ctx, T.handle(eng), b2.h, b1.h, _ptr(GT), _ptr(yv), np1 * M1))
         Y.append(yv[:n2])
-    pairs = [(a_, b_) for a_ in range(M) for b_ in range(a_ + 1, M)]
-    per_l = M + 2 * len(pairs)  # chains per incident energy: diagonals, then v_a + v_b, v_a + i v_b
-
-    def vec(l, a_):
-        s_, j = a_ % nt2, a_ // nt2
-        return Y[s_][:, l + np1 * j]
-
-    gamma_l = max(float(o.get("Gamma2", 0.0)), eps)
-    L2 = max(1, min(ntri2 * M, n2 + 16))  # the block run's Krylov dimension, NTri2 blocks of M
-    # incident energies in chunks of at most ~1 GiB of start vectors (the Lanczos holds six
-    # blocks of that size)
-    chunk = max(1, min(np1, (1 << 30) // (per_l * n2 * 16)))
-    Gm = np.zeros((np1, M, M, ne2 + 1), dtype=np.complex128)
     emin2 = emax2 = g2 = None
-    for l0 in range(0, np1, chunk):
-        ls = range(l0, min(np1, l0 + chunk))
+    Gm = np.zeros((np1, M, M, ne2 + 1), dtype=np.complex128)  # vectors in the order s * M1 + j
+    for p in range(np1):
         with eng.on_stream():
-            Zc = torch.empty((n2, per_l * len(ls)), dtype=torch.complex128, device=dev)
-            c = 0
-            for l in ls:
-                for a_ in range(M):
-                    Zc[:, c] = vec(l, a_)
-                    c += 1
-                for a_, b_ in pairs:
-                    Zc[:, c] = vec(l, a_) + vec(l, b_)
-                    Zc[:, c + 1] = vec(l, a_) + 1j * vec(l, b_)
-                    c += 2
-        A2, B2 = lanczos_block(H2, b2, Zc, L2, eps, gamma_l, eng)
+            Zp = torch.cat([y[:, p * M1:(p + 1) * M1] for y in Y], dim=1).contiguous()
+        A2, B2, _ = block_lanczos(H2, b2, Zp, ntri2, eps, sv, eng)
+        A2, B2 = block_chop(A2, eps), block_chop(B2, eps)
         if emin2 is None:
-            # ranges from the first incident energy's diagonal chains, the block branch's rules
-            lo2, hi2 = np.inf, -np.inf
-            for c in range(M):
-                if B2[c, 0] == 0.0:
-                    continue
-                k = next((q for q in range(1, L2) if B2[c, q] == 0.0), L2)
-                w0, w1_ = _tri_extremes(A2[c, 1:k + 1], B2[c, 1:k])
-                lo2, hi2 = min(lo2, w0 - e2), max(hi2, w1_ - e2)
-            if not np.isfinite(lo2):
-                lo2 = hi2 = 0.0
-            if ntri2 * M > n2:
-                # the reference's second-stage block matrix then ends in unused zero blocks,
-                # whose eigenvalue 0 enters its pole range (its Krylov-basis first stage drops
-                # them)
-                lo2, hi2 = min(lo2, -e2), max(hi2, -e2)
-            emin2, emax2, g2 = _default_window(lo2, hi2, o.get("Emin2"), o.get("Emax2"),
+            val, _ = hermitian_eigh(block_tridiagonal_dense(A2, B2), 0, eng)
+            emin2, emax2, g2 = _default_window(val[0] - e2, val[-1] - e2, o.get("Emin2"), o.get("Emax2"),
                                                float(o.get("Gamma2", 0.0)), ne2)
             st.update(emin2=emin2, emax2=emax2, ne2=ne2, gamma2=g2)
-        Dcf = TriDiagonalMatrixToSpectrum(np.full(A2.shape[0], e2), A2, B2, emin2, emax2, ne2, g2, eng)
-        for q0, l in enumerate(ls):
-            c0 = q0 * per_l
-            diag = Dcf[c0:c0 + M]
-            for a_ in range(M):
-                Gm[l, a_, a_] = diag[a_]
-            for q, (a_, b_) in enumerate(pairs):
-                S_ = Dcf[c0 + M + 2 * q] - diag[a_] - diag[b_]
-                T_ = Dcf[c0 + M + 2 * q + 1] - diag[a_] - diag[b_]
-                Gm[l, a_, b_] = 0.5 * (S_ - 1j * T_)
-                Gm[l, b_, a_] = 0.5 * (S_ + 1j * T_)
+        Gm[p] = BlockTriDiagonalMatrixToSpectra(e2, A2, B2, emin2, emax2, ne2, g2, eng).reshape(M, M, ne2 + 1)
     for r in range(npsi):
         for s_ in range(npsi):
             for i1 in range(nt1):
@@ -1649,7 +1616,7 @@ def _rixs_krylov_tensor(H1, H2, T1s, T2s, psis, o, eng):
                     for m1 in range(nt1):
                         for n2_ in range(nt2):
                             idx = j2 + nt2 * (i1 + nt1 * (n2_ + nt2 * (m1 + nt1 * (r + npsi * s_))))
-                            row = n2_ + nt2 * (m1 + nt1 * r)
-                            col = j2 + nt2 * (i1 + nt1 * s_)
+                            row = n2_ * M1 + (m1 + nt1 * r)
+                            col = j2 * M1 + (i1 + nt1 * s_)
                             G[np1 * idx:np1 * (idx + 1)] = Gm[:, row, col]
     return G, st

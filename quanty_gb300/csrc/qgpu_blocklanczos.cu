@@ -38,6 +38,17 @@ __global__ void k_block_trunc(double2 *v, int ld, int k, int64_t n, double eps2)
   if (a.x * a.x + a.y * a.y < eps2) *p = make_double2(0.0, 0.0);
 }
 
+// the orthonormal block Q (n x m row-major, k live columns) as Krylov vectors k0 .. k0+m-1,
+// vector-major (K[(k0 + c) * n + r]), the columns beyond k zero
+__global__ void k_store_block(const double2 *__restrict__ Q, int m, int k, int64_t n, double2 *__restrict__ K,
+                              int64_t k0) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= n * m) return;
+  const int c = (int)(t / n);
+  const int64_t r = t % n;
+  K[(k0 + c) * n + r] = c < k ? Q[r * m + c] : make_double2(0.0, 0.0);
+}
+
 namespace {
 
 struct BlockCtx {
@@ -124,7 +135,7 @@ struct BlockCtx {
 
 extern "C" qg_status qg_block_lanczos(qg_context ctx, qg_operator op, qg_basis b, const double *v0_dev, int32_t m,
                                       int32_t ntri, double eps, double singular_value, double *a_host, double *b_host,
-                                      int32_t *sizes_host) {
+                                      int32_t *sizes_host, double *krylov_dev) {
   if (!ctx || !op || !b || !v0_dev || m <= 0 || ntri <= 0 || !a_host || !b_host || !sizes_host || op->nf != b->nf)
     return QG_ERR_ARG;
   const int64_t n = b->n;
@@ -170,7 +181,16 @@ extern "C" qg_status qg_block_lanczos(qg_context ctx, qg_operator op, qg_basis b
       for (int j = 0; j < k; j++) B[(size_t)i * m + j] = G[(size_t)j * m + i];
   if (st == QG_OK) sizes[1] = k;
   const double eps2 = eps * eps;
+  if (st == QG_OK && krylov_dev) {  // every block is written, deflated ones as zeros
+    e = cudaMemsetAsync(krylov_dev, 0, (size_t)ntri * m * n * 16, s);
+    if (e != cudaSuccess) st = qg_cuda_fail(ctx, e, "qg_block_lanczos");
+  }
   for (int it = 1; st == QG_OK && k > 0 && it <= ntri; it++) {
+    if (krylov_dev) {
+      k_store_block<<<(unsigned)((n * m + 255) / 256), 256, 0, s>>>(Q, m, k, n, (double2 *)krylov_dev,
+                                                                    (int64_t)(it - 1) * m);
+      ctx->launches++;
+    }
     // W = H Q_it
     st = qg_apply_strided(ctx, op, b, b, (const double *)Q, m, (double *)W, m, k, nullptr);
     if (st != QG_OK) break;

@@ -198,3 +198,20 @@ qg_status qg_block_combine(qg_context ctx, const double2 *K, int64_t n, int ntri
   }
   return block_mul(ctx, K, 1, n, ntri, C, np, out, np, np, n, 1.0, 0.0);
 }
+
+extern "C" qg_status qg_krylov_combine(qg_context ctx, const double *K_dev, int64_t n, int32_t nk, const double *C_host,
+                                       int32_t np, double *out_dev) {
+  if (!ctx || n < 0 || nk < 0 || np <= 0 || (n > 0 && (!K_dev || !out_dev)) || (nk > 0 && !C_host)) return QG_ERR_ARG;
+  if (n == 0) return QG_OK;
+  double2 *Cd = nullptr;
+  QG_CUDA(ctx, cudaMalloc(&Cd, (size_t)std::max(nk, 1) * np * 16));
+  cudaError_t e = cudaMemcpyAsync(Cd, C_host, (size_t)nk * np * 16, cudaMemcpyHostToDevice, ctx->stream);
+  qg_status st = e == cudaSuccess ? qg_block_combine(ctx, (const double2 *)K_dev, n, nk, Cd, np, (double2 *)out_dev)
+                                  : qg_cuda_fail(ctx, e, "qg_krylov_combine");
+  if (st == QG_OK) {
+    e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) st = qg_cuda_fail(ctx, e, "qg_krylov_combine");
+  }
+  cudaFree(Cd);
+  return st;
+}

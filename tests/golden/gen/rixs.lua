@@ -74,4 +74,10 @@ S = CreateResonantSpectra(HX, H, {Tx, Ty}, {Txd, Tyd}, psi1, opts({{"Restriction
 S.Print({{"file", "dump/krylov_res1.dat"}})
 S = CreateResonantSpectra(HX, H, {Tx, Ty}, {Txd, Tyd}, psi1, opts({{"Restrictions1", R1}, {"DenseBorder", 0}, {"Epsilon", 0}, {"Tensor", true}}))
 S.Print({{"file", "dump/krylov_tensor_res1.dat"}})
+-- Krylov tensor form with incomplete Krylov spaces (8 intermediate and 20 final Krylov vectors
+-- on 60 and 45 determinants): the result depends on both block recursions
+S = CreateResonantSpectra(HX, H, {Tx, Ty}, {Txd, Tyd}, psi1, opts({{"DenseBorder", 0}, {"Epsilon", 0}, {"Tensor", true}, {"NTri1", 4}, {"NTri2", 5}}))
+S.Print({{"file", "dump/krylov_tensor_short.dat"}})
+S = CreateResonantSpectra(HX, H, {Tx, Ty}, {Txd}, psi1, {{"NE1", 3}, {"NE2", 48}, {"DenseBorder", 0}, {"Epsilon", 0}, {"Tensor", true}, {"NTri1", 6}, {"NTri2", 8}})
+S.Print({{"file", "dump/krylov_tensor_short_auto.dat"}})
 print("rixs done")

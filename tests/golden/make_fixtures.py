@@ -298,7 +298,7 @@ def gen_rixs():
         out[n] = op(work, n)
     for k in ("dense_lists", "dense_auto", "dense_tensor", "dense_tensor_psi", "krylov_lists", "krylov_tensor",
               "krylov_tensor_auto", "krylov_tensor_psi", "dense_shifts", "dense_e0", "dense_res2", "krylov_res2", "dense_res1", "krylov_res1",
-              "krylov_tensor_res1"):
+              "krylov_tensor_res1", "krylov_tensor_short", "krylov_tensor_short_auto"):
         out[k] = spectra(work, k + ".dat")
     save("rixs.json", out)
 

@@ -2,7 +2,7 @@
 the 16-orbital 2p -> 3d case: the dense branch the reference takes below DenseBorder, with
 lists of absorption operators, emission operators and initial states and with automatic
 energy ranges; the tensor form of the dense branch; the Krylov branch with lists; the Krylov
-tensor form at complete Krylov spaces."""
+tensor form (block Lanczos in both stages) at complete and incomplete Krylov spaces."""
 import numpy as np
 import pytest
 
@@ -29,6 +29,13 @@ CASES = [
     ("krylov_lists", ("Tx", "Ty"), ("Txd", "Tyd"), 2, {"DenseBorder": 0, "Epsilon": 0.0}),
     ("krylov_tensor", ("Tx", "Ty"), ("Txd", "Tyd"), 1,
      {"DenseBorder": 0, "Epsilon": 0.0, "Tensor": True, "NTri1": 40, "NTri2": 40}),
+    # incomplete Krylov spaces (8 intermediate and 20 final vectors): the spectra depend on
+    # both block recursions, not only on the Hamiltonians
+    ("krylov_tensor_short", ("Tx", "Ty"), ("Txd", "Tyd"), 1,
+     {"DenseBorder": 0, "Epsilon": 0.0, "Tensor": True, "NTri1": 4, "NTri2": 5}),
+    ("krylov_tensor_short_auto", ("Tx", "Ty"), ("Txd",), 1,
+     {"auto": True, "NE1": 3, "NE2": 48, "DenseBorder": 0, "Epsilon": 0.0, "Tensor": True, "NTri1": 6,
+      "NTri2": 8}),
 ]
 
 
@@ -39,6 +46,8 @@ def test_rixs_matches_reference(api, key, t1, t2, npsi, extra):
     psis = [api.Wavefunction.from_fixture(p) for p in g["psi"][:npsi]]
     if extra is None:  # automatic intermediate and final energy ranges
         o = {"NE1": 4, "Gamma1": 0.8, "NE2": 64, "Gamma2": 0.3}
+    elif extra.get("auto"):  # automatic ranges and default broadenings
+        o = {k: v for k, v in extra.items() if k != "auto"}
     else:
         o = dict(g["opts"], **extra)
     T1 = [op(t) for t in t1] if len(t1) > 1 else op(t1[0])

@@ -96,6 +96,10 @@ def host_api(monkeypatch, oracle_mod):
                 Y[:dst.n, c] = apply_vec(T, dst, src, X[:src.n, c])
             return 0
 
+        def qg_krylov_combine(self, ctx, K, n, nk, C, npc, out):
+            out.numpy()[:n, :npc] = K.numpy()[:nk, :n].T @ np.asarray(C).reshape(nk, npc)
+            return 0
+
     zeros, empty = torch.zeros, torch.empty
 
     class Eng:
@@ -140,6 +144,68 @@ def host_api(monkeypatch, oracle_mod):
             A.append(a)
             Bv.append(bb)
         return np.array(A), np.array(Bv)
+
+    def lowdin_once(V, reduce, sv):
+        S = V.conj().T @ V
+        w, U = np.linalg.eigh(0.5 * (S + S.conj().T))
+        s = np.sqrt(np.maximum(w, 0.0))
+        zero = max(sv, 3 * np.sqrt(np.finfo(float).eps) * (s.max() if len(s) else 0.0))
+        keep = [i for i in range(len(s)) if (not reduce and s[i] > 0) or s[i] > zero]
+        if len(keep) == len(s):
+            return V @ (U / s) @ U.conj().T
+        return V @ (U[:, keep] / s[keep])
+
+    def block_lanczos(H, b, x, ntri, eps, sv, eng=None, krylov=None):
+        """The block recursion of qg_block_lanczos in numpy on the dense H: Loewdin twice with
+        the deflation rule, six projections, entries below eps zeroed."""
+        Hm = O.dense_matrix(_oop(O, H), b.wf())
+        V0 = x.numpy()[:b.n]
+        m = V0.shape[1]
+        A = np.zeros((ntri + 1, m, m), dtype=np.complex128)
+        Bm = np.zeros((ntri, m, m), dtype=np.complex128)
+        sizes = np.zeros(ntri + 1, dtype=np.int32)
+        sizes[0] = m
+
+        def lowdin(V):
+            Q = lowdin_once(V, True, sv)
+            return lowdin_once(Q, False, sv) if Q.shape[1] else Q
+        Q = lowdin(V0)
+        k = Q.shape[1]
+        sizes[1] = k
+        Bm[0][:, :k] = (Q.conj().T @ V0).T
+        Qp = np.zeros((b.n, 0), dtype=np.complex128)
+        for it in range(1, ntri + 1):
+            if k == 0:
+                break
+            if krylov is not None:
+                krylov.numpy()[(it - 1) * m:(it - 1) * m + k, :b.n] = Q.T
+            W = Hm @ Q
+            A[it][:k, :k] = Q.conj().T @ W
+            if it > 1:
+                Bm[it - 1][:Qp.shape[1], :k] = Qp.conj().T @ W
+            if it == ntri:
+                break
+            for P in (Q, Q, Qp, Qp, Q, Qp):
+                W = W - P @ (P.conj().T @ W)
+            Qn = lowdin(W)
+            if eps > 0:
+                Qn = np.where(np.abs(Qn) ** 2 < eps * eps, 0.0, Qn)
+            sizes[it + 1] = Qn.shape[1]
+            Qp, Q, k = Q, Qn, Qn.shape[1]
+        return A, Bm, sizes
+
+    def block_cf(E0, A, Bm, emin, emax, ne, g, eng=None):
+        m = A.shape[1]
+        out = np.zeros((m * m, ne + 1), dtype=np.complex128)
+        for kf in range(ne + 1):
+            w = emin + kf * (emax - emin) / ne + E0
+            G = np.zeros((m, m), dtype=np.complex128)
+            for blk in range(A.shape[0] - 1, 0, -1):
+                G = np.linalg.inv((w + 0.5j * g) * np.eye(m) - A[blk] - G)
+                Bk = Bm[blk - 1]
+                G = (Bk.conj() @ G @ Bk.T) if blk == 1 else (Bk @ G @ Bk.conj().T)
+            out[:, kf] = G.reshape(-1)
+        return out
 
     def poles(E0, p, W, emin, emax, ne, g, eng=None):
         W = np.atleast_2d(W)
@@ -203,6 +269,8 @@ def host_api(monkeypatch, oracle_mod):
     monkeypatch.setattr(api, "lanczos_block", plain_lanczos)
     monkeypatch.setattr(api, "TriDiagonalMatrixToSpectrum", cf)
     monkeypatch.setattr(api, "_rixs_krylov", krylov_one)
+    monkeypatch.setattr(api, "block_lanczos", block_lanczos)
+    monkeypatch.setattr(api, "BlockTriDiagonalMatrixToSpectra", block_cf)
     return api
 
 
@@ -233,6 +301,10 @@ CASES = [
      dict(GRID, Restrictions1=[16, 0, ["000000 1010101010", 5, 5]], **KRYLOV), "krylov"),
     ("krylov_tensor_res1", ("Tx", "Ty"), ("Txd", "Tyd"), 1,
      dict(GRID, Restrictions1=[16, 0, ["000000 1010101010", 5, 5]], Tensor=True, **KRYLOV), "krylov_tensor"),
+    ("krylov_tensor_short", ("Tx", "Ty"), ("Txd", "Tyd"), 1, dict(GRID, Tensor=True, NTri1=4, NTri2=5, **KRYLOV),
+     "krylov_tensor"),
+    ("krylov_tensor_short_auto", ("Tx", "Ty"), ("Txd",), 1,
+     dict(KRYLOV, NE1=3, NE2=48, Tensor=True, NTri1=6, NTri2=8), "krylov_tensor"),
 ]
 
 
@@ -452,3 +524,31 @@ def test_operator_restrictions_apply_to_h_psi(monkeypatch):
     api.OperatorPsi(O, psi, eng=Eng())
     api.OperatorPsi(O, psi, [4, 0, ["1111", 1, 1]], eng=Eng())
     assert seen == [None, [4, 0, ["1100", 1, 1]], [4, 0, ["1111", 1, 1]]]
+
+
+TENSOR = {
+    "tensor_lanczos": {"Tensor": True, "Method": "Lanczos", "NE": 40, "Emin": -5, "Emax": 15, "Gamma": 0.6,
+                       "Epsilon": 0.0},
+    "tensor_lanczos_short": {"Tensor": True, "Method": "Lanczos", "NTri": 5, "NE": 40, "Emin": -5, "Emax": 15,
+                             "Gamma": 0.6, "Epsilon": 0.0},
+    "tensor_lanczos_short_auto": {"Tensor": True, "Method": "Lanczos", "NTri": 8, "NE": 32},
+}
+
+
+@pytest.mark.parametrize("key", list(TENSOR))
+def test_tensor_spectra_orchestration_matches_reference(host_api, key):
+    """CreateSpectra with Tensor = true, block-Lanczos branch: the block recursion, the pole
+    range from the whole block tridiagonal matrix and the block continued fraction (numpy
+    restatements of the device calls) against the reference's spectra, complete and incomplete
+    Krylov spaces."""
+    api = host_api
+    g = golden("tensor.json")
+    HX = api.Operator.from_fixture(g["HX"])
+    Ts = [api.Operator.from_fixture(g[t]) for t in ("Tx", "Ty", "Tz")]
+    psi = api.Wavefunction.from_fixture(g["psi"])
+    S, _ = api.CreateSpectra(HX, Ts, [psi], TENSOR[key])
+    R = api.Spectra.from_text(g[key])
+    assert S.G.shape == R.G.shape
+    assert abs(S.Emin - R.Emin) < 1e-8 and abs(S.Emax - R.Emax) < 1e-8 and abs(S.Gamma - R.Gamma) < 1e-8
+    assert abs(S.EminPole - R.EminPole) < 1e-8 and abs(S.EmaxPole - R.EmaxPole) < 1e-8
+    assert np.max(np.abs(S.G - R.G)) < TOL * np.max(np.abs(R.G))
