@@ -183,6 +183,35 @@ __device__ __forceinline__ void qg_cmac(double2 &acc, double vr, double vi, bool
   acc.y = fma(vr, xv.y, acc.y);
 }
 
+// The fused Lanczos epilogue's per-block partial of a = Re <x|H x> for each of NV vectors (the
+// Lanczos diagonal is real).  The apply kernels are bound by the FP64 pipe, so the reduction
+// spends as few FP64 adds as it can: the rows' terms go to shared memory in row order (dvs of
+// the row at block position me), eight threads per vector add 32 terms each and one thread adds
+// their eight sums -- about one add per row, where a warp-shuffle tree costs five per row and
+// vector.  Every apply kernel reduces in this order, so their Lanczos chains agree bitwise.
+// Blocks of 256 threads; s_dot holds NV x 256 doubles (stride 256), s_red NV x 8.
+template <int NV>
+__device__ __forceinline__ void fused_dot_partials(const double *dvs, int me, double *s_dot, double *s_red,
+                                                   double2 *part, int ys, int vec0) {
+#pragma unroll
+  for (int k = 0; k < NV; k++) s_dot[k * 256 + me] = dvs[k];
+  __syncthreads();
+  if (threadIdx.x < NV * 8) {
+    const int k = threadIdx.x >> 3, seg = threadIdx.x & 7;
+    double t = 0.0;
+#pragma unroll 8
+    for (int i = 0; i < 32; i++) t += s_dot[k * 256 + seg * 32 + i];
+    s_red[k * 8 + seg] = t;
+  }
+  __syncthreads();
+  if (threadIdx.x < NV) {
+    double t = 0.0;
+#pragma unroll
+    for (int g = 0; g < 8; g++) t += s_red[threadIdx.x * 8 + g];
+    part[blockIdx.x * ys + vec0 + threadIdx.x] = make_double2(t, 0.0);
+  }
+}
+
 template <int W, int NV, bool FUSE, bool SMEM>
 __global__ void __launch_bounds__(256, NV == 1 ? QG_APPLY_MIN_BLOCKS : 1) k_apply(const Key<W> *__restrict__ rows, int64_t n_rows,
                                                const unsigned char *__restrict__ gtab, uint32_t tab_bytes,
@@ -356,37 +385,22 @@ __global__ void __launch_bounds__(256, NV == 1 ? QG_APPLY_MIN_BLOCKS : 1) k_appl
       for (int k = 0; k < NV; k++) y[r * ys + vec0 + k] = acc[k];
     }
   } else {
-    // fused epilogue: dot partials conj(x_r) (Hx)_r and the three-term update
-    __shared__ double2 red[NV][8];
-    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    // fused epilogue: y = H x - beta prev and the block's partial of Re <x|H x>
+    __shared__ double s_dot[NV * 256], s_red[NV * 8];
+    double dvs[NV];
 #pragma unroll
     for (int k = 0; k < NV; k++) {
-      double2 dv = make_double2(0.0, 0.0);
+      double dv = 0.0;
       if (live) {
         double2 xv = x[r * xs + vec0 + k];
-        dv.x = xv.x * acc[k].x + xv.y * acc[k].y;
-        dv.y = xv.x * acc[k].y - xv.y * acc[k].x;
+        dv = xv.x * acc[k].x + xv.y * acc[k].y;
         double2 pv = fz.prev[r * ys + vec0 + k];
         double be = fz.beta[vec0 + k];
         y[r * ys + vec0 + k] = make_double2(acc[k].x - be * pv.x, acc[k].y - be * pv.y);
       }
-#pragma unroll
-      for (int o = 16; o; o >>= 1) {
-        dv.x += __shfl_xor_sync(0xffffffffu, dv.x, o);
-        dv.y += __shfl_xor_sync(0xffffffffu, dv.y, o);
-      }
-      if (lane == 0) red[k][wid] = dv;
+      dvs[k] = dv;
     }
-    __syncthreads();
-    if (threadIdx.x < NV) {
-      int k = threadIdx.x;
-      double2 s = make_double2(0.0, 0.0);
-      for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
-        s.x += red[k][w].x;
-        s.y += red[k][w].y;
-      }
-      fz.dot_part[blockIdx.x * ys + vec0 + k] = s;
-    }
+    fused_dot_partials<NV>(dvs, threadIdx.x, s_dot, s_red, fz.dot_part, ys, vec0);
   }
   if (SMEM && pending) mbar_wait_bounded(smem_addr(&s_bar), 0);  // never leave with a copy in flight
 }
@@ -852,7 +866,8 @@ __global__ void __launch_bounds__(256, NV == 1 ? QG_APPLY_MIN_BLOCKS : 1)
     }
   }
   int me = threadIdx.x;  // the block position of the row this thread finishes
-  __shared__ double2 s_acc[QG_LIST_REGROUP ? NV : 1][QG_LIST_REGROUP ? 256 : 1];  // also the dot partials
+  // regrouped accumulators, then (FUSE) the rows' dot terms in their original order
+  __shared__ double2 s_acc[QG_LIST_REGROUP || FUSE ? NV : 1][QG_LIST_REGROUP || FUSE ? 256 : 1];
   if (QG_LIST_REGROUP) {
     __shared__ int s_cnt[QG_REGROUP_BUCKETS];
     __shared__ int64_t s_p[256], s_pe[256];
@@ -916,50 +931,24 @@ __global__ void __launch_bounds__(256, NV == 1 ? QG_APPLY_MIN_BLOCKS : 1)
       for (int k = 0; k < NV; k++) y[r * ys + vec0 + k] = acc[k];
     }
   } else {
-    __shared__ double2 red[NV][8];
-    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    double2 dvs[NV];
+    // y = H x - beta prev and the block's partial of Re <x|H x>, reduced in the original row
+    // order (the regrouped accumulators' storage holds the rows' terms)
+    __shared__ double s_red[NV * 8];
+    double dvs[NV];
 #pragma unroll
     for (int k = 0; k < NV; k++) {
-      double2 dv = make_double2(0.0, 0.0);
+      double dv = 0.0;
       if (live) {
         double2 xv = x[r * xs + vec0 + k];
-        dv.x = xv.x * acc[k].x + xv.y * acc[k].y;
-        dv.y = xv.x * acc[k].y - xv.y * acc[k].x;
+        dv = xv.x * acc[k].x + xv.y * acc[k].y;
         double2 pv = fz.prev[r * ys + vec0 + k];
         double be = fz.beta[vec0 + k];
         y[r * ys + vec0 + k] = make_double2(acc[k].x - be * pv.x, acc[k].y - be * pv.y);
       }
       dvs[k] = dv;
     }
-    if (QG_LIST_REGROUP) {  // back to the original row order for the reduction
-      __syncthreads();  // every regrouped accumulator has been read
-#pragma unroll
-      for (int k = 0; k < NV; k++) s_acc[k][me] = dvs[k];
-      __syncthreads();
-#pragma unroll
-      for (int k = 0; k < NV; k++) dvs[k] = s_acc[k][threadIdx.x];
-    }
-#pragma unroll
-    for (int k = 0; k < NV; k++) {
-      double2 dv = dvs[k];
-#pragma unroll
-      for (int o = 16; o; o >>= 1) {
-        dv.x += __shfl_xor_sync(0xffffffffu, dv.x, o);
-        dv.y += __shfl_xor_sync(0xffffffffu, dv.y, o);
-      }
-      if (lane == 0) red[k][wid] = dv;
-    }
-    __syncthreads();
-    if (threadIdx.x < NV) {
-      int k = threadIdx.x;
-      double2 s = make_double2(0.0, 0.0);
-      for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
-        s.x += red[k][w].x;
-        s.y += red[k][w].y;
-      }
-      fz.dot_part[blockIdx.x * ys + vec0 + k] = s;
-    }
+    if (QG_LIST_REGROUP) __syncthreads();  // every regrouped accumulator has been read
+    fused_dot_partials<NV>(dvs, me, reinterpret_cast<double *>(&s_acc[0][0]), s_red, fz.dot_part, ys, vec0);
   }
 }
 

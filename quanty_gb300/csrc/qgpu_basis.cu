@@ -33,12 +33,27 @@ __device__ __forceinline__ void qg_cas128(unsigned long long *addr, unsigned lon
 
 // Insert a key into the set; returns 1 if this call inserted it, 0 if it was present, -1 if the probe limit was hit.  The slot index
 // is stored to *slot_out.
+// Each probe reads the slot first (at L2, bypassing L1, which may hold an old copy) and takes
+// the atomic only where that read cannot settle it.  A slot changes once, from empty (both
+// words all ones) to a whole key, so a read with neither word all ones is that key even if the
+// two words were read apart; a read with an all-ones word (an empty slot, one being filled, or
+// a key whose low word is all ones) goes to the CAS, which returns the slot's true contents.
+// Most inserts of a closure find their key already present, so they cost loads, not atomics.
 template <int W>
 __device__ __forceinline__ int qg_set_insert(Slot *slots, uint64_t hmask, const Key<W> &k, int64_t *slot_out) {
   uint64_t h = qg_hash<W>(k) & hmask;
   uint64_t k1 = (W == 1) ? 0ull : k.w[W - 1];
   for (int p = 0; p < QG_PROBE_LIMIT; p++) {
     unsigned long long *a = reinterpret_cast<unsigned long long *>(slots + h);
+    ulonglong2 v = __ldcg(reinterpret_cast<const ulonglong2 *>(a));
+    if (v.x != QG_EMPTY_WORD && v.y != QG_EMPTY_WORD) {
+      if (v.x == k.w[0] && v.y == k1) {
+        *slot_out = (int64_t)h;
+        return 0;
+      }
+      h = (h + 1) & hmask;
+      continue;
+    }
     unsigned long long olo, ohi;
     qg_cas128(a, QG_EMPTY_WORD, QG_EMPTY_WORD, k.w[0], k1, olo, ohi);
     if (olo == QG_EMPTY_WORD && ohi == QG_EMPTY_WORD) {
@@ -424,70 +439,111 @@ extern "C" qg_status qg_basis_find(qg_basis b, int64_t n, const uint8_t *dets_ho
 
 // ------------------------------------------------------------------ growth
 
+// Insert the n keys of a warp's queue, 32 at a time (one per lane, independent probes);
+// true on every lane if any insert hit the probe limit or found the list full.
+template <int W>
+__device__ __forceinline__ bool expand_flush(const Key<W> *q, int n, int lane, Slot *slots, uint64_t hmask,
+                                             Key<W> *list, unsigned long long *count, unsigned long long limit,
+                                             unsigned int *err) {
+  bool bad = false;
+  for (int i = lane; i < n; i += 32) {
+    int64_t hs;
+    int ins = qg_set_insert<W>(slots, hmask, q[i], &hs);
+    if (ins < 0) {
+      atomicOr(err, QG_DEVERR_PROBE);
+      bad = true;
+      break;
+    }
+    if (ins == 1) {
+      unsigned long long pos = atomicAdd(count, 1ull);
+      if (pos >= limit) {
+        atomicOr(err, QG_DEVERR_TABLE_FULL);
+        bad = true;
+        break;
+      }
+      list[pos] = q[i];
+    }
+  }
+  return __any_sync(0xffffffffu, bad);
+}
+
+#define QG_XQ 128  // entries of a warp's insert queue
+
 // Expand the rows [r0, r1) of a key list through the forward (push) table: each applicable
 // term's target that passes the restrictions is inserted into the set; new keys are appended
-// to the list.  Lane per source determinant; groups are tested per lane.  In a closure
-// (skip_diag) the sources are members of the set already, so the terms that leave a
+// to the list.  Lane per source determinant; the warp walks the groups and terms together
+// (a group is skipped when no lane's source has its need1 bits) and queues the targets of all
+// 32 lanes in shared memory, compacted by ballot; a full queue is inserted 32 keys at a time,
+// one independent probe per lane, so inserts neither diverge nor wait on one another.  In a
+// closure (skip_diag) the sources are members of the set already, so the terms that leave a
 // determinant unchanged -- the densities and Coulomb direct terms, most of a Hamiltonian's
 // applicable terms -- are skipped, a whole group at a time where the group holds only those.
+// A round stops early once an insert has found the list full (the host grows the set and
+// repeats the round): a thread checks the error word when it starts and stops at its first
+// new key past the limit, so the set exceeds the list capacity by at most one key per
+// resident thread.
 template <int W>
-__global__ void k_expand(const Key<W> *src, int64_t r0, int64_t r1, const GroupDev<W> *__restrict__ groups, int ngroups,
-                         const TermDev<W> *__restrict__ terms, int nres, const uint64_t *__restrict__ rmask,
-                         const int32_t *__restrict__ rmin, const int32_t *__restrict__ rmax, Slot *slots,
-                         uint64_t hmask, Key<W> *list, unsigned long long *count, unsigned long long limit,
-                         unsigned int *err, int skip_diag) {
+__global__ void __launch_bounds__(256) k_expand(const Key<W> *src, int64_t r0, int64_t r1,
+                                                const GroupDev<W> *__restrict__ groups, int ngroups,
+                                                const TermDev<W> *__restrict__ terms, int nres,
+                                                const uint64_t *__restrict__ rmask, const int32_t *__restrict__ rmin,
+                                                const int32_t *__restrict__ rmax, Slot *slots, uint64_t hmask,
+                                                Key<W> *list, unsigned long long *count, unsigned long long limit,
+                                                unsigned int *err, int skip_diag) {
+  __shared__ Key<W> queue[8][QG_XQ];
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const unsigned below = (1u << lane) - 1u;
+  Key<W> *q = queue[wid];
   int64_t r = r0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (r >= r1) return;
-  Key<W> d = src[r];
-  for (int g = 0; g < ngroups; g++) {
-    GroupDev<W> G = groups[g];
+  bool live = r < r1 && !(*(volatile unsigned int *)err & (QG_DEVERR_TABLE_FULL | QG_DEVERR_PROBE));
+  Key<W> d;
+#pragma unroll
+  for (int i = 0; i < W; i++) d.w[i] = live ? src[r].w[i] : 0ull;
+  if (!__any_sync(0xffffffffu, live)) return;  // warp-uniform
+  int qn = 0;
+  bool halt = false;
+  for (int g = 0; g < ngroups && !halt; g++) {
+    const GroupDev<W> &G = groups[g];
     if (skip_diag && G.diag) continue;
-    bool ok = true;
+    bool ok = live;
 #pragma unroll
     for (int i = 0; i < W; i++) ok &= (d.w[i] & G.need1[i]) == G.need1[i];
-    if (!ok) continue;
-    for (int t = G.begin; t < G.end; t++) {
+    if (!__any_sync(0xffffffffu, ok)) continue;
+    const int tb = G.begin, te = G.end;
+    for (int t = tb; t < te; t++) {
       const TermDev<W> &T = terms[t];
-      bool app = true, moved = false;
+      bool has = ok, moved = false;
 #pragma unroll
       for (int i = 0; i < W; i++) {
-        app &= (d.w[i] & T.need0[i]) == 0;
+        has &= (d.w[i] & T.need0[i]) == 0;
         moved |= T.flip[i] != 0;
       }
       // a term whose value is zero (a sum operator's component scaled to 0) reaches nothing,
       // as in the reference, whose operators hold no zero terms
-      if (!app || (T.vre == 0.0 && T.vim == 0.0) || (skip_diag && !moved)) continue;
+      has &= !(T.vre == 0.0 && T.vim == 0.0) && !(skip_diag && !moved);
       Key<W> tg;
 #pragma unroll
       for (int i = 0; i < W; i++) tg.w[i] = d.w[i] ^ T.flip[i];
-      bool keep = true;
-      for (int q = 0; q < nres && keep; q++) {
-        int c = 0;
+      for (int c = 0; c < nres && has; c++) {
+        int n = 0;
 #pragma unroll
-        for (int i = 0; i < W; i++) c += __popcll(tg.w[i] & rmask[q * W + i]);
-        keep = (c >= rmin[q]) && (c <= rmax[q]);
+        for (int i = 0; i < W; i++) n += __popcll(tg.w[i] & rmask[c * W + i]);
+        has = (n >= rmin[c]) && (n <= rmax[c]);
       }
-      if (!keep) continue;
-      if (*(volatile unsigned long long *)count >= limit) {
-        atomicOr(err, QG_DEVERR_TABLE_FULL);
-        return;
-      }
-      int64_t hs;
-      int ins = qg_set_insert<W>(slots, hmask, tg, &hs);
-      if (ins < 0) {
-        atomicOr(err, QG_DEVERR_PROBE);
-        return;
-      }
-      if (ins == 1) {
-        unsigned long long pos = atomicAdd(count, 1ull);
-        if (pos < limit) {
-          list[pos] = tg;
-        } else {
-          atomicOr(err, QG_DEVERR_TABLE_FULL);
-        }
+      unsigned m = __ballot_sync(0xffffffffu, has);
+      if (has) q[qn + __popc(m & below)] = tg;
+      qn += __popc(m);
+      if (qn > QG_XQ - 32) {
+        __syncwarp();
+        halt = expand_flush<W>(q, qn, lane, slots, hmask, list, count, limit, err);
+        qn = 0;
+        __syncwarp();
+        if (halt) break;
       }
     }
   }
+  __syncwarp();
+  if (!halt && qn) expand_flush<W>(q, qn, lane, slots, hmask, list, count, limit, err);
 }
 
 template <int W>
@@ -565,8 +621,8 @@ static qg_status grow_t(qg_context ctx, qg_operator op, const Key<W> *seed_keys,
     QG_CUDA(ctx, cudaMemcpy(d_rmax, R.mx.data(), R.n * 4, cudaMemcpyHostToDevice));
   }
   // list capacity; the set has 2*cap slots.  An expansion stops inserting once the list is
-  // full, and the threads already past that check can overshoot by at most the number of
-  // resident threads (well under 2^20), so the set stays below 2/3 load.
+  // full; each thread resident at that moment can add at most one key past it (well under
+  // 2^20 in all), so the set stays below 2/3 load.
   int64_t cap = 1 << 20;
   while (cap < 4 * (n_seed + 1)) cap <<= 1;
   Key<W> *list = nullptr;

@@ -355,6 +355,8 @@ bool qg_apply_uses_lists(qg_operator op, qg_basis b);
 // overwritten) -> eigenvalues ascending (w_dev, k) and the lowest nv eigenvectors as the columns
 // of V_dev (k x nv row-major); the host-buffer form copies in and out.
 qg_status qg_eigh_device(qg_context ctx, int k, double2 *A, double *w_dev, double2 *V_dev, int nv);
+// the same for k > 1 by Householder reduction, bisection and inverse iteration (qgpu_hermitian.cu)
+qg_status qg_eigh_tridiag(qg_context ctx, int k, double2 *A, double *w_dev, double2 *V_dev, int nv);
 qg_status qg_eigh_host_io(qg_context ctx, int k, const double *a_host, double *w_host, double *v_host, int nv);
 int qg_partial_blocks(qg_context ctx, int64_t n);
 

@@ -1,14 +1,15 @@
-// Hermitian eigenproblems on the device: cyclic Jacobi with the round-robin (tournament)
-// ordering, so that every step rotates k/2 disjoint index pairs at once.
+// Hermitian eigenproblems on the device, the entry point for every dense eigenproblem of the
+// library: the projected Krylov matrix of the block eigensolver (the reference's LAPACK zheevd,
+// Core/BlockLanczos.cpp:5530), the dense H below DenseBorder (BlockLanczosGroundStateConserveBasisDense,
+// :370-501; HermitianCompactMatrixToListOfPoles, Core/BasicMath/BasicMath_CompactMatrixVector.cpp:3990)
+// and the resolvents of RIXS.
 //
-// The reference diagonalises its dense matrices with LAPACK zheevd: the projected Krylov matrix
-// of the block eigensolver (Core/BlockLanczos.cpp:5530), the dense H below DenseBorder
-// (BlockLanczosGroundStateConserveBasisDense, :370-501; HermitianCompactMatrixToListOfPoles,
-// Core/BasicMath/BasicMath_CompactMatrixVector.cpp:3990) and the resolvents of RIXS.  Jacobi is
-// chosen here because it maps onto many independent rotations (a whole row or column pair per
-// rotation, all pairs of a step in parallel), it resolves degenerate multiplets -- the rule in
-// atomic and impurity spectra -- without the reorthogonalisation inverse iteration would need,
-// and its eigenvalues carry relative accuracy near machine precision.
+// Matrices up to QG_JAC_SMALL run here, in one block with A and the rotations in shared memory,
+// by cyclic Jacobi with the round-robin (tournament) ordering, so that every step rotates k/2
+// disjoint index pairs at once; it resolves degenerate multiplets -- the rule in atomic and
+// impurity spectra -- without reorthogonalisation, and its eigenvalues carry relative accuracy
+// near machine precision.  Larger matrices go through the tridiagonal reduction
+// (qgpu_hermitian.cu), whose cost grows as k^3 once instead of k^3 per sweep.
 //
 // One rotation on the pair (p, q) of a Hermitian matrix with b = A[p][q] = |b| e^{i phi}:
 //   tau = (A[q][q] - A[p][p]) / (2 |b|),  t = sign(tau) / (|tau| + sqrt(1 + tau^2)),
@@ -16,10 +17,7 @@
 // and A <- J^H A J zeroes A[p][q] (the real symmetric rotation conjugated by diag(1, e^{-i phi})).
 // A step applies the row rotations of all its pairs (J^H from the left), then the column
 // rotations (J from the right) and accumulates V <- V J; the eigenvectors are kept as the rows
-// of Vt = V^T so that both updates read and write whole rows.
-//
-// Matrices up to QG_JAC_SMALL run in one block with A and Vt in shared memory; larger ones run
-// three launches per step (rotations, rows, columns), a sweep being k - 1 steps, until the
+// of Vt = V^T so that both updates read and write whole rows.  Sweeps run until the
 // off-diagonal norm falls below 1e-15 of the Frobenius norm (at most QG_JAC_SWEEPS sweeps).
 #include <algorithm>
 #include <cmath>
@@ -200,118 +198,6 @@ __global__ void __launch_bounds__(256) k_jacobi_small(const double2 *__restrict_
   if (threadIdx.x == 0) status[0] = done ? sweep : QG_JAC_SWEEPS + 1;
 }
 
-// ------------------------------------------------------------------ larger matrices: three launches per step
-
-__global__ void k_jac_rot(const double2 *__restrict__ A, int k, int kk, int s, JacRot *__restrict__ rot) {
-  const int m = blockIdx.x * blockDim.x + threadIdx.x;
-  if (m >= kk / 2) return;
-  int p, q;
-  jac_pair(kk, s, m, p, q);
-  rot[m] = q < k ? jac_rotation(A[(int64_t)p * k + p].x, A[(int64_t)q * k + q].x, A[(int64_t)p * k + q])
-                 : JacRot{1.0, 0.0, 1.0, 0.0, 1};
-}
-
-// rows p, q of A (J^H from the left) and of Vt: a block row per pair, threads over columns
-__global__ void k_jac_rows(double2 *__restrict__ A, double2 *__restrict__ Vt, int k, int kk, int s,
-                           const JacRot *__restrict__ rot) {
-  const int m = blockIdx.y;
-  const JacRot r = rot[m];
-  if (r.skip) return;
-  int p, q;
-  jac_pair(kk, s, m, p, q);
-  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < k; j += gridDim.x * blockDim.x) {
-    jac_left(r, A[(int64_t)p * k + j], A[(int64_t)q * k + j]);
-    jac_right(r, Vt[(int64_t)p * k + j], Vt[(int64_t)q * k + j]);
-  }
-}
-
-// columns p, q of A (J from the right); then the rotated pair's exact zeros and real diagonal
-__global__ void k_jac_cols(double2 *__restrict__ A, int k, int kk, int s, const JacRot *__restrict__ rot) {
-  const int m = blockIdx.y;
-  const JacRot r = rot[m];
-  if (r.skip) return;
-  int p, q;
-  jac_pair(kk, s, m, p, q);
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < k; i += gridDim.x * blockDim.x) {
-    if (i == p || i == q) continue;
-    jac_right(r, A[(int64_t)i * k + p], A[(int64_t)i * k + q]);
-  }
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    // the 2 x 2 block: its rows were rotated, the columns finish it; exact zeros off the diagonal
-    double2 pp = A[(int64_t)p * k + p], pq = A[(int64_t)p * k + q];
-    double2 qp = A[(int64_t)q * k + p], qq = A[(int64_t)q * k + q];
-    jac_right(r, pp, pq);
-    jac_right(r, qp, qq);
-    A[(int64_t)p * k + p] = make_double2(pp.x, 0.0);
-    A[(int64_t)q * k + q] = make_double2(qq.x, 0.0);
-    A[(int64_t)p * k + q] = make_double2(0.0, 0.0);
-    A[(int64_t)q * k + p] = make_double2(0.0, 0.0);
-  }
-}
-
-// out[0] = off-diagonal squared norm, out[1] = total (one block, fixed order)
-__global__ void __launch_bounds__(1024) k_jac_norms(const double2 *__restrict__ A, int k, double *__restrict__ out) {
-  __shared__ double red[2][32];
-  double off = 0.0, tot = 0.0;
-  for (int64_t t = threadIdx.x; t < (int64_t)k * k; t += blockDim.x) {
-    const double2 a = A[t];
-    const double m = a.x * a.x + a.y * a.y;
-    tot += m;
-    if (t / k != t % k) off += m;
-  }
-  for (int o = 16; o; o >>= 1) {
-    off += __shfl_xor_sync(0xffffffffu, off, o);
-    tot += __shfl_xor_sync(0xffffffffu, tot, o);
-  }
-  if ((threadIdx.x & 31) == 0) {
-    red[0][threadIdx.x >> 5] = off;
-    red[1][threadIdx.x >> 5] = tot;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double o2 = 0.0, t2 = 0.0;
-    for (int i = 0; i < (int)(blockDim.x >> 5); i++) {
-      o2 += red[0][i];
-      t2 += red[1][i];
-    }
-    out[0] = o2;
-    out[1] = t2;
-  }
-}
-
-__global__ void k_jac_diag(const double2 *__restrict__ A, int k, double *__restrict__ d) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < k) d[i] = A[(int64_t)i * k + i].x;
-}
-
-// ascending ranks of the diagonal (ties by index), then w and the lowest nv eigenvectors
-__global__ void k_jac_order(const double *__restrict__ d, const double2 *__restrict__ Vt, int k, int nv,
-                            double *__restrict__ w, double2 *__restrict__ V) {
-  const int i = blockIdx.x;
-  const double di = d[i];
-  __shared__ int rank_s;
-  if (threadIdx.x == 0) rank_s = 0;
-  __syncthreads();
-  int rank = 0;
-  for (int j = threadIdx.x; j < k; j += blockDim.x) {
-    const double dj = d[j];
-    rank += (dj < di) || (dj == di && j < i);
-  }
-  for (int o = 16; o; o >>= 1) rank += __shfl_xor_sync(0xffffffffu, rank, o);
-  if ((threadIdx.x & 31) == 0) atomicAdd(&rank_s, rank);  // integer: exact in any order
-  __syncthreads();
-  rank = rank_s;
-  if (threadIdx.x == 0) w[rank] = di;
-  if (rank < nv)
-    for (int r = threadIdx.x; r < k; r += blockDim.x) V[(int64_t)r * nv + rank] = Vt[(int64_t)i * k + r];
-}
-
-__global__ void k_jac_identity(double2 *__restrict__ Vt, int k) {
-  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (t >= (int64_t)k * k) return;
-  Vt[t] = make_double2(t / k == t % k ? 1.0 : 0.0, 0.0);
-}
-
 // Eigenpairs of the Hermitian k x k matrix A (device, row-major; overwritten): eigenvalues
 // ascending into w_dev (k), the eigenvectors of the lowest nv into V_dev (k x nv row-major,
 // columns).  Only the Hermitian part of A is meaningful: entries are used as given.
@@ -341,57 +227,7 @@ qg_status qg_eigh_device(qg_context ctx, int k, double2 *A, double *w_dev, doubl
       if (e != cudaSuccess) st = qg_cuda_fail(ctx, e, "qg_eigh_device");
     }
   } else {
-    const int kk = k + (k & 1);
-    double2 *Vt = nullptr;
-    JacRot *rot = nullptr;
-    double *norms = nullptr, *d = nullptr;
-    cudaError_t e = cudaMalloc(&Vt, (size_t)k * k * sizeof(double2));
-    if (e == cudaSuccess) e = cudaMalloc(&rot, (size_t)(kk / 2) * sizeof(JacRot));
-    if (e == cudaSuccess) e = cudaMalloc(&norms, 2 * sizeof(double));
-    if (e == cudaSuccess) e = cudaMalloc(&d, (size_t)k * sizeof(double));
-    if (e != cudaSuccess) st = qg_cuda_fail(ctx, e, "qg_eigh_device");
-    if (st == QG_OK) {
-      k_jac_identity<<<(unsigned)(((int64_t)k * k + 255) / 256), 256, 0, s>>>(Vt, k);
-      ctx->launches++;
-    }
-    const unsigned gx = (unsigned)std::max(1, std::min((k + 255) / 256, 4));
-    double hn[2] = {0.0, 0.0};
-    for (sweeps = 0; st == QG_OK; sweeps++) {
-      k_jac_norms<<<1, 1024, 0, s>>>(A, k, norms);
-      ctx->launches++;
-      e = cudaMemcpyAsync(hn, norms, sizeof(hn), cudaMemcpyDeviceToHost, s);
-      if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-      if (e != cudaSuccess) {
-        st = qg_cuda_fail(ctx, e, "qg_eigh_device");
-        break;
-      }
-      if (!(hn[0] > QG_JAC_TOL2 * hn[1])) break;
-      if (sweeps == QG_JAC_SWEEPS) {
-        sweeps = QG_JAC_SWEEPS + 1;
-        break;
-      }
-      for (int step = 0; step < kk - 1; step++) {
-        k_jac_rot<<<(unsigned)((kk / 2 + 127) / 128), 128, 0, s>>>(A, k, kk, step, rot);
-        k_jac_rows<<<dim3(gx, (unsigned)(kk / 2)), 256, 0, s>>>(A, Vt, k, kk, step, rot);
-        k_jac_cols<<<dim3(gx, (unsigned)(kk / 2)), 256, 0, s>>>(A, k, kk, step, rot);
-        ctx->launches += 3;
-      }
-      st = qg_check_launch(ctx, "qg_eigh_device");
-    }
-    if (st == QG_OK) {
-      k_jac_diag<<<(unsigned)((k + 255) / 256), 256, 0, s>>>(A, k, d);
-      k_jac_order<<<(unsigned)k, 256, 0, s>>>(d, Vt, k, nv, w_dev, V_dev);
-      ctx->launches += 2;
-      st = qg_check_launch(ctx, "qg_eigh_device");
-    }
-    if (st == QG_OK) {
-      e = cudaStreamSynchronize(s);
-      if (e != cudaSuccess) st = qg_cuda_fail(ctx, e, "qg_eigh_device");
-    }
-    cudaFree(Vt);
-    cudaFree(rot);
-    cudaFree(norms);
-    cudaFree(d);
+    st = qg_eigh_tridiag(ctx, k, A, w_dev, V_dev, nv);
   }
   cudaFree(d_status);
   if (st == QG_OK && sweeps > QG_JAC_SWEEPS) {

@@ -224,9 +224,10 @@ extern "C" qg_status qg_expectation(qg_context ctx, qg_operator op, qg_basis b, 
 
 // v = w - a_k v_prev (a from the previous dot), norm partials of v
 __global__ void k_lanczos_axpy_norm(int64_t n, int nvec, const double2 *__restrict__ w, const double2 *__restrict__ vp,
-                                    const double *__restrict__ a, double2 *__restrict__ v, double2 *part) {
+                                    const double *__restrict__ a, double2 *__restrict__ v, double2 *part, int *step) {
   extern __shared__ double2 sh[];
   int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if (blockIdx.x == 0 && threadIdx.x == 0) *step += 1;  // the step this kernel opens
   for (int k = 0; k < nvec; k++) {
     double ak = a[k];
     double s = 0.0;
@@ -251,9 +252,10 @@ __global__ void k_lanczos_axpy_norm(int64_t n, int nvec, const double2 *__restri
 // the same for several vectors, in the flat layout of k_dot_partial_flat
 __global__ void k_lanczos_axpy_norm_flat(int64_t len, int nvec, const double2 *__restrict__ w,
                                          const double2 *__restrict__ vp, const double *__restrict__ a,
-                                         double2 *__restrict__ v, double2 *part) {
+                                         double2 *__restrict__ v, double2 *part, int *step) {
   extern __shared__ double2 sh[];
   int tid = threadIdx.x, T = blockDim.x;
+  if (blockIdx.x == 0 && tid == 0) *step += 1;  // the step this kernel opens
   double ak = a[tid % nvec];
   double s = 0.0;
   for (int64_t i = blockIdx.x * (int64_t)T + tid; i < len; i += (int64_t)gridDim.x * T) {
@@ -271,71 +273,60 @@ __global__ void k_lanczos_axpy_norm_flat(int64_t len, int nvec, const double2 *_
   }
 }
 
-// Sum of the .x parts of vector k's partials, in a fixed order: with at least as many vectors
-// as warps, or few partials, a warp per vector (lanes over the partials, a shuffle tree);
-// otherwise (few vectors over many partials) the whole block per vector (threads over the
-// partials, shuffles, then the warps' sums in order).  Returns the sum on lane 0 (warp form)
-// or thread 0 (block form).
-__device__ __forceinline__ bool fin_warp_form(int nvec, int nblk) {
-  return nvec >= (int)(blockDim.x >> 5) || nblk <= 2048;
-}
-
-__device__ double fin_sum_block(const double2 *part, int nblk, int nvec, int k, double *sh) {
-  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  double s = 0;
-  for (int b = threadIdx.x; b < nblk; b += blockDim.x) s += part[b * nvec + k].x;
+// Sum of the .x parts of vector k's partials in a fixed order, by one block: threads over the
+// partials with four independent accumulators (so a thread's loads overlap instead of waiting
+// on one another), a shuffle tree, then the warps' sums in order.  The total on thread 0.
+__device__ double fin_sum(const double2 *__restrict__ part, int nblk, int nvec, int k, double *sh) {
+  const int T = blockDim.x, lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  double s0 = 0, s1 = 0, s2 = 0, s3 = 0;
+  int b = threadIdx.x;
+  for (; b + 3 * T < nblk; b += 4 * T) {
+    s0 += part[(int64_t)b * nvec + k].x;
+    s1 += part[(int64_t)(b + T) * nvec + k].x;
+    s2 += part[(int64_t)(b + 2 * T) * nvec + k].x;
+    s3 += part[(int64_t)(b + 3 * T) * nvec + k].x;
+  }
+  for (; b < nblk; b += T) s0 += part[(int64_t)b * nvec + k].x;
+  double s = (s0 + s1) + (s2 + s3);
   for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
   if (lane == 0) sh[wid] = s;
   __syncthreads();
   double t = 0;
   if (threadIdx.x == 0)
     for (int w = 0; w < nw; w++) t += sh[w];
-  __syncthreads();
   return t;
 }
 
-__device__ __forceinline__ double fin_sum_warp(const double2 *part, int nblk, int nvec, int k) {
-  int lane = threadIdx.x & 31;
-  double s = 0;
-  for (int b = lane; b < nblk; b += 32) s += part[b * nvec + k].x;
-  for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-  return s;
-}
+#define QG_FIN_THREADS 512
 
-// a[k] <- Re(sum of dot partials); also stores a into the history at column *step + 1 and
-// then advances the device step counter (so a captured step can be replayed)
-__global__ void k_fin_a(const double2 *part, int nblk, int nvec, double *a_now, double *a_hist, int stride,
-                        int *step) {
+// a[k] <- Re(sum of dot partials), one block per vector; also stores a into the history at
+// column *step + 1.  The step counter is advanced by the next step's first kernel
+// (k_lanczos_axpy_norm*), after every block here has read it, so a captured step can be
+// replayed.
+__global__ void __launch_bounds__(QG_FIN_THREADS) k_fin_a(const double2 *part, int nblk, int nvec, double *a_now,
+                                                          double *a_hist, int stride, const int *step) {
   __shared__ double sh[32];
+  const int k = blockIdx.x;
   const int col = *step + 1;
-  auto store = [&](int k, double t) {
+  double t = fin_sum(part, nblk, nvec, k, sh);
+  if (threadIdx.x == 0) {
     a_now[k] = t;
     a_hist[k * stride + col] = t;
-  };
-  if (fin_warp_form(nvec, nblk)) {
-    for (int k = threadIdx.x >> 5; k < nvec; k += blockDim.x >> 5) {
-      double t = fin_sum_warp(part, nblk, nvec, k);
-      if ((threadIdx.x & 31) == 0) store(k, t);
-    }
-  } else {
-    for (int k = 0; k < nvec; k++) {
-      double t = fin_sum_block(part, nblk, nvec, k, sh);
-      if (threadIdx.x == 0) store(k, t);
-    }
   }
-  __syncthreads();  // every thread has read the counter
-  if (threadIdx.x == 0) *step = col;
 }
 
-// b = sqrt(sum of norm partials) into the history at column *step; scale = 1/b (0 for an empty
-// vector); truncation threshold (eps/err)^2 with the err before this step's update;
-// err *= b^2/(b^2+4 gamma^2)
-__global__ void k_fin_b(const double2 *part, int nblk, int nvec, double *b_now, double *b_hist, int stride,
-                        const int *step, double *scale, double *thr2, double *err, double eps, double gamma,
-                        int first) {
+// b = sqrt(sum of norm partials) into the history at column *step, one block per vector;
+// scale = 1/b (0 for an empty vector); truncation threshold (eps/err)^2 with the err before
+// this step's update; err *= b^2/(b^2+4 gamma^2)
+__global__ void __launch_bounds__(QG_FIN_THREADS) k_fin_b(const double2 *part, int nblk, int nvec, double *b_now,
+                                                          double *b_hist, int stride, const int *step, double *scale,
+                                                          double *thr2, double *err, double eps, double gamma,
+                                                          int first) {
   __shared__ double sh[32];
+  const int k = blockIdx.x;
   const int col = *step;
-  auto store = [&](int k, double t) {
+  double t = fin_sum(part, nblk, nvec, k, sh);
+  if (threadIdx.x == 0) {
     double b = sqrt(t);
     b_now[k] = b;
     b_hist[k * stride + col] = b;
@@ -345,17 +336,6 @@ __global__ void k_fin_b(const double2 *part, int nblk, int nvec, double *b_now, 
     thr2[k] = th * th;
     if (!first) err[k] = e * (b * b / (b * b + 4 * gamma * gamma));
     else err[k] = 1.0;
-  };
-  if (fin_warp_form(nvec, nblk)) {
-    for (int k = threadIdx.x >> 5; k < nvec; k += blockDim.x >> 5) {
-      double t = fin_sum_warp(part, nblk, nvec, k);
-      if ((threadIdx.x & 31) == 0) store(k, t);
-    }
-  } else {
-    for (int k = 0; k < nvec; k++) {
-      double t = fin_sum_block(part, nblk, nvec, k, sh);
-      if (threadIdx.x == 0) store(k, t);
-    }
   }
 }
 
@@ -455,7 +435,8 @@ extern "C" qg_status qg_lanczos_tridiag(qg_context ctx, qg_operator op, qg_basis
   };
   // step 0: b0 = |v0|, scale, threshold eps (err = 1)
   launch_dot_partial(P, n, nvec, (const double2 *)v0_dev, nullptr, npart, s);
-  k_fin_b<<<1, 256, 0, s>>>(npart, P, nvec, b_now, b_hist, ntri, step_ctr, scale, thr2, err, eps, gamma, 1);
+  k_fin_b<<<nvec, QG_FIN_THREADS, 0, s>>>(npart, P, nvec, b_now, b_hist, ntri, step_ctr, scale, thr2, err, eps, gamma,
+                                         1);
   ctx->launches += 2;
   st = qg_check_launch(ctx, "lanczos start norm");
   ApplyFuse fz;
@@ -468,7 +449,7 @@ extern "C" qg_status qg_lanczos_tridiag(qg_context ctx, qg_operator op, qg_basis
   if (st == QG_OK && krylov_dev)
     e = cudaMemcpyAsync(krylov_dev, vc, len * 16, cudaMemcpyDeviceToDevice, s);
   if (st == QG_OK) {
-    k_fin_a<<<1, 256, 0, s>>>(dpart, Papply, nvec, a_now, a_hist, ntri + 1, step_ctr);
+    k_fin_a<<<nvec, QG_FIN_THREADS, 0, s>>>(dpart, Papply, nvec, a_now, a_hist, ntri + 1, step_ctr);
     ctx->launches++;
   }
   // one step: every scalar stays on the device
@@ -476,10 +457,11 @@ extern "C" qg_status qg_lanczos_tridiag(qg_context ctx, qg_operator op, qg_basis
     std::swap(vp, vc);  // vp = v_{i-1}
     int T = nvec > 1 ? flat_threads(nvec) : 0;
     if (T)
-      k_lanczos_axpy_norm_flat<<<P, T, T * sizeof(double2), s>>>(len, nvec, w, vp, a_now, vraw, npart);
+      k_lanczos_axpy_norm_flat<<<P, T, T * sizeof(double2), s>>>(len, nvec, w, vp, a_now, vraw, npart, step_ctr);
     else
-      k_lanczos_axpy_norm<<<P, RBLK, (RBLK / 32) * sizeof(double2), s>>>(n, nvec, w, vp, a_now, vraw, npart);
-    k_fin_b<<<1, 256, 0, s>>>(npart, P, nvec, b_now, b_hist, ntri, step_ctr, scale, thr2, err, eps, gamma, 0);
+      k_lanczos_axpy_norm<<<P, RBLK, (RBLK / 32) * sizeof(double2), s>>>(n, nvec, w, vp, a_now, vraw, npart, step_ctr);
+    k_fin_b<<<nvec, QG_FIN_THREADS, 0, s>>>(npart, P, nvec, b_now, b_hist, ntri, step_ctr, scale, thr2, err, eps,
+                                           gamma, 0);
     ctx->launches += 2;
     qg_status sst = normalise(vraw);
     if (sst != QG_OK) return sst;
@@ -491,7 +473,7 @@ extern "C" qg_status qg_lanczos_tridiag(qg_context ctx, qg_operator op, qg_basis
       cudaError_t ce = cudaMemcpyAsync(krylov_dev + 2 * (size_t)i * len, vc, len * 16, cudaMemcpyDeviceToDevice, s);
       if (ce != cudaSuccess) return qg_cuda_fail(ctx, ce, "krylov copy");
     }
-    k_fin_a<<<1, 256, 0, s>>>(dpart, Papply, nvec, a_now, a_hist, ntri + 1, step_ctr);
+    k_fin_a<<<nvec, QG_FIN_THREADS, 0, s>>>(dpart, Papply, nvec, a_now, a_hist, ntri + 1, step_ctr);
     ctx->launches++;
     return sst;
   };
