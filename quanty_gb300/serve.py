@@ -108,6 +108,11 @@ class Server:
         self.cv = threading.Condition()
         self.closed = False
         prev = torch.cuda.current_stream(device)
+        # device clock origin: every job's start and end are also recorded as CUDA events on its
+        # slot's stream and measured from this event, so overlap is checked on the device
+        self.t_ref = torch.cuda.Event(enable_timing=True)
+        self.t_ref.record(prev)
+        self.t_ref.synchronize()
         self.engines = [api.Engine(device) for _ in range(slots)]
         torch.cuda.set_stream(prev)  # the engines' streams are used only by their workers
         self.records = []
@@ -155,10 +160,18 @@ class Server:
                 if rec is None:
                     return
             rec["start"] = time.perf_counter()
+            ev0 = self.torch.cuda.Event(enable_timing=True)
+            ev1 = self.torch.cuda.Event(enable_timing=True)
+            ev0.record(eng.stream)
             try:
                 out = rec["job"].run(eng)
-                self.torch.cuda.current_stream().synchronize()
+                ev1.record(eng.stream)
+                ev1.synchronize()
                 rec["end"] = time.perf_counter()
+                # the job's window on the device: its stream reached the first event before its
+                # first kernel and the second after its last
+                rec["dev_start"] = self.t_ref.elapsed_time(ev0) * 1e-3
+                rec["dev_end"] = self.t_ref.elapsed_time(ev1) * 1e-3
                 rec["future"].set_result(out)
             except Exception as exc:  # reported through the future
                 rec["end"] = time.perf_counter()

@@ -1,5 +1,6 @@
 """Serving form on the GPU: jobs arriving while others run overlap on the device (one context
-and stream per slot), and every job's result equals its result alone."""
+and stream per slot; checked with CUDA events on the slots' streams), and every job's result
+equals its result alone."""
 import numpy as np
 import pytest
 
@@ -62,10 +63,12 @@ def test_jobs_overlap_when_admitted_together(mods):
     srv = serve.Server(slots=3)
     futs = [srv.submit(j) for j in jobs]
     [f.result() for f in futs]
-    recs = sorted(srv.records, key=lambda r: r["start"])
+    recs = sorted(srv.records, key=lambda r: r["dev_start"])
     srv.close()
-    # the second job started before the first finished: their device work overlapped
-    assert recs[1]["start"] < recs[0]["end"]
+    # on the device clock (CUDA events on each slot's stream): the second job's stream began
+    # its work before the first job's last kernel finished
+    assert recs[1]["dev_start"] < recs[0]["dev_end"]
+    assert all(r["dev_end"] > r["dev_start"] >= 0.0 for r in recs)
 
 
 def test_budget_serialises_jobs(mods):
