@@ -269,6 +269,12 @@ qg_status qg_lanczos_tridiag(qg_context ctx, qg_operator op, qg_basis basis, con
                              int32_t nvec, int32_t ntri, double eps, double gamma, double *a_host,
                              double *b_host, double *krylov_dev);
 
+/* Bases of at most 2048 determinants whose rows hold at most 32768 terms run
+ * qg_lanczos_tridiag as one persistent kernel, one block per vector with the whole recursion
+ * on chip; each vector's coefficients are bitwise those of the general path run with that
+ * vector alone.  on = 0 keeps every call on the general path (default 1). */
+qg_status qg_set_small_basis_lanczos(qg_context ctx, int32_t on);
+
 /* Continued fraction G_s(w_k) = a0 + b0^2/(w - a1 + i g/2 - b1^2/(...)) for nspec spectra
  * and w_k = emin + k*de + e0[s], k = 0..ne, in one kernel (TriDiagonalMatrixToSpectrum,
  * Core/Spectral.cpp:1433).  Spectrum s uses a[s*(ntri+1) ..], b[s*ntri ..]; host in; g_host

@@ -27,6 +27,7 @@
 #include <cstring>
 #include <map>
 #include <tuple>
+#include <vector>
 
 #include "qgpu_internal.cuh"
 
@@ -167,21 +168,6 @@ __device__ __forceinline__ uint64_t window_bits(const Key<W> &d, const SrcView &
 // is an integer flip of the sign bits, and a term with a real value (every hopping, Coulomb
 // and one-body real term) costs two FMAs per vector instead of four.  A zero imaginary part
 // contributes fma(-0, x, acc) == acc exactly, so both forms give the same bits.
-__device__ __forceinline__ double qg_flip_sign(double v, int par) {
-  return __longlong_as_double(__double_as_longlong(v) ^ ((long long)(par & 1) << 63));
-}
-
-__device__ __forceinline__ bool qg_is_nonzero(double v) { return (__double_as_longlong(v) << 1) != 0; }
-
-// acc += (vr + i vi) xv, in the operation order of the complex form
-__device__ __forceinline__ void qg_cmac(double2 &acc, double vr, double vi, bool cplx, double2 xv) {
-  if (cplx) {
-    acc.x = fma(-vi, xv.y, acc.x);
-    acc.y = fma(vi, xv.x, acc.y);
-  }
-  acc.x = fma(vr, xv.x, acc.x);
-  acc.y = fma(vr, xv.y, acc.y);
-}
 
 // The fused Lanczos epilogue's per-block partial of a = Re <x|H x> for each of NV vectors (the
 // Lanczos diagonal is real).  The apply kernels are bound by the FP64 pipe, so the reduction
@@ -237,22 +223,10 @@ __global__ void __launch_bounds__(256, NV == 1 ? QG_APPLY_MIN_BLOCKS : 1) k_appl
   if (live) {
     Key<W> d = rows[r];
     if (diag) {
-      double2 dg = diag[r];
-      if (qg_is_nonzero(dg.y)) {
+      const double2 dg = diag[r];
+      const bool dgc = qg_is_nonzero(dg.y);  // Hermitian operators: real diagonal
 #pragma unroll
-        for (int k = 0; k < NV; k++) {
-          double2 xv = x[r * xs + vec0 + k];
-          acc[k].x = dg.x * xv.x - dg.y * xv.y;
-          acc[k].y = dg.x * xv.y + dg.y * xv.x;
-        }
-      } else {  // Hermitian operators: real diagonal
-#pragma unroll
-        for (int k = 0; k < NV; k++) {
-          double2 xv = x[r * xs + vec0 + k];
-          acc[k].x = dg.x * xv.x;
-          acc[k].y = dg.x * xv.y;
-        }
-      }
+      for (int k = 0; k < NV; k++) acc[k] = qg_diag_mul(dg, x[r * xs + vec0 + k], dgc);
     }
     uint64_t okm = 0;
     if (wreq && src.nres) okm = window_bits<W>(d, src);
@@ -392,11 +366,8 @@ __global__ void __launch_bounds__(256, NV == 1 ? QG_APPLY_MIN_BLOCKS : 1) k_appl
     for (int k = 0; k < NV; k++) {
       double dv = 0.0;
       if (live) {
-        double2 xv = x[r * xs + vec0 + k];
-        dv = xv.x * acc[k].x + xv.y * acc[k].y;
-        double2 pv = fz.prev[r * ys + vec0 + k];
-        double be = fz.beta[vec0 + k];
-        y[r * ys + vec0 + k] = make_double2(acc[k].x - be * pv.x, acc[k].y - be * pv.y);
+        dv = qg_redot(x[r * xs + vec0 + k], acc[k]);
+        y[r * ys + vec0 + k] = qg_axpy2(acc[k], fz.beta[vec0 + k], fz.prev[r * ys + vec0 + k]);
       }
       dvs[k] = dv;
     }
@@ -454,16 +425,7 @@ __global__ void __launch_bounds__(256) k_apply_warp(const Key<W> *__restrict__ r
     for (int m = 0; m < VPL; m++) {
       int k = lane + 32 * m;
       acc[m] = make_double2(0.0, 0.0);
-      if (diag && k < nv) {
-        double2 xv = x[r * xs + vec0 + k];
-        if (dgc) {
-          acc[m].x = dg.x * xv.x - dg.y * xv.y;
-          acc[m].y = dg.x * xv.y + dg.y * xv.x;
-        } else {
-          acc[m].x = dg.x * xv.x;
-          acc[m].y = dg.x * xv.y;
-        }
-      }
+      if (diag && k < nv) acc[m] = qg_diag_mul(dg, x[r * xs + vec0 + k], dgc);
     }
     int cnt = 0;
     auto flush = [&]() {
@@ -609,12 +571,8 @@ __global__ void __launch_bounds__(256) k_apply_warp(const Key<W> *__restrict__ r
       if (!FUSE) {
         y[r * ys + vec0 + k] = acc[m];
       } else {
-        double2 xv = x[r * xs + vec0 + k];
-        dsum[m].x += xv.x * acc[m].x + xv.y * acc[m].y;
-        dsum[m].y += xv.x * acc[m].y - xv.y * acc[m].x;
-        double2 pv = fz.prev[r * ys + vec0 + k];
-        double be = fz.beta[vec0 + k];
-        y[r * ys + vec0 + k] = make_double2(acc[m].x - be * pv.x, acc[m].y - be * pv.y);
+        dsum[m].x += qg_redot(x[r * xs + vec0 + k], acc[m]);
+        y[r * ys + vec0 + k] = qg_axpy2(acc[m], fz.beta[vec0 + k], fz.prev[r * ys + vec0 + k]);
       }
     }
   }
@@ -624,12 +582,9 @@ __global__ void __launch_bounds__(256) k_apply_warp(const Key<W> *__restrict__ r
     for (int m = 0; m < VPL; m++) red[wid][lane + 32 * m] = dsum[m];
     __syncthreads();
     for (int k = threadIdx.x; k < nv && k < 32 * VPL; k += blockDim.x) {
-      double2 sacc = make_double2(0.0, 0.0);
-      for (int w = 0; w < 8; w++) {
-        sacc.x += red[w][k].x;
-        sacc.y += red[w][k].y;
-      }
-      fz.dot_part[blockIdx.x * ys + vec0 + k] = sacc;
+      double sacc = 0.0;
+      for (int w = 0; w < 8; w++) sacc += red[w][k].x;
+      fz.dot_part[blockIdx.x * ys + vec0 + k] = make_double2(sacc, 0.0);
     }
   }
   if (SMEM && pending) mbar_wait_bounded(smem_addr(&s_bar), 0);
@@ -814,22 +769,10 @@ __global__ void __launch_bounds__(256, NV == 1 ? QG_APPLY_MIN_BLOCKS : 1)
   int64_t p = 0, pe = 0;
   if (live) {
     if (diag) {
-      double2 dg = diag[r];
-      if (!REAL && qg_is_nonzero(dg.y)) {
+      const double2 dg = diag[r];
+      const bool dgc = !REAL && qg_is_nonzero(dg.y);
 #pragma unroll
-        for (int k = 0; k < NV; k++) {
-          double2 xv = x[r * xs + vec0 + k];
-          acc[k].x = dg.x * xv.x - dg.y * xv.y;
-          acc[k].y = dg.x * xv.y + dg.y * xv.x;
-        }
-      } else {
-#pragma unroll
-        for (int k = 0; k < NV; k++) {
-          double2 xv = x[r * xs + vec0 + k];
-          acc[k].x = dg.x * xv.x;
-          acc[k].y = dg.x * xv.y;
-        }
-      }
+      for (int k = 0; k < NV; k++) acc[k] = qg_diag_mul(dg, x[r * xs + vec0 + k], dgc);
     }
     p = __ldg(cptr + r);
     pe = __ldg(cptr + r + 1);
@@ -939,11 +882,8 @@ __global__ void __launch_bounds__(256, NV == 1 ? QG_APPLY_MIN_BLOCKS : 1)
     for (int k = 0; k < NV; k++) {
       double dv = 0.0;
       if (live) {
-        double2 xv = x[r * xs + vec0 + k];
-        dv = xv.x * acc[k].x + xv.y * acc[k].y;
-        double2 pv = fz.prev[r * ys + vec0 + k];
-        double be = fz.beta[vec0 + k];
-        y[r * ys + vec0 + k] = make_double2(acc[k].x - be * pv.x, acc[k].y - be * pv.y);
+        dv = qg_redot(x[r * xs + vec0 + k], acc[k]);
+        y[r * ys + vec0 + k] = qg_axpy2(acc[k], fz.beta[vec0 + k], fz.prev[r * ys + vec0 + k]);
       }
       dvs[k] = dv;
     }
@@ -1088,7 +1028,7 @@ __global__ void k_pack(const Key<W> *__restrict__ keys, const uint32_t *__restri
     double sc = *scale, t2 = *thr2;
     v.x *= sc;
     v.y *= sc;
-    if (!(v.x * v.x + v.y * v.y > t2)) v = make_double2(0.0, 0.0);  // the reference keeps |a|^2 > eps^2
+    if (!(qg_norm2(v) > t2)) v = make_double2(0.0, 0.0);  // the reference keeps |a|^2 > eps^2
   }
   if (own_out) own_out[r * xs] = v;
   Key<W> k = keys[r];
@@ -1784,6 +1724,161 @@ static void launch_apply_list(qg_context ctx, const OpBasisCache *c, const doubl
       launch_apply_list_t<W, 1, FUSE>(ctx, c, diag, dst, x, xs, y, ys, v, np, fz, lv, real);
     v += per * np;
   }
+}
+
+// ------------------------------------------------------------------ small bases as explicit rows
+
+static bool op_values_real(qg_operator op);
+
+// The rows of the same-basis list apply (k_apply_list) as CSR: per row the diagonal, every local
+// move (certain offset or listed source) and every listed connection, in that kernel's order,
+// each with its source row and the value and form (kind) it multiplies with.  Count pass
+// (FILL false: cnt[r]) and fill pass (FILL true, rowptr given).
+template <int W, bool FILL, bool REAL>
+__global__ void k_small_csr(const Key<W> *__restrict__ rows, int64_t n, const int64_t *__restrict__ cptr,
+                            const uint2 *__restrict__ conn, const double2 *__restrict__ coef,
+                            const double2 *__restrict__ diag, LocalView lv, int *__restrict__ cnt,
+                            const int *__restrict__ rowptr, int *__restrict__ col, double2 *__restrict__ val,
+                            unsigned char *__restrict__ kind) {
+  const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  int c = 0;
+  int64_t o = FILL ? rowptr[r] : 0;
+  auto emit = [&](int64_t j, double2 v, unsigned char kd) {
+    if (FILL) {
+      col[o] = (int)j;
+      val[o] = v;
+      kind[o] = kd;
+      o++;
+    }
+    c++;
+  };
+  if (diag) {
+    const double2 dg = diag[r];
+    emit(r, dg, (!REAL && qg_is_nonzero(dg.y)) ? 1 : 0);
+  }
+  int64_t p = cptr[r];
+  const int64_t pe = cptr[r + 1];
+  if (lv.on) {
+    const Key<W> d = rows[r];
+    const int b = lv.cfg[get_local<W>(d, lv.lo, lv.lmask)];
+    const int64_t off = r - (int64_t)lv.bstart[b];
+    const uint32_t e1 = lv.eoff[b + 1];
+    for (uint32_t e = lv.eoff[b]; e < e1; e++) {
+      const LocalEntry *E = lv.ent + e;
+      int64_t j;
+      if (E->tend >> 31) {
+        j = (int64_t)E->tstart + off;
+      } else {
+        const uint32_t js = p < pe ? conn[p].x : QG_NO_INDEX;
+        p++;
+        if (js == QG_NO_INDEX) continue;
+        j = js;
+      }
+      if (REAL)
+        emit(j, make_double2(E->vre, 0.0), 2);
+      else
+        emit(j, make_double2(E->vre, E->vim), qg_is_nonzero(E->vim) ? 3 : 2);
+    }
+  }
+  for (; p < pe; p++) {
+    const uint2 cn = conn[p];
+    const int par = (int)(cn.y >> 31);
+    const double2 cf = coef[cn.y & 0x7FFFFFFFu];
+    if (REAL)
+      emit(cn.x, make_double2(qg_flip_sign(cf.x, par), 0.0), 2);
+    else
+      emit(cn.x, make_double2(qg_flip_sign(cf.x, par), qg_flip_sign(cf.y, par)), qg_is_nonzero(cf.y) ? 3 : 2);
+  }
+  if (!FILL) cnt[r] = c;
+}
+
+template <int W, bool FILL>
+static void launch_small_csr(qg_context ctx, qg_basis b, const OpBasisCache *c, const LocalView &lv, bool real,
+                             int *cnt, const int *rowptr, int *col, double2 *val, unsigned char *kind) {
+  const Key<W> *keys = (const Key<W> *)b->d_keys;
+  const unsigned g = (unsigned)((b->n + 255) / 256);
+  if (real)
+    k_small_csr<W, FILL, true><<<g, 256, 0, ctx->stream>>>(keys, b->n, c->d_cptr, c->d_conn, c->d_coef,
+                                                            (const double2 *)c->d_diag, lv, cnt, rowptr, col,
+                                                            val, kind);
+  else
+    k_small_csr<W, FILL, false><<<g, 256, 0, ctx->stream>>>(keys, b->n, c->d_cptr, c->d_conn, c->d_coef,
+                                                             (const double2 *)c->d_diag, lv, cnt, rowptr, col,
+                                                             val, kind);
+  ctx->launches++;
+}
+
+void qg_small_csr_free(SmallCsr &c) {
+  cudaFree(c.rowptr);
+  cudaFree(c.col);
+  cudaFree(c.val);
+  cudaFree(c.kind);
+  c = SmallCsr();
+}
+
+qg_status qg_small_csr(qg_context ctx, qg_operator op, qg_basis b, int64_t max_nnz, SmallCsr *out) {
+  *out = SmallCsr();
+  if (!qg_apply_uses_lists(op, b) || b->n > (1 << 30)) return QG_OK;
+  qg_status st = QG_OK;
+  OpBasisCache *c = qg_basis_cache(b, op, &st);
+  if (st != QG_OK) return st;
+  const HostTable *tab;
+  LocalView lv;
+  const uint64_t *wreq;
+  same_basis_view(op, b, c, &tab, &lv, &wreq);
+  const bool real = op_values_real(op);
+  const int n = (int)b->n;
+  SmallCsr s;
+  s.n = n;
+  int *cnt = nullptr;
+  cudaError_t e = cudaMalloc(&cnt, (size_t)n * sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc(&s.rowptr, (size_t)(n + 1) * sizeof(int));
+  if (e == cudaSuccess) {
+    if (b->W == 1)
+      launch_small_csr<1, false>(ctx, b, c, lv, real, cnt, nullptr, nullptr, nullptr, nullptr);
+    else
+      launch_small_csr<2, false>(ctx, b, c, lv, real, cnt, nullptr, nullptr, nullptr, nullptr);
+    e = cudaGetLastError();
+  }
+  std::vector<int> hc(n), hp(n + 1, 0);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(hc.data(), cnt, (size_t)n * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  cudaFree(cnt);
+  if (e != cudaSuccess) {
+    qg_small_csr_free(s);
+    return qg_cuda_fail(ctx, e, "small-basis rows");
+  }
+  int64_t tot = 0;
+  for (int r = 0; r < n; r++) {
+    hp[r] = (int)tot;
+    tot += hc[r];
+  }
+  hp[n] = (int)std::min<int64_t>(tot, INT32_MAX);
+  s.nnz = tot;
+  if (tot > max_nnz) {  // too many terms for one block per chain: the caller takes the general path
+    cudaFree(s.rowptr);
+    out->n = n;
+    out->nnz = tot;
+    return QG_OK;
+  }
+  e = cudaMemcpyAsync(s.rowptr, hp.data(), (size_t)(n + 1) * sizeof(int), cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess) e = cudaMalloc(&s.col, (size_t)std::max<int64_t>(tot, 1) * sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc(&s.val, (size_t)std::max<int64_t>(tot, 1) * sizeof(double2));
+  if (e == cudaSuccess) e = cudaMalloc(&s.kind, (size_t)std::max<int64_t>(tot, 1));
+  if (e == cudaSuccess) {
+    if (b->W == 1)
+      launch_small_csr<1, true>(ctx, b, c, lv, real, nullptr, s.rowptr, s.col, s.val, s.kind);
+    else
+      launch_small_csr<2, true>(ctx, b, c, lv, real, nullptr, s.rowptr, s.col, s.val, s.kind);
+    e = cudaGetLastError();
+  }
+  if (e != cudaSuccess) {
+    qg_small_csr_free(s);
+    return qg_cuda_fail(ctx, e, "small-basis rows");
+  }
+  *out = s;
+  return QG_OK;
 }
 
 // ------------------------------------------------------------------ entry points

@@ -95,6 +95,7 @@ struct qg_context_s {
   bool use_graphs = true;             // capture Lanczos step sequences into CUDA graphs
   bool autotune = true;               // time the vectors-per-pass choices of multi-vector applies
   bool conn_lists = true;             // resolve hashed connections once per (operator, basis)
+  bool small_lanczos = true;          // persistent one-block-per-chain Lanczos on small bases
 };
 
 // A term table in one device allocation: ngroups GroupDev followed by nterms TermDev.
@@ -373,3 +374,62 @@ qg_status qg_block_combine(qg_context ctx, const double2 *K, int64_t n, int ntri
 
 // reductions (qgpu_krylov.cu)
 qg_status qg_dot_dev(qg_context ctx, int64_t n, int nvec, const double *x, const double *y, double *out_dev);
+
+__device__ __forceinline__ double qg_flip_sign(double v, int par) {
+  return __longlong_as_double(__double_as_longlong(v) ^ ((long long)(par & 1) << 63));
+}
+
+__device__ __forceinline__ bool qg_is_nonzero(double v) { return (__double_as_longlong(v) << 1) != 0; }
+
+// acc += (vr + i vi) xv, in the operation order of the complex form
+__device__ __forceinline__ void qg_cmac(double2 &acc, double vr, double vi, bool cplx, double2 xv) {
+  if (cplx) {
+    acc.x = fma(-vi, xv.y, acc.x);
+    acc.y = fma(vi, xv.x, acc.y);
+  }
+  acc.x = fma(vr, xv.x, acc.x);
+  acc.y = fma(vr, xv.y, acc.y);
+}
+
+// Per-element arithmetic of the Lanczos kernels with every fused multiply-add written out, so
+// the general path and the persistent small-basis kernel round alike.
+__device__ __forceinline__ double qg_norm2(double2 v) { return fma(v.x, v.x, v.y * v.y); }
+// Re(conj(x) y)
+__device__ __forceinline__ double qg_redot(double2 x, double2 y) { return fma(x.x, y.x, x.y * y.y); }
+// w - a p
+__device__ __forceinline__ double2 qg_axpy2(double2 w, double a, double2 p) {
+  return make_double2(fma(-a, p.x, w.x), fma(-a, p.y, w.y));
+}
+// the diagonal term dg * x: real dg (two products) or complex
+__device__ __forceinline__ double2 qg_diag_mul(double2 dg, double2 xv, bool cplx) {
+  if (cplx) return make_double2(fma(dg.x, xv.x, -(dg.y * xv.y)), fma(dg.x, xv.y, dg.y * xv.x));
+  return make_double2(dg.x * xv.x, dg.x * xv.y);
+}
+// after a Lanczos norm t = |v|^2: b = sqrt(t), scale = 1/b (0 for an empty vector), truncation
+// threshold (eps/err)^2 with the err before this step, err *= b^2/(b^2 + 4 gamma^2)
+__device__ __forceinline__ void qg_lanczos_norm_scalars(double t, bool first, double eps, double gamma, double &b,
+                                                        double &scale, double &thr2, double &err) {
+  b = sqrt(t);
+  scale = (b > 0.0) ? 1.0 / b : 0.0;
+  const double e = first ? 1.0 : err;
+  const double th = eps / e;
+  thr2 = __dmul_rn(th, th);
+  const double b2 = __dmul_rn(b, b), g4 = __dmul_rn(__dmul_rn(4.0, gamma), gamma);
+  err = first ? 1.0 : e * (b2 / (b2 + g4));
+}
+
+// The same-basis apply of op on b as explicit rows (CSR) for the persistent Lanczos kernel of
+// small bases (qgpu_apply.cu): per row, in the list kernel's order, its terms with the source
+// row and the value that kernel multiplies by; kind 0 / 1 a real / complex diagonal product,
+// 2 / 3 a real / complex multiply-add.  Arrays stay null when the connection lists are not
+// built or the rows hold more than max_nnz terms (nnz then says how many).
+struct SmallCsr {
+  int n = 0;
+  int64_t nnz = 0;
+  int *rowptr = nullptr;
+  int *col = nullptr;
+  double2 *val = nullptr;
+  unsigned char *kind = nullptr;
+};
+qg_status qg_small_csr(qg_context ctx, qg_operator op, qg_basis b, int64_t max_nnz, SmallCsr *out);
+void qg_small_csr_free(SmallCsr &c);

@@ -44,7 +44,7 @@ __global__ void k_dot_partial(int64_t n, int nvec, const double2 *__restrict__ x
         s.x += a.x * b.x + a.y * b.y;
         s.y += a.x * b.y - a.y * b.x;
       } else {
-        s.x += a.x * a.x + a.y * a.y;
+        s.x += qg_norm2(a);
       }
     }
     for (int o = 16; o; o >>= 1) {
@@ -87,7 +87,7 @@ __global__ void k_dot_partial_flat(int64_t len, int nvec, const double2 *__restr
       s.x += a.x * b.x + a.y * b.y;
       s.y += a.x * b.y - a.y * b.x;
     } else {
-      s.x += a.x * a.x + a.y * a.y;
+      s.x += qg_norm2(a);
     }
   }
   sh[tid] = s;
@@ -233,9 +233,9 @@ __global__ void k_lanczos_axpy_norm(int64_t n, int nvec, const double2 *__restri
     double s = 0.0;
     for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
       double2 wv = w[r * nvec + k], pv = vp[r * nvec + k];
-      double2 o = make_double2(wv.x - ak * pv.x, wv.y - ak * pv.y);
+      double2 o = qg_axpy2(wv, ak, pv);
       v[r * nvec + k] = o;
-      s += o.x * o.x + o.y * o.y;
+      s += qg_norm2(o);
     }
     for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
     if (lane == 0) sh[wid].x = s;
@@ -260,9 +260,9 @@ __global__ void k_lanczos_axpy_norm_flat(int64_t len, int nvec, const double2 *_
   double s = 0.0;
   for (int64_t i = blockIdx.x * (int64_t)T + tid; i < len; i += (int64_t)gridDim.x * T) {
     double2 wv = w[i], pv = vp[i];
-    double2 o = make_double2(wv.x - ak * pv.x, wv.y - ak * pv.y);
+    double2 o = qg_axpy2(wv, ak, pv);
     v[i] = o;
-    s += o.x * o.x + o.y * o.y;
+    s += qg_norm2(o);
   }
   sh[tid].x = s;
   __syncthreads();
@@ -327,15 +327,13 @@ __global__ void __launch_bounds__(QG_FIN_THREADS) k_fin_b(const double2 *part, i
   const int col = *step;
   double t = fin_sum(part, nblk, nvec, k, sh);
   if (threadIdx.x == 0) {
-    double b = sqrt(t);
+    double b, sc, th2, e = first ? 1.0 : err[k];
+    qg_lanczos_norm_scalars(t, first != 0, eps, gamma, b, sc, th2, e);
     b_now[k] = b;
     b_hist[k * stride + col] = b;
-    scale[k] = (b > 0.0) ? 1.0 / b : 0.0;
-    double e = first ? 1.0 : err[k];
-    double th = eps / e;
-    thr2[k] = th * th;
-    if (!first) err[k] = e * (b * b / (b * b + 4 * gamma * gamma));
-    else err[k] = 1.0;
+    scale[k] = sc;
+    thr2[k] = th2;
+    err[k] = e;
   }
 }
 
@@ -349,7 +347,7 @@ __global__ void k_scale_trunc(int64_t n, int nvec, const double2 *__restrict__ v
   double sc = scale[k];
   v.x *= sc;
   v.y *= sc;
-  if (!(v.x * v.x + v.y * v.y > thr2[k])) v = make_double2(0.0, 0.0);
+  if (!(qg_norm2(v) > thr2[k])) v = make_double2(0.0, 0.0);
   vout[i] = v;
 }
 
@@ -361,6 +359,221 @@ __global__ void k_zero(double *p, int64_t n) {
 __global__ void k_copy_col(const double2 *src, double2 *dst, int64_t n) {
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i < n) dst[i] = src[i];
+}
+
+// ------------------------------------------------------------------ small bases: a persistent kernel
+
+// Bases this small run every Lanczos chain as one block that keeps its three vectors in shared
+// memory and makes all NTri steps in one launch (a persistent kernel: no launch, graph node or
+// host round trip per step).  Several chains run side by side, one per block.
+#define QG_SMALL_N 2048      // rows: three vectors of 16 B in shared memory (96 KB)
+#define QG_SMALL_NNZ 32768   // terms of the explicit rows: one block's FP64 work per step
+
+// Each block repeats the arithmetic and summation orders of the general path for one vector --
+// the list apply with its fused epilogue (rows in blocks of 256, a row's terms in the list
+// kernel's order, the block partial as fused_dot_partials forms it), the axpy with its norm and
+// the start norm (per 256 rows: a warp-shuffle tree, then the eight warps in order), the scaling
+// with truncation, and the sum of the partials (k_fin_a / k_fin_b: for at most 32 partials, the
+// shuffle tree of warp 0) -- so a chain's coefficients are bitwise those of qg_lanczos_tridiag's
+// general path with one vector.  v0: n x nvec row-major; chain k = blockIdx.x.
+template <bool KRY>
+__global__ void __launch_bounds__(256)
+    k_lanczos_small(int n, int nvec, const int *__restrict__ rowptr, const int *__restrict__ col,
+                    const double2 *__restrict__ val, const unsigned char *__restrict__ kind,
+                    const double2 *__restrict__ v0, int ntri, double eps, double gamma, double *__restrict__ a_hist,
+                    double *__restrict__ b_hist, double2 *__restrict__ krylov) {
+  extern __shared__ double2 sm_vec[];
+  __shared__ double s_part[32], s_warp[8], s_dot[256], s_seg[8], s_scal[4];
+  const int k = blockIdx.x, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int P = (n + 255) / 256;
+  double2 *V = sm_vec, *VP = sm_vec + n, *Wv = sm_vec + 2 * n;
+  double err = 1.0;  // thread 0
+  // the partial of 256 rows as k_dot_partial / k_lanczos_axpy_norm form it
+  auto rows_part = [&](double sv, int vb) {
+    for (int o = 16; o; o >>= 1) sv += __shfl_xor_sync(0xffffffffu, sv, o);
+    if (lane == 0) s_warp[wid] = sv;
+    __syncthreads();
+    if (tid == 0) {
+      double t = 0.0;
+      for (int w = 0; w < 8; w++) t += s_warp[w];
+      s_part[vb] = t;
+    }
+    __syncthreads();
+  };
+  // the sum of the P partials as fin_sum forms it: warp 0's shuffle tree (lane 0)
+  auto fin = [&]() -> double {
+    double t = 0.0;
+    if (wid == 0) {
+      double s0 = 0.0;
+      if (lane < P) s0 += s_part[lane];
+      double sv = (s0 + 0.0) + (0.0 + 0.0);
+      for (int o = 16; o; o >>= 1) sv += __shfl_xor_sync(0xffffffffu, sv, o);
+      t = 0.0 + sv;
+    }
+    return t;  // thread 0
+  };
+  // the norm's scalars into s_scal[1..3] (b, scale, thr2) and the history at column col
+  auto norm_scalars = [&](bool first, int c) {
+    const double t = fin();
+    if (tid == 0) {
+      double bb, sc, th2;
+      qg_lanczos_norm_scalars(t, first, eps, gamma, bb, sc, th2, err);
+      b_hist[(int64_t)k * ntri + c] = bb;
+      s_scal[1] = bb;
+      s_scal[2] = sc;
+      s_scal[3] = th2;
+    }
+    __syncthreads();
+  };
+  // dst = truncate(src * scale), and the Krylov vector of step c
+  auto normalise = [&](const double2 *src, double2 *dst, int c) {
+    const double sc = s_scal[2], th2 = s_scal[3];
+    for (int r = tid; r < n; r += 256) {
+      double2 v = src[r];
+      v.x *= sc;
+      v.y *= sc;
+      if (!(qg_norm2(v) > th2)) v = make_double2(0.0, 0.0);
+      dst[r] = v;
+      if (KRY) krylov[((int64_t)c * n + r) * nvec + k] = v;
+    }
+    __syncthreads();
+  };
+  // Wv = H V - beta prev (prev null: zero), a = Re <V|H V> into s_scal[0] and the history
+  auto apply = [&](const double2 *prev, double beta, int c) {
+    for (int vb = 0; vb < P; vb++) {
+      const int r = vb * 256 + tid;
+      double dv = 0.0;
+      if (r < n) {
+        double2 acc = make_double2(0.0, 0.0);
+        const int e1 = rowptr[r + 1];
+        for (int e = rowptr[r]; e < e1; e++) {
+          const double2 v = val[e], xv = V[col[e]];
+          const unsigned char kd = kind[e];
+          if (kd < 2)
+            acc = qg_diag_mul(v, xv, kd == 1);
+          else if (kd == 3)
+            qg_cmac(acc, v.x, v.y, true, xv);
+          else
+            qg_cmac(acc, v.x, 0.0, false, xv);
+        }
+        dv = qg_redot(V[r], acc);
+        Wv[r] = qg_axpy2(acc, beta, prev ? prev[r] : make_double2(0.0, 0.0));
+      }
+      s_dot[tid] = dv;
+      __syncthreads();
+      if (tid < 8) {
+        double t = 0.0;
+        for (int q = 0; q < 32; q++) t += s_dot[tid * 32 + q];
+        s_seg[tid] = t;
+      }
+      __syncthreads();
+      if (tid == 0) {
+        double t = 0.0;
+        for (int g = 0; g < 8; g++) t += s_seg[g];
+        s_part[vb] = t;
+      }
+      __syncthreads();
+    }
+    const double a = fin();
+    if (tid == 0) {
+      a_hist[(int64_t)k * (ntri + 1) + c] = a;
+      s_scal[0] = a;
+    }
+    __syncthreads();
+  };
+  // step 0: b0 = |v0|, v = truncate(v0 / b0), w = H v, a1
+  for (int vb = 0; vb < P; vb++) {
+    const int r = vb * 256 + tid;
+    double sv = 0.0;
+    if (r < n) sv += qg_norm2(v0[(int64_t)r * nvec + k]);
+    rows_part(sv, vb);
+  }
+  norm_scalars(true, 0);
+  for (int r = tid; r < n; r += 256) Wv[r] = v0[(int64_t)r * nvec + k];
+  __syncthreads();
+  normalise(Wv, V, 0);
+  apply(nullptr, 0.0, 1);
+  for (int i = 1; i < ntri; i++) {
+    // vraw = w - a v (in place of w) and its norm
+    const double a = s_scal[0];
+    for (int vb = 0; vb < P; vb++) {
+      const int r = vb * 256 + tid;
+      double sv = 0.0;
+      if (r < n) {
+        const double2 o = qg_axpy2(Wv[r], a, V[r]);
+        Wv[r] = o;
+        sv += qg_norm2(o);
+      }
+      rows_part(sv, vb);
+    }
+    norm_scalars(false, i);
+    normalise(Wv, VP, i);  // VP held v_(i-2): now v_i
+    double2 *t = V;
+    V = VP;
+    VP = t;
+    apply(VP, s_scal[1], i + 1);
+  }
+}
+
+// The persistent path for nvec chains on a small basis; *done = false when it does not apply
+// (no connection lists, too many rows or terms), leaving the work to the general path.
+static qg_status lanczos_small(qg_context ctx, qg_operator op, qg_basis b, const double *v0_dev, int nvec, int ntri,
+                               double eps, double gamma, double *a_host, double *b_host, double *krylov_dev,
+                               bool *done) {
+  *done = false;
+  if (!ctx->small_lanczos || b->n > QG_SMALL_N || nvec > 65535) return QG_OK;
+  SmallCsr csr;
+  QG_TRY(qg_small_csr(ctx, op, b, QG_SMALL_NNZ, &csr));
+  if (!csr.rowptr) return QG_OK;
+  const int n = (int)b->n;
+  cudaStream_t s = ctx->stream;
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_lanczos_small<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         3 * QG_SMALL_N * (int)sizeof(double2));
+    cudaFuncSetAttribute(k_lanczos_small<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         3 * QG_SMALL_N * (int)sizeof(double2));
+    attr = true;
+  }
+  double *ah = nullptr, *bh = nullptr;
+  cudaError_t e = cudaMalloc(&ah, (size_t)nvec * (ntri + 1) * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc(&bh, (size_t)nvec * ntri * sizeof(double));
+  if (e == cudaSuccess) e = cudaMemsetAsync(ah, 0, (size_t)nvec * (ntri + 1) * sizeof(double), s);
+  qg_status st = e == cudaSuccess ? QG_OK : qg_cuda_fail(ctx, e, "qg_lanczos_tridiag");
+  if (st == QG_OK) {
+    const size_t smem = (size_t)3 * n * sizeof(double2);
+    if (krylov_dev)
+      k_lanczos_small<true><<<(unsigned)nvec, 256, smem, s>>>(n, nvec, csr.rowptr, csr.col, csr.val, csr.kind,
+                                                              (const double2 *)v0_dev, ntri, eps, gamma, ah, bh,
+                                                              (double2 *)krylov_dev);
+    else
+      k_lanczos_small<false><<<(unsigned)nvec, 256, smem, s>>>(n, nvec, csr.rowptr, csr.col, csr.val, csr.kind,
+                                                               (const double2 *)v0_dev, ntri, eps, gamma, ah, bh,
+                                                               nullptr);
+    ctx->launches++;
+    st = qg_check_launch(ctx, "small-basis Lanczos");
+  }
+  if (st == QG_OK) {
+    e = cudaMemcpyAsync(a_host, ah, (size_t)nvec * (ntri + 1) * sizeof(double), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(b_host, bh, (size_t)nvec * ntri * sizeof(double), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) st = qg_cuda_fail(ctx, e, "qg_lanczos_tridiag");
+  }
+  cudaStreamSynchronize(s);
+  cudaFree(ah);
+  cudaFree(bh);
+  qg_small_csr_free(csr);
+  if (st == QG_OK) {
+    for (int q = 0; q < nvec; q++) a_host[q * (ntri + 1)] = 0.0;
+    *done = true;
+  }
+  return st;
+}
+
+extern "C" qg_status qg_set_small_basis_lanczos(qg_context ctx, int32_t on) {
+  if (!ctx) return QG_ERR_ARG;
+  ctx->small_lanczos = on != 0;
+  return QG_OK;
 }
 
 extern "C" qg_status qg_lanczos_tridiag(qg_context ctx, qg_operator op, qg_basis b, const double *v0_dev, int32_t nvec,
@@ -376,6 +589,11 @@ extern "C" qg_status qg_lanczos_tridiag(qg_context ctx, qg_operator op, qg_basis
     for (int64_t k = 0; k < (int64_t)nvec * (ntri + 1); k++) a_host[k] = 0.0;
     for (int64_t k = 0; k < (int64_t)nvec * ntri; k++) b_host[k] = 0.0;
     return QG_OK;
+  }
+  {
+    bool done = false;
+    qg_status sst = lanczos_small(ctx, op, b, v0_dev, nvec, ntri, eps, gamma, a_host, b_host, krylov_dev, &done);
+    if (sst != QG_OK || done) return sst;
   }
   int64_t len = n * nvec;  // complex entries per block vector
   int P = partial_blocks(ctx, n);
