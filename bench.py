@@ -53,6 +53,8 @@ def parse():
     p.add_argument("--slots", type=int, default=4)
     p.add_argument("--restarts", type=int, default=20)
     p.add_argument("--policy", default="sjf", choices=["fifo", "sjf"])
+    p.add_argument("--materials", type=int, default=0,
+                   help="served mode: jobs share this many Hamiltonians (0: every job its own)")
     return p.parse_args()
 
 
@@ -464,7 +466,8 @@ def main():
         import bench_forms
         for key, fn in (("xas_spectra", lambda: xas_spectra_rate(api)),
                         ("batched_xas_c3", bench_forms.batched_secondary),
-                        ("served_c4", bench_forms.served_secondary)):
+                        ("served_c4", bench_forms.served_secondary),
+                        ("served_shared_h", lambda: bench_forms.served_secondary(materials=4))):
             try:
                 secondary[key] = fn()
             except Exception as e:  # reported, never fatal to the headline number

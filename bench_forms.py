@@ -248,6 +248,48 @@ def make_stream(njobs, seed=0, max_det=2e6, min_det=1e3, eigen_frac=0.25):
     return out
 
 
+def make_shared_stream(njobs, materials=4, seed=5, max_det=2e6, min_det=1e3):
+    """Seeded CreateSpectra jobs on a few materials: `materials` impurity Hamiltonians drawn as in
+    make_stream (one Lanczos length each), every job on one of them with its own initial state
+    and its own number of frequencies -- the case the served form merges."""
+    rng = np.random.default_rng(seed)
+    mats = make_stream(materials, seed=seed, max_det=max_det, min_det=min_det, eigen_frac=0.0)
+    out = []
+    for j in range(njobs):
+        m = int(rng.integers(0, materials))
+        p = dict(mats[m], kind="spectra", material=m, ne=int(rng.integers(1024, 4097)),
+                 state_seed=int(rng.integers(0, 1 << 30)))
+        out.append(p)
+    return out
+
+
+def build_shared_job(api, serve, workloads, p, cache):
+    """A job of make_shared_stream: the material's Hamiltonian and operators are built once and
+    shared (one object per material); the initial state is the material's seed determinant plus
+    0.3 times a seeded neighbour determinant (a target of H on the seed) with a seeded phase."""
+    m = p["material"]
+    if m not in cache:
+        H, R, seed, info = workloads.anderson_impurity(nshell=p["nshell"], seed=p["seed"], delta=p["delta"],
+                                                       v2_total=p["v"] ** 2, hole_max=p["hole_max"],
+                                                       particle_max=p["particle_max"])
+        _, Rx, _, _ = workloads.anderson_impurity(nshell=p["nshell"], seed=p["seed"], delta=p["delta"],
+                                                  v2_total=p["v"] ** 2, hole_max=p["hole_max"],
+                                                  particle_max=p["particle_max"], core_holes=1)
+        seed_b = api.dets_to_bytes([seed], H.nf)
+        nb = api.OperatorPsi(H, api.Wavefunction(H.nf, seed_b, np.ones(1, dtype=np.complex128)), R)
+        cache[m] = (H, Rx, seed_b, nb.det, _xas_ops(api, workloads, H.nf))
+    H, Rx, seed_b, neigh, Ts = cache[m]
+    rng = np.random.default_rng(p["state_seed"])
+    k = int(rng.integers(0, len(neigh)))
+    dets = np.concatenate([seed_b.reshape(1, -1), neigh[k:k + 1]])
+    if np.array_equal(dets[0], dets[1]):
+        dets = dets[:1]
+    vals = np.array([1.0, 0.3 * np.exp(2j * np.pi * rng.random())])[:len(dets)]
+    psi = api.Wavefunction(H.nf, dets, vals)
+    o = {"NTri": p["ntri"], "NE": p["ne"], "Emin": -20.0, "Emax": 20.0, "Gamma": 0.5, "Restrictions": Rx}
+    return serve.SpectraJob(H, Ts, [psi], o, n_det_hint=6 * p["sector"])
+
+
 def build_job(api, serve, workloads, p):
     H, R, seed, info = workloads.anderson_impurity(nshell=p["nshell"], seed=p["seed"], delta=p["delta"],
                                                    v2_total=p["v"] ** 2, hole_max=p["hole_max"],
@@ -272,8 +314,14 @@ def served(args):
 def served_line(args):
     """The served stream against the plain one-job-at-a-time path (the JSON line's fields)."""
     from quanty_gb300 import api, serve, workloads
-    params = make_stream(int(args.jobs), seed=0, max_det=float(args.max_det))
-    jobs = [build_job(api, serve, workloads, p) for p in params]
+    shared = int(getattr(args, "materials", 0) or 0)
+    if shared:
+        params = make_shared_stream(int(args.jobs), materials=shared, max_det=float(args.max_det))
+        cache = {}
+        jobs = [build_shared_job(api, serve, workloads, p, cache) for p in params]
+    else:
+        params = make_stream(int(args.jobs), seed=0, max_det=float(args.max_det))
+        jobs = [build_job(api, serve, workloads, p) for p in params]
     nspec = sum(j.nspec for j in jobs)
     rate = float(args.rate)
     # warm-up: one small job of each kind through both paths (builds, graphs)
@@ -282,7 +330,9 @@ def served_line(args):
     for k in warm:
         jobs[k].run(eng)
     _sync(eng)
-    res_s, lat_s, wall_s = serve.run_stream(jobs, rate, slots=int(args.slots), seed=1, policy=args.policy)
+    st = {}
+    res_s, lat_s, wall_s = serve.run_stream(jobs, rate, slots=int(args.slots), seed=1, policy=args.policy,
+                                            stats=st)
     res_p, lat_p, wall_p = serve.run_plain(jobs, rate, seed=1, eng=eng)
     diff = 0.0
     for a, b in zip(res_s, res_p):
@@ -300,13 +350,15 @@ def served_line(args):
         "higher_is_better": True,
         "dtype": "c128",
         "data": "synthetic (seeded impurity Hamiltonians, Poisson arrivals)",
-        "config": {"workload": "poisson_stream_mixed_impurity_jobs", "jobs": len(jobs), "rate_per_s": rate,
+        "config": {"workload": ("poisson_stream_impurity_jobs_%d_materials" % shared) if shared else
+                   "poisson_stream_mixed_impurity_jobs", "jobs": len(jobs), "rate_per_s": rate,
                    "slots": int(args.slots), "policy": args.policy, "spectra": nspec,
                    "eigen_jobs": sum(p["kind"] == "eigen" for p in params),
                    "max_det": float(args.max_det), "determinants_min": int(min(sizes)),
                    "determinants_max": int(max(sizes))},
         "served": {"wall_s": wall_s, "spectra_per_s": nspec / wall_s, "jobs_per_s": len(jobs) / wall_s,
-                   "p50_s": float(np.percentile(lat_s, 50)), "p99_s": float(np.percentile(lat_s, 99))},
+                   "p50_s": float(np.percentile(lat_s, 50)), "p99_s": float(np.percentile(lat_s, 99)),
+                   "merged_jobs": st.get("merged_jobs", 0)},
         "plain": {"wall_s": wall_p, "spectra_per_s": nspec / wall_p, "jobs_per_s": len(jobs) / wall_p,
                   "p50_s": float(np.percentile(lat_p, 50)), "p99_s": float(np.percentile(lat_p, 99))},
         "speedup_vs_plain": wall_p / wall_s,
@@ -360,11 +412,14 @@ def batched_secondary(ntri=200, ne=2048, nstates=16, plain_sample=3):
             "speedup": nspec / t_b * t_p, "plain_sample": len(sample), "max_rel_diff_batched_vs_plain": diff}
 
 
-def served_secondary(jobs=24, rate=50.0, slots=4, max_det=2e6):
-    """The served stream for the default bench line (the --mode served configuration)."""
+def served_secondary(jobs=24, rate=50.0, slots=4, max_det=2e6, materials=0):
+    """The served stream for the default bench line (the --mode served configuration); with
+    materials > 0 the jobs share that many Hamiltonians and the server merges them."""
     import types
-    line = served_line(types.SimpleNamespace(jobs=jobs, rate=rate, slots=slots, max_det=max_det, policy="sjf"))
+    line = served_line(types.SimpleNamespace(jobs=jobs, rate=rate, slots=slots, max_det=max_det, policy="sjf",
+                                             materials=materials))
     return {"workload": line["config"]["workload"], "unit": "spectra/s", "jobs": line["config"]["jobs"],
+            "merged_jobs": line["served"]["merged_jobs"],
             "spectra": line["config"]["spectra"], "determinants_min": line["config"]["determinants_min"],
             "determinants_max": line["config"]["determinants_max"],
             "served": line["served"]["spectra_per_s"], "plain": line["plain"]["spectra_per_s"],

@@ -1030,13 +1030,14 @@ def _krylov_vectors(H, basis, x, ntri, eps, eng):
     return out, a, b
 
 
-def _batched_lanczos_device(H, Ts, psis, o, R, eng):
+def _batched_lanczos_device(H, Ts, psis, o, R, eng, pairs=None):
     """The batched Lanczos branch with every step on the device: the initial states on one
     basis, their energies as one multi-vector expectation value, each T applied to all of them
     at once straight into the final basis (the closure under H of every T's targets, within
     the restrictions), the empty (T, psi) pairs left out, one multi-vector Lanczos for the
-    rest.  Returns (A, B, E0), or None when the dense branch applies (a final basis within
-    DenseBorder and Method not "Lanczos")."""
+    rest.  pairs: the (iT, ipsi) to run, in the order of the result rows (default every pair,
+    iT*Npsi + ipsi).  Returns (A, B, E0), or None when the dense branch applies (a final basis
+    within DenseBorder and Method not "Lanczos")."""
     torch = eng.torch
     nf, npsi = H.nf, len(psis)
     ntri, eps, gamma = int(o["NTri"]), float(o["Epsilon"]), float(o["Gamma"])
@@ -1063,17 +1064,22 @@ def _batched_lanczos_device(H, Ts, psis, o, R, eng):
     bf = closure_of(H, bt, R, -1, eng)
     if method != "lanczos" and 0 < bf.n <= int(o["DenseBorder"]):
         return None
-    nvec = len(Ts) * npsi
+    if pairs is None:
+        pairs = [(j, i) for j in range(len(Ts)) for i in range(npsi)]
+    nvec = len(pairs)
     A = np.zeros((nvec, ntri + 1))
     B = np.zeros((nvec, ntri))
     if bf.n == 0:
         return A, B, E0
     Y = eng.empty(bf.n, nvec)
     for j, t in enumerate(Ts):
+        cols = [c for c, (jt, _) in enumerate(pairs) if jt == j]
+        if not cols:
+            continue
         yj = eng.empty(bf.n, npsi)
         eng.check(eng.L.qg_apply(eng.ctx, t.handle(eng), bf.h, b0.h, _ptr(Xd), _ptr(yj), npsi))
         with eng.on_stream():
-            Y[:, j * npsi:(j + 1) * npsi] = yj
+            Y[:, cols] = yj[:, [pairs[c][1] for c in cols]]
     norms = np.zeros(nvec)
     eng.check(eng.L.qg_norm(eng.ctx, bf.n, nvec, _ptr(Y), _ptr(norms)))
     live = [i for i in range(nvec) if norms[i] > 0.0]
@@ -1084,6 +1090,56 @@ def _batched_lanczos_device(H, Ts, psis, o, R, eng):
         A[live] = a
         B[live] = b
     return A, B, E0
+
+
+def lanczos_merge_key(H, T, psi, options=None, batched=True):
+    """What several CreateSpectra calls must share to run as one multi-vector Lanczos: the
+    Hamiltonian and every option the Lanczos coefficients depend on (NTri, Epsilon, Gamma,
+    E0, Restrictions, DenseBorder, Method).  None when the call does not take the batched
+    Lanczos branch (Tensor, KrylovBasis, the dense method, batched=False)."""
+    o = _opts(options)
+    if not batched or o.get("Tensor") or o.get("KrylovBasis") or _spectra_method(o) == "dense":
+        return None
+    return (id(H), int(o["NTri"]), float(o["Epsilon"]), float(o["Gamma"]), o.get("E0"),
+            repr(o.get("Restrictions")), int(o["DenseBorder"]), _spectra_method(o))
+
+
+def CreateSpectraMerged(H, jobs, eng=None):
+    """Several CreateSpectra calls on one Hamiltonian as one multi-vector Lanczos (the served
+    form's continuous batching): jobs is a list of (T, psi, options) with equal
+    lanczos_merge_key.  Every job's (T, psi) pairs, and only those, run side by side on the
+    closure of all their targets; each job then takes its own rows, its own energy window,
+    broadening and number of frequencies.  A job's coefficients equal those of its call alone
+    to rounding (the closed bases differ only by determinants its vectors never reach).
+    Returns one (Spectra, tri) per job, or each call's own result when the dense branch
+    applies."""
+    eng = eng or engine()
+    Ts, tidx, psis, pairs, rows = [], {}, [], [], []
+    for T, psi, _ in jobs:
+        tl = T if isinstance(T, (list, tuple)) else [T]
+        pl = psi if isinstance(psi, (list, tuple)) else [psi]
+        base = len(psis)
+        psis.extend(pl)
+        r = []
+        for t in tl:
+            if id(t) not in tidx:
+                tidx[id(t)] = len(Ts)
+                Ts.append(t)
+            for i in range(len(pl)):
+                r.append(len(pairs))
+                pairs.append((tidx[id(t)], base + i))
+        rows.append(r)
+    o = _opts(jobs[0][2])
+    got = _batched_lanczos_device(H, Ts, psis, o, parse_restrictions(o.get("Restrictions")), eng, pairs)
+    if got is None:
+        return [CreateSpectra(H, T, psi, opt, eng=eng) for T, psi, opt in jobs]
+    A, B, E0 = got
+    out = []
+    for (T, psi, opt), r in zip(jobs, rows):
+        oj = _opts(opt)
+        e0 = np.array([E0[pairs[c][1]] for c in r])
+        out.append(_lanczos_spectra(A[r], B[r], e0, oj, float(oj["Gamma"]), int(oj["NTri"]), eng))
+    return out
 
 
 def _lanczos_spectra(A, B, e0, o, gamma, ntri, eng):

@@ -4,9 +4,11 @@ Jobs of mixed Hilbert-space sizes arrive over time.  The server keeps ``slots`` 
 with its own context and CUDA stream (``api.Engine``) and its own host thread, so the kernels
 of different jobs overlap on the device.  A job is admitted when a slot is free and its
 estimated device footprint fits into the HBM budget next to the jobs already running; it
-keeps its Krylov state on the device until it finishes.  Every job computes exactly what it
-would compute alone (its own context and stream, deterministic kernels), so results in the
-mix equal results alone.
+keeps its Krylov state on the device until it finishes.  Continuous batching: when a slot
+takes a CreateSpectra job, the waiting CreateSpectra jobs on the same Hamiltonian with the same
+Lanczos settings (``api.lanczos_merge_key``) join it, and all their (T, psi) pairs run as one
+multi-vector Lanczos (``api.CreateSpectraMerged``); each job still gets its own window and
+frequencies.  Results in the mix equal results alone (to rounding for merged jobs).
 
     srv = Server(slots=4, hbm_budget=200e9)
     fut = srv.submit(SpectraJob(H, [T], [psi], {"NTri": 200, "NE": 2048, ...}))
@@ -63,9 +65,22 @@ class SpectraJob:
             self.n_det_hint = _final_basis_size(self.H, self.T, self.psi, self.options)
         return _footprint(self.n_det_hint, self.nspec)
 
+    def merge_key(self):
+        return api.lanczos_merge_key(self.H, self.T, self.psi, self.options, self.batched)
+
     def run(self, eng):
         S, tri = api.CreateSpectra(self.H, self.T, self.psi, self.options, eng=eng, batched=self.batched)
-        return {"G": S.G, "tri": tri, "Emin": S.Emin, "Emax": S.Emax, "Gamma": S.Gamma}
+        return _spectra_result(S, tri)
+
+
+def _spectra_result(S, tri):
+    return {"G": S.G, "tri": tri, "Emin": S.Emin, "Emax": S.Emax, "Gamma": S.Gamma}
+
+
+def run_merged(jobs, eng):
+    """SpectraJobs with equal merge keys as one CreateSpectraMerged call; one result each."""
+    got = api.CreateSpectraMerged(jobs[0].H, [(j.T, j.psi, j.options) for j in jobs], eng)
+    return [_spectra_result(S, tri) for S, tri in got]
 
 
 class EigenJob:
@@ -93,12 +108,14 @@ class EigenJob:
 class Server:
     """Continuous batching over a fixed set of device slots with HBM-budget admission."""
 
-    def __init__(self, slots=4, hbm_budget=None, device=0, policy="fifo"):
+    def __init__(self, slots=4, hbm_budget=None, device=0, policy="fifo", merge=True, max_merge=16, paused=False):
         import torch
         self.torch = torch
         if policy not in ("fifo", "sjf"):
             raise ValueError("policy is 'fifo' or 'sjf'")
         self.policy = policy
+        self.merge, self.max_merge = bool(merge), int(max_merge)
+        self.paused = bool(paused)  # workers admit nothing until resume()
         if hbm_budget is None:
             free, total = torch.cuda.mem_get_info(device)
             hbm_budget = int(0.8 * free)
@@ -142,10 +159,31 @@ class Server:
         need = rec["job"].footprint()
         if self.in_use + need <= self.budget or (self.in_use == 0 and need > self.budget):
             del self.queue[i]
+            group = [rec]
+            merge = getattr(self, "merge", True) and isinstance(rec["job"], SpectraJob)
+            key = rec["job"].merge_key() if merge else None
+            if key is not None:  # waiting jobs that can share this one's Lanczos run join it
+                for other in list(self.queue):
+                    if len(group) >= getattr(self, "max_merge", 16):
+                        break
+                    oj = other["job"]
+                    if isinstance(oj, SpectraJob) and oj.merge_key() == key:
+                        extra = oj.footprint()
+                        if self.in_use + need + extra > self.budget:
+                            break
+                        self.queue.remove(other)
+                        need += extra
+                        group.append(other)
             self.in_use += need
             rec["need"] = need
+            rec["group"] = group
             return rec
         return None
+
+    def resume(self):
+        with self.cv:
+            self.paused = False
+            self.cv.notify_all()
 
     def _worker(self, eng):
         self.torch.cuda.set_stream(eng.stream)
@@ -153,32 +191,40 @@ class Server:
             with self.cv:
                 rec = None
                 while not self.closed:
-                    rec = self._admit()
+                    rec = None if self.paused else self._admit()
                     if rec is not None:
                         break
                     self.cv.wait(0.05)
                 if rec is None:
                     return
-            rec["start"] = time.perf_counter()
+            group = rec["group"]
+            t_start = time.perf_counter()
             ev0 = self.torch.cuda.Event(enable_timing=True)
             ev1 = self.torch.cuda.Event(enable_timing=True)
             ev0.record(eng.stream)
             try:
-                out = rec["job"].run(eng)
+                if len(group) > 1:
+                    outs = run_merged([g["job"] for g in group], eng)
+                else:
+                    outs = [rec["job"].run(eng)]
                 ev1.record(eng.stream)
                 ev1.synchronize()
-                rec["end"] = time.perf_counter()
-                # the job's window on the device: its stream reached the first event before its
-                # first kernel and the second after its last
-                rec["dev_start"] = self.t_ref.elapsed_time(ev0) * 1e-3
-                rec["dev_end"] = self.t_ref.elapsed_time(ev1) * 1e-3
-                rec["future"].set_result(out)
-            except Exception as exc:  # reported through the future
-                rec["end"] = time.perf_counter()
-                rec["future"].set_exception(exc)
+                t_end = time.perf_counter()
+                for g, out in zip(group, outs):
+                    g["start"], g["end"], g["merged"] = t_start, t_end, len(group)
+                    # the job's window on the device: its stream reached the first event before
+                    # its first kernel and the second after its last
+                    g["dev_start"] = self.t_ref.elapsed_time(ev0) * 1e-3
+                    g["dev_end"] = self.t_ref.elapsed_time(ev1) * 1e-3
+                    g["future"].set_result(out)
+            except Exception as exc:  # reported through the futures
+                t_end = time.perf_counter()
+                for g in group:
+                    g["start"], g["end"], g["merged"] = t_start, t_end, len(group)
+                    g["future"].set_exception(exc)
             with self.cv:
                 self.in_use -= rec["need"]
-                self.records.append(rec)
+                self.records.extend(group)
                 self.cv.notify_all()
 
     def close(self):
@@ -194,9 +240,10 @@ class Server:
         return np.array([r["end"] - r["arrival"] for r in self.records])
 
 
-def run_stream(jobs, rate, slots=4, hbm_budget=None, seed=0, server=None, policy="fifo"):
+def run_stream(jobs, rate, slots=4, hbm_budget=None, seed=0, server=None, policy="fifo", stats=None):
     """Submit jobs at Poisson arrival times (mean `rate` per second); wait for all.
-    Returns (results in submission order, latencies, wall seconds)."""
+    Returns (results in submission order, latencies, wall seconds); `stats` (a dict), when
+    given, receives how many jobs ran merged with others."""
     rng = np.random.default_rng(seed)
     gaps = rng.exponential(1.0 / rate, len(jobs))
     srv = server or Server(slots=slots, hbm_budget=hbm_budget, policy=policy)
@@ -210,6 +257,8 @@ def run_stream(jobs, rate, slots=4, hbm_budget=None, seed=0, server=None, policy
     results = [f.result() for f in futs]
     wall = time.perf_counter() - t0
     lat = np.array([r["end"] - r["arrival"] for r in sorted(srv.records, key=lambda r: r["arrival"])])
+    if stats is not None:
+        stats["merged_jobs"] = sum(1 for r in srv.records if r.get("merged", 1) > 1)
     if server is None:
         srv.close()
     return results, lat, wall

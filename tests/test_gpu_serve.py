@@ -1,6 +1,7 @@
 """Serving form on the GPU: jobs arriving while others run overlap on the device (one context
-and stream per slot; checked with CUDA events on the slots' streams), and every job's result
-equals its result alone."""
+and stream per slot; checked with CUDA events on the slots' streams), waiting CreateSpectra jobs
+on one Hamiltonian run merged as one multi-vector Lanczos, and every job's result equals its
+result alone."""
 import numpy as np
 import pytest
 
@@ -81,3 +82,23 @@ def test_budget_serialises_jobs(mods):
     recs = sorted(srv.records, key=lambda r: r["start"])
     srv.close()
     assert recs[1]["start"] >= recs[0]["end"]
+
+
+def test_waiting_jobs_on_one_hamiltonian_run_merged(mods):
+    """Three CreateSpectra jobs on one impurity Hamiltonian, queued before the only slot starts,
+    run as one multi-vector Lanczos; each gets the spectra (and window) of its call alone."""
+    api, serve, workloads = mods
+    jobs = _jobs(api, serve, workloads)[2:5]
+    assert len({j.merge_key() for j in jobs}) == 1
+    eng = api.Engine(0)
+    alone = [j.run(eng) for j in jobs]
+    srv = serve.Server(slots=1, paused=True)
+    futs = [srv.submit(j) for j in jobs]
+    srv.resume()
+    res = [f.result() for f in futs]
+    recs = list(srv.records)
+    srv.close()
+    assert len(recs) == 3 and all(r["merged"] == 3 for r in recs)
+    for a, r in zip(alone, res):
+        assert np.max(np.abs(a["G"] - r["G"])) <= 1e-12 * np.max(np.abs(a["G"]))
+        assert abs(a["Emin"] - r["Emin"]) < 1e-10 and abs(a["Emax"] - r["Emax"]) < 1e-10

@@ -60,3 +60,31 @@ def test_shortest_job_first():
     assert s._admit() is None          # 60 does not fit
     s.in_use = 0
     assert s._admit()["need"] == 60
+
+
+class FakeSpectra(serve.SpectraJob):
+    def __init__(self, need, key):
+        self.need, self.key = need, key
+
+    def footprint(self):
+        return self.need
+
+    def merge_key(self):
+        return self.key
+
+
+def test_waiting_jobs_with_one_merge_key_join_the_admitted_one():
+    s = server(100)
+    for need, key in ((20, "h1"), (20, "h2"), (30, "h1"), (60, "h1"), (5, None)):
+        s.queue.append({"job": FakeSpectra(need, key)})
+    a = s._admit()
+    # the waiting h1 job that fits joins; the one that would exceed the budget waits
+    assert [g["job"].need for g in a["group"]] == [20, 30] and a["need"] == 50 and s.in_use == 50
+    b = s._admit()
+    assert [g["job"].need for g in b["group"]] == [20] and s.in_use == 70
+    assert s._admit() is None  # 60 does not fit next to 70
+    s.in_use = 0
+    c = s._admit()
+    assert [g["job"].need for g in c["group"]] == [60]
+    d = s._admit()
+    assert [g["job"].need for g in d["group"]] == [5]  # no key: runs on its own
