@@ -759,7 +759,7 @@ __global__ void __launch_bounds__(256, NV == 1 ? QG_APPLY_MIN_BLOCKS : 1)
     k_apply_list(const Key<W> *__restrict__ rows, int64_t n_rows, const int64_t *__restrict__ cptr,
                  const uint2 *__restrict__ conn, const double2 *__restrict__ coef, const double2 *__restrict__ diag,
                  const double2 *__restrict__ x, int xs, double2 *__restrict__ y, int ys, int vec0, ApplyFuse fz,
-                 LocalView lv) {
+                 LocalView lv, int ordered_store) {
   vec0 += blockIdx.y * NV;  // passes of NV vectors side by side (gridDim.y of them)
   int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   bool live = r < n_rows;
@@ -869,7 +869,20 @@ __global__ void __launch_bounds__(256, NV == 1 ? QG_APPLY_MIN_BLOCKS : 1)
     }
   }
   if (!FUSE) {
-    if (live) {
+    if (QG_LIST_REGROUP && ordered_store) {
+      // y in host memory (qg_apply_host): back to the original row order, so a warp stores 32
+      // consecutive rows and the host link carries whole lines instead of 16-byte pieces (in
+      // device memory the scattered stores of a block merge in L2 and cost nothing extra)
+      __syncthreads();  // every regrouped accumulator has been read
+#pragma unroll
+      for (int k = 0; k < NV; k++) s_acc[k][me] = acc[k];
+      __syncthreads();
+      const int64_t r0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+      if (r0 < n_rows) {
+#pragma unroll
+        for (int k = 0; k < NV; k++) y[r0 * ys + vec0 + k] = s_acc[k][threadIdx.x];
+      }
+    } else if (live) {
 #pragma unroll
       for (int k = 0; k < NV; k++) y[r * ys + vec0 + k] = acc[k];
     }
@@ -1691,10 +1704,12 @@ static void launch_apply_list_t(qg_context ctx, const OpBasisCache *c, const dou
   dim3 grid((unsigned)qg_apply_grid(dst), (unsigned)npass);
   if (real)
     k_apply_list<W, NV, FUSE, true><<<grid, 256, 0, ctx->stream>>>(
-        (const Key<W> *)dst->d_keys, dst->n, c->d_cptr, c->d_conn, c->d_coef, diag, x, xs, y, ys, vec0, fz, lv);
+        (const Key<W> *)dst->d_keys, dst->n, c->d_cptr, c->d_conn, c->d_coef, diag, x, xs, y, ys, vec0, fz, lv,
+        ctx->y_host ? 1 : 0);
   else
     k_apply_list<W, NV, FUSE, false><<<grid, 256, 0, ctx->stream>>>(
-        (const Key<W> *)dst->d_keys, dst->n, c->d_cptr, c->d_conn, c->d_coef, diag, x, xs, y, ys, vec0, fz, lv);
+        (const Key<W> *)dst->d_keys, dst->n, c->d_cptr, c->d_conn, c->d_coef, diag, x, xs, y, ys, vec0, fz, lv,
+        ctx->y_host ? 1 : 0);
   ctx->launches++;
 }
 
@@ -2104,7 +2119,9 @@ extern "C" qg_status qg_apply_host(qg_context ctx, qg_operator op, qg_basis dst,
   } else {
     QG_CUDA(ctx, cudaMemcpyAsync(dx, x_host, xb, cudaMemcpyHostToDevice, ctx->stream));
   }
+  ctx->y_host = ymap != nullptr;
   qg_status st = qg_apply(ctx, op, dst, src, dx, dy, nvec);
+  ctx->y_host = false;
   if (st != QG_OK) return st;
   if (!ymap) QG_CUDA(ctx, cudaMemcpyAsync(y_host, dy, yb, cudaMemcpyDeviceToHost, ctx->stream));
   QG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));

@@ -93,6 +93,7 @@ struct qg_context_s {
   double *d_io = nullptr;             // staging for host-buffer entry points
   size_t io_bytes = 0;
   bool use_graphs = true;             // capture Lanczos step sequences into CUDA graphs
+  bool y_host = false;                // the apply being launched writes y into host memory
   bool autotune = true;               // time the vectors-per-pass choices of multi-vector applies
   bool conn_lists = true;             // resolve hashed connections once per (operator, basis)
   bool small_lanczos = true;          // persistent one-block-per-chain Lanczos on small bases
