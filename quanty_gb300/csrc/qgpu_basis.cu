@@ -482,14 +482,18 @@ __device__ __forceinline__ bool expand_flush(const Key<W> *q, int n, int lane, S
 // repeats the round): a thread checks the error word when it starts and stops at its first
 // new key past the limit, so the set exceeds the list capacity by at most one key per
 // resident thread.
+// With twreq (one 64-bit word per term) the occupation windows are tested with one AND: bit
+// 5q + D + 2 of a source's mask says its count in window q plus D, D in [-2, 2], stays inside
+// the window, and a term's word holds the bit of its change D_q for every window (D_q = 0
+// included, so a source outside a window passes none of its terms).
 template <int W>
 __global__ void __launch_bounds__(256) k_expand(const Key<W> *src, int64_t r0, int64_t r1,
                                                 const GroupDev<W> *__restrict__ groups, int ngroups,
                                                 const TermDev<W> *__restrict__ terms, int nres,
                                                 const uint64_t *__restrict__ rmask, const int32_t *__restrict__ rmin,
-                                                const int32_t *__restrict__ rmax, Slot *slots, uint64_t hmask,
-                                                Key<W> *list, unsigned long long *count, unsigned long long limit,
-                                                unsigned int *err, int skip_diag) {
+                                                const int32_t *__restrict__ rmax, const uint64_t *__restrict__ twreq,
+                                                Slot *slots, uint64_t hmask, Key<W> *list, unsigned long long *count,
+                                                unsigned long long limit, unsigned int *err, int skip_diag) {
   __shared__ Key<W> queue[8][QG_XQ];
   const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const unsigned below = (1u << lane) - 1u;
@@ -500,6 +504,17 @@ __global__ void __launch_bounds__(256) k_expand(const Key<W> *src, int64_t r0, i
 #pragma unroll
   for (int i = 0; i < W; i++) d.w[i] = live ? src[r].w[i] : 0ull;
   if (!__any_sync(0xffffffffu, live)) return;  // warp-uniform
+  uint64_t okm = 0;
+  if (twreq) {
+    for (int c = 0; c < nres; c++) {
+      int n = 0;
+#pragma unroll
+      for (int i = 0; i < W; i++) n += __popcll(d.w[i] & rmask[c * W + i]);
+#pragma unroll
+      for (int D = -2; D <= 2; D++)
+        if (n + D >= rmin[c] && n + D <= rmax[c]) okm |= 1ull << (5 * c + D + 2);
+    }
+  }
   int qn = 0;
   bool halt = false;
   for (int g = 0; g < ngroups && !halt; g++) {
@@ -524,11 +539,16 @@ __global__ void __launch_bounds__(256) k_expand(const Key<W> *src, int64_t r0, i
       Key<W> tg;
 #pragma unroll
       for (int i = 0; i < W; i++) tg.w[i] = d.w[i] ^ T.flip[i];
-      for (int c = 0; c < nres && has; c++) {
-        int n = 0;
+      if (twreq) {
+        const uint64_t req = twreq[t];
+        has &= (okm & req) == req;
+      } else {
+        for (int c = 0; c < nres && has; c++) {
+          int n = 0;
 #pragma unroll
-        for (int i = 0; i < W; i++) n += __popcll(tg.w[i] & rmask[c * W + i]);
-        has = (n >= rmin[c]) && (n <= rmax[c]);
+          for (int i = 0; i < W; i++) n += __popcll(tg.w[i] & rmask[c * W + i]);
+          has = (n >= rmin[c]) && (n <= rmax[c]);
+        }
       }
       unsigned m = __ballot_sync(0xffffffffu, has);
       if (has) q[qn + __popc(m & below)] = tg;
@@ -610,8 +630,34 @@ static qg_status grow_t(qg_context ctx, qg_operator op, const Key<W> *seed_keys,
   cudaStream_t s = ctx->stream;
   Restrictions R;
   if (!convert_restrictions(op->nf, W, res, R)) return QG_ERR_ARG;
-  uint64_t *d_rmask = nullptr;
+  uint64_t *d_rmask = nullptr, *d_twreq = nullptr;
   int32_t *d_rmin = nullptr, *d_rmax = nullptr;
+  // per push term, the window bits its target needs (when every window change fits the code)
+  std::vector<uint64_t> twreq;
+  if (R.n > 0 && R.n <= 12 && op->push.nterms > 0) {
+    const GroupDev<W> *hg = (const GroupDev<W> *)op->push.h_blob.data();
+    const TermDev<W> *ht = (const TermDev<W> *)(op->push.h_blob.data() + op->push.ngroups * sizeof(GroupDev<W>));
+    twreq.assign(op->push.nterms, 0);
+    bool exact = true;
+    for (int g = 0; g < op->push.ngroups && exact; g++)
+      for (int t = hg[g].begin; t < hg[g].end && exact; t++)
+        for (int q = 0; q < R.n && exact; q++) {
+          int D = 0;
+          for (int i = 0; i < W; i++) {
+            // every flipped orbital has a fixed state in the source (need0 or need1), so the
+            // window change is a term constant; otherwise fall back to counting the target
+            if (ht[t].flip[i] & ~(ht[t].need0[i] | hg[g].need1[i])) exact = false;
+            const uint64_t m = R.mask[(size_t)q * W + i];
+            D += __builtin_popcountll(ht[t].flip[i] & ht[t].need0[i] & m) -
+                 __builtin_popcountll(ht[t].flip[i] & hg[g].need1[i] & m);
+          }
+          if (D < -2 || D > 2)
+            exact = false;
+          else
+            twreq[t] |= 1ull << (5 * q + D + 2);
+        }
+    if (!exact) twreq.clear();
+  }
   if (R.n) {
     QG_CUDA(ctx, cudaMalloc(&d_rmask, R.mask.size() * 8));
     QG_CUDA(ctx, cudaMalloc(&d_rmin, R.n * 4));
@@ -619,6 +665,10 @@ static qg_status grow_t(qg_context ctx, qg_operator op, const Key<W> *seed_keys,
     QG_CUDA(ctx, cudaMemcpy(d_rmask, R.mask.data(), R.mask.size() * 8, cudaMemcpyHostToDevice));
     QG_CUDA(ctx, cudaMemcpy(d_rmin, R.mn.data(), R.n * 4, cudaMemcpyHostToDevice));
     QG_CUDA(ctx, cudaMemcpy(d_rmax, R.mx.data(), R.n * 4, cudaMemcpyHostToDevice));
+    if (!twreq.empty()) {
+      QG_CUDA(ctx, cudaMalloc(&d_twreq, twreq.size() * 8));
+      QG_CUDA(ctx, cudaMemcpy(d_twreq, twreq.data(), twreq.size() * 8, cudaMemcpyHostToDevice));
+    }
   }
   // list capacity; the set has 2*cap slots.  An expansion stops inserting once the list is
   // full; each thread resident at that moment can add at most one key past it (well under
@@ -665,8 +715,8 @@ static qg_status grow_t(qg_context ctx, qg_operator op, const Key<W> *seed_keys,
     if (e != cudaSuccess) break;
     k_expand<W><<<grid_for(f1 - f0), 256, 0, s>>>(
         front, f0, f1, (const GroupDev<W> *)op->push.d_groups, op->push.ngroups, (const TermDev<W> *)op->push.d_terms,
-        R.n, d_rmask, d_rmin, d_rmax, slots, (uint64_t)(2 * cap - 1), list, d_count, (unsigned long long)cap,
-        ctx->d_err, include_seed ? 1 : 0);
+        R.n, d_rmask, d_rmin, d_rmax, d_twreq, slots, (uint64_t)(2 * cap - 1), list, d_count,
+        (unsigned long long)cap, ctx->d_err, include_seed ? 1 : 0);
     ctx->launches++;
     unsigned int herr = 0;
     e = cudaMemcpyAsync(&count, d_count, 8, cudaMemcpyDeviceToHost, s);
@@ -739,6 +789,7 @@ static qg_status grow_t(qg_context ctx, qg_operator op, const Key<W> *seed_keys,
   cudaFree(d_rmask);
   cudaFree(d_rmin);
   cudaFree(d_rmax);
+  cudaFree(d_twreq);
   if (rounds_done) *rounds_done = rounds;
   return st;
 }
