@@ -754,12 +754,13 @@ static_assert(sizeof(LocalEntry) == 32 && offsetof(LocalEntry, tend) == 4 && off
 // coefficients), so each connection is two FMAs and no imaginary part is read or tested.  The
 // general form's per-connection test of the imaginary part compiles to predicated FMAs, which
 // hold the FP64 pipe whether or not they take effect; a real operator would pay for all four.
-template <int W, int NV, bool FUSE, bool REAL>
+// ORD: y is host memory (see the store at the end).
+template <int W, int NV, bool FUSE, bool REAL, bool ORD = false>
 __global__ void __launch_bounds__(256, NV == 1 ? QG_APPLY_MIN_BLOCKS : 1)
     k_apply_list(const Key<W> *__restrict__ rows, int64_t n_rows, const int64_t *__restrict__ cptr,
                  const uint2 *__restrict__ conn, const double2 *__restrict__ coef, const double2 *__restrict__ diag,
                  const double2 *__restrict__ x, int xs, double2 *__restrict__ y, int ys, int vec0, ApplyFuse fz,
-                 LocalView lv, int ordered_store) {
+                 LocalView lv) {
   vec0 += blockIdx.y * NV;  // passes of NV vectors side by side (gridDim.y of them)
   int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   bool live = r < n_rows;
@@ -869,7 +870,7 @@ __global__ void __launch_bounds__(256, NV == 1 ? QG_APPLY_MIN_BLOCKS : 1)
     }
   }
   if (!FUSE) {
-    if (QG_LIST_REGROUP && ordered_store) {
+    if (QG_LIST_REGROUP && ORD) {
       // y in host memory (qg_apply_host): back to the original row order, so a warp stores 32
       // consecutive rows and the host link carries whole lines instead of 16-byte pieces (in
       // device memory the scattered stores of a block merge in L2 and cost nothing extra)
@@ -1702,14 +1703,21 @@ static void launch_apply_list_t(qg_context ctx, const OpBasisCache *c, const dou
                                 const double2 *x, int xs, double2 *y, int ys, int vec0, int npass,
                                 const ApplyFuse &fz, const LocalView &lv, bool real) {
   dim3 grid((unsigned)qg_apply_grid(dst), (unsigned)npass);
-  if (real)
-    k_apply_list<W, NV, FUSE, true><<<grid, 256, 0, ctx->stream>>>(
-        (const Key<W> *)dst->d_keys, dst->n, c->d_cptr, c->d_conn, c->d_coef, diag, x, xs, y, ys, vec0, fz, lv,
-        ctx->y_host ? 1 : 0);
-  else
-    k_apply_list<W, NV, FUSE, false><<<grid, 256, 0, ctx->stream>>>(
-        (const Key<W> *)dst->d_keys, dst->n, c->d_cptr, c->d_conn, c->d_coef, diag, x, xs, y, ys, vec0, fz, lv,
-        ctx->y_host ? 1 : 0);
+  const Key<W> *keys = (const Key<W> *)dst->d_keys;
+  if (NV == 1 && !FUSE && ctx->y_host) {  // one vector into host memory: rows stored in order
+    if (real)
+      k_apply_list<W, 1, false, true, true><<<grid, 256, 0, ctx->stream>>>(keys, dst->n, c->d_cptr, c->d_conn,
+                                                                        c->d_coef, diag, x, xs, y, ys, vec0, fz, lv);
+    else
+      k_apply_list<W, 1, false, false, true><<<grid, 256, 0, ctx->stream>>>(keys, dst->n, c->d_cptr, c->d_conn,
+                                                                         c->d_coef, diag, x, xs, y, ys, vec0, fz, lv);
+  } else if (real) {
+    k_apply_list<W, NV, FUSE, true><<<grid, 256, 0, ctx->stream>>>(keys, dst->n, c->d_cptr, c->d_conn, c->d_coef,
+                                                                   diag, x, xs, y, ys, vec0, fz, lv);
+  } else {
+    k_apply_list<W, NV, FUSE, false><<<grid, 256, 0, ctx->stream>>>(keys, dst->n, c->d_cptr, c->d_conn, c->d_coef,
+                                                                    diag, x, xs, y, ys, vec0, fz, lv);
+  }
   ctx->launches++;
 }
 
