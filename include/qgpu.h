@@ -275,6 +275,14 @@ qg_status qg_lanczos_tridiag(qg_context ctx, qg_operator op, qg_basis basis, con
  * vector alone.  on = 0 keeps every call on the general path (default 1). */
 qg_status qg_set_small_basis_lanczos(qg_context ctx, int32_t on);
 
+/* With a real operator (every value real), start vectors whose imaginary or real part is zero
+ * are real Lanczos chains (the reference's real-vector variants, LanczosTriDiagonalizeRR,
+ * Core/Lanczos.cpp:1905-2830), and qg_lanczos_tridiag runs them two per complex vector (real
+ * and imaginary parts), one apply serving both; each chain's coefficients equal those of its
+ * run alone (bitwise for a single pair, to rounding otherwise).  on = 0 runs every vector as
+ * complex (default 1). */
+qg_status qg_set_split_chains(qg_context ctx, int32_t on);
+
 /* Continued fraction G_s(w_k) = a0 + b0^2/(w - a1 + i g/2 - b1^2/(...)) for nspec spectra
  * and w_k = emin + k*de + e0[s], k = 0..ne, in one kernel (TriDiagonalMatrixToSpectrum,
  * Core/Spectral.cpp:1433).  Spectrum s uses a[s*(ntri+1) ..], b[s*ntri ..]; host in; g_host

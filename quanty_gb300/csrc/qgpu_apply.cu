@@ -176,13 +176,14 @@ __device__ __forceinline__ uint64_t window_bits(const Key<W> &d, const SrcView &
 // their eight sums -- about one add per row, where a warp-shuffle tree costs five per row and
 // vector.  Every apply kernel reduces in this order, so their Lanczos chains agree bitwise.
 // Blocks of 256 threads; s_dot holds NV x 256 doubles (stride 256), s_red NV x 8.
-template <int NV>
+// NS sums per row (NV, or 2 NV with PAIR: the two parts of each vector, written as .x and .y).
+template <int NS, bool PAIR>
 __device__ __forceinline__ void fused_dot_partials(const double *dvs, int me, double *s_dot, double *s_red,
                                                    double2 *part, int ys, int vec0) {
 #pragma unroll
-  for (int k = 0; k < NV; k++) s_dot[k * 256 + me] = dvs[k];
+  for (int k = 0; k < NS; k++) s_dot[k * 256 + me] = dvs[k];
   __syncthreads();
-  if (threadIdx.x < NV * 8) {
+  if (threadIdx.x < NS * 8) {
     const int k = threadIdx.x >> 3, seg = threadIdx.x & 7;
     double t = 0.0;
 #pragma unroll 8
@@ -190,11 +191,19 @@ __device__ __forceinline__ void fused_dot_partials(const double *dvs, int me, do
     s_red[k * 8 + seg] = t;
   }
   __syncthreads();
-  if (threadIdx.x < NV) {
+  if (!PAIR && threadIdx.x < NS) {
     double t = 0.0;
 #pragma unroll
     for (int g = 0; g < 8; g++) t += s_red[threadIdx.x * 8 + g];
     part[blockIdx.x * ys + vec0 + threadIdx.x] = make_double2(t, 0.0);
+  }
+  if (PAIR && threadIdx.x < NS / 2) {
+    double ta = 0.0, tb = 0.0;
+#pragma unroll
+    for (int g = 0; g < 8; g++) ta += s_red[2 * threadIdx.x * 8 + g];
+#pragma unroll
+    for (int g = 0; g < 8; g++) tb += s_red[(2 * threadIdx.x + 1) * 8 + g];
+    part[blockIdx.x * ys + vec0 + threadIdx.x] = make_double2(ta, tb);
   }
 }
 
@@ -371,7 +380,7 @@ __global__ void __launch_bounds__(256, NV == 1 ? QG_APPLY_MIN_BLOCKS : 1) k_appl
       }
       dvs[k] = dv;
     }
-    fused_dot_partials<NV>(dvs, threadIdx.x, s_dot, s_red, fz.dot_part, ys, vec0);
+    fused_dot_partials<NV, false>(dvs, threadIdx.x, s_dot, s_red, fz.dot_part, ys, vec0);
   }
   if (SMEM && pending) mbar_wait_bounded(smem_addr(&s_bar), 0);  // never leave with a copy in flight
 }
@@ -754,8 +763,9 @@ static_assert(sizeof(LocalEntry) == 32 && offsetof(LocalEntry, tend) == 4 && off
 // coefficients), so each connection is two FMAs and no imaginary part is read or tested.  The
 // general form's per-connection test of the imaginary part compiles to predicated FMAs, which
 // hold the FP64 pipe whether or not they take effect; a real operator would pay for all four.
-// ORD: y is host memory (see the store at the end).
-template <int W, int NV, bool FUSE, bool REAL, bool ORD = false>
+// ORD: y is host memory (see the store at the end).  SPLIT (with FUSE and REAL): each complex
+// vector carries two real Lanczos chains, its real and imaginary parts.
+template <int W, int NV, bool FUSE, bool REAL, bool ORD = false, bool SPLIT = false>
 __global__ void __launch_bounds__(256, NV == 1 ? QG_APPLY_MIN_BLOCKS : 1)
     k_apply_list(const Key<W> *__restrict__ rows, int64_t n_rows, const int64_t *__restrict__ cptr,
                  const uint2 *__restrict__ conn, const double2 *__restrict__ coef, const double2 *__restrict__ diag,
@@ -887,6 +897,29 @@ __global__ void __launch_bounds__(256, NV == 1 ? QG_APPLY_MIN_BLOCKS : 1)
 #pragma unroll
       for (int k = 0; k < NV; k++) y[r * ys + vec0 + k] = acc[k];
     }
+  } else if (SPLIT) {
+    // two real chains per vector: the real operator keeps the parts apart, so each part is
+    // updated and reduced with exactly the arithmetic of its chain run alone (a zero
+    // imaginary part adds nothing to the real one): y = H x - beta prev per part with its
+    // own beta, the partials of <x|H x> per part as .x and .y
+    __shared__ double s_red[2 * NV * 8];
+    double dvs[2 * NV];
+#pragma unroll
+    for (int k = 0; k < NV; k++) {
+      double da = 0.0, db = 0.0;
+      if (live) {
+        const double2 xv = x[r * xs + vec0 + k], pv = fz.prev[r * ys + vec0 + k];
+        da = __dmul_rn(xv.x, acc[k].x);
+        db = __dmul_rn(xv.y, acc[k].y);
+        y[r * ys + vec0 + k] = make_double2(fma(-fz.beta[2 * (vec0 + k)], pv.x, acc[k].x),
+                                            fma(-fz.beta[2 * (vec0 + k) + 1], pv.y, acc[k].y));
+      }
+      dvs[2 * k] = da;
+      dvs[2 * k + 1] = db;
+    }
+    if (QG_LIST_REGROUP) __syncthreads();  // every regrouped accumulator has been read
+    fused_dot_partials<2 * NV, true>(dvs, me, reinterpret_cast<double *>(&s_acc[0][0]), s_red, fz.dot_part, ys,
+                                     vec0);
   } else {
     // y = H x - beta prev and the block's partial of Re <x|H x>, reduced in the original row
     // order (the regrouped accumulators' storage holds the rows' terms)
@@ -902,7 +935,7 @@ __global__ void __launch_bounds__(256, NV == 1 ? QG_APPLY_MIN_BLOCKS : 1)
       dvs[k] = dv;
     }
     if (QG_LIST_REGROUP) __syncthreads();  // every regrouped accumulator has been read
-    fused_dot_partials<NV>(dvs, me, reinterpret_cast<double *>(&s_acc[0][0]), s_red, fz.dot_part, ys, vec0);
+    fused_dot_partials<NV, false>(dvs, me, reinterpret_cast<double *>(&s_acc[0][0]), s_red, fz.dot_part, ys, vec0);
   }
 }
 
@@ -1711,6 +1744,9 @@ static void launch_apply_list_t(qg_context ctx, const OpBasisCache *c, const dou
     else
       k_apply_list<W, 1, false, false, true><<<grid, 256, 0, ctx->stream>>>(keys, dst->n, c->d_cptr, c->d_conn,
                                                                          c->d_coef, diag, x, xs, y, ys, vec0, fz, lv);
+  } else if (FUSE && fz.split) {  // real operators only (the caller checks)
+    k_apply_list<W, NV, true, true, false, true><<<grid, 256, 0, ctx->stream>>>(
+        keys, dst->n, c->d_cptr, c->d_conn, c->d_coef, diag, x, xs, y, ys, vec0, fz, lv);
   } else if (real) {
     k_apply_list<W, NV, FUSE, true><<<grid, 256, 0, ctx->stream>>>(keys, dst->n, c->d_cptr, c->d_conn, c->d_coef,
                                                                    diag, x, xs, y, ys, vec0, fz, lv);
@@ -1913,6 +1949,8 @@ static bool op_values_real(qg_operator op) {
     if (h.im != 0.0) return false;
   return true;
 }
+
+bool qg_operator_values_real(qg_operator op) { return op_values_real(op); }
 
 static int tuned_chunk(const OpBasisCache *c, int nvec) {
   if (c)

@@ -97,6 +97,7 @@ struct qg_context_s {
   bool autotune = true;               // time the vectors-per-pass choices of multi-vector applies
   bool conn_lists = true;             // resolve hashed connections once per (operator, basis)
   bool small_lanczos = true;          // persistent one-block-per-chain Lanczos on small bases
+  bool split_chains = true;           // real Lanczos chains of a real operator two per vector
 };
 
 // A term table in one device allocation: ngroups GroupDev followed by nterms TermDev.
@@ -335,8 +336,11 @@ void qg_cache_free(OpBasisCache &c);
 //   dot_part:   per-block partial sums of conj(x_r) * (H x)_r.
 struct ApplyFuse {
   const double2 *prev = nullptr;
-  const double *beta = nullptr;  // [nvec]
+  const double *beta = nullptr;  // [nvec], or [2 nvec] when split
   double2 *dot_part = nullptr;   // [gridDim.x * nvec]
+  // two real Lanczos chains per complex vector (real and imaginary parts, a real operator):
+  // each part has its own beta and its own dot partial (.x and .y of dot_part)
+  int split = 0;
 };
 qg_status qg_apply_launch(qg_context ctx, qg_operator op, qg_basis dst, qg_basis src, const double *x, double *y,
                           int nvec, const ApplyFuse *fz);
@@ -352,6 +356,8 @@ int qg_apply_grid(qg_basis dst);
 // True when the same-basis apply of op on b gathers through connection lists (builds the
 // per-(operator, basis) cache first), so a caller need not pack x into the hash slots.
 bool qg_apply_uses_lists(qg_operator op, qg_basis b);
+// every current value of the operator is real
+bool qg_operator_values_real(qg_operator op);
 
 // Hermitian eigenproblems on the device (qgpu_jacobi.cu): A (k x k row-major, device,
 // overwritten) -> eigenvalues ascending (w_dev, k) and the lowest nv eigenvectors as the columns

@@ -13,6 +13,7 @@
 // the truncation on the fly, writes the stored Krylov vector, forms <v_i|H v_i> partials and
 // the three-term update in its epilogue.  Two single-block kernels finish the reductions so
 // the scalars stay on the device; the host reads a and b once at the end.
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -127,6 +128,57 @@ __global__ void k_reduce_partials(const double2 *part, int nblk, int nvec, doubl
       out[k] = t;
     }
     __syncthreads();
+  }
+}
+
+// Norm partials of the two parts of every vector (split Lanczos chains) in the orders of the
+// kernels above for one part: .x the real parts, .y the imaginary parts.
+__global__ void k_norm_partial_split(int64_t n, int nvec, const double2 *__restrict__ x, double2 *part) {
+  extern __shared__ double2 sh[];
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int k = 0; k < nvec; k++) {
+    double2 s = make_double2(0.0, 0.0);
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+      double2 a = x[r * nvec + k];
+      s.x += __dmul_rn(a.x, a.x);  // each product rounded alone, as in one chain
+      s.y += __dmul_rn(a.y, a.y);
+    }
+    for (int o = 16; o; o >>= 1) {
+      s.x += __shfl_xor_sync(0xffffffffu, s.x, o);
+      s.y += __shfl_xor_sync(0xffffffffu, s.y, o);
+    }
+    if (lane == 0) sh[wid] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double2 t = make_double2(0.0, 0.0);
+      for (int w = 0; w < nw; w++) {
+        t.x += sh[w].x;
+        t.y += sh[w].y;
+      }
+      part[blockIdx.x * nvec + k] = t;
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void k_norm_partial_split_flat(int64_t len, int nvec, const double2 *__restrict__ x, double2 *part) {
+  extern __shared__ double2 sh[];
+  int tid = threadIdx.x, T = blockDim.x;
+  double2 s = make_double2(0.0, 0.0);
+  for (int64_t i = blockIdx.x * (int64_t)T + tid; i < len; i += (int64_t)gridDim.x * T) {
+    double2 a = x[i];
+    s.x += __dmul_rn(a.x, a.x);
+    s.y += __dmul_rn(a.y, a.y);
+  }
+  sh[tid] = s;
+  __syncthreads();
+  if (tid < nvec) {
+    double2 t = make_double2(0.0, 0.0);
+    for (int j = tid; j < T; j += nvec) {
+      t.x += sh[j].x;
+      t.y += sh[j].y;
+    }
+    part[blockIdx.x * nvec + tid] = t;
   }
 }
 
@@ -273,20 +325,81 @@ __global__ void k_lanczos_axpy_norm_flat(int64_t len, int nvec, const double2 *_
   }
 }
 
+// The same for split chains: part k.x of every row with a[2k], part k.y with a[2k + 1]; the
+// norm partials per part (.x, .y), each in its one-part kernel's order and arithmetic.
+__global__ void k_lanczos_axpy_norm_split(int64_t n, int nvec, const double2 *__restrict__ w,
+                                          const double2 *__restrict__ vp, const double *__restrict__ a,
+                                          double2 *__restrict__ v, double2 *part, int *step) {
+  extern __shared__ double2 sh[];
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if (blockIdx.x == 0 && threadIdx.x == 0) *step += 1;  // the step this kernel opens
+  for (int k = 0; k < nvec; k++) {
+    const double aa = a[2 * k], ab = a[2 * k + 1];
+    double sa = 0.0, sb = 0.0;
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+      double2 wv = w[r * nvec + k], pv = vp[r * nvec + k];
+      double2 o = make_double2(fma(-aa, pv.x, wv.x), fma(-ab, pv.y, wv.y));
+      v[r * nvec + k] = o;
+      sa += __dmul_rn(o.x, o.x);
+      sb += __dmul_rn(o.y, o.y);
+    }
+    for (int o = 16; o; o >>= 1) {
+      sa += __shfl_xor_sync(0xffffffffu, sa, o);
+      sb += __shfl_xor_sync(0xffffffffu, sb, o);
+    }
+    if (lane == 0) sh[wid] = make_double2(sa, sb);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double ta = 0, tb = 0;
+      for (int w2 = 0; w2 < nw; w2++) ta += sh[w2].x;
+      for (int w2 = 0; w2 < nw; w2++) tb += sh[w2].y;
+      part[blockIdx.x * nvec + k] = make_double2(ta, tb);
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void k_lanczos_axpy_norm_split_flat(int64_t len, int nvec, const double2 *__restrict__ w,
+                                               const double2 *__restrict__ vp, const double *__restrict__ a,
+                                               double2 *__restrict__ v, double2 *part, int *step) {
+  extern __shared__ double2 sh[];
+  int tid = threadIdx.x, T = blockDim.x;
+  if (blockIdx.x == 0 && tid == 0) *step += 1;  // the step this kernel opens
+  const double aa = a[2 * (tid % nvec)], ab = a[2 * (tid % nvec) + 1];
+  double sa = 0.0, sb = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)T + tid; i < len; i += (int64_t)gridDim.x * T) {
+    double2 wv = w[i], pv = vp[i];
+    double2 o = make_double2(fma(-aa, pv.x, wv.x), fma(-ab, pv.y, wv.y));
+    v[i] = o;
+    sa += __dmul_rn(o.x, o.x);
+    sb += __dmul_rn(o.y, o.y);
+  }
+  sh[tid] = make_double2(sa, sb);
+  __syncthreads();
+  if (tid < nvec) {
+    double ta = 0, tb = 0;
+    for (int j = tid; j < T; j += nvec) ta += sh[j].x;
+    for (int j = tid; j < T; j += nvec) tb += sh[j].y;
+    part[blockIdx.x * nvec + tid] = make_double2(ta, tb);
+  }
+}
+
 // Sum of the .x parts of vector k's partials in a fixed order, by one block: threads over the
 // partials with four independent accumulators (so a thread's loads overlap instead of waiting
 // on one another), a shuffle tree, then the warps' sums in order.  The total on thread 0.
-__device__ double fin_sum(const double2 *__restrict__ part, int nblk, int nvec, int k, double *sh) {
+// c: 0 sums the .x parts, 1 the .y parts (the second chain of a split vector)
+__device__ double fin_sum(const double2 *__restrict__ part, int nblk, int nvec, int k, double *sh, int c = 0) {
   const int T = blockDim.x, lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const double *pd = reinterpret_cast<const double *>(part) + c;
   double s0 = 0, s1 = 0, s2 = 0, s3 = 0;
   int b = threadIdx.x;
   for (; b + 3 * T < nblk; b += 4 * T) {
-    s0 += part[(int64_t)b * nvec + k].x;
-    s1 += part[(int64_t)(b + T) * nvec + k].x;
-    s2 += part[(int64_t)(b + 2 * T) * nvec + k].x;
-    s3 += part[(int64_t)(b + 3 * T) * nvec + k].x;
+    s0 += pd[2 * ((int64_t)b * nvec + k)];
+    s1 += pd[2 * ((int64_t)(b + T) * nvec + k)];
+    s2 += pd[2 * ((int64_t)(b + 2 * T) * nvec + k)];
+    s3 += pd[2 * ((int64_t)(b + 3 * T) * nvec + k)];
   }
-  for (; b < nblk; b += T) s0 += part[(int64_t)b * nvec + k].x;
+  for (; b < nblk; b += T) s0 += pd[2 * ((int64_t)b * nvec + k)];
   double s = (s0 + s1) + (s2 + s3);
   for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
   if (lane == 0) sh[wid] = s;
@@ -299,16 +412,16 @@ __device__ double fin_sum(const double2 *__restrict__ part, int nblk, int nvec, 
 
 #define QG_FIN_THREADS 512
 
-// a[k] <- Re(sum of dot partials), one block per vector; also stores a into the history at
+// a[k] <- Re(sum of dot partials), one block per chain; also stores a into the history at
 // column *step + 1.  The step counter is advanced by the next step's first kernel
 // (k_lanczos_axpy_norm*), after every block here has read it, so a captured step can be
-// replayed.
+// replayed.  split: chain k is part k & 1 of vector k >> 1.
 __global__ void __launch_bounds__(QG_FIN_THREADS) k_fin_a(const double2 *part, int nblk, int nvec, double *a_now,
-                                                          double *a_hist, int stride, const int *step) {
+                                                          double *a_hist, int stride, const int *step, int split) {
   __shared__ double sh[32];
   const int k = blockIdx.x;
   const int col = *step + 1;
-  double t = fin_sum(part, nblk, nvec, k, sh);
+  double t = split ? fin_sum(part, nblk, nvec, k >> 1, sh, k & 1) : fin_sum(part, nblk, nvec, k, sh);
   if (threadIdx.x == 0) {
     a_now[k] = t;
     a_hist[k * stride + col] = t;
@@ -321,11 +434,11 @@ __global__ void __launch_bounds__(QG_FIN_THREADS) k_fin_a(const double2 *part, i
 __global__ void __launch_bounds__(QG_FIN_THREADS) k_fin_b(const double2 *part, int nblk, int nvec, double *b_now,
                                                           double *b_hist, int stride, const int *step, double *scale,
                                                           double *thr2, double *err, double eps, double gamma,
-                                                          int first) {
+                                                          int first, int split) {
   __shared__ double sh[32];
   const int k = blockIdx.x;
   const int col = *step;
-  double t = fin_sum(part, nblk, nvec, k, sh);
+  double t = split ? fin_sum(part, nblk, nvec, k >> 1, sh, k & 1) : fin_sum(part, nblk, nvec, k, sh);
   if (threadIdx.x == 0) {
     double b, sc, th2, e = first ? 1.0 : err[k];
     qg_lanczos_norm_scalars(t, first != 0, eps, gamma, b, sc, th2, e);
@@ -348,6 +461,21 @@ __global__ void k_scale_trunc(int64_t n, int nvec, const double2 *__restrict__ v
   v.x *= sc;
   v.y *= sc;
   if (!(qg_norm2(v) > thr2[k])) v = make_double2(0.0, 0.0);
+  vout[i] = v;
+}
+
+// split chains: part .x with scale[2k], thr2[2k]; part .y with scale[2k + 1], thr2[2k + 1]
+__global__ void k_scale_trunc_split(int64_t n, int nvec, const double2 *__restrict__ vin,
+                                    const double *__restrict__ scale, const double *__restrict__ thr2,
+                                    double2 *__restrict__ vout) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n * nvec) return;
+  int k = (int)(i % nvec);
+  double2 v = vin[i];
+  v.x *= scale[2 * k];
+  v.y *= scale[2 * k + 1];
+  if (!(__dmul_rn(v.x, v.x) > thr2[2 * k])) v.x = 0.0;
+  if (!(__dmul_rn(v.y, v.y) > thr2[2 * k + 1])) v.y = 0.0;
   vout[i] = v;
 }
 
@@ -576,25 +704,15 @@ extern "C" qg_status qg_set_small_basis_lanczos(qg_context ctx, int32_t on) {
   return QG_OK;
 }
 
-extern "C" qg_status qg_lanczos_tridiag(qg_context ctx, qg_operator op, qg_basis b, const double *v0_dev, int32_t nvec,
-                                        int32_t ntri, double eps, double gamma, double *a_host, double *b_host,
-                                        double *krylov_dev) {
-  if (!ctx || !op || !b || !v0_dev || nvec <= 0 || ntri <= 0 || !a_host || !b_host || op->nf != b->nf) {
-    if (ctx) ctx->last_error = "qg_lanczos_tridiag: bad argument";
-    return QG_ERR_ARG;
-  }
+// The general path: nvec vectors of n rows, every step on the device.  split: each vector holds
+// two real chains (real and imaginary parts; a real operator with connection lists), chain
+// 2k + c being part c of vector k; the coefficients of 2 nvec chains come back.
+static qg_status lanczos_general(qg_context ctx, qg_operator op, qg_basis b, const double *v0_dev, int nvec,
+                                 int ntri, double eps, double gamma, double *a_host, double *b_host,
+                                 double *krylov_dev, int split) {
   cudaStream_t s = ctx->stream;
   int64_t n = b->n;
-  if (n == 0) {  // an empty start vector: every coefficient is zero (the spectrum vanishes)
-    for (int64_t k = 0; k < (int64_t)nvec * (ntri + 1); k++) a_host[k] = 0.0;
-    for (int64_t k = 0; k < (int64_t)nvec * ntri; k++) b_host[k] = 0.0;
-    return QG_OK;
-  }
-  {
-    bool done = false;
-    qg_status sst = lanczos_small(ctx, op, b, v0_dev, nvec, ntri, eps, gamma, a_host, b_host, krylov_dev, &done);
-    if (sst != QG_OK || done) return sst;
-  }
+  const int nchain = split ? 2 * nvec : nvec;
   int64_t len = n * nvec;  // complex entries per block vector
   int P = partial_blocks(ctx, n);
   int Papply = qg_apply_grid(b);
@@ -614,8 +732,8 @@ extern "C" qg_status qg_lanczos_tridiag(qg_context ctx, qg_operator op, qg_basis
   ALLOC(zero, vb);
   ALLOC(npart, (size_t)P * nvec * 16);
   ALLOC(dpart, (size_t)Papply * nvec * 16);
-  // the scalars, then one slot for the device step counter (zeroed with them)
-  size_t nscal = 6 * (size_t)nvec + (size_t)nvec * (ntri + 1) + (size_t)nvec * ntri + 1;
+  // the scalars (one per chain), then one slot for the device step counter (zeroed with them)
+  size_t nscal = 6 * (size_t)nchain + (size_t)nchain * (ntri + 1) + (size_t)nchain * ntri + 1;
   ALLOC(scal, nscal * 8);
 #undef ALLOC
   if (e != cudaSuccess) {
@@ -624,9 +742,9 @@ extern "C" qg_status qg_lanczos_tridiag(qg_context ctx, qg_operator op, qg_basis
     ctx->last_error = "qg_lanczos_tridiag: out of device memory";
     return QG_ERR_OOM;
   }
-  double *a_now = scal, *b_now = scal + nvec, *scale = scal + 2 * nvec, *thr2 = scal + 3 * nvec,
-         *err = scal + 4 * nvec, *zb = scal + 5 * nvec;
-  double *a_hist = scal + 6 * nvec, *b_hist = a_hist + (size_t)nvec * (ntri + 1);
+  double *a_now = scal, *b_now = scal + nchain, *scale = scal + 2 * nchain, *thr2 = scal + 3 * nchain,
+         *err = scal + 4 * nchain, *zb = scal + 5 * nchain;
+  double *a_hist = scal + 6 * nchain, *b_hist = a_hist + (size_t)nchain * (ntri + 1);
   int *step_ctr = reinterpret_cast<int *>(scal + nscal - 1);
   qg_status st = QG_OK;
   k_zero<<<(unsigned)((nscal + 255) / 256), 256, 0, s>>>(scal, (int64_t)nscal);
@@ -644,42 +762,60 @@ extern "C" qg_status qg_lanczos_tridiag(qg_context ctx, qg_operator op, qg_basis
   // the normalised, truncated Krylov vector vc from a raw vector: for one vector the same
   // kernel also writes it into the basis' hash slots for the gather
   // (with connection lists the apply gathers from vc itself and the slots are not needed)
-  const bool pack1 = nvec == 1 && !qg_apply_uses_lists(op, b);
+  const bool pack1 = !split && nvec == 1 && !qg_apply_uses_lists(op, b);
   auto normalise = [&](const double2 *raw) -> qg_status {
     if (pack1) return qg_pack(ctx, b, (const double *)raw, 1, scale, thr2, (double *)vc);
-    k_scale_trunc<<<(unsigned)((len + 255) / 256), 256, 0, s>>>(n, nvec, raw, scale, thr2, vc);
+    if (split)
+      k_scale_trunc_split<<<(unsigned)((len + 255) / 256), 256, 0, s>>>(n, nvec, raw, scale, thr2, vc);
+    else
+      k_scale_trunc<<<(unsigned)((len + 255) / 256), 256, 0, s>>>(n, nvec, raw, scale, thr2, vc);
     ctx->launches++;
     return qg_check_launch(ctx, "scale");
   };
   // step 0: b0 = |v0|, scale, threshold eps (err = 1)
-  launch_dot_partial(P, n, nvec, (const double2 *)v0_dev, nullptr, npart, s);
-  k_fin_b<<<nvec, QG_FIN_THREADS, 0, s>>>(npart, P, nvec, b_now, b_hist, ntri, step_ctr, scale, thr2, err, eps, gamma,
-                                         1);
+  if (split) {
+    int T = nvec > 1 ? flat_threads(nvec) : 0;
+    if (T)
+      k_norm_partial_split_flat<<<P, T, T * sizeof(double2), s>>>(len, nvec, (const double2 *)v0_dev, npart);
+    else
+      k_norm_partial_split<<<P, RBLK, (RBLK / 32) * sizeof(double2), s>>>(n, nvec, (const double2 *)v0_dev, npart);
+  } else {
+    launch_dot_partial(P, n, nvec, (const double2 *)v0_dev, nullptr, npart, s);
+  }
+  k_fin_b<<<nchain, QG_FIN_THREADS, 0, s>>>(npart, P, nvec, b_now, b_hist, ntri, step_ctr, scale, thr2, err, eps,
+                                           gamma, 1, split);
   ctx->launches += 2;
   st = qg_check_launch(ctx, "lanczos start norm");
   ApplyFuse fz;
   fz.prev = zero;
   fz.beta = zb;
   fz.dot_part = dpart;
+  fz.split = split;
   if (st == QG_OK) st = normalise((const double2 *)v0_dev);
   if (st == QG_OK)
     st = qg_apply_strided(ctx, op, b, b, (const double *)vc, nvec, (double *)w, nvec, nvec, &fz, pack1);
   if (st == QG_OK && krylov_dev)
     e = cudaMemcpyAsync(krylov_dev, vc, len * 16, cudaMemcpyDeviceToDevice, s);
   if (st == QG_OK) {
-    k_fin_a<<<nvec, QG_FIN_THREADS, 0, s>>>(dpart, Papply, nvec, a_now, a_hist, ntri + 1, step_ctr);
+    k_fin_a<<<nchain, QG_FIN_THREADS, 0, s>>>(dpart, Papply, nvec, a_now, a_hist, ntri + 1, step_ctr, split);
     ctx->launches++;
   }
   // one step: every scalar stays on the device
   auto step = [&](int i) -> qg_status {
     std::swap(vp, vc);  // vp = v_{i-1}
     int T = nvec > 1 ? flat_threads(nvec) : 0;
-    if (T)
+    if (split && T)
+      k_lanczos_axpy_norm_split_flat<<<P, T, T * sizeof(double2), s>>>(len, nvec, w, vp, a_now, vraw, npart,
+                                                                       step_ctr);
+    else if (split)
+      k_lanczos_axpy_norm_split<<<P, RBLK, (RBLK / 32) * sizeof(double2), s>>>(n, nvec, w, vp, a_now, vraw, npart,
+                                                                               step_ctr);
+    else if (T)
       k_lanczos_axpy_norm_flat<<<P, T, T * sizeof(double2), s>>>(len, nvec, w, vp, a_now, vraw, npart, step_ctr);
     else
       k_lanczos_axpy_norm<<<P, RBLK, (RBLK / 32) * sizeof(double2), s>>>(n, nvec, w, vp, a_now, vraw, npart, step_ctr);
-    k_fin_b<<<nvec, QG_FIN_THREADS, 0, s>>>(npart, P, nvec, b_now, b_hist, ntri, step_ctr, scale, thr2, err, eps,
-                                           gamma, 0);
+    k_fin_b<<<nchain, QG_FIN_THREADS, 0, s>>>(npart, P, nvec, b_now, b_hist, ntri, step_ctr, scale, thr2, err, eps,
+                                             gamma, 0, split);
     ctx->launches += 2;
     qg_status sst = normalise(vraw);
     if (sst != QG_OK) return sst;
@@ -691,7 +827,7 @@ extern "C" qg_status qg_lanczos_tridiag(qg_context ctx, qg_operator op, qg_basis
       cudaError_t ce = cudaMemcpyAsync(krylov_dev + 2 * (size_t)i * len, vc, len * 16, cudaMemcpyDeviceToDevice, s);
       if (ce != cudaSuccess) return qg_cuda_fail(ctx, ce, "krylov copy");
     }
-    k_fin_a<<<nvec, QG_FIN_THREADS, 0, s>>>(dpart, Papply, nvec, a_now, a_hist, ntri + 1, step_ctr);
+    k_fin_a<<<nchain, QG_FIN_THREADS, 0, s>>>(dpart, Papply, nvec, a_now, a_hist, ntri + 1, step_ctr, split);
     ctx->launches++;
     return sst;
   };
@@ -738,8 +874,8 @@ extern "C" qg_status qg_lanczos_tridiag(qg_context ctx, qg_operator op, qg_basis
   }
   for (int i = 1; !graphed && i < ntri && st == QG_OK && e == cudaSuccess; i++) st = step(i);
   if (st == QG_OK && e == cudaSuccess) {
-    e = cudaMemcpyAsync(a_host, a_hist, (size_t)nvec * (ntri + 1) * 8, cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(b_host, b_hist, (size_t)nvec * ntri * 8, cudaMemcpyDeviceToHost, s);
+    e = cudaMemcpyAsync(a_host, a_hist, (size_t)nchain * (ntri + 1) * 8, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(b_host, b_hist, (size_t)nchain * ntri * 8, cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   }
   if (e != cudaSuccess && st == QG_OK) st = qg_cuda_fail(ctx, e, "qg_lanczos_tridiag");
@@ -747,10 +883,161 @@ extern "C" qg_status qg_lanczos_tridiag(qg_context ctx, qg_operator op, qg_basis
   cudaFree(vp); cudaFree(vc); cudaFree(w); cudaFree(w2); cudaFree(vraw); cudaFree(zero);
   cudaFree(npart); cudaFree(dpart); cudaFree(scal);
   if (st == QG_OK) {
-    for (int k = 0; k < nvec; k++) a_host[k * (ntri + 1)] = 0.0;
+    for (int k = 0; k < nchain; k++) a_host[k * (ntri + 1)] = 0.0;
     st = qg_check_device_error(ctx, "qg_lanczos_tridiag");
   }
   return st;
+}
+
+// per column k of v (n x nvec): flags[2k] set when a real part is non-zero, flags[2k + 1] when an
+// imaginary part is
+__global__ void k_column_parts(int64_t n, int nvec, const double2 *__restrict__ v, unsigned int *flags) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n * nvec) return;
+  const double2 a = v[i];
+  const int k = (int)(i % nvec);
+  if (a.x != 0.0) atomicOr(flags + 2 * k, 1u);
+  if (a.y != 0.0) atomicOr(flags + 2 * k + 1, 1u);
+}
+
+// out (n x nout): column j takes part part[j] (0 real, 1 imaginary, -1 zero) of column src[j]
+// of v into its real part, and part part2[j] of column src2[j] into its imaginary part
+// (split pairs); with src2 null, whole columns (complex) are copied.
+__global__ void k_pack_columns(int64_t n, int nvec, const double2 *__restrict__ v, int nout, const int *src,
+                               const int *part, const int *src2, const int *part2, double2 *__restrict__ out) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n * nout) return;
+  const int64_t r = i / nout;
+  const int j = (int)(i % nout);
+  const double2 a = v[r * nvec + src[j]];
+  if (!src2) {
+    out[i] = a;
+    return;
+  }
+  const double re = part[j] == 0 ? a.x : part[j] == 1 ? a.y : 0.0;
+  double im = 0.0;
+  if (part2[j] >= 0) {
+    const double2 c = v[r * nvec + src2[j]];
+    im = part2[j] == 0 ? c.x : c.y;
+  }
+  out[i] = make_double2(re, im);
+}
+
+extern "C" qg_status qg_lanczos_tridiag(qg_context ctx, qg_operator op, qg_basis b, const double *v0_dev, int32_t nvec,
+                                        int32_t ntri, double eps, double gamma, double *a_host, double *b_host,
+                                        double *krylov_dev) {
+  if (!ctx || !op || !b || !v0_dev || nvec <= 0 || ntri <= 0 || !a_host || !b_host || op->nf != b->nf) {
+    if (ctx) ctx->last_error = "qg_lanczos_tridiag: bad argument";
+    return QG_ERR_ARG;
+  }
+  cudaStream_t s = ctx->stream;
+  int64_t n = b->n;
+  if (n == 0) {  // an empty start vector: every coefficient is zero (the spectrum vanishes)
+    for (int64_t k = 0; k < (int64_t)nvec * (ntri + 1); k++) a_host[k] = 0.0;
+    for (int64_t k = 0; k < (int64_t)nvec * ntri; k++) b_host[k] = 0.0;
+    return QG_OK;
+  }
+  {
+    bool done = false;
+    qg_status sst = lanczos_small(ctx, op, b, v0_dev, nvec, ntri, eps, gamma, a_host, b_host, krylov_dev, &done);
+    if (sst != QG_OK || done) return sst;
+  }
+  // Real chains in pairs.  With a real operator a start vector whose imaginary (or real) part
+  // is zero stays so, and two such chains share one complex vector: one apply serves both, so
+  // each costs half.  A purely imaginary vector has the coefficients of its imaginary part.
+  // Each part is updated with exactly the arithmetic of its chain run alone; with one pair the
+  // reductions run in the same order too and the coefficients are bitwise those of the runs
+  // alone, with more pairs the multi-vector reductions add in another order (rounding only).
+  if (ctx->split_chains && nvec >= 2 && !krylov_dev && qg_operator_values_real(op) && qg_apply_uses_lists(op, b)) {
+    unsigned int *d_flags = nullptr;
+    std::vector<unsigned int> fl(2 * (size_t)nvec, 0u);
+    cudaError_t e = cudaMalloc(&d_flags, fl.size() * sizeof(unsigned int));
+    if (e == cudaSuccess) e = cudaMemsetAsync(d_flags, 0, fl.size() * sizeof(unsigned int), s);
+    if (e == cudaSuccess) {
+      k_column_parts<<<(unsigned)((n * nvec + 255) / 256), 256, 0, s>>>(n, nvec, (const double2 *)v0_dev, d_flags);
+      ctx->launches++;
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(fl.data(), d_flags, fl.size() * sizeof(unsigned int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFree(d_flags);
+    if (e != cudaSuccess) return qg_cuda_fail(ctx, e, "qg_lanczos_tridiag");
+    std::vector<int> rcol, rpart, ccol;  // real chains (column, part) and complex columns
+    for (int k = 0; k < nvec; k++) {
+      if (fl[2 * k] && fl[2 * k + 1]) {
+        ccol.push_back(k);
+      } else {
+        rcol.push_back(k);
+        rpart.push_back(fl[2 * k + 1] ? 1 : 0);
+      }
+    }
+    if (rcol.size() >= 2) {
+      const int np = (int)(rcol.size() + 1) / 2, nc = (int)ccol.size();
+      std::vector<int> sa(np), pa(np), sb(np), pb(np);
+      for (int j = 0; j < np; j++) {
+        sa[j] = rcol[2 * j];
+        pa[j] = rpart[2 * j];
+        const bool has = 2 * j + 1 < (int)rcol.size();
+        sb[j] = has ? rcol[2 * j + 1] : 0;
+        pb[j] = has ? rpart[2 * j + 1] : -1;  // an odd chain out pairs with an empty one
+      }
+      int *d_idx = nullptr;
+      double2 *zp = nullptr, *zc = nullptr;
+      const int ni = 4 * np + nc;
+      std::vector<int> idx;
+      idx.insert(idx.end(), sa.begin(), sa.end());
+      idx.insert(idx.end(), pa.begin(), pa.end());
+      idx.insert(idx.end(), sb.begin(), sb.end());
+      idx.insert(idx.end(), pb.begin(), pb.end());
+      idx.insert(idx.end(), ccol.begin(), ccol.end());
+      e = cudaMalloc(&d_idx, (size_t)ni * sizeof(int));
+      if (e == cudaSuccess) e = cudaMemcpyAsync(d_idx, idx.data(), (size_t)ni * sizeof(int), cudaMemcpyHostToDevice, s);
+      if (e == cudaSuccess) e = cudaMalloc(&zp, (size_t)n * np * sizeof(double2));
+      if (e == cudaSuccess && nc) e = cudaMalloc(&zc, (size_t)n * nc * sizeof(double2));
+      if (e == cudaSuccess) {
+        k_pack_columns<<<(unsigned)((n * np + 255) / 256), 256, 0, s>>>(n, nvec, (const double2 *)v0_dev, np, d_idx,
+                                                                       d_idx + np, d_idx + 2 * np, d_idx + 3 * np, zp);
+        if (nc)
+          k_pack_columns<<<(unsigned)((n * nc + 255) / 256), 256, 0, s>>>(n, nvec, (const double2 *)v0_dev, nc,
+                                                                         d_idx + 4 * np, nullptr, nullptr, nullptr,
+                                                                         zc);
+        ctx->launches += nc ? 2 : 1;
+        e = cudaGetLastError();
+      }
+      qg_status st = e == cudaSuccess ? QG_OK : qg_cuda_fail(ctx, e, "qg_lanczos_tridiag");
+      std::vector<double> ah((size_t)2 * np * (ntri + 1)), bh((size_t)2 * np * ntri);
+      if (st == QG_OK)
+        st = lanczos_general(ctx, op, b, (const double *)zp, np, ntri, eps, gamma, ah.data(), bh.data(), nullptr, 1);
+      if (st == QG_OK) {
+        for (size_t q = 0; q < rcol.size(); q++) {
+          std::copy(ah.begin() + q * (ntri + 1), ah.begin() + (q + 1) * (ntri + 1), a_host + (size_t)rcol[q] * (ntri + 1));
+          std::copy(bh.begin() + q * ntri, bh.begin() + (q + 1) * ntri, b_host + (size_t)rcol[q] * ntri);
+        }
+      }
+      if (st == QG_OK && nc) {
+        std::vector<double> ac((size_t)nc * (ntri + 1)), bc((size_t)nc * ntri);
+        st = lanczos_general(ctx, op, b, (const double *)zc, nc, ntri, eps, gamma, ac.data(), bc.data(), nullptr, 0);
+        if (st == QG_OK)
+          for (int q = 0; q < nc; q++) {
+            std::copy(ac.begin() + (size_t)q * (ntri + 1), ac.begin() + (size_t)(q + 1) * (ntri + 1),
+                      a_host + (size_t)ccol[q] * (ntri + 1));
+            std::copy(bc.begin() + (size_t)q * ntri, bc.begin() + (size_t)(q + 1) * ntri, b_host + (size_t)ccol[q] * ntri);
+          }
+      }
+      cudaStreamSynchronize(s);
+      cudaFree(d_idx);
+      cudaFree(zp);
+      cudaFree(zc);
+      return st;
+    }
+  }
+  return lanczos_general(ctx, op, b, v0_dev, nvec, ntri, eps, gamma, a_host, b_host, krylov_dev, 0);
+}
+
+extern "C" qg_status qg_set_split_chains(qg_context ctx, int32_t on) {
+  if (!ctx) return QG_ERR_ARG;
+  ctx->split_chains = on != 0;
+  return QG_OK;
 }
 
 // ------------------------------------------------------------------ continued fraction

@@ -68,6 +68,7 @@ def load(path=LIB_PATH):
         "qg_apply_set_chunk": (C.c_int, [P, P, P, I32, I32]),
         "qg_set_connection_lists": (C.c_int, [P, I32]),
         "qg_set_small_basis_lanczos": (C.c_int, [P, I32]),
+        "qg_set_split_chains": (C.c_int, [P, I32]),
         "qg_apply_list_info": (C.c_int, [P, P, P, P, P]),
         "qg_apply_fp64_ops": (C.c_int, [P, P, P, P]),
         "qg_expectation": (C.c_int, [P, P, P, P, I32, P]),
