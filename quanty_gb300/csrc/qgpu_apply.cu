@@ -763,9 +763,20 @@ static_assert(sizeof(LocalEntry) == 32 && offsetof(LocalEntry, tend) == 4 && off
 // coefficients), so each connection is two FMAs and no imaginary part is read or tested.  The
 // general form's per-connection test of the imaginary part compiles to predicated FMAs, which
 // hold the FP64 pipe whether or not they take effect; a real operator would pay for all four.
+// acc += v x[idx] for a real value v: RV, x holds one real number per row (a real vector; the
+// products a complex vector with a zero imaginary part would form, without the zero half)
+template <bool RV>
+__device__ __forceinline__ void acc_real_term(double2 &acc, double v, const double2 *__restrict__ x, int64_t idx) {
+  if (RV)
+    acc.x = fma(v, __ldg(reinterpret_cast<const double *>(x) + idx), acc.x);
+  else
+    qg_cmac(acc, v, 0.0, false, __ldg(x + idx));
+}
+
 // ORD: y is host memory (see the store at the end).  SPLIT (with FUSE and REAL): each complex
-// vector carries two real Lanczos chains, its real and imaginary parts.
-template <int W, int NV, bool FUSE, bool REAL, bool ORD = false, bool SPLIT = false>
+// vector carries two real Lanczos chains, its real and imaginary parts.  RV (with FUSE, REAL
+// and NV = 1): x, y and prev hold one real number per row.
+template <int W, int NV, bool FUSE, bool REAL, bool ORD = false, bool SPLIT = false, bool RV = false>
 __global__ void __launch_bounds__(256, NV == 1 ? QG_APPLY_MIN_BLOCKS : 1)
     k_apply_list(const Key<W> *__restrict__ rows, int64_t n_rows, const int64_t *__restrict__ cptr,
                  const uint2 *__restrict__ conn, const double2 *__restrict__ coef, const double2 *__restrict__ diag,
@@ -783,7 +794,9 @@ __global__ void __launch_bounds__(256, NV == 1 ? QG_APPLY_MIN_BLOCKS : 1)
       const double2 dg = diag[r];
       const bool dgc = !REAL && qg_is_nonzero(dg.y);
 #pragma unroll
-      for (int k = 0; k < NV; k++) acc[k] = qg_diag_mul(dg, x[r * xs + vec0 + k], dgc);
+      for (int k = 0; k < NV; k++)
+        acc[k] = RV ? make_double2(dg.x * reinterpret_cast<const double *>(x)[r], 0.0)
+                    : qg_diag_mul(dg, x[r * xs + vec0 + k], dgc);
     }
     p = __ldg(cptr + r);
     pe = __ldg(cptr + r + 1);
@@ -809,7 +822,7 @@ __global__ void __launch_bounds__(256, NV == 1 ? QG_APPLY_MIN_BLOCKS : 1)
         if (REAL) {
           const double v = __ldg(&E->vre);
 #pragma unroll
-          for (int k = 0; k < NV; k++) qg_cmac(acc[k], v, 0.0, false, __ldg(x + j * xs + vec0 + k));
+          for (int k = 0; k < NV; k++) acc_real_term<RV>(acc[k], v, x, j * xs + vec0 + k);
         } else {
           const double2 v = __ldg(reinterpret_cast<const double2 *>(&E->vre));
           bool cplx = qg_is_nonzero(v.y);
@@ -869,7 +882,7 @@ __global__ void __launch_bounds__(256, NV == 1 ? QG_APPLY_MIN_BLOCKS : 1)
       if (REAL) {
         double vr = qg_flip_sign(__ldg(&coef[cn.y & 0x7FFFFFFFu].x), par);
 #pragma unroll
-        for (int k = 0; k < NV; k++) qg_cmac(acc[k], vr, 0.0, false, __ldg(x + j * xs + vec0 + k));
+        for (int k = 0; k < NV; k++) acc_real_term<RV>(acc[k], vr, x, j * xs + vec0 + k);
       } else {
         double2 cf = __ldg(coef + (cn.y & 0x7FFFFFFFu));
         bool cplx = qg_is_nonzero(cf.y);
@@ -897,6 +910,18 @@ __global__ void __launch_bounds__(256, NV == 1 ? QG_APPLY_MIN_BLOCKS : 1)
 #pragma unroll
       for (int k = 0; k < NV; k++) y[r * ys + vec0 + k] = acc[k];
     }
+  } else if (RV) {
+    // one real chain: y = H x - beta prev and the partial of <x|H x>, the arithmetic of the
+    // real part of a complex chain whose imaginary part is zero
+    __shared__ double s_red[8];
+    double dvs[1] = {0.0};
+    if (live) {
+      const double xv = reinterpret_cast<const double *>(x)[r], pv = reinterpret_cast<const double *>(fz.prev)[r];
+      dvs[0] = __dmul_rn(xv, acc[0].x);
+      reinterpret_cast<double *>(y)[r] = fma(-fz.beta[0], pv, acc[0].x);
+    }
+    if (QG_LIST_REGROUP) __syncthreads();  // every regrouped accumulator has been read
+    fused_dot_partials<1, false>(dvs, me, reinterpret_cast<double *>(&s_acc[0][0]), s_red, fz.dot_part, ys, vec0);
   } else if (SPLIT) {
     // two real chains per vector: the real operator keeps the parts apart, so each part is
     // updated and reduced with exactly the arithmetic of its chain run alone (a zero
@@ -1744,6 +1769,9 @@ static void launch_apply_list_t(qg_context ctx, const OpBasisCache *c, const dou
     else
       k_apply_list<W, 1, false, false, true><<<grid, 256, 0, ctx->stream>>>(keys, dst->n, c->d_cptr, c->d_conn,
                                                                          c->d_coef, diag, x, xs, y, ys, vec0, fz, lv);
+  } else if (NV == 1 && FUSE && fz.real_vector) {  // real operators only (the caller checks)
+    k_apply_list<W, 1, true, true, false, false, true><<<grid, 256, 0, ctx->stream>>>(
+        keys, dst->n, c->d_cptr, c->d_conn, c->d_coef, diag, x, xs, y, ys, vec0, fz, lv);
   } else if (FUSE && fz.split) {  // real operators only (the caller checks)
     k_apply_list<W, NV, true, true, false, true><<<grid, 256, 0, ctx->stream>>>(
         keys, dst->n, c->d_cptr, c->d_conn, c->d_coef, diag, x, xs, y, ys, vec0, fz, lv);

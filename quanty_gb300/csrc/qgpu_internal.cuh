@@ -341,6 +341,8 @@ struct ApplyFuse {
   // two real Lanczos chains per complex vector (real and imaginary parts, a real operator):
   // each part has its own beta and its own dot partial (.x and .y of dot_part)
   int split = 0;
+  // one real chain (a real operator, nvec 1): x, y and prev hold one real number per row
+  int real_vector = 0;
 };
 qg_status qg_apply_launch(qg_context ctx, qg_operator op, qg_basis dst, qg_basis src, const double *x, double *y,
                           int nvec, const ApplyFuse *fz);

@@ -479,6 +479,63 @@ __global__ void k_scale_trunc_split(int64_t n, int nvec, const double2 *__restri
   vout[i] = v;
 }
 
+// One real chain (x one real number per row): the start norm, the axpy with its norm and the
+// scaling with truncation, each in the order and arithmetic its complex kernel above uses for
+// a vector whose imaginary part is zero.
+__global__ void k_norm_partial_real(int64_t n, const double *__restrict__ x, double2 *part) {
+  __shared__ double sh[32];
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  double s = 0.0;
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x)
+    s += __dmul_rn(x[r], x[r]);
+  for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) sh[wid] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < nw; w++) t += sh[w];
+    part[blockIdx.x] = make_double2(t, 0.0);
+  }
+}
+
+__global__ void k_lanczos_axpy_norm_real(int64_t n, const double *__restrict__ w, const double *__restrict__ vp,
+                                         const double *__restrict__ a, double *__restrict__ v, double2 *part,
+                                         int *step) {
+  __shared__ double sh[32];
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if (blockIdx.x == 0 && threadIdx.x == 0) *step += 1;  // the step this kernel opens
+  const double ak = a[0];
+  double s = 0.0;
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    const double o = fma(-ak, vp[r], w[r]);
+    v[r] = o;
+    s += __dmul_rn(o, o);
+  }
+  for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) sh[wid] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0;
+    for (int w2 = 0; w2 < nw; w2++) t += sh[w2];
+    part[blockIdx.x] = make_double2(t, 0.0);
+  }
+}
+
+__global__ void k_scale_trunc_real(int64_t n, const double *__restrict__ vin, const double *__restrict__ scale,
+                                   const double *__restrict__ thr2, double *__restrict__ vout) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double v = vin[i] * scale[0];
+  if (!(__dmul_rn(v, v) > thr2[0])) v = 0.0;
+  vout[i] = v;
+}
+
+// out[r] = part c (0 real, 1 imaginary) of v[r]
+__global__ void k_take_part(int64_t n, const double2 *__restrict__ v, int c, double *__restrict__ out) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) out[i] = c ? v[i].y : v[i].x;
+}
+
 __global__ void k_zero(double *p, int64_t n) {
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i < n) p[i] = 0.0;
@@ -707,9 +764,10 @@ extern "C" qg_status qg_set_small_basis_lanczos(qg_context ctx, int32_t on) {
 // The general path: nvec vectors of n rows, every step on the device.  split: each vector holds
 // two real chains (real and imaginary parts; a real operator with connection lists), chain
 // 2k + c being part c of vector k; the coefficients of 2 nvec chains come back.
+// rv: one real chain, v0_dev one real number per row (nvec 1).
 static qg_status lanczos_general(qg_context ctx, qg_operator op, qg_basis b, const double *v0_dev, int nvec,
                                  int ntri, double eps, double gamma, double *a_host, double *b_host,
-                                 double *krylov_dev, int split) {
+                                 double *krylov_dev, int split, int rv = 0) {
   cudaStream_t s = ctx->stream;
   int64_t n = b->n;
   const int nchain = split ? 2 * nvec : nvec;
@@ -762,10 +820,13 @@ static qg_status lanczos_general(qg_context ctx, qg_operator op, qg_basis b, con
   // the normalised, truncated Krylov vector vc from a raw vector: for one vector the same
   // kernel also writes it into the basis' hash slots for the gather
   // (with connection lists the apply gathers from vc itself and the slots are not needed)
-  const bool pack1 = !split && nvec == 1 && !qg_apply_uses_lists(op, b);
+  const bool pack1 = !split && !rv && nvec == 1 && !qg_apply_uses_lists(op, b);
   auto normalise = [&](const double2 *raw) -> qg_status {
     if (pack1) return qg_pack(ctx, b, (const double *)raw, 1, scale, thr2, (double *)vc);
-    if (split)
+    if (rv)
+      k_scale_trunc_real<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, (const double *)raw, scale, thr2,
+                                                                      (double *)vc);
+    else if (split)
       k_scale_trunc_split<<<(unsigned)((len + 255) / 256), 256, 0, s>>>(n, nvec, raw, scale, thr2, vc);
     else
       k_scale_trunc<<<(unsigned)((len + 255) / 256), 256, 0, s>>>(n, nvec, raw, scale, thr2, vc);
@@ -773,7 +834,9 @@ static qg_status lanczos_general(qg_context ctx, qg_operator op, qg_basis b, con
     return qg_check_launch(ctx, "scale");
   };
   // step 0: b0 = |v0|, scale, threshold eps (err = 1)
-  if (split) {
+  if (rv) {
+    k_norm_partial_real<<<P, RBLK, 0, s>>>(n, v0_dev, npart);
+  } else if (split) {
     int T = nvec > 1 ? flat_threads(nvec) : 0;
     if (T)
       k_norm_partial_split_flat<<<P, T, T * sizeof(double2), s>>>(len, nvec, (const double2 *)v0_dev, npart);
@@ -791,6 +854,7 @@ static qg_status lanczos_general(qg_context ctx, qg_operator op, qg_basis b, con
   fz.beta = zb;
   fz.dot_part = dpart;
   fz.split = split;
+  fz.real_vector = rv;
   if (st == QG_OK) st = normalise((const double2 *)v0_dev);
   if (st == QG_OK)
     st = qg_apply_strided(ctx, op, b, b, (const double *)vc, nvec, (double *)w, nvec, nvec, &fz, pack1);
@@ -804,7 +868,10 @@ static qg_status lanczos_general(qg_context ctx, qg_operator op, qg_basis b, con
   auto step = [&](int i) -> qg_status {
     std::swap(vp, vc);  // vp = v_{i-1}
     int T = nvec > 1 ? flat_threads(nvec) : 0;
-    if (split && T)
+    if (rv)
+      k_lanczos_axpy_norm_real<<<P, RBLK, 0, s>>>(n, (const double *)w, (const double *)vp, a_now, (double *)vraw,
+                                                  npart, step_ctr);
+    else if (split && T)
       k_lanczos_axpy_norm_split_flat<<<P, T, T * sizeof(double2), s>>>(len, nvec, w, vp, a_now, vraw, npart,
                                                                        step_ctr);
     else if (split)
@@ -942,13 +1009,13 @@ extern "C" qg_status qg_lanczos_tridiag(qg_context ctx, qg_operator op, qg_basis
     qg_status sst = lanczos_small(ctx, op, b, v0_dev, nvec, ntri, eps, gamma, a_host, b_host, krylov_dev, &done);
     if (sst != QG_OK || done) return sst;
   }
-  // Real chains in pairs.  With a real operator a start vector whose imaginary (or real) part
-  // is zero stays so, and two such chains share one complex vector: one apply serves both, so
-  // each costs half.  A purely imaginary vector has the coefficients of its imaginary part.
+  // Real chains.  With a real operator a start vector whose imaginary (or real) part is zero
+  // stays so: a single such chain runs on real vectors (one FMA per connection, half the
+  // bytes), and two share one complex vector (one apply serves both), so each costs half.  A purely imaginary vector has the coefficients of its imaginary part.
   // Each part is updated with exactly the arithmetic of its chain run alone; with one pair the
   // reductions run in the same order too and the coefficients are bitwise those of the runs
   // alone, with more pairs the multi-vector reductions add in another order (rounding only).
-  if (ctx->split_chains && nvec >= 2 && !krylov_dev && qg_operator_values_real(op) && qg_apply_uses_lists(op, b)) {
+  if (ctx->split_chains && !krylov_dev && qg_operator_values_real(op) && qg_apply_uses_lists(op, b)) {
     unsigned int *d_flags = nullptr;
     std::vector<unsigned int> fl(2 * (size_t)nvec, 0u);
     cudaError_t e = cudaMalloc(&d_flags, fl.size() * sizeof(unsigned int));
@@ -970,6 +1037,20 @@ extern "C" qg_status qg_lanczos_tridiag(qg_context ctx, qg_operator op, qg_basis
         rcol.push_back(k);
         rpart.push_back(fl[2 * k + 1] ? 1 : 0);
       }
+    }
+    if (nvec == 1 && rcol.size() == 1) {
+      double *xr = nullptr;
+      e = cudaMalloc(&xr, (size_t)n * sizeof(double));
+      if (e == cudaSuccess) {
+        k_take_part<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, (const double2 *)v0_dev, rpart[0], xr);
+        ctx->launches++;
+        e = cudaGetLastError();
+      }
+      qg_status st = e == cudaSuccess ? lanczos_general(ctx, op, b, xr, 1, ntri, eps, gamma, a_host, b_host, nullptr, 0, 1)
+                                      : qg_cuda_fail(ctx, e, "qg_lanczos_tridiag");
+      cudaStreamSynchronize(s);
+      cudaFree(xr);
+      return st;
     }
     if (rcol.size() >= 2) {
       const int np = (int)(rcol.size() + 1) / 2, nc = (int)ccol.size();

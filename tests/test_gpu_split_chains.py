@@ -67,3 +67,27 @@ def test_paired_real_chains_match_their_runs_alone(api, eps, gamma):
         eng.check(eng.L.qg_set_small_basis_lanczos(eng.ctx, 1))
     for k in range(2):
         assert np.array_equal(A2[k], alone[k][0][0]) and np.array_equal(B2[k], alone[k][1][0]), k
+
+
+@pytest.mark.parametrize("eps,gamma", [(0.0, 0.0), (1e-5, 0.4)])
+def test_single_real_chain_on_real_vectors(api, eps, gamma):
+    """One real (or purely imaginary) chain runs on real vectors: coefficients bitwise those of the
+    same chain run as a complex vector."""
+    import torch
+    from quanty_gb300 import workloads
+    eng = api.engine()
+    H, R, s0, info = workloads.anderson_impurity(nshell=2, hole_max=2, particle_max=2)
+    b = api.closure(H, api.dets_to_bytes([s0], H.nf), H.nf, R)
+    rng = np.random.default_rng(11)
+    for col in (rng.normal(size=b.n) + 0j, 1j * rng.normal(size=b.n)):
+        x = torch.from_numpy(col.reshape(-1, 1)).cuda()
+        out = {}
+        try:
+            eng.check(eng.L.qg_set_small_basis_lanczos(eng.ctx, 0))
+            for on in (0, 1):
+                eng.check(eng.L.qg_set_split_chains(eng.ctx, on))
+                out[on] = api.lanczos_block(H, b, x.clone(), 40, eps, gamma, eng)
+        finally:
+            eng.check(eng.L.qg_set_split_chains(eng.ctx, 1))
+            eng.check(eng.L.qg_set_small_basis_lanczos(eng.ctx, 1))
+        assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
