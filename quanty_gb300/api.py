@@ -1292,7 +1292,11 @@ def EigensystemOnBasis(H, basis, Npsi, options=None, eng=None, seed=12345, max_r
     o = _opts(options)
     n = basis.n
     rng = np.random.default_rng(seed)
-    x0 = rng.standard_normal((n, Npsi)) + 1j * rng.standard_normal((n, Npsi))
+    x0 = rng.standard_normal((n, Npsi)).astype(np.complex128)
+    if any(v.imag != 0 for _, v in H.terms):
+        x0 += 1j * rng.standard_normal((n, Npsi))
+    # a real H starts from real vectors and keeps them real, as the reference's real-vector
+    # solver does: the eigenstates come out real, and so do the Lanczos chains built on them
     with eng.on_stream():
         x = eng.torch.from_numpy(x0).to("cuda:%d" % eng.device).contiguous()
     en = np.zeros(Npsi)

@@ -171,8 +171,9 @@ __global__ void k_scale_col(double2 *B, int ldb, int col, int64_t n, double s) {
   B[r * ldb + col] = make_double2(v.x * s, v.y * s);
 }
 
-// deterministic pseudo-random fill of columns c0 .. c0+k-1 (guard vectors)
-__global__ void k_fill_cols(double2 *B, int ldb, int c0, int k, int64_t n, uint64_t salt) {
+// deterministic pseudo-random fill of columns c0 .. c0+k-1 (guard vectors); real entries for
+// a real operator, so real start vectors keep the whole block, and the eigenvectors, real
+__global__ void k_fill_cols(double2 *B, int ldb, int c0, int k, int64_t n, uint64_t salt, int real) {
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n * k) return;
   int64_t r = i / k;
@@ -180,7 +181,7 @@ __global__ void k_fill_cols(double2 *B, int ldb, int c0, int k, int64_t n, uint6
   uint64_t h = qg_mix64((uint64_t)i * 0x9e3779b97f4a7c15ull + salt);
   double a = (double)(h >> 11) * (1.0 / 9007199254740992.0) - 0.5;
   double b = (double)(qg_mix64(h) >> 11) * (1.0 / 9007199254740992.0) - 0.5;
-  B[r * ldb + c0 + c] = make_double2(a, b);
+  B[r * ldb + c0 + c] = make_double2(a, real ? 0.0 : b);
 }
 
 __global__ void k_copy_cols(const double2 *src, int lds, int s0, double2 *dst, int ldd, int d0, int k, int64_t n) {
@@ -304,7 +305,8 @@ extern "C" qg_status qg_block_groundstate(qg_context ctx, qg_operator op, qg_bas
   k_copy_cols<<<grid(n * nwant), 256, 0, s>>>((const double2 *)x_dev, nwant, 0, X, p, 0, nwant, n);
   ctx->launches++;
   if (p > nwant) {
-    k_fill_cols<<<grid(n * (p - nwant)), 256, 0, s>>>(X, p, nwant, p - nwant, n, 0x5eedull);
+    k_fill_cols<<<grid(n * (p - nwant)), 256, 0, s>>>(X, p, nwant, p - nwant, n, 0x5eedull,
+                                                      qg_operator_values_real(op) ? 1 : 0);
     ctx->launches++;
   }
   Gram G;
