@@ -20,7 +20,9 @@
 
 #define QG_GT 16  // Gram tile edge (outputs per block: QG_GT x QG_GT)
 
-// part[chunk][i * kb + j] = sum over the chunk's rows r of conj(A[r][i]) B[r][j]
+// part[chunk][i * kb + j] = sum over the chunk's rows r of conj(A[r][i]) B[r][j].  REAL: both
+// blocks are real (zero imaginary parts), one FMA per term instead of four.
+template <bool REAL>
 __global__ void __launch_bounds__(256) k_block_gram_part(const double2 *__restrict__ A, int lda, int ka,
                                                          const double2 *__restrict__ B, int ldb, int kb, int64_t n,
                                                          int64_t rows_per_chunk, double2 *__restrict__ part) {
@@ -40,9 +42,11 @@ __global__ void __launch_bounds__(256) k_block_gram_part(const double2 *__restri
     for (int q = 0; q < QG_GT; q++) {
       const double2 a = sa[q][ty], b = sb[q][tx];
       re = fma(a.x, b.x, re);
-      re = fma(a.y, b.y, re);
-      im = fma(a.x, b.y, im);
-      im = fma(-a.y, b.x, im);
+      if (!REAL) {
+        re = fma(a.y, b.y, re);
+        im = fma(a.x, b.y, im);
+        im = fma(-a.y, b.x, im);
+      }
     }
     __syncthreads();
   }
@@ -67,7 +71,7 @@ __global__ void k_block_gram_sum(const double2 *__restrict__ part, int nchunk, i
 // are split into chunks whose partial tiles (in `work`, `work_elems` complex entries) are summed
 // in chunk order.
 qg_status qg_block_gram(qg_context ctx, const double2 *A, int lda, int ka, const double2 *B, int ldb, int kb,
-                        int64_t n, double2 *C, double2 *work, int64_t work_elems) {
+                        int64_t n, double2 *C, double2 *work, int64_t work_elems, bool real) {
   if (ka <= 0 || kb <= 0) return QG_OK;
   const int64_t m = (int64_t)ka * kb;
   if (n <= 0) {
@@ -87,8 +91,12 @@ qg_status qg_block_gram(qg_context ctx, const double2 *A, int lda, int ka, const
   int64_t rows = (n + nchunk - 1) / nchunk;
   rows = (rows + QG_GT - 1) / QG_GT * QG_GT;
   nchunk = (n + rows - 1) / rows;
-  k_block_gram_part<<<dim3((unsigned)tiles, (unsigned)nchunk), 256, 0, ctx->stream>>>(A, lda, ka, B, ldb, kb, n,
-                                                                                        rows, work);
+  if (real)
+    k_block_gram_part<true><<<dim3((unsigned)tiles, (unsigned)nchunk), 256, 0, ctx->stream>>>(A, lda, ka, B, ldb, kb,
+                                                                                              n, rows, work);
+  else
+    k_block_gram_part<false><<<dim3((unsigned)tiles, (unsigned)nchunk), 256, 0, ctx->stream>>>(A, lda, ka, B, ldb,
+                                                                                               kb, n, rows, work);
   k_block_gram_sum<<<(unsigned)((m + 255) / 256), 256, 0, ctx->stream>>>(work, (int)nchunk, (int)m, C);
   ctx->launches += 2;
   return qg_check_launch(ctx, "qg_block_gram");
@@ -97,7 +105,7 @@ qg_status qg_block_gram(qg_context ctx, const double2 *A, int lda, int ka, const
 // X[r][j] = beta X[r][j] + alpha sum_i A(r, i) M[i][j] for the rows and columns of this block,
 // A(r, i) = A[r * ars + i * acs].  JT columns per block, 256 / JT thread rows, 4 rows per
 // thread; the factor tiles (IT values of i at a time) staged in shared memory.
-template <int JT>
+template <int JT, bool REAL>
 __global__ void __launch_bounds__(256) k_block_mul(const double2 *__restrict__ A, int64_t ars, int64_t acs, int ka,
                                                    const double2 *__restrict__ M, int ldm, double2 *__restrict__ X,
                                                    int ldx, int kb, int64_t n, double alpha, double beta) {
@@ -137,9 +145,11 @@ __global__ void __launch_bounds__(256) k_block_mul(const double2 *__restrict__ A
       for (int q = 0; q < 4; q++) {
         const double2 a = sa[ii][ty + q * TY];
         acc[q].x = fma(a.x, mv.x, acc[q].x);
-        acc[q].x = fma(-a.y, mv.y, acc[q].x);
-        acc[q].y = fma(a.x, mv.y, acc[q].y);
-        acc[q].y = fma(a.y, mv.x, acc[q].y);
+        if (!REAL) {
+          acc[q].x = fma(-a.y, mv.y, acc[q].x);
+          acc[q].y = fma(a.x, mv.y, acc[q].y);
+          acc[q].y = fma(a.y, mv.x, acc[q].y);
+        }
       }
     }
     __syncthreads();
@@ -161,20 +171,30 @@ __global__ void __launch_bounds__(256) k_block_mul(const double2 *__restrict__ A
   }
 }
 
-static qg_status block_mul(qg_context ctx, const double2 *A, int64_t ars, int64_t acs, int ka, const double2 *M,
-                           int ldm, double2 *X, int ldx, int kb, int64_t n, double alpha, double beta) {
-  if (kb <= 0 || n <= 0) return QG_OK;
+template <bool REAL>
+static void block_mul_t(qg_context ctx, const double2 *A, int64_t ars, int64_t acs, int ka, const double2 *M, int ldm,
+                        double2 *X, int ldx, int kb, int64_t n, double alpha, double beta) {
   cudaStream_t s = ctx->stream;
   if (kb <= 8) {
     dim3 g((unsigned)((n + 127) / 128), (unsigned)((kb + 7) / 8));
-    k_block_mul<8><<<g, 256, 0, s>>>(A, ars, acs, ka, M, ldm, X, ldx, kb, n, alpha, beta);
+    k_block_mul<8, REAL><<<g, 256, 0, s>>>(A, ars, acs, ka, M, ldm, X, ldx, kb, n, alpha, beta);
   } else if (kb <= 16) {
     dim3 g((unsigned)((n + 63) / 64), (unsigned)((kb + 15) / 16));
-    k_block_mul<16><<<g, 256, 0, s>>>(A, ars, acs, ka, M, ldm, X, ldx, kb, n, alpha, beta);
+    k_block_mul<16, REAL><<<g, 256, 0, s>>>(A, ars, acs, ka, M, ldm, X, ldx, kb, n, alpha, beta);
   } else {
     dim3 g((unsigned)((n + 31) / 32), (unsigned)((kb + 31) / 32));
-    k_block_mul<32><<<g, 256, 0, s>>>(A, ars, acs, ka, M, ldm, X, ldx, kb, n, alpha, beta);
+    k_block_mul<32, REAL><<<g, 256, 0, s>>>(A, ars, acs, ka, M, ldm, X, ldx, kb, n, alpha, beta);
   }
+}
+
+static qg_status block_mul(qg_context ctx, const double2 *A, int64_t ars, int64_t acs, int ka, const double2 *M,
+                           int ldm, double2 *X, int ldx, int kb, int64_t n, double alpha, double beta,
+                           bool real = false) {
+  if (kb <= 0 || n <= 0) return QG_OK;
+  if (real)
+    block_mul_t<true>(ctx, A, ars, acs, ka, M, ldm, X, ldx, kb, n, alpha, beta);
+  else
+    block_mul_t<false>(ctx, A, ars, acs, ka, M, ldm, X, ldx, kb, n, alpha, beta);
   ctx->launches++;
   return qg_check_launch(ctx, "block product");
 }
@@ -182,10 +202,10 @@ static qg_status block_mul(qg_context ctx, const double2 *A, int64_t ars, int64_
 // X (n x kb, ld ldx) = beta X + alpha A M; A: n x ka (ld lda), M: ka x kb row-major (ld kb).
 // ka == 0 leaves beta X (beta must then be 1: the solver never asks for a bare rescale).
 qg_status qg_block_update(qg_context ctx, const double2 *A, int lda, int ka, const double2 *M, double2 *X, int ldx,
-                          int kb, int64_t n, double alpha, double beta) {
+                          int kb, int64_t n, double alpha, double beta, bool real) {
   if (kb <= 0 || n <= 0) return QG_OK;
   if (ka <= 0) return beta == 1.0 ? QG_OK : QG_ERR_ARG;
-  return block_mul(ctx, A, lda, 1, ka, M, kb, X, ldx, kb, n, alpha, beta);
+  return block_mul(ctx, A, lda, 1, ka, M, kb, X, ldx, kb, n, alpha, beta, real);
 }
 
 // out (n x np row-major) = sum_i K_i C[i][:], the vectors K_i stored vector-major (K[i * n + r]).

@@ -48,7 +48,8 @@ __global__ void k_gram_partial(const double2 *__restrict__ A, int lda, int a0, i
 // registers; with more columns a warp takes a row and its lanes take the columns (coalesced
 // reads of the row).  Grid-stride over rows with many blocks, so the reduction is wide rather
 // than a long serial walk per thread; sums are combined in a fixed order.
-template <int KMAX>
+// REAL (also below): both sides are real, one multiply-add per term.
+template <int KMAX, bool REAL>
 __global__ void k_gram_col_rows(const double2 *__restrict__ A, int lda, int a0, int ka, const double2 *__restrict__ B,
                                 int ldb, int b0, int64_t n, double2 *part) {
   __shared__ double2 sh[8][KMAX];
@@ -61,8 +62,12 @@ __global__ void k_gram_col_rows(const double2 *__restrict__ A, int lda, int a0, 
     for (int i = 0; i < KMAX; i++) {
       if (i < ka) {
         double2 a = A[r * lda + a0 + i];
-        acc[i].x += a.x * b.x + a.y * b.y;
-        acc[i].y += a.x * b.y - a.y * b.x;
+        if (REAL) {
+          acc[i].x += a.x * b.x;
+        } else {
+          acc[i].x += a.x * b.x + a.y * b.y;
+          acc[i].y += a.x * b.y - a.y * b.x;
+        }
       }
     }
   }
@@ -88,7 +93,7 @@ __global__ void k_gram_col_rows(const double2 *__restrict__ A, int lda, int a0, 
 }
 
 #define QG_GRAM_LANE_COLS 8  // columns per lane at most: ka <= 256
-template <int M>
+template <int M, bool REAL>
 __global__ void k_gram_col_lanes(const double2 *__restrict__ A, int lda, int a0, int ka,
                                  const double2 *__restrict__ B, int ldb, int b0, int64_t n, double2 *part) {
   __shared__ double2 sh[8][32 * M];
@@ -103,8 +108,12 @@ __global__ void k_gram_col_lanes(const double2 *__restrict__ A, int lda, int a0,
       int i = lane + 32 * m;
       if (i < ka) {
         double2 a = A[r * lda + a0 + i];
-        acc[m].x += a.x * b.x + a.y * b.y;
-        acc[m].y += a.x * b.y - a.y * b.x;
+        if (REAL) {
+          acc[m].x += a.x * b.x;
+        } else {
+          acc[m].x += a.x * b.x + a.y * b.y;
+          acc[m].y += a.x * b.y - a.y * b.x;
+        }
       }
     }
   }
@@ -149,6 +158,7 @@ __global__ void k_gram_reduce_warp(const double2 *part, int nchunk, int m, doubl
 }
 
 // B[r][b0+j] -= sum_i A[r][a0+i] C[i*kb + j]
+template <bool REAL>
 __global__ void k_sub_mul(const double2 *__restrict__ A, int lda, int a0, int ka, const double2 *__restrict__ C,
                           double2 *B, int ldb, int b0, int kb, int64_t n) {
   int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -158,8 +168,12 @@ __global__ void k_sub_mul(const double2 *__restrict__ A, int lda, int a0, int ka
   double2 acc = B[r * ldb + b0 + j];
   for (int i = 0; i < ka; i++) {
     double2 a = A[r * lda + a0 + i], c = C[i * kb + j];
-    acc.x -= a.x * c.x - a.y * c.y;
-    acc.y -= a.x * c.y + a.y * c.x;
+    if (REAL) {
+      acc.x -= a.x * c.x;
+    } else {
+      acc.x -= a.x * c.x - a.y * c.y;
+      acc.y -= a.x * c.y + a.y * c.x;
+    }
   }
   B[r * ldb + b0 + j] = acc;
 }
@@ -184,6 +198,12 @@ __global__ void k_fill_cols(double2 *B, int ldb, int c0, int k, int64_t n, uint6
   B[r * ldb + c0 + c] = make_double2(a, real ? 0.0 : b);
 }
 
+// flag = 1 when any of the n values has a non-zero imaginary part
+__global__ void k_any_imag(const double2 *__restrict__ v, int64_t n, unsigned int *flag) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n && v[i].y != 0.0) atomicOr(flag, 1u);
+}
+
 __global__ void k_copy_cols(const double2 *src, int lds, int s0, double2 *dst, int ldd, int d0, int k, int64_t n) {
   int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (t >= n * k) return;
@@ -202,6 +222,7 @@ struct Gram {
   int nchunk = 1;
   int64_t chunk = 1;
   int nblk = 1;  // blocks of the one-column Gram kernels
+  bool real = false;  // every vector real
   qg_status init(qg_context c, int64_t nn, int maxm, int kcol) {
     ctx = c;
     n = nn;
@@ -222,29 +243,36 @@ struct Gram {
     cudaFree(part);
     cudaFree(out);
   }
+  template <bool REAL>
+  void col_gram(cudaStream_t s, const double2 *A, int lda, int a0, int ka, const double2 *B, int ldb, int b0) {
+    if (ka == 1)
+      k_gram_col_rows<1, REAL><<<nblk, 256, 0, s>>>(A, lda, a0, ka, B, ldb, b0, n, part);
+    else if (ka <= 4)
+      k_gram_col_rows<4, REAL><<<nblk, 256, 0, s>>>(A, lda, a0, ka, B, ldb, b0, n, part);
+    else if (ka <= 8)
+      k_gram_col_rows<8, REAL><<<nblk, 256, 0, s>>>(A, lda, a0, ka, B, ldb, b0, n, part);
+    else if (ka <= 32)
+      k_gram_col_lanes<1, REAL><<<nblk, 256, 0, s>>>(A, lda, a0, ka, B, ldb, b0, n, part);
+    else if (ka <= 64)
+      k_gram_col_lanes<2, REAL><<<nblk, 256, 0, s>>>(A, lda, a0, ka, B, ldb, b0, n, part);
+    else if (ka <= 128)
+      k_gram_col_lanes<4, REAL><<<nblk, 256, 0, s>>>(A, lda, a0, ka, B, ldb, b0, n, part);
+    else
+      k_gram_col_lanes<8, REAL><<<nblk, 256, 0, s>>>(A, lda, a0, ka, B, ldb, b0, n, part);
+  }
   // out (device) and host = A[:, a0:a0+ka]^dag B[:, b0:b0+kb]
   qg_status run(const double2 *A, int lda, int a0, int ka, const double2 *B, int ldb, int b0, int kb,
                 std::vector<cd> *host) {
     int m = ka * kb;
     if (m > cap || m <= 0) return QG_ERR_ARG;
     if (kb > 1) {  // a block against a block: tiled products, partial sums per row chunk
-      QG_TRY(qg_block_gram(ctx, A + a0, lda, ka, B + b0, ldb, kb, n, out, part, part_elems));
+      QG_TRY(qg_block_gram(ctx, A + a0, lda, ka, B + b0, ldb, kb, n, out, part, part_elems, real));
     } else if (ka <= 32 * QG_GRAM_LANE_COLS) {  // one column: wide partial sums, fixed-order reduction
       cudaStream_t s = ctx->stream;
-      if (ka == 1)
-        k_gram_col_rows<1><<<nblk, 256, 0, s>>>(A, lda, a0, ka, B, ldb, b0, n, part);
-      else if (ka <= 4)
-        k_gram_col_rows<4><<<nblk, 256, 0, s>>>(A, lda, a0, ka, B, ldb, b0, n, part);
-      else if (ka <= 8)
-        k_gram_col_rows<8><<<nblk, 256, 0, s>>>(A, lda, a0, ka, B, ldb, b0, n, part);
-      else if (ka <= 32)
-        k_gram_col_lanes<1><<<nblk, 256, 0, s>>>(A, lda, a0, ka, B, ldb, b0, n, part);
-      else if (ka <= 64)
-        k_gram_col_lanes<2><<<nblk, 256, 0, s>>>(A, lda, a0, ka, B, ldb, b0, n, part);
-      else if (ka <= 128)
-        k_gram_col_lanes<4><<<nblk, 256, 0, s>>>(A, lda, a0, ka, B, ldb, b0, n, part);
+      if (real)
+        col_gram<true>(s, A, lda, a0, ka, B, ldb, b0);
       else
-        k_gram_col_lanes<8><<<nblk, 256, 0, s>>>(A, lda, a0, ka, B, ldb, b0, n, part);
+        col_gram<false>(s, A, lda, a0, ka, B, ldb, b0);
       k_gram_reduce_warp<<<(m + 7) / 8, 256, 0, s>>>(part, nblk, m, out);
       ctx->launches += 2;
     } else {
@@ -311,6 +339,23 @@ extern "C" qg_status qg_block_groundstate(qg_context ctx, qg_operator op, qg_bas
   }
   Gram G;
   qg_status st = G.init(ctx, n, K * std::max(K, p), K);
+  // a real operator with real start vectors keeps every vector, every projection and the Ritz
+  // vectors real (the reference's real-vector solver): the block products then run in real
+  // arithmetic, one FMA per term instead of four
+  if (st == QG_OK && qg_operator_values_real(op)) {
+    unsigned int *d_im = nullptr, h_im = 1;
+    e = cudaMalloc(&d_im, sizeof(unsigned int));
+    if (e == cudaSuccess) e = cudaMemsetAsync(d_im, 0, sizeof(unsigned int), s);
+    if (e == cudaSuccess) {
+      k_any_imag<<<grid(n * p), 256, 0, s>>>(X, n * p, d_im);
+      ctx->launches++;
+      e = cudaMemcpyAsync(&h_im, d_im, sizeof(unsigned int), cudaMemcpyDeviceToHost, s);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFree(d_im);
+    if (e != cudaSuccess) st = qg_cuda_fail(ctx, e, "qg_block_groundstate");
+    G.real = h_im == 0;
+  }
   std::vector<double> theta(p, 0.0);
   int it = 0;
   bool converged = false;
@@ -350,7 +395,10 @@ extern "C" qg_status qg_block_groundstate(qg_context ctx, qg_operator op, qg_bas
             std::vector<cd> h;
             st = G.run(V, K, lo, col - lo, V, K, col, 1, &h);
             if (st != QG_OK) break;
-            k_sub_mul<<<grid(n), 256, 0, s>>>(V, K, lo, col - lo, G.out, V, K, col, 1, n);
+            if (G.real)
+              k_sub_mul<true><<<grid(n), 256, 0, s>>>(V, K, lo, col - lo, G.out, V, K, col, 1, n);
+            else
+              k_sub_mul<false><<<grid(n), 256, 0, s>>>(V, K, lo, col - lo, G.out, V, K, col, 1, n);
             ctx->launches++;
             if (coef)
               for (int i = lo; i < col; i++) (*coef)[(size_t)i * cnt + j] += h[i - lo];
@@ -394,7 +442,7 @@ extern "C" qg_status qg_block_groundstate(qg_context ctx, qg_operator op, qg_bas
         if (st != QG_OK) break;
         for (int i = 0; i < k; i++)
           for (int j = 0; j < bs; j++) T[(size_t)i * K + j0 + j] += c[(size_t)i * bs + j];
-        st = qg_block_update(ctx, V, K, k, G.out, W, p, bs, n, -1.0, 1.0);
+        st = qg_block_update(ctx, V, K, k, G.out, W, p, bs, n, -1.0, 1.0, G.real);
       }
       if (st != QG_OK || k + bs > Kcur) break;
       // append W as new columns and orthonormalise them
@@ -454,7 +502,7 @@ extern "C" qg_status qg_block_groundstate(qg_context ctx, qg_operator op, qg_bas
         break;
       }
     }
-    st = qg_block_update(ctx, V, K, k, Cd, X, p, p, n, 1.0, 0.0);
+    st = qg_block_update(ctx, V, K, k, Cd, X, p, p, n, 1.0, 0.0, G.real);
     if (st != QG_OK) break;
     std::vector<double> w(nv);
     e = cudaMemcpyAsync(w.data(), wd, (size_t)nv * sizeof(double), cudaMemcpyDeviceToHost, s);
@@ -477,7 +525,7 @@ extern "C" qg_status qg_block_groundstate(qg_context ctx, qg_operator op, qg_bas
         st = qg_cuda_fail(ctx, e, "residual");
         break;
       }
-      st = qg_block_update(ctx, X, p, p, Cd, W, p, p, n, -1.0, 1.0);
+      st = qg_block_update(ctx, X, p, p, Cd, W, p, p, n, -1.0, 1.0, G.real);
       if (st != QG_OK) break;
     }
     std::vector<cd> hh;

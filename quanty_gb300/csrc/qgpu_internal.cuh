@@ -373,10 +373,11 @@ int qg_partial_blocks(qg_context ctx, int64_t n);
 // dense complex block products (qgpu_blocks.cu); row-major n x k blocks
 //   C (ka x kb row-major) = A^H B, with a work buffer of work_elems complex entries for the
 //   partial sums;   X = beta X + alpha A M  (M ka x kb row-major)
+//   real: every value of A, B (and M) is real: one FMA per term instead of four
 qg_status qg_block_gram(qg_context ctx, const double2 *A, int lda, int ka, const double2 *B, int ldb, int kb,
-                        int64_t n, double2 *C, double2 *work, int64_t work_elems);
+                        int64_t n, double2 *C, double2 *work, int64_t work_elems, bool real = false);
 qg_status qg_block_update(qg_context ctx, const double2 *A, int lda, int ka, const double2 *M, double2 *X, int ldx,
-                          int kb, int64_t n, double alpha, double beta);
+                          int kb, int64_t n, double alpha, double beta, bool real = false);
 // out (n x np row-major) = sum_i K_i C[i][:], K vector-major (K[i * n + r])
 qg_status qg_block_combine(qg_context ctx, const double2 *K, int64_t n, int ntri, const double2 *C, int np,
                            double2 *out);
