@@ -484,9 +484,54 @@ def layouts(args):
     return 0
 
 
+def chains(args):
+    """Real Lanczos chains on the XAS final-state basis of the 76-spin-orbital impurity (6 bath
+    shells): Tx psi (real) and Ty psi (purely imaginary) of a real psi, as one complex chain, as
+    one chain on real vectors, and as a pair in one complex vector; the coefficients of each form
+    against the others (bitwise) and the time per chain and step (CUDA events over --ntri steps).
+    Three short runs of each form come first (the ncu target: -k regex:k_apply_list)."""
+    from quanty_gb300 import api, workloads
+    eng = api.engine()
+    torch = eng.torch
+    H, R, seed, info = workloads.anderson_impurity(nshell=6, hole_max=1, particle_max=2)
+    _, Rx, _, _ = workloads.anderson_impurity(nshell=6, hole_max=1, particle_max=2, core_holes=1)
+    Ts = _xas_ops(api, workloads, H.nf)
+    g = api.closure(H, api.dets_to_bytes([seed], H.nf), H.nf, R, -1, eng)
+    rng = np.random.default_rng(1)
+    X = torch.from_numpy(rng.normal(size=(g.n, 1)) + 0j).cuda()
+    bf, Y = _final_vectors(api, H, Ts[:2], g, X, Rx, eng)
+    pair, one = Y.contiguous(), Y[:, :1].contiguous()
+
+    def run(x, ntri, split):
+        eng.check(eng.L.qg_set_split_chains(eng.ctx, split))
+        try:
+            return api.lanczos_block(H, bf, x, ntri, 0.0, 0.0, eng)
+        finally:
+            eng.check(eng.L.qg_set_split_chains(eng.ctx, 1))
+
+    short = {"pair": run(pair, 3, 1), "real": run(one, 3, 1), "complex": run(one, 3, 0)}
+    same = bool(np.array_equal(short["pair"][0][0], short["real"][0][0]) and
+                np.array_equal(short["real"][0], short["complex"][0]))
+    ntri = int(args.ntri)
+    out = {}
+    for name, x, split, nch in (("complex", one, 0, 1), ("real", one, 1, 1), ("pair", pair, 1, 2)):
+        run(x, 4, split)  # warm (graphs)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(eng.stream)
+        run(x, ntri, split)
+        e1.record(eng.stream)
+        e1.synchronize()
+        out[name] = e0.elapsed_time(e1) / ntri / nch
+    line = {"mode": "chains", "n": bf.n, "ntri": ntri, "ms_per_chain_step": out, "bitwise_equal_forms": same}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main(args):
     if args.mode == "batched":
         return batched(args)
     if args.mode == "layouts":
         return layouts(args)
+    if args.mode == "chains":
+        return chains(args)
     return served(args)
