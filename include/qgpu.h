@@ -326,6 +326,18 @@ qg_status qg_block_lanczos(qg_context ctx, qg_operator op, qg_basis basis, const
                            int32_t ntri, double eps, double singular_value, double *a_host, double *b_host,
                            int32_t *sizes_host, double *krylov_dev);
 
+/* Dense complex block products on device arrays (row-major, complex interleaved), by the
+ * library's own FP64 kernels (no BLAS): C (ka x kb) = A^H B over n rows, and
+ * X (n x kb) = beta X + alpha A M with M ka x kb.  They replace the reference's BLAS products
+ * of eigenvector matrices in the dense RIXS branch (ResonantSpectraDense,
+ * Core/ResonantSpectra.cpp:290-660). */
+qg_status qg_block_adjoint_product(qg_context ctx, const double *A_dev, int32_t lda, int32_t ka,
+                                   const double *B_dev, int32_t ldb, int32_t kb, int64_t n,
+                                   double *C_dev);
+qg_status qg_block_product(qg_context ctx, const double *A_dev, int32_t lda, int32_t ka,
+                           const double *M_dev, int32_t kb, int64_t n, double alpha, double beta,
+                           double *X_dev, int32_t ldx);
+
 /* out_dev (n x np row-major) = sum_i K_i C[i][:] for nk vectors K_i stored vector-major (K_dev,
  * K_i at [i * n]) and C_host (nk x np row-major complex): the combination of stored Krylov
  * vectors with the coefficients of a projected resolvent (the G1 T1 psi of RIXS,

@@ -1457,17 +1457,45 @@ def _rixs_range(emin, emax, ne, gamma, lo_ev, hi_ev, e_lo, e_hi):
     return float(emin), float(emax), int(ne), float(gamma)
 
 
-def _apply_between(O, dst, src, X, eng):
-    """O applied to every column of the host matrix X (rows on src) into dst, one multi-vector
-    pull launch sequence on the device; returns the host matrix (dst.n x columns)."""
+def _apply_between(O, dst, src, X, eng, device=False):
+    """O applied to every column of the matrix X (rows on src; host, or a device tensor) into
+    dst, one multi-vector pull launch sequence on the device; returns the host matrix
+    (dst.n x columns), or the device tensor with device=True."""
     k = X.shape[1]
     if not dst.n or not src.n or not k:
-        return np.zeros((dst.n, k), dtype=np.complex128)
-    with eng.on_stream():
-        x = eng.torch.from_numpy(np.ascontiguousarray(X, dtype=np.complex128)).to("cuda:%d" % eng.device)
+        z = np.zeros((dst.n, k), dtype=np.complex128)
+        return _to_dev(eng, z) if device else z
+    x = X if not isinstance(X, np.ndarray) else _to_dev(eng, X)
     y = eng.empty(dst.n, k)
     eng.check(eng.L.qg_apply(eng.ctx, O.handle(eng), dst.h, src.h, _ptr(x), _ptr(y), k))
-    return eng.to_host(y[:dst.n])
+    return y[:dst.n] if device else eng.to_host(y[:dst.n])
+
+
+def _to_dev(eng, A):
+    with eng.on_stream():
+        return eng.torch.from_numpy(np.ascontiguousarray(A, dtype=np.complex128)).to("cuda:%d" % eng.device)
+
+
+def _adjoint_product(eng, A, B):
+    """A^H B of device tensors A (n x ka), B (n x kb), by the library's block kernels."""
+    n, ka = A.shape
+    kb = B.shape[1]
+    A, B = A.contiguous(), B.contiguous()
+    C = eng.empty(ka, kb)
+    if n and ka and kb:
+        eng.check(eng.L.qg_block_adjoint_product(eng.ctx, _ptr(A), ka, ka, _ptr(B), kb, kb, n, _ptr(C)))
+    return C[:ka]
+
+
+def _block_product(eng, A, M):
+    """A M of device tensors A (n x ka), M (ka x kb), by the library's block kernels."""
+    n, ka = A.shape
+    kb = M.shape[1]
+    A, M = A.contiguous(), M.contiguous()
+    X = eng.empty(n, kb)
+    if n and ka and kb:
+        eng.check(eng.L.qg_block_product(eng.ctx, _ptr(A), ka, ka, _ptr(M), kb, n, 1.0, 0.0, _ptr(X), kb))
+    return X[:n]
 
 
 def _poles_complex(e0, poles, W, emin, emax, ne, gamma, eng):
@@ -1513,8 +1541,12 @@ def _rixs_dense(H1, H2, T1s, T2s, psis, o, b1, b2, tensor, eng):
         w2, V2 = hermitian_eigh(OperatorToDeterminantMatrix(H2, b2, eng), n2, eng)
     else:
         w2, V2 = np.zeros(1), np.zeros((0, 0), dtype=np.complex128)
-    A = V1.conj().T @ X
-    B = [V2.conj().T @ _apply_between(T, b2, b1, V1, eng) for T in T2s]
+    # the eigenvector products on the device (the reference's BLAS products)
+    V1d = _to_dev(eng, V1) if n1 else None
+    V2d = _to_dev(eng, V2) if n2 else None
+    A = eng.to_host(_adjoint_product(eng, V1d, _to_dev(eng, X))) if n1 else np.zeros((0, M1), dtype=np.complex128)
+    Bd = [_adjoint_product(eng, V2d, _apply_between(T, b2, b1, V1d, eng, device=True)) for T in T2s] \
+        if n1 and n2 else []
     # unset Emin/Emax (None) are derived from the extreme eigenvalues
     emin1, emax1, ne1, g1 = _rixs_range(o.get("Emin1"), o.get("Emax1"), int(o.get("NE1", 1000)),
                                         float(o.get("Gamma1", 0.0)), w1[0], w1[-1], e1.min(), e1.max())
@@ -1524,7 +1556,12 @@ def _rixs_dense(H1, H2, T1s, T2s, psis, o, b1, b2, tensor, eng):
     wres = np.array([emin1 + (emax1 - emin1) * l / ne1 for l in range(np1)])
     psi_of = np.arange(M1) // nt1
     Cm = A[None, :, :] / (wres[:, None, None] - w1[None, :n1, None] + e1[psi_of][None, None, :] + 0.5j * g1)
-    D = np.stack([Bk @ Cm for Bk in B]) if n2 and n1 else np.zeros((nt2, np1, n2, M1), dtype=np.complex128)
+    if n2 and n1:  # D_k[l] = B_k Cm[l] for every l at once: (n2 x n1) (n1 x np1 M1)
+        Md = _to_dev(eng, np.ascontiguousarray(Cm.transpose(1, 0, 2)).reshape(n1, np1 * M1))
+        D = np.stack([eng.to_host(_block_product(eng, Bk, Md)).reshape(n2, np1, M1).transpose(1, 0, 2)
+                      for Bk in Bd])
+    else:
+        D = np.zeros((nt2, np1, n2, M1), dtype=np.complex128)
     st = {"method": "dense", "emin1": emin1, "emax1": emax1, "ne1": ne1, "gamma1": g1, "emin2": emin2,
           "emax2": emax2, "ne2": ne2, "gamma2": g2, "energy1": e1.tolist(), "energy2": e2.tolist(),
           "n1": n1, "n2": n2, "resonant_energies": wres.tolist()}

@@ -235,3 +235,30 @@ extern "C" qg_status qg_krylov_combine(qg_context ctx, const double *K_dev, int6
   cudaFree(Cd);
   return st;
 }
+
+// ------------------------------------------------------------------ C ABI
+
+// C (ka x kb row-major, device) = A^H B over n rows; A: n x ka (ld lda), B: n x kb (ld ldb).
+extern "C" qg_status qg_block_adjoint_product(qg_context ctx, const double *A_dev, int32_t lda, int32_t ka,
+                                              const double *B_dev, int32_t ldb, int32_t kb, int64_t n,
+                                              double *C_dev) {
+  if (!ctx || !A_dev || !B_dev || !C_dev || ka <= 0 || kb <= 0 || n < 0 || lda < ka || ldb < kb) return QG_ERR_ARG;
+  const int64_t m = (int64_t)ka * kb;
+  // partial tiles of up to 64 row chunks, at most 256 MB of them
+  const int64_t work = std::max<int64_t>(m, std::min<int64_t>(64 * m, (256LL << 20) / 16));
+  double2 *w = nullptr;
+  QG_CUDA(ctx, cudaMalloc(&w, (size_t)work * 16));
+  qg_status st = qg_block_gram(ctx, (const double2 *)A_dev, lda, ka, (const double2 *)B_dev, ldb, kb, n,
+                               (double2 *)C_dev, w, work);
+  cudaStreamSynchronize(ctx->stream);
+  cudaFree(w);
+  return st;
+}
+
+// X (n x kb, ld ldx, device) = beta X + alpha A M; A: n x ka (ld lda), M: ka x kb row-major.
+extern "C" qg_status qg_block_product(qg_context ctx, const double *A_dev, int32_t lda, int32_t ka, const double *M_dev,
+                                      int32_t kb, int64_t n, double alpha, double beta, double *X_dev, int32_t ldx) {
+  if (!ctx || !A_dev || !M_dev || !X_dev || ka <= 0 || kb <= 0 || n < 0 || lda < ka || ldx < kb) return QG_ERR_ARG;
+  return qg_block_update(ctx, (const double2 *)A_dev, lda, ka, (const double2 *)M_dev, (double2 *)X_dev, ldx, kb, n,
+                         alpha, beta);
+}

@@ -80,6 +80,8 @@ def load(path=LIB_PATH):
         "qg_cf_spectra": (C.c_int, [P, I32, I32, P, P, P, D, D, I32, D, P]),
         "qg_block_lanczos": (C.c_int, [P, P, P, P, I32, I32, D, D, P, P, P, P]),
         "qg_krylov_combine": (C.c_int, [P, P, I64, I32, P, I32, P]),
+        "qg_block_adjoint_product": (C.c_int, [P, P, I32, I32, P, I32, I32, I64, P]),
+        "qg_block_product": (C.c_int, [P, P, I32, I32, P, I32, I64, D, D, P, I32]),
         "qg_block_cf_spectra": (C.c_int, [P, I32, I32, P, P, D, D, D, I32, D, P]),
         "qg_block_groundstate": (C.c_int, [P, P, P, I32, P, P, D, I32, I32, P]),
         "qg_lanczos_krylov": (C.c_int, [P, P, P, P, I32, D, P, P, P]),

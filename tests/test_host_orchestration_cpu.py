@@ -100,6 +100,15 @@ def host_api(monkeypatch, oracle_mod):
             out.numpy()[:n, :npc] = K.numpy()[:nk, :n].T @ np.asarray(C).reshape(nk, npc)
             return 0
 
+        def qg_block_adjoint_product(self, ctx, A, lda, ka, B, ldb, kb, n, C):
+            C.numpy()[:ka, :kb] = A.numpy()[:n, :ka].conj().T @ B.numpy()[:n, :kb]
+            return 0
+
+        def qg_block_product(self, ctx, A, lda, ka, M, kb, n, alpha, beta, X, ldx):
+            Xn = X.numpy()
+            Xn[:n, :kb] = beta * Xn[:n, :kb] + alpha * (A.numpy()[:n, :ka] @ M.numpy()[:ka, :kb])
+            return 0
+
     zeros, empty = torch.zeros, torch.empty
 
     class Eng:
@@ -263,8 +272,13 @@ def host_api(monkeypatch, oracle_mod):
                         lambda H, p, eng=None: O.expectation(_oop(O, H), O.WF(p.nf, p.det, p.val)))
     monkeypatch.setattr(api, "OperatorToDeterminantMatrix", lambda H, b, eng=None: O.dense_matrix(_oop(O, H), b.wf()))
     monkeypatch.setattr(api, "hermitian_eigh", eigh)
-    monkeypatch.setattr(api, "_apply_between", lambda T, dst, src, X, eng: np.stack(
-        [apply_vec(T, dst, src, X[:, c]) for c in range(X.shape[1])], 1) if X.shape[1] else np.zeros((dst.n, 0)))
+    def apply_between(T, dst, src, X, eng, device=False):
+        X = X if isinstance(X, np.ndarray) else X.numpy()
+        Y = np.stack([apply_vec(T, dst, src, X[:, c]) for c in range(X.shape[1])], 1) if X.shape[1] \
+            else np.zeros((dst.n, 0), dtype=np.complex128)
+        return torch.from_numpy(np.ascontiguousarray(Y, dtype=np.complex128)) if device else Y
+
+    monkeypatch.setattr(api, "_apply_between", apply_between)
     monkeypatch.setattr(api, "ListOfPolesToSpectrum", poles)
     monkeypatch.setattr(api, "lanczos_block", plain_lanczos)
     monkeypatch.setattr(api, "TriDiagonalMatrixToSpectrum", cf)
