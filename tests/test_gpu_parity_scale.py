@@ -9,8 +9,9 @@
   OperatorPsiConserveBasisPreAllocated, Core/OperatorWaveFunction.cpp:784-838).
 * The batched XAS form at its own basis sizes: 6 bath shells, 1,701,795 ground and
   3,899,040 core-excited determinants, 16 states x 3 polarisations = 48 chains in one
-  multi-vector Lanczos, against the reference's three-term recursion (Core/Lanczos.cpp:1905-2830,
-  restated below at Epsilon 0 on the closed basis) with the oracle's multi-vector push.
+  multi-vector Lanczos (and 8 real states, whose 24 real chains run two per complex vector),
+  against the reference's three-term recursion (Core/Lanczos.cpp:1905-2830, restated below at
+  Epsilon 0 on the closed basis) with the oracle's multi-vector push.
 """
 import ctypes as C
 
@@ -101,7 +102,11 @@ def _lanczos_oracle(O, op, h, n, Y, ntri):
     return A, B
 
 
-def test_batched_xas_at_its_basis_sizes(api, oracle_mod):
+@pytest.mark.parametrize("states", ["complex", "real"])
+def test_batched_xas_at_its_basis_sizes(api, oracle_mod, states):
+    """Complex states run as complex multi-vector chains; real states (those of this real
+    Hamiltonian) give real Tx/Tz and purely imaginary Ty chains, which run two per complex
+    vector."""
     import torch
     from quanty_gb300 import workloads
     O = oracle_mod
@@ -112,9 +117,9 @@ def test_batched_xas_at_its_basis_sizes(api, oracle_mod):
     Ts = [api.Operator(H.nf, at[k].terms, name=k) for k in ("Tx", "Ty", "Tz")]
     g = api.closure(H, api.dets_to_bytes([seed], H.nf), H.nf, R, -1, eng)
     assert g.n == 1701795
-    nstate, ntri = 16, 3
+    nstate, ntri = (16, 3) if states == "complex" else (8, 3)
     rng = np.random.default_rng(16)
-    X = rng.normal(size=(g.n, nstate)) + 1j * rng.normal(size=(g.n, nstate))
+    X = rng.normal(size=(g.n, nstate)) + (1j * rng.normal(size=(g.n, nstate)) if states == "complex" else 0j)
     o = {"NTri": ntri, "NE": 512, "Emin": -20.0, "Emax": 20.0, "Gamma": 0.5, "Epsilon": 0.0, "Restrictions": Rx}
     S, A, B = api.CreateSpectraResident(H, Ts, g, torch.from_numpy(X).cuda(), np.zeros(nstate), o, eng)
     # the final basis: the closure under H of every T's targets, within the core-hole windows
