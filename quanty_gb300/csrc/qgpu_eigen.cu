@@ -198,10 +198,13 @@ __global__ void k_fill_cols(double2 *B, int ldb, int c0, int k, int64_t n, uint6
   B[r * ldb + c0 + c] = make_double2(a, real ? 0.0 : b);
 }
 
-// flag = 1 when any of the n values has a non-zero imaginary part
+// flag = 1 when any of the n values has a non-zero imaginary part (one global OR per block)
 __global__ void k_any_imag(const double2 *__restrict__ v, int64_t n, unsigned int *flag) {
-  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i < n && v[i].y != 0.0) atomicOr(flag, 1u);
+  int found = 0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n && !found;
+       i += (int64_t)gridDim.x * blockDim.x)
+    found = v[i].y != 0.0;
+  if (__syncthreads_or(found) && threadIdx.x == 0) atomicOr(flag, 1u);
 }
 
 __global__ void k_copy_cols(const double2 *src, int lds, int s0, double2 *dst, int ldd, int d0, int k, int64_t n) {
@@ -347,7 +350,7 @@ extern "C" qg_status qg_block_groundstate(qg_context ctx, qg_operator op, qg_bas
     e = cudaMalloc(&d_im, sizeof(unsigned int));
     if (e == cudaSuccess) e = cudaMemsetAsync(d_im, 0, sizeof(unsigned int), s);
     if (e == cudaSuccess) {
-      k_any_imag<<<grid(n * p), 256, 0, s>>>(X, n * p, d_im);
+      k_any_imag<<<(unsigned)std::min<int64_t>((n * p + 255) / 256, 4LL * ctx->num_sms), 256, 0, s>>>(X, n * p, d_im);
       ctx->launches++;
       e = cudaMemcpyAsync(&h_im, d_im, sizeof(unsigned int), cudaMemcpyDeviceToHost, s);
     }

@@ -957,14 +957,22 @@ static qg_status lanczos_general(qg_context ctx, qg_operator op, qg_basis b, con
 }
 
 // per column k of v (n x nvec): flags[2k] set when a real part is non-zero, flags[2k + 1] when an
-// imaginary part is
+// imaginary part is.  Each thread keeps its bits for its columns, the block merges them in
+// shared memory, and one global OR per column and block remains (no contention on the flags).
 __global__ void k_column_parts(int64_t n, int nvec, const double2 *__restrict__ v, unsigned int *flags) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= n * nvec) return;
-  const double2 a = v[i];
-  const int k = (int)(i % nvec);
-  if (a.x != 0.0) atomicOr(flags + 2 * k, 1u);
-  if (a.y != 0.0) atomicOr(flags + 2 * k + 1, 1u);
+  extern __shared__ unsigned int sfl[];  // 2 nvec
+  for (int k = threadIdx.x; k < 2 * nvec; k += blockDim.x) sfl[k] = 0u;
+  __syncthreads();
+  const int64_t total = n * nvec, stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += stride) {
+    const double2 a = v[i];
+    const int k = (int)(i % nvec);
+    if (a.x != 0.0 && !sfl[2 * k]) atomicOr(sfl + 2 * k, 1u);
+    if (a.y != 0.0 && !sfl[2 * k + 1]) atomicOr(sfl + 2 * k + 1, 1u);
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < 2 * nvec; k += blockDim.x)
+    if (sfl[k]) atomicOr(flags + k, 1u);
 }
 
 // out (n x nout): column j takes part part[j] (0 real, 1 imaginary, -1 zero) of column src[j]
@@ -1015,13 +1023,14 @@ extern "C" qg_status qg_lanczos_tridiag(qg_context ctx, qg_operator op, qg_basis
   // Each part is updated with exactly the arithmetic of its chain run alone; with one pair the
   // reductions run in the same order too and the coefficients are bitwise those of the runs
   // alone, with more pairs the multi-vector reductions add in another order (rounding only).
-  if (ctx->split_chains && !krylov_dev && qg_operator_values_real(op) && qg_apply_uses_lists(op, b)) {
+  if (ctx->split_chains && !krylov_dev && nvec <= 4096 && qg_operator_values_real(op) && qg_apply_uses_lists(op, b)) {
     unsigned int *d_flags = nullptr;
     std::vector<unsigned int> fl(2 * (size_t)nvec, 0u);
     cudaError_t e = cudaMalloc(&d_flags, fl.size() * sizeof(unsigned int));
     if (e == cudaSuccess) e = cudaMemsetAsync(d_flags, 0, fl.size() * sizeof(unsigned int), s);
     if (e == cudaSuccess) {
-      k_column_parts<<<(unsigned)((n * nvec + 255) / 256), 256, 0, s>>>(n, nvec, (const double2 *)v0_dev, d_flags);
+      const unsigned g = (unsigned)std::min<int64_t>((n * nvec + 255) / 256, 4LL * ctx->num_sms);
+      k_column_parts<<<g, 256, 2 * nvec * sizeof(unsigned int), s>>>(n, nvec, (const double2 *)v0_dev, d_flags);
       ctx->launches++;
       e = cudaGetLastError();
     }
