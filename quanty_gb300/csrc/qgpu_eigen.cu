@@ -157,33 +157,6 @@ __global__ void k_gram_reduce_warp(const double2 *part, int nchunk, int m, doubl
   if (lane == 0) out[q] = make_double2(sr, si);
 }
 
-// B[r][b0+j] -= sum_i A[r][a0+i] C[i*kb + j]
-template <bool REAL>
-__global__ void k_sub_mul(const double2 *__restrict__ A, int lda, int a0, int ka, const double2 *__restrict__ C,
-                          double2 *B, int ldb, int b0, int kb, int64_t n) {
-  int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (t >= n * kb) return;
-  int64_t r = t / kb;
-  int j = (int)(t % kb);
-  double2 acc = B[r * ldb + b0 + j];
-  for (int i = 0; i < ka; i++) {
-    double2 a = A[r * lda + a0 + i], c = C[i * kb + j];
-    if (REAL) {
-      acc.x -= a.x * c.x;
-    } else {
-      acc.x -= a.x * c.x - a.y * c.y;
-      acc.y -= a.x * c.y + a.y * c.x;
-    }
-  }
-  B[r * ldb + b0 + j] = acc;
-}
-
-__global__ void k_scale_col(double2 *B, int ldb, int col, int64_t n, double s) {
-  int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (r >= n) return;
-  double2 v = B[r * ldb + col];
-  B[r * ldb + col] = make_double2(v.x * s, v.y * s);
-}
 
 // deterministic pseudo-random fill of columns c0 .. c0+k-1 (guard vectors); real entries for
 // a real operator, so real start vectors keep the whole block, and the eigenvectors, real
@@ -312,7 +285,7 @@ extern "C" qg_status qg_block_groundstate(qg_context ctx, qg_operator op, qg_bas
   K = (K / p) * p;
   if (K < p) K = p;
   cudaStream_t s = ctx->stream;
-  double2 *V = nullptr, *W = nullptr, *Cd = nullptr, *X = nullptr, *Md = nullptr;
+  double2 *V = nullptr, *W = nullptr, *Cd = nullptr, *X = nullptr, *Md = nullptr, *Sd = nullptr;
   double *wd = nullptr;
   size_t vb = (size_t)n * K * 16, wb = (size_t)n * p * 16;
   cudaError_t e = cudaMalloc(&V, vb);
@@ -321,6 +294,7 @@ extern "C" qg_status qg_block_groundstate(qg_context ctx, qg_operator op, qg_bas
   if (e == cudaSuccess) e = cudaMalloc(&Cd, (size_t)K * std::max(K, p) * 16);
   if (e == cudaSuccess) e = cudaMalloc(&Md, (size_t)K * K * 16);
   if (e == cudaSuccess) e = cudaMalloc(&wd, (size_t)K * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc(&Sd, (size_t)p * p * 16);
   if (e != cudaSuccess) {
     cudaFree(V);
     cudaFree(W);
@@ -328,6 +302,7 @@ extern "C" qg_status qg_block_groundstate(qg_context ctx, qg_operator op, qg_bas
     cudaFree(Cd);
     cudaFree(Md);
     cudaFree(wd);
+    cudaFree(Sd);
     ctx->last_error = "qg_block_groundstate: out of device memory";
     return QG_ERR_OOM;
   }
@@ -373,58 +348,90 @@ extern "C" qg_status qg_block_groundstate(qg_context ctx, qg_operator op, qg_bas
     ctx->launches++;
     int k = 0;  // orthonormal columns in V
     T.assign((size_t)K * K, cd(0, 0));
-    auto orth_block = [&](int c0, int cnt, std::vector<cd> *coef) -> int {
-      // orthonormalise V[:, c0:c0+cnt] among themselves (modified Gram-Schmidt, twice);
-      // returns how many columns survived (kept contiguous from c0); coef gets R.  The block
-      // has already been projected twice against V[:, 0:c0] as a whole, so a column is
-      // projected against the old columns again only when the in-block passes cancelled most
-      // of it (norm below a tenth of its start: "twice is enough" no longer holds for it).
-      int kept = 0;
-      for (int j = 0; j < cnt && st == QG_OK; j++) {
-        int col = c0 + kept;
-        if (col != c0 + j) {
-          k_copy_cols<<<grid(n), 256, 0, s>>>(V, K, c0 + j, V, K, col, 1, n);
-          ctx->launches++;
+    // Loewdin orthonormalisation of the ka columns of A (ld lda): the eigenvectors U and values
+    // s^2 of the Gram matrix A^H A; directions with s at most 1e-10 of the largest are dropped.
+    // Sm (ka x kk row-major) makes Q = A Sm orthonormal and Rm (kk x ka) gives A = Q Rm on the
+    // kept span; *cond gets the smallest kept s over the largest.  Returns kk.
+    auto lowdin_pass = [&](const double2 *A, int lda, int ka, std::vector<cd> &Sm, std::vector<cd> &Rm,
+                           double *cond) -> int {
+      std::vector<cd> Gh;
+      st = G.run(A, lda, 0, ka, A, lda, 0, ka, &Gh);
+      if (st != QG_OK) return 0;
+      for (int r = 0; r < ka; r++)
+        for (int c = r; c < ka; c++) {
+          const cd h = 0.5 * (Gh[(size_t)r * ka + c] + std::conj(Gh[(size_t)c * ka + r]));
+          Gh[(size_t)r * ka + c] = h;
+          Gh[(size_t)c * ka + r] = std::conj(h);
         }
-        double nrm0 = 0;
-        {
-          std::vector<cd> h;
-          st = G.run(V, K, col, 1, V, K, col, 1, &h);
-          nrm0 = std::sqrt(std::max(0.0, h[0].real()));
+      std::vector<double> w(ka);
+      std::vector<cd> U((size_t)ka * ka);
+      st = qg_eigh_host_io(ctx, ka, (const double *)Gh.data(), w.data(), (double *)U.data(), ka);
+      if (st != QG_OK) return 0;
+      const double smax = std::sqrt(std::max(w[ka - 1], 0.0));
+      std::vector<int> keep;
+      for (int q = ka - 1; q >= 0; q--)
+        if (smax > 0.0 && std::sqrt(std::max(w[q], 0.0)) > 1e-10 * smax) keep.push_back(q);
+      const int kk = (int)keep.size();
+      *cond = kk ? std::sqrt(std::max(w[keep[kk - 1]], 0.0)) / smax : 0.0;
+      Sm.assign((size_t)ka * std::max(kk, 1), cd(0, 0));
+      Rm.assign((size_t)std::max(kk, 1) * ka, cd(0, 0));
+      for (int c = 0; c < kk; c++) {
+        const double sv = std::sqrt(w[keep[c]]);
+        for (int r = 0; r < ka; r++) {
+          const cd u = U[(size_t)r * ka + keep[c]];
+          Sm[(size_t)r * kk + c] = u / sv;
+          Rm[(size_t)c * ka + r] = sv * std::conj(u);
         }
-        // project v_col against columns lo .. col-1, twice
-        auto project = [&](int lo) {
-          for (int pass = 0; pass < 2 && st == QG_OK && col > lo; pass++) {
-            std::vector<cd> h;
-            st = G.run(V, K, lo, col - lo, V, K, col, 1, &h);
-            if (st != QG_OK) break;
-            if (G.real)
-              k_sub_mul<true><<<grid(n), 256, 0, s>>>(V, K, lo, col - lo, G.out, V, K, col, 1, n);
-            else
-              k_sub_mul<false><<<grid(n), 256, 0, s>>>(V, K, lo, col - lo, G.out, V, K, col, 1, n);
-            ctx->launches++;
-            if (coef)
-              for (int i = lo; i < col; i++) (*coef)[(size_t)i * cnt + j] += h[i - lo];
-          }
-        };
-        project(c0);
-        std::vector<cd> h;
-        if (st == QG_OK) st = G.run(V, K, col, 1, V, K, col, 1, &h);
-        if (st != QG_OK) break;
-        double nrm = std::sqrt(std::max(0.0, h[0].real()));
-        if (c0 > 0 && nrm < 0.1 * nrm0) {
-          project(0);
-          if (st == QG_OK) st = G.run(V, K, col, 1, V, K, col, 1, &h);
-          if (st != QG_OK) break;
-          nrm = std::sqrt(std::max(0.0, h[0].real()));
-        }
-        if (nrm <= 1e-10 * std::max(nrm0, 1e-300) || nrm == 0.0) continue;  // deflate
-        k_scale_col<<<grid(n), 256, 0, s>>>(V, K, col, n, 1.0 / nrm);
-        ctx->launches++;
-        if (coef) (*coef)[(size_t)col * cnt + j] = nrm;
-        kept++;
       }
-      return kept;
+      return kk;
+    };
+    // orthonormalise V[:, c0:c0+cnt] with Loewdin inside the block, twice.  The block has already
+    // been projected twice against V[:, 0:c0] as a whole, which stays enough unless the block
+    // is nearly dependent: when the first pass's smallest kept s is below a tenth of the largest
+    // (its 1/s scaling amplifies what the projections left), the result is projected against
+    // V[:, 0:c0] once more before the second pass.  The result lands in V[:, c0:c0+kept].
+    // coef (c0 + cnt rows x cnt) gets R with W_j = sum_i V_i R[i][j] over old and new columns.
+    auto orth_block = [&](int c0, int cnt, std::vector<cd> *coef) -> int {
+      std::vector<cd> S1, R1, S2, R2, Ch;
+      double cond1 = 0.0, cond2 = 0.0;
+      const int k1 = lowdin_pass(V + c0, K, cnt, S1, R1, &cond1);
+      if (st != QG_OK || k1 == 0) return 0;
+      cudaError_t ce = cudaMemcpyAsync(Sd, S1.data(), S1.size() * 16, cudaMemcpyHostToDevice, s);
+      if (ce != cudaSuccess) {
+        st = qg_cuda_fail(ctx, ce, "block orthonormalisation");
+        return 0;
+      }
+      st = qg_block_update(ctx, V + c0, K, cnt, Sd, W, p, k1, n, 1.0, 0.0, G.real);  // Q1 = V_b S1
+      if (st != QG_OK) return 0;
+      if (c0 > 0 && cond1 < 0.1) {  // Q1 -= V_old (V_old^H Q1)
+        st = G.run(V, K, 0, c0, W, p, 0, k1, &Ch);
+        if (st == QG_OK) st = qg_block_update(ctx, V, K, c0, G.out, W, p, k1, n, -1.0, 1.0, G.real);
+        if (st != QG_OK) return 0;
+      }
+      const int k2 = lowdin_pass(W, p, k1, S2, R2, &cond2);
+      if (st != QG_OK || k2 == 0) return 0;
+      ce = cudaMemcpyAsync(Sd, S2.data(), S2.size() * 16, cudaMemcpyHostToDevice, s);
+      if (ce != cudaSuccess) {
+        st = qg_cuda_fail(ctx, ce, "block orthonormalisation");
+        return 0;
+      }
+      st = qg_block_update(ctx, W, p, k1, Sd, V + c0, K, k2, n, 1.0, 0.0, G.real);  // Q2 = Q1 S2
+      if (st != QG_OK) return 0;
+      if (coef) {
+        for (int i = 0; i < k2; i++)  // new columns: R2 R1
+          for (int j = 0; j < cnt; j++) {
+            cd a(0, 0);
+            for (int t = 0; t < k1; t++) a += R2[(size_t)i * k1 + t] * R1[(size_t)t * cnt + j];
+            (*coef)[(size_t)(c0 + i) * cnt + j] = a;
+          }
+        for (int i = 0; i < c0 && !Ch.empty(); i++)  // old columns: C R1
+          for (int j = 0; j < cnt; j++) {
+            cd a(0, 0);
+            for (int t = 0; t < k1; t++) a += Ch[(size_t)i * k1 + t] * R1[(size_t)t * cnt + j];
+            (*coef)[(size_t)i * cnt + j] += a;
+          }
+      }
+      return k2;
     };
     k = orth_block(0, p, nullptr);
     if (st != QG_OK) break;
@@ -552,6 +559,7 @@ extern "C" qg_status qg_block_groundstate(qg_context ctx, qg_operator op, qg_bas
   cudaFree(Cd);
   cudaFree(Md);
   cudaFree(wd);
+  cudaFree(Sd);
   for (int j = 0; j < nwant; j++) energies_host[j] = theta[j];
   if (iterations) *iterations = it;
   if (st == QG_OK) st = qg_check_device_error(ctx, "qg_block_groundstate");
