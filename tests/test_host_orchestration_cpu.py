@@ -100,6 +100,10 @@ def host_api(monkeypatch, oracle_mod):
             out.numpy()[:n, :npc] = K.numpy()[:nk, :n].T @ np.asarray(C).reshape(nk, npc)
             return 0
 
+        def qg_norm(self, ctx, n, k, x, out):
+            out[:k] = np.linalg.norm(x.numpy()[:n, :k], axis=0)
+            return 0
+
         def qg_block_adjoint_product(self, ctx, A, lda, ka, B, ldb, kb, n, C):
             C.numpy()[:ka, :kb] = A.numpy()[:n, :ka].conj().T @ B.numpy()[:n, :kb]
             return 0
@@ -566,3 +570,25 @@ def test_tensor_spectra_orchestration_matches_reference(host_api, key):
     assert abs(S.Emin - R.Emin) < 1e-8 and abs(S.Emax - R.Emax) < 1e-8 and abs(S.Gamma - R.Gamma) < 1e-8
     assert abs(S.EminPole - R.EminPole) < 1e-8 and abs(S.EmaxPole - R.EmaxPole) < 1e-8
     assert np.max(np.abs(S.G - R.G)) < TOL * np.max(np.abs(R.G))
+
+
+def test_merged_calls_match_separate_calls(host_api):
+    """The served form's continuous batching: CreateSpectra calls on one Hamiltonian with the same
+    Lanczos settings but their own operators, states, windows and frequencies run as one
+    multi-vector Lanczos over exactly their pairs, and each gets the spectra of its call alone."""
+    api = host_api
+    g = golden("rixs.json")
+    HX, Tx, Ty = (api.Operator.from_fixture(g[k]) for k in ("HX", "Tx", "Ty"))
+    psi1, psi2 = (api.Wavefunction.from_fixture(p) for p in g["psi"][:2])
+    base = {"Method": "Lanczos", "NTri": 40, "Epsilon": 0.0, "Gamma": 0.5}
+    jobs = [(Tx, psi1, dict(base, NE=32, Emin=-10, Emax=20)),
+            ([Tx, Ty], [psi1, psi2], dict(base, NE=16)),
+            (Ty, psi2, dict(base, NE=24, Emin=-5, Emax=15))]
+    assert len({api.lanczos_merge_key(HX, *j) for j in jobs}) == 1
+    assert api.lanczos_merge_key(HX, Tx, psi1, dict(base, NTri=41)) != api.lanczos_merge_key(HX, *jobs[0])
+    merged = api.CreateSpectraMerged(HX, jobs)
+    for (T, psi, o), (S, tri) in zip(jobs, merged):
+        S1, tri1 = api.CreateSpectra(HX, T, psi, o)
+        assert S.G.shape == S1.G.shape
+        assert np.max(np.abs(S.G - S1.G)) <= 1e-10 * np.max(np.abs(S1.G))
+        assert abs(S.Emin - S1.Emin) < 1e-10 and abs(S.Emax - S1.Emax) < 1e-10
