@@ -9,8 +9,9 @@
 //     product (every block forms v from row j of A, the conjugate of column j, and the last
 //     block to finish forms w), then the rank-2 update.  T = Q^H A Q, Q = H_0 H_1 ... H_(k-2),
 //     T real: diagonal d, off-diagonal beta.
-//  2. Eigenvalues of T by bisection on Sturm counts (the method of LAPACK's dstebz), one thread
-//     per eigenvalue, down to the last representable midpoint.
+//  2. Eigenvalues of T by bisection on Sturm counts (the method of LAPACK's dstebz), as
+//     multisection: one warp per eigenvalue, 32 counts per round, down to the last
+//     representable midpoint.
 //  3. Eigenvectors of T for the lowest nv eigenvalues by inverse iteration (the method of
 //     LAPACK's dstein): T - lambda I factored with partial pivoting, tiny pivots replaced by
 //     eps |T|, three solves from a pseudo-random start, each followed by modified Gram-Schmidt
@@ -25,7 +26,7 @@
 
 #include "qgpu_internal.cuh"
 
-#define HH_WARPS 16       // rows (one per warp) per block of the reflector / matrix-vector kernel
+#define HH_WARPS 4        // rows (one per warp) per block of the reflector / matrix-vector kernel
 #define HH_BT_VECS 8      // eigenvectors (one per warp) per block of the back-transformation
 #define HH_MAX_K 12000    // shared memory holds one reflector (16 B per entry)
 #define HH_INV_THREADS 128
@@ -36,16 +37,21 @@ __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
   return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
 
-// block-wide sum in a fixed order (threads, then the warps in order); every thread gets it
+// block-wide sum in a fixed order (threads, then the warps in order), combined by one thread
+// and shared: every thread gets it.  red holds one entry per warp plus one.
 __device__ double block_sum(double s, double *red) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
   __syncthreads();  // red may still be read from a previous call
   if (lane == 0) red[wid] = s;
   __syncthreads();
-  double t = 0.0;
-  for (int w = 0; w < nw; w++) t += red[w];
-  return t;
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < nw; w++) t += red[w];
+    red[nw] = t;
+  }
+  __syncthreads();
+  return red[nw];
 }
 
 __device__ double2 block_sum2(double2 s, double2 *red) {
@@ -57,12 +63,16 @@ __device__ double2 block_sum2(double2 s, double2 *red) {
   __syncthreads();
   if (lane == 0) red[wid] = s;
   __syncthreads();
-  double2 t = make_double2(0.0, 0.0);
-  for (int w = 0; w < nw; w++) {
-    t.x += red[w].x;
-    t.y += red[w].y;
+  if (threadIdx.x == 0) {
+    double2 t = make_double2(0.0, 0.0);
+    for (int w = 0; w < nw; w++) {
+      t.x += red[w].x;
+      t.y += red[w].y;
+    }
+    red[nw] = t;
   }
-  return t;
+  __syncthreads();
+  return red[nw];
 }
 
 }  // namespace
@@ -75,8 +85,8 @@ __global__ void __launch_bounds__(HH_WARPS * 32)
              double *__restrict__ d, double *__restrict__ e, double2 *__restrict__ p, double2 *__restrict__ w,
              unsigned int *counter) {
   extern __shared__ double2 sv[];  // v, m entries
-  __shared__ double red[HH_WARPS];
-  __shared__ double2 red2[HH_WARPS];
+  __shared__ double red[HH_WARPS + 1];
+  __shared__ double2 red2[HH_WARPS + 1];
   __shared__ double2 s_tau, s_sc, s_k;
   __shared__ int s_last;
   const int m = k - j - 1;
@@ -203,21 +213,39 @@ __device__ int tri_sturm(const double *__restrict__ d, const double *__restrict_
   return cnt;
 }
 
-// eigenvalue i of T (ascending) by bisection of [gl, gu] down to the last representable midpoint
+// eigenvalue i of T (ascending), a warp per eigenvalue, by multisection of [gl, gu]: each round
+// the 32 lanes take Sturm counts at 32 points spread evenly over the interval and keep the
+// 33rd part holding eigenvalue i (count(lo) <= i < count(hi) throughout).  When the points fall
+// onto the ends (an interval a few ulps wide) a round halves instead, and the search ends at the
+// last representable midpoint, as a bisection does; 72 rounds resolve at least what 256
+// halvings do.
 __global__ void k_tri_bisect(const double *__restrict__ d, const double *__restrict__ e2, int k, double gl, double gu,
                              double pivmin, double *__restrict__ w) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= k) return;
+  const int lane = threadIdx.x & 31;
+  const int i = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
+  if (i >= k) return;  // i is the same on every lane of a warp
+  const double frac = (double)(lane + 1) * (1.0 / 33.0);
   double lo = gl, hi = gu;
-  for (int it = 0; it < 256; it++) {
+  for (int it = 0; it < 72; it++) {
     const double mid = 0.5 * (lo + hi);
     if (!(mid > lo && mid < hi)) break;
-    if (tri_sturm(d, e2, k, mid, pivmin) > i)
-      hi = mid;
-    else
-      lo = mid;
+    const double x = lo + (hi - lo) * frac;
+    const unsigned above = __ballot_sync(0xffffffffu, tri_sturm(d, e2, k, x, pivmin) > i);
+    const int f = above ? __ffs((int)above) - 1 : 32;  // the first point with count > i
+    const double xl = __shfl_sync(0xffffffffu, x, f > 0 ? f - 1 : 0);
+    const double xh = __shfl_sync(0xffffffffu, x, f < 32 ? f : 31);
+    const double nlo = f > 0 ? xl : lo, nhi = f < 32 ? xh : hi;
+    if (nlo == lo && nhi == hi) {  // no point strictly inside: halve
+      if (tri_sturm(d, e2, k, mid, pivmin) > i)
+        hi = mid;
+      else
+        lo = mid;
+    } else {
+      lo = nlo;
+      hi = nhi;
+    }
   }
-  w[i] = 0.5 * (lo + hi);
+  if (lane == 0) w[i] = 0.5 * (lo + hi);
 }
 
 // T - lambda I = P L U with partial pivoting: U has the diagonal u0 and two superdiagonals
@@ -284,7 +312,7 @@ __device__ __forceinline__ double start_value(int idx, int i, int salt) {
 __global__ void __launch_bounds__(HH_INV_THREADS)
     k_tri_invit(const double *__restrict__ d, const double *__restrict__ e, int k, const double *__restrict__ w,
                 const int *__restrict__ cl, int ncl, double *__restrict__ Z, double *__restrict__ scratch, double tol) {
-  __shared__ double red[HH_INV_THREADS / 32];
+  __shared__ double red[HH_INV_THREADS / 32 + 1];
   double *u0 = scratch + (int64_t)blockIdx.x * 5 * k, *u1 = u0 + k, *u2 = u1 + k, *ml = u2 + k, *pv = ml + k;
   for (int ci = blockIdx.x; ci < ncl; ci += gridDim.x) {
     const int cs = cl[ci], ce = cl[ci + 1];
@@ -440,7 +468,7 @@ qg_status qg_eigh_tridiag(qg_context ctx, int k, double2 *A, double *w_dev, doub
     ce = cudaMemcpyAsync(e2, he2.data(), (size_t)k * sizeof(double), cudaMemcpyHostToDevice, s);
     if (ce != cudaSuccess) st = qg_cuda_fail(ctx, ce, "qg_eigh_tridiag");
     if (st == QG_OK) {
-      k_tri_bisect<<<(unsigned)((k + 31) / 32), 32, 0, s>>>(d, e2, k, gl, gu, pivmin, w_dev);
+      k_tri_bisect<<<(unsigned)((k + 3) / 4), 128, 0, s>>>(d, e2, k, gl, gu, pivmin, w_dev);  // a warp each
       ctx->launches++;
       st = qg_check_launch(ctx, "bisection");
     }
