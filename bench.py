@@ -45,7 +45,8 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-secondary", action="store_true")
-    p.add_argument("--mode", default="hpsi", choices=["hpsi", "batched", "served", "layouts", "chains"])
+    p.add_argument("--mode", default="hpsi", choices=["hpsi", "batched", "served", "layouts", "chains", "eigh"])
+    p.add_argument("--k", type=int, default=190, help="eigh mode: order of the matrix")
     p.add_argument("--layout", type=int, default=None)
     p.add_argument("--jobs", type=int, default=24)
     p.add_argument("--states", type=int, default=16)

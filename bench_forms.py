@@ -527,7 +527,36 @@ def chains(args):
     return 0
 
 
+def eigh(args):
+    """The dense Hermitian eigensolver (qg_hermitian_eigh) on a seeded random Hermitian matrix of
+    order --k: three calls with the lowest three eigenvectors, then two with all of them, each
+    timed on the host around the call (host matrix in, eigenpairs out), and the eigenvalues
+    against LAPACK (numpy)."""
+    from quanty_gb300 import api
+    eng = api.engine()
+    k = int(args.k)
+    rng = np.random.default_rng(0)
+    A = rng.normal(size=(k, k)) + 1j * rng.normal(size=(k, k))
+    A = A + A.conj().T
+    out = {}
+    for name, nv, reps in (("three_vectors", 3, 3), ("all_vectors", k, 2)):
+        ts = []
+        for _ in range(reps):
+            eng.stream.synchronize()
+            t0 = time.perf_counter()
+            w, V = api.hermitian_eigh(A, nv, eng)
+            eng.stream.synchronize()
+            ts.append(time.perf_counter() - t0)
+        out[name + "_ms"] = 1e3 * min(ts)
+    ref = np.linalg.eigvalsh(A)
+    out["eigenvalues_max_rel_vs_lapack"] = float(np.max(np.abs(w - ref)) / np.max(np.abs(ref)))
+    print(json.dumps({"mode": "eigh", "k": k, **out}), flush=True)
+    return 0
+
+
 def main(args):
+    if args.mode == "eigh":
+        return eigh(args)
     if args.mode == "batched":
         return batched(args)
     if args.mode == "layouts":
