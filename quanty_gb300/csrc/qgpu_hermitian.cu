@@ -5,10 +5,12 @@
 //  1. Householder tridiagonalisation (the unblocked reduction of LAPACK's zhetd2).  For column j
 //     the reflector H_j = I - tau_j v_j v_j^H, v_j[0] = 1, satisfies H_j^H x = beta_j e_1 with
 //     beta_j real, x = A[j+1:, j]; then p = tau A22 v, w = p - (tau/2)(p^H v) v and
-//     A22 -= v w^H + w v^H.  Two launches per column: the reflector with the matrix-vector
-//     product (every block forms v from row j of A, the conjugate of column j, and the last
-//     block to finish forms w), then the rank-2 update.  T = Q^H A Q, Q = H_0 H_1 ... H_(k-2),
-//     T real: diagonal d, off-diagonal beta.
+//     A22 -= v w^H + w v^H.  Per column a launch in which every block forms v from row j of A
+//     (the conjugate of column j), the matrix-vector product runs a warp per row and the last
+//     block to finish forms w; the rank-2 update is a launch of its own for the large columns,
+//     and below HH_FOLD_ROWS rows it is applied by the next column's launch to what it reads
+//     (the last one by the launch that reads the last diagonal entry).
+//     T = Q^H A Q, Q = H_0 H_1 ... H_(k-2), T real: diagonal d, off-diagonal beta.
 //  2. Eigenvalues of T by bisection on Sturm counts (the method of LAPACK's dstebz), as
 //     multisection: one warp per eigenvalue, 32 counts per round, down to the last
 //     representable midpoint.
@@ -27,6 +29,8 @@
 #include "qgpu_internal.cuh"
 
 #define HH_WARPS 4        // rows (one per warp) per block of the reflector / matrix-vector kernel
+#define HH_FOLD_ROWS 512  // below this many rows a column's rank-2 update is folded into the next
+                          // column's launch; above, it is a launch of its own
 #define HH_BT_VECS 8      // eigenvectors (one per warp) per block of the back-transformation
 #define HH_MAX_K 12000    // shared memory holds one reflector (16 B per entry)
 #define HH_INV_THREADS 128
@@ -77,29 +81,47 @@ __device__ double2 block_sum2(double2 s, double2 *red) {
 
 }  // namespace
 
-// Column j: the reflector from x = A[j+1:, j] (read as the conjugate of row j), v into vbuf
-// row j, tau_j, beta_j = e[j], d[j] = A[j][j]; p = tau A22 v (a warp per row); the last block
-// forms w = p - (tau/2)(p^H v) v and resets the counter.  m = k - j - 1 >= 1 rows.
+// A22(j-1)[r][c] after the rank-2 update of column j - 1: a - (v_r conj(w_c) + w_r conj(v_c)),
+// with v, w of that column indexed over A22(j-1) (entry 0 is row / column j).
+__device__ __forceinline__ double2 hh_updated(double2 a, double2 vr, double2 wr, double2 vc, double2 wc) {
+  a.x -= (vr.x * wc.x + vr.y * wc.y) + (wr.x * vc.x + wr.y * vc.y);
+  a.y -= (vr.y * wc.x - vr.x * wc.y) + (wr.y * vc.x - wr.x * vc.y);
+  return a;
+}
+
+// Column j, with the rank-2 update of column j - 1 (A22 -= v w^H + w v^H) folded in when it is
+// pending: every block brings row j up to date as it reads it, and the warp that owns a row of
+// the trailing matrix updates it, writes it back and uses it.  Then the reflector from x = A[j+1:, j] (read as the
+// conjugate of row j), v into vbuf row j, tau_j, beta_j = e[j], d[j] = A[j][j]; p = tau A22 v
+// (a warp per row, blockDim.x / 32 rows per block); the last block forms
+// w = p - (tau/2)(p^H v) v into w buffer j % 2 and resets the counter.  m = k - j - 1 >= 1 rows.
 __global__ void __launch_bounds__(HH_WARPS * 32)
     k_hh_col(double2 *__restrict__ A, int k, int j, double2 *__restrict__ vbuf, double2 *__restrict__ tau,
-             double *__restrict__ d, double *__restrict__ e, double2 *__restrict__ p, double2 *__restrict__ w,
-             unsigned int *counter) {
+             double *__restrict__ d, double *__restrict__ e, double2 *__restrict__ p, double2 *__restrict__ wv,
+             int pending, unsigned int *counter) {
   extern __shared__ double2 sv[];  // v, m entries
   __shared__ double red[HH_WARPS + 1];
   __shared__ double2 red2[HH_WARPS + 1];
   __shared__ double2 s_tau, s_sc, s_k;
   __shared__ int s_last;
   const int m = k - j - 1;
-  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, T = blockDim.x;
-  const double2 *rowj = A + (int64_t)j * k + j + 1;  // rowj[c] = conj(x_c)
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, T = blockDim.x, rows = T >> 5;
+  const bool upd = pending != 0;  // column j - 1's update still to apply
+  const double2 *pv = vbuf + (int64_t)(upd ? j - 1 : 0) * k;
+  const double2 *pw = wv + (int64_t)((j + 1) & 1) * k;  // w of column j - 1
+  double2 *wout = wv + (int64_t)(j & 1) * k;
+  const double2 z = make_double2(0.0, 0.0);
+  const double2 v0 = upd ? pv[0] : z, w0 = upd ? pw[0] : z;
+  const double2 *rowj = A + (int64_t)j * k + j + 1;  // rowj[c] = conj(x_c), once brought up to date
   double ss = 0.0;
   for (int c = 1 + tid; c < m; c += T) {
-    const double2 a = rowj[c];
+    const double2 a = upd ? hh_updated(rowj[c], v0, w0, pv[c + 1], pw[c + 1]) : rowj[c];
     ss += a.x * a.x + a.y * a.y;
   }
   ss = block_sum(ss, red);
   if (tid == 0) {
-    const double2 al = make_double2(rowj[0].x, -rowj[0].y);
+    const double2 r0 = upd ? hh_updated(rowj[0], v0, w0, pv[1], pw[1]) : rowj[0];
+    const double2 al = make_double2(r0.x, -r0.y);
     double2 tv, sc;
     double beta;
     if (ss == 0.0 && al.y == 0.0) {  // already in tridiagonal form: H = I
@@ -119,7 +141,8 @@ __global__ void __launch_bounds__(HH_WARPS * 32)
     if (blockIdx.x == 0) {
       tau[j] = tv;
       e[j] = beta;
-      d[j] = A[(int64_t)j * k + j].x;
+      const double2 ajj = A[(int64_t)j * k + j];
+      d[j] = upd ? hh_updated(ajj, v0, w0, v0, w0).x : ajj.x;
     }
   }
   __syncthreads();
@@ -129,19 +152,25 @@ __global__ void __launch_bounds__(HH_WARPS * 32)
     if (c == 0) {
       v = make_double2(1.0, 0.0);
     } else {
-      const double2 x = make_double2(rowj[c].x, -rowj[c].y);
-      v = cmul(x, sc);
+      const double2 a = upd ? hh_updated(rowj[c], v0, w0, pv[c + 1], pw[c + 1]) : rowj[c];
+      v = cmul(make_double2(a.x, -a.y), sc);
     }
     sv[c] = v;
     if (blockIdx.x == 0) vbuf[(int64_t)j * k + c] = v;
   }
   __syncthreads();
-  const int r = blockIdx.x * HH_WARPS + wid;
+  const int r = blockIdx.x * rows + wid;
   if (r < m) {
-    const double2 *row = A + (int64_t)(j + 1 + r) * k + j + 1;
+    double2 *row = A + (int64_t)(j + 1 + r) * k + j + 1;
+    const double2 vr = upd ? pv[r + 1] : z, wr = upd ? pw[r + 1] : z;
     double2 s = make_double2(0.0, 0.0);
     for (int c = lane; c < m; c += 32) {
-      const double2 a = row[c], v = sv[c];
+      double2 a = row[c];
+      if (upd) {
+        a = hh_updated(a, vr, wr, pv[c + 1], pw[c + 1]);
+        row[c] = a;
+      }
+      const double2 v = sv[c];
       s.x += a.x * v.x - a.y * v.y;
       s.y += a.x * v.y + a.y * v.x;
     }
@@ -174,11 +203,13 @@ __global__ void __launch_bounds__(HH_WARPS * 32)
   const double2 kk = s_k;
   for (int c = tid; c < m; c += T) {
     const double2 pc = __ldcg(p + c), kv = cmul(kk, sv[c]);
-    w[c] = make_double2(pc.x - kv.x, pc.y - kv.y);
+    wout[c] = make_double2(pc.x - kv.x, pc.y - kv.y);
   }
 }
 
-// A22 -= v w^H + w v^H over the trailing m x m block; 32 x 32 tiles, 8 rows per pass.
+// A22 -= v w^H + w v^H over the trailing m x m block of column j, as its own launch (the large
+// columns: there every block of the next column would repeat the update of row j); 32 x 32
+// tiles, 8 rows per pass.
 __global__ void __launch_bounds__(256)
     k_hh_rank2(double2 *__restrict__ A, int k, int j, const double2 *__restrict__ vbuf, const double2 *__restrict__ w) {
   const int m = k - j - 1;
@@ -188,17 +219,21 @@ __global__ void __launch_bounds__(256)
   const double2 vc = v[c], wc = w[c];
   const int r1 = min(m, (int)blockIdx.y * 32 + 32);
   for (int r = blockIdx.y * 32 + (threadIdx.x >> 5); r < r1; r += 8) {
-    const double2 vr = v[r], wr = w[r];
     double2 *a = A + (int64_t)(j + 1 + r) * k + j + 1 + c;
-    double2 x = *a;
-    // vr conj(wc) + wr conj(vc)
-    x.x -= (vr.x * wc.x + vr.y * wc.y) + (wr.x * vc.x + wr.y * vc.y);
-    x.y -= (vr.y * wc.x - vr.x * wc.y) + (wr.y * vc.x - wr.x * vc.y);
-    *a = x;
+    *a = hh_updated(*a, v[r], w[r], vc, wc);
   }
 }
 
-__global__ void k_hh_last(const double2 *A, int k, double *d) { d[k - 1] = A[(int64_t)(k - 1) * k + k - 1].x; }
+// d[k-1]: the last diagonal entry, after the rank-2 update of column k - 2 when that is pending
+__global__ void k_hh_last(const double2 *A, int k, const double2 *vbuf, const double2 *wv, int pending, double *d) {
+  const double2 a = A[(int64_t)(k - 1) * k + k - 1];
+  if (!pending) {
+    d[k - 1] = a.x;
+    return;
+  }
+  const double2 v = vbuf[(int64_t)(k - 2) * k], w = wv[(int64_t)((k - 2) & 1) * k];
+  d[k - 1] = hh_updated(a, v, w, v, w).x;
+}
 
 // number of eigenvalues of T below x (Sturm count; tiny pivots replaced by -pivmin)
 __device__ int tri_sturm(const double *__restrict__ d, const double *__restrict__ e2, int k, double x, double pivmin) {
@@ -419,7 +454,7 @@ qg_status qg_eigh_tridiag(qg_context ctx, int k, double2 *A, double *w_dev, doub
   cudaError_t ce = cudaMalloc(&vbuf, (size_t)k * k * sizeof(double2));
   if (ce == cudaSuccess) ce = cudaMalloc(&tau, (size_t)k * sizeof(double2));
   if (ce == cudaSuccess) ce = cudaMalloc(&p, (size_t)k * sizeof(double2));
-  if (ce == cudaSuccess) ce = cudaMalloc(&wv, (size_t)k * sizeof(double2));
+  if (ce == cudaSuccess) ce = cudaMalloc(&wv, (size_t)2 * k * sizeof(double2));  // w of two columns
   if (ce == cudaSuccess) ce = cudaMalloc(&d, (size_t)k * sizeof(double));
   if (ce == cudaSuccess) ce = cudaMalloc(&e, (size_t)k * sizeof(double));
   if (ce == cudaSuccess) ce = cudaMalloc(&e2, (size_t)k * sizeof(double));
@@ -428,16 +463,22 @@ qg_status qg_eigh_tridiag(qg_context ctx, int k, double2 *A, double *w_dev, doub
   if (ce == cudaSuccess) ce = cudaMemsetAsync(e, 0, (size_t)k * sizeof(double), s);
   qg_status st = ce == cudaSuccess ? QG_OK : qg_cuda_fail(ctx, ce, "qg_eigh_tridiag");
   // 1. reduction to tridiagonal form
+  int pending = 0;  // the previous column's rank-2 update is left to this column's launch
   for (int j = 0; st == QG_OK && j < k - 1; j++) {
     const int m = k - j - 1;
     k_hh_col<<<(unsigned)((m + HH_WARPS - 1) / HH_WARPS), HH_WARPS * 32, (size_t)m * sizeof(double2), s>>>(
-        A, k, j, vbuf, tau, d, e, p, wv, counter);
-    k_hh_rank2<<<dim3((unsigned)((m + 31) / 32), (unsigned)((m + 31) / 32)), 256, 0, s>>>(A, k, j, vbuf, wv);
-    ctx->launches += 2;
+        A, k, j, vbuf, tau, d, e, p, wv, pending, counter);
+    ctx->launches++;
+    pending = m < HH_FOLD_ROWS;
+    if (!pending) {
+      k_hh_rank2<<<dim3((unsigned)((m + 31) / 32), (unsigned)((m + 31) / 32)), 256, 0, s>>>(
+          A, k, j, vbuf, wv + (size_t)(j & 1) * k);
+      ctx->launches++;
+    }
     if ((j & 255) == 0) st = qg_check_launch(ctx, "tridiagonal reduction");
   }
   if (st == QG_OK) {
-    k_hh_last<<<1, 1, 0, s>>>(A, k, d);
+    k_hh_last<<<1, 1, 0, s>>>(A, k, vbuf, wv, pending, d);
     ctx->launches++;
     st = qg_check_launch(ctx, "tridiagonal reduction");
   }
