@@ -733,7 +733,8 @@ def OperatorToDeterminantMatrix(O, basis, eng=None):
 
 def hermitian_eigh(M, nvec=None, eng=None):
     """All eigenvalues (ascending) and the lowest nvec eigenvectors (columns) of a Hermitian
-    matrix, by the library's device eigensolver (cyclic Jacobi)."""
+    matrix, by the library's device eigensolver (cyclic Jacobi up to order 40; above, Householder
+    reduction to a tridiagonal matrix, multisection and inverse iteration)."""
     eng = eng or engine()
     k = M.shape[0]
     nv = k if nvec is None else int(nvec)
