@@ -164,13 +164,16 @@ qg_status qg_poles_spectra(qg_context ctx, int32_t nspec, int32_t npole, const d
                            const double *b_host, const double *e0_host, double emin, double de,
                            int32_t ne, double gamma, double *g_host);
 
-/* Eigenpairs of a dense Hermitian matrix, computed on the device (cyclic Jacobi with the
- * round-robin ordering: every step rotates k/2 disjoint index pairs at once): a_host is k x k
- * row-major with interleaved (re, im); w_host receives all k eigenvalues ascending, v_host
+/* Eigenpairs of a dense Hermitian matrix, computed on the device: up to k = 40 by cyclic Jacobi
+ * in one block (round-robin ordering: every step rotates k/2 disjoint index pairs at once);
+ * above, by Householder reduction to a real tridiagonal matrix, eigenvalues by multisection on
+ * Sturm counts, eigenvectors by inverse iteration and the reflectors (k <= 12000).  a_host is
+ * k x k row-major with interleaved (re, im); w_host receives all k eigenvalues ascending, v_host
  * (k x nv row-major, interleaved) the eigenvectors of the lowest nv as columns.  Replaces the
  * reference's zheevd calls on dense and projected matrices (Core/BlockLanczos.cpp:5530, :370-501;
  * HermitianCompactMatrixToListOfPoles, Core/BasicMath/BasicMath_CompactMatrixVector.cpp:3990).
- * QG_ERR_TIMEOUT if the rotations have not converged after 60 sweeps. */
+ * QG_ERR_TIMEOUT if the Jacobi rotations have not converged after 60 sweeps, QG_ERR_ARG above
+ * k = 12000. */
 qg_status qg_hermitian_eigh(qg_context ctx, int32_t k, const double *a_host, double *w_host, double *v_host,
                             int32_t nv);
 
