@@ -61,6 +61,13 @@ def time_lf(reps=3, threads=None, timeout=900):
     "spectra_s": [...], "energies": [3], "spectra_text": Spectra.Print of the last repetition}."""
     threads = int(threads or os.cpu_count() or 1)
     work = tempfile.mkdtemp(prefix="qref_lf_")
+    try:
+        return _run_lf(work, reps, threads, timeout)
+    finally:
+        shutil.rmtree(work, ignore_errors=True)
+
+
+def _run_lf(work, reps, threads, timeout):
     with open(os.path.join(GEN, "common.lua")) as f, open(os.path.join(work, "common.lua"), "w") as g:
         g.write(f.read())
     with open(os.path.join(work, "lf_time.lua"), "w") as f:
@@ -94,6 +101,5 @@ def time_lf(reps=3, threads=None, timeout=900):
         prev = marks["S%d" % r]
     with open(os.path.join(work, "spectra.dat")) as f:
         text = f.read()
-    shutil.rmtree(work, ignore_errors=True)
     return {"threads": threads, "eigensystem_s": eig, "spectra_s": spec, "energies": energies,
             "spectra_text": text}
