@@ -15,6 +15,7 @@ import os
 import shutil
 import subprocess
 import tempfile
+import threading
 import time
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -76,20 +77,21 @@ def _run_lf(work, reps, threads, timeout):
     p = subprocess.Popen([BINARY, "lf_time.lua"], cwd=work, env=env, stdout=subprocess.PIPE,
                          stderr=subprocess.STDOUT, text=True)
     marks, energies, tail = {}, None, []
-    t_end = time.perf_counter() + timeout
-    for ln in p.stdout:
-        now = time.perf_counter()
-        s = ln.split()
-        if len(s) == 2 and s[0] == "QTMARK":
-            marks[s[1]] = now
-        elif s and s[0] == "QTENERGY":
-            energies = [float(v) for v in s[1:4]]
-        else:
-            tail = (tail + [ln])[-20:]
-        if now > t_end:
-            p.kill()
-            break
-    rc = p.wait()
+    watchdog = threading.Timer(timeout, p.kill)  # a run that stops printing still ends
+    watchdog.start()
+    try:
+        for ln in p.stdout:
+            now = time.perf_counter()
+            s = ln.split()
+            if len(s) == 2 and s[0] == "QTMARK":
+                marks[s[1]] = now
+            elif s and s[0] == "QTENERGY":
+                energies = [float(v) for v in s[1:4]]
+            else:
+                tail = (tail + [ln])[-20:]
+        rc = p.wait()
+    finally:
+        watchdog.cancel()
     if rc != 0 or energies is None or any(("E%d" % r) not in marks or ("S%d" % r) not in marks
                                           for r in range(1, reps + 1)):
         raise RuntimeError("reference run failed (%s): %s" % (rc, "".join(tail)[-600:]))
